@@ -1,0 +1,153 @@
+"""ctypes binding of the C ABI in include/incflo_gb300.h (the Python-side stub a caller binds).
+
+Loads the in-tree libincflo_gb300.so. There is no fallback: if the library or a CUDA device is
+missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libincflo_gb300.so")
+
+GBP_OK, GBP_NOT_CONVERGED, GBP_NAN, GBP_BAD_ARG, GBP_CUDA_ERROR, GBP_TIMEOUT, GBP_NO_DEVICE = range(7)
+GBP_NODAL, GBP_MAC = 0, 1
+BC_PERIODIC, BC_DIRICHLET, BC_NEUMANN, BC_INFLOW, BC_ROBIN = range(5)
+PREC_FP64, PREC_MIXED = 0, 1
+
+# every symbol include/incflo_gb300.h declares
+EXPORTS = (
+    "gbp_abi_version", "gbp_status_string", "gbp_last_error", "gbp_device_check",
+    "gbp_options_default", "gbp_options_set", "gbp_options_parse",
+    "gbp_plan_create", "gbp_plan_destroy", "gbp_plan_set_options", "gbp_plan_device_bytes",
+    "gbp_nodal_set_sigma_from_density", "gbp_nodal_set_sigma", "gbp_nodal_project",
+    "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
+    "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel",
+)
+
+
+class Array4(ctypes.Structure):
+    _fields_ = [
+        ("data", ctypes.c_void_p),
+        ("lo", ctypes.c_int * 3),
+        ("hi", ctypes.c_int * 3),
+        ("ncomp", ctypes.c_int),
+        ("jstride", ctypes.c_longlong),
+        ("kstride", ctypes.c_longlong),
+        ("nstride", ctypes.c_longlong),
+    ]
+
+
+class Geometry(ctypes.Structure):
+    _fields_ = [
+        ("n_cell", ctypes.c_int * 3),
+        ("prob_lo", ctypes.c_double * 3),
+        ("prob_hi", ctypes.c_double * 3),
+    ]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [
+        ("rtol", ctypes.c_double),
+        ("atol", ctypes.c_double),
+        ("max_coarsening_level", ctypes.c_int),
+        ("maxiter", ctypes.c_int),
+        ("bottom_maxiter", ctypes.c_int),
+        ("bottom_rtol", ctypes.c_double),
+        ("bottom_atol", ctypes.c_double),
+        ("verbose", ctypes.c_int),
+        ("bottom_verbose", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("nu1", ctypes.c_int),
+        ("nu2", ctypes.c_int),
+        ("omega", ctypes.c_double),
+        ("ir_inner_cycles", ctypes.c_int),
+        ("use_graphs", ctypes.c_int),
+        ("always_use_bnorm", ctypes.c_int),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("status", ctypes.c_int),
+        ("vcycles", ctypes.c_int),
+        ("outer_iters", ctypes.c_int),
+        ("num_levels", ctypes.c_int),
+        ("rhs_norm", ctypes.c_double),
+        ("initial_rel_resid", ctypes.c_double),
+        ("final_rel_resid", ctypes.c_double),
+        ("ms_total", ctypes.c_double),
+        ("ms_solve", ctypes.c_double),
+        ("kernel_launches", ctypes.c_longlong),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the shared library and declare every entry point's signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with incflo_gb300.build.build()")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    A4 = ctypes.POINTER(Array4)
+    i, d = ctypes.c_int, ctypes.c_double
+    sig = {
+        "gbp_abi_version": (i, []),
+        "gbp_status_string": (ctypes.c_char_p, [i]),
+        "gbp_last_error": (ctypes.c_char_p, []),
+        "gbp_device_check": (i, []),
+        "gbp_options_default": (i, [i, ctypes.POINTER(Options)]),
+        "gbp_options_set": (i, [ctypes.POINTER(Options), ctypes.c_char_p, ctypes.c_char_p]),
+        "gbp_options_parse": (i, [ctypes.POINTER(Options), ctypes.c_char_p, ctypes.c_char_p]),
+        "gbp_plan_create": (i, [ctypes.POINTER(Geometry), i, ctypes.POINTER(ctypes.c_int),
+                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(Options), P,
+                                ctypes.POINTER(P)]),
+        "gbp_plan_destroy": (i, [P]),
+        "gbp_plan_set_options": (i, [P, ctypes.POINTER(Options)]),
+        "gbp_plan_device_bytes": (ctypes.c_size_t, [P]),
+        "gbp_nodal_set_sigma_from_density": (i, [P, A4, d, d]),
+        "gbp_nodal_set_sigma": (i, [P, A4, d]),
+        "gbp_nodal_project": (i, [P, A4, A4, A4, i, ctypes.POINTER(Stats)]),
+        "gbp_apply_nodal_projection": (i, [P, A4, A4, A4, d, A4, A4, d, d, d, d, i, i,
+                                           ctypes.POINTER(Stats)]),
+        "gbp_mac_set_beta": (i, [P, A4, A4, A4, d]),
+        "gbp_mac_set_beta_from_density": (i, [P, A4, d]),
+        "gbp_mac_project": (i, [P, A4, A4, A4, A4, i, ctypes.POINTER(Stats)]),
+        "gbp_apply_nodal_projection_host": (i, [P, P, P, d, P, P, d, i, ctypes.POINTER(Stats)]),
+        "gbp_plan_time_kernel": (i, [P, i, i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class ProjectionError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        L = load()
+        msg = L.gbp_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {L.gbp_status_string(status).decode()} ({status}): {msg}")
+        self.status = status
+
+
+def check(status: int, where: str, allow_not_converged: bool = False) -> int:
+    if status == GBP_OK or (allow_not_converged and status == GBP_NOT_CONVERGED):
+        return status
+    raise ProjectionError(status, where)
+
+
+def default_options(kind: int) -> Options:
+    o = Options()
+    check(load().gbp_options_default(kind, ctypes.byref(o)), "gbp_options_default")
+    return o

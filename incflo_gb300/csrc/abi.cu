@@ -1,0 +1,587 @@
+// The C ABI (include/incflo_gb300.h): plans, options (the nodal_proj.* / mac_proj.* inputs surface),
+// and the projection entry points. Never aborts; every failure is a status code plus a message
+// retrievable with gbp_last_error().
+#include <ctype.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+#include <string>
+
+#include "gbp_internal.cuh"
+#include "mac_solver.h"
+#include "nodal_solver.h"
+
+namespace gbp {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return GBP_CUDA_ERROR;
+}
+
+}  // namespace gbp
+
+using namespace gbp;
+
+struct gbp_plan {
+    int kind;
+    cudaStream_t stream;
+    gbp_geometry geom;
+    int bc_lo[3], bc_hi[3];
+    NodalSolver* nodal = nullptr;
+    MacSolver* mac = nullptr;
+    // device staging for the host-buffer entry point
+    double* hbuf = nullptr;
+    size_t hbuf_bytes = 0;
+};
+
+static bool valid_array(const gbp_array4* a, int ncomp_min)
+{
+    return a && a->data && a->ncomp >= ncomp_min && a->jstride > 0 && a->kstride > 0 &&
+           (a->ncomp == 1 || a->nstride > 0);
+}
+
+// the region [lo,hi] (inclusive, per direction) must lie inside the array's allocated bounds
+static bool covers(const gbp_array4* a, const int lo[3], const int hi[3])
+{
+    for (int d = 0; d < 3; ++d)
+        if (lo[d] < a->lo[d] || hi[d] > a->hi[d]) return false;
+    return true;
+}
+
+extern "C" {
+
+int gbp_abi_version(void) { return GBP_ABI_VERSION; }
+
+const char* gbp_status_string(int status)
+{
+    switch (status) {
+    case GBP_OK: return "ok";
+    case GBP_NOT_CONVERGED: return "not converged";
+    case GBP_NAN: return "residual is NaN or Inf";
+    case GBP_BAD_ARG: return "bad argument";
+    case GBP_CUDA_ERROR: return "CUDA error";
+    case GBP_TIMEOUT: return "device wait timed out";
+    case GBP_NO_DEVICE: return "no usable CUDA device";
+    default: return "unknown status";
+    }
+}
+
+const char* gbp_last_error(void) { return g_last_error.c_str(); }
+
+int gbp_device_check(void)
+{
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error("no CUDA device visible");
+        return GBP_NO_DEVICE;
+    }
+    int dev = 0, major = 0, minor = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3) {
+        set_error("this library is built for sm_103 (GB300) only; device is sm_" + std::to_string(major) +
+                  std::to_string(minor));
+        return GBP_NO_DEVICE;
+    }
+    return GBP_OK;
+}
+
+int gbp_options_default(int kind, gbp_options* o)
+{
+    if (!o) return GBP_BAD_ARG;
+    memset(o, 0, sizeof(*o));
+    o->rtol = 1.0e-11;
+    o->atol = 1.0e-14;
+    o->max_coarsening_level = 100;
+    o->maxiter = kind == GBP_MAC ? 200 : 100;
+    o->bottom_maxiter = 200;
+    o->bottom_rtol = 1.0e-4;
+    o->bottom_atol = -1.0;
+    o->verbose = 0;
+    o->bottom_verbose = 0;
+    o->precision = GBP_PREC_FP64;
+    o->nu1 = 2;
+    o->nu2 = 2;
+    o->omega = 0.85;
+    o->ir_inner_cycles = 4;
+    o->use_graphs = 1;
+    o->always_use_bnorm = 1;
+    return GBP_OK;
+}
+
+static bool parse_double(const char* v, double* out)
+{
+    char* end = nullptr;
+    double x = strtod(v, &end);
+    if (end == v) return false;
+    while (*end && isspace((unsigned char)*end)) ++end;
+    if (*end) return false;
+    *out = x;
+    return true;
+}
+
+static bool parse_int(const char* v, int* out)
+{
+    double x;
+    if (!parse_double(v, &x) || x != floor(x)) return false;
+    *out = (int)x;
+    return true;
+}
+
+int gbp_options_set(gbp_options* o, const char* key, const char* value)
+{
+    if (!o || !key || !value) return GBP_BAD_ARG;
+    std::string k(key);
+    std::string v(value);
+    while (!v.empty() && isspace((unsigned char)v.back())) v.pop_back();
+    size_t a = 0;
+    while (a < v.size() && isspace((unsigned char)v[a])) ++a;
+    v = v.substr(a);
+    if (v.size() >= 2 && v.front() == '"' && v.back() == '"') v = v.substr(1, v.size() - 2);
+    const char* s = v.c_str();
+    bool ok = true;
+    if (k == "mg_rtol")
+        ok = parse_double(s, &o->rtol);
+    else if (k == "mg_atol")
+        ok = parse_double(s, &o->atol);
+    else if (k == "mg_max_coarsening_level")
+        ok = parse_int(s, &o->max_coarsening_level);
+    else if (k == "maxiter")
+        ok = parse_int(s, &o->maxiter);
+    else if (k == "bottom_maxiter")
+        ok = parse_int(s, &o->bottom_maxiter);
+    else if (k == "bottom_rtol")
+        ok = parse_double(s, &o->bottom_rtol);
+    else if (k == "bottom_atol")
+        ok = parse_double(s, &o->bottom_atol);
+    else if (k == "verbose")
+        ok = parse_int(s, &o->verbose);
+    else if (k == "bottom_verbose")
+        ok = parse_int(s, &o->bottom_verbose);
+    else if (k == "bottom_solver")
+        // the coarsest level is always solved by conjugate gradients in one CTA; every MLMG bottom
+        // solver name incflo decks use is accepted (InputsMultigrid.rst)
+        ok = v == "bicgstab" || v == "bicgcg" || v == "cg" || v == "cgbicg" || v == "smoother" || v == "hypre" ||
+             v == "petsc" || v == "default";
+    else if (k == "precision") {
+        if (v == "fp64" || v == "double")
+            o->precision = GBP_PREC_FP64;
+        else if (v == "mixed" || v == "fp32-ir")
+            o->precision = GBP_PREC_MIXED;
+        else
+            ok = false;
+    } else if (k == "num_pre_smooth")
+        ok = parse_int(s, &o->nu1);
+    else if (k == "num_post_smooth")
+        ok = parse_int(s, &o->nu2);
+    else if (k == "jacobi_weight")
+        ok = parse_double(s, &o->omega);
+    else if (k == "ir_inner_cycles")
+        ok = parse_int(s, &o->ir_inner_cycles);
+    else if (k == "use_graphs")
+        ok = parse_int(s, &o->use_graphs);
+    else if (k == "always_use_bnorm")
+        ok = parse_int(s, &o->always_use_bnorm);
+    else if (k == "smoother")
+        ok = v == "jacobi" || v == "rbgs" || v == "default";
+    else {
+        set_error("unknown projection option '" + k + "'");
+        return GBP_BAD_ARG;
+    }
+    if (!ok) {
+        set_error("bad value '" + v + "' for projection option '" + k + "'");
+        return GBP_BAD_ARG;
+    }
+    return GBP_OK;
+}
+
+int gbp_options_parse(gbp_options* o, const char* prefix, const char* text)
+{
+    if (!o || !prefix || !text) return GBP_BAD_ARG;
+    const std::string pre = std::string(prefix) + ".";
+    const char* p = text;
+    while (*p) {
+        const char* e = strchr(p, '\n');
+        std::string line = e ? std::string(p, e - p) : std::string(p);
+        p = e ? e + 1 : p + strlen(p);
+        size_t hash = line.find('#');
+        if (hash != std::string::npos) line = line.substr(0, hash);
+        size_t eq = line.find('=');
+        if (eq == std::string::npos) continue;
+        std::string key = line.substr(0, eq);
+        std::string val = line.substr(eq + 1);
+        while (!key.empty() && isspace((unsigned char)key.back())) key.pop_back();
+        size_t a = 0;
+        while (a < key.size() && isspace((unsigned char)key[a])) ++a;
+        key = key.substr(a);
+        if (key.compare(0, pre.size(), pre) != 0) continue;
+        int rc = gbp_options_set(o, key.substr(pre.size()).c_str(), val.c_str());
+        if (rc) return rc;
+    }
+    return GBP_OK;
+}
+
+int gbp_plan_create(const gbp_geometry* geom, int kind, const int bc_lo[3], const int bc_hi[3],
+                    const gbp_options* opt, void* stream, gbp_plan** plan)
+{
+    if (!geom || !bc_lo || !bc_hi || !plan || (kind != GBP_NODAL && kind != GBP_MAC)) {
+        set_error("gbp_plan_create: null argument or unknown kind");
+        return GBP_BAD_ARG;
+    }
+    *plan = nullptr;
+    int rc = gbp_device_check();
+    if (rc) return rc;
+    gbp_options o;
+    if (opt)
+        o = *opt;
+    else
+        gbp_options_default(kind, &o);
+    gbp_plan* p = new (std::nothrow) gbp_plan();
+    if (!p) return GBP_BAD_ARG;
+    p->kind = kind;
+    p->stream = (cudaStream_t)stream;
+    p->geom = *geom;
+    for (int d = 0; d < 3; ++d) {
+        p->bc_lo[d] = bc_lo[d];
+        p->bc_hi[d] = bc_hi[d];
+    }
+    if (kind == GBP_NODAL) {
+        p->nodal = new NodalSolver();
+        rc = p->nodal->init(*geom, bc_lo, bc_hi, o, p->stream);
+    } else {
+        p->mac = new MacSolver();
+        rc = p->mac->init(*geom, bc_lo, bc_hi, o, p->stream);
+    }
+    if (rc) {
+        gbp_plan_destroy(p);
+        return rc;
+    }
+    *plan = p;
+    return GBP_OK;
+}
+
+int gbp_plan_destroy(gbp_plan* p)
+{
+    if (!p) return GBP_OK;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    delete p->nodal;
+    delete p->mac;
+    if (p->hbuf) cudaFree(p->hbuf);
+    delete p;
+    return GBP_OK;
+}
+
+int gbp_plan_set_options(gbp_plan* p, const gbp_options* opt)
+{
+    if (!p || !opt) return GBP_BAD_ARG;
+    return p->nodal ? p->nodal->set_options(*opt) : p->mac->set_options(*opt);
+}
+
+size_t gbp_plan_device_bytes(const gbp_plan* p)
+{
+    if (!p) return 0;
+    size_t b = p->hbuf_bytes;
+    b += p->nodal ? p->nodal->device_bytes() : p->mac->device_bytes();
+    return b;
+}
+
+int gbp_nodal_set_sigma_from_density(gbp_plan* p, const gbp_array4* rho, double scaling_factor, double rho0)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_nodal_set_sigma_from_density: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    if (rho) {
+        const int lo[3] = {0, 0, 0};
+        const int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+        if (!valid_array(rho, 1) || !covers(rho, lo, hi)) {
+            set_error("gbp_nodal_set_sigma_from_density: rho must cover the valid cells");
+            return GBP_BAD_ARG;
+        }
+    }
+    return p->nodal->set_sigma_from_density(rho, scaling_factor, rho0);
+}
+
+int gbp_nodal_set_sigma(gbp_plan* p, const gbp_array4* sigma, double const_sigma)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_nodal_set_sigma: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    if (sigma) {
+        const int lo[3] = {0, 0, 0};
+        const int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+        if (!valid_array(sigma, 1) || !covers(sigma, lo, hi)) {
+            set_error("gbp_nodal_set_sigma: sigma must cover the valid cells");
+            return GBP_BAD_ARG;
+        }
+    }
+    return p->nodal->set_sigma(sigma, const_sigma);
+}
+
+static int check_vel(const gbp_plan* p, const gbp_array4* vel, bool need_ghost)
+{
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        const bool inflow = p->bc_lo[d] == GBP_BC_INFLOW || p->bc_hi[d] == GBP_BC_INFLOW;
+        const int g = (need_ghost && inflow) ? 1 : 0;
+        lo[d] = -g;
+        hi[d] = p->geom.n_cell[d] - 1 + g;
+    }
+    if (!valid_array(vel, 3) || !covers(vel, lo, hi)) {
+        set_error("velocity array must hold 3 components over the valid cells (plus one ghost cell "
+                  "across inflow faces)");
+        return GBP_BAD_ARG;
+    }
+    return GBP_OK;
+}
+
+static int check_cells(const gbp_plan* p, const gbp_array4* a, int ncomp, const char* what)
+{
+    const int lo[3] = {0, 0, 0};
+    const int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+    if (!valid_array(a, ncomp) || !covers(a, lo, hi)) {
+        set_error(std::string(what) + " must cover the valid cells with enough components");
+        return GBP_BAD_ARG;
+    }
+    return GBP_OK;
+}
+
+static int check_nodes(const gbp_plan* p, const gbp_array4* a, const char* what)
+{
+    const int lo[3] = {0, 0, 0};
+    const int hi[3] = {p->geom.n_cell[0], p->geom.n_cell[1], p->geom.n_cell[2]};
+    if (!valid_array(a, 1) || !covers(a, lo, hi)) {
+        set_error(std::string(what) + " must cover nodes 0..n in every direction");
+        return GBP_BAD_ARG;
+    }
+    return GBP_OK;
+}
+
+static void fill_rhs_corr(const gbp_plan* p, RhsArgs& ra, CorrArgs& ca)
+{
+    const NodalGeom& g = p->nodal->geom0();
+    for (int d = 0; d < 3; ++d) {
+        ra.inflow_lo[d] = p->bc_lo[d] == GBP_BC_INFLOW;
+        ra.inflow_hi[d] = p->bc_hi[d] == GBP_BC_INFLOW;
+        ca.inv4h[d] = 1.0 / (4.0 * g.h[d]);
+    }
+    ra.cf[0] = 0.25 * g.h[1] * g.h[2];
+    ra.cf[1] = 0.25 * g.h[0] * g.h[2];
+    ra.cf[2] = 0.25 * g.h[0] * g.h[1];
+}
+
+int gbp_nodal_project(gbp_plan* p, gbp_array4* vel, gbp_array4* phi, gbp_array4* gradphi, int phi_guess,
+                      gbp_stats* stats)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_nodal_project: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    int rc = check_vel(p, vel, true);
+    if (rc) return rc;
+    if (phi && phi->data && (rc = check_nodes(p, phi, "phi"))) return rc;
+    if (gradphi && gradphi->data && (rc = check_cells(p, gradphi, 3, "gradphi"))) return rc;
+    if (phi_guess && !(phi && phi->data)) {
+        set_error("gbp_nodal_project: phi_guess set without phi");
+        return GBP_BAD_ARG;
+    }
+    RhsArgs ra{};
+    CorrArgs ca{};
+    fill_rhs_corr(p, ra, ca);
+    ra.vel = *vel;
+    ca.vel = *vel;
+    if (gradphi) ca.gradphi = *gradphi;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    p->nodal->reset_count();
+    return p->nodal->project(ra, ca, phi, 0, phi_guess ? phi : nullptr, stats);
+}
+
+int gbp_apply_nodal_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
+                               double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
+                               double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_apply_nodal_projection: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    // incflo_apply_nodal_projection.cpp:36: the small-dt form projects (U* - U^n + dt Gp)
+    const bool small_dt = time > 0.0 && dt < 0.1 * prev_dt;
+    const bool sub_old = small_dt || incremental;
+    int rc = check_vel(p, vel, set_inflow_bc != 0);
+    if (rc) return rc;
+    if (sub_old && (rc = check_cells(p, vel_old, 3, "vel_old"))) return rc;
+    if (gp && (rc = check_cells(p, gp, 3, "gp"))) return rc;
+    if (p_nd && (rc = check_nodes(p, p_nd, "p_nd"))) return rc;
+    if (!incremental && !gp) {
+        set_error("gbp_apply_nodal_projection: gp is required (its add-back is part of the projection)");
+        return GBP_BAD_ARG;
+    }
+    p->nodal->reset_count();
+    rc = gbp_nodal_set_sigma_from_density(p, rho, scaling_factor, rho0);
+    if (rc) return rc;
+    RhsArgs ra{};
+    CorrArgs ca{};
+    fill_rhs_corr(p, ra, ca);
+    ra.vel = *vel;
+    if (gp) ra.gp = *gp;
+    if (sub_old) ra.vel_old = *vel_old;
+    ra.add_gp = !incremental;
+    ra.sub_old = sub_old;
+    if (!(set_inflow_bc && !small_dt && !incremental))
+        for (int d = 0; d < 3; ++d) ra.inflow_lo[d] = ra.inflow_hi[d] = 0;
+    ca.vel = *vel;
+    if (gp) ca.gp = *gp;
+    ca.add_gp = !incremental;
+    ca.incremental = incremental;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    return p->nodal->project(ra, ca, p_nd, incremental, nullptr, stats);
+}
+
+int gbp_mac_set_beta(gbp_plan* p, const gbp_array4* bx, const gbp_array4* by, const gbp_array4* bz,
+                     double const_beta)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_mac_set_beta: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    const gbp_array4* src[3] = {bx, by, bz};
+    const bool arrays = bx || by || bz;
+    if (arrays) {
+        for (int d = 0; d < 3; ++d) {
+            int lo[3] = {0, 0, 0};
+            int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+            hi[d] += 1;
+            if (!valid_array(src[d], 1) || !covers(src[d], lo, hi)) {
+                set_error("gbp_mac_set_beta: each beta array must cover its faces 0..n");
+                return GBP_BAD_ARG;
+            }
+        }
+    }
+    return p->mac->set_beta(arrays ? 0 : 1, src, const_beta);
+}
+
+int gbp_mac_set_beta_from_density(gbp_plan* p, const gbp_array4* rho, double dt)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_mac_set_beta_from_density: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) {
+        const bool dir = p->bc_lo[d] == GBP_BC_DIRICHLET || p->bc_hi[d] == GBP_BC_DIRICHLET;
+        lo[d] = (dir && p->bc_lo[d] == GBP_BC_DIRICHLET) ? -1 : 0;
+        hi[d] = p->geom.n_cell[d] - 1 + ((dir && p->bc_hi[d] == GBP_BC_DIRICHLET) ? 1 : 0);
+    }
+    if (!valid_array(rho, 1) || !covers(rho, lo, hi)) {
+        set_error("gbp_mac_set_beta_from_density: rho must cover the valid cells and one ghost cell "
+                  "across Dirichlet faces");
+        return GBP_BAD_ARG;
+    }
+    const gbp_array4* src[3] = {rho, nullptr, nullptr};
+    return p->mac->set_beta(2, src, dt);
+}
+
+int gbp_mac_project(gbp_plan* p, gbp_array4* ux, gbp_array4* uy, gbp_array4* uz, gbp_array4* phi, int phi_guess,
+                    gbp_stats* stats)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_mac_project: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    gbp_array4* u[3] = {ux, uy, uz};
+    for (int d = 0; d < 3; ++d) {
+        int lo[3] = {0, 0, 0};
+        int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+        hi[d] += 1;
+        if (!valid_array(u[d], 1) || !covers(u[d], lo, hi)) {
+            set_error("gbp_mac_project: each umac array must cover its faces 0..n");
+            return GBP_BAD_ARG;
+        }
+    }
+    if (phi && phi->data) {
+        int rc = check_cells(p, phi, 1, "phi");
+        if (rc) return rc;
+    }
+    if (stats) memset(stats, 0, sizeof(*stats));
+    return p->mac->project(u, phi, phi_guess, stats);
+}
+
+int gbp_plan_time_kernel(gbp_plan* p, int which, int reps, double* ms_per_launch, double* bytes_per_launch)
+{
+    if (!p || !p->nodal || !ms_per_launch || !bytes_per_launch) {
+        set_error("gbp_plan_time_kernel: needs a nodal plan and output pointers");
+        return GBP_BAD_ARG;
+    }
+    return p->nodal->time_kernel(which, reps, ms_per_launch, bytes_per_launch);
+}
+
+int gbp_apply_nodal_projection_host(gbp_plan* p, double* vel, const double* rho, double rho0, double* gp,
+                                    double* p_nd, double scaling_factor, int incremental, gbp_stats* stats)
+{
+    if (!p || !p->nodal || !vel || !gp) {
+        set_error("gbp_apply_nodal_projection_host: nodal plan, vel and gp are required");
+        return GBP_BAD_ARG;
+    }
+    const int nx = p->geom.n_cell[0], ny = p->geom.n_cell[1], nz = p->geom.n_cell[2];
+    const size_t nc = (size_t)nx * ny * nz;
+    const size_t nn = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+    const size_t need = (3 * nc + (rho ? nc : 0) + 3 * nc + (p_nd ? nn : 0)) * sizeof(double);
+    if (p->hbuf_bytes < need) {
+        if (p->hbuf) cudaFree(p->hbuf);
+        p->hbuf = nullptr;
+        p->hbuf_bytes = 0;
+        GBP_CUDA(cudaMalloc(&p->hbuf, need));
+        p->hbuf_bytes = need;
+    }
+    double* dvel = p->hbuf;
+    double* dgp = dvel + 3 * nc;
+    double* drho = dgp + 3 * nc;
+    double* dp = drho + (rho ? nc : 0);
+    const cudaStream_t s = p->stream;
+    GBP_CUDA(cudaMemcpyAsync(dvel, vel, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, s));
+    GBP_CUDA(cudaMemcpyAsync(dgp, gp, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (rho) GBP_CUDA(cudaMemcpyAsync(drho, rho, nc * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (p_nd && incremental) GBP_CUDA(cudaMemcpyAsync(dp, p_nd, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    auto cells = [&](double* d, int nc_) {
+        gbp_array4 a{};
+        a.data = d;
+        a.hi[0] = nx - 1;
+        a.hi[1] = ny - 1;
+        a.hi[2] = nz - 1;
+        a.ncomp = nc_;
+        a.jstride = nx;
+        a.kstride = (long long)nx * ny;
+        a.nstride = (long long)nx * ny * nz;
+        return a;
+    };
+    gbp_array4 av = cells(dvel, 3), ag = cells(dgp, 3), ar = cells(drho, 1);
+    gbp_array4 ap{};
+    ap.data = dp;
+    ap.hi[0] = nx;
+    ap.hi[1] = ny;
+    ap.hi[2] = nz;
+    ap.ncomp = 1;
+    ap.jstride = nx + 1;
+    ap.kstride = (long long)(nx + 1) * (ny + 1);
+    ap.nstride = (long long)nn;
+    int rc = gbp_apply_nodal_projection(p, &av, nullptr, rho ? &ar : nullptr, rho0, &ag, p_nd ? &ap : nullptr, 0.0,
+                                        1.0, 1.0, scaling_factor, incremental, 0, stats);
+    if (rc != GBP_OK && rc != GBP_NOT_CONVERGED) return rc;
+    GBP_CUDA(cudaMemcpyAsync(vel, dvel, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GBP_CUDA(cudaMemcpyAsync(gp, dgp, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (p_nd) GBP_CUDA(cudaMemcpyAsync(p_nd, dp, nn * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GBP_CUDA(cudaStreamSynchronize(s));
+    return rc;
+}
+
+}  // extern "C"

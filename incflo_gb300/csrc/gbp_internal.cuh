@@ -1,0 +1,178 @@
+// Internal declarations shared by the projection kernels and the host driver.
+//
+// Device layout of every multigrid level (nodal and cell-centred alike): one padded box
+// that covers indices -1..n+1 in each direction, x fastest, with the x extent rounded up to
+// a multiple of 8 elements so that every row starts on a 64-byte boundary. Entry (i,j,k) of
+// a level sits at (i+1) + sy*(j+1) + sz*(k+1). A cell (i,j,k) and the node (i,j,k) at its low
+// corner share that offset, so nodal stencils address their 8 surrounding cells with the same
+// arithmetic as their 27 neighbouring nodes.
+//
+// Boundaries live in the padding, never in branches of the stencil:
+//   periodic     every kernel that writes a value also writes its periodic aliases
+//                (node 0 -> n, node 1 -> n+1, node n-1 -> -1; cell 0 -> n, cell n-1 -> -1);
+//   non-periodic the padding holds 0: cell coefficients outside the domain are 0, so a node
+//                on a Neumann/inflow face sees only its interior cells (the natural boundary
+//                condition of the weak form) and a MAC Dirichlet face uses a zero ghost with
+//                a doubled face coefficient.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/incflo_gb300.h"
+
+namespace gbp {
+
+constexpr int kMaxLevels = 24;
+
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// Geometry of one nodal level, passed to kernels by value.
+struct NodalGeom {
+    int n[3];      // cells
+    int nu[3];     // unique nodes: n (periodic) or n+1
+    int per[3];
+    int dlo[3];    // Dirichlet face on the low side
+    int dhi[3];
+    long long sy, sz, count;
+    double K[8];   // element stiffness integral(grad N_a . grad N_b) by differing-direction mask
+    double vol;    // cell volume
+    double h[3];
+    int iso;       // hx == hy == hz: K[1] = K[2] = K[4] = 0 and K[3..7] equal
+};
+
+// Geometry of one cell-centred (MAC) level.
+struct CellGeom {
+    int n[3];
+    int per[3];
+    int dlo[3];
+    int dhi[3];
+    long long sy, sz, count;
+    double w[3];   // V / h_d^2: face weight per unit beta
+    double vol;
+    double h[3];
+};
+
+__host__ __device__ inline long long pidx(long long sy, long long sz, int i, int j, int k)
+{
+    return (long long)(i + 1) + sy * (long long)(j + 1) + sz * (long long)(k + 1);
+}
+
+// Positions in the padded box that alias unique node i of a direction with n cells.
+__device__ __forceinline__ int node_aliases(int i, int n, int per, int out[3])
+{
+    out[0] = i;
+    int m = 1;
+    if (per) {
+        if (i == 0) out[m++] = n;
+        if (i == 1) out[m++] = n + 1;
+        if (i == n - 1) out[m++] = -1;
+    }
+    return m;
+}
+
+__device__ __forceinline__ int cell_aliases(int i, int n, int per, int out[3])
+{
+    out[0] = i;
+    int m = 1;
+    if (per) {
+        if (i == 0) out[m++] = n;
+        if (i == n - 1) out[m++] = -1;
+    }
+    return m;
+}
+
+template <typename T>
+__device__ __forceinline__ void store_node(T* a, const NodalGeom& g, int i, int j, int k, T v)
+{
+    int xs[3], ys[3], zs[3];
+    int nx = node_aliases(i, g.n[0], g.per[0], xs);
+    int ny = node_aliases(j, g.n[1], g.per[1], ys);
+    int nz = node_aliases(k, g.n[2], g.per[2], zs);
+    for (int c = 0; c < nz; ++c)
+        for (int b = 0; b < ny; ++b)
+            for (int q = 0; q < nx; ++q) a[pidx(g.sy, g.sz, xs[q], ys[b], zs[c])] = v;
+}
+
+template <typename T>
+__device__ __forceinline__ void store_cell(T* a, const CellGeom& g, int i, int j, int k, T v)
+{
+    int xs[2], ys[2], zs[2];
+    int nx = cell_aliases(i, g.n[0], g.per[0], xs);
+    int ny = cell_aliases(j, g.n[1], g.per[1], ys);
+    int nz = cell_aliases(k, g.n[2], g.per[2], zs);
+    for (int c = 0; c < nz; ++c)
+        for (int b = 0; b < ny; ++b)
+            for (int q = 0; q < nx; ++q) a[pidx(g.sy, g.sz, xs[q], ys[b], zs[c])] = v;
+}
+
+// Sigma of the 8 cells around a node, used with periodic aliases of cells.
+template <typename T>
+__device__ __forceinline__ void store_sigma_cell(T* a, const NodalGeom& g, int i, int j, int k, T v)
+{
+    int xs[2], ys[2], zs[2];
+    int nx = cell_aliases(i, g.n[0], g.per[0], xs);
+    int ny = cell_aliases(j, g.n[1], g.per[1], ys);
+    int nz = cell_aliases(k, g.n[2], g.per[2], zs);
+    for (int c = 0; c < nz; ++c)
+        for (int b = 0; b < ny; ++b)
+            for (int q = 0; q < nx; ++q) a[pidx(g.sy, g.sz, xs[q], ys[b], zs[c])] = v;
+}
+
+__device__ __forceinline__ bool node_is_dirichlet(const NodalGeom& g, int i, int j, int k)
+{
+    return (g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) ||
+           (g.dhi[1] && j == g.n[1]) || (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+}
+
+// Control volume of a node: h per direction, h/2 on a non-periodic boundary.
+__device__ __forceinline__ double node_volume(const NodalGeom& g, int i, int j, int k)
+{
+    double v = g.vol;
+    if (!g.per[0] && (i == 0 || i == g.n[0])) v *= 0.5;
+    if (!g.per[1] && (j == 0 || j == g.n[1])) v *= 0.5;
+    if (!g.per[2] && (k == 0 || k == g.n[2])) v *= 0.5;
+    return v;
+}
+
+// Order-preserving atomic max of a non-negative double (NaN propagates as the largest).
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, double v)
+{
+    unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    if (v != v) bits = 0x7ff8000000000000ull;
+    atomicMax(dst, bits);
+}
+
+__device__ __forceinline__ double block_max(double v)
+{
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    lane = lin & 31;
+    wid = lin >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < nw ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    return v;  // valid in warp 0
+}
+
+// ---------------------------------------------------------------------------------------
+// error reporting
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define GBP_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+    } while (0)
+
+}  // namespace gbp

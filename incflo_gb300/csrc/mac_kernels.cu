@@ -1,0 +1,507 @@
+// MAC (cell-centred) projection kernels: the 7-point flux-form operator div(beta grad phi) with
+// face beta, red-black Gauss-Seidel smoother, residual, restriction (sum of the 8 fine weak-form
+// residuals), piecewise-constant prolongation, single-CTA bottom CG, and the right-hand side /
+// correction kernels of Hydro::MacProjector as driven by incflo
+// (src/convection/incflo_compute_MAC_projected_velocities.cpp:69-133, 272-299).
+//
+// Weak form per cell (volume V): (A phi)_c = sum_faces w_d beta_f (phi_c - phi_nbr), w_d = V/h_d^2.
+// Boundary faces carry an effective beta: 0 on Neumann/inflow faces (no flux), 2*beta on
+// Dirichlet faces with a zero ghost (phi = 0 on the face, linear through the first cell).
+// The right-hand side is g = -V div(umac), the correction umac -= beta_eff grad phi.
+#include <cuda_runtime.h>
+
+#include "gbp_internal.cuh"
+#include "mac_kernels.h"
+
+namespace gbp {
+
+__device__ __forceinline__ bool decode_cell(const CellGeom& g, long long t, int& i, int& j, int& k)
+{
+    const long long nxy = (long long)g.n[0] * g.n[1];
+    if (t >= nxy * g.n[2]) return false;
+    k = (int)(t / nxy);
+    long long r = t - (long long)k * nxy;
+    j = (int)(r / g.n[0]);
+    i = (int)(r - (long long)j * g.n[0]);
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ T mac_Ax(const CellGeom& g, const T* __restrict__ x, const T* __restrict__ bx,
+                                    const T* __restrict__ by, const T* __restrict__ bz, long long p, T& diag,
+                                    T& offsum)
+{
+    const T xc = x[p];
+    const T wx = (T)g.w[0], wy = (T)g.w[1], wz = (T)g.w[2];
+    const T b0 = bx[p] * wx, b1 = bx[p + 1] * wx;
+    const T b2 = by[p] * wy, b3 = by[p + g.sy] * wy;
+    const T b4 = bz[p] * wz, b5 = bz[p + g.sz] * wz;
+    diag = ((b0 + b1) + (b2 + b3)) + (b4 + b5);
+    offsum = ((b0 * x[p - 1] + b1 * x[p + 1]) + (b2 * x[p - g.sy] + b3 * x[p + g.sy])) +
+             (b4 * x[p - g.sz] + b5 * x[p + g.sz]);
+    return ((b0 * (xc - x[p - 1]) + b1 * (xc - x[p + 1])) + (b2 * (xc - x[p - g.sy]) + b3 * (xc - x[p + g.sy]))) +
+           (b4 * (xc - x[p - g.sz]) + b5 * (xc - x[p + g.sz]));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mac_rbgs(CellGeom g, const T* __restrict__ bx, const T* __restrict__ by,
+                                                  const T* __restrict__ bz, const T* __restrict__ b, T* x, int color)
+{
+    // thread t handles the t-th cell of this colour along x
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int hx = (g.n[0] + 1) / 2;
+    const long long rows = (long long)g.n[1] * g.n[2];
+    if (t >= rows * hx) return;
+    const long long row = t / hx;
+    const int k = (int)(row / g.n[1]);
+    const int j = (int)(row - (long long)k * g.n[1]);
+    const int i = 2 * (int)(t - row * hx) + ((j + k + color) & 1);
+    if (i >= g.n[0]) return;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    T diag, off;
+    (void)mac_Ax<T>(g, x, bx, by, bz, p, diag, off);
+    const T v = diag != T(0) ? (b[p] + off) / diag : T(0);
+    store_cell(x, g, i, j, k, v);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mac_resid(CellGeom g, const T* __restrict__ bx, const T* __restrict__ by,
+                                                   const T* __restrict__ bz, const T* __restrict__ x,
+                                                   const T* __restrict__ b, T* __restrict__ r,
+                                                   unsigned long long* norm)
+{
+    int i, j, k;
+    double nv = 0.0;
+    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        T diag, off;
+        const T v = b[p] - mac_Ax<T>(g, x, bx, by, bz, p, diag, off);
+        r[p] = v;
+        if (norm) nv = fabs((double)v) / g.vol;
+    }
+    if (norm) {
+        nv = block_max(nv);
+        if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+    }
+}
+
+template <typename T>
+__global__ void k_mac_restrict(CellGeom gf, CellGeom gc, const T* __restrict__ rf, T* __restrict__ bc)
+{
+    int I, J, K;
+    if (!decode_cell(gc, blockIdx.x * (long long)blockDim.x + threadIdx.x, I, J, K)) return;
+    const long long f = pidx(gf.sy, gf.sz, 2 * I, 2 * J, 2 * K);
+    const T v = ((rf[f] + rf[f + 1]) + (rf[f + gf.sy] + rf[f + 1 + gf.sy])) +
+                ((rf[f + gf.sz] + rf[f + 1 + gf.sz]) + (rf[f + gf.sy + gf.sz] + rf[f + 1 + gf.sy + gf.sz]));
+    bc[pidx(gc.sy, gc.sz, I, J, K)] = v;
+}
+
+template <typename T>
+__global__ void k_mac_prolong_add(CellGeom gf, CellGeom gc, const T* __restrict__ xc, T* __restrict__ xf)
+{
+    int i, j, k;
+    if (!decode_cell(gf, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const long long p = pidx(gf.sy, gf.sz, i, j, k);
+    store_cell(xf, gf, i, j, k, xf[p] + xc[pidx(gc.sy, gc.sz, i >> 1, j >> 1, k >> 1)]);
+}
+
+__device__ double mac_block_sum(double v, double* red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += red[w];
+    return t;
+}
+
+// Jacobi-preconditioned CG in FP64 on the coarsest level, one CTA.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mac_bottom(CellGeom g, const double* __restrict__ bx,
+                                                     const double* __restrict__ by, const double* __restrict__ bz,
+                                                     const T* __restrict__ bin, T* __restrict__ xout,
+                                                     double* __restrict__ scr, int maxiter, double rtol,
+                                                     double atol, int singular)
+{
+    __shared__ double red[32];
+    const long long P = g.count;
+    double* x = scr;
+    double* r = scr + P;
+    double* p = scr + 2 * P;
+    double* q = scr + 3 * P;
+    double* dg = scr + 4 * P;
+    const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
+    for (long long t = threadIdx.x; t < 5 * P; t += blockDim.x) scr[t] = 0.0;
+    __syncthreads();
+    double bs = 0.0;
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_cell(g, t, i, j, k);
+        const long long c = pidx(g.sy, g.sz, i, j, k);
+        const double bv = (double)bin[c];
+        r[c] = bv;
+        bs += bv;
+        double d, off;
+        (void)mac_Ax<double>(g, x, bx, by, bz, c, d, off);
+        dg[c] = d;
+    }
+    if (singular) {
+        const double mean = mac_block_sum(bs, red) / (double)N;
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+            int i, j, k;
+            decode_cell(g, t, i, j, k);
+            r[pidx(g.sy, g.sz, i, j, k)] -= mean;
+        }
+    }
+    __syncthreads();
+    double rz = 0.0, rr = 0.0;
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_cell(g, t, i, j, k);
+        const long long c = pidx(g.sy, g.sz, i, j, k);
+        const double z = dg[c] != 0.0 ? r[c] / dg[c] : 0.0;
+        store_cell(p, g, i, j, k, z);
+        rz += r[c] * z;
+        rr += r[c] * r[c];
+    }
+    rz = mac_block_sum(rz, red);
+    rr = mac_block_sum(rr, red);
+    const double r0 = sqrt(rr);
+    const double target = fmax(rtol * r0, atol > 0 ? atol : 0.0);
+    if (r0 > 0.0) {
+        for (int it = 1; it <= maxiter; ++it) {
+            __syncthreads();
+            double pq = 0.0;
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                int i, j, k;
+                decode_cell(g, t, i, j, k);
+                const long long c = pidx(g.sy, g.sz, i, j, k);
+                double d, off;
+                const double v = mac_Ax<double>(g, p, bx, by, bz, c, d, off);
+                q[c] = v;
+                pq += p[c] * v;
+            }
+            pq = mac_block_sum(pq, red);
+            if (!(pq > 0.0)) break;
+            const double alpha = rz / pq;
+            double rz2 = 0.0;
+            rr = 0.0;
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                int i, j, k;
+                decode_cell(g, t, i, j, k);
+                const long long c = pidx(g.sy, g.sz, i, j, k);
+                x[c] += alpha * p[c];
+                r[c] -= alpha * q[c];
+                const double z = dg[c] != 0.0 ? r[c] / dg[c] : 0.0;
+                q[c] = z;
+                rz2 += r[c] * z;
+                rr += r[c] * r[c];
+            }
+            rz2 = mac_block_sum(rz2, red);
+            rr = mac_block_sum(rr, red);
+            if (sqrt(rr) <= target) break;
+            const double beta = rz2 / rz;
+            rz = rz2;
+            __syncthreads();
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                int i, j, k;
+                decode_cell(g, t, i, j, k);
+                const long long c = pidx(g.sy, g.sz, i, j, k);
+                store_cell(p, g, i, j, k, q[c] + beta * p[c]);
+            }
+        }
+    }
+    __syncthreads();
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_cell(g, t, i, j, k);
+        store_cell(xout, g, i, j, k, (T)x[pidx(g.sy, g.sz, i, j, k)]);
+    }
+}
+
+// ------------------------------------------------------------------ level-0 set-up kernels
+__device__ __forceinline__ double a4(const gbp_array4& a, int i, int j, int k, int n)
+{
+    return a.data[(long long)(i - a.lo[0]) + (long long)(j - a.lo[1]) * a.jstride +
+                  (long long)(k - a.lo[2]) * a.kstride + (long long)n * a.nstride];
+}
+__device__ __forceinline__ double* a4p(const gbp_array4& a, int i, int j, int k, int n)
+{
+    return a.data + (long long)(i - a.lo[0]) + (long long)(j - a.lo[1]) * a.jstride +
+           (long long)(k - a.lo[2]) * a.kstride + (long long)n * a.nstride;
+}
+
+// Effective face beta of direction d for faces 0..n[d]: source 0 = array, 1 = constant,
+// 2 = dt / (0.5 (rho_lo + rho_hi)) (incflo: average_cellcenter_to_face then invert(dt)).
+__global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double cval, int bclo, int bchi,
+                           double* __restrict__ b64, float* __restrict__ b32)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int fn[3] = {g.n[0], g.n[1], g.n[2]};
+    fn[d] += 1;
+    const long long nxy = (long long)fn[0] * fn[1];
+    if (t >= nxy * fn[2]) return;
+    int f[3];
+    f[2] = (int)(t / nxy);
+    const long long rem = t - (long long)f[2] * nxy;
+    f[1] = (int)(rem / fn[0]);
+    f[0] = (int)(rem - (long long)f[1] * fn[0]);
+    const int fd = f[d];
+    const bool per = g.per[d];
+    double beta;
+    int q[3] = {f[0], f[1], f[2]};
+    if (per && fd == g.n[d]) q[d] = 0;  // face n is face 0
+    if (source == 0) {
+        beta = a4(src, q[0], q[1], q[2], 0);
+    } else if (source == 1) {
+        beta = cval;
+    } else {
+        int lo[3] = {q[0], q[1], q[2]};
+        lo[d] -= 1;
+        if (per && lo[d] < 0) lo[d] += g.n[d];
+        beta = cval / (0.5 * (a4(src, lo[0], lo[1], lo[2], 0) + a4(src, q[0], q[1], q[2], 0)));
+    }
+    double eff = beta;
+    if (!per && (fd == 0 || fd == g.n[d])) {
+        const int bc = fd == 0 ? bclo : bchi;
+        eff = bc == GBP_BC_DIRICHLET ? 2.0 * beta : 0.0;
+    }
+    const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
+    b64[p] = eff;
+    b32[p] = (float)eff;
+}
+
+__global__ void k_mac_beta_coarsen(CellGeom gf, CellGeom gc, int d, const double* __restrict__ bf,
+                                   double* __restrict__ bc64, float* __restrict__ bc32)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int fn[3] = {gc.n[0], gc.n[1], gc.n[2]};
+    fn[d] += 1;
+    const long long nxy = (long long)fn[0] * fn[1];
+    if (t >= nxy * fn[2]) return;
+    int f[3];
+    f[2] = (int)(t / nxy);
+    const long long rem = t - (long long)f[2] * nxy;
+    f[1] = (int)(rem / fn[0]);
+    f[0] = (int)(rem - (long long)f[1] * fn[0]);
+    const long long base = pidx(gf.sy, gf.sz, 2 * f[0], 2 * f[1], 2 * f[2]);
+    const long long s1 = d == 0 ? gf.sy : 1;
+    const long long s2 = d == 2 ? gf.sy : gf.sz;
+    const double v = 0.25 * ((bf[base] + bf[base + s1]) + (bf[base + s2] + bf[base + s1 + s2]));
+    const long long p = pidx(gc.sy, gc.sz, f[0], f[1], f[2]);
+    bc64[p] = v;
+    bc32[p] = (float)v;
+}
+
+__global__ void __launch_bounds__(256) k_mac_rhs(CellGeom g, gbp_array4 ux, gbp_array4 uy, gbp_array4 uz,
+                                                 double* __restrict__ b)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const int ip = (g.per[0] && i + 1 == g.n[0]) ? 0 : i + 1;
+    const int jp = (g.per[1] && j + 1 == g.n[1]) ? 0 : j + 1;
+    const int kp = (g.per[2] && k + 1 == g.n[2]) ? 0 : k + 1;
+    const double dv = (a4(ux, ip, j, k, 0) - a4(ux, i, j, k, 0)) / g.h[0] +
+                      (a4(uy, i, jp, k, 0) - a4(uy, i, j, k, 0)) / g.h[1] +
+                      (a4(uz, i, j, kp, 0) - a4(uz, i, j, k, 0)) / g.h[2];
+    b[pidx(g.sy, g.sz, i, j, k)] = -g.vol * dv;
+}
+
+__global__ void __launch_bounds__(256) k_mac_correct(CellGeom g, int d, gbp_array4 u, const double* __restrict__ beta,
+                                                     const double* __restrict__ phi)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int fn[3] = {g.n[0], g.n[1], g.n[2]};
+    fn[d] += 1;
+    const long long nxy = (long long)fn[0] * fn[1];
+    if (t >= nxy * fn[2]) return;
+    int f[3];
+    f[2] = (int)(t / nxy);
+    const long long rem = t - (long long)f[2] * nxy;
+    f[1] = (int)(rem / fn[0]);
+    f[0] = (int)(rem - (long long)f[1] * fn[0]);
+    const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
+    const long long s = d == 0 ? 1 : (d == 1 ? g.sy : g.sz);
+    const double be = beta[p];
+    if (be == 0.0) return;
+    double* up = a4p(u, f[0], f[1], f[2], 0);
+    *up -= be * (phi[p] - phi[p - s]) / g.h[d];
+}
+
+__global__ void k_mac_load_phi(CellGeom g, gbp_array4 in, double* __restrict__ phi)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    store_cell(phi, g, i, j, k, a4(in, i, j, k, 0));
+}
+
+__global__ void k_mac_store_phi(CellGeom g, gbp_array4 out, const double* __restrict__ phi)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    *a4p(out, i, j, k, 0) = phi[pidx(g.sy, g.sz, i, j, k)];
+}
+
+__global__ void __launch_bounds__(256) k_mac_norm(CellGeom g, const double* __restrict__ v, unsigned long long* norm)
+{
+    int i, j, k;
+    double nv = 0.0;
+    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k))
+        nv = fabs(v[pidx(g.sy, g.sz, i, j, k)]) / g.vol;
+    nv = block_max(nv);
+    if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+}
+
+__global__ void k_mac_sums(CellGeom g, const double* __restrict__ v, double* __restrict__ part)
+{
+    __shared__ double red[32];
+    int i, j, k;
+    double acc = 0.0;
+    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) acc = v[pidx(g.sy, g.sz, i, j, k)];
+    acc = mac_block_sum(acc, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// mode 0: b -= mean(b); mode 1: x -= mean(x) with periodic aliases
+__global__ void k_mac_remove_mean(CellGeom g, double* __restrict__ v, const double* __restrict__ part, int nparts,
+                                  int mode)
+{
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int t = threadIdx.x; t < nparts; t += blockDim.x) acc += part[t];
+    acc = mac_block_sum(acc, red);
+    const double c = acc / ((double)g.n[0] * g.n[1] * g.n[2]);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        if (!decode_cell(g, t, i, j, k)) break;
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        if (mode == 0)
+            v[p] -= c * g.vol;
+        else
+            store_cell(v, g, i, j, k, v[p] - c);
+    }
+}
+
+template <typename TE>
+__global__ void k_mac_add_correction(CellGeom g, double* __restrict__ x, const TE* __restrict__ e, double inv_scale)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    store_cell(x, g, i, j, k, x[p] + (double)e[p] * inv_scale);
+}
+
+__global__ void k_mac_to_f32(CellGeom g, const double* __restrict__ r, float* __restrict__ r32, double scale)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    r32[p] = (float)(r[p] * scale);
+}
+
+// ------------------------------------------------------------------------------ launchers
+static inline unsigned nblk(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+static inline long long ncell(const CellGeom& g) { return (long long)g.n[0] * g.n[1] * g.n[2]; }
+static inline long long nface(const CellGeom& g, int d)
+{
+    long long v = 1;
+    for (int e = 0; e < 3; ++e) v *= g.n[e] + (e == d);
+    return v;
+}
+
+template <typename T>
+void mac_rbgs(const CellGeom& g, const T* bx, const T* by, const T* bz, const T* b, T* x, int color, cudaStream_t st)
+{
+    const long long n = (long long)g.n[1] * g.n[2] * ((g.n[0] + 1) / 2);
+    k_mac_rbgs<T><<<nblk(n, 256), 256, 0, st>>>(g, bx, by, bz, b, x, color);
+}
+template <typename T>
+void mac_resid(const CellGeom& g, const T* bx, const T* by, const T* bz, const T* x, const T* b, T* r,
+               unsigned long long* norm, cudaStream_t st)
+{
+    k_mac_resid<T><<<nblk(ncell(g), 256), 256, 0, st>>>(g, bx, by, bz, x, b, r, norm);
+}
+template <typename T>
+void mac_restrict(const CellGeom& gf, const CellGeom& gc, const T* rf, T* bc, cudaStream_t st)
+{
+    k_mac_restrict<T><<<nblk(ncell(gc), 256), 256, 0, st>>>(gf, gc, rf, bc);
+}
+template <typename T>
+void mac_prolong_add(const CellGeom& gf, const CellGeom& gc, const T* xc, T* xf, cudaStream_t st)
+{
+    k_mac_prolong_add<T><<<nblk(ncell(gf), 256), 256, 0, st>>>(gf, gc, xc, xf);
+}
+template <typename T>
+void mac_bottom(const CellGeom& g, const double* bx, const double* by, const double* bz, const T* b, T* x,
+                double* scratch, int maxiter, double rtol, double atol, int singular, cudaStream_t st)
+{
+    k_mac_bottom<T><<<1, 1024, 0, st>>>(g, bx, by, bz, b, x, scratch, maxiter, rtol, atol, singular);
+}
+
+#define GBP_MAC_INST(T)                                                                                        \
+    template void mac_rbgs<T>(const CellGeom&, const T*, const T*, const T*, const T*, T*, int, cudaStream_t); \
+    template void mac_resid<T>(const CellGeom&, const T*, const T*, const T*, const T*, const T*, T*,          \
+                               unsigned long long*, cudaStream_t);                                            \
+    template void mac_restrict<T>(const CellGeom&, const CellGeom&, const T*, T*, cudaStream_t);              \
+    template void mac_prolong_add<T>(const CellGeom&, const CellGeom&, const T*, T*, cudaStream_t);           \
+    template void mac_bottom<T>(const CellGeom&, const double*, const double*, const double*, const T*, T*,   \
+                                double*, int, double, double, int, cudaStream_t);
+GBP_MAC_INST(double)
+GBP_MAC_INST(float)
+
+void mac_set_beta(const CellGeom& g, int d, int source, const gbp_array4* src, double cval, int bclo, int bchi,
+                  double* b64, float* b32, cudaStream_t st)
+{
+    gbp_array4 a{};
+    if (src) a = *src;
+    k_mac_beta<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, source, a, cval, bclo, bchi, b64, b32);
+}
+void mac_coarsen_beta(const CellGeom& gf, const CellGeom& gc, int d, const double* bf, double* bc64, float* bc32,
+                      cudaStream_t st)
+{
+    k_mac_beta_coarsen<<<nblk(nface(gc, d), 256), 256, 0, st>>>(gf, gc, d, bf, bc64, bc32);
+}
+void mac_rhs(const CellGeom& g, const gbp_array4& ux, const gbp_array4& uy, const gbp_array4& uz, double* b,
+             cudaStream_t st)
+{
+    k_mac_rhs<<<nblk(ncell(g), 256), 256, 0, st>>>(g, ux, uy, uz, b);
+}
+void mac_correct(const CellGeom& g, int d, const gbp_array4& u, const double* beta, const double* phi,
+                 cudaStream_t st)
+{
+    k_mac_correct<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, u, beta, phi);
+}
+void mac_load_phi(const CellGeom& g, const gbp_array4& in, double* phi, cudaStream_t st)
+{
+    k_mac_load_phi<<<nblk(ncell(g), 256), 256, 0, st>>>(g, in, phi);
+}
+void mac_store_phi(const CellGeom& g, const gbp_array4& out, const double* phi, cudaStream_t st)
+{
+    k_mac_store_phi<<<nblk(ncell(g), 256), 256, 0, st>>>(g, out, phi);
+}
+void mac_norm(const CellGeom& g, const double* v, unsigned long long* norm, cudaStream_t st)
+{
+    k_mac_norm<<<nblk(ncell(g), 256), 256, 0, st>>>(g, v, norm);
+}
+int mac_partials_needed(const CellGeom& g) { return (int)nblk(ncell(g), 256); }
+void mac_remove_mean(const CellGeom& g, double* v, double* partials, int mode, cudaStream_t st)
+{
+    const unsigned nb = nblk(ncell(g), 256);
+    k_mac_sums<<<nb, 256, 0, st>>>(g, v, partials);
+    k_mac_remove_mean<<<nb < 1024 ? nb : 1024, 256, 0, st>>>(g, v, partials, (int)nb, mode);
+}
+template <typename TE>
+void mac_add_correction(const CellGeom& g, double* x, const TE* e, double inv_scale, cudaStream_t st)
+{
+    k_mac_add_correction<TE><<<nblk(ncell(g), 256), 256, 0, st>>>(g, x, e, inv_scale);
+}
+template void mac_add_correction<double>(const CellGeom&, double*, const double*, double, cudaStream_t);
+template void mac_add_correction<float>(const CellGeom&, double*, const float*, double, cudaStream_t);
+void mac_to_f32(const CellGeom& g, const double* r, float* r32, double scale, cudaStream_t st)
+{
+    k_mac_to_f32<<<nblk(ncell(g), 256), 256, 0, st>>>(g, r, r32, scale);
+}
+
+}  // namespace gbp

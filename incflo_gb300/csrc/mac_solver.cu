@@ -1,0 +1,392 @@
+// MAC multigrid driver (host side): the same residual-correction / iterative-refinement loop as
+// the nodal driver, on the cell-centred 7-point operator with red-black Gauss-Seidel smoothing.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "mac_solver.h"
+
+namespace gbp {
+
+static CellGeom make_cgeom(const int n[3], const double h[3], const int per[3], const int dlo[3], const int dhi[3])
+{
+    CellGeom g;
+    memset(&g, 0, sizeof(g));
+    for (int d = 0; d < 3; ++d) {
+        g.n[d] = n[d];
+        g.per[d] = per[d];
+        g.dlo[d] = per[d] ? 0 : dlo[d];
+        g.dhi[d] = per[d] ? 0 : dhi[d];
+        g.h[d] = h[d];
+    }
+    const long long P0 = round_up(n[0] + 2, 8);
+    g.sy = P0;
+    g.sz = P0 * (long long)(n[1] + 2);
+    g.count = g.sz * (long long)(n[2] + 2);
+    g.vol = h[0] * h[1] * h[2];
+    for (int d = 0; d < 3; ++d) g.w[d] = g.vol / (h[d] * h[d]);
+    return g;
+}
+
+void MacSolver::destroy()
+{
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    if (hnorm) cudaFreeHost(hnorm);
+    hnorm = nullptr;
+    if (cap) cudaStreamDestroy(cap);
+    cap = nullptr;
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (ev2) cudaEventDestroy(ev2);
+    ev0 = ev1 = ev2 = nullptr;
+    pool.release();
+    L.clear();
+    beta_ready = false;
+}
+
+int MacSolver::set_options(const gbp_options& o)
+{
+    if (o.nu1 < 0 || o.nu2 < 0 || o.nu1 + o.nu2 < 1 || o.ir_inner_cycles < 1 || o.maxiter < 0) {
+        set_error("mac options: need nu1+nu2 >= 1, ir_inner_cycles >= 1, maxiter >= 0");
+        return GBP_BAD_ARG;
+    }
+    const int maxc = opt.max_coarsening_level;
+    opt = o;
+    opt.max_coarsening_level = maxc;
+    if (gexec) {
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    return GBP_OK;
+}
+
+int MacSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_hi[3], const gbp_options& o,
+                    cudaStream_t stream)
+{
+    destroy();
+    opt = o;
+    st = stream;
+    int n[3], per[3], dlo[3], dhi[3];
+    double h[3];
+    singular = true;
+    for (int d = 0; d < 3; ++d) {
+        n[d] = geom.n_cell[d];
+        bclo[d] = bc_lo[d];
+        bchi[d] = bc_hi[d];
+        if (n[d] < 2) {
+            set_error("mac plan: every direction needs at least 2 cells");
+            return GBP_BAD_ARG;
+        }
+        h[d] = (geom.prob_hi[d] - geom.prob_lo[d]) / n[d];
+        if (!(h[d] > 0.0)) {
+            set_error("mac plan: prob_hi must exceed prob_lo");
+            return GBP_BAD_ARG;
+        }
+        if ((bc_lo[d] == GBP_BC_PERIODIC) != (bc_hi[d] == GBP_BC_PERIODIC)) {
+            set_error("mac plan: a periodic direction must be periodic on both sides");
+            return GBP_BAD_ARG;
+        }
+        for (int s = 0; s < 2; ++s) {
+            int b = s ? bc_hi[d] : bc_lo[d];
+            if (b == GBP_BC_ROBIN) {
+                set_error("mac plan: Robin (mixed) boundaries are not supported yet");
+                return GBP_BAD_ARG;
+            }
+            if (b < GBP_BC_PERIODIC || b > GBP_BC_INFLOW) {
+                set_error("mac plan: unknown boundary type");
+                return GBP_BAD_ARG;
+            }
+        }
+        per[d] = bc_lo[d] == GBP_BC_PERIODIC;
+        if (per[d] && (n[d] & 1)) {
+            set_error("mac plan: a periodic direction needs an even cell count (red-black ordering)");
+            return GBP_BAD_ARG;
+        }
+        dlo[d] = bc_lo[d] == GBP_BC_DIRICHLET;
+        dhi[d] = bc_hi[d] == GBP_BC_DIRICHLET;
+        if (dlo[d] || dhi[d]) singular = false;
+    }
+    int rc = set_options(o);
+    if (rc) return rc;
+    opt.max_coarsening_level = o.max_coarsening_level;
+    L.clear();
+    int cn[3] = {n[0], n[1], n[2]};
+    double ch[3] = {h[0], h[1], h[2]};
+    for (;;) {
+        MacLevel lv;
+        lv.g = make_cgeom(cn, ch, per, dlo, dhi);
+        L.push_back(lv);
+        bool ok = (int)L.size() <= opt.max_coarsening_level && (int)L.size() < kMaxLevels;
+        for (int d = 0; d < 3; ++d) ok = ok && (cn[d] % 2 == 0) && (cn[d] / 2 >= 2);
+        if (!ok) break;
+        for (int d = 0; d < 3; ++d) {
+            cn[d] /= 2;
+            ch[d] *= 2.0;
+        }
+    }
+    const MacLevel& B = L.back();
+    if ((long long)B.g.n[0] * B.g.n[1] * B.g.n[2] > 200000) {
+        set_error("mac plan: the coarsest level is too large for the single-CTA bottom solver");
+        return GBP_BAD_ARG;
+    }
+    size_t need = 0;
+    auto add = [&](size_t cnt, size_t sz) { need = ((need + 255) & ~size_t(255)) + cnt * sz; };
+    for (auto& lv : L) {
+        for (int q = 0; q < 6; ++q) add(lv.g.count, 8);
+        for (int q = 0; q < 6; ++q) add(lv.g.count, 4);
+    }
+    const CellGeom& G0 = L[0].g;
+    for (int q = 0; q < 3; ++q) add(G0.count, 8);
+    add(mac_partials_needed(G0) + 64, 8);
+    add(5 * B.g.count, 8);
+    add(8, 8);
+    need += 4096;
+    rc = pool.reserve(need);
+    if (rc) return rc;
+    for (auto& lv : L) {
+        for (int d = 0; d < 3; ++d) lv.b64[d] = pool.take<double>(lv.g.count);
+        lv.x64 = pool.take<double>(lv.g.count);
+        lv.rhs64 = pool.take<double>(lv.g.count);
+        lv.r64 = pool.take<double>(lv.g.count);
+        for (int d = 0; d < 3; ++d) lv.b32[d] = pool.take<float>(lv.g.count);
+        lv.x32 = pool.take<float>(lv.g.count);
+        lv.rhs32 = pool.take<float>(lv.g.count);
+        lv.r32 = pool.take<float>(lv.g.count);
+    }
+    phi = pool.take<double>(G0.count);
+    rhs0 = pool.take<double>(G0.count);
+    res = pool.take<double>(G0.count);
+    partials = pool.take<double>(mac_partials_needed(G0) + 64);
+    bscr = pool.take<double>(5 * B.g.count);
+    dnorm = pool.take<unsigned long long>(8);
+    GBP_CUDA(cudaMallocHost(&hnorm, 8 * sizeof(unsigned long long)));
+    memset(hnorm, 0, 8 * sizeof(unsigned long long));
+    GBP_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    GBP_CUDA(cudaEventCreate(&ev0));
+    GBP_CUDA(cudaEventCreate(&ev1));
+    GBP_CUDA(cudaEventCreate(&ev2));
+    return GBP_OK;
+}
+
+int MacSolver::set_beta(int source, const gbp_array4* src[3], double cval)
+{
+    for (int d = 0; d < 3; ++d) {
+        const gbp_array4* s = source == 0 ? src[d] : (source == 2 ? src[0] : nullptr);
+        mac_set_beta(L[0].g, d, source, s, cval, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st);
+    }
+    for (size_t l = 1; l < L.size(); ++l)
+        for (int d = 0; d < 3; ++d)
+            mac_coarsen_beta(L[l - 1].g, L[l].g, d, L[l - 1].b64[d], L[l].b64[d], L[l].b32[d], st);
+    GBP_CUDA(cudaGetLastError());
+    beta_ready = true;
+    return GBP_OK;
+}
+
+template <typename T>
+struct MacBufs;
+template <>
+struct MacBufs<double> {
+    static double* const* b(const MacLevel& l) { return l.b64; }
+    static double* x(const MacLevel& l) { return l.x64; }
+    static double* rhs(const MacLevel& l) { return l.rhs64; }
+    static double* r(const MacLevel& l) { return l.r64; }
+};
+template <>
+struct MacBufs<float> {
+    static float* const* b(const MacLevel& l) { return l.b32; }
+    static float* x(const MacLevel& l) { return l.x32; }
+    static float* rhs(const MacLevel& l) { return l.rhs32; }
+    static float* r(const MacLevel& l) { return l.r32; }
+};
+
+template <typename T>
+void MacSolver::vcycle(int l, const T* b, bool zero)
+{
+    using B = MacBufs<T>;
+    const MacLevel& lv = L[l];
+    const cudaStream_t s = cap_or_st;
+    T* x = B::x(lv);
+    if (l == (int)L.size() - 1) {
+        mac_bottom<T>(lv.g, lv.b64[0], lv.b64[1], lv.b64[2], b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol,
+                      opt.bottom_atol, singular ? 1 : 0, s);
+        return;
+    }
+    T* const* be = B::b(lv);
+    if (zero) cudaMemsetAsync(x, 0, sizeof(T) * lv.g.count, s);
+    for (int q = 0; q < opt.nu1; ++q) {
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 0, s);
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 1, s);
+    }
+    mac_resid<T>(lv.g, be[0], be[1], be[2], x, b, B::r(lv), nullptr, s);
+    const MacLevel& cv = L[l + 1];
+    mac_restrict<T>(lv.g, cv.g, B::r(lv), B::rhs(cv), s);
+    vcycle<T>(l + 1, B::rhs(cv), true);
+    mac_prolong_add<T>(lv.g, cv.g, B::x(cv), x, s);
+    for (int q = 0; q < opt.nu2; ++q) {
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 1, s);
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 0, s);
+    }
+}
+
+void MacSolver::record_iteration()
+{
+    const MacLevel& l0 = L[0];
+    const cudaStream_t s = cap_or_st;
+    if (opt.precision == GBP_PREC_MIXED) {
+        mac_to_f32(l0.g, res, l0.rhs32, scale32, s);
+        vcycle<float>(0, l0.rhs32, true);
+        for (int c = 1; c < opt.ir_inner_cycles; ++c) vcycle<float>(0, l0.rhs32, false);
+        mac_add_correction<float>(l0.g, phi, l0.x32, 1.0 / scale32, s);
+    } else {
+        vcycle<double>(0, res, true);
+        mac_add_correction<double>(l0.g, phi, l0.x64, 1.0, s);
+    }
+    cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), s);
+    mac_resid<double>(l0.g, l0.b64[0], l0.b64[1], l0.b64[2], phi, rhs0, res, dnorm + 1, s);
+    cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+}
+
+int MacSolver::run_iteration()
+{
+    if (!opt.use_graphs) {
+        cap_or_st = st;
+        record_iteration();
+        GBP_CUDA(cudaGetLastError());
+        return GBP_OK;
+    }
+    if (!gexec || gexec_prec != opt.precision || gexec_scale != scale32) {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        cudaGraph_t graph = nullptr;
+        cap_or_st = cap;
+        GBP_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        record_iteration();
+        cudaError_t e = cudaStreamEndCapture(cap, &graph);
+        cap_or_st = st;
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(mac refinement step)");
+        e = cudaGraphInstantiate(&gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            gexec = nullptr;
+            return cuda_fail(e, "cudaGraphInstantiate(mac refinement step)");
+        }
+        gexec_prec = opt.precision;
+        gexec_scale = scale32;
+    }
+    GBP_CUDA(cudaGraphLaunch(gexec, st));
+    return GBP_OK;
+}
+
+static inline double bits_to_double(unsigned long long b)
+{
+    double v;
+    memcpy(&v, &b, sizeof(v));
+    return v;
+}
+
+int MacSolver::solve(bool have_guess, gbp_stats* stats)
+{
+    const MacLevel& l0 = L[0];
+    cap_or_st = st;
+    GBP_CUDA(cudaEventRecord(ev1, st));
+    if (!have_guess) GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
+    GBP_CUDA(cudaMemsetAsync(dnorm, 0, 4 * sizeof(unsigned long long), st));
+    mac_norm(l0.g, rhs0, dnorm, st);
+    mac_resid<double>(l0.g, l0.b64[0], l0.b64[1], l0.b64[2], phi, rhs0, res, dnorm + 1, st);
+    GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    const double bnorm = bits_to_double(hnorm[0]);
+    double rn = bits_to_double(hnorm[1]);
+    if (!isfinite(bnorm) || !isfinite(rn)) {
+        set_error("mac solve: right-hand side or initial residual is not finite");
+        if (stats) stats->status = GBP_NAN;
+        return GBP_NAN;
+    }
+    const double ref = opt.always_use_bnorm ? bnorm : rn;
+    const double target = std::max(opt.rtol * ref, opt.atol);
+    if (bnorm > 0.0) {
+        int ex = 0;
+        frexp(bnorm * l0.g.vol, &ex);
+        scale32 = ldexp(1.0, -ex);
+    }
+    int it = 0, status = GBP_OK;
+    const double r0 = rn;
+    while (rn > target) {
+        if (it >= opt.maxiter) {
+            status = GBP_NOT_CONVERGED;
+            break;
+        }
+        int rc = run_iteration();
+        if (rc) return rc;
+        GBP_CUDA(cudaStreamSynchronize(st));
+        rn = bits_to_double(hnorm[1]);
+        ++it;
+        if (opt.verbose > 1) fprintf(stderr, "gbp mac: iter %d rel resid %.3e\n", it, bnorm > 0 ? rn / bnorm : rn);
+        if (!isfinite(rn)) {
+            status = GBP_NAN;
+            set_error("mac solve: residual became NaN/Inf");
+            break;
+        }
+    }
+    if (singular) mac_remove_mean(l0.g, phi, partials, 1, st);
+    GBP_CUDA(cudaEventRecord(ev2, st));
+    GBP_CUDA(cudaGetLastError());
+    if (stats) {
+        stats->status = status;
+        stats->outer_iters = it + 1;
+        stats->vcycles = it * (opt.precision == GBP_PREC_MIXED ? opt.ir_inner_cycles : 1);
+        stats->num_levels = (int)L.size();
+        stats->rhs_norm = bnorm;
+        stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;
+        stats->final_rel_resid = bnorm > 0 ? rn / bnorm : rn;
+        GBP_CUDA(cudaEventSynchronize(ev2));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev1, ev2);
+        stats->ms_solve = ms;
+    }
+    if (opt.verbose)
+        fprintf(stderr, "gbp mac: %s after %d steps, rel resid %.3e\n", status == GBP_OK ? "converged" : "stopped", it,
+                bnorm > 0 ? rn / bnorm : rn);
+    return status;
+}
+
+int MacSolver::project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats)
+{
+    if (!beta_ready) {
+        set_error("mac project: beta was never set on this plan");
+        return GBP_BAD_ARG;
+    }
+    const MacLevel& l0 = L[0];
+    GBP_CUDA(cudaEventRecord(ev0, st));
+    mac_rhs(l0.g, *u[0], *u[1], *u[2], rhs0, st);
+    if (singular) mac_remove_mean(l0.g, rhs0, partials, 0, st);
+    const bool guess = phi_guess && phi_io && phi_io->data;
+    if (guess) mac_load_phi(l0.g, *phi_io, phi, st);
+    GBP_CUDA(cudaGetLastError());
+    int status = solve(guess, stats);
+    if (status != GBP_OK && status != GBP_NOT_CONVERGED) return status;
+    for (int d = 0; d < 3; ++d) mac_correct(l0.g, d, *u[d], l0.b64[d], phi, st);
+    if (phi_io && phi_io->data) mac_store_phi(l0.g, *phi_io, phi, st);
+    GBP_CUDA(cudaEventRecord(ev2, st));
+    GBP_CUDA(cudaGetLastError());
+    if (stats) {
+        GBP_CUDA(cudaEventSynchronize(ev2));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev2);
+        stats->ms_total = ms;
+        // kernels per V-cycle: 2 sweeps (red, black) per smoothing step, residual, restriction and
+        // prolongation on every level above the bottom, one bottom solve
+        const long long per_v = (long long)(L.size() - 1) * (2LL * (opt.nu1 + opt.nu2) + 3) + 1;
+        const int mixed = opt.precision == GBP_PREC_MIXED;
+        const long long per_step = (mixed ? opt.ir_inner_cycles : 1) * per_v + 2 + mixed;
+        const int steps = stats->outer_iters - 1;
+        stats->kernel_launches = 1 + (singular ? 4 : 0) + (guess ? 1 : 0) + 2 + steps * per_step + 3 +
+                                 ((phi_io && phi_io->data) ? 1 : 0);
+    }
+    return status;
+}
+
+}  // namespace gbp

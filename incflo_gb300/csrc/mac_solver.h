@@ -1,0 +1,58 @@
+// MAC multigrid solver: the replacement of Hydro::MacProjector + MLPoisson/MLABecLaplacian + MLMG for one
+// single-box level (incflo::compute_MAC_projected_velocities,
+// src/convection/incflo_compute_MAC_projected_velocities.cpp:93-133, 272-299).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "gbp_internal.cuh"
+#include "mac_kernels.h"
+#include "nodal_solver.h"
+
+namespace gbp {
+
+struct MacLevel {
+    CellGeom g;
+    double *b64[3] = {}, *x64 = nullptr, *rhs64 = nullptr, *r64 = nullptr;
+    float *b32[3] = {}, *x32 = nullptr, *rhs32 = nullptr, *r32 = nullptr;
+};
+
+class MacSolver {
+public:
+    int init(const gbp_geometry& geom, const int bc_lo[3], const int bc_hi[3], const gbp_options& opt,
+             cudaStream_t stream);
+    void destroy();
+    ~MacSolver() { destroy(); }
+    int set_options(const gbp_options& opt);
+    // source: 0 = arrays, 1 = constant, 2 = dt / face average of rho
+    int set_beta(int source, const gbp_array4* src[3], double cval);
+    int project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats);
+    size_t device_bytes() const { return pool.bytes; }
+
+private:
+    template <typename T>
+    void vcycle(int l, const T* b, bool zero);
+    void record_iteration();
+    int run_iteration();
+    int solve(bool have_guess, gbp_stats* stats);
+
+    gbp_options opt{};
+    cudaStream_t st = nullptr, cap = nullptr, cap_or_st = nullptr;
+    int bclo[3] = {}, bchi[3] = {};
+    std::vector<MacLevel> L;
+    DevicePool pool;
+    double *phi = nullptr, *rhs0 = nullptr, *res = nullptr, *partials = nullptr, *bscr = nullptr;
+    unsigned long long* dnorm = nullptr;
+    unsigned long long* hnorm = nullptr;
+    bool singular = false;
+    bool beta_ready = false;
+    double scale32 = 1.0;
+    cudaGraphExec_t gexec = nullptr;
+    int gexec_prec = -1;
+    double gexec_scale = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+};
+
+}  // namespace gbp

@@ -1,0 +1,759 @@
+// Nodal projection kernels: the Q1 (trilinear finite-element) variable-coefficient operator
+// with cell sigma, its Jacobi smoother, residual, restriction, prolongation, single-CTA
+// bottom solve, and the fused right-hand-side / correction kernels around the solve.
+//
+// Discretisation (the approximate projection behind Hydro::NodalProjector as used by
+// incflo::ApplyNodalProjection, src/projection/incflo_apply_nodal_projection.cpp:95-267):
+//   A_ij = sum over cells c of sigma_c * integral_c(grad N_i . grad N_j)   (weak form, SPD)
+//   g_i  = integral(u . grad N_i) - inflow flux through the boundary        (= -V_i div u)
+//   (grad phi)_c = average over the 4 cell edges of the nodal differences per direction
+//   u_c -= sigma_c (grad phi)_c
+// Relative residuals use the strong form |g_i - (A phi)_i| / V_i, V_i the node's control
+// volume (h^3, halved per non-periodic boundary face), so they measure div(sigma grad phi) -
+// div(u) like the max-norm convergence test of MLMG.
+#include <cuda_runtime.h>
+
+#include "gbp_internal.cuh"
+#include "nodal_kernels.h"
+
+namespace gbp {
+
+// ---------------------------------------------------------------------------------------
+// operator at one node
+// ---------------------------------------------------------------------------------------
+template <typename T>
+struct NodalOp;
+
+// FP64: the isotropic form sums sigma-weighted far-corner sums and subtracts the centre once
+// (fewest FP64 instructions; FP64 issue rate, not HBM, bounds these kernels on GB300).
+template <>
+struct NodalOp<double> {
+    template <bool ISO>
+    __device__ __forceinline__ static double apply(const double* __restrict__ x, const double* __restrict__ s,
+                                                   long long c, long long sy, long long sz,
+                                                   const NodalGeom& g, double& diag)
+    {
+        const double xc = x[c];
+        double acc = 0.0, ssum = 0.0;
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                for (int cx = 0; cx < 2; ++cx) {
+                    const long long cell = c + (cx - 1) + (cy - 1) * sy + (cz - 1) * sz;
+                    const double sg = s[cell];
+                    const long long ox = cx ? 1 : -1, oy = cy ? sy : -sy, oz = cz ? sz : -sz;
+                    ssum += sg;
+                    if (ISO) {
+                        double S = (x[c + ox + oy] + x[c + ox + oz]) + (x[c + oy + oz] + x[c + ox + oy + oz]);
+                        acc = fma(sg, S, acc);
+                    } else {
+                        double t = g.K[1] * (x[c + ox] - xc) + g.K[2] * (x[c + oy] - xc) +
+                                   g.K[4] * (x[c + oz] - xc) + g.K[3] * (x[c + ox + oy] - xc) +
+                                   g.K[5] * (x[c + ox + oz] - xc) + g.K[6] * (x[c + oy + oz] - xc) +
+                                   g.K[7] * (x[c + ox + oy + oz] - xc);
+                        acc = fma(sg, t, acc);
+                    }
+                }
+        diag = g.K[0] * ssum;
+        if (ISO) return g.K[3] * fma(-4.0 * xc, ssum, acc);
+        return acc;
+    }
+};
+
+// FP32: explicit differences to the centre keep the rounding error proportional to the
+// local variation of x rather than to x itself.
+template <>
+struct NodalOp<float> {
+    template <bool ISO>
+    __device__ __forceinline__ static float apply(const float* __restrict__ x, const float* __restrict__ s,
+                                                  long long c, long long sy, long long sz,
+                                                  const NodalGeom& g, float& diag)
+    {
+        const float xc = x[c];
+        float acc = 0.f, ssum = 0.f;
+        const float k1 = (float)g.K[1], k2 = (float)g.K[2], k4 = (float)g.K[4], k3 = (float)g.K[3],
+                    k5 = (float)g.K[5], k6 = (float)g.K[6], k7 = (float)g.K[7];
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                for (int cx = 0; cx < 2; ++cx) {
+                    const long long cell = c + (cx - 1) + (cy - 1) * sy + (cz - 1) * sz;
+                    const float sg = s[cell];
+                    const long long ox = cx ? 1 : -1, oy = cy ? sy : -sy, oz = cz ? sz : -sz;
+                    ssum += sg;
+                    if (ISO) {
+                        float S = ((x[c + ox + oy] - xc) + (x[c + ox + oz] - xc)) +
+                                  ((x[c + oy + oz] - xc) + (x[c + ox + oy + oz] - xc));
+                        acc = fmaf(sg, S, acc);
+                    } else {
+                        float t = k1 * (x[c + ox] - xc) + k2 * (x[c + oy] - xc) + k4 * (x[c + oz] - xc) +
+                                  k3 * (x[c + ox + oy] - xc) + k5 * (x[c + ox + oz] - xc) +
+                                  k6 * (x[c + oy + oz] - xc) + k7 * (x[c + ox + oy + oz] - xc);
+                        acc = fmaf(sg, t, acc);
+                    }
+                }
+        diag = (float)g.K[0] * ssum;
+        if (ISO) return (float)g.K[3] * acc;
+        return acc;
+    }
+};
+
+// Smoother weight / diagonal. A Jacobi smoother only needs an approximate reciprocal, so the
+// FP64 path uses the single-precision reciprocal when the diagonal is in range.
+__device__ __forceinline__ double approx_recip(double d)
+{
+    double a = fabs(d);
+    if (a > 1e-30 && a < 1e30) return (double)__frcp_rn((float)d);
+    return 1.0 / d;
+}
+__device__ __forceinline__ float approx_recip(float d) { return __frcp_rn(d); }
+
+__device__ __forceinline__ bool decode_node(const NodalGeom& g, long long t, int& i, int& j, int& k)
+{
+    const long long nxy = (long long)g.nu[0] * g.nu[1];
+    if (t >= nxy * g.nu[2]) return false;
+    k = (int)(t / nxy);
+    long long r = t - (long long)k * nxy;
+    j = (int)(r / g.nu[0]);
+    i = (int)(r - (long long)j * g.nu[0]);
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------
+// smoother / residual / transfer
+// ---------------------------------------------------------------------------------------
+template <typename T, bool ISO, bool ZERO>
+__global__ void __launch_bounds__(256) k_jacobi(NodalGeom g, const T* __restrict__ s, const T* __restrict__ xin,
+                                                const T* __restrict__ b, T* __restrict__ xout, T omega)
+{
+    int i, j, k;
+    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    T v = T(0);
+    if (!node_is_dirichlet(g, i, j, k)) {
+        const long long c = pidx(g.sy, g.sz, i, j, k);
+        T diag;
+        if (ZERO) {
+            T ssum = T(0);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                ssum += s[c + ((q & 1) - 1) + (((q >> 1) & 1) - 1) * g.sy + (((q >> 2) & 1) - 1) * g.sz];
+            diag = T(g.K[0]) * ssum;
+            v = omega * b[c] * approx_recip(diag);
+        } else {
+            T ax = NodalOp<T>::template apply<ISO>(xin, s, c, g.sy, g.sz, g, diag);
+            v = xin[c] + omega * (b[c] - ax) * approx_recip(diag);
+        }
+    }
+    store_node(xout, g, i, j, k, v);
+}
+
+// r = b - A x, with the strong-form max norm accumulated into *norm when norm != nullptr.
+// NodalOp::apply() evaluates sum_c sigma_c sum_{b != i} K(i,b) (x_b - x_i), which equals
+// (A x)_i because every element row of K sums to zero.
+template <typename T, bool ISO>
+__global__ void __launch_bounds__(256) k_resid(NodalGeom g, const T* __restrict__ s, const T* __restrict__ x,
+                                               const T* __restrict__ b, T* __restrict__ r,
+                                               unsigned long long* norm)
+{
+    int i, j, k;
+    double nv = 0.0;
+    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+        T v = T(0);
+        if (!node_is_dirichlet(g, i, j, k)) {
+            const long long c = pidx(g.sy, g.sz, i, j, k);
+            T diag;
+            T ax = NodalOp<T>::template apply<ISO>(x, s, c, g.sy, g.sz, g, diag);
+            v = b[c] - ax;
+            if (norm) nv = fabs((double)v) / node_volume(g, i, j, k);
+        }
+        store_node(r, g, i, j, k, v);
+    }
+    if (norm) {
+        nv = block_max(nv);
+        if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_restrict(NodalGeom gf, NodalGeom gc, const T* __restrict__ rf,
+                                                  T* __restrict__ bc)
+{
+    int I, J, K;
+    if (!decode_node(gc, blockIdx.x * (long long)blockDim.x + threadIdx.x, I, J, K)) return;
+    T v = T(0);
+    if (!node_is_dirichlet(gc, I, J, K)) {
+        const long long f = pidx(gf.sy, gf.sz, 2 * I, 2 * J, 2 * K);
+        T acc = T(0);
+#pragma unroll
+        for (int c = -1; c <= 1; ++c) {
+            T accy = T(0);
+#pragma unroll
+            for (int b = -1; b <= 1; ++b) {
+                const long long row = f + b * gf.sy + c * gf.sz;
+                T rx = T(0.5) * (rf[row - 1] + rf[row + 1]) + rf[row];
+                accy += (b == 0 ? T(1) : T(0.5)) * rx;
+            }
+            acc += (c == 0 ? T(1) : T(0.5)) * accy;
+        }
+        v = acc;
+    }
+    bc[pidx(gc.sy, gc.sz, I, J, K)] = v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong_add(NodalGeom gf, NodalGeom gc, const T* __restrict__ xc,
+                                                     T* __restrict__ xf)
+{
+    int i, j, k;
+    if (!decode_node(gf, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    if (node_is_dirichlet(gf, i, j, k)) return;
+    const int I0 = i >> 1, J0 = j >> 1, K0 = k >> 1;
+    const int oi = i & 1, oj = j & 1, ok = k & 1;
+    const long long base = pidx(gc.sy, gc.sz, I0, J0, K0);
+    T acc = T(0);
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        if (c && !ok) break;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            if (b && !oj) break;
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                if (a && !oi) break;
+                acc += xc[base + a + b * gc.sy + c * gc.sz];
+            }
+        }
+    }
+    const T w = T(1) / T(1 << (oi + oj + ok));
+    const long long p = pidx(gf.sy, gf.sz, i, j, k);
+    store_node(xf, gf, i, j, k, xf[p] + w * acc);
+}
+
+// ---------------------------------------------------------------------------------------
+// bottom solve: Jacobi-preconditioned CG in FP64 inside one CTA
+// ---------------------------------------------------------------------------------------
+__device__ double block_sum(double v, double* red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += red[w];  // same order in every thread: deterministic
+    return t;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_bottom_cg(NodalGeom g, const double* __restrict__ s,
+                                                    const T* __restrict__ bin, T* __restrict__ xout,
+                                                    double* __restrict__ scr, int maxiter, double rtol,
+                                                    double atol, int* info)
+{
+    __shared__ double red[32];
+    const long long P = g.count;
+    double* x = scr;
+    double* r = scr + P;
+    double* p = scr + 2 * P;
+    double* q = scr + 3 * P;
+    double* dg = scr + 4 * P;
+    const long long N = (long long)g.nu[0] * g.nu[1] * g.nu[2];
+    const bool singular = !(g.dlo[0] || g.dhi[0] || g.dlo[1] || g.dhi[1] || g.dlo[2] || g.dhi[2]);
+
+    // clear the scratch (padding must hold zeros for the stencil)
+    for (long long t = threadIdx.x; t < 5 * P; t += blockDim.x) scr[t] = 0.0;
+    __syncthreads();
+
+    double bs = 0.0;
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        const long long c = pidx(g.sy, g.sz, i, j, k);
+        double bv = node_is_dirichlet(g, i, j, k) ? 0.0 : (double)bin[c];
+        r[c] = bv;
+        bs += bv;
+        double d;
+        double zero_unused = NodalOp<double>::apply<false>(x, s, c, g.sy, g.sz, g, d);
+        (void)zero_unused;
+        dg[c] = d;
+    }
+    if (singular) {
+        // make the right-hand side consistent: remove its component along the null space
+        double tot = block_sum(bs, red);
+        double vtot = 0.0;
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+            int i, j, k;
+            decode_node(g, t, i, j, k);
+            vtot += node_volume(g, i, j, k);
+        }
+        vtot = block_sum(vtot, red);
+        double cfac = tot / vtot;
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+            int i, j, k;
+            decode_node(g, t, i, j, k);
+            r[pidx(g.sy, g.sz, i, j, k)] -= cfac * node_volume(g, i, j, k);
+        }
+    }
+    __syncthreads();
+
+    // z = r / diag, p = z (with periodic aliases)
+    double rz = 0.0, rr = 0.0;
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        const long long c = pidx(g.sy, g.sz, i, j, k);
+        double z = node_is_dirichlet(g, i, j, k) ? 0.0 : r[c] / dg[c];
+        store_node(p, g, i, j, k, z);
+        rz += r[c] * z;
+        rr += r[c] * r[c];
+    }
+    rz = block_sum(rz, red);
+    rr = block_sum(rr, red);
+    const double r0 = sqrt(rr);
+    const double target = fmax(rtol * r0, atol > 0 ? atol : 0.0);
+    int it = 0;
+    if (r0 > 0.0) {
+        for (it = 1; it <= maxiter; ++it) {
+            __syncthreads();
+            double pq = 0.0;
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                int i, j, k;
+                decode_node(g, t, i, j, k);
+                const long long c = pidx(g.sy, g.sz, i, j, k);
+                double d, v = 0.0;
+                if (!node_is_dirichlet(g, i, j, k)) v = NodalOp<double>::apply<false>(p, s, c, g.sy, g.sz, g, d);
+                q[c] = v;
+                pq += p[c] * v;
+            }
+            pq = block_sum(pq, red);
+            if (!(pq > 0.0)) break;
+            const double alpha = rz / pq;
+            double rz2 = 0.0;
+            rr = 0.0;
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                int i, j, k;
+                decode_node(g, t, i, j, k);
+                const long long c = pidx(g.sy, g.sz, i, j, k);
+                x[c] += alpha * p[c];
+                r[c] -= alpha * q[c];
+                double z = node_is_dirichlet(g, i, j, k) ? 0.0 : r[c] / dg[c];
+                q[c] = z;  // reuse q for z
+                rz2 += r[c] * z;
+                rr += r[c] * r[c];
+            }
+            rz2 = block_sum(rz2, red);
+            rr = block_sum(rr, red);
+            if (sqrt(rr) <= target) break;
+            const double beta = rz2 / rz;
+            rz = rz2;
+            __syncthreads();
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                int i, j, k;
+                decode_node(g, t, i, j, k);
+                const long long c = pidx(g.sy, g.sz, i, j, k);
+                store_node(p, g, i, j, k, q[c] + beta * p[c]);
+            }
+        }
+    }
+    __syncthreads();
+    for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        store_node(xout, g, i, j, k, (T)x[pidx(g.sy, g.sz, i, j, k)]);
+    }
+    if (threadIdx.x == 0 && info) {
+        int used = it > maxiter ? maxiter : it;
+        if (used > info[0]) info[0] = used;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// level-0 set-up and the fused kernels around the solve
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ double a4(const gbp_array4& a, int i, int j, int k, int n)
+{
+    return a.data[(long long)(i - a.lo[0]) + (long long)(j - a.lo[1]) * a.jstride +
+                  (long long)(k - a.lo[2]) * a.kstride + (long long)n * a.nstride];
+}
+__device__ __forceinline__ double* a4p(const gbp_array4& a, int i, int j, int k, int n)
+{
+    return a.data + (long long)(i - a.lo[0]) + (long long)(j - a.lo[1]) * a.jstride +
+           (long long)(k - a.lo[2]) * a.kstride + (long long)n * a.nstride;
+}
+
+__global__ void k_sigma_from_rho(NodalGeom g, gbp_array4 rho, int have_rho, double scale, double rho0,
+                                 double* __restrict__ s64, float* __restrict__ s32)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nxy = (long long)g.n[0] * g.n[1];
+    if (t >= nxy * g.n[2]) return;
+    const int k = (int)(t / nxy);
+    const long long rem = t - (long long)k * nxy;
+    const int j = (int)(rem / g.n[0]);
+    const int i = (int)(rem - (long long)j * g.n[0]);
+    const double v = have_rho ? scale / a4(rho, i, j, k, 0) : scale / rho0;
+    store_sigma_cell(s64, g, i, j, k, v);
+    if (s32) store_sigma_cell(s32, g, i, j, k, (float)v);
+}
+
+__global__ void k_sigma_copy(NodalGeom g, gbp_array4 sig, int have_sig, double cval, double* __restrict__ s64,
+                             float* __restrict__ s32)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nxy = (long long)g.n[0] * g.n[1];
+    if (t >= nxy * g.n[2]) return;
+    const int k = (int)(t / nxy);
+    const long long rem = t - (long long)k * nxy;
+    const int j = (int)(rem / g.n[0]);
+    const int i = (int)(rem - (long long)j * g.n[0]);
+    const double v = have_sig ? a4(sig, i, j, k, 0) : cval;
+    store_sigma_cell(s64, g, i, j, k, v);
+    if (s32) store_sigma_cell(s32, g, i, j, k, (float)v);
+}
+
+__global__ void k_sigma_coarsen(NodalGeom gf, NodalGeom gc, const double* __restrict__ sf,
+                                double* __restrict__ sc64, float* __restrict__ sc32)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nxy = (long long)gc.n[0] * gc.n[1];
+    if (t >= nxy * gc.n[2]) return;
+    const int k = (int)(t / nxy);
+    const long long rem = t - (long long)k * nxy;
+    const int j = (int)(rem / gc.n[0]);
+    const int i = (int)(rem - (long long)j * gc.n[0]);
+    const long long f = pidx(gf.sy, gf.sz, 2 * i, 2 * j, 2 * k);
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc += sf[f + (q & 1) + ((q >> 1) & 1) * gf.sy + ((q >> 2) & 1) * gf.sz];
+    const double v = 0.125 * acc;
+    store_sigma_cell(sc64, gc, i, j, k, v);
+    if (sc32) store_sigma_cell(sc32, gc, i, j, k, (float)v);
+}
+
+// g = -(weak divergence) of u' = u + (add_gp ? sigma*gp : 0) - (sub_old ? u_old : 0).
+// Ghost cells enter only across an inflow face, and only with their normal component.
+__global__ void __launch_bounds__(256) k_nodal_rhs(NodalGeom g, RhsArgs a, const double* __restrict__ s64,
+                                                   double* __restrict__ b, unsigned long long* norm)
+{
+    int i, j, k;
+    double nv = 0.0;
+    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+        double acc = 0.0;
+        if (!node_is_dirichlet(g, i, j, k)) {
+            const int idx[3] = {i, j, k};
+#pragma unroll 1
+            for (int q = 0; q < 8; ++q) {
+                const int sel[3] = {q & 1, (q >> 1) & 1, (q >> 2) & 1};
+                int cell[3];
+                int nout = 0, dout = -1;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    int ci = idx[d] - 1 + sel[d];
+                    if (g.per[d]) {
+                        if (ci < 0) ci += g.n[d];
+                        if (ci >= g.n[d]) ci -= g.n[d];
+                    } else if (ci < 0 || ci >= g.n[d]) {
+                        ++nout;
+                        dout = d;
+                    }
+                    cell[d] = ci;
+                }
+                if (nout == 0) {
+                    const double sg = a.add_gp ? s64[pidx(g.sy, g.sz, cell[0], cell[1], cell[2])] : 0.0;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        double u = a4(a.vel, cell[0], cell[1], cell[2], d);
+                        if (a.add_gp) u += a4(a.gp, cell[0], cell[1], cell[2], d) * sg;
+                        if (a.sub_old) u -= a4(a.vel_old, cell[0], cell[1], cell[2], d);
+                        acc += (sel[d] ? a.cf[d] : -a.cf[d]) * u;
+                    }
+                } else if (nout == 1) {
+                    const int inflow = cell[dout] < 0 ? a.inflow_lo[dout] : a.inflow_hi[dout];
+                    if (inflow) {
+                        double u = a4(a.vel, cell[0], cell[1], cell[2], dout);
+                        acc += (sel[dout] ? a.cf[dout] : -a.cf[dout]) * u;
+                    }
+                }
+            }
+            if (norm) nv = fabs(acc) / node_volume(g, i, j, k);
+        }
+        b[pidx(g.sy, g.sz, i, j, k)] = -acc;
+    }
+    if (norm) {
+        nv = block_max(nv);
+        if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+    }
+}
+
+// strong-form max norm max_i |v_i| / V_i over the unique non-Dirichlet nodes
+__global__ void __launch_bounds__(256) k_node_norm(NodalGeom g, const double* __restrict__ v, unsigned long long* norm)
+{
+    int i, j, k;
+    double nv = 0.0;
+    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k))
+        if (!node_is_dirichlet(g, i, j, k)) nv = fabs(v[pidx(g.sy, g.sz, i, j, k)]) / node_volume(g, i, j, k);
+    nv = block_max(nv);
+    if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+}
+
+// Deterministic two-pass sums: per-block partials, then one block folds them.
+__global__ void k_node_sums(NodalGeom g, const double* __restrict__ v, int weighted, double* __restrict__ part)
+{
+    __shared__ double red[32];
+    int i, j, k;
+    double acc = 0.0;
+    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+        double x = v[pidx(g.sy, g.sz, i, j, k)];
+        acc = weighted ? x * node_volume(g, i, j, k) : x;
+    }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// mode 0: b_i -= V_i * sum(b) / sum(V) (consistent right-hand side of a singular system)
+// mode 1: x_i -= sum(V x) / sum(V)       (gauge: volume-weighted mean zero), with aliases
+__global__ void k_remove_mean(NodalGeom g, double* __restrict__ v, const double* __restrict__ part, int nparts,
+                              double vtot, int mode)
+{
+    __shared__ double tot;
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int t = threadIdx.x; t < nparts; t += blockDim.x) acc += part[t];
+    // fold in a fixed order per block (identical in every block)
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) tot = acc;
+    __syncthreads();
+    const double c = tot / vtot;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        if (!decode_node(g, t, i, j, k)) break;
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        if (mode == 0)
+            v[p] -= c * node_volume(g, i, j, k);
+        else
+            store_node(v, g, i, j, k, v[p] - c);
+    }
+}
+
+template <typename TE>
+__global__ void __launch_bounds__(256) k_add_correction(NodalGeom g, double* __restrict__ x, const TE* __restrict__ e,
+                                                        double inv_scale)
+{
+    int i, j, k;
+    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    store_node(x, g, i, j, k, x[p] + (double)e[p] * inv_scale);
+}
+
+__global__ void __launch_bounds__(256) k_to_f32(NodalGeom g, const double* __restrict__ r, float* __restrict__ r32,
+                                                double scale)
+{
+    int i, j, k;
+    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    r32[p] = (float)(r[p] * scale);
+}
+
+// u <- u + (add_gp ? sigma*gp : 0) - sigma*G phi; gradphi <- G phi; gp <- G phi (+= if incremental)
+__global__ void __launch_bounds__(256) k_nodal_correct(NodalGeom g, CorrArgs a, const double* __restrict__ s64,
+                                                       const double* __restrict__ phi)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nxy = (long long)g.n[0] * g.n[1];
+    if (t >= nxy * g.n[2]) return;
+    const int k = (int)(t / nxy);
+    const long long rem = t - (long long)k * nxy;
+    const int j = (int)(rem / g.n[0]);
+    const int i = (int)(rem - (long long)j * g.n[0]);
+    const long long c = pidx(g.sy, g.sz, i, j, k);
+    const long long sy = g.sy, sz = g.sz;
+    const double p000 = phi[c], p100 = phi[c + 1], p010 = phi[c + sy], p110 = phi[c + 1 + sy];
+    const double p001 = phi[c + sz], p101 = phi[c + 1 + sz], p011 = phi[c + sy + sz], p111 = phi[c + 1 + sy + sz];
+    double G[3];
+    G[0] = ((p100 - p000) + (p110 - p010) + (p101 - p001) + (p111 - p011)) * a.inv4h[0];
+    G[1] = ((p010 - p000) + (p110 - p100) + (p011 - p001) + (p111 - p101)) * a.inv4h[1];
+    G[2] = ((p001 - p000) + (p101 - p100) + (p011 - p010) + (p111 - p110)) * a.inv4h[2];
+    const double sg = s64[c];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double* up = a4p(a.vel, i, j, k, d);
+        double u = *up;
+        double gpo = 0.0;
+        if (a.gp.data) gpo = a4(a.gp, i, j, k, d);
+        if (a.add_gp) u += gpo * sg;
+        *up = u - sg * G[d];
+        if (a.gradphi.data) *a4p(a.gradphi, i, j, k, d) = G[d];
+        if (a.gp.data) *a4p(a.gp, i, j, k, d) = a.incremental ? gpo + G[d] : G[d];
+    }
+}
+
+// p_nd (nodal, all nodes 0..n) <- phi (+= if incremental)
+__global__ void k_nodal_store_phi(NodalGeom g, gbp_array4 out, const double* __restrict__ phi, int accumulate)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int n0 = g.n[0] + 1, n1 = g.n[1] + 1, n2 = g.n[2] + 1;
+    const long long nxy = (long long)n0 * n1;
+    if (t >= nxy * n2) return;
+    const int k = (int)(t / nxy);
+    const long long rem = t - (long long)k * nxy;
+    const int j = (int)(rem / n0);
+    const int i = (int)(rem - (long long)j * n0);
+    const double v = phi[pidx(g.sy, g.sz, i, j, k)];
+    double* p = a4p(out, i, j, k, 0);
+    *p = accumulate ? *p + v : v;
+}
+
+__global__ void k_nodal_load_phi(NodalGeom g, gbp_array4 in, double* __restrict__ phi)
+{
+    int i, j, k;
+    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const double v = node_is_dirichlet(g, i, j, k) ? 0.0 : a4(in, i, j, k, 0);
+    store_node(phi, g, i, j, k, v);
+}
+
+// ---------------------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------------------
+static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+static inline long long nunique(const NodalGeom& g) { return (long long)g.nu[0] * g.nu[1] * g.nu[2]; }
+static inline long long ncells(const NodalGeom& g) { return (long long)g.n[0] * g.n[1] * g.n[2]; }
+
+template <typename T>
+void nodal_jacobi(const NodalGeom& g, const T* s, const T* xin, const T* b, T* xout, double omega, bool zero,
+                  cudaStream_t st)
+{
+    const unsigned nb = nblocks(nunique(g), 256);
+    if (zero) {
+        k_jacobi<T, true, true><<<nb, 256, 0, st>>>(g, s, xin, b, xout, (T)omega);
+    } else if (g.iso) {
+        k_jacobi<T, true, false><<<nb, 256, 0, st>>>(g, s, xin, b, xout, (T)omega);
+    } else {
+        k_jacobi<T, false, false><<<nb, 256, 0, st>>>(g, s, xin, b, xout, (T)omega);
+    }
+}
+
+template <typename T>
+void nodal_resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
+                 cudaStream_t st)
+{
+    const unsigned nb = nblocks(nunique(g), 256);
+    if (g.iso)
+        k_resid<T, true><<<nb, 256, 0, st>>>(g, s, x, b, r, norm);
+    else
+        k_resid<T, false><<<nb, 256, 0, st>>>(g, s, x, b, r, norm);
+}
+
+template <typename T>
+void nodal_restrict(const NodalGeom& gf, const NodalGeom& gc, const T* rf, T* bc, cudaStream_t st)
+{
+    k_restrict<T><<<nblocks(nunique(gc), 256), 256, 0, st>>>(gf, gc, rf, bc);
+}
+
+template <typename T>
+void nodal_prolong_add(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T* xf, cudaStream_t st)
+{
+    k_prolong_add<T><<<nblocks(nunique(gf), 256), 256, 0, st>>>(gf, gc, xc, xf);
+}
+
+template <typename T>
+void nodal_bottom(const NodalGeom& g, const double* s64, const T* b, T* x, double* scratch, int maxiter,
+                  double rtol, double atol, int* info, cudaStream_t st)
+{
+    k_bottom_cg<T><<<1, 1024, 0, st>>>(g, s64, b, x, scratch, maxiter, rtol, atol, info);
+}
+
+template void nodal_jacobi<double>(const NodalGeom&, const double*, const double*, const double*, double*, double,
+                                   bool, cudaStream_t);
+template void nodal_jacobi<float>(const NodalGeom&, const float*, const float*, const float*, float*, double, bool,
+                                  cudaStream_t);
+template void nodal_resid<double>(const NodalGeom&, const double*, const double*, const double*, double*,
+                                  unsigned long long*, cudaStream_t);
+template void nodal_resid<float>(const NodalGeom&, const float*, const float*, const float*, float*,
+                                 unsigned long long*, cudaStream_t);
+template void nodal_restrict<double>(const NodalGeom&, const NodalGeom&, const double*, double*, cudaStream_t);
+template void nodal_restrict<float>(const NodalGeom&, const NodalGeom&, const float*, float*, cudaStream_t);
+template void nodal_prolong_add<double>(const NodalGeom&, const NodalGeom&, const double*, double*, cudaStream_t);
+template void nodal_prolong_add<float>(const NodalGeom&, const NodalGeom&, const float*, float*, cudaStream_t);
+template void nodal_bottom<double>(const NodalGeom&, const double*, const double*, double*, double*, int, double,
+                                   double, int*, cudaStream_t);
+template void nodal_bottom<float>(const NodalGeom&, const double*, const float*, float*, double*, int, double,
+                                  double, int*, cudaStream_t);
+
+void nodal_sigma_from_rho(const NodalGeom& g, const gbp_array4* rho, double scale, double rho0, double* s64,
+                          float* s32, cudaStream_t st)
+{
+    gbp_array4 r{};
+    if (rho) r = *rho;
+    k_sigma_from_rho<<<nblocks(ncells(g), 256), 256, 0, st>>>(g, r, rho != nullptr, scale, rho0, s64, s32);
+}
+
+void nodal_sigma_copy(const NodalGeom& g, const gbp_array4* sig, double cval, double* s64, float* s32,
+                      cudaStream_t st)
+{
+    gbp_array4 r{};
+    if (sig) r = *sig;
+    k_sigma_copy<<<nblocks(ncells(g), 256), 256, 0, st>>>(g, r, sig != nullptr, cval, s64, s32);
+}
+
+void nodal_sigma_coarsen(const NodalGeom& gf, const NodalGeom& gc, const double* sf, double* sc64, float* sc32,
+                         cudaStream_t st)
+{
+    k_sigma_coarsen<<<nblocks(ncells(gc), 256), 256, 0, st>>>(gf, gc, sf, sc64, sc32);
+}
+
+void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, unsigned long long* norm,
+               cudaStream_t st)
+{
+    k_nodal_rhs<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, a, s64, b, norm);
+}
+
+void nodal_remove_mean(const NodalGeom& g, double* v, double* partials, int mode, cudaStream_t st)
+{
+    const unsigned nb = nblocks(nunique(g), 256);
+    k_node_sums<<<nb, 256, 0, st>>>(g, v, mode == 1, partials);
+    const double vtot = (double)g.n[0] * g.h[0] * (double)g.n[1] * g.h[1] * (double)g.n[2] * g.h[2];
+    unsigned nb2 = nb < 1024 ? nb : 1024;
+    k_remove_mean<<<nb2, 256, 0, st>>>(g, v, partials, (int)nb, vtot, mode);
+}
+
+void nodal_norm(const NodalGeom& g, const double* v, unsigned long long* norm, cudaStream_t st)
+{
+    k_node_norm<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, v, norm);
+}
+
+int nodal_partials_needed(const NodalGeom& g) { return (int)nblocks(nunique(g), 256); }
+
+template <typename TE>
+void nodal_add_correction(const NodalGeom& g, double* x, const TE* e, double inv_scale, cudaStream_t st)
+{
+    k_add_correction<TE><<<nblocks(nunique(g), 256), 256, 0, st>>>(g, x, e, inv_scale);
+}
+template void nodal_add_correction<double>(const NodalGeom&, double*, const double*, double, cudaStream_t);
+template void nodal_add_correction<float>(const NodalGeom&, double*, const float*, double, cudaStream_t);
+
+void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale, cudaStream_t st)
+{
+    k_to_f32<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, r, r32, scale);
+}
+
+void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st)
+{
+    k_nodal_correct<<<nblocks(ncells(g), 256), 256, 0, st>>>(g, a, s64, phi);
+}
+
+void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* phi, int accumulate, cudaStream_t st)
+{
+    const long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
+    k_nodal_store_phi<<<nblocks(n, 256), 256, 0, st>>>(g, out, phi, accumulate);
+}
+
+void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaStream_t st)
+{
+    k_nodal_load_phi<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, in, phi);
+}
+
+}  // namespace gbp

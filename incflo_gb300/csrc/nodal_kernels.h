@@ -1,0 +1,65 @@
+// Host-side launchers of the nodal projection kernels (nodal_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gbp_internal.cuh"
+
+namespace gbp {
+
+// Inputs of the fused right-hand-side kernel: u' = u + (add_gp ? sigma*gp : 0) - (sub_old ? u_old : 0)
+struct RhsArgs {
+    gbp_array4 vel;
+    gbp_array4 gp;
+    gbp_array4 vel_old;
+    int add_gp;
+    int sub_old;
+    int inflow_lo[3];
+    int inflow_hi[3];
+    double cf[3];  // h_e h_f / 4: integral of dN/dx_d over one cell, up to sign
+};
+
+// Outputs of the fused correction kernel.
+struct CorrArgs {
+    gbp_array4 vel;
+    gbp_array4 gp;       // data == nullptr: not written
+    gbp_array4 gradphi;  // data == nullptr: not written
+    int add_gp;
+    int incremental;
+    double inv4h[3];
+};
+
+template <typename T>
+void nodal_jacobi(const NodalGeom& g, const T* s, const T* xin, const T* b, T* xout, double omega, bool zero,
+                  cudaStream_t st);
+template <typename T>
+void nodal_resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
+                 cudaStream_t st);
+template <typename T>
+void nodal_restrict(const NodalGeom& gf, const NodalGeom& gc, const T* rf, T* bc, cudaStream_t st);
+template <typename T>
+void nodal_prolong_add(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T* xf, cudaStream_t st);
+template <typename T>
+void nodal_bottom(const NodalGeom& g, const double* s64, const T* b, T* x, double* scratch, int maxiter,
+                  double rtol, double atol, int* info, cudaStream_t st);
+
+void nodal_sigma_from_rho(const NodalGeom& g, const gbp_array4* rho, double scale, double rho0, double* s64,
+                          float* s32, cudaStream_t st);
+void nodal_sigma_copy(const NodalGeom& g, const gbp_array4* sig, double cval, double* s64, float* s32,
+                      cudaStream_t st);
+void nodal_sigma_coarsen(const NodalGeom& gf, const NodalGeom& gc, const double* sf, double* sc64, float* sc32,
+                         cudaStream_t st);
+void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, unsigned long long* norm,
+               cudaStream_t st);
+// mode 0: make b consistent (remove V-weighted mean); mode 1: gauge x to zero V-weighted mean
+void nodal_remove_mean(const NodalGeom& g, double* v, double* partials, int mode, cudaStream_t st);
+int nodal_partials_needed(const NodalGeom& g);
+void nodal_norm(const NodalGeom& g, const double* v, unsigned long long* norm, cudaStream_t st);
+template <typename TE>
+void nodal_add_correction(const NodalGeom& g, double* x, const TE* e, double inv_scale, cudaStream_t st);
+void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale, cudaStream_t st);
+void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st);
+void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* phi, int accumulate, cudaStream_t st);
+void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaStream_t st);
+
+}  // namespace gbp

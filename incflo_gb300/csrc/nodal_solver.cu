@@ -1,0 +1,560 @@
+// Nodal multigrid driver (host side). One plan = one level geometry + boundary set, kept across
+// calls; the reference rebuilds its NodalProjector on every projection
+// (src/projection/incflo_apply_nodal_projection.cpp:124,187-192).
+//
+// Solve structure (residual-correction form, the same loop for both precisions):
+//   r = g - A phi (FP64, max norm on the device)        -> stop when |r| <= max(rtol |g|, atol)
+//   e = V-cycle(r)   FP64 levels            (plain form)
+//     = m V-cycles on (float) r, FP64 bottom (mixed form: FP32 inner solve of iterative refinement)
+//   phi += e
+// One refinement step (V-cycles + update + residual + norm read-back) is captured once as a
+// CUDA graph and replayed; the host reads one 8-byte norm per step.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "nodal_solver.h"
+
+namespace gbp {
+
+int DevicePool::reserve(size_t nbytes)
+{
+    release();
+    cudaError_t e = cudaMalloc(&base, nbytes);
+    if (e != cudaSuccess) {
+        base = nullptr;
+        return cuda_fail(e, "cudaMalloc(plan pool)");
+    }
+    bytes = nbytes;
+    used = 0;
+    e = cudaMemset(base, 0, nbytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset(plan pool)");
+    return GBP_OK;
+}
+
+void DevicePool::release()
+{
+    if (base) cudaFree(base);
+    base = nullptr;
+    bytes = used = 0;
+}
+
+static void q1_element(const double h[3], double K[8])
+{
+    const double V = h[0] * h[1] * h[2];
+    for (int mask = 0; mask < 8; ++mask) {
+        double acc = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            double t = ((mask >> d) & 1) ? -1.0 : 1.0;
+            t /= h[d] * h[d];
+            for (int e = 0; e < 3; ++e) {
+                if (e == d) continue;
+                t *= ((mask >> e) & 1) ? (1.0 / 6.0) : (1.0 / 3.0);
+            }
+            acc += t;
+        }
+        K[mask] = V * acc;
+    }
+}
+
+static NodalGeom make_geom(const int n[3], const double h[3], const int per[3], const int dlo[3], const int dhi[3])
+{
+    NodalGeom g;
+    memset(&g, 0, sizeof(g));
+    for (int d = 0; d < 3; ++d) {
+        g.n[d] = n[d];
+        g.per[d] = per[d];
+        g.nu[d] = per[d] ? n[d] : n[d] + 1;
+        g.dlo[d] = per[d] ? 0 : dlo[d];
+        g.dhi[d] = per[d] ? 0 : dhi[d];
+        g.h[d] = h[d];
+    }
+    const long long P0 = round_up(n[0] + 3, 8);
+    g.sy = P0;
+    g.sz = P0 * (long long)(n[1] + 3);
+    g.count = g.sz * (long long)(n[2] + 3);
+    q1_element(h, g.K);
+    g.vol = h[0] * h[1] * h[2];
+    const double hm = std::max(h[0], std::max(h[1], h[2]));
+    g.iso = fabs(h[0] - h[1]) <= 1e-12 * hm && fabs(h[0] - h[2]) <= 1e-12 * hm;
+    if (g.iso) {
+        // equal spacing: edge-neighbour couplings vanish, the four far corners share one weight
+        const double kc = (g.K[3] + g.K[5] + g.K[6] + g.K[7]) * 0.25;
+        g.K[1] = g.K[2] = g.K[4] = 0.0;
+        g.K[3] = g.K[5] = g.K[6] = g.K[7] = kc;
+        g.K[0] = -4.0 * kc;
+    }
+    return g;
+}
+
+void NodalSolver::destroy()
+{
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    if (hnorm) cudaFreeHost(hnorm);
+    hnorm = nullptr;
+    if (cap) cudaStreamDestroy(cap);
+    cap = nullptr;
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (ev2) cudaEventDestroy(ev2);
+    ev0 = ev1 = ev2 = nullptr;
+    pool.release();
+    L.clear();
+    sigma_ready = false;
+}
+
+int NodalSolver::set_options(const gbp_options& o)
+{
+    if (o.nu1 < 0 || o.nu2 < 0 || o.nu1 + o.nu2 < 1 || !(o.omega > 0.0 && o.omega < 2.0) ||
+        o.ir_inner_cycles < 1 || o.maxiter < 0) {
+        set_error("nodal options: need nu1+nu2 >= 1, 0 < omega < 2, ir_inner_cycles >= 1, maxiter >= 0");
+        return GBP_BAD_ARG;
+    }
+    const bool regraph = o.precision != opt.precision || o.nu1 != opt.nu1 || o.nu2 != opt.nu2 ||
+                         o.omega != opt.omega || o.ir_inner_cycles != opt.ir_inner_cycles ||
+                         o.bottom_maxiter != opt.bottom_maxiter || o.bottom_rtol != opt.bottom_rtol ||
+                         o.bottom_atol != opt.bottom_atol;
+    const int maxc = opt.max_coarsening_level;
+    opt = o;
+    opt.max_coarsening_level = maxc;  // hierarchy depth is fixed at plan creation
+    if (regraph && gexec) {
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    return GBP_OK;
+}
+
+int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_hi[3], const gbp_options& o,
+                      cudaStream_t stream)
+{
+    destroy();
+    opt = o;
+    st = stream;
+    int n[3], per[3], dlo[3], dhi[3];
+    double h[3];
+    singular = true;
+    for (int d = 0; d < 3; ++d) {
+        n[d] = geom.n_cell[d];
+        if (n[d] < 2) {
+            set_error("nodal plan: every direction needs at least 2 cells");
+            return GBP_BAD_ARG;
+        }
+        h[d] = (geom.prob_hi[d] - geom.prob_lo[d]) / n[d];
+        if (!(h[d] > 0.0)) {
+            set_error("nodal plan: prob_hi must exceed prob_lo");
+            return GBP_BAD_ARG;
+        }
+        if ((bc_lo[d] == GBP_BC_PERIODIC) != (bc_hi[d] == GBP_BC_PERIODIC)) {
+            set_error("nodal plan: a periodic direction must be periodic on both sides");
+            return GBP_BAD_ARG;
+        }
+        for (int s = 0; s < 2; ++s) {
+            int b = s ? bc_hi[d] : bc_lo[d];
+            if (b < GBP_BC_PERIODIC || b > GBP_BC_INFLOW) {
+                set_error("nodal plan: boundary type must be periodic, Dirichlet, Neumann or inflow");
+                return GBP_BAD_ARG;
+            }
+        }
+        per[d] = bc_lo[d] == GBP_BC_PERIODIC;
+        dlo[d] = bc_lo[d] == GBP_BC_DIRICHLET;
+        dhi[d] = bc_hi[d] == GBP_BC_DIRICHLET;
+        if (dlo[d] || dhi[d]) singular = false;
+    }
+    int rc = set_options(o);
+    if (rc) return rc;
+    opt.max_coarsening_level = o.max_coarsening_level;
+    // hierarchy: coarsen by 2 while every direction stays even with >= 2 coarse cells
+    L.clear();
+    int cn[3] = {n[0], n[1], n[2]};
+    double ch[3] = {h[0], h[1], h[2]};
+    for (;;) {
+        NodalLevel lv;
+        lv.g = make_geom(cn, ch, per, dlo, dhi);
+        L.push_back(lv);
+        bool ok = (int)L.size() <= opt.max_coarsening_level && (int)L.size() < kMaxLevels;
+        for (int d = 0; d < 3; ++d) ok = ok && (cn[d] % 2 == 0) && (cn[d] / 2 >= 2);
+        if (!ok) break;
+        for (int d = 0; d < 3; ++d) {
+            cn[d] /= 2;
+            ch[d] *= 2.0;
+        }
+    }
+    const NodalLevel& B = L.back();
+    if ((long long)B.g.nu[0] * B.g.nu[1] * B.g.nu[2] > 200000) {
+        set_error("nodal plan: the coarsest level is too large for the single-CTA bottom solver "
+                  "(cell counts need more factors of 2)");
+        return GBP_BAD_ARG;
+    }
+    // one device pool for the whole plan, zeroed so that all padding holds 0
+    size_t need = 0;
+    auto add = [&](size_t cnt, size_t sz) { need = ((need + 255) & ~size_t(255)) + cnt * sz; };
+    for (auto& lv : L) {
+        for (int q = 0; q < 5; ++q) add(lv.g.count, 8);
+        for (int q = 0; q < 5; ++q) add(lv.g.count, 4);
+    }
+    const NodalGeom& G0 = L[0].g;
+    for (int q = 0; q < 3; ++q) add(G0.count, 8);
+    add(nodal_partials_needed(G0) + 64, 8);
+    add(5 * B.g.count, 8);
+    add(16, 4);
+    add(8, 8);
+    need += 4096;
+    rc = pool.reserve(need);
+    if (rc) return rc;
+    for (auto& lv : L) {
+        lv.s64 = pool.take<double>(lv.g.count);
+        lv.x64 = pool.take<double>(lv.g.count);
+        lv.t64 = pool.take<double>(lv.g.count);
+        lv.b64 = pool.take<double>(lv.g.count);
+        lv.r64 = pool.take<double>(lv.g.count);
+        lv.s32 = pool.take<float>(lv.g.count);
+        lv.x32 = pool.take<float>(lv.g.count);
+        lv.t32 = pool.take<float>(lv.g.count);
+        lv.b32 = pool.take<float>(lv.g.count);
+        lv.r32 = pool.take<float>(lv.g.count);
+    }
+    phi = pool.take<double>(G0.count);
+    rhs0 = pool.take<double>(G0.count);
+    res = pool.take<double>(G0.count);
+    partials = pool.take<double>(nodal_partials_needed(G0) + 64);
+    bscr = pool.take<double>(5 * B.g.count);
+    dinfo = pool.take<int>(16);
+    dnorm = pool.take<unsigned long long>(8);
+    GBP_CUDA(cudaMallocHost(&hnorm, 8 * sizeof(unsigned long long)));
+    memset(hnorm, 0, 8 * sizeof(unsigned long long));
+    GBP_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    GBP_CUDA(cudaEventCreate(&ev0));
+    GBP_CUDA(cudaEventCreate(&ev1));
+    GBP_CUDA(cudaEventCreate(&ev2));
+    return GBP_OK;
+}
+
+int NodalSolver::set_sigma_from_density(const gbp_array4* rho, double scale, double rho0)
+{
+    if (!rho && !(rho0 > 0.0)) {
+        set_error("sigma: constant density rho0 must be positive");
+        return GBP_BAD_ARG;
+    }
+    nodal_sigma_from_rho(L[0].g, rho, scale, rho0, L[0].s64, L[0].s32, st);
+    for (size_t l = 1; l < L.size(); ++l)
+        nodal_sigma_coarsen(L[l - 1].g, L[l].g, L[l - 1].s64, L[l].s64, L[l].s32, st);
+    nk += (long long)L.size();
+    GBP_CUDA(cudaGetLastError());
+    sigma_ready = true;
+    return GBP_OK;
+}
+
+int NodalSolver::set_sigma(const gbp_array4* sigma, double cval)
+{
+    nodal_sigma_copy(L[0].g, sigma, cval, L[0].s64, L[0].s32, st);
+    for (size_t l = 1; l < L.size(); ++l)
+        nodal_sigma_coarsen(L[l - 1].g, L[l].g, L[l - 1].s64, L[l].s64, L[l].s32, st);
+    nk += (long long)L.size();
+    GBP_CUDA(cudaGetLastError());
+    sigma_ready = true;
+    return GBP_OK;
+}
+
+template <>
+void NodalSolver::bottom<double>(int l, const double* b, double* x)
+{
+    const NodalLevel& lv = L[l];
+    nodal_bottom<double>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
+                         cap_or_st);
+    xres[l] = x;
+}
+
+template <>
+void NodalSolver::bottom<float>(int l, const float* b, float* x)
+{
+    const NodalLevel& lv = L[l];
+    nodal_bottom<float>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
+                        cap_or_st);
+    xres[l] = x;
+}
+
+template <typename T>
+struct LevelBufs;
+template <>
+struct LevelBufs<double> {
+    static double* s(const NodalLevel& l) { return l.s64; }
+    static double* x(const NodalLevel& l) { return l.x64; }
+    static double* t(const NodalLevel& l) { return l.t64; }
+    static double* b(const NodalLevel& l) { return l.b64; }
+    static double* r(const NodalLevel& l) { return l.r64; }
+};
+template <>
+struct LevelBufs<float> {
+    static float* s(const NodalLevel& l) { return l.s32; }
+    static float* x(const NodalLevel& l) { return l.x32; }
+    static float* t(const NodalLevel& l) { return l.t32; }
+    static float* b(const NodalLevel& l) { return l.b32; }
+    static float* r(const NodalLevel& l) { return l.r32; }
+};
+
+// V-cycle for A x = b on level l. zero: x starts at 0; otherwise from xres[l].
+template <typename T>
+void NodalSolver::vcycle(int l, const T* b, bool zero)
+{
+    using B = LevelBufs<T>;
+    const NodalLevel& lv = L[l];
+    const cudaStream_t s = cap_or_st;
+    if (l == (int)L.size() - 1) {
+        bottom<T>(l, b, B::x(lv));
+        ++nk;
+        return;
+    }
+    T* x = zero ? B::x(lv) : (T*)xres[l];
+    T* t = (x == B::x(lv)) ? B::t(lv) : B::x(lv);
+    int pre = opt.nu1;
+    if (zero) {
+        if (pre > 0) {
+            nodal_jacobi<T>(lv.g, B::s(lv), nullptr, b, x, opt.omega, true, s);
+            ++nk;
+            --pre;
+        } else {
+            cudaMemsetAsync(x, 0, sizeof(T) * lv.g.count, s);
+        }
+    }
+    for (int q = 0; q < pre; ++q) {
+        nodal_jacobi<T>(lv.g, B::s(lv), x, b, t, opt.omega, false, s);
+        ++nk;
+        std::swap(x, t);
+    }
+    nodal_resid<T>(lv.g, B::s(lv), x, b, B::r(lv), nullptr, s);
+    const NodalLevel& cv = L[l + 1];
+    nodal_restrict<T>(lv.g, cv.g, B::r(lv), B::b(cv), s);
+    nk += 2;
+    vcycle<T>(l + 1, B::b(cv), true);
+    nodal_prolong_add<T>(lv.g, cv.g, (const T*)xres[l + 1], x, s);
+    ++nk;
+    for (int q = 0; q < opt.nu2; ++q) {
+        nodal_jacobi<T>(lv.g, B::s(lv), x, b, t, opt.omega, false, s);
+        ++nk;
+        std::swap(x, t);
+    }
+    xres[l] = x;
+}
+
+// one refinement step, issued on cap_or_st: V-cycle(s) on res, phi += e, res = g - A phi, norm
+void NodalSolver::record_iteration()
+{
+    const NodalLevel& l0 = L[0];
+    const cudaStream_t s = cap_or_st;
+    const long long nk0 = nk;
+    if (opt.precision == GBP_PREC_MIXED) {
+        nodal_to_f32(l0.g, res, l0.b32, scale32, s);
+        vcycle<float>(0, l0.b32, true);
+        for (int c = 1; c < opt.ir_inner_cycles; ++c) vcycle<float>(0, l0.b32, false);
+        nodal_add_correction<float>(l0.g, phi, (const float*)xres[0], 1.0 / scale32, s);
+        ++nk;
+    } else {
+        vcycle<double>(0, res, true);
+        nodal_add_correction<double>(l0.g, phi, (const double*)xres[0], 1.0, s);
+    }
+    cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), s);
+    nodal_resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, s);
+    nk += 2;
+    cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+    step_kernels = nk - nk0;
+}
+
+int NodalSolver::run_iteration()
+{
+    if (!opt.use_graphs) {
+        cap_or_st = st;
+        record_iteration();
+        GBP_CUDA(cudaGetLastError());
+        return GBP_OK;
+    }
+    if (!gexec || gexec_prec != opt.precision || gexec_scale != scale32) {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        cudaGraph_t graph = nullptr;
+        cap_or_st = cap;
+        GBP_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        record_iteration();
+        cudaError_t e = cudaStreamEndCapture(cap, &graph);
+        cap_or_st = st;
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(refinement step)");
+        e = cudaGraphInstantiate(&gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            gexec = nullptr;
+            return cuda_fail(e, "cudaGraphInstantiate(refinement step)");
+        }
+        gexec_prec = opt.precision;
+        gexec_scale = scale32;
+        nk -= step_kernels;  // capture issued nothing; the launch below runs them
+    }
+    GBP_CUDA(cudaGraphLaunch(gexec, st));
+    nk += step_kernels;
+    return GBP_OK;
+}
+
+static inline double bits_to_double(unsigned long long b)
+{
+    double v;
+    memcpy(&v, &b, sizeof(v));
+    return v;
+}
+
+int NodalSolver::solve(bool have_guess, gbp_stats* stats)
+{
+    const NodalLevel& l0 = L[0];
+    cap_or_st = st;
+    GBP_CUDA(cudaEventRecord(ev1, st));
+    if (!have_guess) GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
+    GBP_CUDA(cudaMemsetAsync(dnorm, 0, 4 * sizeof(unsigned long long), st));
+    GBP_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int), st));
+    nodal_norm(l0.g, rhs0, dnorm, st);
+    nodal_resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
+    nk += 2;
+    GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    const double bnorm = bits_to_double(hnorm[0]);
+    double rn = bits_to_double(hnorm[1]);
+    if (!isfinite(bnorm) || !isfinite(rn)) {
+        set_error("nodal solve: right-hand side or initial residual is not finite");
+        if (stats) stats->status = GBP_NAN;
+        return GBP_NAN;
+    }
+    const double ref = opt.always_use_bnorm ? bnorm : rn;
+    const double target = std::max(opt.rtol * ref, opt.atol);
+    // power-of-two scale that keeps the FP32 inner right-hand side near unit size
+    if (bnorm > 0.0) {
+        int ex = 0;
+        frexp(bnorm * l0.g.vol, &ex);
+        scale32 = ldexp(1.0, -ex);
+    }
+    int it = 0;
+    int status = GBP_OK;
+    const double r0 = rn;
+    while (rn > target) {
+        if (it >= opt.maxiter) {
+            status = GBP_NOT_CONVERGED;
+            break;
+        }
+        int rc = run_iteration();
+        if (rc) return rc;
+        GBP_CUDA(cudaStreamSynchronize(st));
+        rn = bits_to_double(hnorm[1]);
+        ++it;
+        if (opt.verbose > 1) fprintf(stderr, "gbp nodal: iter %d rel resid %.3e\n", it, bnorm > 0 ? rn / bnorm : rn);
+        if (!isfinite(rn)) {
+            status = GBP_NAN;
+            set_error("nodal solve: residual became NaN/Inf");
+            break;
+        }
+    }
+    if (singular) {
+        nodal_remove_mean(l0.g, phi, partials, 1, st);
+        nk += 2;
+    }
+    GBP_CUDA(cudaEventRecord(ev2, st));
+    GBP_CUDA(cudaGetLastError());
+    if (stats) {
+        stats->status = status;
+        stats->outer_iters = it + 1;
+        stats->vcycles = it * (opt.precision == GBP_PREC_MIXED ? opt.ir_inner_cycles : 1);
+        stats->num_levels = (int)L.size();
+        stats->rhs_norm = bnorm;
+        stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;
+        stats->final_rel_resid = bnorm > 0 ? rn / bnorm : rn;
+        GBP_CUDA(cudaEventSynchronize(ev2));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev1, ev2);
+        stats->ms_solve = ms;
+    }
+    if (opt.verbose)
+        fprintf(stderr, "gbp nodal: %s after %d steps, rel resid %.3e\n", status == GBP_OK ? "converged" : "stopped",
+                it, bnorm > 0 ? rn / bnorm : rn);
+    return status;
+}
+
+int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
+                         const gbp_array4* phi_guess, gbp_stats* stats)
+{
+    if (!sigma_ready) {
+        set_error("nodal project: sigma was never set on this plan");
+        return GBP_BAD_ARG;
+    }
+    const NodalLevel& l0 = L[0];
+    GBP_CUDA(cudaEventRecord(ev0, st));
+    nodal_rhs(l0.g, rhs, l0.s64, rhs0, nullptr, st);
+    ++nk;
+    if (singular) {
+        nodal_remove_mean(l0.g, rhs0, partials, 0, st);
+        nk += 2;
+    }
+    if (phi_guess) {
+        nodal_load_phi(l0.g, *phi_guess, phi, st);
+        ++nk;
+    }
+    GBP_CUDA(cudaGetLastError());
+    int status = solve(phi_guess != nullptr, stats);
+    if (status != GBP_OK && status != GBP_NOT_CONVERGED) return status;
+    nodal_correct(l0.g, corr, l0.s64, phi, st);
+    ++nk;
+    if (phi_out && phi_out->data) {
+        nodal_store_phi(l0.g, *phi_out, phi, phi_accumulate, st);
+        ++nk;
+    }
+    GBP_CUDA(cudaEventRecord(ev2, st));
+    GBP_CUDA(cudaGetLastError());
+    if (stats) {
+        GBP_CUDA(cudaEventSynchronize(ev2));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev2);
+        stats->ms_total = ms;
+        stats->kernel_launches = nk;
+    }
+    return status;
+}
+
+}  // namespace gbp
+
+namespace gbp {
+
+int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
+{
+    if (which < 0 || which > 3 || reps < 1 || !sigma_ready) {
+        set_error("time_kernel: which must be 0..3, reps >= 1, and sigma must be set");
+        return GBP_BAD_ARG;
+    }
+    const NodalLevel& l0 = L[0];
+    const NodalGeom& g = l0.g;
+    const bool f32 = which & 1;
+    const double w = f32 ? 4.0 : 8.0;
+    const double nn = (double)g.nu[0] * g.nu[1] * g.nu[2];
+    const double nc = (double)g.n[0] * g.n[1] * g.n[2];
+    // Jacobi: x, b read + x written per node, sigma read per cell; residual: x, b read, r written
+    *bytes = w * (3.0 * nn + nc);
+    if (f32) nodal_to_f32(g, res, l0.b32, scale32, st);
+    GBP_CUDA(cudaEventRecord(ev0, st));
+    for (int r = 0; r < reps; ++r) {
+        switch (which) {
+        case 0:
+            nodal_jacobi<double>(g, l0.s64, (r & 1) ? l0.t64 : l0.x64, res, (r & 1) ? l0.x64 : l0.t64, opt.omega,
+                                 false, st);
+            break;
+        case 1:
+            nodal_jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, opt.omega,
+                                false, st);
+            break;
+        case 2: nodal_resid<double>(g, l0.s64, phi, rhs0, l0.r64, nullptr, st); break;
+        default: nodal_resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st); break;
+        }
+    }
+    GBP_CUDA(cudaEventRecord(ev1, st));
+    GBP_CUDA(cudaEventSynchronize(ev1));
+    float t = 0.f;
+    GBP_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
+    *ms = t / reps;
+    return GBP_OK;
+}
+
+}  // namespace gbp

@@ -1,0 +1,100 @@
+// Nodal multigrid solver: the replacement of Hydro::NodalProjector + MLNodeLaplacian + MLMG for
+// one single-box level (incflo::ApplyNodalProjection, src/projection/incflo_apply_nodal_projection.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "gbp_internal.cuh"
+#include "nodal_kernels.h"
+
+namespace gbp {
+
+struct DevicePool {
+    char* base = nullptr;
+    size_t bytes = 0;
+    size_t used = 0;
+    int reserve(size_t nbytes);
+    template <typename T>
+    T* take(size_t count)
+    {
+        size_t off = (used + 255) & ~size_t(255);
+        used = off + count * sizeof(T);
+        return reinterpret_cast<T*>(base + off);
+    }
+    void release();
+};
+
+struct NodalLevel {
+    NodalGeom g;
+    double *s64 = nullptr, *x64 = nullptr, *t64 = nullptr, *b64 = nullptr, *r64 = nullptr;
+    float *s32 = nullptr, *x32 = nullptr, *t32 = nullptr, *b32 = nullptr, *r32 = nullptr;
+};
+
+class NodalSolver {
+public:
+    int init(const gbp_geometry& geom, const int bc_lo[3], const int bc_hi[3], const gbp_options& opt,
+             cudaStream_t stream);
+    void destroy();
+    ~NodalSolver() { destroy(); }
+
+    int set_options(const gbp_options& opt);
+    int set_sigma_from_density(const gbp_array4* rho, double scale, double rho0);
+    int set_sigma(const gbp_array4* sigma, double cval);
+
+    // full projection: rhs from vel (+ fused add-back / U^n subtraction), solve, correct
+    int project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
+                const gbp_array4* phi_guess, gbp_stats* stats);
+
+    const NodalGeom& geom0() const { return L[0].g; }
+    size_t device_bytes() const { return pool.bytes; }
+    cudaStream_t stream() const { return st; }
+    // solve A phi = g on the level-0 arrays already in place (used by project and tests)
+    int solve(bool have_guess, gbp_stats* stats);
+
+    void reset_count() { nk = 0; }
+    long long kernel_count() const { return nk; }
+    // time `reps` launches of one level-0 kernel (0/1: FP64/FP32 Jacobi, 2/3: FP64/FP32 residual)
+    int time_kernel(int which, int reps, double* ms, double* bytes);
+
+    double* phi64() const { return phi; }
+    double* rhs64() const { return rhs0; }
+    double* sigma64() const { return L[0].s64; }
+
+private:
+    template <typename T>
+    void vcycle(int l, const T* b, bool zero);
+    template <typename T>
+    void bottom(int l, const T* b, T* x);
+    void record_iteration();
+    int run_iteration();
+
+    gbp_options opt{};
+    cudaStream_t st = nullptr;
+    cudaStream_t cap = nullptr;  // capture stream (graphs cannot be captured on the legacy stream)
+    cudaStream_t cap_or_st = nullptr;  // stream the kernels of a refinement step are issued on
+    std::vector<NodalLevel> L;
+    DevicePool pool;
+    double* phi = nullptr;       // level-0 solution (FP64)
+    double* rhs0 = nullptr;      // level-0 right-hand side (FP64, weak form)
+    double* res = nullptr;       // level-0 outer residual (FP64)
+    double* partials = nullptr;  // reduction scratch
+    double* bscr = nullptr;      // bottom CG scratch
+    int* dinfo = nullptr;        // bottom iteration count
+    unsigned long long* dnorm = nullptr;  // [0] rhs norm, [1] residual norm
+    unsigned long long* hnorm = nullptr;  // pinned mirror
+    bool singular = false;
+    bool sigma_ready = false;
+    double scale32 = 1.0;
+    // result buffer of each level's V-cycle (ping-pong aware)
+    void* xres[kMaxLevels] = {};
+    cudaGraphExec_t gexec = nullptr;
+    int gexec_prec = -1;
+    double gexec_scale = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    long long nk = 0;            // kernels issued (or replayed through graphs) since reset_count()
+    long long step_kernels = 0;  // kernels in one refinement step
+};
+
+}  // namespace gbp

@@ -1,0 +1,318 @@
+"""Host-side mirror of the reference's projection interface, over the C ABI.
+
+Classes and methods keep the names and argument meaning of the AMReX-Hydro projectors that incflo
+drives, so code written against them reads the same:
+
+  NodalProjector   Hydro::NodalProjector as used in incflo::ApplyNodalProjection
+                   (src/projection/incflo_apply_nodal_projection.cpp:181-219)
+  MacProjector     Hydro::MacProjector as used in incflo::compute_MAC_projected_velocities
+                   (src/convection/incflo_compute_MAC_projected_velocities.cpp:93-133, 272-299)
+  apply_nodal_projection   incflo::ApplyNodalProjection(density, time, scaling_factor,
+                   incremental) for one level (:29-93 plus :95-267), fused on the device.
+
+Fields are CUDA float64 torch tensors (torch is only the allocator here). Layout, last axis x:
+  cell fields   (ncomp, nz+2g, ny+2g, nx+2g) or (nz+2g, ny+2g, nx+2g); ``ng`` gives g
+  nodal fields  (nz+1, ny+1, nx+1)
+  face fields   x: (nz, ny, nx+1), y: (nz, ny+1, nx), z: (nz+1, ny, nx)
+Errors raise ProjectionError (status code + message); nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import torch
+
+from . import _abi as A
+from ._abi import BC_DIRICHLET, BC_INFLOW, BC_NEUMANN, BC_PERIODIC, BC_ROBIN  # noqa: F401
+
+LinOpBCType = {
+    "Periodic": BC_PERIODIC,
+    "Dirichlet": BC_DIRICHLET,
+    "Neumann": BC_NEUMANN,
+    "inflow": BC_INFLOW,
+    "Robin": BC_ROBIN,
+}
+
+
+@dataclass
+class Geometry:
+    """amrex::Geometry of one single-box level: cell counts and physical extent."""
+
+    n_cell: tuple
+    prob_lo: tuple = (0.0, 0.0, 0.0)
+    prob_hi: tuple = (1.0, 1.0, 1.0)
+
+    def c(self) -> A.Geometry:
+        g = A.Geometry()
+        for d in range(3):
+            g.n_cell[d] = int(self.n_cell[d])
+            g.prob_lo[d] = float(self.prob_lo[d])
+            g.prob_hi[d] = float(self.prob_hi[d])
+        return g
+
+    @property
+    def dx(self):
+        return tuple((self.prob_hi[d] - self.prob_lo[d]) / self.n_cell[d] for d in range(3))
+
+
+@dataclass
+class LPInfo:
+    """amrex::LPInfo: only the coarsening depth matters to this solver."""
+
+    max_coarsening_level: int = 100
+
+    def setMaxCoarseningLevel(self, n):  # noqa: N802 (reference name)
+        self.max_coarsening_level = int(n)
+        return self
+
+
+def array4(t: torch.Tensor, ng: int = 0, lo=None) -> A.Array4:
+    """Describe a CUDA float64 tensor as an amrex::Array4-like view for the C ABI."""
+    if not isinstance(t, torch.Tensor) or t.dtype != torch.float64 or not t.is_cuda:
+        raise TypeError("fields must be CUDA float64 tensors")
+    if t.dim() not in (3, 4):
+        raise ValueError("fields are 3-D (one component) or 4-D (components first)")
+    a = A.Array4()
+    a.data = t.data_ptr()
+    shape = t.shape[-3:]
+    lo = (-ng, -ng, -ng) if lo is None else lo
+    for d in range(3):
+        a.lo[d] = int(lo[d])
+        a.hi[d] = int(lo[d]) + int(shape[2 - d]) - 1
+    if t.stride(-1) != 1:
+        raise ValueError("the x axis (last) must be contiguous")
+    a.jstride = t.stride(-2)
+    a.kstride = t.stride(-3)
+    a.ncomp = int(t.shape[0]) if t.dim() == 4 else 1
+    a.nstride = t.stride(0) if t.dim() == 4 else 0
+    return a
+
+
+def _ref(a):
+    return ctypes.byref(a) if a is not None else None
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+class _Plan:
+    def __init__(self, geom: Geometry, kind: int, bc_lo, bc_hi, options: A.Options, stream=None):
+        A.load()
+        self.geom = geom
+        self.kind = kind
+        self.options = options
+        self.ptr = ctypes.c_void_p()
+        lo = (ctypes.c_int * 3)(*[int(v) for v in bc_lo])
+        hi = (ctypes.c_int * 3)(*[int(v) for v in bc_hi])
+        A.check(A.load().gbp_plan_create(ctypes.byref(geom.c()), kind, lo, hi, ctypes.byref(options),
+                                         _stream_ptr(stream), ctypes.byref(self.ptr)), "gbp_plan_create")
+        self.bc_lo, self.bc_hi = tuple(bc_lo), tuple(bc_hi)
+
+    def set_options(self, options: A.Options):
+        self.options = options
+        A.check(A.load().gbp_plan_set_options(self.ptr, ctypes.byref(options)), "gbp_plan_set_options")
+
+    def device_bytes(self) -> int:
+        return int(A.load().gbp_plan_device_bytes(self.ptr))
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                A.load().gbp_plan_destroy(self.ptr)
+                self.ptr = ctypes.c_void_p()
+        except Exception:
+            pass
+
+
+def make_options(kind: int, **kw) -> A.Options:
+    """Options from keyword overrides; keys are the inputs-file keys (mg_rtol, maxiter, precision ...)."""
+    o = A.default_options(kind)
+    for k, v in kw.items():
+        A.check(A.load().gbp_options_set(ctypes.byref(o), k.encode(), str(v).encode()), f"option {k}")
+    return o
+
+
+def options_from_inputs(kind: int, text: str, prefix=None) -> A.Options:
+    """Parse ParmParse-style inputs text for the nodal_proj.* (or mac_proj.*) keys."""
+    o = A.default_options(kind)
+    prefix = prefix or ("nodal_proj" if kind == A.GBP_NODAL else "mac_proj")
+    A.check(A.load().gbp_options_parse(ctypes.byref(o), prefix.encode(), text.encode()), "gbp_options_parse")
+    return o
+
+
+# ---------------------------------------------------------------------------------- nodal
+class NodalProjector:
+    """Hydro::NodalProjector(vel, sigma, geom, info) for one level.
+
+    ``sigma`` is a cell tensor (nz, ny, nx) or a float (constant-density form). The plan (the
+    multigrid hierarchy) is cached per geometry/boundary set and reused across projectors.
+    """
+
+    _plans: dict = {}
+
+    def __init__(self, vel, sigma, geom: Geometry, info: LPInfo | None = None, ng: int = 1,
+                 options: A.Options | None = None, stream=None):
+        self.vel = vel
+        self.sigma = sigma
+        self.geom = geom
+        self.info = info or LPInfo()
+        self.ng = ng
+        self.options = options or A.default_options(A.GBP_NODAL)
+        self.options.max_coarsening_level = self.info.max_coarsening_level
+        self.stream = stream
+        self.bc_lo = self.bc_hi = None
+        self.phi = None
+        self.gradphi = None
+        self.stats = None
+
+    def setDomainBC(self, lo, hi):  # noqa: N802 (reference name)
+        self.bc_lo = tuple(LinOpBCType.get(b, b) for b in lo)
+        self.bc_hi = tuple(LinOpBCType.get(b, b) for b in hi)
+
+    def _plan(self) -> _Plan:
+        if self.bc_lo is None:
+            raise RuntimeError("setDomainBC must be called before project")
+        key = (tuple(self.geom.n_cell), tuple(self.geom.prob_lo), tuple(self.geom.prob_hi), self.bc_lo,
+               self.bc_hi, self.options.max_coarsening_level, torch.cuda.current_device())
+        plan = NodalProjector._plans.get(key)
+        if plan is None:
+            plan = _Plan(self.geom, A.GBP_NODAL, self.bc_lo, self.bc_hi, self.options, self.stream)
+            NodalProjector._plans[key] = plan
+        else:
+            plan.set_options(self.options)
+        return plan
+
+    def project(self, rtol=None, atol=None, phi_guess: torch.Tensor | None = None):
+        if rtol is not None:
+            self.options.rtol = float(rtol)
+        if atol is not None:
+            self.options.atol = float(atol)
+        plan = self._plan()
+        L = A.load()
+        if isinstance(self.sigma, torch.Tensor):
+            A.check(L.gbp_nodal_set_sigma(plan.ptr, _ref(array4(self.sigma)), 0.0), "gbp_nodal_set_sigma")
+        else:
+            A.check(L.gbp_nodal_set_sigma(plan.ptr, None, float(self.sigma)), "gbp_nodal_set_sigma")
+        n = self.geom.n_cell
+        dev = self.vel.device
+        if phi_guess is not None:
+            self.phi = phi_guess
+        elif self.phi is None:
+            self.phi = torch.zeros((n[2] + 1, n[1] + 1, n[0] + 1), dtype=torch.float64, device=dev)
+        if self.gradphi is None:
+            self.gradphi = torch.zeros((3, n[2], n[1], n[0]), dtype=torch.float64, device=dev)
+        st = A.Stats()
+        A.check(L.gbp_nodal_project(plan.ptr, _ref(array4(self.vel, self.ng)), _ref(array4(self.phi)),
+                                    _ref(array4(self.gradphi)), int(phi_guess is not None), ctypes.byref(st)),
+                "gbp_nodal_project")
+        self.stats = st.as_dict()
+        return self.stats
+
+    def getPhi(self):  # noqa: N802
+        return self.phi
+
+    def getGradPhi(self):  # noqa: N802
+        return self.gradphi
+
+
+def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd, *, time=0.0, dt=1.0,
+                           prev_dt=1.0, scaling_factor=1.0, incremental=False, set_inflow_bc=True,
+                           vel_old=None, rho0=1.0, ng=1, options: A.Options | None = None, stream=None,
+                           constant_density=False):
+    """incflo::ApplyNodalProjection for one level, fused on the device; returns the stats dict."""
+    options = options or A.default_options(A.GBP_NODAL)
+    key = (tuple(geom.n_cell), tuple(geom.prob_lo), tuple(geom.prob_hi), tuple(bc_lo), tuple(bc_hi),
+           options.max_coarsening_level, torch.cuda.current_device())
+    plan = NodalProjector._plans.get(key)
+    if plan is None:
+        plan = _Plan(geom, A.GBP_NODAL, bc_lo, bc_hi, options, stream)
+        NodalProjector._plans[key] = plan
+    else:
+        plan.set_options(options)
+    st = A.Stats()
+    rho_a = None if constant_density else array4(density, 0)
+    A.check(A.load().gbp_apply_nodal_projection(
+        plan.ptr, _ref(array4(vel, ng)), _ref(array4(vel_old, 0)) if vel_old is not None else None, _ref(rho_a),
+        float(rho0), _ref(array4(gp)), _ref(array4(p_nd)) if p_nd is not None else None, float(time), float(dt),
+        float(prev_dt), float(scaling_factor), int(incremental), int(set_inflow_bc), ctypes.byref(st)),
+        "gbp_apply_nodal_projection")
+    return st.as_dict()
+
+
+# ------------------------------------------------------------------------------------ MAC
+class MacProjector:
+    """Hydro::MacProjector(geom) for one level: initProjector / updateCoeffs / setUMAC / project."""
+
+    def __init__(self, geom: Geometry, options: A.Options | None = None, stream=None):
+        self.geom = geom
+        self.options = options or A.default_options(A.GBP_MAC)
+        self.stream = stream
+        self.plan = None
+        self.bc_lo = self.bc_hi = None
+        self.beta = None
+        self.umac = None
+        self.stats = None
+
+    def needInitialization(self):  # noqa: N802
+        return self.plan is None
+
+    def initProjector(self, info: LPInfo | None = None, beta=None):  # noqa: N802
+        """beta: [bx, by, bz] face tensors, or a float (the constant-density form dt/rho0)."""
+        if info is not None:
+            self.options.max_coarsening_level = info.max_coarsening_level
+        self.beta = beta
+        self.plan = None
+
+    def setDomainBC(self, lo, hi):  # noqa: N802
+        self.bc_lo = tuple(LinOpBCType.get(b, b) for b in lo)
+        self.bc_hi = tuple(LinOpBCType.get(b, b) for b in hi)
+        self.plan = None
+
+    def updateCoeffs(self, beta):  # noqa: N802
+        self.beta = beta
+        self._push_beta()
+
+    def updateBeta(self, beta):  # noqa: N802
+        self.beta = float(beta)
+        self._push_beta()
+
+    def setUMAC(self, umac):  # noqa: N802
+        self.umac = list(umac)
+
+    def _ensure(self):
+        if self.plan is None:
+            if self.bc_lo is None:
+                raise RuntimeError("setDomainBC must be called before project")
+            self.plan = _Plan(self.geom, A.GBP_MAC, self.bc_lo, self.bc_hi, self.options, self.stream)
+            self._push_beta()
+        else:
+            self.plan.set_options(self.options)
+
+    def _push_beta(self):
+        if self.plan is None:
+            return
+        L = A.load()
+        if isinstance(self.beta, (list, tuple)):
+            b = [array4(x) for x in self.beta]
+            A.check(L.gbp_mac_set_beta(self.plan.ptr, _ref(b[0]), _ref(b[1]), _ref(b[2]), 0.0), "gbp_mac_set_beta")
+        else:
+            A.check(L.gbp_mac_set_beta(self.plan.ptr, None, None, None, float(self.beta)), "gbp_mac_set_beta")
+
+    def project(self, rtol=None, atol=None, phi: torch.Tensor | None = None, phi_guess=True, ng_phi=0):
+        """project(rtol, atol) or project(phi, rtol, atol): phi (cells) is the initial guess and output."""
+        if rtol is not None:
+            self.options.rtol = float(rtol)
+        if atol is not None:
+            self.options.atol = float(atol)
+        self._ensure()
+        u = [array4(x) for x in self.umac]
+        st = A.Stats()
+        pa = array4(phi, ng_phi) if phi is not None else None
+        A.check(A.load().gbp_mac_project(self.plan.ptr, _ref(u[0]), _ref(u[1]), _ref(u[2]), _ref(pa),
+                                         int(phi is not None and phi_guess), ctypes.byref(st)), "gbp_mac_project")
+        self.stats = st.as_dict()
+        return self.stats

@@ -1,0 +1,106 @@
+"""Seeded synthetic inputs of the projection workloads (numpy PCG64; no datasets are read).
+
+incflo itself cannot run here, so these generators stand in for the states incflo would hand to
+its projections. Every array uses the C-order layout of incflo_gb300.projection (last axis x).
+
+  taylor_green_noise     [0,2pi]^3 triply periodic, u = sin x cos y cos z, v = -cos x sin y cos z,
+                         w = 0, plus U(-a, a) noise per component (seed 1, a = 1e-2)
+  variable_density_rt    unit cube, periodic x/y, walls in z: rho = 1 below / 3 above a tanh
+                         interface of width 2 cells at z = 0.5 + h(x, y), h a seeded sum of
+                         cosine modes 1..8 with max amplitude 0.01 (seed 2); velocity a Gaussian
+                         random field with E(k) ~ k^-2, zero mean, unit RMS (seed 3)
+  double_shear_layer     u = tanh(30 (y - 1/4)) for y <= 1/2, tanh(30 (3/4 - y)) above,
+                         v = 0.05 sin(2 pi x), w = 0 (the reference's form,
+                         src/prob/prob_init_fluid.cpp:879-898)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+PERIODIC, DIRICHLET, NEUMANN, INFLOW = 0, 1, 2, 3
+
+
+def _cell_centres(n, lo, hi):
+    h = [(hi[d] - lo[d]) / n[d] for d in range(3)]
+    xs = [lo[d] + (np.arange(n[d]) + 0.5) * h[d] for d in range(3)]
+    Z, Y, X = np.meshgrid(xs[2], xs[1], xs[0], indexing="ij")
+    return X, Y, Z
+
+
+def taylor_green_noise(n=64, seed=1, amp=1e-2):
+    lo, hi = (0.0,) * 3, (2 * np.pi,) * 3
+    X, Y, Z = _cell_centres((n, n, n), lo, hi)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    vel = np.empty((3, n, n, n))
+    vel[0] = np.sin(X) * np.cos(Y) * np.cos(Z)
+    vel[1] = -np.cos(X) * np.sin(Y) * np.cos(Z)
+    vel[2] = 0.0
+    vel += rng.uniform(-amp, amp, size=vel.shape)
+    rho = np.ones((n, n, n))
+    return dict(n=(n, n, n), lo=lo, hi=hi, bclo=(PERIODIC,) * 3, bchi=(PERIODIC,) * 3, vel=vel, rho=rho)
+
+
+def gaussian_random_field(n, seed, slope=-2.0, ncomp=3):
+    """Periodic Gaussian random vector field with energy spectrum E(k) ~ k^slope, zero mean, unit RMS."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    k = [np.fft.fftfreq(n[d]) * n[d] for d in range(3)]
+    kz, ky, kx = np.meshgrid(k[2], k[1], np.fft.rfftfreq(n[0]) * n[0], indexing="ij")
+    kk = np.sqrt(kx * kx + ky * ky + kz * kz)
+    # |u_hat|^2 ~ E(k) / k^2 in three dimensions
+    amp = np.zeros_like(kk)
+    nz = kk > 0
+    amp[nz] = kk[nz] ** ((slope - 2.0) / 2.0)
+    out = np.empty((ncomp, n[2], n[1], n[0]))
+    for c in range(ncomp):
+        white = rng.standard_normal((n[2], n[1], n[0]))
+        f = np.fft.rfftn(white) * amp
+        out[c] = np.fft.irfftn(f, s=(n[2], n[1], n[0]))
+    out -= out.mean(axis=(1, 2, 3), keepdims=True)
+    out /= np.sqrt(np.mean(np.sum(out * out, axis=0)))
+    return out
+
+
+def interface_height(n, seed=2, modes=8, amplitude=0.01):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x = (np.arange(n[0]) + 0.5) / n[0]
+    y = (np.arange(n[1]) + 0.5) / n[1]
+    Y, X = np.meshgrid(y, x, indexing="ij")
+    a = rng.uniform(-1.0, 1.0, size=(2, modes))
+    th = rng.uniform(0.0, 2 * np.pi, size=(2, modes))
+    h = np.zeros_like(X)
+    for m in range(1, modes + 1):
+        h += a[0, m - 1] * np.cos(2 * np.pi * m * X + th[0, m - 1])
+        h += a[1, m - 1] * np.cos(2 * np.pi * m * Y + th[1, m - 1])
+    h *= amplitude / np.abs(h).max()
+    return 0.5 + h
+
+
+def variable_density_rt(n=256, seed_h=2, seed_u=3, rho_lo=1.0, rho_hi=3.0):
+    nn = (n, n, n) if np.isscalar(n) else tuple(n)
+    lo, hi = (0.0,) * 3, (1.0,) * 3
+    dz = 1.0 / nn[2]
+    z = (np.arange(nn[2]) + 0.5) * dz
+    hxy = interface_height(nn, seed_h)
+    rho = rho_lo + (rho_hi - rho_lo) * 0.5 * (1.0 + np.tanh((z[:, None, None] - hxy[None, :, :]) / (2.0 * dz)))
+    vel = gaussian_random_field(nn, seed_u)
+    return dict(n=nn, lo=lo, hi=hi, bclo=(PERIODIC, PERIODIC, NEUMANN), bchi=(PERIODIC, PERIODIC, NEUMANN),
+                vel=vel, rho=rho)
+
+
+def double_shear_layer(n=128, seed=None, amp_noise=0.0):
+    nn = (n, n, n) if np.isscalar(n) else tuple(n)
+    lo, hi = (0.0,) * 3, (1.0,) * 3
+    X, Y, Z = _cell_centres(nn, lo, hi)
+    vel = np.zeros((3,) + X.shape)
+    vel[0] = np.where(Y <= 0.5, np.tanh(30.0 * (Y - 0.25)), np.tanh(30.0 * (0.75 - Y)))
+    vel[1] = 0.05 * np.sin(2 * np.pi * X)
+    if seed is not None and amp_noise > 0:
+        rng = np.random.Generator(np.random.PCG64(seed))
+        vel += rng.uniform(-amp_noise, amp_noise, size=vel.shape)
+    rho = np.ones(X.shape)
+    return dict(n=nn, lo=lo, hi=hi, bclo=(PERIODIC,) * 3, bchi=(PERIODIC,) * 3, vel=vel, rho=rho)
+
+
+def with_ghosts(vel, ng=1):
+    """Pad a (3, nz, ny, nx) cell field with ng zero ghost layers (the state after setBndry(0))."""
+    return np.pad(vel, ((0, 0),) + ((ng, ng),) * 3)

@@ -1,0 +1,207 @@
+/*
+ * incflo_gb300 -- GB300-native projection hot path of incflo behind a C ABI.
+ *
+ * The reference drives two C++ classes from AMReX-Hydro, not a C ABI:
+ *   Hydro::NodalProjector, created per call in
+ *     incflo::ApplyNodalProjection  (src/projection/incflo_apply_nodal_projection.cpp:29-267,
+ *     constructor :187-192, setDomainBC :194, project :215, getPhi :218, getGradPhi :219)
+ *   Hydro::MacProjector, held as incflo::macproj (src/incflo.H:420) and driven by
+ *     incflo::compute_MAC_projected_velocities
+ *     (src/convection/incflo_compute_MAC_projected_velocities.cpp:93-133 init/update,
+ *      :272 setUMAC, :287-299 project).
+ * Every entry point below replaces one of those calls; the one it replaces is cited beside it.
+ * The header-only C++ shim include/gb_projectors.H re-exposes the Hydro method names.
+ *
+ * Conventions
+ *  - All field pointers are DEVICE pointers unless an entry point says otherwise. They are
+ *    described by gbp_array4, a plain mirror of amrex::Array4: element (i,j,k,n) lives at
+ *    data[(i-lo[0]) + (j-lo[1])*jstride + (k-lo[2])*kstride + n*nstride], where lo/hi bound
+ *    the allocated region including ghost cells, in the global index space of the level.
+ *    AMReX MultiFab FABs therefore pass through with zero copies.
+ *  - Cell-centred data is valid on cells 0..n-1; nodal data on nodes 0..n; face data in
+ *    direction d on faces 0..n[d] (and cells in the other two directions).
+ *  - Every call returns a gbp_status (never aborts) and runs on the plan's CUDA stream.
+ *  - The library computes in FP64 (plain form) or FP32 V-cycles inside FP64 iterative
+ *    refinement (mixed form); it never falls back to the CPU.
+ */
+#ifndef INCFLO_GB300_H
+#define INCFLO_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBP_ABI_VERSION 1
+
+typedef enum {
+    GBP_OK = 0,
+    GBP_NOT_CONVERGED = 1, /* maxiter reached before max(rtol*|b|, atol) */
+    GBP_NAN = 2,           /* a residual norm became NaN or Inf */
+    GBP_BAD_ARG = 3,       /* invalid pointer, size, layout or option */
+    GBP_CUDA_ERROR = 4,    /* a CUDA runtime call failed; see gbp_last_error() */
+    GBP_TIMEOUT = 5,       /* a bounded device-side wait ran out */
+    GBP_NO_DEVICE = 6      /* no CUDA device, or not an sm_103 device */
+} gbp_status;
+
+typedef enum { GBP_NODAL = 0, GBP_MAC = 1 } gbp_kind;
+
+/* Mirrors amrex::LinOpBCType as produced by incflo::get_projection_bc and
+ * incflo::get_mac_projection_bc (src/projection/incflo_projection_bc.cpp:5-79). */
+typedef enum {
+    GBP_BC_PERIODIC = 0,
+    GBP_BC_DIRICHLET = 1, /* pressure_inflow / pressure_outflow: phi = 0 */
+    GBP_BC_NEUMANN = 2,   /* slip / no-slip wall */
+    GBP_BC_INFLOW = 3,    /* mass_inflow / direction_dependent (nodal): Neumann for phi, the
+                             normal inflow velocity from the ghost cells enters the RHS */
+    GBP_BC_ROBIN = 4      /* mixed (MAC only); not supported yet: GBP_BAD_ARG */
+} gbp_bc;
+
+typedef enum { GBP_PREC_FP64 = 0, GBP_PREC_MIXED = 1 } gbp_precision;
+
+typedef struct {
+    double* data;
+    int lo[3];
+    int hi[3];
+    int ncomp;
+    long long jstride;
+    long long kstride;
+    long long nstride;
+} gbp_array4;
+
+typedef struct {
+    int n_cell[3];       /* cells of the (single-box) level */
+    double prob_lo[3];
+    double prob_hi[3];
+} gbp_geometry;
+
+/* Solver options. gbp_options_default() gives incflo's defaults (src/incflo.H:425-455,
+ * src/setup/init.cpp:165-177) and the MLMG defaults incflo relies on; gbp_options_set()
+ * accepts the ParmParse keys of the nodal_proj.* / mac_proj.* prefixes. */
+typedef struct {
+    double rtol;                 /* mg_rtol  (1e-11) */
+    double atol;                 /* mg_atol  (1e-14) */
+    int max_coarsening_level;    /* mg_max_coarsening_level (100) */
+    int maxiter;                 /* maxiter (nodal 100, mac 200) */
+    int bottom_maxiter;          /* bottom_maxiter (200) */
+    double bottom_rtol;          /* bottom_rtol (1e-4) */
+    double bottom_atol;          /* bottom_atol (-1: unused) */
+    int verbose;                 /* verbose (0) */
+    int bottom_verbose;          /* bottom_verbose (0) */
+    int precision;               /* precision = fp64 | mixed  (new key; default fp64) */
+    int nu1;                     /* num_pre_smooth  (2) */
+    int nu2;                     /* num_post_smooth (2) */
+    double omega;                /* Jacobi weight of the nodal smoother (0.85) */
+    int ir_inner_cycles;         /* mixed form: FP32 V-cycles per FP64 refinement step (4) */
+    int use_graphs;              /* capture each V-cycle as a CUDA graph (1) */
+    int always_use_bnorm;        /* relative tolerance against |b| (1) or |r0| (0) */
+} gbp_options;
+
+typedef struct {
+    int status;
+    int vcycles;                 /* V-cycles over all refinement steps */
+    int outer_iters;             /* FP64 residual evaluations (refinement steps + 1) */
+    int num_levels;
+    double rhs_norm;             /* max_i |b_i| (strong form: the divergence) */
+    double initial_rel_resid;
+    double final_rel_resid;      /* max_i |b_i - (L phi)_i| / rhs_norm */
+    double ms_total;             /* device time of the whole call, CUDA events */
+    double ms_solve;             /* device time of the solve alone */
+    long long kernel_launches;   /* kernels this call ran on the device (graph nodes included) */
+} gbp_stats;
+
+typedef struct gbp_plan gbp_plan;
+
+/* ---- library ------------------------------------------------------------------------- */
+int         gbp_abi_version(void);
+const char* gbp_status_string(int status);
+const char* gbp_last_error(void);
+int         gbp_device_check(void);
+
+/* ---- options: the nodal_proj.* / mac_proj.* inputs surface ---------------------------- */
+int gbp_options_default(int kind, gbp_options* opt);
+/* key without prefix, e.g. "mg_rtol", "maxiter", "bottom_solver", "precision" */
+int gbp_options_set(gbp_options* opt, const char* key, const char* value);
+/* parse ParmParse-style text ("prefix.key = value" lines, '#' comments) for one prefix */
+int gbp_options_parse(gbp_options* opt, const char* prefix, const char* text);
+
+/* ---- plans ----------------------------------------------------------------------------
+ * A plan owns the multigrid hierarchy for one level geometry and boundary set. It replaces
+ * the per-call construction of Hydro::NodalProjector
+ * (incflo_apply_nodal_projection.cpp:124,187-194) and Hydro::MacProjector construction plus
+ * setDomainBC (src/incflo.cpp:286-292, incflo_compute_MAC_projected_velocities.cpp:93-114).
+ * stream: a cudaStream_t (NULL = legacy default stream). */
+int gbp_plan_create(const gbp_geometry* geom, int kind, const int bc_lo[3], const int bc_hi[3],
+                    const gbp_options* opt, void* stream, gbp_plan** plan);
+int gbp_plan_destroy(gbp_plan* plan);
+int gbp_plan_set_options(gbp_plan* plan, const gbp_options* opt);
+size_t gbp_plan_device_bytes(const gbp_plan* plan);
+
+/* ---- nodal projection -----------------------------------------------------------------
+ * sigma = scaling_factor / rho per cell, computed on the device
+ * (incflo_apply_nodal_projection.cpp:101-121); constant density: rho == NULL and
+ * sigma = scaling_factor / rho0 (:184-188). */
+int gbp_nodal_set_sigma_from_density(gbp_plan* plan, const gbp_array4* rho, double scaling_factor,
+                                     double rho0);
+/* sigma given directly (cell array) or as a constant (sigma == NULL). */
+int gbp_nodal_set_sigma(gbp_plan* plan, const gbp_array4* sigma, double const_sigma);
+
+/* Hydro::NodalProjector::project(rtol, atol) plus getPhi/getGradPhi
+ * (incflo_apply_nodal_projection.cpp:215-219): b = nodal div(vel), solve
+ * div(sigma grad phi) = b, vel -= sigma grad phi in place. vel: 3 components, >= 1 ghost
+ * cell; ghost cells are read only on GBP_BC_INFLOW faces (normal component). phi (nodal)
+ * and gradphi (cell, 3 comps) may be NULL. phi_guess != 0: phi holds the initial guess. */
+int gbp_nodal_project(gbp_plan* plan, gbp_array4* vel, gbp_array4* phi, gbp_array4* gradphi,
+                      int phi_guess, gbp_stats* stats);
+
+/* incflo::ApplyNodalProjection(density, time, scaling_factor, incremental) end to end
+ * (incflo_apply_nodal_projection.cpp:29-93 and :95-267 for one level): fuses the
+ * add-back of scaling_factor*gp/rho (:39-62), the U^n subtraction for incremental or
+ * small-dt projections (:65-71, :86-92), sigma = scaling_factor/rho, the solve, the
+ * velocity correction and the gp / p_nd update (:221-256) into a few kernels.
+ * vel_old may be NULL when neither incremental nor small-dt applies. rho == NULL means
+ * constant density rho0. */
+int gbp_apply_nodal_projection(gbp_plan* plan, gbp_array4* vel, const gbp_array4* vel_old,
+                               const gbp_array4* rho, double rho0, gbp_array4* gp,
+                               gbp_array4* p_nd, double time, double dt, double prev_dt,
+                               double scaling_factor, int incremental, int set_inflow_bc,
+                               gbp_stats* stats);
+
+/* ---- MAC projection -------------------------------------------------------------------
+ * beta on faces: MacProjector::initProjector(lp_info, beta) / updateCoeffs(beta)
+ * (incflo_compute_MAC_projected_velocities.cpp:96-133). beta == NULL: constant beta
+ * (initProjector(ba, dm, lp_info, dt/rho0) and updateBeta(dt/rho0)). */
+int gbp_mac_set_beta(gbp_plan* plan, const gbp_array4* beta_x, const gbp_array4* beta_y,
+                     const gbp_array4* beta_z, double const_beta);
+/* beta = dt / (arithmetic face average of rho), the incflo construction
+ * (average_cellcenter_to_face + invert(dt), :82-91); rho needs one ghost cell in every
+ * non-periodic direction it is averaged across (read only at interior faces). */
+int gbp_mac_set_beta_from_density(gbp_plan* plan, const gbp_array4* rho, double dt);
+
+/* MacProjector::setUMAC + project(rtol, atol) or project(phi, rtol, atol)
+ * (:272, :287-299): rhs = div(umac), solve div(beta grad phi) = rhs, umac -= beta grad phi
+ * in place. phi (cell) may be NULL; phi_guess != 0 uses phi as the initial guess. */
+int gbp_mac_project(gbp_plan* plan, gbp_array4* umac_x, gbp_array4* umac_y, gbp_array4* umac_z,
+                    gbp_array4* phi, int phi_guess, gbp_stats* stats);
+
+/* ---- host-buffer convenience (end-to-end path) ----------------------------------------
+ * Same as gbp_apply_nodal_projection with contiguous HOST arrays (no ghost cells):
+ * vel [3][nz][ny][nx], rho [nz][ny][nx], gp [3][nz][ny][nx], p_nd nodal [nz+1][ny+1][nx+1].
+ * The copies in and out run on the plan's stream inside the call. */
+int gbp_apply_nodal_projection_host(gbp_plan* plan, double* vel, const double* rho, double rho0,
+                                    double* gp, double* p_nd, double scaling_factor,
+                                    int incremental, gbp_stats* stats);
+
+/* ---- diagnostics ---------------------------------------------------------------------
+ * No counterpart in the reference (its MLMG has only TINY_PROFILE timers). Times `reps`
+ * back-to-back launches of one level-0 kernel of a nodal plan on the plan's stream with CUDA
+ * events, on the arrays of the last solve, and reports the kernel's algorithmic bytes per launch.
+ * which: 0 = FP64 Jacobi sweep, 1 = FP32 Jacobi sweep, 2 = FP64 residual, 3 = FP32 residual. */
+int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_launch,
+                         double* bytes_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,147 @@
+"""Nodal projection on the GPU (through the C ABI) against the CPU oracle.
+
+Parity bar: phi relative L2 <= 1e-9 (gauge: zero volume-weighted mean on singular systems),
+projected velocity and grad(phi) within 1e-9 of the oracle's scale, final relative residual
+<= the requested tolerance. Both the plain FP64 form and the mixed form (FP32 V-cycles inside
+FP64 iterative refinement) must meet it: the FP64 outer residual is the judge.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from incflo_gb300 import Geometry, NodalProjector, apply_nodal_projection, make_options
+from tests.helpers import D, I, N, P, cuda, nodal_case, rel_l2, unique_nodes
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ((16, 16, 16), (1.0, 1.0, 1.0), (P, P, P), (P, P, P)),
+    ((16, 12, 20), (1.0, 0.75, 1.25), (P, P, N), (P, P, N)),
+    ((12, 16, 8), (1.5, 2.0, 1.0), (N, D, P), (I, N, P)),
+    ((16, 8, 8), (1.0, 1.0, 0.5), (D, N, N), (D, I, D)),   # anisotropic spacing
+    ((10, 12, 14), (1.0, 1.2, 1.4), (N, N, N), (N, N, N)),  # odd coarse sizes
+    ((2, 2, 2), (1.0, 1.0, 1.0), (P, N, N), (P, N, N)),     # bottom-only hierarchy
+    ((32, 32, 32), (1.0, 1.0, 1.0), (P, P, N), (P, P, N)),
+]
+
+
+def _run(case, precision, graphs=True, seed=0):
+    n, ext, bclo, bchi = case
+    g, sigma, vel = nodal_case(n, ext, bclo, bchi, seed=seed)
+    vel_or, phi_or, grad_or, st_or = O.nodal_project(g, sigma, vel, rtol=1e-13)
+    assert st_or["status"] == 0
+    vt = cuda(vel)
+    opts = make_options(0, precision=precision, use_graphs=int(graphs))
+    proj = NodalProjector(vt, cuda(sigma), Geometry(n, (0, 0, 0), ext), options=opts)
+    proj.setDomainBC(bclo, bchi)
+    st = proj.project(rtol=1e-12, atol=0.0)
+    phi = unique_nodes(g, proj.getPhi().cpu().numpy())
+    return g, st, st_or, phi, phi_or, vt.cpu().numpy(), vel_or, proj.getGradPhi().cpu().numpy(), grad_or
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}-{c[2]}-{c[3]}" for c in CASES])
+def test_nodal_project_matches_oracle(gpu_lib, case, precision):
+    g, st, st_or, phi, phi_or, vel, vel_or, grad, grad_or = _run(case, precision)
+    assert st["status"] == 0, st
+    assert st["final_rel_resid"] <= 1e-12
+    assert rel_l2(phi, phi_or) <= 1e-9, (rel_l2(phi, phi_or), st)
+    scale = np.abs(vel_or[:, 1:-1, 1:-1, 1:-1]).max()
+    assert np.abs(vel[:, 1:-1, 1:-1, 1:-1] - vel_or[:, 1:-1, 1:-1, 1:-1]).max() <= 1e-9 * scale
+    assert np.abs(grad - grad_or).max() <= 1e-9 * max(np.abs(grad_or).max(), 1e-30)
+    # ghost cells are never written
+    np.testing.assert_array_equal(vel[:, 0], vel_or[:, 0])
+
+
+def test_nodal_graphs_and_direct_launch_agree(gpu_lib):
+    case = CASES[1]
+    a = _run(case, "fp64", graphs=True)
+    b = _run(case, "fp64", graphs=False)
+    np.testing.assert_array_equal(a[3], b[3])
+    assert a[1]["outer_iters"] == b[1]["outer_iters"]
+
+
+def test_nodal_plan_reuse_is_deterministic(gpu_lib):
+    case = CASES[2]
+    a = _run(case, "mixed")
+    b = _run(case, "mixed")
+    np.testing.assert_array_equal(a[3], b[3])
+
+
+def test_apply_nodal_projection_fused_semantics(gpu_lib):
+    """incflo::ApplyNodalProjection (non-incremental and incremental) against the oracle composition."""
+    n, ext, bclo, bchi = (16, 16, 16), (1.0, 1.0, 1.0), (P, P, N), (P, P, N)
+    g = O.Grid(n, hi=ext, bclo=bclo, bchi=bchi)
+    rng = np.random.default_rng(4)
+    rho = rng.uniform(1.0, 3.0, g.cell_shape)
+    s = 0.01
+    vel = np.zeros((3, n[2] + 2, n[1] + 2, n[0] + 2))
+    vel[:, 1:-1, 1:-1, 1:-1] = rng.standard_normal((3,) + g.cell_shape)
+    vel_o = rng.standard_normal((3,) + g.cell_shape)
+    gp = rng.standard_normal((3,) + g.cell_shape)
+    p_nd = rng.standard_normal((n[2] + 1, n[1] + 1, n[0] + 1))
+    sigma = s / rho
+    for incremental in (False, True):
+        # oracle composition of incflo_apply_nodal_projection.cpp:29-93, 221-256
+        v = vel.copy()
+        if not incremental:
+            v[:, 1:-1, 1:-1, 1:-1] += gp * sigma
+        else:
+            v[:, 1:-1, 1:-1, 1:-1] -= vel_o
+        vn, phi_or, grad_or, st = O.nodal_project(g, sigma, v, rtol=1e-13)
+        if incremental:
+            vn[:, 1:-1, 1:-1, 1:-1] += vel_o
+        gp_ref = gp + grad_or if incremental else grad_or
+        vt, gpt, pt = cuda(vel), cuda(gp), cuda(p_nd)
+        st = apply_nodal_projection(Geometry(n, (0, 0, 0), ext), bclo, bchi, vt, cuda(rho), gpt, pt,
+                                    time=1.0, dt=s, prev_dt=s, scaling_factor=s, incremental=incremental,
+                                    vel_old=cuda(vel_o), options=make_options(0, mg_rtol=1e-12, mg_atol=0))
+        assert st["status"] == 0
+        p_gpu = pt.cpu().numpy()
+        phi_gpu = unique_nodes(g, p_gpu - p_nd) if incremental else unique_nodes(g, p_gpu)
+        assert rel_l2(phi_gpu, phi_or) <= 1e-9
+        np.testing.assert_allclose(vt.cpu().numpy()[:, 1:-1, 1:-1, 1:-1], vn[:, 1:-1, 1:-1, 1:-1], rtol=0,
+                                   atol=1e-9 * np.abs(vn).max())
+        np.testing.assert_allclose(gpt.cpu().numpy(), gp_ref, rtol=0, atol=1e-9 * np.abs(gp_ref).max())
+        # periodic duplicate nodes of p_nd carry the same value
+        np.testing.assert_array_equal(p_gpu[:, :, -1], p_gpu[:, :, 0])
+
+
+def test_divergence_after_projection_no_worse_than_oracle(gpu_lib):
+    case = ((24, 24, 24), (1.0, 1.0, 1.0), (P, P, N), (P, P, N))
+    g, st, st_or, phi, phi_or, vel, vel_or, grad, grad_or = _run(case, "mixed", seed=3)
+    div_gpu = np.abs(O.nodal_rhs(g, vel)).max()
+    div_or = np.abs(O.nodal_rhs(g, vel_or)).max()
+    assert div_gpu <= div_or * (1 + 1e-6) + 1e-12
+
+
+def test_not_converged_status_and_bad_args(gpu_lib):
+    from incflo_gb300 import ProjectionError
+
+    n = (16, 16, 16)
+    g, sigma, vel = nodal_case(n, (1, 1, 1), (P, P, P), (P, P, P), seed=1)
+    proj = NodalProjector(cuda(vel), cuda(sigma), Geometry(n), options=make_options(0, maxiter=1))
+    proj.setDomainBC((P, P, P), (P, P, P))
+    with pytest.raises(ProjectionError) as e:
+        proj.project(rtol=1e-14, atol=0)
+    assert e.value.status == 1
+    bad = NodalProjector(cuda(vel[:, 1:-1]), cuda(sigma), Geometry(n))
+    bad.setDomainBC((P, P, P), (P, P, P))
+    with pytest.raises(ProjectionError) as e:
+        bad.project()
+    assert e.value.status == 3
+
+
+def test_nan_rhs_reported(gpu_lib):
+    from incflo_gb300 import ProjectionError
+
+    n = (8, 8, 8)
+    g, sigma, vel = nodal_case(n, (1, 1, 1), (P, P, N), (P, P, N), seed=2)
+    vel[0, 3, 3, 3] = np.nan
+    proj = NodalProjector(cuda(vel), cuda(sigma), Geometry(n))
+    proj.setDomainBC((P, P, N), (P, P, N))
+    with pytest.raises(ProjectionError) as e:
+        proj.project()
+    assert e.value.status == 2
+    torch.cuda.synchronize()
