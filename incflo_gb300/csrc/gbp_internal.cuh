@@ -149,11 +149,9 @@ __device__ __forceinline__ double block_max(double v)
 {
     __shared__ double red[32];
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
-    int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
-    lane = lin & 31;
-    wid = lin >> 5;
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    const int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = lin & 31, wid = lin >> 5;
     __syncthreads();
     if (lane == 0) red[wid] = v;
     __syncthreads();
@@ -161,7 +159,37 @@ __device__ __forceinline__ double block_max(double v)
         v = lane < nw ? red[lane] : 0.0;
         for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     }
-    return v;  // valid in warp 0
+    return v;  // valid in thread 0
+}
+
+// Deterministic block sum (fixed shuffle tree), the result valid in every thread.
+__device__ __forceinline__ double block_sum_all(double v)
+{
+    __shared__ double red[33];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    const int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = lin & 31, wid = lin >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double t = lane < nw ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// inverse control volume of a node (1/V_i): 1/h^3 doubled per non-periodic boundary face
+__device__ __forceinline__ double node_inv_volume(const NodalGeom& g, int i, int j, int k)
+{
+    double f = 1.0;
+    if (!g.per[0] && (i == 0 || i == g.n[0])) f *= 2.0;
+    if (!g.per[1] && (j == 0 || j == g.n[1])) f *= 2.0;
+    if (!g.per[2] && (k == 0 || k == g.n[2])) f *= 2.0;
+    return f / g.vol;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -105,17 +105,7 @@ __global__ void k_mac_prolong_add(CellGeom gf, CellGeom gc, const T* __restrict_
     store_cell(xf, gf, i, j, k, xf[p] + xc[pidx(gc.sy, gc.sz, i >> 1, j >> 1, k >> 1)]);
 }
 
-__device__ double mac_block_sum(double v, double* red)
-{
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    __syncthreads();
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    double t = 0.0;
-    for (int w = 0; w < nw; ++w) t += red[w];
-    return t;
-}
+__device__ __forceinline__ double mac_block_sum(double v, double*) { return block_sum_all(v); }
 
 // Jacobi-preconditioned CG in FP64 on the coarsest level, one CTA.
 template <typename T>

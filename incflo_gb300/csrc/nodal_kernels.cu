@@ -13,6 +13,8 @@
 // div(u) like the max-norm convergence test of MLMG.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "gbp_internal.cuh"
 #include "nodal_kernels.h"
 
@@ -236,17 +238,7 @@ __global__ void __launch_bounds__(256) k_prolong_add(NodalGeom gf, NodalGeom gc,
 // ---------------------------------------------------------------------------------------
 // bottom solve: Jacobi-preconditioned CG in FP64 inside one CTA
 // ---------------------------------------------------------------------------------------
-__device__ double block_sum(double v, double* red)
-{
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    __syncthreads();
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    double t = 0.0;
-    for (int w = 0; w < nw; ++w) t += red[w];  // same order in every thread: deterministic
-    return t;
-}
+__device__ __forceinline__ double block_sum(double v, double*) { return block_sum_all(v); }
 
 template <typename T>
 __global__ void __launch_bounds__(1024) k_bottom_cg(NodalGeom g, const double* __restrict__ s,
@@ -371,6 +363,59 @@ __global__ void __launch_bounds__(1024) k_bottom_cg(NodalGeom g, const double* _
     }
 }
 
+// Dense bottom solve: x = M b with M the precomputed FP64 inverse of the coarsest operator
+// (singular systems: the inverse of A + c 1 1^T, exact for consistent b). M is symmetric and
+// stored so that step v of the product reads a contiguous row across the threads.
+template <typename T>
+__global__ void __launch_bounds__(256) k_bottom_dense(NodalGeom g, const double* __restrict__ M,
+                                                      const T* __restrict__ bin, T* __restrict__ xout, int singular)
+{
+    extern __shared__ double bb[];
+    const int N = g.nu[0] * g.nu[1] * g.nu[2];
+    double part = 0.0, vpart = 0.0;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        const double v = node_is_dirichlet(g, i, j, k) ? 0.0 : (double)bin[pidx(g.sy, g.sz, i, j, k)];
+        bb[t] = v;
+        part += v;
+        vpart += node_volume(g, i, j, k);
+    }
+    if (singular) {
+        // consistent right-hand side: remove the component along the constants
+        const double s = block_sum_all(part);
+        const double vs = block_sum_all(vpart);
+        const double c = s / vs;
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            int i, j, k;
+            decode_node(g, t, i, j, k);
+            bb[t] -= c * node_volume(g, i, j, k);
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        double a0 = 0.0, a1 = 0.0;
+        int v = 0;
+        for (; v + 1 < N; v += 2) {
+            a0 = fma(M[(size_t)v * N + t], bb[v], a0);
+            a1 = fma(M[(size_t)(v + 1) * N + t], bb[v + 1], a1);
+        }
+        if (v < N) a0 = fma(M[(size_t)v * N + t], bb[v], a0);
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        store_node(xout, g, i, j, k, (T)(a0 + a1));
+    }
+}
+
+template <typename T>
+void nodal_bottom_dense(const NodalGeom& g, const double* M, const T* b, T* x, int singular, cudaStream_t st)
+{
+    const int N = g.nu[0] * g.nu[1] * g.nu[2];
+    k_bottom_dense<T><<<1, 256, N * sizeof(double), st>>>(g, M, b, x, singular);
+}
+template void nodal_bottom_dense<double>(const NodalGeom&, const double*, const double*, double*, int, cudaStream_t);
+template void nodal_bottom_dense<float>(const NodalGeom&, const double*, const float*, float*, int, cudaStream_t);
+
 // ---------------------------------------------------------------------------------------
 // level-0 set-up and the fused kernels around the solve
 // ---------------------------------------------------------------------------------------
@@ -435,107 +480,149 @@ __global__ void k_sigma_coarsen(NodalGeom gf, NodalGeom gc, const double* __rest
 }
 
 // g = -(weak divergence) of u' = u + (add_gp ? sigma*gp : 0) - (sub_old ? u_old : 0).
-// Ghost cells enter only across an inflow face, and only with their normal component.
-__global__ void __launch_bounds__(256) k_nodal_rhs(NodalGeom g, RhsArgs a, const double* __restrict__ s64,
-                                                   double* __restrict__ b, unsigned long long* norm)
+// A CTA covers a 32x4x4 box of nodes. Its 33x5x5 surrounding cells are read once (coalesced along
+// x) into shared memory as the per-cell weak fluxes F_d = (h_e h_f / 4) u'_d; every node then sums
+// +-F over its 8 cells. Ghost cells carry F only across an inflow face, and only the normal
+// component (the inflow velocity); every other ghost carries 0 (the wall / outflow case).
+// part: per-block sums of g for the consistency correction of singular systems.
+constexpr int RX = 32, RY = 4, RZ = 4;
+__global__ void __launch_bounds__(RX* RY* RZ) k_nodal_rhs(NodalGeom g, RhsArgs a, const double* __restrict__ s64,
+                                                          double* __restrict__ b, double* __restrict__ part)
 {
-    int i, j, k;
-    double nv = 0.0;
-    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
-        double acc = 0.0;
-        if (!node_is_dirichlet(g, i, j, k)) {
-            const int idx[3] = {i, j, k};
-#pragma unroll 1
-            for (int q = 0; q < 8; ++q) {
-                const int sel[3] = {q & 1, (q >> 1) & 1, (q >> 2) & 1};
-                int cell[3];
-                int nout = 0, dout = -1;
+    __shared__ double F[3][RZ + 1][RY + 1][RX + 1];
+    const int x0 = blockIdx.x * RX, y0 = blockIdx.y * RY, z0 = blockIdx.z * RZ;
+    const int tid = threadIdx.x + RX * (threadIdx.y + RY * threadIdx.z);
+    constexpr int NC = (RX + 1) * (RY + 1) * (RZ + 1);
+    for (int q = tid; q < NC; q += RX * RY * RZ) {
+        const int cx = q % (RX + 1), cy = (q / (RX + 1)) % (RY + 1), cz = q / ((RX + 1) * (RY + 1));
+        int cell[3] = {x0 - 1 + cx, y0 - 1 + cy, z0 - 1 + cz};
+        int nout = 0, dout = -1;
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    int ci = idx[d] - 1 + sel[d];
-                    if (g.per[d]) {
-                        if (ci < 0) ci += g.n[d];
-                        if (ci >= g.n[d]) ci -= g.n[d];
-                    } else if (ci < 0 || ci >= g.n[d]) {
-                        ++nout;
-                        dout = d;
-                    }
-                    cell[d] = ci;
-                }
-                if (nout == 0) {
-                    const double sg = a.add_gp ? s64[pidx(g.sy, g.sz, cell[0], cell[1], cell[2])] : 0.0;
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        double u = a4(a.vel, cell[0], cell[1], cell[2], d);
-                        if (a.add_gp) u += a4(a.gp, cell[0], cell[1], cell[2], d) * sg;
-                        if (a.sub_old) u -= a4(a.vel_old, cell[0], cell[1], cell[2], d);
-                        acc += (sel[d] ? a.cf[d] : -a.cf[d]) * u;
-                    }
-                } else if (nout == 1) {
-                    const int inflow = cell[dout] < 0 ? a.inflow_lo[dout] : a.inflow_hi[dout];
-                    if (inflow) {
-                        double u = a4(a.vel, cell[0], cell[1], cell[2], dout);
-                        acc += (sel[dout] ? a.cf[dout] : -a.cf[dout]) * u;
-                    }
-                }
+        for (int d = 0; d < 3; ++d) {
+            int ci = cell[d];
+            if (g.per[d]) {
+                if (ci < 0) ci += g.n[d];
+                if (ci >= g.n[d]) ci -= g.n[d];
+            } else if (ci < 0 || ci >= g.n[d]) {
+                ++nout;
+                dout = d;
             }
-            if (norm) nv = fabs(acc) / node_volume(g, i, j, k);
+            cell[d] = ci;
         }
-        b[pidx(g.sy, g.sz, i, j, k)] = -acc;
+        double f[3] = {0.0, 0.0, 0.0};
+        if (nout == 0 && cell[0] < g.n[0] + 1 && cell[1] < g.n[1] + 1 && cell[2] < g.n[2] + 1) {
+            const long long off = (long long)(cell[0] - a.vel.lo[0]) + (long long)(cell[1] - a.vel.lo[1]) * a.vel.jstride +
+                                  (long long)(cell[2] - a.vel.lo[2]) * a.vel.kstride;
+            const double sg = a.add_gp ? s64[pidx(g.sy, g.sz, cell[0], cell[1], cell[2])] : 0.0;
+            long long og = 0, oo = 0;
+            if (a.add_gp)
+                og = (long long)(cell[0] - a.gp.lo[0]) + (long long)(cell[1] - a.gp.lo[1]) * a.gp.jstride +
+                     (long long)(cell[2] - a.gp.lo[2]) * a.gp.kstride;
+            if (a.sub_old)
+                oo = (long long)(cell[0] - a.vel_old.lo[0]) + (long long)(cell[1] - a.vel_old.lo[1]) * a.vel_old.jstride +
+                     (long long)(cell[2] - a.vel_old.lo[2]) * a.vel_old.kstride;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                double u = a.vel.data[off + d * a.vel.nstride];
+                if (a.add_gp) u = fma(a.gp.data[og + d * a.gp.nstride], sg, u);
+                if (a.sub_old) u -= a.vel_old.data[oo + d * a.vel_old.nstride];
+                f[d] = a.cf[d] * u;
+            }
+        } else if (nout == 1) {
+            const int inflow = cell[dout] < 0 ? a.inflow_lo[dout] : a.inflow_hi[dout];
+            if (inflow) f[dout] = a.cf[dout] * a4(a.vel, cell[0], cell[1], cell[2], dout);
+        }
+        F[0][cz][cy][cx] = f[0];
+        F[1][cz][cy][cx] = f[1];
+        F[2][cz][cy][cx] = f[2];
     }
-    if (norm) {
-        nv = block_max(nv);
-        if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+    const int i = x0 + tx, j = y0 + ty, k = z0 + tz;
+    double gv = 0.0;
+    if (i < g.nu[0] && j < g.nu[1] && k < g.nu[2]) {
+        if (!node_is_dirichlet(g, i, j, k)) {
+            double dx = 0.0, dy = 0.0, dz = 0.0;
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+#pragma unroll
+                for (int bq = 0; bq < 2; ++bq) {
+                    dx += F[0][tz + c][ty + bq][tx + 1] - F[0][tz + c][ty + bq][tx];
+                    dy += F[1][tz + c][ty + 1][tx + bq] - F[1][tz + c][ty][tx + bq];
+                    dz += F[2][tz + 1][ty + c][tx + bq] - F[2][tz][ty + c][tx + bq];
+                }
+            gv = -((dx + dy) + dz);
+        }
+        b[pidx(g.sy, g.sz, i, j, k)] = gv;
+    }
+    if (part) {
+        const double t = block_sum_all(gv);
+        if (tid == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = t;
     }
 }
 
 // strong-form max norm max_i |v_i| / V_i over the unique non-Dirichlet nodes
 __global__ void __launch_bounds__(256) k_node_norm(NodalGeom g, const double* __restrict__ v, unsigned long long* norm)
 {
-    int i, j, k;
     double nv = 0.0;
-    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k))
-        if (!node_is_dirichlet(g, i, j, k)) nv = fabs(v[pidx(g.sy, g.sz, i, j, k)]) / node_volume(g, i, j, k);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        if (!decode_node(g, t, i, j, k)) break;
+        if (!node_is_dirichlet(g, i, j, k))
+            nv = fmax(nv, fabs(v[pidx(g.sy, g.sz, i, j, k)]) * node_inv_volume(g, i, j, k));
+    }
     nv = block_max(nv);
     if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
 }
 
-// Deterministic two-pass sums: per-block partials, then one block folds them.
-__global__ void k_node_sums(NodalGeom g, const double* __restrict__ v, int weighted, double* __restrict__ part)
+// Per-block partial sums (weighted: sum V_i v_i), grid-stride over the unique nodes.
+__global__ void __launch_bounds__(256) k_node_sums(NodalGeom g, const double* __restrict__ v, int weighted,
+                                                   double* __restrict__ part)
 {
-    __shared__ double red[32];
-    int i, j, k;
     double acc = 0.0;
-    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
-        double x = v[pidx(g.sy, g.sz, i, j, k)];
-        acc = weighted ? x * node_volume(g, i, j, k) : x;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        if (!decode_node(g, t, i, j, k)) break;
+        const double x = v[pidx(g.sy, g.sz, i, j, k)];
+        acc += weighted ? x * node_volume(g, i, j, k) : x;
     }
-    acc = block_sum(acc, red);
+    acc = block_sum_all(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-// mode 0: b_i -= V_i * sum(b) / sum(V) (consistent right-hand side of a singular system)
-// mode 1: x_i -= sum(V x) / sum(V)       (gauge: volume-weighted mean zero), with aliases
-__global__ void k_remove_mean(NodalGeom g, double* __restrict__ v, const double* __restrict__ part, int nparts,
-                              double vtot, int mode)
+// One block folds the partials in a fixed order: scal = sum / vtot.
+__global__ void __launch_bounds__(1024) k_fold(const double* __restrict__ part, int nparts, double vtot,
+                                               double* __restrict__ scal)
 {
-    __shared__ double tot;
-    __shared__ double red[32];
     double acc = 0.0;
     for (int t = threadIdx.x; t < nparts; t += blockDim.x) acc += part[t];
-    // fold in a fixed order per block (identical in every block)
-    acc = block_sum(acc, red);
-    if (threadIdx.x == 0) tot = acc;
-    __syncthreads();
-    const double c = tot / vtot;
+    acc = block_sum_all(acc);
+    if (threadIdx.x == 0) *scal = acc / vtot;
+}
+
+// mode 0: b_i -= V_i c (consistent right-hand side of a singular system), and the strong-form
+//         max norm of the corrected b into *norm
+// mode 1: x_i -= c (gauge: volume-weighted mean zero), with periodic aliases
+__global__ void __launch_bounds__(256) k_remove_mean(NodalGeom g, double* __restrict__ v, const double* __restrict__ scal,
+                                                     int mode, unsigned long long* norm)
+{
+    const double c = *scal;
+    double nv = 0.0;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         if (!decode_node(g, t, i, j, k)) break;
         const long long p = pidx(g.sy, g.sz, i, j, k);
-        if (mode == 0)
-            v[p] -= c * node_volume(g, i, j, k);
-        else
+        if (mode == 0) {
+            const double bv = v[p] - c * node_volume(g, i, j, k);
+            v[p] = bv;
+            nv = fmax(nv, fabs(bv) * node_inv_volume(g, i, j, k));
+        } else {
             store_node(v, g, i, j, k, v[p] - c);
+        }
+    }
+    if (mode == 0 && norm) {
+        nv = block_max(nv);
+        if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
     }
 }
 
@@ -705,27 +792,48 @@ void nodal_sigma_coarsen(const NodalGeom& gf, const NodalGeom& gc, const double*
     k_sigma_coarsen<<<nblocks(ncells(gc), 256), 256, 0, st>>>(gf, gc, sf, sc64, sc32);
 }
 
-void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, unsigned long long* norm,
-               cudaStream_t st)
+void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, double* part, cudaStream_t st)
 {
-    k_nodal_rhs<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, a, s64, b, norm);
+    dim3 grid((g.nu[0] + RX - 1) / RX, (g.nu[1] + RY - 1) / RY, (g.nu[2] + RZ - 1) / RZ);
+    k_nodal_rhs<<<grid, dim3(RX, RY, RZ), 0, st>>>(g, a, s64, b, part);
 }
 
-void nodal_remove_mean(const NodalGeom& g, double* v, double* partials, int mode, cudaStream_t st)
+int nodal_rhs_partials(const NodalGeom& g)
 {
-    const unsigned nb = nblocks(nunique(g), 256);
-    k_node_sums<<<nb, 256, 0, st>>>(g, v, mode == 1, partials);
-    const double vtot = (double)g.n[0] * g.h[0] * (double)g.n[1] * g.h[1] * (double)g.n[2] * g.h[2];
-    unsigned nb2 = nb < 1024 ? nb : 1024;
-    k_remove_mean<<<nb2, 256, 0, st>>>(g, v, partials, (int)nb, vtot, mode);
+    return ((g.nu[0] + RX - 1) / RX) * ((g.nu[1] + RY - 1) / RY) * ((g.nu[2] + RZ - 1) / RZ);
+}
+
+static inline unsigned stride_blocks(long long n) { return (unsigned)std::min<long long>(nblocks(n, 256), 1184); }
+
+static double domain_volume(const NodalGeom& g)
+{
+    return (double)g.n[0] * g.h[0] * (double)g.n[1] * g.h[1] * (double)g.n[2] * g.h[2];
+}
+
+// fold `nparts` partial sums into scal = sum / domain volume
+void nodal_fold(const NodalGeom& g, const double* part, int nparts, double* scal, cudaStream_t st)
+{
+    k_fold<<<1, 1024, 0, st>>>(part, nparts, domain_volume(g), scal);
+}
+
+void nodal_remove_mean(const NodalGeom& g, double* v, double* partials, double* scal, int mode, int have_partials,
+                       int nparts, unsigned long long* norm, cudaStream_t st)
+{
+    if (!have_partials) {
+        const unsigned nb = stride_blocks(nunique(g));
+        k_node_sums<<<nb, 256, 0, st>>>(g, v, mode == 1, partials);
+        nparts = (int)nb;
+    }
+    k_fold<<<1, 1024, 0, st>>>(partials, nparts, domain_volume(g), scal);
+    k_remove_mean<<<stride_blocks(nunique(g)), 256, 0, st>>>(g, v, scal, mode, norm);
 }
 
 void nodal_norm(const NodalGeom& g, const double* v, unsigned long long* norm, cudaStream_t st)
 {
-    k_node_norm<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, v, norm);
+    k_node_norm<<<stride_blocks(nunique(g)), 256, 0, st>>>(g, v, norm);
 }
 
-int nodal_partials_needed(const NodalGeom& g) { return (int)nblocks(nunique(g), 256); }
+int nodal_partials_needed(const NodalGeom& g) { return std::max(nodal_rhs_partials(g), 1184); }
 
 template <typename TE>
 void nodal_add_correction(const NodalGeom& g, double* x, const TE* e, double inv_scale, cudaStream_t st)

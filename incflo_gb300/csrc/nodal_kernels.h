@@ -43,16 +43,23 @@ template <typename T>
 void nodal_bottom(const NodalGeom& g, const double* s64, const T* b, T* x, double* scratch, int maxiter,
                   double rtol, double atol, int* info, cudaStream_t st);
 
+template <typename T>
+void nodal_bottom_dense(const NodalGeom& g, const double* M, const T* b, T* x, int singular, cudaStream_t st);
+
 void nodal_sigma_from_rho(const NodalGeom& g, const gbp_array4* rho, double scale, double rho0, double* s64,
                           float* s32, cudaStream_t st);
 void nodal_sigma_copy(const NodalGeom& g, const gbp_array4* sig, double cval, double* s64, float* s32,
                       cudaStream_t st);
 void nodal_sigma_coarsen(const NodalGeom& gf, const NodalGeom& gc, const double* sf, double* sc64, float* sc32,
                          cudaStream_t st);
-void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, unsigned long long* norm,
-               cudaStream_t st);
-// mode 0: make b consistent (remove V-weighted mean); mode 1: gauge x to zero V-weighted mean
-void nodal_remove_mean(const NodalGeom& g, double* v, double* partials, int mode, cudaStream_t st);
+// part: per-block sums of the right-hand side (nodal_rhs_partials(g) of them), or nullptr
+void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, double* part, cudaStream_t st);
+int nodal_rhs_partials(const NodalGeom& g);
+// mode 0: make b consistent (remove V-weighted mean; max norm of the result into *norm);
+// mode 1: gauge x to zero V-weighted mean. have_partials: `partials` already holds nparts sums of v.
+void nodal_remove_mean(const NodalGeom& g, double* v, double* partials, double* scal, int mode, int have_partials,
+                       int nparts, unsigned long long* norm, cudaStream_t st);
+void nodal_fold(const NodalGeom& g, const double* part, int nparts, double* scal, cudaStream_t st);
 int nodal_partials_needed(const NodalGeom& g);
 void nodal_norm(const NodalGeom& g, const double* v, unsigned long long* norm, cudaStream_t st);
 template <typename TE>

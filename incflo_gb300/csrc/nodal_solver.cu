@@ -14,8 +14,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "nodal_solver.h"
+#include "nodal_sweep.h"
 
 namespace gbp {
 
@@ -101,6 +103,7 @@ void NodalSolver::destroy()
     if (ev1) cudaEventDestroy(ev1);
     if (ev2) cudaEventDestroy(ev2);
     ev0 = ev1 = ev2 = nullptr;
+    if (pool.base) sweep_forget_maps(pool.base, pool.bytes);
     pool.release();
     L.clear();
     sigma_ready = false;
@@ -201,6 +204,10 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
     add(5 * B.g.count, 8);
     add(16, 4);
     add(8, 8);
+    add(8, 8);
+    nbottom = B.g.nu[0] * B.g.nu[1] * B.g.nu[2];
+    dense_bottom = nbottom <= kDenseBottomMax;
+    if (dense_bottom) add((size_t)nbottom * nbottom, 8);
     need += 4096;
     rc = pool.reserve(need);
     if (rc) return rc;
@@ -222,7 +229,10 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
     partials = pool.take<double>(nodal_partials_needed(G0) + 64);
     bscr = pool.take<double>(5 * B.g.count);
     dinfo = pool.take<int>(16);
+    derr = reinterpret_cast<unsigned*>(dinfo + 8);
     dnorm = pool.take<unsigned long long>(8);
+    dscal = pool.take<double>(8);
+    if (dense_bottom) dmat = pool.take<double>((size_t)nbottom * nbottom);
     GBP_CUDA(cudaMallocHost(&hnorm, 8 * sizeof(unsigned long long)));
     memset(hnorm, 0, 8 * sizeof(unsigned long long));
     GBP_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -244,7 +254,7 @@ int NodalSolver::set_sigma_from_density(const gbp_array4* rho, double scale, dou
     nk += (long long)L.size();
     GBP_CUDA(cudaGetLastError());
     sigma_ready = true;
-    return GBP_OK;
+    return build_bottom();
 }
 
 int NodalSolver::set_sigma(const gbp_array4* sigma, double cval)
@@ -255,6 +265,112 @@ int NodalSolver::set_sigma(const gbp_array4* sigma, double cval)
     nk += (long long)L.size();
     GBP_CUDA(cudaGetLastError());
     sigma_ready = true;
+    return build_bottom();
+}
+
+// Dense inverse of the coarsest operator, assembled on the host from the coarsest sigma: the
+// bottom solve becomes one FP64 matrix-vector product in one CTA. Singular systems (no Dirichlet
+// face) use (A + c 1 1^T)^-1, which solves A x = b exactly for consistent b (sum b = 0).
+int NodalSolver::build_bottom()
+{
+    if (!dense_bottom) return GBP_OK;
+    const NodalLevel& B = L.back();
+    const NodalGeom& g = B.g;
+    std::vector<double> sg((size_t)g.count);
+    GBP_CUDA(cudaMemcpyAsync(sg.data(), B.s64, sizeof(double) * g.count, cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    const int N = nbottom;
+    std::vector<double> A((size_t)N * N, 0.0);
+    auto wrapn = [&](int i, int d) { return g.per[d] ? ((i % g.n[d]) + g.n[d]) % g.n[d] : i; };
+    auto dir = [&](int i, int j, int k) {
+        return (g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) || (g.dhi[1] && j == g.n[1]) ||
+               (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+    };
+    for (int k = 0; k < g.nu[2]; ++k)
+        for (int j = 0; j < g.nu[1]; ++j)
+            for (int i = 0; i < g.nu[0]; ++i) {
+                const int u = i + g.nu[0] * (j + g.nu[1] * k);
+                if (dir(i, j, k)) {
+                    A[(size_t)u * N + u] = 1.0;
+                    continue;
+                }
+                for (int c = 0; c < 2; ++c)
+                    for (int b = 0; b < 2; ++b)
+                        for (int a = 0; a < 2; ++a) {
+                            int cell[3] = {i - 1 + a, j - 1 + b, k - 1 + c};
+                            bool inside = true;
+                            for (int d = 0; d < 3; ++d) {
+                                if (g.per[d])
+                                    cell[d] = wrapn(cell[d], d);
+                                else if (cell[d] < 0 || cell[d] >= g.n[d])
+                                    inside = false;
+                            }
+                            if (!inside) continue;
+                            const double s = sg[(size_t)pidx(g.sy, g.sz, cell[0], cell[1], cell[2])];
+                            for (int r = 0; r < 2; ++r)
+                                for (int q = 0; q < 2; ++q)
+                                    for (int pp = 0; pp < 2; ++pp) {
+                                        int nd[3] = {cell[0] + pp, cell[1] + q, cell[2] + r};
+                                        for (int d = 0; d < 3; ++d)
+                                            if (g.per[d]) nd[d] = wrapn(nd[d], d);
+                                        if (dir(nd[0], nd[1], nd[2])) continue;
+                                        const int mask = (pp != 1 - a) | ((q != 1 - b) << 1) | ((r != 1 - c) << 2);
+                                        const int v = nd[0] + g.nu[0] * (nd[1] + g.nu[1] * nd[2]);
+                                        A[(size_t)u * N + v] += s * g.K[mask];
+                                    }
+                        }
+            }
+    if (singular) {
+        double tr = 0.0;
+        for (int u = 0; u < N; ++u) tr += A[(size_t)u * N + u];
+        const double c = tr / ((double)N * N);
+        for (auto& v : A) v += c;
+    }
+    // Gauss-Jordan inverse with partial pivoting
+    std::vector<double> M((size_t)N * N, 0.0);
+    for (int u = 0; u < N; ++u) M[(size_t)u * N + u] = 1.0;
+    for (int col = 0; col < N; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < N; ++r)
+            if (fabs(A[(size_t)r * N + col]) > fabs(A[(size_t)piv * N + col])) piv = r;
+        if (A[(size_t)piv * N + col] == 0.0) {
+            set_error("nodal plan: the coarsest operator is singular beyond its constant null space");
+            return GBP_BAD_ARG;
+        }
+        if (piv != col)
+            for (int q = 0; q < N; ++q) {
+                std::swap(A[(size_t)piv * N + q], A[(size_t)col * N + q]);
+                std::swap(M[(size_t)piv * N + q], M[(size_t)col * N + q]);
+            }
+        const double inv = 1.0 / A[(size_t)col * N + col];
+        for (int q = 0; q < N; ++q) {
+            A[(size_t)col * N + q] *= inv;
+            M[(size_t)col * N + q] *= inv;
+        }
+        for (int r = 0; r < N; ++r) {
+            if (r == col) continue;
+            const double f = A[(size_t)r * N + col];
+            if (f == 0.0) continue;
+            for (int q = 0; q < N; ++q) {
+                A[(size_t)r * N + q] -= f * A[(size_t)col * N + q];
+                M[(size_t)r * N + q] -= f * M[(size_t)col * N + q];
+            }
+        }
+    }
+    // Dirichlet nodes stay 0: zero their rows and columns
+    for (int k = 0; k < g.nu[2]; ++k)
+        for (int j = 0; j < g.nu[1]; ++j)
+            for (int i = 0; i < g.nu[0]; ++i)
+                if (dir(i, j, k)) {
+                    const int u = i + g.nu[0] * (j + g.nu[1] * k);
+                    for (int q = 0; q < N; ++q) M[(size_t)u * N + q] = M[(size_t)q * N + u] = 0.0;
+                }
+    // stored transposed: step v of the product reads M[v][*] across the threads
+    std::vector<double> Mt((size_t)N * N);
+    for (int u = 0; u < N; ++u)
+        for (int v = 0; v < N; ++v) Mt[(size_t)v * N + u] = M[(size_t)u * N + v];
+    GBP_CUDA(cudaMemcpyAsync(dmat, Mt.data(), sizeof(double) * Mt.size(), cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
     return GBP_OK;
 }
 
@@ -262,8 +378,11 @@ template <>
 void NodalSolver::bottom<double>(int l, const double* b, double* x)
 {
     const NodalLevel& lv = L[l];
-    nodal_bottom<double>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
-                         cap_or_st);
+    if (dense_bottom)
+        nodal_bottom_dense<double>(lv.g, dmat, b, x, singular ? 1 : 0, cap_or_st);
+    else
+        nodal_bottom<double>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
+                             cap_or_st);
     xres[l] = x;
 }
 
@@ -271,8 +390,11 @@ template <>
 void NodalSolver::bottom<float>(int l, const float* b, float* x)
 {
     const NodalLevel& lv = L[l];
-    nodal_bottom<float>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
-                        cap_or_st);
+    if (dense_bottom)
+        nodal_bottom_dense<float>(lv.g, dmat, b, x, singular ? 1 : 0, cap_or_st);
+    else
+        nodal_bottom<float>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
+                            cap_or_st);
     xres[l] = x;
 }
 
@@ -294,6 +416,29 @@ struct LevelBufs<float> {
     static float* b(const NodalLevel& l) { return l.b32; }
     static float* r(const NodalLevel& l) { return l.r32; }
 };
+
+template <typename T>
+void NodalSolver::jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, cudaStream_t s_)
+{
+    if (use_tma && sweep_supported(g)) {
+        int rc = nodal_sweep<T>(g, 0, s, x, b, out, opt.omega, derr, nullptr, s_);
+        if (rc && !launch_rc) launch_rc = rc;
+    } else {
+        nodal_jacobi<T>(g, s, x, b, out, opt.omega, false, s_);
+    }
+}
+
+template <typename T>
+void NodalSolver::resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
+                        cudaStream_t s_)
+{
+    if (use_tma && sweep_supported(g)) {
+        int rc = nodal_sweep<T>(g, 1, s, x, b, r, opt.omega, derr, norm, s_);
+        if (rc && !launch_rc) launch_rc = rc;
+    } else {
+        nodal_resid<T>(g, s, x, b, r, norm, s_);
+    }
+}
 
 // V-cycle for A x = b on level l. zero: x starts at 0; otherwise from xres[l].
 template <typename T>
@@ -320,11 +465,11 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
         }
     }
     for (int q = 0; q < pre; ++q) {
-        nodal_jacobi<T>(lv.g, B::s(lv), x, b, t, opt.omega, false, s);
+        jacobi<T>(lv.g, B::s(lv), x, b, t, s);
         ++nk;
         std::swap(x, t);
     }
-    nodal_resid<T>(lv.g, B::s(lv), x, b, B::r(lv), nullptr, s);
+    resid<T>(lv.g, B::s(lv), x, b, B::r(lv), nullptr, s);
     const NodalLevel& cv = L[l + 1];
     nodal_restrict<T>(lv.g, cv.g, B::r(lv), B::b(cv), s);
     nk += 2;
@@ -332,7 +477,7 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     nodal_prolong_add<T>(lv.g, cv.g, (const T*)xres[l + 1], x, s);
     ++nk;
     for (int q = 0; q < opt.nu2; ++q) {
-        nodal_jacobi<T>(lv.g, B::s(lv), x, b, t, opt.omega, false, s);
+        jacobi<T>(lv.g, B::s(lv), x, b, t, s);
         ++nk;
         std::swap(x, t);
     }
@@ -356,7 +501,7 @@ void NodalSolver::record_iteration()
         nodal_add_correction<double>(l0.g, phi, (const double*)xres[0], 1.0, s);
     }
     cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), s);
-    nodal_resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, s);
+    resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, s);
     nk += 2;
     cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     step_kernels = nk - nk0;
@@ -380,6 +525,10 @@ int NodalSolver::run_iteration()
         cudaError_t e = cudaStreamEndCapture(cap, &graph);
         cap_or_st = st;
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(refinement step)");
+        if (launch_rc) {
+            cudaGraphDestroy(graph);
+            return launch_rc;
+        }
         e = cudaGraphInstantiate(&gexec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
@@ -410,8 +559,11 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
     if (!have_guess) GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
     GBP_CUDA(cudaMemsetAsync(dnorm, 0, 4 * sizeof(unsigned long long), st));
     GBP_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int), st));
+    GBP_CUDA(cudaMemsetAsync(derr, 0, sizeof(unsigned), st));
+    launch_rc = 0;
     nodal_norm(l0.g, rhs0, dnorm, st);
-    nodal_resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
+    resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
+    if (launch_rc) return launch_rc;
     nk += 2;
     GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     GBP_CUDA(cudaStreamSynchronize(st));
@@ -451,8 +603,19 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
         }
     }
     if (singular) {
-        nodal_remove_mean(l0.g, phi, partials, 1, st);
-        nk += 2;
+        nodal_remove_mean(l0.g, phi, partials, dscal, 1, 0, 0, nullptr, st);
+        nk += 3;
+    }
+    if (launch_rc) return launch_rc;
+    {
+        unsigned herr = 0;
+        GBP_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+        if (herr) {
+            set_error("nodal solve: a bounded device wait (TMA pipeline) ran out");
+            if (stats) stats->status = GBP_TIMEOUT;
+            return GBP_TIMEOUT;
+        }
     }
     GBP_CUDA(cudaEventRecord(ev2, st));
     GBP_CUDA(cudaGetLastError());
@@ -484,11 +647,16 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
     }
     const NodalLevel& l0 = L[0];
     GBP_CUDA(cudaEventRecord(ev0, st));
-    nodal_rhs(l0.g, rhs, l0.s64, rhs0, nullptr, st);
+    GBP_CUDA(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), st));
+    nodal_rhs(l0.g, rhs, l0.s64, rhs0, singular ? partials : nullptr, st);
     ++nk;
     if (singular) {
-        nodal_remove_mean(l0.g, rhs0, partials, 0, st);
+        // consistent right-hand side, and its max norm (the relative-tolerance reference)
+        nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, 1, nodal_rhs_partials(l0.g), dnorm, st);
         nk += 2;
+    } else {
+        nodal_norm(l0.g, rhs0, dnorm, st);
+        ++nk;
     }
     if (phi_guess) {
         nodal_load_phi(l0.g, *phi_guess, phi, st);
@@ -537,16 +705,10 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
     GBP_CUDA(cudaEventRecord(ev0, st));
     for (int r = 0; r < reps; ++r) {
         switch (which) {
-        case 0:
-            nodal_jacobi<double>(g, l0.s64, (r & 1) ? l0.t64 : l0.x64, res, (r & 1) ? l0.x64 : l0.t64, opt.omega,
-                                 false, st);
-            break;
-        case 1:
-            nodal_jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, opt.omega,
-                                false, st);
-            break;
-        case 2: nodal_resid<double>(g, l0.s64, phi, rhs0, l0.r64, nullptr, st); break;
-        default: nodal_resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st); break;
+        case 0: jacobi<double>(g, l0.s64, (r & 1) ? l0.t64 : l0.x64, res, (r & 1) ? l0.x64 : l0.t64, st); break;
+        case 1: jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, st); break;
+        case 2: resid<double>(g, l0.s64, phi, rhs0, l0.r64, nullptr, st); break;
+        default: resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st); break;
         }
     }
     GBP_CUDA(cudaEventRecord(ev1, st));

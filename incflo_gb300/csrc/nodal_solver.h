@@ -67,8 +67,16 @@ private:
     void vcycle(int l, const T* b, bool zero);
     template <typename T>
     void bottom(int l, const T* b, T* x);
+    // Jacobi sweep / residual on one level: the TMA-staged sweep where the level is large enough,
+    // the plain kernels on small levels
+    template <typename T>
+    void jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, cudaStream_t s_);
+    template <typename T>
+    void resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
+               cudaStream_t s_);
     void record_iteration();
     int run_iteration();
+    int build_bottom();
 
     gbp_options opt{};
     cudaStream_t st = nullptr;
@@ -93,6 +101,14 @@ private:
     int gexec_prec = -1;
     double gexec_scale = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    static constexpr int kDenseBottomMax = 216;
+    int nbottom = 0;
+    bool dense_bottom = false;
+    double* dmat = nullptr;      // dense inverse of the coarsest operator (transposed)
+    double* dscal = nullptr;     // device scalars of the mean / gauge corrections
+    unsigned* derr = nullptr;    // device error word of the TMA sweeps (bit 0: a bounded wait ran out)
+    int launch_rc = 0;           // first failure while issuing a sweep (tensor-map encoding)
+    bool use_tma = true;
     long long nk = 0;            // kernels issued (or replayed through graphs) since reset_count()
     long long step_kernels = 0;  // kernels in one refinement step
 };
