@@ -39,6 +39,7 @@ struct NodalGeom {
     long long sy, sz, count;
     double K[8];   // element stiffness integral(grad N_a . grad N_b) by differing-direction mask
     double vol;    // cell volume
+    double ivol;   // 1 / vol
     double h[3];
     int iso;       // hx == hy == hz: K[1] = K[2] = K[4] = 0 and K[3..7] equal
 };
@@ -137,6 +138,9 @@ __device__ __forceinline__ double node_volume(const NodalGeom& g, int i, int j, 
     return v;
 }
 
+// max that propagates NaN (fmax would drop it): a NaN residual must surface as a NaN norm
+__device__ __forceinline__ double nanmax(double a, double b) { return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000ll) : fmax(a, b); }
+
 // Order-preserving atomic max of a non-negative double (NaN propagates as the largest).
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, double v)
 {
@@ -148,7 +152,7 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, doubl
 __device__ __forceinline__ double block_max(double v)
 {
     __shared__ double red[32];
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
     const int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int lane = lin & 31, wid = lin >> 5;
@@ -157,7 +161,7 @@ __device__ __forceinline__ double block_max(double v)
     __syncthreads();
     if (wid == 0) {
         v = lane < nw ? red[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     }
     return v;  // valid in thread 0
 }
@@ -189,7 +193,7 @@ __device__ __forceinline__ double node_inv_volume(const NodalGeom& g, int i, int
     if (!g.per[0] && (i == 0 || i == g.n[0])) f *= 2.0;
     if (!g.per[1] && (j == 0 || j == g.n[1])) f *= 2.0;
     if (!g.per[2] && (k == 0 || k == g.n[2])) f *= 2.0;
-    return f / g.vol;
+    return f * g.ivol;
 }
 
 // ---------------------------------------------------------------------------------------

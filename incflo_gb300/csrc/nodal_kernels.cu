@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(256) k_resid(NodalGeom g, const T* __restrict_
             T diag;
             T ax = NodalOp<T>::template apply<ISO>(x, s, c, g.sy, g.sz, g, diag);
             v = b[c] - ax;
-            if (norm) nv = fabs((double)v) / node_volume(g, i, j, k);
+            if (norm) nv = fabs((double)v) * node_inv_volume(g, i, j, k);
         }
         store_node(r, g, i, j, k, v);
     }
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(256) k_node_norm(NodalGeom g, const double* __
         int i, j, k;
         if (!decode_node(g, t, i, j, k)) break;
         if (!node_is_dirichlet(g, i, j, k))
-            nv = fmax(nv, fabs(v[pidx(g.sy, g.sz, i, j, k)]) * node_inv_volume(g, i, j, k));
+            nv = nanmax(nv, fabs(v[pidx(g.sy, g.sz, i, j, k)]) * node_inv_volume(g, i, j, k));
     }
     nv = block_max(nv);
     if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(256) k_remove_mean(NodalGeom g, double* __rest
         if (mode == 0) {
             const double bv = v[p] - c * node_volume(g, i, j, k);
             v[p] = bv;
-            nv = fmax(nv, fabs(bv) * node_inv_volume(g, i, j, k));
+            nv = nanmax(nv, fabs(bv) * node_inv_volume(g, i, j, k));
         } else {
             store_node(v, g, i, j, k, v[p] - c);
         }

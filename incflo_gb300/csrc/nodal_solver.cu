@@ -79,6 +79,7 @@ static NodalGeom make_geom(const int n[3], const double h[3], const int per[3], 
     g.count = g.sz * (long long)(n[2] + 3);
     q1_element(h, g.K);
     g.vol = h[0] * h[1] * h[2];
+    g.ivol = 1.0 / g.vol;
     const double hm = std::max(h[0], std::max(h[1], h[2]));
     g.iso = fabs(h[0] - h[1]) <= 1e-12 * hm && fabs(h[0] - h[2]) <= 1e-12 * hm;
     if (g.iso) {
@@ -557,14 +558,20 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
     cap_or_st = st;
     GBP_CUDA(cudaEventRecord(ev1, st));
     if (!have_guess) GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
-    GBP_CUDA(cudaMemsetAsync(dnorm, 0, 4 * sizeof(unsigned long long), st));
+    // dnorm[0] holds |b| (written by project); dnorm[1] receives the initial residual norm
+    GBP_CUDA(cudaMemsetAsync(dnorm + 1, 0, 3 * sizeof(unsigned long long), st));
     GBP_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int), st));
     GBP_CUDA(cudaMemsetAsync(derr, 0, sizeof(unsigned), st));
     launch_rc = 0;
-    nodal_norm(l0.g, rhs0, dnorm, st);
-    resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
-    if (launch_rc) return launch_rc;
-    nk += 2;
+    if (have_guess) {
+        resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
+        if (launch_rc) return launch_rc;
+        ++nk;
+    } else {
+        // phi = 0: the initial residual is b itself, no FP64 stencil needed
+        GBP_CUDA(cudaMemcpyAsync(res, rhs0, sizeof(double) * l0.g.count, cudaMemcpyDeviceToDevice, st));
+        GBP_CUDA(cudaMemcpyAsync(dnorm + 1, dnorm, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+    }
     GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     GBP_CUDA(cudaStreamSynchronize(st));
     const double bnorm = bits_to_double(hnorm[0]);

@@ -1,11 +1,15 @@
 // Level sweeps of the nodal operator staged through shared memory by TMA.
 //
-// A CTA owns a 32 x 8 column of nodes in (x, y) and marches up a chunk of z planes. Per plane it
+// A CTA owns a 32 x TY column of nodes in (x, y) and marches up a chunk of z planes. Per plane it
 // needs x on plane k+1 with a one-node halo, sigma on cell plane k with a one-cell halo and b on
 // plane k; one elected thread brings these in with three cp.async.bulk.tensor loads that complete
-// on one mbarrier per pipeline slot (3 slots, prefetch distance 3). Planes k-1 and k of the 3x3
+// on one mbarrier per pipeline slot (NS slots, prefetch distance NS). Planes k-1 and k of the 3x3
 // neighbourhood and cell plane k-1 stay in registers, so each node reads 9 + 4 + 1 values from
 // shared memory and each array is read from HBM once (halos come from L2).
+//
+// FP32 sweeps are HBM-bound: 32 x 16 tiles and 4 slots keep ~60 KB per SM in flight, and the z
+// chunking is chosen so the grid is a whole number of waves of resident CTAs. FP64 sweeps are
+// bound by the FP64 issue rate of GB300, so their tile is smaller (32 x 8, 3 slots).
 //
 // Boundary handling follows the padded layout of gbp_internal.cuh: a TMA box may start at the
 // ghost row/plane (-1) and run past the padded end (zero fill); tile x origins are multiples of 32
@@ -15,6 +19,7 @@
 
 #include <map>
 #include <mutex>
+#include <string>
 #include <tuple>
 
 #include "gbp_internal.cuh"
@@ -23,14 +28,24 @@
 
 namespace gbp {
 
-constexpr int SW_TX = 32, SW_TY = 8, SW_NS = 3;
+template <typename T>
+struct SweepCfg;
+template <>
+struct SweepCfg<float> {
+    static constexpr int TX = 32, TY = 16, NS = 4;
+};
+template <>
+struct SweepCfg<double> {
+    static constexpr int TX = 32, TY = 8, NS = 3;
+};
 
 template <typename T>
 struct SweepShape {
-    static constexpr int BX = (((SW_TX + 2) * (int)sizeof(T) + 15) / 16 * 16) / (int)sizeof(T);
-    static constexpr int XB = (SW_TY + 2) * BX * (int)sizeof(T);
-    static constexpr int SB = (SW_TY + 1) * BX * (int)sizeof(T);
-    static constexpr int BB = SW_TY * BX * (int)sizeof(T);
+    static constexpr int TX = SweepCfg<T>::TX, TY = SweepCfg<T>::TY, NS = SweepCfg<T>::NS;
+    static constexpr int BX = (((TX + 2) * (int)sizeof(T) + 15) / 16 * 16) / (int)sizeof(T);
+    static constexpr int XB = (TY + 2) * BX * (int)sizeof(T);
+    static constexpr int SB = (TY + 1) * BX * (int)sizeof(T);
+    static constexpr int BB = TY * BX * (int)sizeof(T);
     static constexpr int XO = 0;
     static constexpr int SO = (XB + 127) / 128 * 128;
     static constexpr int BO = SO + (SB + 127) / 128 * 128;
@@ -44,14 +59,8 @@ __device__ __forceinline__ bool has_alias(const NodalGeom& g, int i, int j, int 
            (g.per[2] && (k <= 1 || k == g.n[2] - 1));
 }
 
-template <typename T>
-__device__ __forceinline__ T diff(T a, T c)
-{
-    return a - c;
-}
-
-// (A x)_i from the register planes: Pn = plane k, Pd = plane k -/+ 1 (far plane of the cell layer),
-// sg = sigma of the 2x2 cells of that layer; accumulates into acc and the sigma sum.
+// One cell layer of (A x)_i from the register planes: Pn = plane k, Pd = the layer's far plane
+// (k-1 or k+1), sg = sigma of the layer's 2x2 cells; accumulates into acc and the sigma sum.
 template <typename T, bool ISO>
 __device__ __forceinline__ void layer(const T (&Pn)[3][3], const T (&Pd)[3][3], const T (&sg)[2][2], const NodalGeom& g,
                                       T& acc, T& ssum)
@@ -69,7 +78,7 @@ __device__ __forceinline__ void layer(const T (&Pn)[3][3], const T (&Pd)[3][3], 
                     const T S = (Pn[oy][ox] + Pd[1][ox]) + (Pd[oy][1] + Pd[oy][ox]);
                     acc = fma(s, S, acc);
                 } else {
-                    const T S = (diff(Pn[oy][ox], xc) + diff(Pd[1][ox], xc)) + (diff(Pd[oy][1], xc) + diff(Pd[oy][ox], xc));
+                    const T S = ((Pn[oy][ox] - xc) + (Pd[1][ox] - xc)) + ((Pd[oy][1] - xc) + (Pd[oy][ox] - xc));
                     acc = fmaf(s, S, acc);
                 }
             } else {
@@ -82,21 +91,20 @@ __device__ __forceinline__ void layer(const T (&Pn)[3][3], const T (&Pd)[3][3], 
 }
 
 template <typename T, int MODE, bool ISO>
-__global__ void __launch_bounds__(SW_TX* SW_TY) k_nodal_sweep(const __grid_constant__ CUtensorMap mx,
-                                                               const __grid_constant__ CUtensorMap ms,
-                                                               const __grid_constant__ CUtensorMap mb, NodalGeom g,
-                                                               T* __restrict__ out, T omega, int kchunk,
-                                                               unsigned* err, unsigned long long* norm)
+__global__ void __launch_bounds__(SweepCfg<T>::TX* SweepCfg<T>::TY)
+    k_nodal_sweep(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
+                  const __grid_constant__ CUtensorMap mb, NodalGeom g, T* __restrict__ out, T omega, int kchunk,
+                  unsigned* err, unsigned long long* norm)
 {
     using S = SweepShape<T>;
-    constexpr int BX = S::BX;
-    __shared__ __align__(1024) unsigned char smem[SW_NS * S::STAGE];
-    __shared__ uint64_t bar[SW_NS];
+    constexpr int BX = S::BX, TX = S::TX, NS = S::NS;
+    __shared__ __align__(1024) unsigned char smem[NS * S::STAGE];
+    __shared__ uint64_t bar[NS];
     __shared__ int abort_flag;
 
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + SW_TX * ty;
-    const int x0 = blockIdx.x * SW_TX, y0 = blockIdx.y * SW_TY;
+    const int tid = tx + TX * ty;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * S::TY;
     const int kbeg = blockIdx.z * kchunk;
     const int kend = min(kbeg + kchunk, g.nu[2]);
     const int nsteps = kend - kbeg + 2;
@@ -104,7 +112,7 @@ __global__ void __launch_bounds__(SW_TX* SW_TY) k_nodal_sweep(const __grid_const
     const bool active = i < g.nu[0] && j < g.nu[1];
 
     auto issue = [&](int s) {
-        const int slot = s % SW_NS;
+        const int slot = s % NS;
         unsigned char* base = smem + slot * S::STAGE;
         const int k = kbeg - 2 + s;
         mbar_arrive_expect_tx(&bar[slot], S::TX_BYTES);
@@ -115,13 +123,13 @@ __global__ void __launch_bounds__(SW_TX* SW_TY) k_nodal_sweep(const __grid_const
     };
 
     if (tid == 0) {
-        for (int q = 0; q < SW_NS; ++q) mbar_init(&bar[q], 1);
+        for (int q = 0; q < NS; ++q) mbar_init(&bar[q], 1);
         mbar_fence_init();
         abort_flag = 0;
     }
     __syncthreads();
     if (tid == 0)
-        for (int s = 0; s < SW_NS && s < nsteps; ++s) issue(s);
+        for (int s = 0; s < NS && s < nsteps; ++s) issue(s);
 
     T P0[3][3], P1[3][3], P2[3][3], S0[2][2], S1[2][2];
 #pragma unroll
@@ -132,9 +140,9 @@ __global__ void __launch_bounds__(SW_TX* SW_TY) k_nodal_sweep(const __grid_const
     double nmax = 0.0;
 
     for (int s = 0; s < nsteps; ++s) {
-        const int slot = s % SW_NS;
+        const int slot = s % NS;
         const unsigned char* base = smem + slot * S::STAGE;
-        if (!mbar_wait_bounded(&bar[slot], (uint32_t)((s / SW_NS) & 1), err)) abort_flag = 1;
+        if (!mbar_wait_bounded(&bar[slot], (uint32_t)((s / NS) & 1), err)) abort_flag = 1;
         __syncthreads();
         if (abort_flag) break;
         const T* sx = reinterpret_cast<const T*>(base + S::XO);
@@ -178,7 +186,7 @@ __global__ void __launch_bounds__(SW_TX* SW_TY) k_nodal_sweep(const __grid_const
                     v = xc + omega * (bv - ax) * rd;
                 } else {
                     v = bv - ax;
-                    if (norm) nmax = fmax(nmax, fabs((double)v) / node_volume(g, i, j, k));
+                    if (norm) nmax = nanmax(nmax, fabs((double)v) * node_inv_volume(g, i, j, k));
                 }
             }
             const long long p = pidx(g.sy, g.sz, i, j, k);
@@ -199,14 +207,14 @@ __global__ void __launch_bounds__(SW_TX* SW_TY) k_nodal_sweep(const __grid_const
 #pragma unroll
             for (int b = 0; b < 2; ++b) S0[a][b] = S1[a][b];
         __syncthreads();  // every thread is done with this slot
-        if (tid == 0 && s + SW_NS < nsteps) {
+        if (tid == 0 && s + NS < nsteps) {
             fence_proxy_async();
-            issue(s + SW_NS);
+            issue(s + NS);
         }
     }
     if (abort_flag && tid == 0) {
         // drain the loads still in flight (bounded) before the CTA's shared memory goes away
-        for (int q = 0; q < SW_NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
+        for (int q = 0; q < NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
     }
     if (MODE == 1 && norm) {
         nmax = block_max(nmax);
@@ -232,21 +240,22 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 
 struct MapKey {
     const void* base;
-    int rows;
-    int esize;
+    int boxx, rows, esize;
     long long sy, sz, count;
     bool operator<(const MapKey& o) const
     {
-        return std::tie(base, rows, esize, sy, sz, count) < std::tie(o.base, o.rows, o.esize, o.sy, o.sz, o.count);
+        return std::tie(base, boxx, rows, esize, sy, sz, count) <
+               std::tie(o.base, o.boxx, o.rows, o.esize, o.sy, o.sz, o.count);
     }
 };
 
 static std::mutex g_map_mu;
 static std::map<MapKey, CUtensorMap> g_maps;
 
-static int make_map(const void* base, int esize, const NodalGeom& g, int boxx, int rows, CUtensorMap* out)
+int make_tensor_map(const void* base, int esize, long long sy, long long sz, long long count, int boxx, int rows,
+                    CUtensorMap* out)
 {
-    MapKey key{base, rows, esize, g.sy, g.sz, g.count};
+    MapKey key{base, boxx, rows, esize, sy, sz, count};
     std::lock_guard<std::mutex> lk(g_map_mu);
     auto it = g_maps.find(key);
     if (it != g_maps.end()) {
@@ -259,8 +268,8 @@ static int make_map(const void* base, int esize, const NodalGeom& g, int boxx, i
         return GBP_CUDA_ERROR;
     }
     CUtensorMap m;
-    const cuuint64_t dims[3] = {(cuuint64_t)g.sy, (cuuint64_t)(g.sz / g.sy), (cuuint64_t)(g.count / g.sz)};
-    const cuuint64_t strides[2] = {(cuuint64_t)(g.sy * esize), (cuuint64_t)(g.sz * esize)};
+    const cuuint64_t dims[3] = {(cuuint64_t)sy, (cuuint64_t)(sz / sy), (cuuint64_t)(count / sz)};
+    const cuuint64_t strides[2] = {(cuuint64_t)(sy * esize), (cuuint64_t)(sz * esize)};
     const cuuint32_t box[3] = {(cuuint32_t)boxx, (cuuint32_t)rows, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(&m, esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
@@ -292,30 +301,81 @@ void sweep_forget_maps(const void* pool_base, size_t pool_bytes)
 
 bool sweep_supported(const NodalGeom& g) { return g.nu[0] >= 16 && g.nu[1] >= 4 && g.nu[2] >= 4; }
 
+static int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// z chunking: a whole number of waves of resident CTAs, chunks of at least 16 planes
+template <typename T, int MODE, bool ISO>
+static int z_chunks(const NodalGeom& g, int xy_tiles)
+{
+    static int resident = 0;
+    if (!resident) {
+        using C = SweepCfg<T>;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_nodal_sweep<T, MODE, ISO>, C::TX * C::TY, 0) !=
+                cudaSuccess ||
+            resident < 1)
+            resident = 1;
+    }
+    const int slots = resident * sm_count();
+    const int max_chunks = (g.nu[2] + 15) / 16;
+    int best = 1;
+    double best_eff = 0.0;
+    for (int nz = 1; nz <= max_chunks; ++nz) {
+        const int kchunk = (g.nu[2] + nz - 1) / nz;
+        const int nzc = (g.nu[2] + kchunk - 1) / kchunk;
+        const long long ctas = (long long)xy_tiles * nzc;
+        const long long waves = (ctas + slots - 1) / slots;
+        // efficiency: useful CTA slots over occupied ones, discounted by the 2 warm-up planes per chunk
+        const double eff = (double)ctas / (double)(waves * slots) * (double)kchunk / (double)(kchunk + 2);
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = nzc;
+        }
+    }
+    return best;
+}
+
+template <typename T, int MODE, bool ISO>
+static void launch_sweep(const CUtensorMap& mx, const CUtensorMap& ms, const CUtensorMap& mb, const NodalGeom& g,
+                         T* out, double omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
+{
+    using C = SweepCfg<T>;
+    const int tx = (g.nu[0] + C::TX - 1) / C::TX, ty = (g.nu[1] + C::TY - 1) / C::TY;
+    const int nz = z_chunks<T, MODE, ISO>(g, tx * ty);
+    const int kchunk = (g.nu[2] + nz - 1) / nz;
+    dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
+    k_nodal_sweep<T, MODE, ISO><<<grid, dim3(C::TX, C::TY), 0, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
+}
+
 template <typename T>
 int nodal_sweep(const NodalGeom& g, int mode, const T* s, const T* x, const T* b, T* out, double omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
     using S = SweepShape<T>;
     CUtensorMap mx, ms, mb;
-    int rc = make_map(x, sizeof(T), g, S::BX, SW_TY + 2, &mx);
-    if (!rc) rc = make_map(s, sizeof(T), g, S::BX, SW_TY + 1, &ms);
-    if (!rc) rc = make_map(b, sizeof(T), g, S::BX, SW_TY, &mb);
+    int rc = make_tensor_map(x, sizeof(T), g.sy, g.sz, g.count, S::BX, S::TY + 2, &mx);
+    if (!rc) rc = make_tensor_map(s, sizeof(T), g.sy, g.sz, g.count, S::BX, S::TY + 1, &ms);
+    if (!rc) rc = make_tensor_map(b, sizeof(T), g.sy, g.sz, g.count, S::BX, S::TY, &mb);
     if (rc) return rc;
-    const int nzc = (g.nu[2] + 63) / 64;
-    const int kchunk = (g.nu[2] + nzc - 1) / nzc;
-    dim3 grid((g.nu[0] + SW_TX - 1) / SW_TX, (g.nu[1] + SW_TY - 1) / SW_TY, (g.nu[2] + kchunk - 1) / kchunk);
-    dim3 block(SW_TX, SW_TY);
     if (mode == 0) {
         if (g.iso)
-            k_nodal_sweep<T, 0, true><<<grid, block, 0, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
+            launch_sweep<T, 0, true>(mx, ms, mb, g, out, omega, err, norm, st);
         else
-            k_nodal_sweep<T, 0, false><<<grid, block, 0, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
+            launch_sweep<T, 0, false>(mx, ms, mb, g, out, omega, err, norm, st);
     } else {
         if (g.iso)
-            k_nodal_sweep<T, 1, true><<<grid, block, 0, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
+            launch_sweep<T, 1, true>(mx, ms, mb, g, out, omega, err, norm, st);
         else
-            k_nodal_sweep<T, 1, false><<<grid, block, 0, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
+            launch_sweep<T, 1, false>(mx, ms, mb, g, out, omega, err, norm, st);
     }
     return GBP_OK;
 }
