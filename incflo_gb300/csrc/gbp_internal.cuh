@@ -56,9 +56,15 @@ struct CellGeom {
     double h[3];
 };
 
+// x position of index 0 in a padded row: 4 elements, so that node/cell 0 starts a 16-byte (FP32) /
+// 32-byte (FP64) boundary and even-indexed pairs can be stored as one vector; index -1 (the ghost)
+// sits at position 3. Rows hold positions 0 .. n+5 rounded up to a multiple of 8 elements.
+constexpr int kOX = 4;
+inline int padded_row(int n) { return round_up(n + kOX + 2, 8); }
+
 __host__ __device__ inline long long pidx(long long sy, long long sz, int i, int j, int k)
 {
-    return (long long)(i + 1) + sy * (long long)(j + 1) + sz * (long long)(k + 1);
+    return (long long)(i + kOX) + sy * (long long)(j + 1) + sz * (long long)(k + 1);
 }
 
 // Positions in the padded box that alias unique node i of a direction with n cells.
@@ -85,16 +91,36 @@ __device__ __forceinline__ int cell_aliases(int i, int n, int per, int out[3])
     return m;
 }
 
+// candidate c (0..3) of the padded positions aliasing unique node i, or kNoAlias
+constexpr int kNoAlias = -1000;
+__device__ __forceinline__ int node_alias_cand(int i, int n, int per, int c)
+{
+    if (c == 0) return i;
+    if (!per) return kNoAlias;
+    if (c == 1) return i == 0 ? n : kNoAlias;
+    if (c == 2) return i == 1 ? n + 1 : kNoAlias;
+    return i == n - 1 ? -1 : kNoAlias;
+}
+
 template <typename T>
 __device__ __forceinline__ void store_node(T* a, const NodalGeom& g, int i, int j, int k, T v)
 {
-    int xs[3], ys[3], zs[3];
-    int nx = node_aliases(i, g.n[0], g.per[0], xs);
-    int ny = node_aliases(j, g.n[1], g.per[1], ys);
-    int nz = node_aliases(k, g.n[2], g.per[2], zs);
-    for (int c = 0; c < nz; ++c)
-        for (int b = 0; b < ny; ++b)
-            for (int q = 0; q < nx; ++q) a[pidx(g.sy, g.sz, xs[q], ys[b], zs[c])] = v;
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        const int kk = node_alias_cand(k, g.n[2], g.per[2], c);
+        if (kk == kNoAlias) continue;
+#pragma unroll 1
+        for (int b = 0; b < 4; ++b) {
+            const int jj = node_alias_cand(j, g.n[1], g.per[1], b);
+            if (jj == kNoAlias) continue;
+#pragma unroll 1
+            for (int q = 0; q < 4; ++q) {
+                const int ii = node_alias_cand(i, g.n[0], g.per[0], q);
+                if (ii == kNoAlias) continue;
+                a[pidx(g.sy, g.sz, ii, jj, kk)] = v;
+            }
+        }
+    }
 }
 
 template <typename T>

@@ -21,7 +21,7 @@ static CellGeom make_cgeom(const int n[3], const double h[3], const int per[3], 
         g.dhi[d] = per[d] ? 0 : dhi[d];
         g.h[d] = h[d];
     }
-    const long long P0 = round_up(n[0] + 2, 8);
+    const long long P0 = padded_row(n[0]);
     g.sy = P0;
     g.sz = P0 * (long long)(n[1] + 2);
     g.count = g.sz * (long long)(n[2] + 2);

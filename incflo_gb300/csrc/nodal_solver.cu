@@ -73,7 +73,7 @@ static NodalGeom make_geom(const int n[3], const double h[3], const int per[3], 
         g.dhi[d] = per[d] ? 0 : dhi[d];
         g.h[d] = h[d];
     }
-    const long long P0 = round_up(n[0] + 3, 8);
+    const long long P0 = padded_row(n[0]);
     g.sy = P0;
     g.sz = P0 * (long long)(n[1] + 3);
     g.count = g.sz * (long long)(n[2] + 3);

@@ -1,19 +1,19 @@
 // Level sweeps of the nodal operator staged through shared memory by TMA.
 //
-// A CTA owns a 32 x TY column of nodes in (x, y) and marches up a chunk of z planes. Per plane it
-// needs x on plane k+1 with a one-node halo, sigma on cell plane k with a one-cell halo and b on
-// plane k; one elected thread brings these in with three cp.async.bulk.tensor loads that complete
-// on one mbarrier per pipeline slot (NS slots, prefetch distance NS). Planes k-1 and k of the 3x3
-// neighbourhood and cell plane k-1 stay in registers, so each node reads 9 + 4 + 1 values from
-// shared memory and each array is read from HBM once (halos come from L2).
+// A CTA owns a column of nodes in (x, y) and marches up a chunk of z planes. Per plane it needs x on
+// plane k+1 with a one-node halo, sigma on cell plane k with a one-cell halo and b on plane k; one
+// elected thread brings these in with three cp.async.bulk.tensor loads that complete on one
+// mbarrier per pipeline slot (NS slots, prefetch distance NS). Planes k-1 and k of each thread's
+// neighbourhood window and cell plane k-1 stay in registers, so every array is read from HBM once
+// per sweep (halos come from L2) and each node reads only plane k+1 from shared memory.
 //
-// FP32 sweeps are HBM-bound: 32 x 16 tiles and 4 slots keep ~60 KB per SM in flight, and the z
-// chunking is chosen so the grid is a whole number of waves of resident CTAs. FP64 sweeps are
-// bound by the FP64 issue rate of GB300, so their tile is smaller (32 x 8, 3 slots).
+// FP32 sweeps (HBM-bound): a thread owns two x-adjacent nodes, a CTA 64 x 16 nodes, 4 slots, and
+// the z chunking is chosen so the grid is a whole number of waves of resident CTAs. FP64 sweeps
+// (FP64-issue-bound on GB300): one node per thread, 32 x 8 nodes per CTA, 3 slots.
 //
-// Boundary handling follows the padded layout of gbp_internal.cuh: a TMA box may start at the
-// ghost row/plane (-1) and run past the padded end (zero fill); tile x origins are multiples of 32
-// nodes, so every box starts on a 16-byte boundary of its row (padded index x0 = node x0 - 1).
+// Padded layout (gbp_internal.cuh): node / cell q of a row sits at position q + 4. Every x box
+// starts at position x0 (node x0 - 4), a multiple of 32 elements, so it is 16-byte aligned; a box
+// may start at the ghost row / plane -1 and run past the padded end (zero fill).
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -28,100 +28,164 @@
 
 namespace gbp {
 
+constexpr int round16(int bytes) { return (bytes + 15) / 16 * 16; }
+constexpr int round128(int bytes) { return (bytes + 127) / 128 * 128; }
+
+// Tile shapes. NX = nodes per CTA row, TY = rows, NPT = nodes per thread (x-adjacent).
 template <typename T>
 struct SweepCfg;
 template <>
 struct SweepCfg<float> {
-    static constexpr int TX = 32, TY = 16, NS = 4;
+    static constexpr int NX = 64, TY = 16, NS = 4, NPT = 2;
 };
 template <>
 struct SweepCfg<double> {
-    static constexpr int TX = 32, TY = 8, NS = 3;
+    static constexpr int NX = 32, TY = 8, NS = 3, NPT = 1;
 };
 
 template <typename T>
 struct SweepShape {
-    static constexpr int TX = SweepCfg<T>::TX, TY = SweepCfg<T>::TY, NS = SweepCfg<T>::NS;
-    static constexpr int BX = (((TX + 2) * (int)sizeof(T) + 15) / 16 * 16) / (int)sizeof(T);
-    static constexpr int XB = (TY + 2) * BX * (int)sizeof(T);
-    static constexpr int SB = (TY + 1) * BX * (int)sizeof(T);
-    static constexpr int BB = TY * BX * (int)sizeof(T);
+    using C = SweepCfg<T>;
+    static constexpr int NX = C::NX, TY = C::TY, NS = C::NS, NPT = C::NPT;
+    static constexpr int THREADS = (NX / NPT) * TY;
+    static constexpr int ES = (int)sizeof(T);
+    // x box: nodes x0-4 .. x0+NX (smem column of node q: q - x0 + 4)
+    static constexpr int BXX = round16((NX + 5) * ES) / ES;
+    // sigma box: cells x0-4 .. x0+NX-1 (column of cell c: c - x0 + 4)
+    static constexpr int BXS = round16((NX + 4) * ES) / ES;
+    // b box: nodes x0 .. x0+NX-1 (column of node q: q - x0)
+    static constexpr int BXB = NX;
+    static constexpr int XB = (TY + 2) * BXX * ES;
+    static constexpr int SB = (TY + 1) * BXS * ES;
+    static constexpr int BB = TY * BXB * ES;
     static constexpr int XO = 0;
-    static constexpr int SO = (XB + 127) / 128 * 128;
-    static constexpr int BO = SO + (SB + 127) / 128 * 128;
-    static constexpr int STAGE = BO + (BB + 127) / 128 * 128;
+    static constexpr int SO = round128(XB);
+    static constexpr int BO = SO + round128(SB);
+    static constexpr int STAGE = BO + round128(BB);
+    static constexpr int SMEM = NS * STAGE;
     static constexpr uint32_t TX_BYTES = (uint32_t)(XB + SB + BB);
 };
 
-__device__ __forceinline__ bool has_alias(const NodalGeom& g, int i, int j, int k)
+__device__ __forceinline__ bool alias_k(const NodalGeom& g, int k) { return g.per[2] && (k <= 1 || k == g.n[2] - 1); }
+__device__ __forceinline__ bool alias_xy(const NodalGeom& g, int i, int j)
 {
-    return (g.per[0] && (i <= 1 || i == g.n[0] - 1)) || (g.per[1] && (j <= 1 || j == g.n[1] - 1)) ||
-           (g.per[2] && (k <= 1 || k == g.n[2] - 1));
+    return (g.per[0] && (i <= 1 || i == g.n[0] - 1)) || (g.per[1] && (j <= 1 || j == g.n[1] - 1));
 }
-
-// One cell layer of (A x)_i from the register planes: Pn = plane k, Pd = the layer's far plane
-// (k-1 or k+1), sg = sigma of the layer's 2x2 cells; accumulates into acc and the sigma sum.
-template <typename T, bool ISO>
-__device__ __forceinline__ void layer(const T (&Pn)[3][3], const T (&Pd)[3][3], const T (&sg)[2][2], const NodalGeom& g,
-                                      T& acc, T& ssum)
+__device__ __forceinline__ bool dir_xy(const NodalGeom& g, int i, int j)
 {
-    const T xc = Pn[1][1];
+    return (g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) || (g.dhi[1] && j == g.n[1]);
+}
+__device__ __forceinline__ bool dir_k(const NodalGeom& g, int k) { return (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]); }
+
+// (A x) at the node in window column c (FP32). P0/P1/P2: planes k-1, k, k+1 of the window (3 rows x
+// W columns, column q = node i0-1+q); Sb/Sa: sigma of the cell layers below / above (2 rows x W-1,
+// column q = cell i0-1+q). Isotropic form: couplings summed per neighbour with the sigma of every
+// cell that contains both nodes (edge-diagonal pairs, corners single), differences to the centre.
+template <int W, bool ISO>
+__device__ __forceinline__ float apply32(const float (&P0)[3][W], const float (&P1)[3][W], const float (&P2)[3][W],
+                                         const float (&Sb)[2][W - 1], const float (&Sa)[2][W - 1], int c,
+                                         const float (&K)[8], float& ssum)
+{
+    const float xc = P1[1][c];
+    if (ISO) {
+        // pair weights of the cells below / above
+        const float bx0 = Sb[0][c - 1] + Sb[1][c - 1], bx1 = Sb[0][c] + Sb[1][c];  // x-edge pairs
+        const float by0 = Sb[0][c - 1] + Sb[0][c], by1 = Sb[1][c - 1] + Sb[1][c];  // y-edge pairs
+        const float ax0 = Sa[0][c - 1] + Sa[1][c - 1], ax1 = Sa[0][c] + Sa[1][c];
+        const float ay0 = Sa[0][c - 1] + Sa[0][c], ay1 = Sa[1][c - 1] + Sa[1][c];
+        ssum = (bx0 + bx1) + (ax0 + ax1);
+        float acc;
+        // in-plane face diagonals: both layers
+        acc = (Sb[0][c - 1] + Sa[0][c - 1]) * (P1[0][c - 1] - xc);
+        acc = fmaf(Sb[0][c] + Sa[0][c], P1[0][c + 1] - xc, acc);
+        acc = fmaf(Sb[1][c - 1] + Sa[1][c - 1], P1[2][c - 1] - xc, acc);
+        acc = fmaf(Sb[1][c] + Sa[1][c], P1[2][c + 1] - xc, acc);
+        // plane k-1: x/y edge neighbours (two cells each) and corners
+        acc = fmaf(bx0, P0[1][c - 1] - xc, acc);
+        acc = fmaf(bx1, P0[1][c + 1] - xc, acc);
+        acc = fmaf(by0, P0[0][c] - xc, acc);
+        acc = fmaf(by1, P0[2][c] - xc, acc);
+        acc = fmaf(Sb[0][c - 1], P0[0][c - 1] - xc, acc);
+        acc = fmaf(Sb[0][c], P0[0][c + 1] - xc, acc);
+        acc = fmaf(Sb[1][c - 1], P0[2][c - 1] - xc, acc);
+        acc = fmaf(Sb[1][c], P0[2][c + 1] - xc, acc);
+        // plane k+1
+        acc = fmaf(ax0, P2[1][c - 1] - xc, acc);
+        acc = fmaf(ax1, P2[1][c + 1] - xc, acc);
+        acc = fmaf(ay0, P2[0][c] - xc, acc);
+        acc = fmaf(ay1, P2[2][c] - xc, acc);
+        acc = fmaf(Sa[0][c - 1], P2[0][c - 1] - xc, acc);
+        acc = fmaf(Sa[0][c], P2[0][c + 1] - xc, acc);
+        acc = fmaf(Sa[1][c - 1], P2[2][c - 1] - xc, acc);
+        acc = fmaf(Sa[1][c], P2[2][c + 1] - xc, acc);
+        return K[3] * acc;
+    } else {
+        float acc = 0.f;
+        ssum = 0.f;
 #pragma unroll
-    for (int cy = 0; cy < 2; ++cy)
+        for (int cz = 0; cz < 2; ++cz)
 #pragma unroll
-        for (int cx = 0; cx < 2; ++cx) {
-            const int ox = cx ? 2 : 0, oy = cy ? 2 : 0;
-            const T s = sg[cy][cx];
-            ssum += s;
-            if (ISO) {
-                if constexpr (sizeof(T) == 8) {
-                    const T S = (Pn[oy][ox] + Pd[1][ox]) + (Pd[oy][1] + Pd[oy][ox]);
-                    acc = fma(s, S, acc);
-                } else {
-                    const T S = ((Pn[oy][ox] - xc) + (Pd[1][ox] - xc)) + ((Pd[oy][1] - xc) + (Pd[oy][ox] - xc));
-                    acc = fmaf(s, S, acc);
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                for (int cx = 0; cx < 2; ++cx) {
+                    const float s = cz ? Sa[cy][c - 1 + cx] : Sb[cy][c - 1 + cx];
+                    const int ox = cx ? c + 1 : c - 1, oy = cy ? 2 : 0;
+                    const float(&Pd)[3][W] = cz ? P2 : P0;
+                    ssum += s;
+                    const float t = K[1] * (P1[1][ox] - xc) + K[2] * (P1[oy][c] - xc) + K[4] * (Pd[1][c] - xc) +
+                                    K[3] * (P1[oy][ox] - xc) + K[5] * (Pd[1][ox] - xc) + K[6] * (Pd[oy][c] - xc) +
+                                    K[7] * (Pd[oy][ox] - xc);
+                    acc = fmaf(s, t, acc);
                 }
-            } else {
-                const T t = (T)g.K[1] * (Pn[1][ox] - xc) + (T)g.K[2] * (Pn[oy][1] - xc) + (T)g.K[4] * (Pd[1][1] - xc) +
-                            (T)g.K[3] * (Pn[oy][ox] - xc) + (T)g.K[5] * (Pd[1][ox] - xc) +
-                            (T)g.K[6] * (Pd[oy][1] - xc) + (T)g.K[7] * (Pd[oy][ox] - xc);
-                acc += s * t;
-            }
-        }
+        return acc;
+    }
 }
 
-template <typename T, int MODE, bool ISO>
-__global__ void __launch_bounds__(SweepCfg<T>::TX* SweepCfg<T>::TY)
-    k_nodal_sweep(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
-                  const __grid_constant__ CUtensorMap mb, NodalGeom g, T* __restrict__ out, T omega, int kchunk,
-                  unsigned* err, unsigned long long* norm)
+template <typename T>
+__device__ __forceinline__ void store_with_aliases(T* out, const NodalGeom& g, int i, int j, int k, T v, bool alias)
 {
-    using S = SweepShape<T>;
-    constexpr int BX = S::BX, TX = S::TX, NS = S::NS;
-    __shared__ __align__(1024) unsigned char smem[NS * S::STAGE];
+    if (alias)
+        store_node(out, g, i, j, k, v);
+    else
+        out[pidx(g.sy, g.sz, i, j, k)] = v;
+}
+
+// ------------------------------------------------------------------------------------ FP32
+template <int MODE, bool ISO>
+__global__ void __launch_bounds__(SweepShape<float>::THREADS)
+    k_sweep32(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
+              const __grid_constant__ CUtensorMap mb, NodalGeom g, float* __restrict__ out, float omega, int kchunk,
+              unsigned* err, unsigned long long* norm)
+{
+    using S = SweepShape<float>;
+    constexpr int NS = S::NS, W = 4;
+    extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t bar[NS];
     __shared__ int abort_flag;
 
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + TX * ty;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * S::TY;
+    const int tid = tx + 32 * ty;
+    const int x0 = blockIdx.x * S::NX, y0 = blockIdx.y * S::TY;
     const int kbeg = blockIdx.z * kchunk;
     const int kend = min(kbeg + kchunk, g.nu[2]);
     const int nsteps = kend - kbeg + 2;
-    const int i = x0 + tx, j = y0 + ty;
-    const bool active = i < g.nu[0] && j < g.nu[1];
+    const int i0 = x0 + 2 * tx, j = y0 + ty;
+    const bool actA = i0 < g.nu[0] && j < g.nu[1], actB = i0 + 1 < g.nu[0] && j < g.nu[1];
+    const bool dirA = dir_xy(g, i0, j), dirB = dir_xy(g, i0 + 1, j);
+    const bool aliA = alias_xy(g, i0, j), aliB = alias_xy(g, i0 + 1, j);
+    float K[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) K[q] = (float)g.K[q];
 
     auto issue = [&](int s) {
         const int slot = s % NS;
         unsigned char* base = smem + slot * S::STAGE;
         const int k = kbeg - 2 + s;
         mbar_arrive_expect_tx(&bar[slot], S::TX_BYTES);
-        // padded coordinates: node / cell index q sits at q + 1
-        tma_load_3d(base + S::XO, &mx, &bar[slot], x0, y0, k + 2);      // x nodes y0-1.., plane k+1
-        tma_load_3d(base + S::SO, &ms, &bar[slot], x0, y0, k + 1);      // sigma cells y0-1.., plane k
-        tma_load_3d(base + S::BO, &mb, &bar[slot], x0, y0 + 1, k + 1);  // b nodes y0.., plane k
+        tma_load_3d(base + S::XO, &mx, &bar[slot], x0, y0, k + 2);          // x: rows j-1.., plane k+1
+        tma_load_3d(base + S::SO, &ms, &bar[slot], x0, y0, k + 1);          // sigma: cell rows j-1.., plane k
+        tma_load_3d(base + S::BO, &mb, &bar[slot], x0 + kOX, y0 + 1, k + 1);  // b: rows j.., plane k
     };
-
     if (tid == 0) {
         for (int q = 0; q < NS; ++q) mbar_init(&bar[q], 1);
         mbar_fence_init();
@@ -131,12 +195,171 @@ __global__ void __launch_bounds__(SweepCfg<T>::TX* SweepCfg<T>::TY)
     if (tid == 0)
         for (int s = 0; s < NS && s < nsteps; ++s) issue(s);
 
-    T P0[3][3], P1[3][3], P2[3][3], S0[2][2], S1[2][2];
+    float P0[3][W], P1[3][W], P2[3][W], Sb[2][W - 1], Sa[2][W - 1];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int q = 0; q < W; ++q) P0[r][q] = P1[r][q] = 0.f;
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int q = 0; q < W - 1; ++q) Sb[r][q] = 0.f;
+    float nmax = 0.f;
+
+    for (int s = 0; s < nsteps; ++s) {
+        const int slot = s % NS;
+        const unsigned char* base = smem + slot * S::STAGE;
+        if (!mbar_wait_bounded(&bar[slot], (uint32_t)((s / NS) & 1), err)) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) break;
+        const float* sx = reinterpret_cast<const float*>(base + S::XO) + 2 * tx + 3;  // node i0-1
+        const float* ss = reinterpret_cast<const float*>(base + S::SO) + 2 * tx + 3;  // cell i0-1
+        const float* sb = reinterpret_cast<const float*>(base + S::BO) + 2 * tx;      // node i0
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const float* row = sx + (ty + r) * S::BXX;
+            P2[r][0] = row[0];
+            const float2 m = *reinterpret_cast<const float2*>(row + 1);
+            P2[r][1] = m.x;
+            P2[r][2] = m.y;
+            P2[r][3] = row[3];
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const float* row = ss + (ty + r) * S::BXS;
+            Sa[r][0] = row[0];
+            const float2 m = *reinterpret_cast<const float2*>(row + 1);
+            Sa[r][1] = m.x;
+            Sa[r][2] = m.y;
+        }
+        const float2 bv = *reinterpret_cast<const float2*>(sb + ty * S::BXB);
+        const int k = kbeg - 2 + s;
+        if (s >= 2 && actA) {
+            const bool dk = dir_k(g, k);
+            float vA = 0.f, vB = 0.f;
+            float ssA, ssB;
+            const float axA = apply32<W, ISO>(P0, P1, P2, Sb, Sa, 1, K, ssA);
+            const float axB = apply32<W, ISO>(P0, P1, P2, Sb, Sa, 2, K, ssB);
+            if (MODE == 0) {
+                vA = fmaf(omega * (bv.x - axA), __frcp_rn(K[0] * ssA), P1[1][1]);
+                vB = fmaf(omega * (bv.y - axB), __frcp_rn(K[0] * ssB), P1[1][2]);
+            } else {
+                vA = bv.x - axA;
+                vB = bv.y - axB;
+            }
+            if (dk || dirA) vA = 0.f;
+            if (dk || dirB) vB = 0.f;
+            if (MODE == 1 && norm) {
+                nmax = fmaxf(nmax, fabsf(vA) * (float)node_inv_volume(g, i0, j, k));
+                if (actB) nmax = fmaxf(nmax, fabsf(vB) * (float)node_inv_volume(g, i0 + 1, j, k));
+                if (vA != vA || vB != vB) nmax = __int_as_float(0x7fc00000);
+            }
+            const bool ak = alias_k(g, k);
+            if (actB && !(ak || aliA || aliB)) {
+                *reinterpret_cast<float2*>(out + pidx(g.sy, g.sz, i0, j, k)) = make_float2(vA, vB);
+            } else {
+                store_with_aliases(out, g, i0, j, k, vA, ak || aliA);
+                if (actB) store_with_aliases(out, g, i0 + 1, j, k, vB, ak || aliB);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int q = 0; q < W; ++q) {
+                P0[r][q] = P1[r][q];
+                P1[r][q] = P2[r][q];
+            }
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int q = 0; q < W - 1; ++q) Sb[r][q] = Sa[r][q];
+        __syncthreads();  // every thread is done with this slot
+        if (tid == 0 && s + NS < nsteps) {
+            fence_proxy_async();
+            issue(s + NS);
+        }
+    }
+    if (abort_flag && tid == 0)
+        for (int q = 0; q < NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
+    if (MODE == 1 && norm) {
+        const double m = block_max((double)nmax);
+        if (tid == 0) atomic_max_nonneg(norm, m);
+    }
+}
+
+// ------------------------------------------------------------------------------------ FP64
+// One cell layer of (A x)_i from the register planes: Pn = plane k, Pd = the layer's far plane
+// (k-1 or k+1), sg = sigma of the layer's 2x2 cells; accumulates into acc and the sigma sum.
+template <bool ISO>
+__device__ __forceinline__ void layer64(const double (&Pn)[3][3], const double (&Pd)[3][3], const double (&sg)[2][2],
+                                        const NodalGeom& g, double& acc, double& ssum)
+{
+    const double xc = Pn[1][1];
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+        for (int cx = 0; cx < 2; ++cx) {
+            const int ox = cx ? 2 : 0, oy = cy ? 2 : 0;
+            const double s = sg[cy][cx];
+            ssum += s;
+            if (ISO) {
+                const double S = (Pn[oy][ox] + Pd[1][ox]) + (Pd[oy][1] + Pd[oy][ox]);
+                acc = fma(s, S, acc);
+            } else {
+                const double t = g.K[1] * (Pn[1][ox] - xc) + g.K[2] * (Pn[oy][1] - xc) + g.K[4] * (Pd[1][1] - xc) +
+                                 g.K[3] * (Pn[oy][ox] - xc) + g.K[5] * (Pd[1][ox] - xc) +
+                                 g.K[6] * (Pd[oy][1] - xc) + g.K[7] * (Pd[oy][ox] - xc);
+                acc = fma(s, t, acc);
+            }
+        }
+}
+
+template <int MODE, bool ISO>
+__global__ void __launch_bounds__(SweepShape<double>::THREADS)
+    k_sweep64(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
+              const __grid_constant__ CUtensorMap mb, NodalGeom g, double* __restrict__ out, double omega, int kchunk,
+              unsigned* err, unsigned long long* norm)
+{
+    using S = SweepShape<double>;
+    constexpr int NS = S::NS;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bar[NS];
+    __shared__ int abort_flag;
+
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = tx + 32 * ty;
+    const int x0 = blockIdx.x * S::NX, y0 = blockIdx.y * S::TY;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(kbeg + kchunk, g.nu[2]);
+    const int nsteps = kend - kbeg + 2;
+    const int i = x0 + tx, j = y0 + ty;
+    const bool active = i < g.nu[0] && j < g.nu[1];
+    const bool dxy = dir_xy(g, i, j), axy = alias_xy(g, i, j);
+
+    auto issue = [&](int s) {
+        const int slot = s % NS;
+        unsigned char* base = smem + slot * S::STAGE;
+        const int k = kbeg - 2 + s;
+        mbar_arrive_expect_tx(&bar[slot], S::TX_BYTES);
+        tma_load_3d(base + S::XO, &mx, &bar[slot], x0, y0, k + 2);
+        tma_load_3d(base + S::SO, &ms, &bar[slot], x0, y0, k + 1);
+        tma_load_3d(base + S::BO, &mb, &bar[slot], x0 + kOX, y0 + 1, k + 1);
+    };
+    if (tid == 0) {
+        for (int q = 0; q < NS; ++q) mbar_init(&bar[q], 1);
+        mbar_fence_init();
+        abort_flag = 0;
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int s = 0; s < NS && s < nsteps; ++s) issue(s);
+
+    double P0[3][3], P1[3][3], P2[3][3], S0[2][2], S1[2][2];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) P0[a][b] = P1[a][b] = T(0);
-    S0[0][0] = S0[0][1] = S0[1][0] = S0[1][1] = T(0);
+        for (int b = 0; b < 3; ++b) P0[a][b] = P1[a][b] = 0.0;
+    S0[0][0] = S0[0][1] = S0[1][0] = S0[1][1] = 0.0;
     double nmax = 0.0;
 
     for (int s = 0; s < nsteps; ++s) {
@@ -145,55 +368,38 @@ __global__ void __launch_bounds__(SweepCfg<T>::TX* SweepCfg<T>::TY)
         if (!mbar_wait_bounded(&bar[slot], (uint32_t)((s / NS) & 1), err)) abort_flag = 1;
         __syncthreads();
         if (abort_flag) break;
-        const T* sx = reinterpret_cast<const T*>(base + S::XO);
-        const T* ss = reinterpret_cast<const T*>(base + S::SO);
-        const T* sb = reinterpret_cast<const T*>(base + S::BO);
+        const double* sx = reinterpret_cast<const double*>(base + S::XO) + tx + 3;
+        const double* ss = reinterpret_cast<const double*>(base + S::SO) + tx + 3;
+        const double* sb = reinterpret_cast<const double*>(base + S::BO) + tx;
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) P2[a][b] = sx[(ty + a) * BX + tx + b];
+            for (int b = 0; b < 3; ++b) P2[a][b] = sx[(ty + a) * S::BXX + b];
 #pragma unroll
         for (int a = 0; a < 2; ++a)
 #pragma unroll
-            for (int b = 0; b < 2; ++b) S1[a][b] = ss[(ty + a) * BX + tx + b];
-        const T bv = sb[ty * BX + tx + 1];
+            for (int b = 0; b < 2; ++b) S1[a][b] = ss[(ty + a) * S::BXS + b];
+        const double bv = sb[ty * S::BXB];
         const int k = kbeg - 2 + s;
         if (s >= 2 && active) {
-            T v = T(0);
-            if (!node_is_dirichlet(g, i, j, k)) {
-                T acc = T(0), ssum = T(0);
-                layer<T, ISO>(P1, P0, S0, g, acc, ssum);
-                layer<T, ISO>(P1, P2, S1, g, acc, ssum);
-                const T xc = P1[1][1];
-                T ax;
-                if (ISO) {
-                    if constexpr (sizeof(T) == 8)
-                        ax = (T)g.K[3] * fma(-4.0 * xc, ssum, acc);
-                    else
-                        ax = (T)g.K[3] * acc;
-                } else {
-                    ax = acc;
-                }
-                const T diag = (T)g.K[0] * ssum;
+            double v = 0.0;
+            if (!(dxy || dir_k(g, k))) {
+                double acc = 0.0, ssum = 0.0;
+                layer64<ISO>(P1, P0, S0, g, acc, ssum);
+                layer64<ISO>(P1, P2, S1, g, acc, ssum);
+                const double xc = P1[1][1];
+                const double ax = ISO ? g.K[3] * fma(-4.0 * xc, ssum, acc) : acc;
+                const double diag = g.K[0] * ssum;
                 if (MODE == 0) {
-                    T rd;
-                    if constexpr (sizeof(T) == 8) {
-                        const double ad = fabs(diag);
-                        rd = (ad > 1e-30 && ad < 1e30) ? (double)__frcp_rn((float)diag) : 1.0 / diag;
-                    } else {
-                        rd = __frcp_rn(diag);
-                    }
+                    const double ad = fabs(diag);
+                    const double rd = (ad > 1e-30 && ad < 1e30) ? (double)__frcp_rn((float)diag) : 1.0 / diag;
                     v = xc + omega * (bv - ax) * rd;
                 } else {
                     v = bv - ax;
-                    if (norm) nmax = nanmax(nmax, fabs((double)v) * node_inv_volume(g, i, j, k));
+                    if (norm) nmax = nanmax(nmax, fabs(v) * node_inv_volume(g, i, j, k));
                 }
             }
-            const long long p = pidx(g.sy, g.sz, i, j, k);
-            if (has_alias(g, i, j, k))
-                store_node(out, g, i, j, k, v);
-            else
-                out[p] = v;
+            store_with_aliases(out, g, i, j, k, v, axy || alias_k(g, k));
         }
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -206,16 +412,14 @@ __global__ void __launch_bounds__(SweepCfg<T>::TX* SweepCfg<T>::TY)
         for (int a = 0; a < 2; ++a)
 #pragma unroll
             for (int b = 0; b < 2; ++b) S0[a][b] = S1[a][b];
-        __syncthreads();  // every thread is done with this slot
+        __syncthreads();
         if (tid == 0 && s + NS < nsteps) {
             fence_proxy_async();
             issue(s + NS);
         }
     }
-    if (abort_flag && tid == 0) {
-        // drain the loads still in flight (bounded) before the CTA's shared memory goes away
+    if (abort_flag && tid == 0)
         for (int q = 0; q < NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
-    }
     if (MODE == 1 && norm) {
         nmax = block_max(nmax);
         if (tid == 0) atomic_max_nonneg(norm, nmax);
@@ -314,17 +518,8 @@ static int sm_count()
 }
 
 // z chunking: a whole number of waves of resident CTAs, chunks of at least 16 planes
-template <typename T, int MODE, bool ISO>
-static int z_chunks(const NodalGeom& g, int xy_tiles)
+static int z_chunks(const NodalGeom& g, int xy_tiles, int resident)
 {
-    static int resident = 0;
-    if (!resident) {
-        using C = SweepCfg<T>;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_nodal_sweep<T, MODE, ISO>, C::TX * C::TY, 0) !=
-                cudaSuccess ||
-            resident < 1)
-            resident = 1;
-    }
     const int slots = resident * sm_count();
     const int max_chunks = (g.nu[2] + 15) / 16;
     int best = 1;
@@ -334,7 +529,6 @@ static int z_chunks(const NodalGeom& g, int xy_tiles)
         const int nzc = (g.nu[2] + kchunk - 1) / kchunk;
         const long long ctas = (long long)xy_tiles * nzc;
         const long long waves = (ctas + slots - 1) / slots;
-        // efficiency: useful CTA slots over occupied ones, discounted by the 2 warm-up planes per chunk
         const double eff = (double)ctas / (double)(waves * slots) * (double)kchunk / (double)(kchunk + 2);
         if (eff > best_eff + 1e-9) {
             best_eff = eff;
@@ -345,15 +539,35 @@ static int z_chunks(const NodalGeom& g, int xy_tiles)
 }
 
 template <typename T, int MODE, bool ISO>
-static void launch_sweep(const CUtensorMap& mx, const CUtensorMap& ms, const CUtensorMap& mb, const NodalGeom& g,
-                         T* out, double omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
+struct SweepKernel;
+template <int MODE, bool ISO>
+struct SweepKernel<float, MODE, ISO> {
+    static constexpr auto fn = k_sweep32<MODE, ISO>;
+};
+template <int MODE, bool ISO>
+struct SweepKernel<double, MODE, ISO> {
+    static constexpr auto fn = k_sweep64<MODE, ISO>;
+};
+
+template <typename T, int MODE, bool ISO>
+static int launch_sweep(const CUtensorMap& mx, const CUtensorMap& ms, const CUtensorMap& mb, const NodalGeom& g,
+                        T* out, double omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
-    using C = SweepCfg<T>;
-    const int tx = (g.nu[0] + C::TX - 1) / C::TX, ty = (g.nu[1] + C::TY - 1) / C::TY;
-    const int nz = z_chunks<T, MODE, ISO>(g, tx * ty);
+    using S = SweepShape<T>;
+    auto kern = SweepKernel<T, MODE, ISO>::fn;
+    static int resident = 0;
+    if (!resident) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, S::THREADS, S::SMEM) != cudaSuccess ||
+            resident < 1)
+            resident = 1;
+    }
+    const int tx = (g.nu[0] + S::NX - 1) / S::NX, ty = (g.nu[1] + S::TY - 1) / S::TY;
+    const int nz = z_chunks(g, tx * ty, resident);
     const int kchunk = (g.nu[2] + nz - 1) / nz;
     dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
-    k_nodal_sweep<T, MODE, ISO><<<grid, dim3(C::TX, C::TY), 0, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
+    kern<<<grid, dim3(32, S::TY), S::SMEM, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
+    return GBP_OK;
 }
 
 template <typename T>
@@ -362,22 +576,15 @@ int nodal_sweep(const NodalGeom& g, int mode, const T* s, const T* x, const T* b
 {
     using S = SweepShape<T>;
     CUtensorMap mx, ms, mb;
-    int rc = make_tensor_map(x, sizeof(T), g.sy, g.sz, g.count, S::BX, S::TY + 2, &mx);
-    if (!rc) rc = make_tensor_map(s, sizeof(T), g.sy, g.sz, g.count, S::BX, S::TY + 1, &ms);
-    if (!rc) rc = make_tensor_map(b, sizeof(T), g.sy, g.sz, g.count, S::BX, S::TY, &mb);
+    int rc = make_tensor_map(x, sizeof(T), g.sy, g.sz, g.count, S::BXX, S::TY + 2, &mx);
+    if (!rc) rc = make_tensor_map(s, sizeof(T), g.sy, g.sz, g.count, S::BXS, S::TY + 1, &ms);
+    if (!rc) rc = make_tensor_map(b, sizeof(T), g.sy, g.sz, g.count, S::BXB, S::TY, &mb);
     if (rc) return rc;
-    if (mode == 0) {
-        if (g.iso)
-            launch_sweep<T, 0, true>(mx, ms, mb, g, out, omega, err, norm, st);
-        else
-            launch_sweep<T, 0, false>(mx, ms, mb, g, out, omega, err, norm, st);
-    } else {
-        if (g.iso)
-            launch_sweep<T, 1, true>(mx, ms, mb, g, out, omega, err, norm, st);
-        else
-            launch_sweep<T, 1, false>(mx, ms, mb, g, out, omega, err, norm, st);
-    }
-    return GBP_OK;
+    if (mode == 0)
+        return g.iso ? launch_sweep<T, 0, true>(mx, ms, mb, g, out, omega, err, norm, st)
+                     : launch_sweep<T, 0, false>(mx, ms, mb, g, out, omega, err, norm, st);
+    return g.iso ? launch_sweep<T, 1, true>(mx, ms, mb, g, out, omega, err, norm, st)
+                 : launch_sweep<T, 1, false>(mx, ms, mb, g, out, omega, err, norm, st);
 }
 
 template int nodal_sweep<double>(const NodalGeom&, int, const double*, const double*, const double*, double*, double,
