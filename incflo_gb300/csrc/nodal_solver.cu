@@ -421,7 +421,7 @@ struct LevelBufs<float> {
 template <typename T>
 void NodalSolver::jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, cudaStream_t s_)
 {
-    if (use_tma && sweep_supported(g)) {
+    if (use_tma && sweep_supported(g, (int)sizeof(T))) {
         int rc = nodal_sweep<T>(g, 0, s, x, b, out, opt.omega, derr, nullptr, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else {
@@ -433,7 +433,7 @@ template <typename T>
 void NodalSolver::resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
                         cudaStream_t s_)
 {
-    if (use_tma && sweep_supported(g)) {
+    if (use_tma && sweep_supported(g, (int)sizeof(T))) {
         int rc = nodal_sweep<T>(g, 1, s, x, b, r, opt.omega, derr, norm, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else {

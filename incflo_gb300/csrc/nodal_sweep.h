@@ -1,6 +1,8 @@
-// TMA-staged level sweeps of the nodal operator (nodal_sweep.cu).
+// TMA-staged level sweeps of the nodal operator (nodal_sweep64.cu: FP64 sweep, tensor maps and launch
+// helpers; nodal_sweep32.cu: FP32 producer/consumer sweep).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "gbp_internal.cuh"
@@ -12,7 +14,16 @@ namespace gbp {
 template <typename T>
 int nodal_sweep(const NodalGeom& g, int mode, const T* s, const T* x, const T* b, T* out, double omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st);
-bool sweep_supported(const NodalGeom& g);
+// whether the TMA sweep handles this level for elements of esize bytes (else the plain kernels do)
+bool sweep_supported(const NodalGeom& g, int esize);
 void sweep_forget_maps(const void* pool_base, size_t pool_bytes);
+
+// helpers shared by the two sweep files
+int make_tensor_map(const void* base, int esize, long long sy, long long sz, long long count, int boxx, int rows,
+                    CUtensorMap* out);
+int sweep_z_chunks(const NodalGeom& g, int xy_tiles, int resident);
+int sm_count_cached();
+int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
+                unsigned* err, unsigned long long* norm, cudaStream_t st);
 
 }  // namespace gbp

@@ -7,9 +7,8 @@
 // neighbourhood window and cell plane k-1 stay in registers, so every array is read from HBM once
 // per sweep (halos come from L2) and each node reads only plane k+1 from shared memory.
 //
-// FP32 sweeps (HBM-bound): a thread owns two x-adjacent nodes, a CTA 64 x 16 nodes, 4 slots, and
-// the z chunking is chosen so the grid is a whole number of waves of resident CTAs. FP64 sweeps
-// (FP64-issue-bound on GB300): one node per thread, 32 x 8 nodes per CTA, 3 slots.
+// This file holds the FP64 sweep (FP64-issue-bound on GB300: one node per thread, 32 x 8 nodes per
+// CTA, 3 slots), the tensor-map cache and the launch helpers; the FP32 sweep is in nodal_sweep32.cu.
 //
 // Padded layout (gbp_internal.cuh): node / cell q of a row sits at position q + 4. Every x box
 // starts at position x0 (node x0 - 4), a multiple of 32 elements, so it is 16-byte aligned; a box
@@ -77,70 +76,6 @@ __device__ __forceinline__ bool dir_xy(const NodalGeom& g, int i, int j)
 }
 __device__ __forceinline__ bool dir_k(const NodalGeom& g, int k) { return (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]); }
 
-// (A x) at the node in window column c (FP32). P0/P1/P2: planes k-1, k, k+1 of the window (3 rows x
-// W columns, column q = node i0-1+q); Sb/Sa: sigma of the cell layers below / above (2 rows x W-1,
-// column q = cell i0-1+q). Isotropic form: couplings summed per neighbour with the sigma of every
-// cell that contains both nodes (edge-diagonal pairs, corners single), differences to the centre.
-template <int W, bool ISO>
-__device__ __forceinline__ float apply32(const float (&P0)[3][W], const float (&P1)[3][W], const float (&P2)[3][W],
-                                         const float (&Sb)[2][W - 1], const float (&Sa)[2][W - 1], int c,
-                                         const float (&K)[8], float& ssum)
-{
-    const float xc = P1[1][c];
-    if (ISO) {
-        // pair weights of the cells below / above
-        const float bx0 = Sb[0][c - 1] + Sb[1][c - 1], bx1 = Sb[0][c] + Sb[1][c];  // x-edge pairs
-        const float by0 = Sb[0][c - 1] + Sb[0][c], by1 = Sb[1][c - 1] + Sb[1][c];  // y-edge pairs
-        const float ax0 = Sa[0][c - 1] + Sa[1][c - 1], ax1 = Sa[0][c] + Sa[1][c];
-        const float ay0 = Sa[0][c - 1] + Sa[0][c], ay1 = Sa[1][c - 1] + Sa[1][c];
-        ssum = (bx0 + bx1) + (ax0 + ax1);
-        float acc;
-        // in-plane face diagonals: both layers
-        acc = (Sb[0][c - 1] + Sa[0][c - 1]) * (P1[0][c - 1] - xc);
-        acc = fmaf(Sb[0][c] + Sa[0][c], P1[0][c + 1] - xc, acc);
-        acc = fmaf(Sb[1][c - 1] + Sa[1][c - 1], P1[2][c - 1] - xc, acc);
-        acc = fmaf(Sb[1][c] + Sa[1][c], P1[2][c + 1] - xc, acc);
-        // plane k-1: x/y edge neighbours (two cells each) and corners
-        acc = fmaf(bx0, P0[1][c - 1] - xc, acc);
-        acc = fmaf(bx1, P0[1][c + 1] - xc, acc);
-        acc = fmaf(by0, P0[0][c] - xc, acc);
-        acc = fmaf(by1, P0[2][c] - xc, acc);
-        acc = fmaf(Sb[0][c - 1], P0[0][c - 1] - xc, acc);
-        acc = fmaf(Sb[0][c], P0[0][c + 1] - xc, acc);
-        acc = fmaf(Sb[1][c - 1], P0[2][c - 1] - xc, acc);
-        acc = fmaf(Sb[1][c], P0[2][c + 1] - xc, acc);
-        // plane k+1
-        acc = fmaf(ax0, P2[1][c - 1] - xc, acc);
-        acc = fmaf(ax1, P2[1][c + 1] - xc, acc);
-        acc = fmaf(ay0, P2[0][c] - xc, acc);
-        acc = fmaf(ay1, P2[2][c] - xc, acc);
-        acc = fmaf(Sa[0][c - 1], P2[0][c - 1] - xc, acc);
-        acc = fmaf(Sa[0][c], P2[0][c + 1] - xc, acc);
-        acc = fmaf(Sa[1][c - 1], P2[2][c - 1] - xc, acc);
-        acc = fmaf(Sa[1][c], P2[2][c + 1] - xc, acc);
-        return K[3] * acc;
-    } else {
-        float acc = 0.f;
-        ssum = 0.f;
-#pragma unroll
-        for (int cz = 0; cz < 2; ++cz)
-#pragma unroll
-            for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-                for (int cx = 0; cx < 2; ++cx) {
-                    const float s = cz ? Sa[cy][c - 1 + cx] : Sb[cy][c - 1 + cx];
-                    const int ox = cx ? c + 1 : c - 1, oy = cy ? 2 : 0;
-                    const float(&Pd)[3][W] = cz ? P2 : P0;
-                    ssum += s;
-                    const float t = K[1] * (P1[1][ox] - xc) + K[2] * (P1[oy][c] - xc) + K[4] * (Pd[1][c] - xc) +
-                                    K[3] * (P1[oy][ox] - xc) + K[5] * (Pd[1][ox] - xc) + K[6] * (Pd[oy][c] - xc) +
-                                    K[7] * (Pd[oy][ox] - xc);
-                    acc = fmaf(s, t, acc);
-                }
-        return acc;
-    }
-}
-
 template <typename T>
 __device__ __forceinline__ void store_with_aliases(T* out, const NodalGeom& g, int i, int j, int k, T v, bool alias)
 {
@@ -150,143 +85,10 @@ __device__ __forceinline__ void store_with_aliases(T* out, const NodalGeom& g, i
         out[pidx(g.sy, g.sz, i, j, k)] = v;
 }
 
-// ------------------------------------------------------------------------------------ FP32
-template <int MODE, bool ISO>
-__global__ void __launch_bounds__(SweepShape<float>::THREADS)
-    k_sweep32(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
-              const __grid_constant__ CUtensorMap mb, NodalGeom g, float* __restrict__ out, float omega, int kchunk,
-              unsigned* err, unsigned long long* norm)
-{
-    using S = SweepShape<float>;
-    constexpr int NS = S::NS, W = 4;
-    extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t bar[NS];
-    __shared__ int abort_flag;
-
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + 32 * ty;
-    const int x0 = blockIdx.x * S::NX, y0 = blockIdx.y * S::TY;
-    const int kbeg = blockIdx.z * kchunk;
-    const int kend = min(kbeg + kchunk, g.nu[2]);
-    const int nsteps = kend - kbeg + 2;
-    const int i0 = x0 + 2 * tx, j = y0 + ty;
-    const bool actA = i0 < g.nu[0] && j < g.nu[1], actB = i0 + 1 < g.nu[0] && j < g.nu[1];
-    const bool dirA = dir_xy(g, i0, j), dirB = dir_xy(g, i0 + 1, j);
-    const bool aliA = alias_xy(g, i0, j), aliB = alias_xy(g, i0 + 1, j);
-    float K[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) K[q] = (float)g.K[q];
-
-    auto issue = [&](int s) {
-        const int slot = s % NS;
-        unsigned char* base = smem + slot * S::STAGE;
-        const int k = kbeg - 2 + s;
-        mbar_arrive_expect_tx(&bar[slot], S::TX_BYTES);
-        tma_load_3d(base + S::XO, &mx, &bar[slot], x0, y0, k + 2);          // x: rows j-1.., plane k+1
-        tma_load_3d(base + S::SO, &ms, &bar[slot], x0, y0, k + 1);          // sigma: cell rows j-1.., plane k
-        tma_load_3d(base + S::BO, &mb, &bar[slot], x0 + kOX, y0 + 1, k + 1);  // b: rows j.., plane k
-    };
-    if (tid == 0) {
-        for (int q = 0; q < NS; ++q) mbar_init(&bar[q], 1);
-        mbar_fence_init();
-        abort_flag = 0;
-    }
-    __syncthreads();
-    if (tid == 0)
-        for (int s = 0; s < NS && s < nsteps; ++s) issue(s);
-
-    float P0[3][W], P1[3][W], P2[3][W], Sb[2][W - 1], Sa[2][W - 1];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int q = 0; q < W; ++q) P0[r][q] = P1[r][q] = 0.f;
-#pragma unroll
-    for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int q = 0; q < W - 1; ++q) Sb[r][q] = 0.f;
-    float nmax = 0.f;
-
-    for (int s = 0; s < nsteps; ++s) {
-        const int slot = s % NS;
-        const unsigned char* base = smem + slot * S::STAGE;
-        if (!mbar_wait_bounded(&bar[slot], (uint32_t)((s / NS) & 1), err)) abort_flag = 1;
-        __syncthreads();
-        if (abort_flag) break;
-        const float* sx = reinterpret_cast<const float*>(base + S::XO) + 2 * tx + 3;  // node i0-1
-        const float* ss = reinterpret_cast<const float*>(base + S::SO) + 2 * tx + 3;  // cell i0-1
-        const float* sb = reinterpret_cast<const float*>(base + S::BO) + 2 * tx;      // node i0
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            const float* row = sx + (ty + r) * S::BXX;
-            P2[r][0] = row[0];
-            const float2 m = *reinterpret_cast<const float2*>(row + 1);
-            P2[r][1] = m.x;
-            P2[r][2] = m.y;
-            P2[r][3] = row[3];
-        }
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const float* row = ss + (ty + r) * S::BXS;
-            Sa[r][0] = row[0];
-            const float2 m = *reinterpret_cast<const float2*>(row + 1);
-            Sa[r][1] = m.x;
-            Sa[r][2] = m.y;
-        }
-        const float2 bv = *reinterpret_cast<const float2*>(sb + ty * S::BXB);
-        const int k = kbeg - 2 + s;
-        if (s >= 2 && actA) {
-            const bool dk = dir_k(g, k);
-            float vA = 0.f, vB = 0.f;
-            float ssA, ssB;
-            const float axA = apply32<W, ISO>(P0, P1, P2, Sb, Sa, 1, K, ssA);
-            const float axB = apply32<W, ISO>(P0, P1, P2, Sb, Sa, 2, K, ssB);
-            if (MODE == 0) {
-                vA = fmaf(omega * (bv.x - axA), __frcp_rn(K[0] * ssA), P1[1][1]);
-                vB = fmaf(omega * (bv.y - axB), __frcp_rn(K[0] * ssB), P1[1][2]);
-            } else {
-                vA = bv.x - axA;
-                vB = bv.y - axB;
-            }
-            if (dk || dirA) vA = 0.f;
-            if (dk || dirB) vB = 0.f;
-            if (MODE == 1 && norm) {
-                nmax = fmaxf(nmax, fabsf(vA) * (float)node_inv_volume(g, i0, j, k));
-                if (actB) nmax = fmaxf(nmax, fabsf(vB) * (float)node_inv_volume(g, i0 + 1, j, k));
-                if (vA != vA || vB != vB) nmax = __int_as_float(0x7fc00000);
-            }
-            const bool ak = alias_k(g, k);
-            if (actB && !(ak || aliA || aliB)) {
-                *reinterpret_cast<float2*>(out + pidx(g.sy, g.sz, i0, j, k)) = make_float2(vA, vB);
-            } else {
-                store_with_aliases(out, g, i0, j, k, vA, ak || aliA);
-                if (actB) store_with_aliases(out, g, i0 + 1, j, k, vB, ak || aliB);
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int q = 0; q < W; ++q) {
-                P0[r][q] = P1[r][q];
-                P1[r][q] = P2[r][q];
-            }
-#pragma unroll
-        for (int r = 0; r < 2; ++r)
-#pragma unroll
-            for (int q = 0; q < W - 1; ++q) Sb[r][q] = Sa[r][q];
-        __syncthreads();  // every thread is done with this slot
-        if (tid == 0 && s + NS < nsteps) {
-            fence_proxy_async();
-            issue(s + NS);
-        }
-    }
-    if (abort_flag && tid == 0)
-        for (int q = 0; q < NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
-    if (MODE == 1 && norm) {
-        const double m = block_max((double)nmax);
-        if (tid == 0) atomic_max_nonneg(norm, m);
-    }
-}
-
+// (A x) at the node in window column c (FP32). P0/P1/P2: planes k-1, k, k+1 of the window (3 rows x
+// W columns, column q = node i0-1+q); Sb/Sa: sigma of the cell layers below / above (2 rows x W-1,
+// column q = cell i0-1+q). Isotropic form: couplings summed per neighbour with the sigma of every
+// cell that contains both nodes (edge-diagonal pairs, corners single), differences to the centre.
 // ------------------------------------------------------------------------------------ FP64
 // One cell layer of (A x)_i from the register planes: Pn = plane k, Pd = the layer's far plane
 // (k-1 or k+1), sg = sigma of the layer's 2x2 cells; accumulates into acc and the sigma sum.
@@ -503,9 +305,15 @@ void sweep_forget_maps(const void* pool_base, size_t pool_bytes)
     }
 }
 
-bool sweep_supported(const NodalGeom& g) { return g.nu[0] >= 16 && g.nu[1] >= 4 && g.nu[2] >= 4; }
+bool sweep_supported(const NodalGeom& g, int esize)
+{
+    if (esize == 4) return g.iso && g.nu[0] >= 32 && g.nu[1] >= 4 && g.nu[2] >= 4;
+    return g.nu[0] >= 16 && g.nu[1] >= 4 && g.nu[2] >= 4;
+}
 
-static int sm_count()
+int sm_count_cached();
+
+int sm_count_cached()
 {
     static int n = 0;
     if (!n) {
@@ -518,9 +326,9 @@ static int sm_count()
 }
 
 // z chunking: a whole number of waves of resident CTAs, chunks of at least 16 planes
-static int z_chunks(const NodalGeom& g, int xy_tiles, int resident)
+int sweep_z_chunks(const NodalGeom& g, int xy_tiles, int resident)
 {
-    const int slots = resident * sm_count();
+    const int slots = resident * sm_count_cached();
     const int max_chunks = (g.nu[2] + 15) / 16;
     int best = 1;
     double best_eff = 0.0;
@@ -541,10 +349,6 @@ static int z_chunks(const NodalGeom& g, int xy_tiles, int resident)
 template <typename T, int MODE, bool ISO>
 struct SweepKernel;
 template <int MODE, bool ISO>
-struct SweepKernel<float, MODE, ISO> {
-    static constexpr auto fn = k_sweep32<MODE, ISO>;
-};
-template <int MODE, bool ISO>
 struct SweepKernel<double, MODE, ISO> {
     static constexpr auto fn = k_sweep64<MODE, ISO>;
 };
@@ -563,33 +367,34 @@ static int launch_sweep(const CUtensorMap& mx, const CUtensorMap& ms, const CUte
             resident = 1;
     }
     const int tx = (g.nu[0] + S::NX - 1) / S::NX, ty = (g.nu[1] + S::TY - 1) / S::TY;
-    const int nz = z_chunks(g, tx * ty, resident);
+    const int nz = sweep_z_chunks(g, tx * ty, resident);
     const int kchunk = (g.nu[2] + nz - 1) / nz;
     dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
     kern<<<grid, dim3(32, S::TY), S::SMEM, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
     return GBP_OK;
 }
 
-template <typename T>
-int nodal_sweep(const NodalGeom& g, int mode, const T* s, const T* x, const T* b, T* out, double omega,
-                unsigned* err, unsigned long long* norm, cudaStream_t st)
+template <>
+int nodal_sweep<double>(const NodalGeom& g, int mode, const double* s, const double* x, const double* b, double* out,
+                        double omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
-    using S = SweepShape<T>;
+    using S = SweepShape<double>;
     CUtensorMap mx, ms, mb;
-    int rc = make_tensor_map(x, sizeof(T), g.sy, g.sz, g.count, S::BXX, S::TY + 2, &mx);
-    if (!rc) rc = make_tensor_map(s, sizeof(T), g.sy, g.sz, g.count, S::BXS, S::TY + 1, &ms);
-    if (!rc) rc = make_tensor_map(b, sizeof(T), g.sy, g.sz, g.count, S::BXB, S::TY, &mb);
+    int rc = make_tensor_map(x, sizeof(double), g.sy, g.sz, g.count, S::BXX, S::TY + 2, &mx);
+    if (!rc) rc = make_tensor_map(s, sizeof(double), g.sy, g.sz, g.count, S::BXS, S::TY + 1, &ms);
+    if (!rc) rc = make_tensor_map(b, sizeof(double), g.sy, g.sz, g.count, S::BXB, S::TY, &mb);
     if (rc) return rc;
     if (mode == 0)
-        return g.iso ? launch_sweep<T, 0, true>(mx, ms, mb, g, out, omega, err, norm, st)
-                     : launch_sweep<T, 0, false>(mx, ms, mb, g, out, omega, err, norm, st);
-    return g.iso ? launch_sweep<T, 1, true>(mx, ms, mb, g, out, omega, err, norm, st)
-                 : launch_sweep<T, 1, false>(mx, ms, mb, g, out, omega, err, norm, st);
+        return g.iso ? launch_sweep<double, 0, true>(mx, ms, mb, g, out, omega, err, norm, st)
+                     : launch_sweep<double, 0, false>(mx, ms, mb, g, out, omega, err, norm, st);
+    return g.iso ? launch_sweep<double, 1, true>(mx, ms, mb, g, out, omega, err, norm, st)
+                 : launch_sweep<double, 1, false>(mx, ms, mb, g, out, omega, err, norm, st);
 }
 
-template int nodal_sweep<double>(const NodalGeom&, int, const double*, const double*, const double*, double*, double,
-                                 unsigned*, unsigned long long*, cudaStream_t);
-template int nodal_sweep<float>(const NodalGeom&, int, const float*, const float*, const float*, float*, double,
-                                unsigned*, unsigned long long*, cudaStream_t);
-
+template <>
+int nodal_sweep<float>(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out,
+                       double omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
+{
+    return sweep32_run(g, mode, s, x, b, out, (float)omega, err, norm, st);
+}
 }  // namespace gbp

@@ -89,6 +89,38 @@ def test_plan_create_without_device_fails_cleanly(lib):
     assert rc == A.GBP_NO_DEVICE and not p.value
 
 
+def _build_shim(tmp_path):
+    import shutil
+    import subprocess
+
+    from incflo_gb300.build import LIB
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path / "shim_check"
+    cuda_inc = "/usr/local/cuda/include"
+    cuda_lib = "/usr/local/cuda/lib64"
+    cmd = [cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc,
+           os.path.join(ROOT, "tests", "shim_check.cpp"), LIB, "-L", cuda_lib, "-lcudart",
+           f"-Wl,-rpath,{os.path.dirname(LIB)}", f"-Wl,-rpath,{cuda_lib}", "-o", str(exe)]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+def test_cpp_shim_compiles_and_reports_status(lib, tmp_path):
+    """include/gb_projectors.H compiles as incflo would include it; without a GPU the call
+    surfaces GBP_NO_DEVICE through gb::Error instead of aborting."""
+    import subprocess
+
+    exe = _build_shim(tmp_path)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    if torch.cuda.is_available():
+        assert r.returncode == 0, r.stdout + r.stderr
+    else:
+        assert r.returncode == 3, r.stdout + r.stderr
+
+
 def test_null_arguments_rejected(lib):
     assert lib.gbp_plan_create(None, 0, None, None, None, None, None) == A.GBP_BAD_ARG
     assert lib.gbp_nodal_project(None, None, None, None, 0, None) == A.GBP_BAD_ARG
