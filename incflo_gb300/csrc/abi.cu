@@ -406,6 +406,24 @@ int gbp_nodal_project(gbp_plan* p, gbp_array4* vel, gbp_array4* phi, gbp_array4*
     return p->nodal->project(ra, ca, phi, 0, phi_guess ? phi : nullptr, stats);
 }
 
+int gbp_nodal_divergence(gbp_plan* p, const gbp_array4* vel, int use_inflow, gbp_array4* div_out, double* max_norm)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_nodal_divergence: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    int rc = check_vel(p, vel, use_inflow != 0);
+    if (rc) return rc;
+    if (div_out && div_out->data && (rc = check_nodes(p, div_out, "div_out"))) return rc;
+    RhsArgs ra{};
+    CorrArgs ca{};
+    fill_rhs_corr(p, ra, ca);
+    ra.vel = *vel;
+    if (!use_inflow)
+        for (int d = 0; d < 3; ++d) ra.inflow_lo[d] = ra.inflow_hi[d] = 0;
+    return p->nodal->divergence(ra, div_out, max_norm);
+}
+
 int gbp_apply_nodal_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
                                double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
                                double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats)

@@ -58,9 +58,10 @@ struct CellGeom {
 
 // x position of index 0 in a padded row: 4 elements, so that node/cell 0 starts a 16-byte (FP32) /
 // 32-byte (FP64) boundary and even-indexed pairs can be stored as one vector; index -1 (the ghost)
-// sits at position 3. Rows hold positions 0 .. n+5 rounded up to a multiple of 8 elements.
+// sits at position 3. Rows hold positions 0 .. n+6 (one spare past the last ghost, so a pair read
+// starting at the last node stays inside its row) rounded up to a multiple of 8 elements.
 constexpr int kOX = 4;
-inline int padded_row(int n) { return round_up(n + kOX + 2, 8); }
+inline int padded_row(int n) { return round_up(n + kOX + 3, 8); }
 
 __host__ __device__ inline long long pidx(long long sy, long long sz, int i, int j, int k)
 {

@@ -694,12 +694,54 @@ __global__ void k_nodal_store_phi(NodalGeom g, gbp_array4 out, const double* __r
     *p = accumulate ? *p + v : v;
 }
 
+// div(i,j,k) = -g_i / V_i (strong-form nodal divergence) on all nodes 0..n; the periodic duplicate
+// node n reads its unique node 0
+__global__ void k_nodal_store_div(NodalGeom g, gbp_array4 out, const double* __restrict__ b)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int n0 = g.n[0] + 1, n1 = g.n[1] + 1, n2 = g.n[2] + 1;
+    const long long nxy = (long long)n0 * n1;
+    if (t >= nxy * n2) return;
+    const int k = (int)(t / nxy);
+    const long long rem = t - (long long)k * nxy;
+    const int j = (int)(rem / n0);
+    const int i = (int)(rem - (long long)j * n0);
+    const int iu = (g.per[0] && i == g.n[0]) ? 0 : i;
+    const int ju = (g.per[1] && j == g.n[1]) ? 0 : j;
+    const int ku = (g.per[2] && k == g.n[2]) ? 0 : k;
+    *a4p(out, i, j, k, 0) = -b[pidx(g.sy, g.sz, iu, ju, ku)] * node_inv_volume(g, iu, ju, ku);
+}
+
+void nodal_store_div(const NodalGeom& g, const gbp_array4& out, const double* b, cudaStream_t st)
+{
+    const long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
+    k_nodal_store_div<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, out, b);
+}
+
 __global__ void k_nodal_load_phi(NodalGeom g, gbp_array4 in, double* __restrict__ phi)
 {
     int i, j, k;
     if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
     const double v = node_is_dirichlet(g, i, j, k) ? 0.0 : a4(in, i, j, k, 0);
     store_node(phi, g, i, j, k, v);
+}
+
+// Streaming reference for the sweep rooflines: out = a + b + c over whole padded arrays (three reads,
+// one write, perfectly coalesced float4) -- the best any level sweep of the same arrays can do.
+__global__ void __launch_bounds__(256) k_stream_triad(const float4* __restrict__ a, const float4* __restrict__ b,
+                                                      const float4* __restrict__ c, float4* __restrict__ out, long long n4)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n4; t += (long long)gridDim.x * blockDim.x) {
+        const float4 x = __ldg(a + t), y = __ldg(b + t), z = __ldg(c + t);
+        out[t] = make_float4(x.x + y.x + z.x, x.y + y.y + z.y, x.z + y.z + z.z, x.w + y.w + z.w);
+    }
+}
+
+void stream_triad(const float* a, const float* b, const float* c, float* out, long long n, cudaStream_t st)
+{
+    const long long n4 = n / 4;
+    k_stream_triad<<<152 * 8, 256, 0, st>>>(reinterpret_cast<const float4*>(a), reinterpret_cast<const float4*>(b),
+                                            reinterpret_cast<const float4*>(c), reinterpret_cast<float4*>(out), n4);
 }
 
 // ---------------------------------------------------------------------------------------

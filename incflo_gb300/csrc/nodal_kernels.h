@@ -68,5 +68,9 @@ void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale,
 void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st);
 void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* phi, int accumulate, cudaStream_t st);
 void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaStream_t st);
+// streaming reference: out = a + b + c over n floats (n a multiple of 4, 16-byte aligned arrays)
+void stream_triad(const float* a, const float* b, const float* c, float* out, long long n, cudaStream_t st);
+// strong-form divergence -b_i / V_i into a nodal array (all nodes 0..n)
+void nodal_store_div(const NodalGeom& g, const gbp_array4& out, const double* b, cudaStream_t st);
 
 }  // namespace gbp

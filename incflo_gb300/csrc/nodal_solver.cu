@@ -696,18 +696,19 @@ namespace gbp {
 
 int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
 {
-    if (which < 0 || which > 3 || reps < 1 || !sigma_ready) {
-        set_error("time_kernel: which must be 0..3, reps >= 1, and sigma must be set");
+    if (which < 0 || which > 5 || reps < 1 || !sigma_ready) {
+        set_error("time_kernel: which must be 0..5, reps >= 1, and sigma must be set");
         return GBP_BAD_ARG;
     }
     const NodalLevel& l0 = L[0];
     const NodalGeom& g = l0.g;
-    const bool f32 = which & 1;
+    const bool f32 = (which & 1) || which >= 4;
     const double w = f32 ? 4.0 : 8.0;
     const double nn = (double)g.nu[0] * g.nu[1] * g.nu[2];
     const double nc = (double)g.n[0] * g.n[1] * g.n[2];
-    // Jacobi: x, b read + x written per node, sigma read per cell; residual: x, b read, r written
-    *bytes = w * (3.0 * nn + nc);
+    // Jacobi: x, b read + x written per node, sigma read per cell; residual: x, b read, r written;
+    // triad (which 4): three padded arrays read, one written
+    *bytes = which == 4 ? 4.0 * 4.0 * (double)g.count : w * (3.0 * nn + nc);
     if (f32) nodal_to_f32(g, res, l0.b32, scale32, st);
     GBP_CUDA(cudaEventRecord(ev0, st));
     for (int r = 0; r < reps; ++r) {
@@ -715,7 +716,12 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
         case 0: jacobi<double>(g, l0.s64, (r & 1) ? l0.t64 : l0.x64, res, (r & 1) ? l0.x64 : l0.t64, st); break;
         case 1: jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, st); break;
         case 2: resid<double>(g, l0.s64, phi, rhs0, l0.r64, nullptr, st); break;
-        default: resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st); break;
+        case 3: resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st); break;
+        case 4: stream_triad(l0.x32, l0.s32, l0.b32, l0.r32, g.count, st); break;
+        default:
+            nodal_jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, opt.omega,
+                                false, st);
+            break;
         }
     }
     GBP_CUDA(cudaEventRecord(ev1, st));
@@ -723,6 +729,23 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
     float t = 0.f;
     GBP_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
     *ms = t / reps;
+    return GBP_OK;
+}
+
+int NodalSolver::divergence(const RhsArgs& rhs, const gbp_array4* out, double* max_norm)
+{
+    const NodalLevel& l0 = L[0];
+    GBP_CUDA(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), st));
+    nodal_rhs(l0.g, rhs, l0.s64, rhs0, singular ? partials : nullptr, st);
+    if (singular)
+        nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, 1, nodal_rhs_partials(l0.g), dnorm, st);
+    else
+        nodal_norm(l0.g, rhs0, dnorm, st);
+    if (out && out->data) nodal_store_div(l0.g, *out, rhs0, st);
+    GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    GBP_CUDA(cudaGetLastError());
+    if (max_norm) *max_norm = bits_to_double(hnorm[0]);
     return GBP_OK;
 }
 

@@ -47,6 +47,9 @@ public:
     int project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
                 const gbp_array4* phi_guess, gbp_stats* stats);
 
+    // nodal divergence of vel as the projection sees it (consistent for singular systems), strong form
+    int divergence(const RhsArgs& rhs, const gbp_array4* out, double* max_norm);
+
     const NodalGeom& geom0() const { return L[0].g; }
     size_t device_bytes() const { return pool.bytes; }
     cudaStream_t stream() const { return st; }

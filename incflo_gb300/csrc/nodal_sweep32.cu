@@ -17,6 +17,7 @@
 // nodes (x/y-edge pairs, in-plane diagonals below+above, corners single), always as differences to
 // the centre so FP32 rounding scales with the local variation of x, not with x itself.
 #include <cuda.h>
+#include <stdlib.h>
 
 #include "gbp_internal.cuh"
 #include "nodal_sweep.h"
@@ -278,11 +279,347 @@ int launch(const CUtensorMap& mx, const CUtensorMap& ms, const CUtensorMap& mb, 
     return GBP_OK;
 }
 
+// ----------------------------------------------------------------------------------------------
+// Register-queue z-march without shared memory: one node per thread, 32 x 8 threads per CTA, all
+// loads through the read-only path (the 3x3 windows of neighbouring threads overlap in L1). High
+// occupancy (no shared memory, few registers) hides the latency that the TMA pipeline cannot at
+// one CTA per SM. Same carried-coupling formulation as above; accumulations split in two chains.
+constexpr int ZX = 32, ZY = 8;
+
+struct Win1 {
+    float p[3][3];
+};
+struct Lay1 {
+    float s[2][2];
+};
+
+__device__ __forceinline__ void far1(const Win1& far, const Lay1& L, float xc, float& acc0, float& acc1, float& ssum)
+{
+    const float ax0 = L.s[0][0] + L.s[1][0], ax1 = L.s[0][1] + L.s[1][1];
+    const float ay0 = L.s[0][0] + L.s[0][1], ay1 = L.s[1][0] + L.s[1][1];
+    ssum = ax0 + ax1;
+    acc0 = fmaf(ax0, far.p[1][0] - xc, acc0);
+    acc1 = fmaf(ax1, far.p[1][2] - xc, acc1);
+    acc0 = fmaf(ay0, far.p[0][1] - xc, acc0);
+    acc1 = fmaf(ay1, far.p[2][1] - xc, acc1);
+    acc0 = fmaf(L.s[0][0], far.p[0][0] - xc, acc0);
+    acc1 = fmaf(L.s[0][1], far.p[0][2] - xc, acc1);
+    acc0 = fmaf(L.s[1][0], far.p[2][0] - xc, acc0);
+    acc1 = fmaf(L.s[1][1], far.p[2][2] - xc, acc1);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(ZX* ZY) k_zmarch32(NodalGeom g, const float* __restrict__ sg, const float* __restrict__ xin,
+                                                     const float* __restrict__ bin, float* __restrict__ out, Consts cst,
+                                                     int kchunk, unsigned long long* norm)
+{
+    const int i = blockIdx.x * ZX + threadIdx.x, j = blockIdx.y * ZY + threadIdx.y;
+    const int kbeg = blockIdx.z * kchunk;
+    // inactive threads march nothing but still take part in the block reduction below
+    const int kend = (i < g.nu[0] && j < g.nu[1]) ? min(kbeg + kchunk, g.nu[2]) : kbeg;
+    const long long sy = g.sy, sz = g.sz;
+    const bool dxy = (g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) || (g.dhi[1] && j == g.n[1]);
+    const bool axy = (g.per[0] && (i <= 1 || i == g.n[0] - 1)) || (g.per[1] && (j <= 1 || j == g.n[1] - 1));
+    // node (i,j,k) at c0 + k*sz; the window of plane q starts at node (i-1, j-1, q); the cell layer q
+    // (between node planes q and q+1) starts at cell (i-1, j-1, q)
+    const long long c0 = pidx(sy, sz, i, j, 0);
+    const float* xw = xin + c0 - 1 - sy;
+    const float* sw = sg + c0 - 1 - sy;
+    auto load_win = [&](int q, Win1& w) {
+        const float* p = xw + (long long)q * sz;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) w.p[r][c] = __ldg(p + r * sy + c);
+    };
+    auto load_lay = [&](int q, Lay1& l) {
+        const float* p = sw + (long long)q * sz;
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) l.s[r][c] = __ldg(p + r * sy + c);
+    };
+    Win1 WA, WB;
+    Lay1 LA, LB;
+    float carry = 0.f, sb = 0.f;
+    if (kend > kbeg) {
+        // prologue: plane kbeg-1 and kbeg, layer kbeg-1, and the coupling of node kbeg to plane kbeg-1
+        load_win(kbeg - 1, WA);
+        load_win(kbeg, WB);
+        load_lay(kbeg - 1, LA);
+        float carry0 = 0.f, carry1 = 0.f;
+        far1(WA, LA, WB.p[1][1], carry0, carry1, sb);
+        carry = carry0 + carry1;
+    }
+    float nmax = 0.f;
+    float* op = out + c0 + (long long)kbeg * sz;
+    const float* bp = bin + c0 + (long long)kbeg * sz;
+
+    // ctr = plane k, nxt <- plane k+1, lb = layer k-1, la <- layer k
+    auto step = [&](Win1& ctr, Win1& nxt, Lay1& lb, Lay1& la, int k) {
+        load_win(k + 1, nxt);
+        load_lay(k, la);
+        const float bv = __ldg(bp);
+        const float xc = ctr.p[1][1];
+        float a0 = carry, a1 = 0.f, sa;
+        // in-plane diagonals (sigma below + above)
+        a0 = fmaf(lb.s[0][0] + la.s[0][0], ctr.p[0][0] - xc, a0);
+        a1 = fmaf(lb.s[0][1] + la.s[0][1], ctr.p[0][2] - xc, a1);
+        a0 = fmaf(lb.s[1][0] + la.s[1][0], ctr.p[2][0] - xc, a0);
+        a1 = fmaf(lb.s[1][1] + la.s[1][1], ctr.p[2][2] - xc, a1);
+        far1(nxt, la, xc, a0, a1, sa);
+        // coupling of node k+1 to this plane through layer k, carried to the next step
+        float n0 = 0.f, n1 = 0.f, dummy;
+        far1(ctr, la, nxt.p[1][1], n0, n1, dummy);
+        const float ax = cst.k3 * (a0 + a1);
+        float v;
+        if (MODE == 0)
+            v = fmaf(cst.omega * (bv - ax), __frcp_rn(cst.k0 * (sb + sa)), xc);
+        else
+            v = bv - ax;
+        if (dxy || (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2])) v = 0.f;
+        if (MODE == 1 && norm) nmax = (v != v || nmax != nmax) ? __int_as_float(0x7fc00000)
+                                                              : fmaxf(nmax, fabsf(v) * (float)node_inv_volume(g, i, j, k));
+        if (axy || (g.per[2] && (k <= 1 || k == g.n[2] - 1)))
+            store_node(out, g, i, j, k, v);
+        else
+            *op = v;
+        op += sz;
+        bp += sz;
+        carry = n0 + n1;
+        sb = sa;
+    };
+    int k = kbeg;
+    for (; k + 1 < kend; k += 2) {
+        step(WB, WA, LA, LB, k);
+        step(WA, WB, LB, LA, k + 1);
+    }
+    if (k < kend) step(WB, WA, LA, LB, k);
+    if (MODE == 1 && norm) {
+        const double m = block_max((double)nmax);
+        if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(norm, m);
+    }
+}
+
+template <int MODE>
+int launch_zmarch(const NodalGeom& g, const float* s, const float* x, const float* b, float* out, float omega,
+                  unsigned long long* norm, cudaStream_t st)
+{
+    static int resident = 0;
+    if (!resident) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_zmarch32<MODE>, ZX * ZY, 0) != cudaSuccess ||
+            resident < 1)
+            resident = 1;
+    }
+    const int tx = (g.nu[0] + ZX - 1) / ZX, ty = (g.nu[1] + ZY - 1) / ZY;
+    const int nz = sweep_z_chunks(g, tx * ty, resident);
+    const int kchunk = (g.nu[2] + nz - 1) / nz;
+    const Consts c{(float)g.K[0], (float)g.K[3], omega};
+    dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
+    k_zmarch32<MODE><<<grid, dim3(ZX, ZY), 0, st>>>(g, s, x, b, out, c, kchunk, norm);
+    return GBP_OK;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Packed-pair z-march: a thread owns two x-adjacent nodes and does all stencil arithmetic in packed
+// FP32x2 (one fma.rn.f32x2 per coupling for both nodes), halving the FP32 instruction count that
+// bounds the scalar variants. The windows of plane k+2 and cell layer k+1 are loaded one step ahead
+// (three-way register rotation, loop unrolled by three) so their latency overlaps the arithmetic.
+constexpr int PX = 32, PY = 8;  // threads; a CTA covers 64 x 8 nodes
+
+struct PWin {
+    float2 c[3];     // rows j-1..j+1: (x[i0], x[i0+1])
+    float l[3], r[3];  // x[i0-1], x[i0+2]
+};
+struct PLay {
+    float2 c[2];  // rows j-1, j: (s[i0], s[i0+1])
+    float l[2];   // s[i0-1]
+};
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 lft(const PWin& w, int r) { return f2(w.l[r], w.c[r].x); }   // node i-1
+__device__ __forceinline__ float2 rgt(const PWin& w, int r) { return f2(w.c[r].y, w.r[r]); }   // node i+1
+__device__ __forceinline__ float2 slo(const PLay& L, int r) { return f2(L.l[r], L.c[r].x); }  // cell i-1
+__device__ __forceinline__ float2 shi(const PLay& L, int r) { return L.c[r]; }                // cell i
+
+// couplings of the centre pair to the far plane through layer L (edge pairs + corners), packed;
+// returns the layer's sigma sum for each node
+__device__ __forceinline__ float2 pfar(const PWin& far, const PLay& L, float2 xc, float2& a0, float2& a1)
+{
+    const float2 s00 = slo(L, 0), s01 = shi(L, 0), s10 = slo(L, 1), s11 = shi(L, 1);
+    const float2 ax0 = __fadd2_rn(s00, s10), ax1 = __fadd2_rn(s01, s11);
+    const float2 ay0 = __fadd2_rn(s00, s01), ay1 = __fadd2_rn(s10, s11);
+    const float2 nxc = f2(-xc.x, -xc.y);
+    a0 = __ffma2_rn(ax0, __fadd2_rn(lft(far, 1), nxc), a0);
+    a1 = __ffma2_rn(ax1, __fadd2_rn(rgt(far, 1), nxc), a1);
+    a0 = __ffma2_rn(ay0, __fadd2_rn(far.c[0], nxc), a0);
+    a1 = __ffma2_rn(ay1, __fadd2_rn(far.c[2], nxc), a1);
+    a0 = __ffma2_rn(s00, __fadd2_rn(lft(far, 0), nxc), a0);
+    a1 = __ffma2_rn(s01, __fadd2_rn(rgt(far, 0), nxc), a1);
+    a0 = __ffma2_rn(s10, __fadd2_rn(lft(far, 2), nxc), a0);
+    a1 = __ffma2_rn(s11, __fadd2_rn(rgt(far, 2), nxc), a1);
+    return __fadd2_rn(ax0, ax1);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(PX* PY) k_zpair32(NodalGeom g, const float* __restrict__ sg, const float* __restrict__ xin,
+                                                    const float* __restrict__ bin, float* __restrict__ out, Consts cst,
+                                                    int kchunk, unsigned long long* norm)
+{
+    const int i0 = 2 * (blockIdx.x * PX + threadIdx.x), j = blockIdx.y * PY + threadIdx.y;
+    const int kbeg = blockIdx.z * kchunk;
+    const bool act = i0 < g.nu[0] && j < g.nu[1];
+    const bool actB = i0 + 1 < g.nu[0];
+    const int kend = act ? min(kbeg + kchunk, g.nu[2]) : kbeg;
+    const long long sy = g.sy, sz = g.sz;
+    const bool dA = (g.dlo[0] && i0 == 0) || (g.dhi[0] && i0 == g.n[0]) || (g.dlo[1] && j == 0) || (g.dhi[1] && j == g.n[1]);
+    const bool dB = !actB || (g.dlo[0] && i0 + 1 == 0) || (g.dhi[0] && i0 + 1 == g.n[0]) || (g.dlo[1] && j == 0) ||
+                    (g.dhi[1] && j == g.n[1]);
+    const bool axy = (g.per[0] && (i0 <= 1 || i0 + 1 >= g.n[0] - 1)) || (g.per[1] && (j <= 1 || j == g.n[1] - 1));
+    const long long c0 = pidx(sy, sz, i0, j, 0);  // node (i0, j, 0); even i0: 8-byte aligned pair
+    const float* xw = xin + c0 - sy;              // node (i0, j-1, 0)
+    const float* sw = sg + c0 - sy;               // cell (i0, j-1, 0)
+    auto load_win = [&](int q, PWin& w) {
+        const float* p = xw + (long long)q * sz;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const float* rp = p + r * sy;
+            w.c[r] = __ldg(reinterpret_cast<const float2*>(rp));
+            w.l[r] = __ldg(rp - 1);
+            w.r[r] = __ldg(rp + 2);
+        }
+    };
+    auto load_lay = [&](int q, PLay& l) {
+        const float* p = sw + (long long)q * sz;
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const float* rp = p + r * sy;
+            l.c[r] = __ldg(reinterpret_cast<const float2*>(rp));
+            l.l[r] = __ldg(rp - 1);
+        }
+    };
+
+    PWin W0, W1, W2;
+    PLay L0, L1, L2;
+    float2 carry = f2(0.f, 0.f), sb = f2(0.f, 0.f);
+    float nmax = 0.f;
+    float* op = out + c0 + (long long)kbeg * sz;
+    const float* bp = bin + c0 + (long long)kbeg * sz;
+    if (kend > kbeg) {
+        load_win(kbeg - 1, W2);  // plane kbeg-1 (temporarily in W2)
+        load_win(kbeg, W0);
+        load_lay(kbeg - 1, L2);
+        float2 a0 = f2(0.f, 0.f), a1 = f2(0.f, 0.f);
+        sb = pfar(W2, L2, W0.c[1], a0, a1);
+        carry = __fadd2_rn(a0, a1);
+        load_lay(kbeg - 1, L0);
+        load_win(kbeg + 1, W1);  // planes beyond the chunk are in the padded box (<= n+1)
+        load_lay(kbeg, L1);
+    }
+    const float2 k3 = f2(cst.k3, cst.k3), k0 = f2(cst.k0, cst.k0), om = f2(cst.omega, cst.omega);
+
+    // ctr = plane k, nxt = plane k+1 (both loaded), pre <- plane k+2; lb = layer k-1, la = layer k, lp <- layer k+1
+    auto step = [&](PWin& ctr, PWin& nxt, PWin& pre, PLay& lb, PLay& la, PLay& lp, int k) {
+        if (k + 1 < kend) {
+            load_win(k + 2, pre);
+            load_lay(k + 1, lp);
+        }
+        const float2 bv = __ldg(reinterpret_cast<const float2*>(bp));
+        const float2 xc = ctr.c[1];
+        const float2 nxc = f2(-xc.x, -xc.y);
+        float2 a0 = carry, a1 = f2(0.f, 0.f);
+        // in-plane face diagonals: sigma below + above
+        a0 = __ffma2_rn(__fadd2_rn(slo(lb, 0), slo(la, 0)), __fadd2_rn(lft(ctr, 0), nxc), a0);
+        a1 = __ffma2_rn(__fadd2_rn(shi(lb, 0), shi(la, 0)), __fadd2_rn(rgt(ctr, 0), nxc), a1);
+        a0 = __ffma2_rn(__fadd2_rn(slo(lb, 1), slo(la, 1)), __fadd2_rn(lft(ctr, 2), nxc), a0);
+        a1 = __ffma2_rn(__fadd2_rn(shi(lb, 1), shi(la, 1)), __fadd2_rn(rgt(ctr, 2), nxc), a1);
+        const float2 sa = pfar(nxt, la, xc, a0, a1);
+        // coupling of node k+1 to this plane through layer k, carried to the next step
+        float2 n0 = f2(0.f, 0.f), n1 = f2(0.f, 0.f);
+        (void)pfar(ctr, la, nxt.c[1], n0, n1);
+        const float2 ax = __fmul2_rn(k3, __fadd2_rn(a0, a1));
+        const float2 rr = __fadd2_rn(bv, f2(-ax.x, -ax.y));
+        float2 v;
+        if (MODE == 0) {
+            const float2 dg = __fmul2_rn(k0, __fadd2_rn(sb, sa));
+            v = __ffma2_rn(__fmul2_rn(om, rr), f2(__frcp_rn(dg.x), __frcp_rn(dg.y)), xc);
+        } else {
+            v = rr;
+        }
+        const bool dk = (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+        if (dk || dA) v.x = 0.f;
+        if (dk || dB) v.y = 0.f;
+        if (MODE == 1 && norm) {
+            const float m = fmaxf(fabsf(v.x) * (float)node_inv_volume(g, i0, j, k),
+                                  actB ? fabsf(v.y) * (float)node_inv_volume(g, i0 + 1, j, k) : 0.f);
+            nmax = (v.x != v.x || v.y != v.y || nmax != nmax) ? __int_as_float(0x7fc00000) : fmaxf(nmax, m);
+        }
+        if (axy || (g.per[2] && (k <= 1 || k == g.n[2] - 1)) || !actB) {
+            store_node(out, g, i0, j, k, v.x);
+            if (actB) store_node(out, g, i0 + 1, j, k, v.y);
+        } else {
+            *reinterpret_cast<float2*>(op) = v;
+        }
+        op += sz;
+        bp += sz;
+        carry = __fadd2_rn(n0, n1);
+        sb = sa;
+    };
+    int k = kbeg;
+    for (; k + 2 < kend; k += 3) {
+        step(W0, W1, W2, L0, L1, L2, k);
+        step(W1, W2, W0, L1, L2, L0, k + 1);
+        step(W2, W0, W1, L2, L0, L1, k + 2);
+    }
+    if (k < kend) step(W0, W1, W2, L0, L1, L2, k);
+    if (k + 1 < kend) step(W1, W2, W0, L1, L2, L0, k + 1);
+    if (MODE == 1 && norm) {
+        const double m = block_max((double)nmax);
+        if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(norm, m);
+    }
+}
+
+template <int MODE>
+int launch_zpair(const NodalGeom& g, const float* s, const float* x, const float* b, float* out, float omega,
+                 unsigned long long* norm, cudaStream_t st)
+{
+    static int resident = 0;
+    if (!resident) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_zpair32<MODE>, PX * PY, 0) != cudaSuccess ||
+            resident < 1)
+            resident = 1;
+    }
+    const int tx = (g.nu[0] + 2 * PX - 1) / (2 * PX), ty = (g.nu[1] + PY - 1) / PY;
+    const int nz = sweep_z_chunks(g, tx * ty, resident);
+    const int kchunk = (g.nu[2] + nz - 1) / nz;
+    const Consts c{(float)g.K[0], (float)g.K[3], omega};
+    dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
+    k_zpair32<MODE><<<grid, dim3(PX, PY), 0, st>>>(g, s, x, b, out, c, kchunk, norm);
+    return GBP_OK;
+}
+
+int sweep_variant()
+{
+    static int v = -1;
+    if (v < 0) {
+        const char* e = getenv("GBP_SWEEP32");
+        // 2: packed-pair z-march (default), 0: scalar z-march, 1: TMA producer/consumer
+        v = !e ? 2 : (e[0] == 't' ? 1 : (e[0] == 's' ? 0 : 2));
+    }
+    return v;
+}
+
 }  // namespace
 
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
+    if (sweep_variant() == 2)
+        return mode == 0 ? launch_zpair<0>(g, s, x, b, out, omega, norm, st)
+                         : launch_zpair<1>(g, s, x, b, out, omega, norm, st);
+    if (sweep_variant() == 0)
+        return mode == 0 ? launch_zmarch<0>(g, s, x, b, out, omega, norm, st)
+                         : launch_zmarch<1>(g, s, x, b, out, omega, norm, st);
     CUtensorMap mx, ms, mb;
     int rc = make_tensor_map(x, 4, g.sy, g.sz, g.count, BXX, TY + 2, &mx);
     if (!rc) rc = make_tensor_map(s, 4, g.sy, g.sz, g.count, BXS, TY + 1, &ms);

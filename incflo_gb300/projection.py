@@ -243,6 +243,24 @@ def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd,
     return st.as_dict()
 
 
+def nodal_divergence(geom: Geometry, bc_lo, bc_hi, vel, ng=1, use_inflow=True, out=None, stream=None):
+    """Nodal divergence of vel as the projection sees it (strong form, consistent for singular
+    boundary sets). Returns (max |div|, out) with out a nodal (nz+1, ny+1, nx+1) tensor."""
+    key = (tuple(geom.n_cell), tuple(geom.prob_lo), tuple(geom.prob_hi), tuple(bc_lo), tuple(bc_hi), 100,
+           torch.cuda.current_device())
+    plan = NodalProjector._plans.get(key)
+    if plan is None:
+        plan = _Plan(geom, A.GBP_NODAL, bc_lo, bc_hi, A.default_options(A.GBP_NODAL), stream)
+        NodalProjector._plans[key] = plan
+    n = geom.n_cell
+    if out is None:
+        out = torch.zeros((n[2] + 1, n[1] + 1, n[0] + 1), dtype=torch.float64, device=vel.device)
+    m = ctypes.c_double()
+    A.check(A.load().gbp_nodal_divergence(plan.ptr, _ref(array4(vel, ng)), int(use_inflow), _ref(array4(out)),
+                                          ctypes.byref(m)), "gbp_nodal_divergence")
+    return m.value, out
+
+
 # ------------------------------------------------------------------------------------ MAC
 class MacProjector:
     """Hydro::MacProjector(geom) for one level: initProjector / updateCoeffs / setUMAC / project."""

@@ -155,6 +155,15 @@ int gbp_nodal_set_sigma(gbp_plan* plan, const gbp_array4* sigma, double const_si
 int gbp_nodal_project(gbp_plan* plan, gbp_array4* vel, gbp_array4* phi, gbp_array4* gradphi,
                       int phi_guess, gbp_stats* stats);
 
+/* The nodal divergence of vel as the projection sees it: the right-hand side of the nodal solve
+ * (div_i = weak divergence / control volume, inflow normal velocity from the ghost cells when
+ * use_inflow != 0, 0 on Dirichlet nodes), made consistent for singular boundary sets. div_out
+ * (nodal, nodes 0..n, may be NULL) and its max norm (host double). This is the post-projection
+ * check max|div u|; the reference computes the same quantity inside NodalProjector::project
+ * (incflo_apply_nodal_projection.cpp:215) but exposes no call for it. */
+int gbp_nodal_divergence(gbp_plan* plan, const gbp_array4* vel, int use_inflow, gbp_array4* div_out,
+                         double* max_norm);
+
 /* incflo::ApplyNodalProjection(density, time, scaling_factor, incremental) end to end
  * (incflo_apply_nodal_projection.cpp:29-93 and :95-267 for one level): fuses the
  * add-back of scaling_factor*gp/rho (:39-62), the U^n subtraction for incremental or

@@ -110,6 +110,23 @@ def test_apply_nodal_projection_fused_semantics(gpu_lib):
             np.testing.assert_array_equal(p_gpu[:, -1, :], p_gpu[:, 0, :])
 
 
+@pytest.mark.parametrize("case", CASES[:4], ids=[f"{c[0]}-{c[2]}-{c[3]}" for c in CASES[:4]])
+def test_nodal_divergence_matches_oracle(gpu_lib, case):
+    from incflo_gb300.projection import nodal_divergence
+
+    n, ext, bclo, bchi = case
+    g, sigma, vel = nodal_case(n, ext, bclo, bchi, seed=5)
+    rhs = O.nodal_rhs(g, vel)
+    V = O.nodal_volume(g)
+    if D not in bclo + bchi:
+        rhs = rhs - V * rhs.sum() / V.sum()
+    ref = -rhs / V
+    m, out = nodal_divergence(Geometry(n, (0, 0, 0), ext), bclo, bchi, cuda(vel))
+    div = unique_nodes(g, out.cpu().numpy())
+    np.testing.assert_allclose(div, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    assert abs(m - np.abs(ref).max()) <= 1e-12 * np.abs(ref).max()
+
+
 def test_divergence_after_projection_no_worse_than_oracle(gpu_lib):
     case = ((24, 24, 24), (1.0, 1.0, 1.0), (P, P, N), (P, P, N))
     g, st, st_or, phi, phi_or, vel, vel_or, grad, grad_or = _run(case, "mixed", seed=3)
