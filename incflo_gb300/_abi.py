@@ -24,7 +24,7 @@ EXPORTS = (
     "gbp_nodal_set_sigma_from_density", "gbp_nodal_set_sigma", "gbp_nodal_project",
     "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
     "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel",
-    "gbp_nodal_divergence",
+    "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc",
 )
 
 
@@ -126,6 +126,9 @@ def load(path: str = LIB_PATH):
         "gbp_apply_nodal_projection_host": (i, [P, P, P, d, P, P, d, i, ctypes.POINTER(Stats)]),
         "gbp_plan_time_kernel": (i, [P, i, i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "gbp_nodal_divergence": (i, [P, A4, i, A4, ctypes.POINTER(ctypes.c_double)]),
+        "gbp_nodal_divergence_noalloc": (i, [ctypes.POINTER(Geometry), ctypes.POINTER(ctypes.c_int),
+                                             ctypes.POINTER(ctypes.c_int), A4, i, A4,
+                                             ctypes.POINTER(ctypes.c_double), P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -164,6 +164,19 @@ int gbp_nodal_project(gbp_plan* plan, gbp_array4* vel, gbp_array4* phi, gbp_arra
 int gbp_nodal_divergence(gbp_plan* plan, const gbp_array4* vel, int use_inflow, gbp_array4* div_out,
                          double* max_norm);
 
+/* Allocation-free gbp_nodal_divergence. No counterpart in the reference. For callers that cannot
+ * allocate device memory: code inside a CUDA stream capture that must not add allocation nodes, or
+ * a host program whose device memory belongs to another allocator. Needs no plan; the only scratch
+ * is a static device array built into the library (512 KB per GPU, held until the process exits),
+ * which caps the grid at 65536 blocks of 32x4x4 nodes (about 33.5 million nodes; larger grids return
+ * GBP_BAD_ARG). The first call on a device looks up that array's address with the device current,
+ * so make it before any stream capture. All calls share the array: calls that overlap on the GPU
+ * race, so serialise them. Arguments as gbp_nodal_divergence, plus the level geometry, boundary
+ * types and stream that a plan would otherwise hold; *max_norm is written on return. */
+int gbp_nodal_divergence_noalloc(const gbp_geometry* geom, const int bc_lo[3], const int bc_hi[3],
+                                 const gbp_array4* vel, int use_inflow, gbp_array4* div_out,
+                                 double* max_norm, void* stream);
+
 /* incflo::ApplyNodalProjection(density, time, scaling_factor, incremental) end to end
  * (incflo_apply_nodal_projection.cpp:29-93 and :95-267 for one level): fuses the
  * add-back of scaling_factor*gp/rho (:39-62), the U^n subtraction for incremental or
