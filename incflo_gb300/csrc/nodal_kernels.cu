@@ -125,6 +125,15 @@ __device__ __forceinline__ bool decode_node(const NodalGeom& g, long long t, int
     return true;
 }
 
+// 3-D launch over the unique nodes: block (32, 4, 2), no index division
+__device__ __forceinline__ bool grid3_node(const NodalGeom& g, int& i, int& j, int& k)
+{
+    i = blockIdx.x * blockDim.x + threadIdx.x;
+    j = blockIdx.y * blockDim.y + threadIdx.y;
+    k = blockIdx.z * blockDim.z + threadIdx.z;
+    return i < g.nu[0] && j < g.nu[1] && k < g.nu[2];
+}
+
 // ---------------------------------------------------------------------------------------
 // smoother / residual / transfer
 // ---------------------------------------------------------------------------------------
@@ -133,7 +142,7 @@ __global__ void __launch_bounds__(256) k_jacobi(NodalGeom g, const T* __restrict
                                                 const T* __restrict__ b, T* __restrict__ xout, T omega)
 {
     int i, j, k;
-    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    if (!grid3_node(g, i, j, k)) return;
     T v = T(0);
     if (!node_is_dirichlet(g, i, j, k)) {
         const long long c = pidx(g.sy, g.sz, i, j, k);
@@ -163,7 +172,7 @@ __global__ void __launch_bounds__(256) k_resid(NodalGeom g, const T* __restrict_
 {
     int i, j, k;
     double nv = 0.0;
-    if (decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+    if (grid3_node(g, i, j, k)) {
         T v = T(0);
         if (!node_is_dirichlet(g, i, j, k)) {
             const long long c = pidx(g.sy, g.sz, i, j, k);
@@ -185,7 +194,7 @@ __global__ void __launch_bounds__(256) k_restrict(NodalGeom gf, NodalGeom gc, co
                                                   T* __restrict__ bc)
 {
     int I, J, K;
-    if (!decode_node(gc, blockIdx.x * (long long)blockDim.x + threadIdx.x, I, J, K)) return;
+    if (!grid3_node(gc, I, J, K)) return;
     T v = T(0);
     if (!node_is_dirichlet(gc, I, J, K)) {
         const long long f = pidx(gf.sy, gf.sz, 2 * I, 2 * J, 2 * K);
@@ -211,7 +220,7 @@ __global__ void __launch_bounds__(256) k_prolong_add(NodalGeom gf, NodalGeom gc,
                                                      T* __restrict__ xf)
 {
     int i, j, k;
-    if (!decode_node(gf, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    if (!grid3_node(gf, i, j, k)) return;
     if (node_is_dirichlet(gf, i, j, k)) return;
     const int I0 = i >> 1, J0 = j >> 1, K0 = k >> 1;
     const int oi = i & 1, oj = j & 1, ok = k & 1;
@@ -631,7 +640,7 @@ __global__ void __launch_bounds__(256) k_add_correction(NodalGeom g, double* __r
                                                         double inv_scale)
 {
     int i, j, k;
-    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    if (!grid3_node(g, i, j, k)) return;
     const long long p = pidx(g.sy, g.sz, i, j, k);
     store_node(x, g, i, j, k, x[p] + (double)e[p] * inv_scale);
 }
@@ -640,7 +649,7 @@ __global__ void __launch_bounds__(256) k_to_f32(NodalGeom g, const double* __res
                                                 double scale)
 {
     int i, j, k;
-    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    if (!grid3_node(g, i, j, k)) return;
     const long long p = pidx(g.sy, g.sz, i, j, k);
     r32[p] = (float)(r[p] * scale);
 }
@@ -721,7 +730,7 @@ void nodal_store_div(const NodalGeom& g, const gbp_array4& out, const double* b,
 __global__ void k_nodal_load_phi(NodalGeom g, gbp_array4 in, double* __restrict__ phi)
 {
     int i, j, k;
-    if (!decode_node(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    if (!grid3_node(g, i, j, k)) return;
     const double v = node_is_dirichlet(g, i, j, k) ? 0.0 : a4(in, i, j, k, 0);
     store_node(phi, g, i, j, k, v);
 }
@@ -751,17 +760,22 @@ static inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs 
 static inline long long nunique(const NodalGeom& g) { return (long long)g.nu[0] * g.nu[1] * g.nu[2]; }
 static inline long long ncells(const NodalGeom& g) { return (long long)g.n[0] * g.n[1] * g.n[2]; }
 
+static const dim3 kBlock3(32, 4, 2);
+static inline dim3 grid3(const NodalGeom& g)
+{
+    return dim3((g.nu[0] + 31) / 32, (g.nu[1] + 3) / 4, (g.nu[2] + 1) / 2);
+}
+
 template <typename T>
 void nodal_jacobi(const NodalGeom& g, const T* s, const T* xin, const T* b, T* xout, double omega, bool zero,
                   cudaStream_t st)
 {
-    const unsigned nb = nblocks(nunique(g), 256);
     if (zero) {
-        k_jacobi<T, true, true><<<nb, 256, 0, st>>>(g, s, xin, b, xout, (T)omega);
+        k_jacobi<T, true, true><<<grid3(g), kBlock3, 0, st>>>(g, s, xin, b, xout, (T)omega);
     } else if (g.iso) {
-        k_jacobi<T, true, false><<<nb, 256, 0, st>>>(g, s, xin, b, xout, (T)omega);
+        k_jacobi<T, true, false><<<grid3(g), kBlock3, 0, st>>>(g, s, xin, b, xout, (T)omega);
     } else {
-        k_jacobi<T, false, false><<<nb, 256, 0, st>>>(g, s, xin, b, xout, (T)omega);
+        k_jacobi<T, false, false><<<grid3(g), kBlock3, 0, st>>>(g, s, xin, b, xout, (T)omega);
     }
 }
 
@@ -769,23 +783,22 @@ template <typename T>
 void nodal_resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
                  cudaStream_t st)
 {
-    const unsigned nb = nblocks(nunique(g), 256);
     if (g.iso)
-        k_resid<T, true><<<nb, 256, 0, st>>>(g, s, x, b, r, norm);
+        k_resid<T, true><<<grid3(g), kBlock3, 0, st>>>(g, s, x, b, r, norm);
     else
-        k_resid<T, false><<<nb, 256, 0, st>>>(g, s, x, b, r, norm);
+        k_resid<T, false><<<grid3(g), kBlock3, 0, st>>>(g, s, x, b, r, norm);
 }
 
 template <typename T>
 void nodal_restrict(const NodalGeom& gf, const NodalGeom& gc, const T* rf, T* bc, cudaStream_t st)
 {
-    k_restrict<T><<<nblocks(nunique(gc), 256), 256, 0, st>>>(gf, gc, rf, bc);
+    k_restrict<T><<<grid3(gc), kBlock3, 0, st>>>(gf, gc, rf, bc);
 }
 
 template <typename T>
 void nodal_prolong_add(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T* xf, cudaStream_t st)
 {
-    k_prolong_add<T><<<nblocks(nunique(gf), 256), 256, 0, st>>>(gf, gc, xc, xf);
+    k_prolong_add<T><<<grid3(gf), kBlock3, 0, st>>>(gf, gc, xc, xf);
 }
 
 template <typename T>
@@ -880,14 +893,14 @@ int nodal_partials_needed(const NodalGeom& g) { return std::max(nodal_rhs_partia
 template <typename TE>
 void nodal_add_correction(const NodalGeom& g, double* x, const TE* e, double inv_scale, cudaStream_t st)
 {
-    k_add_correction<TE><<<nblocks(nunique(g), 256), 256, 0, st>>>(g, x, e, inv_scale);
+    k_add_correction<TE><<<grid3(g), kBlock3, 0, st>>>(g, x, e, inv_scale);
 }
 template void nodal_add_correction<double>(const NodalGeom&, double*, const double*, double, cudaStream_t);
 template void nodal_add_correction<float>(const NodalGeom&, double*, const float*, double, cudaStream_t);
 
 void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale, cudaStream_t st)
 {
-    k_to_f32<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, r, r32, scale);
+    k_to_f32<<<grid3(g), kBlock3, 0, st>>>(g, r, r32, scale);
 }
 
 void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st)
@@ -903,7 +916,7 @@ void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* ph
 
 void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaStream_t st)
 {
-    k_nodal_load_phi<<<nblocks(nunique(g), 256), 256, 0, st>>>(g, in, phi);
+    k_nodal_load_phi<<<grid3(g), kBlock3, 0, st>>>(g, in, phi);
 }
 
 }  // namespace gbp

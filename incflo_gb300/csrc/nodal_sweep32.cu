@@ -598,13 +598,205 @@ int launch_zpair(const NodalGeom& g, const float* s, const float* x, const float
     return GBP_OK;
 }
 
+// ----------------------------------------------------------------------------------------------
+// Register-blocked z-march: a thread owns an x-pair of nodes in RY consecutive rows (2 x RY nodes),
+// packed FP32x2 arithmetic, windows of RY+2 rows and cell layers of RY+1 rows shared by the RY node
+// rows, so loads and loop overhead are amortised over 2*RY nodes and the RY independent rows give
+// the scheduler parallel FMA chains. Two planes in registers, the far-plane coupling carried.
+constexpr int QX = 32, QY = 4;  // threads per CTA: 32 x-pairs (64 nodes) x QY row blocks
+
+template <int RY>
+struct BWin {
+    float2 c[RY + 2];
+    float l[RY + 2], r[RY + 2];
+};
+template <int RY>
+struct BLay {
+    float2 c[RY + 1];
+    float l[RY + 1];
+};
+
+template <int RY>
+__device__ __forceinline__ float2 blft(const BWin<RY>& w, int r) { return f2(w.l[r], w.c[r].x); }
+template <int RY>
+__device__ __forceinline__ float2 brgt(const BWin<RY>& w, int r) { return f2(w.c[r].y, w.r[r]); }
+template <int RY>
+__device__ __forceinline__ float2 bslo(const BLay<RY>& L, int r) { return f2(L.l[r], L.c[r].x); }
+
+// couplings of node row q of the centre pair to the far plane through layer L, packed
+template <int RY>
+__device__ __forceinline__ float2 bfar(const BWin<RY>& far, const BLay<RY>& L, int q, float2 xc, float2& a0, float2& a1)
+{
+    const float2 s00 = bslo(L, q), s01 = L.c[q], s10 = bslo(L, q + 1), s11 = L.c[q + 1];
+    const float2 ax0 = __fadd2_rn(s00, s10), ax1 = __fadd2_rn(s01, s11);
+    const float2 ay0 = __fadd2_rn(s00, s01), ay1 = __fadd2_rn(s10, s11);
+    const float2 nxc = f2(-xc.x, -xc.y);
+    a0 = __ffma2_rn(ax0, __fadd2_rn(blft(far, q + 1), nxc), a0);
+    a1 = __ffma2_rn(ax1, __fadd2_rn(brgt(far, q + 1), nxc), a1);
+    a0 = __ffma2_rn(ay0, __fadd2_rn(far.c[q], nxc), a0);
+    a1 = __ffma2_rn(ay1, __fadd2_rn(far.c[q + 2], nxc), a1);
+    a0 = __ffma2_rn(s00, __fadd2_rn(blft(far, q), nxc), a0);
+    a1 = __ffma2_rn(s01, __fadd2_rn(brgt(far, q), nxc), a1);
+    a0 = __ffma2_rn(s10, __fadd2_rn(blft(far, q + 2), nxc), a0);
+    a1 = __ffma2_rn(s11, __fadd2_rn(brgt(far, q + 2), nxc), a1);
+    return __fadd2_rn(ax0, ax1);
+}
+
+template <int MODE, int RY>
+__global__ void __launch_bounds__(QX* QY) k_zblock32(NodalGeom g, const float* __restrict__ sg, const float* __restrict__ xin,
+                                                     const float* __restrict__ bin, float* __restrict__ out, Consts cst,
+                                                     int kchunk, unsigned long long* norm)
+{
+    const int i0 = 2 * (blockIdx.x * QX + threadIdx.x);
+    const int j0 = (blockIdx.y * QY + threadIdx.y) * RY;
+    const int kbeg = blockIdx.z * kchunk;
+    const bool act = i0 < g.nu[0] && j0 < g.nu[1];
+    const bool actB = i0 + 1 < g.nu[0];
+    const int kend = act ? min(kbeg + kchunk, g.nu[2]) : kbeg;
+    const long long sy = g.sy, sz = g.sz;
+    const bool dxA = (g.dlo[0] && i0 == 0) || (g.dhi[0] && i0 == g.n[0]);
+    const bool dxB = !actB || (g.dlo[0] && i0 + 1 == 0) || (g.dhi[0] && i0 + 1 == g.n[0]);
+    const bool ax_ = g.per[0] && (i0 <= 1 || i0 + 1 >= g.n[0] - 1);
+    const long long c0 = pidx(sy, sz, i0, j0, 0);
+    const float* xw = xin + c0 - sy;  // node (i0, j0-1, 0)
+    const float* sw = sg + c0 - sy;   // cell (i0, j0-1, 0)
+    auto load_win = [&](int q, BWin<RY>& w) {
+        const float* p = xw + (long long)q * sz;
+#pragma unroll
+        for (int r = 0; r < RY + 2; ++r) {
+            const float* rp = p + r * sy;
+            w.c[r] = __ldg(reinterpret_cast<const float2*>(rp));
+            w.l[r] = __ldg(rp - 1);
+            w.r[r] = __ldg(rp + 2);
+        }
+    };
+    auto load_lay = [&](int q, BLay<RY>& l) {
+        const float* p = sw + (long long)q * sz;
+#pragma unroll
+        for (int r = 0; r < RY + 1; ++r) {
+            const float* rp = p + r * sy;
+            l.c[r] = __ldg(reinterpret_cast<const float2*>(rp));
+            l.l[r] = __ldg(rp - 1);
+        }
+    };
+    BWin<RY> WA, WB;
+    BLay<RY> LA, LB;
+    float2 carry[RY], sb[RY];
+#pragma unroll
+    for (int q = 0; q < RY; ++q) carry[q] = sb[q] = f2(0.f, 0.f);
+    float nmax = 0.f;
+    if (kend > kbeg) {
+        load_win(kbeg - 1, WA);
+        load_win(kbeg, WB);
+        load_lay(kbeg - 1, LA);
+#pragma unroll
+        for (int q = 0; q < RY; ++q) {
+            float2 a0 = f2(0.f, 0.f), a1 = f2(0.f, 0.f);
+            sb[q] = bfar(WA, LA, q, WB.c[q + 1], a0, a1);
+            carry[q] = __fadd2_rn(a0, a1);
+        }
+    }
+    const float2 k3 = f2(cst.k3, cst.k3), k0 = f2(cst.k0, cst.k0), om = f2(cst.omega, cst.omega);
+    float* op = out + c0 + (long long)kbeg * sz;
+    const float* bp = bin + c0 + (long long)kbeg * sz;
+
+    auto step = [&](BWin<RY>& ctr, BWin<RY>& nxt, BLay<RY>& lb, BLay<RY>& la, int k) {
+        load_win(k + 1, nxt);
+        load_lay(k, la);
+        const bool dk = (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+        const bool ak = g.per[2] && (k <= 1 || k == g.n[2] - 1);
+#pragma unroll
+        for (int q = 0; q < RY; ++q) {
+            const int j = j0 + q;
+            const float2 bv = __ldg(reinterpret_cast<const float2*>(bp + q * sy));
+            const float2 xc = ctr.c[q + 1];
+            const float2 nxc = f2(-xc.x, -xc.y);
+            float2 a0 = carry[q], a1 = f2(0.f, 0.f);
+            a0 = __ffma2_rn(__fadd2_rn(bslo(lb, q), bslo(la, q)), __fadd2_rn(blft(ctr, q), nxc), a0);
+            a1 = __ffma2_rn(__fadd2_rn(lb.c[q], la.c[q]), __fadd2_rn(brgt(ctr, q), nxc), a1);
+            a0 = __ffma2_rn(__fadd2_rn(bslo(lb, q + 1), bslo(la, q + 1)), __fadd2_rn(blft(ctr, q + 2), nxc), a0);
+            a1 = __ffma2_rn(__fadd2_rn(lb.c[q + 1], la.c[q + 1]), __fadd2_rn(brgt(ctr, q + 2), nxc), a1);
+            const float2 sa = bfar(nxt, la, q, xc, a0, a1);
+            float2 n0 = f2(0.f, 0.f), n1 = f2(0.f, 0.f);
+            (void)bfar(ctr, la, q, nxt.c[q + 1], n0, n1);
+            const float2 ax = __fmul2_rn(k3, __fadd2_rn(a0, a1));
+            const float2 rr = __fadd2_rn(bv, f2(-ax.x, -ax.y));
+            float2 v;
+            if (MODE == 0) {
+                const float2 dg = __fmul2_rn(k0, __fadd2_rn(sb[q], sa));
+                v = __ffma2_rn(__fmul2_rn(om, rr), f2(__frcp_rn(dg.x), __frcp_rn(dg.y)), xc);
+            } else {
+                v = rr;
+            }
+            carry[q] = __fadd2_rn(n0, n1);
+            sb[q] = sa;
+            if (j < g.nu[1]) {
+                const bool dy = (g.dlo[1] && j == 0) || (g.dhi[1] && j == g.n[1]);
+                if (dk || dy || dxA) v.x = 0.f;
+                if (dk || dy || dxB) v.y = 0.f;
+                if (MODE == 1 && norm) {
+                    const float m = fmaxf(fabsf(v.x) * (float)node_inv_volume(g, i0, j, k),
+                                          actB ? fabsf(v.y) * (float)node_inv_volume(g, i0 + 1, j, k) : 0.f);
+                    nmax = (v.x != v.x || v.y != v.y || nmax != nmax) ? __int_as_float(0x7fc00000) : fmaxf(nmax, m);
+                }
+                const bool ay = g.per[1] && (j <= 1 || j == g.n[1] - 1);
+                if (ak || ay || ax_ || !actB) {
+                    store_node(out, g, i0, j, k, v.x);
+                    if (actB) store_node(out, g, i0 + 1, j, k, v.y);
+                } else {
+                    *reinterpret_cast<float2*>(op + q * sy) = v;
+                }
+            }
+        }
+        op += sz;
+        bp += sz;
+    };
+    int k = kbeg;
+    for (; k + 1 < kend; k += 2) {
+        step(WB, WA, LA, LB, k);
+        step(WA, WB, LB, LA, k + 1);
+    }
+    if (k < kend) step(WB, WA, LA, LB, k);
+    if (MODE == 1 && norm) {
+        const double m = block_max((double)nmax);
+        if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(norm, m);
+    }
+}
+
+template <int MODE, int RY>
+int launch_zblock(const NodalGeom& g, const float* s, const float* x, const float* b, float* out, float omega,
+                  unsigned long long* norm, cudaStream_t st)
+{
+    static int resident = 0;
+    if (!resident) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_zblock32<MODE, RY>, QX * QY, 0) != cudaSuccess ||
+            resident < 1)
+            resident = 1;
+    }
+    const int tx = (g.nu[0] + 2 * QX - 1) / (2 * QX), ty = (g.nu[1] + QY * RY - 1) / (QY * RY);
+    const int nz = sweep_z_chunks(g, tx * ty, resident);
+    const int kchunk = (g.nu[2] + nz - 1) / nz;
+    const Consts c{(float)g.K[0], (float)g.K[3], omega};
+    dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
+    k_zblock32<MODE, RY><<<grid, dim3(QX, QY), 0, st>>>(g, s, x, b, out, c, kchunk, norm);
+    return GBP_OK;
+}
+
 int sweep_variant()
 {
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("GBP_SWEEP32");
-        // 2: packed-pair z-march (default), 0: scalar z-march, 1: TMA producer/consumer
-        v = !e ? 2 : (e[0] == 't' ? 1 : (e[0] == 's' ? 0 : 2));
+        // 3: register-blocked 2x4 (default), 4: register-blocked 2x2, 2: packed pair,
+        // 0: scalar z-march, 1: TMA producer/consumer
+        v = 5;
+        if (e) {
+            if (e[0] == 'b') v = 3;
+            else if (e[0] == 't') v = 1;
+            else if (e[0] == 's') v = 0;
+            else if (e[0] == 'p') v = 2;
+            else if (e[0] == '2') v = 4;
+        }
     }
     return v;
 }
@@ -614,6 +806,13 @@ int sweep_variant()
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
+    if (sweep_variant() == 5) return sweep32_tma1_run(g, mode, s, x, b, out, omega, err, norm, st);
+    if (sweep_variant() == 3)
+        return mode == 0 ? launch_zblock<0, 4>(g, s, x, b, out, omega, norm, st)
+                         : launch_zblock<1, 4>(g, s, x, b, out, omega, norm, st);
+    if (sweep_variant() == 4)
+        return mode == 0 ? launch_zblock<0, 2>(g, s, x, b, out, omega, norm, st)
+                         : launch_zblock<1, 2>(g, s, x, b, out, omega, norm, st);
     if (sweep_variant() == 2)
         return mode == 0 ? launch_zpair<0>(g, s, x, b, out, omega, norm, st)
                          : launch_zpair<1>(g, s, x, b, out, omega, norm, st);

@@ -35,7 +35,7 @@ template <typename T>
 struct SweepCfg;
 template <>
 struct SweepCfg<float> {
-    static constexpr int NX = 64, TY = 16, NS = 4, NPT = 2;
+    static constexpr int NX = 32, TY = 8, NS = 3, NPT = 1;
 };
 template <>
 struct SweepCfg<double> {
@@ -114,6 +114,142 @@ __device__ __forceinline__ void layer64(const double (&Pn)[3][3], const double (
                 acc = fma(s, t, acc);
             }
         }
+}
+
+// FP32 counterpart of layer64 for the isotropic operator: differences to the centre, so rounding
+// scales with the local variation of x rather than with x
+__device__ __forceinline__ void layer32(const float (&Pn)[3][3], const float (&Pd)[3][3], const float (&sg)[2][2],
+                                        float& acc, float& ssum)
+{
+    const float xc = Pn[1][1];
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+        for (int cx = 0; cx < 2; ++cx) {
+            const int ox = cx ? 2 : 0, oy = cy ? 2 : 0;
+            const float s = sg[cy][cx];
+            ssum += s;
+            const float S = ((Pn[oy][ox] - xc) + (Pd[1][ox] - xc)) + ((Pd[oy][1] - xc) + (Pd[oy][ox] - xc));
+            acc = fmaf(s, S, acc);
+        }
+}
+
+// FP32 sweep of the same design as the FP64 one below (isotropic spacing only): one node per
+// thread, 32 x 8 nodes per CTA, 3-slot TMA ring, one block barrier per plane, float constants
+// passed in (no FP64 conversions in the loop). Several CTAs per SM keep enough warps in flight.
+template <int MODE>
+__global__ void __launch_bounds__(SweepShape<float>::THREADS)
+    k_sweep32t(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
+               const __grid_constant__ CUtensorMap mb, NodalGeom g, float* __restrict__ out, float k0, float k3,
+               float omega, int kchunk, unsigned* err, unsigned long long* norm)
+{
+    using S = SweepShape<float>;
+    constexpr int NS = S::NS;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bar[NS];
+    __shared__ int abort_flag;
+
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = tx + 32 * ty;
+    const int x0 = blockIdx.x * S::NX, y0 = blockIdx.y * S::TY;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(kbeg + kchunk, g.nu[2]);
+    const int nsteps = kend - kbeg + 2;
+    const int i = x0 + tx, j = y0 + ty;
+    const bool active = i < g.nu[0] && j < g.nu[1];
+    const bool dxy = dir_xy(g, i, j), axy = alias_xy(g, i, j);
+    float* op = out + pidx(g.sy, g.sz, i, j, kbeg);
+
+    auto issue = [&](int s) {
+        const int slot = s % NS;
+        unsigned char* base = smem + slot * S::STAGE;
+        const int k = kbeg - 2 + s;
+        mbar_arrive_expect_tx(&bar[slot], S::TX_BYTES);
+        tma_load_3d(base + S::XO, &mx, &bar[slot], x0, y0, k + 2);
+        tma_load_3d(base + S::SO, &ms, &bar[slot], x0, y0, k + 1);
+        tma_load_3d(base + S::BO, &mb, &bar[slot], x0 + kOX, y0 + 1, k + 1);
+    };
+    if (tid == 0) {
+        for (int q = 0; q < NS; ++q) mbar_init(&bar[q], 1);
+        mbar_fence_init();
+        abort_flag = 0;
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int s = 0; s < NS && s < nsteps; ++s) issue(s);
+
+    float P0[3][3], P1[3][3], P2[3][3], S0[2][2], S1[2][2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) P0[a][b] = P1[a][b] = 0.f;
+    S0[0][0] = S0[0][1] = S0[1][0] = S0[1][1] = 0.f;
+    float nmax = 0.f;
+
+    for (int s = 0; s < nsteps; ++s) {
+        const int slot = s % NS;
+        const unsigned char* base = smem + slot * S::STAGE;
+        if (!mbar_wait_bounded(&bar[slot], (uint32_t)((s / NS) & 1), err)) abort_flag = 1;
+        __syncthreads();
+        if (abort_flag) break;
+        const float* sx = reinterpret_cast<const float*>(base + S::XO) + tx + 3;
+        const float* ss = reinterpret_cast<const float*>(base + S::SO) + tx + 3;
+        const float* sb = reinterpret_cast<const float*>(base + S::BO) + tx;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) P2[a][b] = sx[(ty + a) * S::BXX + b];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) S1[a][b] = ss[(ty + a) * S::BXS + b];
+        const float bv = sb[ty * S::BXB];
+        const int k = kbeg - 2 + s;
+        if (s >= 2 && active) {
+            float v = 0.f;
+            if (!(dxy || dir_k(g, k))) {
+                float acc = 0.f, ssum = 0.f;
+                layer32(P1, P0, S0, acc, ssum);
+                layer32(P1, P2, S1, acc, ssum);
+                const float ax = k3 * acc;
+                if (MODE == 0) {
+                    v = fmaf(omega * (bv - ax), __frcp_rn(k0 * ssum), P1[1][1]);
+                } else {
+                    v = bv - ax;
+                    if (norm)
+                        nmax = (v != v || nmax != nmax) ? __int_as_float(0x7fc00000)
+                                                        : fmaxf(nmax, fabsf(v) * (float)node_inv_volume(g, i, j, k));
+                }
+            }
+            if (axy || alias_k(g, k))
+                store_node(out, g, i, j, k, v);
+            else
+                *op = v;
+            op += g.sz;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                P0[a][b] = P1[a][b];
+                P1[a][b] = P2[a][b];
+            }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) S0[a][b] = S1[a][b];
+        __syncthreads();
+        if (tid == 0 && s + NS < nsteps) {
+            fence_proxy_async();
+            issue(s + NS);
+        }
+    }
+    if (abort_flag && tid == 0)
+        for (int q = 0; q < NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
+    if (MODE == 1 && norm) {
+        const double m = block_max((double)nmax);
+        if (tid == 0) atomic_max_nonneg(norm, m);
+    }
 }
 
 template <int MODE, bool ISO>
@@ -372,6 +508,41 @@ static int launch_sweep(const CUtensorMap& mx, const CUtensorMap& ms, const CUte
     dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
     kern<<<grid, dim3(32, S::TY), S::SMEM, st>>>(mx, ms, mb, g, out, (T)omega, kchunk, err, norm);
     return GBP_OK;
+}
+
+template <int MODE>
+static int launch_sweep32t(const CUtensorMap& mx, const CUtensorMap& ms, const CUtensorMap& mb, const NodalGeom& g,
+                           float* out, float omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
+{
+    using S = SweepShape<float>;
+    static int resident = 0;
+    if (!resident) {
+        cudaFuncSetAttribute(k_sweep32t<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_sweep32t<MODE>, S::THREADS, S::SMEM) !=
+                cudaSuccess ||
+            resident < 1)
+            resident = 1;
+    }
+    const int tx = (g.nu[0] + S::NX - 1) / S::NX, ty = (g.nu[1] + S::TY - 1) / S::TY;
+    const int nz = sweep_z_chunks(g, tx * ty, resident);
+    const int kchunk = (g.nu[2] + nz - 1) / nz;
+    dim3 grid(tx, ty, (g.nu[2] + kchunk - 1) / kchunk);
+    k_sweep32t<MODE><<<grid, dim3(32, S::TY), S::SMEM, st>>>(mx, ms, mb, g, out, (float)g.K[0], (float)g.K[3], omega,
+                                                              kchunk, err, norm);
+    return GBP_OK;
+}
+
+int sweep32_tma1_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out,
+                     float omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
+{
+    using S = SweepShape<float>;
+    CUtensorMap mx, ms, mb;
+    int rc = make_tensor_map(x, 4, g.sy, g.sz, g.count, S::BXX, S::TY + 2, &mx);
+    if (!rc) rc = make_tensor_map(s, 4, g.sy, g.sz, g.count, S::BXS, S::TY + 1, &ms);
+    if (!rc) rc = make_tensor_map(b, 4, g.sy, g.sz, g.count, S::BXB, S::TY, &mb);
+    if (rc) return rc;
+    return mode == 0 ? launch_sweep32t<0>(mx, ms, mb, g, out, omega, err, norm, st)
+                     : launch_sweep32t<1>(mx, ms, mb, g, out, omega, err, norm, st);
 }
 
 template <>
