@@ -122,15 +122,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel_key):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+def ncu_traffic(summary_name):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel,
+    read from the committed ncu summary's `traffic_bytes_per_launch:` line, if present."""
+    p = os.path.join(ROOT, "profiles", summary_name)
     if os.path.exists(p):
-        d = json.load(open(p))
-        v = d.get(kernel_key)
-        if isinstance(v, dict):
-            return v.get("bytes_per_launch_full_size")
-        return v
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":", 1)[1].strip())
     return None
 
 
@@ -312,9 +311,9 @@ def run_ours(args, ws, rank, local):
                    "final_rel_resid": st_mixed[0]["final_rel_resid"],
                    "speedup_vs_plain_fp64": round(fp64_ms / per_step, 3)},
         "wall_ms_per_step": round(wall_mixed * 1e3 / len(ms_mixed), 3),
-        "roofline": {"bound": "hbm", "kernel": "k_jacobi<float> level 0", "achieved": round(ach, 1),
+        "roofline": {"bound": "hbm", "kernel": "k_sweep32t<0> (FP32 Jacobi sweep, level 0)", "achieved": round(ach, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
-                     "traffic": ncu_traffic("k_jacobi_f32"), "peak_kind": peak_kind,
+                     "traffic": ncu_traffic("k_sweep32t_nodal_256.md"), "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": bytes_k.value, "ms_per_launch": round(ms_k.value, 5)},
         "roofline_fp64_jacobi": {"achieved_gbs": round(ach64, 1), "frac_hbm": round(ach64 / peak, 4),
                                  "ms_per_launch": round(ms64.value, 5)},

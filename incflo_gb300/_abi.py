@@ -25,6 +25,7 @@ EXPORTS = (
     "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
     "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel",
     "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc",
+    "gbp_nn_conv3d", "gbp_nn_conv3d_wgrad",
 )
 
 
@@ -129,6 +130,10 @@ def load(path: str = LIB_PATH):
         "gbp_nodal_divergence_noalloc": (i, [ctypes.POINTER(Geometry), ctypes.POINTER(ctypes.c_int),
                                              ctypes.POINTER(ctypes.c_int), A4, i, A4,
                                              ctypes.POINTER(ctypes.c_double), P]),
+        "gbp_nn_conv3d": (i, [ctypes.POINTER(ctypes.c_int), i, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int), P,
+                              i, i, i, P, i, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int),
+                              i, P]),
+        "gbp_nn_conv3d_wgrad": (i, [ctypes.POINTER(ctypes.c_int), P, i, i, i, P, i, i, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include "gbp_internal.cuh"
@@ -21,6 +22,8 @@ void sweep_forget_maps(const void* pool_base, size_t pool_bytes);
 // helpers shared by the two sweep files
 int make_tensor_map(const void* base, int esize, long long sy, long long sz, long long count, int boxx, int rows,
                     CUtensorMap* out);
+// cuTensorMapEncodeTiled from the driver (nullptr when unavailable)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 int sweep_z_chunks(const NodalGeom& g, int xy_tiles, int resident);
 int sm_count_cached();
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,

@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(SweepShape<double>::THREADS)
 }
 
 // ------------------------------------------------------------------------------- host side
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     static std::once_flag once;
@@ -404,7 +404,7 @@ int make_tensor_map(const void* base, int esize, long long sy, long long sz, lon
         *out = it->second;
         return GBP_OK;
     }
-    auto fn = encode_fn();
+    auto fn = tensor_map_encoder();
     if (!fn) {
         set_error("cuTensorMapEncodeTiled is unavailable from the driver");
         return GBP_CUDA_ERROR;

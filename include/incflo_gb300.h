@@ -223,6 +223,27 @@ int gbp_apply_nodal_projection_host(gbp_plan* plan, double* vel, const double* r
 int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_launch,
                          double* bytes_per_launch);
 
+/* ---- warm-start network building blocks (no reference counterpart) -------------------
+ * Activations are channels-last BF16 matrices [R][C] over a grid of dims[0] x dims[1] x
+ * dims[2] voxels with a one-voxel zero halo, R = (dims[0]+2)(dims[1]+2)(dims[2]+2), row
+ * p = (z+1)(dims[1]+2)(dims[0]+2) + (y+1)(dims[0]+2) + (x+1). Channel counts are 16, 32 or
+ * multiples of 64; all pointers are device pointers, 16-byte aligned. Both calls
+ * synchronise the stream and return GBP_TIMEOUT if a bounded wait inside the kernel ran out. */
+
+/* out = epilogue(sum over inputs i, taps t, channels c of in_i[p + off(t)][c] w[t][n][c0_i + c])
+ * with w [ntaps][cout][sum cin] BF16 (ntaps 27: 3x3x3 cross-correlation, tap t = 9(dz+1) +
+ * 3(dy+1) + (dx+1); ntaps 1: pointwise), off negated when flip != 0. Output channel n goes to
+ * segment s (seg_c[s] channels each, [R][seg_c[s]]). flags: 1 = forward GELU (out = gelu(acc +
+ * bias), aux = acc + bias when aux[s] != NULL), 2 = add the existing out, 4 = multiply by
+ * gelu'(aux). Halo rows of out are written as zeros. */
+int gbp_nn_conv3d(const int dims[3], int nin, void* const in[], const int cin[], const void* w,
+                  int ntaps, int flip, int cout, const float* bias, int nseg, void* const out[],
+                  void* const aux[], const int seg_c[], int flags, void* stream);
+
+/* dw[t][o][ci0 + c] += sum_p gout[p][o] in[p + off(t)][c], FP32 dw [ntaps][cout][cin_tot]. */
+int gbp_nn_conv3d_wgrad(const int dims[3], const void* in, int cin, int ci0, int cin_tot,
+                        const void* gout, int cout, int ntaps, float* dw, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
