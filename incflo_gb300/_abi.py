@@ -26,6 +26,10 @@ EXPORTS = (
     "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel",
     "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc",
     "gbp_nn_conv3d", "gbp_nn_conv3d_wgrad",
+    "gbp_surrogate_create", "gbp_surrogate_destroy", "gbp_surrogate_num_params", "gbp_surrogate_get_params",
+    "gbp_surrogate_set_params", "gbp_surrogate_get_grads", "gbp_surrogate_save", "gbp_surrogate_load",
+    "gbp_surrogate_train_pair", "gbp_surrogate_predict", "gbp_surrogate_add_sample", "gbp_surrogate_num_samples",
+    "gbp_surrogate_clear_samples", "gbp_surrogate_train", "gbp_plan_set_surrogate",
 )
 
 
@@ -82,6 +86,9 @@ class Stats(ctypes.Structure):
         ("ms_total", ctypes.c_double),
         ("ms_solve", ctypes.c_double),
         ("kernel_launches", ctypes.c_longlong),
+        ("warm_start", ctypes.c_int),
+        ("warm_rel_resid", ctypes.c_double),
+        ("ms_warm", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -134,6 +141,22 @@ def load(path: str = LIB_PATH):
                               i, i, i, P, i, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int),
                               i, P]),
         "gbp_nn_conv3d_wgrad": (i, [ctypes.POINTER(ctypes.c_int), P, i, i, i, P, i, i, P, P]),
+        "gbp_surrogate_create": (i, [i, ctypes.c_ulonglong, ctypes.POINTER(P)]),
+        "gbp_surrogate_destroy": (i, [P]),
+        "gbp_surrogate_num_params": (ctypes.c_longlong, [P]),
+        "gbp_surrogate_get_params": (i, [P, P, ctypes.c_longlong]),
+        "gbp_surrogate_set_params": (i, [P, P, ctypes.c_longlong]),
+        "gbp_surrogate_get_grads": (i, [P, P, ctypes.c_longlong]),
+        "gbp_surrogate_save": (i, [P, ctypes.c_char_p]),
+        "gbp_surrogate_load": (i, [P, ctypes.c_char_p]),
+        "gbp_surrogate_train_pair": (i, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), P, P,
+                                         ctypes.c_float, ctypes.POINTER(ctypes.c_double), P]),
+        "gbp_surrogate_predict": (i, [P, ctypes.POINTER(ctypes.c_int), P, P, P]),
+        "gbp_surrogate_add_sample": (i, [P, P, A4]),
+        "gbp_surrogate_num_samples": (i, [P]),
+        "gbp_surrogate_clear_samples": (i, [P]),
+        "gbp_surrogate_train": (i, [P, i, ctypes.c_float, ctypes.c_ulonglong, P, P]),
+        "gbp_plan_set_surrogate": (i, [P, P, i, i]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

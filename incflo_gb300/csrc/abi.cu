@@ -12,6 +12,7 @@
 #include "gbp_internal.cuh"
 #include "mac_solver.h"
 #include "nodal_solver.h"
+#include "plan.h"
 
 namespace gbp {
 
@@ -29,17 +30,6 @@ int cuda_fail(cudaError_t e, const char* what)
 
 using namespace gbp;
 
-struct gbp_plan {
-    int kind;
-    cudaStream_t stream;
-    gbp_geometry geom;
-    int bc_lo[3], bc_hi[3];
-    NodalSolver* nodal = nullptr;
-    MacSolver* mac = nullptr;
-    // device staging for the host-buffer entry point
-    double* hbuf = nullptr;
-    size_t hbuf_bytes = 0;
-};
 
 static bool valid_array(const gbp_array4* a, int ncomp_min)
 {

@@ -25,6 +25,22 @@ inline Grid3 make_grid3(int X, int Y, int Z)
     return g;
 }
 
+#ifdef __CUDACC__
+// GELU, tanh form (Hendrycks & Gimpel 2016), and its derivative
+__device__ __forceinline__ float gelu_f(float x)
+{
+    const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
+    return 0.5f * x * (1.f + tanhf(u));
+}
+
+__device__ __forceinline__ float dgelu_f(float x)
+{
+    const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
+    const float t = tanhf(u);
+    return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * 0.7978845608f * (1.f + 3.f * 0.044715f * x * x);
+}
+#endif
+
 // epilogue flags
 constexpr int kGelu = 1;     // forward: out = gelu(acc + bias), aux (if set) = acc + bias
 constexpr int kAccum = 2;    // backward: acc += out (existing gradient)

@@ -3,10 +3,15 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <new>
+#include <vector>
 
 #include "gbp_internal.cuh"
 #include "incflo_gb300.h"
 #include "nn.h"
+#include "nn_unet.h"
+#include "nodal_kernels.h"
+#include "plan.h"
 
 using namespace gbp;
 
@@ -35,6 +40,31 @@ int finish_sync(unsigned* err, cudaStream_t st)
 }
 
 }  // namespace
+
+// One training pair kept on the device: the network input and the normalised target.
+struct SurrogateSample {
+    __nv_bfloat16* x0 = nullptr;
+    float* target = nullptr;
+};
+
+struct gbp_surrogate {
+    nn::UNet net;
+    int dims[3] = {0, 0, 0};  // network grid of the samples
+    int dom[3] = {0, 0, 0};   // unique nodes of the sampled level (the loss domain)
+    std::vector<SurrogateSample> samples;
+    double* scr = nullptr;    // device scratch: statistics, losses
+    double* phi_prev = nullptr;
+    size_t phi_prev_count = 0;
+    ~gbp_surrogate()
+    {
+        for (auto& q : samples) {
+            cudaFree(q.x0);
+            cudaFree(q.target);
+        }
+        if (scr) cudaFree(scr);
+        if (phi_prev) cudaFree(phi_prev);
+    }
+};
 
 extern "C" {
 
@@ -101,6 +131,220 @@ int gbp_nn_conv3d_wgrad(const int dims[3], const void* in, int cin, int ci0, int
     int rc = nn::conv3d_wgrad(L, st);
     if (rc) return rc;
     return finish_sync(err, st);
+}
+
+int gbp_surrogate_create(int base_channels, unsigned long long seed, gbp_surrogate** out)
+{
+    if (!out) {
+        set_error("gbp_surrogate_create: out is NULL");
+        return GBP_BAD_ARG;
+    }
+    *out = nullptr;
+    gbp_surrogate* s = new (std::nothrow) gbp_surrogate();
+    if (!s) {
+        set_error("gbp_surrogate_create: out of host memory");
+        return GBP_BAD_ARG;
+    }
+    int rc = s->net.create(base_channels, seed);
+    if (!rc && cudaMalloc(&s->scr, 64 * sizeof(double)) != cudaSuccess) rc = cuda_fail(cudaGetLastError(), "cudaMalloc");
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return GBP_OK;
+}
+
+int gbp_surrogate_destroy(gbp_surrogate* s)
+{
+    if (s) {
+        cudaDeviceSynchronize();
+        delete s;
+    }
+    return GBP_OK;
+}
+
+long long gbp_surrogate_num_params(const gbp_surrogate* s) { return s ? (long long)s->net.num_params() : 0; }
+
+int gbp_surrogate_get_params(const gbp_surrogate* s, float* host, long long n)
+{
+    if (!s || !host) return GBP_BAD_ARG;
+    return s->net.get_params(host, (size_t)n);
+}
+
+int gbp_surrogate_set_params(gbp_surrogate* s, const float* host, long long n)
+{
+    if (!s || !host) return GBP_BAD_ARG;
+    return s->net.set_params(host, (size_t)n);
+}
+
+int gbp_surrogate_get_grads(const gbp_surrogate* s, float* host, long long n)
+{
+    if (!s || !host) return GBP_BAD_ARG;
+    return s->net.get_grads(host, (size_t)n);
+}
+
+int gbp_surrogate_save(const gbp_surrogate* s, const char* path)
+{
+    if (!s || !path) return GBP_BAD_ARG;
+    return s->net.save(path);
+}
+
+int gbp_surrogate_load(gbp_surrogate* s, const char* path)
+{
+    if (!s || !path) return GBP_BAD_ARG;
+    return s->net.load(path);
+}
+
+int gbp_surrogate_train_pair(gbp_surrogate* s, const int dims[3], const int dom[3], const void* x0,
+                             const float* target, float lr, double* loss, void* stream)
+{
+    if (!s || !dims || !dom || !x0 || !target) {
+        set_error("gbp_surrogate_train_pair: bad arguments");
+        return GBP_BAD_ARG;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = s->net.workspace(dims, true);
+    if (rc) return rc;
+    GBP_CUDA(cudaMemsetAsync(s->scr, 0, sizeof(double), st));
+    GBP_CUDA(cudaMemsetAsync(s->net.err_word(), 0, sizeof(unsigned), st));
+    rc = s->net.forward_backward(static_cast<const __nv_bfloat16*>(x0), target, dom, s->scr, st);
+    if (!rc && lr > 0.f) rc = s->net.adam_step(lr, st);
+    if (rc) return rc;
+    double h = 0.0;
+    GBP_CUDA(cudaMemcpyAsync(&h, s->scr, sizeof(double), cudaMemcpyDeviceToHost, st));
+    rc = finish_sync(s->net.err_word(), st);
+    if (loss) *loss = h;
+    return rc;
+}
+
+int gbp_surrogate_predict(gbp_surrogate* s, const int dims[3], const void* x0, void* hout, void* stream)
+{
+    if (!s || !dims || !x0) {
+        set_error("gbp_surrogate_predict: bad arguments");
+        return GBP_BAD_ARG;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = s->net.workspace(dims, false);
+    if (rc) return rc;
+    GBP_CUDA(cudaMemsetAsync(s->net.err_word(), 0, sizeof(unsigned), st));
+    rc = s->net.forward(static_cast<const __nv_bfloat16*>(x0), st);
+    if (rc) return rc;
+    if (hout) {
+        const nn::Grid3& g = s->net.grid0();
+        GBP_CUDA(cudaMemcpyAsync(hout, s->net.hout(), (size_t)g.R * nn::kHeadC * sizeof(__nv_bfloat16),
+                                 cudaMemcpyDeviceToDevice, st));
+    }
+    return finish_sync(s->net.err_word(), st);
+}
+
+int gbp_surrogate_add_sample(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev)
+{
+    if (!s || !plan || !plan->nodal) {
+        set_error("gbp_surrogate_add_sample: needs a surrogate and a nodal plan after a projection");
+        return GBP_BAD_ARG;
+    }
+    NodalSolver& ns = *plan->nodal;
+    const NodalGeom& g = ns.geom0();
+    cudaStream_t st = ns.stream();
+    int dims[3];
+    nn::net_dims(g, dims);
+    if (!s->samples.empty() && (dims[0] != s->dims[0] || dims[1] != s->dims[1] || dims[2] != s->dims[2])) {
+        set_error("gbp_surrogate_add_sample: all samples must come from plans of the same size");
+        return GBP_BAD_ARG;
+    }
+    const nn::Grid3 g0 = nn::make_grid3(dims[0], dims[1], dims[2]);
+    const double* prev = nullptr;
+    if (phi_prev && phi_prev->data) {
+        if ((size_t)g.count > s->phi_prev_count) {
+            if (s->phi_prev) cudaFree(s->phi_prev);
+            s->phi_prev = nullptr;
+            s->phi_prev_count = 0;
+            GBP_CUDA(cudaMalloc(&s->phi_prev, sizeof(double) * g.count));
+            s->phi_prev_count = g.count;
+        }
+        GBP_CUDA(cudaMemsetAsync(s->phi_prev, 0, sizeof(double) * g.count, st));
+        nodal_load_phi(g, *phi_prev, s->phi_prev, st);
+        prev = s->phi_prev;
+    }
+    SurrogateSample q;
+    GBP_CUDA(cudaMalloc(&q.x0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16)));
+    if (cudaMalloc(&q.target, (size_t)g0.R * sizeof(float)) != cudaSuccess) {
+        cudaFree(q.x0);
+        return cuda_fail(cudaGetLastError(), "cudaMalloc(sample)");
+    }
+    cudaMemsetAsync(q.x0, 0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16), st);
+    cudaMemsetAsync(q.target, 0, (size_t)g0.R * sizeof(float), st);
+    int rc = nn::build_input<double>(g, ns.rhs64(), ns.sigma64(), prev, g0, q.x0, s->scr, st);
+    if (!rc) rc = nn::build_target(g, ns.phi64(), g0, q.target, s->scr + 4, st);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_fail(e, "add_sample");
+    }
+    if (rc) {
+        cudaFree(q.x0);
+        cudaFree(q.target);
+        return rc;
+    }
+    for (int d = 0; d < 3; ++d) {
+        s->dims[d] = dims[d];
+        s->dom[d] = g.nu[d];
+    }
+    s->samples.push_back(q);
+    return GBP_OK;
+}
+
+int gbp_surrogate_num_samples(const gbp_surrogate* s) { return s ? (int)s->samples.size() : 0; }
+
+int gbp_surrogate_clear_samples(gbp_surrogate* s)
+{
+    if (!s) return GBP_BAD_ARG;
+    cudaDeviceSynchronize();
+    for (auto& q : s->samples) {
+        cudaFree(q.x0);
+        cudaFree(q.target);
+    }
+    s->samples.clear();
+    return GBP_OK;
+}
+
+int gbp_surrogate_train(gbp_surrogate* s, int steps, float lr, unsigned long long seed, float* losses, void* stream)
+{
+    if (!s || steps < 0 || s->samples.empty() || steps > 60) {
+        if (!s || s->samples.empty()) set_error("gbp_surrogate_train: no samples");
+        else set_error("gbp_surrogate_train: steps must be 0..60 per call (losses are kept on the device)");
+        return GBP_BAD_ARG;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = s->net.workspace(s->dims, true);
+    if (rc) return rc;
+    GBP_CUDA(cudaMemsetAsync(s->scr, 0, 64 * sizeof(double), st));
+    GBP_CUDA(cudaMemsetAsync(s->net.err_word(), 0, sizeof(unsigned), st));
+    uint64_t x = seed * 0x9E3779B97F4A7C15ull + 1;
+    for (int k = 0; k < steps; ++k) {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        const SurrogateSample& q = s->samples[x % s->samples.size()];
+        rc = s->net.forward_backward(q.x0, q.target, s->dom, s->scr + k, st);
+        if (!rc) rc = s->net.adam_step(lr, st);
+        if (rc) return rc;
+    }
+    double h[64];
+    GBP_CUDA(cudaMemcpyAsync(h, s->scr, 64 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    rc = finish_sync(s->net.err_word(), st);
+    if (losses)
+        for (int k = 0; k < steps; ++k) losses[k] = (float)h[k];
+    return rc;
+}
+
+int gbp_plan_set_surrogate(gbp_plan* plan, gbp_surrogate* s, int level, int mode)
+{
+    if (!plan || !plan->nodal) {
+        set_error("gbp_plan_set_surrogate: needs a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    return plan->nodal->set_surrogate(s ? &s->net : nullptr, level, mode);
 }
 
 }  // extern "C"

@@ -58,19 +58,6 @@ struct ConvParams {
     uint32_t a_bytes, stage_bytes, tmem_cols, idesc;
 };
 
-__device__ __forceinline__ float gelu_f(float x)
-{
-    const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
-    return 0.5f * x * (1.f + tanhf(u));
-}
-
-__device__ __forceinline__ float dgelu_f(float x)
-{
-    const float u = 0.7978845608f * (x + 0.044715f * x * x * x);
-    const float t = tanhf(u);
-    return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * 0.7978845608f * (1.f + 3.f * 0.044715f * x * x);
-}
-
 __device__ __forceinline__ bool row_interior(long long p, int X, int Y, int Z, long long PX, long long PXY)
 {
     const long long z = p / PXY;

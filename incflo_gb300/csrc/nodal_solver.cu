@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "nn_unet.h"
 #include "nodal_solver.h"
 #include "nodal_sweep.h"
 
@@ -103,7 +104,14 @@ void NodalSolver::destroy()
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (ev2) cudaEventDestroy(ev2);
-    ev0 = ev1 = ev2 = nullptr;
+    if (evw) cudaEventDestroy(evw);
+    ev0 = ev1 = ev2 = evw = nullptr;
+    if (net_x0) cudaFree(net_x0);
+    if (net_scr) cudaFree(net_scr);
+    net_x0 = nullptr;
+    net_scr = nullptr;
+    net_x0_bytes = 0;
+    net = nullptr;
     if (pool.base) sweep_forget_maps(pool.base, pool.bytes);
     pool.release();
     L.clear();
@@ -581,6 +589,7 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
         if (stats) stats->status = GBP_NAN;
         return GBP_NAN;
     }
+    // the tolerance refers to the caller's start (zero or the given guess), not to a warm start
     const double ref = opt.always_use_bnorm ? bnorm : rn;
     const double target = std::max(opt.rtol * ref, opt.atol);
     // power-of-two scale that keeps the FP32 inner right-hand side near unit size
@@ -588,6 +597,15 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
         int ex = 0;
         frexp(bnorm * l0.g.vol, &ex);
         scale32 = ldexp(1.0, -ex);
+    }
+    if (stats) {
+        stats->warm_start = 0;
+        stats->warm_rel_resid = 0.0;
+        stats->ms_warm = 0.0;
+    }
+    if (!have_guess && net && net_mode && rn > target) {
+        int rc = warm_start(bnorm, &rn, stats);
+        if (rc) return rc;
     }
     int it = 0;
     int status = GBP_OK;
@@ -643,6 +661,101 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
         fprintf(stderr, "gbp nodal: %s after %d steps, rel resid %.3e\n", status == GBP_OK ? "converged" : "stopped",
                 it, bnorm > 0 ? rn / bnorm : rn);
     return status;
+}
+
+int NodalSolver::set_surrogate(nn::UNet* n, int level, int mode)
+{
+    if (n && (level < 0 || level >= (int)L.size() || !sigma_ready)) {
+        set_error("set_surrogate: level must be a multigrid level of the plan and sigma must be set");
+        return GBP_BAD_ARG;
+    }
+    net = n;
+    net_level = level;
+    net_mode = n ? mode : 0;
+    if (!n) return GBP_OK;
+    int dims[3];
+    nn::net_dims(L[level].g, dims);
+    const size_t need = (size_t)(dims[0] + 2) * (dims[1] + 2) * (dims[2] + 2) * nn::kInC * sizeof(__nv_bfloat16);
+    if (need > net_x0_bytes) {
+        if (net_x0) cudaFree(net_x0);
+        net_x0 = nullptr;
+        net_x0_bytes = 0;
+        GBP_CUDA(cudaMalloc(&net_x0, need));
+        GBP_CUDA(cudaMemset(net_x0, 0, need));
+        net_x0_bytes = need;
+    }
+    if (!net_scr) GBP_CUDA(cudaMalloc(&net_scr, 8 * sizeof(double)));
+    if (!evw) GBP_CUDA(cudaEventCreate(&evw));
+    return net->workspace(dims, false);
+}
+
+// Warm start from the network: restrict the FP32 right-hand side to the network's level, predict,
+// prolong to level 0, scale by the Galerkin factor alpha = x.b / x.Ax (the scaled prediction is
+// the best multiple of x in the energy norm), then take it only if its FP64 residual beats the
+// zero start's. On return phi / res / *rn describe the chosen start.
+int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
+{
+    const NodalLevel& l0 = L[0];
+    const int lv = net_level;
+    const long long nk0 = net->launches();
+    GBP_CUDA(cudaEventRecord(evw, st));
+    launch_rc = 0;
+    nodal_to_f32(l0.g, rhs0, l0.b32, scale32, st);
+    for (int l = 0; l < lv; ++l) nodal_restrict<float>(L[l].g, L[l + 1].g, L[l].b32, L[l + 1].b32, st);
+    int dims[3];
+    nn::net_dims(L[lv].g, dims);
+    int rc = net->workspace(dims, false);
+    if (!rc) rc = nn::build_input<float>(L[lv].g, L[lv].b32, L[lv].s32, nullptr, net->grid0(), net_x0, net_scr, st);
+    if (!rc) rc = net->forward(net_x0, st);
+    if (!rc) rc = nn::extract_output(net->grid0(), net->hout(), L[lv].g, L[lv].x32, st);
+    if (rc) return rc;
+    for (int l = lv - 1; l >= 0; --l) {
+        GBP_CUDA(cudaMemsetAsync(L[l].x32, 0, sizeof(float) * L[l].g.count, st));
+        nodal_prolong_add<float>(L[l].g, L[l + 1].g, L[l + 1].x32, L[l].x32, st);
+    }
+    resid<float>(l0.g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st);
+    if (launch_rc) return launch_rc;
+    rc = nn::node_dot2(l0.g, l0.x32, l0.b32, l0.r32, net_scr, st);
+    if (rc) return rc;
+    double d[2] = {0.0, 0.0};
+    GBP_CUDA(cudaMemcpyAsync(d, net_scr, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    const double xax = d[0] - d[1];  // x.(b - r) = x.Ax in the scaled units of b32
+    const double alpha = (xax > 0.0 && isfinite(d[0])) ? d[0] / xax / scale32 : 0.0;
+    nk += net->launches() - nk0 + 6 + 2 * lv;
+    double rw = bnorm;
+    if (alpha != 0.0) {
+        rc = nn::scale_to64(l0.g.count, l0.x32, alpha, phi, st);
+        if (rc) return rc;
+        resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
+        if (launch_rc) return launch_rc;
+        nk += 2;
+        GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+        rw = bits_to_double(hnorm[1]);
+    }
+    const bool take = alpha != 0.0 && isfinite(rw) && rw < *rn;
+    if (!take) {
+        // bypass: back to the zero start
+        GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
+        GBP_CUDA(cudaMemcpyAsync(res, rhs0, sizeof(double) * l0.g.count, cudaMemcpyDeviceToDevice, st));
+        GBP_CUDA(cudaMemcpyAsync(dnorm + 1, dnorm, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+    } else {
+        *rn = rw;
+    }
+    GBP_CUDA(cudaEventRecord(ev2, st));
+    GBP_CUDA(cudaEventSynchronize(ev2));
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, evw, ev2);
+        stats->warm_start = take ? 1 : 2;
+        stats->warm_rel_resid = bnorm > 0.0 ? rw / bnorm : rw;
+        stats->ms_warm = ms;
+    }
+    if (opt.verbose)
+        fprintf(stderr, "gbp nodal: warm start alpha %.4e, rel resid %.3e (%s)\n", alpha, bnorm > 0 ? rw / bnorm : rw,
+                take ? "used" : "bypassed");
+    return GBP_OK;
 }
 
 int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,

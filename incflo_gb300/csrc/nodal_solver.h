@@ -2,6 +2,7 @@
 // one single-box level (incflo::ApplyNodalProjection, src/projection/incflo_apply_nodal_projection.cpp).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -10,6 +11,10 @@
 #include "nodal_kernels.h"
 
 namespace gbp {
+
+namespace nn {
+class UNet;
+}
 
 struct DevicePool {
     char* base = nullptr;
@@ -61,6 +66,13 @@ public:
     // time `reps` launches of one level-0 kernel (0/1: FP64/FP32 Jacobi, 2/3: FP64/FP32 residual)
     int time_kernel(int which, int reps, double* ms, double* bytes);
 
+    // Learned warm start for zero-guess solves: the network runs on multigrid level `level` (its
+    // prediction is prolonged to level 0 and scaled by the Galerkin factor x.b / x.Ax); mode 0 off,
+    // 1 on. The scaled prediction replaces the zero start only when its residual is smaller.
+    int set_surrogate(nn::UNet* net, int level, int mode);
+    const NodalLevel& level(int l) const { return L[l]; }
+    int num_levels() const { return (int)L.size(); }
+
     double* phi64() const { return phi; }
     double* rhs64() const { return rhs0; }
     double* sigma64() const { return L[0].s64; }
@@ -78,6 +90,7 @@ private:
     void resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
                cudaStream_t s_);
     void record_iteration();
+    int warm_start(double bnorm, double* rn, gbp_stats* stats);
     int run_iteration();
     int build_bottom();
 
@@ -114,6 +127,12 @@ private:
     bool use_tma = true;
     long long nk = 0;            // kernels issued (or replayed through graphs) since reset_count()
     long long step_kernels = 0;  // kernels in one refinement step
+    nn::UNet* net = nullptr;     // warm-start network (not owned)
+    int net_level = 1, net_mode = 0;
+    __nv_bfloat16* net_x0 = nullptr;  // network input tensor
+    size_t net_x0_bytes = 0;
+    double* net_scr = nullptr;   // 8 device doubles: input statistics, Galerkin dot products
+    cudaEvent_t evw = nullptr;
 };
 
 }  // namespace gbp

@@ -1,0 +1,20 @@
+// The object behind the C ABI's gbp_plan handle (shared by the ABI translation units).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "incflo_gb300.h"
+#include "mac_solver.h"
+#include "nodal_solver.h"
+
+struct gbp_plan {
+    int kind;
+    cudaStream_t stream;
+    gbp_geometry geom;
+    int bc_lo[3], bc_hi[3];
+    gbp::NodalSolver* nodal = nullptr;
+    gbp::MacSolver* mac = nullptr;
+    // device staging for the host-buffer entry point
+    double* hbuf = nullptr;
+    size_t hbuf_bytes = 0;
+};

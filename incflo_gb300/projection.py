@@ -168,10 +168,18 @@ class NodalProjector:
         self.phi = None
         self.gradphi = None
         self.stats = None
+        self.surrogate = None
+        self.surrogate_level = 1
 
     def setDomainBC(self, lo, hi):  # noqa: N802 (reference name)
         self.bc_lo = tuple(LinOpBCType.get(b, b) for b in lo)
         self.bc_hi = tuple(LinOpBCType.get(b, b) for b in hi)
+
+    def setSurrogate(self, surrogate, level: int = 1):  # noqa: N802 (no reference counterpart)
+        """Learned warm start for zero-guess solves (incflo_gb300.surrogate.Surrogate), evaluated on
+        multigrid level ``level``; None detaches it."""
+        self.surrogate = surrogate
+        self.surrogate_level = int(level)
 
     def _plan(self) -> _Plan:
         if self.bc_lo is None:
@@ -197,6 +205,10 @@ class NodalProjector:
             A.check(L.gbp_nodal_set_sigma(plan.ptr, _ref(array4(self.sigma)), 0.0), "gbp_nodal_set_sigma")
         else:
             A.check(L.gbp_nodal_set_sigma(plan.ptr, None, float(self.sigma)), "gbp_nodal_set_sigma")
+        # plans are shared between projectors of one geometry: (re)state the warm start every call
+        s = self.surrogate
+        A.check(L.gbp_plan_set_surrogate(plan.ptr, s.ptr if s is not None else None, self.surrogate_level,
+                                         int(s is not None)), "gbp_plan_set_surrogate")
         n = self.geom.n_cell
         dev = self.vel.device
         if phi_guess is not None:

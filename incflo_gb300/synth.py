@@ -54,7 +54,7 @@ def gaussian_random_field(n, seed, slope=-2.0, ncomp=3):
     for c in range(ncomp):
         white = rng.standard_normal((n[2], n[1], n[0]))
         f = np.fft.rfftn(white) * amp
-        out[c] = np.fft.irfftn(f, s=(n[2], n[1], n[0]))
+        out[c] = np.fft.irfftn(f, s=(n[2], n[1], n[0]), axes=(0, 1, 2))
     out -= out.mean(axis=(1, 2, 3), keepdims=True)
     out /= np.sqrt(np.mean(np.sum(out * out, axis=0)))
     return out

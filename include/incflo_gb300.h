@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define GBP_ABI_VERSION 1
+#define GBP_ABI_VERSION 2
 
 typedef enum {
     GBP_OK = 0,
@@ -109,6 +109,9 @@ typedef struct {
     double ms_total;             /* device time of the whole call, CUDA events */
     double ms_solve;             /* device time of the solve alone */
     long long kernel_launches;   /* kernels this call ran on the device (graph nodes included) */
+    int warm_start;              /* learned warm start: 0 not attached, 1 used, 2 bypassed */
+    double warm_rel_resid;       /* residual of the scaled prediction / rhs_norm (when attempted) */
+    double ms_warm;              /* device time of the warm start (network + scaling + residual) */
 } gbp_stats;
 
 typedef struct gbp_plan gbp_plan;
@@ -243,6 +246,41 @@ int gbp_nn_conv3d(const int dims[3], int nin, void* const in[], const int cin[],
 /* dw[t][o][ci0 + c] += sum_p gout[p][o] in[p + off(t)][c], FP32 dw [ntaps][cout][cin_tot]. */
 int gbp_nn_conv3d_wgrad(const int dims[3], const void* in, int cin, int ci0, int cin_tot,
                         const void* gout, int cout, int ntaps, float* dw, void* stream);
+
+/* ---- learned warm start (surrogate U-Net) ----------------------------------------------
+ * A four-level 3-D U-Net (16/32/64/128 channels, 3x3x3 convolutions + GELU, ~1.5 M
+ * parameters) that predicts the shape of phi from the nodal right-hand side, the node-averaged
+ * sigma and (optionally) the previous phi. Trained on the GPU with Adam on pairs produced by this
+ * library's own solver; attached to a nodal plan it supplies the initial guess of zero-guess
+ * solves, scaled by the Galerkin factor x.b / x.Ax, and is bypassed when the scaled guess has a
+ * larger residual than the zero start (stats.warm_start = 2). No reference counterpart. */
+typedef struct gbp_surrogate gbp_surrogate;
+int gbp_surrogate_create(int base_channels, unsigned long long seed, gbp_surrogate** out);
+int gbp_surrogate_destroy(gbp_surrogate* s);
+long long gbp_surrogate_num_params(const gbp_surrogate* s);
+int gbp_surrogate_get_params(const gbp_surrogate* s, float* host, long long n);
+int gbp_surrogate_set_params(gbp_surrogate* s, const float* host, long long n);
+int gbp_surrogate_get_grads(const gbp_surrogate* s, float* host, long long n);
+int gbp_surrogate_save(const gbp_surrogate* s, const char* path);
+int gbp_surrogate_load(gbp_surrogate* s, const char* path);
+/* one forward + backward (+ Adam step when lr > 0) on a device input [R][16] BF16 and target
+ * [R] FP32 over a network grid dims (multiples of 8); loss over voxels below dom */
+int gbp_surrogate_train_pair(gbp_surrogate* s, const int dims[3], const int dom[3], const void* x0,
+                             const float* target, float lr, double* loss, void* stream);
+/* forward pass; hout (device, [R][16] BF16, channel 0 = prediction) may be NULL */
+int gbp_surrogate_predict(gbp_surrogate* s, const int dims[3], const void* x0, void* hout,
+                          void* stream);
+/* append a training pair from a nodal plan after gbp_nodal_project: input from the plan's
+ * right-hand side, sigma and phi_prev (nodal, may be NULL), target = the plan's phi */
+int gbp_surrogate_add_sample(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev);
+int gbp_surrogate_num_samples(const gbp_surrogate* s);
+int gbp_surrogate_clear_samples(gbp_surrogate* s);
+/* steps (<= 60 per call) Adam steps on randomly drawn samples; losses[steps] (host) may be NULL */
+int gbp_surrogate_train(gbp_surrogate* s, int steps, float lr, unsigned long long seed,
+                        float* losses, void* stream);
+/* attach (s != NULL) or detach a surrogate: the network runs on multigrid level `level` of the
+ * plan (0 = finest); mode 1 = use with the bypass rule, 0 = off */
+int gbp_plan_set_surrogate(gbp_plan* plan, gbp_surrogate* s, int level, int mode);
 
 #ifdef __cplusplus
 }

@@ -171,8 +171,9 @@ def test_conv_weight_gradient_matches_torch(gpu_lib, cin, cout, ntaps):
     ref = ref.permute(2, 3, 4, 0, 1).reshape(ntaps, cout, cin)
     # write into the second half of a wider dw (channel offset ci0 = cin of a concatenated input)
     dw = torch.zeros(ntaps, cout, 2 * cin, device="cuda")
-    rc = gpu_lib.gbp_nn_conv3d_wgrad(ints(dims), ctypes.c_void_p(pad_cl(x).data_ptr()), cin, cin, 2 * cin,
-                                     ctypes.c_void_p(pad_cl(g).data_ptr()), cout, ntaps,
+    xp, gp = pad_cl(x), pad_cl(g)  # keep both alive across the call
+    rc = gpu_lib.gbp_nn_conv3d_wgrad(ints(dims), ctypes.c_void_p(xp.data_ptr()), cin, cin, 2 * cin,
+                                     ctypes.c_void_p(gp.data_ptr()), cout, ntaps,
                                      ctypes.c_void_p(dw.data_ptr()),
                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == 0, gpu_lib.gbp_last_error().decode()
