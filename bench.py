@@ -203,7 +203,15 @@ def run_ours(args, ws, rank, local):
     p_nd = torch.zeros((n + 1, n + 1, n + 1), dtype=torch.float64, device=dev)
     lib = _abi.load()
 
-    def run_form(precision, steps, warmup):
+    surrogate = None
+    if not args.no_warm_start:
+        from incflo_gb300.surrogate import WEIGHTS, Surrogate
+
+        if not os.path.exists(WEIGHTS):
+            raise RuntimeError(f"{WEIGHTS} is missing: train it with python -m incflo_gb300.train_surrogate")
+        surrogate = Surrogate(path=WEIGHTS)
+
+    def run_form(precision, steps, warmup, sur=None):
         opts = make_options(0, precision=precision, mg_rtol=args.rtol, mg_atol=0.0,
                             ir_inner_cycles=args.inner)
         stream = torch.cuda.current_stream()
@@ -220,7 +228,8 @@ def run_ours(args, ws, rank, local):
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             st = apply_nodal_projection(geom, bclo, bchi, vel, rho, gp, p_nd, scaling_factor=1.0, incremental=False,
-                                        set_inflow_bc=False, options=opts)
+                                        set_inflow_bc=False, options=opts, surrogate=sur,
+                                        surrogate_level=args.warm_level)
             e1.record(stream)
             if st["status"] != 0:
                 raise RuntimeError(f"projection failed: {st}")
@@ -235,8 +244,19 @@ def run_ours(args, ws, rank, local):
 
     sampler = ClockSampler(local)
     sampler.start()
-    ms_mixed, st_mixed, wall_mixed = run_form("mixed", args.steps, args.warmup)
+    ms_mixed, st_mixed, wall_mixed = run_form("mixed", args.steps, args.warmup, surrogate)
     clocks = sampler.stop()
+    warm = None
+    if surrogate is not None:
+        codes = [s_["warm_start"] for s_ in st_mixed]
+        attempted = [s_ for s_ in st_mixed if s_["warm_start"] in (1, 2)]
+        ms_plain_mixed, st_plain_mixed, _ = run_form("mixed", max(1, min(args.steps, 5)), 1)
+        warm = {"network_level": args.warm_level, "used": codes.count(1), "bypassed": codes.count(2),
+                "skipped": codes.count(3),
+                "warm_rel_resid": attempted[0]["warm_rel_resid"] if attempted else None,
+                "ms_warm_attempt": round(attempted[0]["ms_warm"], 3) if attempted else None,
+                "mixed_without_warm_start_ms": round(sum(ms_plain_mixed) / len(ms_plain_mixed), 4),
+                "mixed_without_warm_start_vcycles": st_plain_mixed[0]["vcycles"]}
     ms_fp64, st_fp64, wall_fp64 = run_form("fp64", max(1, min(args.steps, args.fp64_steps)), 1)
 
     tot_mixed = allreduce_max(ws, sum(ms_mixed))
@@ -269,6 +289,8 @@ def run_ours(args, ws, rank, local):
         p_h = torch.zeros((n + 1, n + 1, n + 1), dtype=torch.float64).pin_memory()
         hplan = _Plan(geom, _abi.GBP_NODAL, bclo, bchi,
                       make_options(0, precision="mixed", mg_rtol=args.rtol, mg_atol=0.0, ir_inner_cycles=args.inner))
+        if surrogate is not None:
+            _abi.check(lib.gbp_plan_set_surrogate(hplan.ptr, surrogate.ptr, args.warm_level, 1), "set_surrogate")
         times = []
         for i in range(1 + args.e2e_steps):
             vel_h.numpy()[...] = vel_h0
@@ -302,7 +324,8 @@ def run_ours(args, ws, rank, local):
         "data": "synthetic (seeded PCG64)",
         "config": {"workload": f"variable-density nodal projection {n}^3 (rho 1->3 tanh interface, k^-2 random "
                                f"velocity), periodic x/y, walls z, sigma=1/rho, rtol {args.rtol:g}",
-                   "n": n, "form": "FP32 V-cycles inside FP64 iterative refinement (learned warm start: not yet)",
+                   "n": n, "form": ("learned warm start (U-Net on multigrid level 1, bypass rule) + " if surrogate
+                                    else "") + "FP32 V-cycles inside FP64 iterative refinement",
                    "ir_inner_cycles": args.inner, "l2": "inputs larger than L2 (no flush)",
                    "parallelism": f"replicas x{ws}"},
         "plain_fp64": {"ms_per_projection": round(fp64_ms, 3), "vcycles": st_fp64[0]["vcycles"],
@@ -310,6 +333,7 @@ def run_ours(args, ws, rank, local):
         "chosen": {"vcycles": st_mixed[0]["vcycles"], "outer_iters": st_mixed[0]["outer_iters"],
                    "final_rel_resid": st_mixed[0]["final_rel_resid"],
                    "speedup_vs_plain_fp64": round(fp64_ms / per_step, 3)},
+        "warm_start": warm,
         "wall_ms_per_step": round(wall_mixed * 1e3 / len(ms_mixed), 3),
         "roofline": {"bound": "hbm", "kernel": "k_sweep32t<0> (FP32 Jacobi sweep, level 0)", "achieved": round(ach, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
@@ -334,11 +358,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--inner", type=int, default=4)
+    ap.add_argument("--inner", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-warm-start", action="store_true")
+    ap.add_argument("--warm-level", type=int, default=1)
     args = ap.parse_args()
     ws, rank, local = dist_init()
     if args.impl == "reference":

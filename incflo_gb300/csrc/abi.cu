@@ -13,6 +13,8 @@
 #include "mac_solver.h"
 #include "nodal_solver.h"
 #include "plan.h"
+#include "cc_projection.h"
+#include "solvability.h"
 
 namespace gbp {
 
@@ -102,7 +104,7 @@ int gbp_options_default(int kind, gbp_options* o)
     o->nu1 = 2;
     o->nu2 = 2;
     o->omega = 0.85;
-    o->ir_inner_cycles = 4;
+    o->ir_inner_cycles = 5;
     o->use_graphs = 1;
     o->always_use_bnorm = 1;
     return GBP_OK;
@@ -266,6 +268,8 @@ int gbp_plan_destroy(gbp_plan* p)
     delete p->nodal;
     delete p->mac;
     if (p->hbuf) cudaFree(p->hbuf);
+    if (p->dflux) cudaFree(p->dflux);
+    if (p->ccbuf) cudaFree(p->ccbuf);
     delete p;
     return GBP_OK;
 }
@@ -522,6 +526,125 @@ int gbp_mac_project(gbp_plan* p, gbp_array4* ux, gbp_array4* uy, gbp_array4* uz,
     }
     if (stats) memset(stats, 0, sizeof(*stats));
     return p->mac->project(u, phi, phi_guess, stats);
+}
+
+int gbp_apply_cc_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
+                            double rho0, gbp_array4* gp, gbp_array4* p_cc, gbp_array4* umac_x, gbp_array4* umac_y,
+                            gbp_array4* umac_z, double time, double dt, double prev_dt, double scaling_factor,
+                            int incremental, int set_inflow_bc, gbp_stats* stats)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_apply_cc_projection: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    // incflo_apply_cc_projection.cpp:212: the small-dt form projects (U* - U^n + dt Gp)
+    const bool small_dt = time > 0.0 && dt < 0.1 * prev_dt;
+    const bool sub_old = small_dt || incremental;
+    int rc = check_vel(p, vel, true);
+    if (rc) return rc;
+    if (sub_old && (rc = check_cells(p, vel_old, 3, "vel_old"))) return rc;
+    if (gp && (rc = check_cells(p, gp, 3, "gp"))) return rc;
+    if (p_cc && (rc = check_cells(p, p_cc, 1, "p_cc"))) return rc;
+    if (!incremental && !gp) {
+        set_error("gbp_apply_cc_projection: gp is required (its add-back is part of the projection)");
+        return GBP_BAD_ARG;
+    }
+    if (!(scaling_factor > 0.0) || (!rho && !(rho0 > 0.0))) {
+        set_error("gbp_apply_cc_projection: scaling_factor and rho0 must be positive");
+        return GBP_BAD_ARG;
+    }
+    if (rho) {
+        int lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = p->bc_lo[d] == GBP_BC_DIRICHLET ? -1 : 0;
+            hi[d] = p->geom.n_cell[d] - 1 + (p->bc_hi[d] == GBP_BC_DIRICHLET ? 1 : 0);
+        }
+        if (!valid_array(rho, 1) || !covers(rho, lo, hi)) {
+            set_error("gbp_apply_cc_projection: rho must cover the cells and one ghost across Dirichlet faces");
+            return GBP_BAD_ARG;
+        }
+    }
+    gbp_array4* u[3] = {umac_x, umac_y, umac_z};
+    for (int d = 0; d < 3; ++d) {
+        int lo[3] = {0, 0, 0};
+        int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+        hi[d] += 1;
+        if (!valid_array(u[d], 1) || !covers(u[d], lo, hi)) {
+            set_error("gbp_apply_cc_projection: each umac array must cover its faces 0..n");
+            return GBP_BAD_ARG;
+        }
+    }
+    if (!p->ccbuf) GBP_CUDA(cudaMalloc(&p->ccbuf, cc_scratch_doubles(p->geom) * sizeof(double)));
+    CcArgs a{};
+    a.vel = *vel;
+    if (sub_old) a.vel_old = *vel_old;
+    if (rho) a.rho = *rho;
+    if (gp) a.gp = *gp;
+    if (p_cc) a.p_cc = *p_cc;
+    a.rho0 = rho0;
+    a.s = scaling_factor;
+    a.add_gp = !incremental;
+    a.sub_old = sub_old;
+    a.use_inflow = set_inflow_bc && !sub_old;
+    a.incremental = incremental;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    return cc_projection(p->geom, p->bc_lo, p->bc_hi, a, u, p->ccbuf, *p->mac, stats, p->stream);
+}
+
+static int plan_flux(gbp_plan* p)
+{
+    if (!p->dflux) GBP_CUDA(cudaMalloc(&p->dflux, 2 * sizeof(double)));
+    return GBP_OK;
+}
+
+int gbp_enforce_inout_solvability(gbp_plan* p, gbp_array4* vel, const int dd_lo[3], const int dd_hi[3],
+                                  double* inflow_outflow)
+{
+    if (!p || !dd_lo || !dd_hi || !valid_array(vel, 3)) {
+        set_error("gbp_enforce_inout_solvability: plan, 3-component vel and dd_lo/dd_hi are required");
+        return GBP_BAD_ARG;
+    }
+    const int lo[3] = {-1, -1, -1};
+    const int hi[3] = {p->geom.n_cell[0], p->geom.n_cell[1], p->geom.n_cell[2]};
+    if (!covers(vel, lo, hi)) {
+        set_error("gbp_enforce_inout_solvability: vel must hold one ghost layer");
+        return GBP_BAD_ARG;
+    }
+    int rc = plan_flux(p);
+    if (!rc) rc = enforce_inout_cell(p->geom, dd_lo, dd_hi, *vel, p->dflux, p->stream);
+    if (!rc && inflow_outflow) {
+        GBP_CUDA(cudaMemcpyAsync(inflow_outflow, p->dflux, 2 * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+        GBP_CUDA(cudaStreamSynchronize(p->stream));
+    }
+    return rc;
+}
+
+int gbp_mac_enforce_inout_solvability(gbp_plan* p, gbp_array4* ux, gbp_array4* uy, gbp_array4* uz,
+                                      const int dd_lo[3], const int dd_hi[3], double* inflow_outflow)
+{
+    gbp_array4* u[3] = {ux, uy, uz};
+    if (!p || !dd_lo || !dd_hi) {
+        set_error("gbp_mac_enforce_inout_solvability: plan and dd_lo/dd_hi are required");
+        return GBP_BAD_ARG;
+    }
+    gbp_array4 uu[3];
+    for (int d = 0; d < 3; ++d) {
+        int lo[3] = {0, 0, 0};
+        int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+        hi[d] += 1;
+        if (!valid_array(u[d], 1) || !covers(u[d], lo, hi)) {
+            set_error("gbp_mac_enforce_inout_solvability: face arrays must cover faces 0..n");
+            return GBP_BAD_ARG;
+        }
+        uu[d] = *u[d];
+    }
+    int rc = plan_flux(p);
+    if (!rc) rc = enforce_inout_faces(p->geom, dd_lo, dd_hi, uu, p->dflux, p->stream);
+    if (!rc && inflow_outflow) {
+        GBP_CUDA(cudaMemcpyAsync(inflow_outflow, p->dflux, 2 * sizeof(double), cudaMemcpyDeviceToHost, p->stream));
+        GBP_CUDA(cudaStreamSynchronize(p->stream));
+    }
+    return rc;
 }
 
 int gbp_plan_time_kernel(gbp_plan* p, int which, int reps, double* ms_per_launch, double* bytes_per_launch)

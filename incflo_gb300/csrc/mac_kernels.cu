@@ -240,6 +240,13 @@ __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double
     f[0] = (int)(rem - (long long)f[1] * fn[0]);
     const int fd = f[d];
     const bool per = g.per[d];
+    const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
+    if (!per && (fd == 0 || fd == g.n[d]) && (fd == 0 ? bclo : bchi) != GBP_BC_DIRICHLET) {
+        // wall / inflow face: no flux through it, and no ghost value is read
+        b64[p] = 0.0;
+        b32[p] = 0.f;
+        return;
+    }
     double beta;
     int q[3] = {f[0], f[1], f[2]};
     if (per && fd == g.n[d]) q[d] = 0;  // face n is face 0
@@ -253,12 +260,8 @@ __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double
         if (per && lo[d] < 0) lo[d] += g.n[d];
         beta = cval / (0.5 * (a4(src, lo[0], lo[1], lo[2], 0) + a4(src, q[0], q[1], q[2], 0)));
     }
-    double eff = beta;
-    if (!per && (fd == 0 || fd == g.n[d])) {
-        const int bc = fd == 0 ? bclo : bchi;
-        eff = bc == GBP_BC_DIRICHLET ? 2.0 * beta : 0.0;
-    }
-    const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
+    // Dirichlet face: the ghost value sits half a cell out, so the face weight doubles
+    const double eff = (!per && (fd == 0 || fd == g.n[d])) ? 2.0 * beta : beta;
     b64[p] = eff;
     b32[p] = (float)eff;
 }

@@ -95,8 +95,7 @@ static NodalGeom make_geom(const int n[3], const double h[3], const int per[3], 
 
 void NodalSolver::destroy()
 {
-    if (gexec) cudaGraphExecDestroy(gexec);
-    gexec = nullptr;
+    drop_graphs();
     if (hnorm) cudaFreeHost(hnorm);
     hnorm = nullptr;
     if (cap) cudaStreamDestroy(cap);
@@ -132,9 +131,8 @@ int NodalSolver::set_options(const gbp_options& o)
     const int maxc = opt.max_coarsening_level;
     opt = o;
     opt.max_coarsening_level = maxc;  // hierarchy depth is fixed at plan creation
-    if (regraph && gexec) {
-        cudaGraphExecDestroy(gexec);
-        gexec = nullptr;
+    if (regraph) {
+        drop_graphs();
     }
     return GBP_OK;
 }
@@ -493,8 +491,17 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     xres[l] = x;
 }
 
+void NodalSolver::drop_graphs()
+{
+    for (auto& g : gexec) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+}
+
 // one refinement step, issued on cap_or_st: V-cycle(s) on res, phi += e, res = g - A phi, norm
-void NodalSolver::record_iteration()
+// (m: FP32 V-cycles of the mixed form's inner solve)
+void NodalSolver::record_iteration(int m)
 {
     const NodalLevel& l0 = L[0];
     const cudaStream_t s = cap_or_st;
@@ -502,7 +509,7 @@ void NodalSolver::record_iteration()
     if (opt.precision == GBP_PREC_MIXED) {
         nodal_to_f32(l0.g, res, l0.b32, scale32, s);
         vcycle<float>(0, l0.b32, true);
-        for (int c = 1; c < opt.ir_inner_cycles; ++c) vcycle<float>(0, l0.b32, false);
+        for (int c = 1; c < m; ++c) vcycle<float>(0, l0.b32, false);
         nodal_add_correction<float>(l0.g, phi, (const float*)xres[0], 1.0 / scale32, s);
         ++nk;
     } else {
@@ -516,21 +523,25 @@ void NodalSolver::record_iteration()
     step_kernels = nk - nk0;
 }
 
-int NodalSolver::run_iteration()
+int NodalSolver::run_iteration(int m)
 {
     if (!opt.use_graphs) {
         cap_or_st = st;
-        record_iteration();
+        record_iteration(m);
         GBP_CUDA(cudaGetLastError());
         return GBP_OK;
     }
-    if (!gexec || gexec_prec != opt.precision || gexec_scale != scale32) {
-        if (gexec) cudaGraphExecDestroy(gexec);
-        gexec = nullptr;
+    if (gexec_prec != opt.precision || gexec_scale != scale32) {
+        drop_graphs();
+        gexec_prec = opt.precision;
+        gexec_scale = scale32;
+    }
+    cudaGraphExec_t& ge = gexec[m];
+    if (!ge) {
         cudaGraph_t graph = nullptr;
         cap_or_st = cap;
         GBP_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        record_iteration();
+        record_iteration(m);
         cudaError_t e = cudaStreamEndCapture(cap, &graph);
         cap_or_st = st;
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(refinement step)");
@@ -538,18 +549,17 @@ int NodalSolver::run_iteration()
             cudaGraphDestroy(graph);
             return launch_rc;
         }
-        e = cudaGraphInstantiate(&gexec, graph, 0);
+        e = cudaGraphInstantiate(&ge, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
-            gexec = nullptr;
+            ge = nullptr;
             return cuda_fail(e, "cudaGraphInstantiate(refinement step)");
         }
-        gexec_prec = opt.precision;
-        gexec_scale = scale32;
         nk -= step_kernels;  // capture issued nothing; the launch below runs them
+        step_kernels_m[m] = step_kernels;
     }
-    GBP_CUDA(cudaGraphLaunch(gexec, st));
-    nk += step_kernels;
+    GBP_CUDA(cudaGraphLaunch(ge, st));
+    nk += step_kernels_m[m];
     return GBP_OK;
 }
 
@@ -604,22 +614,41 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
         stats->ms_warm = 0.0;
     }
     if (!have_guess && net && net_mode && rn > target) {
-        int rc = warm_start(bnorm, &rn, stats);
-        if (rc) return rc;
+        if (warm_skip > 0) {
+            // the last attempts were all bypassed: do not pay for the network on this solve
+            --warm_skip;
+            if (stats) stats->warm_start = 3;
+        } else {
+            int rc = warm_start(bnorm, &rn, stats);
+            if (rc) return rc;
+        }
     }
-    int it = 0;
+    int it = 0, vcycles = 0;
     int status = GBP_OK;
     const double r0 = rn;
+    const bool mixed = opt.precision == GBP_PREC_MIXED;
+    const int mmax = std::min(opt.ir_inner_cycles, kMaxInner);
+    int m = mixed ? mmax : 1;
     while (rn > target) {
         if (it >= opt.maxiter) {
             status = GBP_NOT_CONVERGED;
             break;
         }
-        int rc = run_iteration();
+        int rc = run_iteration(m);
         if (rc) return rc;
         GBP_CUDA(cudaStreamSynchronize(st));
+        const double rprev = rn;
         rn = bits_to_double(hnorm[1]);
         ++it;
+        vcycles += m;
+        if (mixed && rn > target && rn < rprev && rn > 0.0) {
+            // next inner solve: as many V-cycles as the observed per-cycle contraction says the
+            // remaining reduction needs (+1/4 cycle of margin), capped by ir_inner_cycles and by
+            // what an FP32 inner solve can deliver (about 1e-6 of its right-hand side)
+            const double rho = std::min(0.9, std::max(1e-3, pow(rn / rprev, 1.0 / m)));
+            const double need = log(std::max(target / rn, 1e-6)) / log(rho);
+            m = std::max(1, std::min(mmax, (int)ceil(need + 0.25)));
+        }
         if (opt.verbose > 1) fprintf(stderr, "gbp nodal: iter %d rel resid %.3e\n", it, bnorm > 0 ? rn / bnorm : rn);
         if (!isfinite(rn)) {
             status = GBP_NAN;
@@ -647,7 +676,7 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
     if (stats) {
         stats->status = status;
         stats->outer_iters = it + 1;
-        stats->vcycles = it * (opt.precision == GBP_PREC_MIXED ? opt.ir_inner_cycles : 1);
+        stats->vcycles = vcycles;
         stats->num_levels = (int)L.size();
         stats->rhs_norm = bnorm;
         stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;
@@ -665,10 +694,11 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
 
 int NodalSolver::set_surrogate(nn::UNet* n, int level, int mode)
 {
-    if (n && (level < 0 || level >= (int)L.size() || !sigma_ready)) {
-        set_error("set_surrogate: level must be a multigrid level of the plan and sigma must be set");
+    if (n && (level < 0 || level >= (int)L.size())) {
+        set_error("set_surrogate: level must be a multigrid level of the plan");
         return GBP_BAD_ARG;
     }
+    if (n != net || level != net_level) warm_streak = warm_skip = 0;
     net = n;
     net_level = level;
     net_mode = n ? mode : 0;
@@ -735,6 +765,12 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
         rw = bits_to_double(hnorm[1]);
     }
     const bool take = alpha != 0.0 && isfinite(rw) && rw < *rn;
+    // two bypasses in a row: skip the next 16 attempts, then try again
+    warm_streak = take ? 0 : warm_streak + 1;
+    if (warm_streak >= 2) {
+        warm_skip = 16;
+        warm_streak = 0;
+    }
     if (!take) {
         // bypass: back to the zero start
         GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));

@@ -39,6 +39,8 @@ struct NodalLevel {
 
 class NodalSolver {
 public:
+    static constexpr int kMaxInner = 8;  // FP32 V-cycles per refinement step, at most
+
     int init(const gbp_geometry& geom, const int bc_lo[3], const int bc_hi[3], const gbp_options& opt,
              cudaStream_t stream);
     void destroy();
@@ -89,9 +91,10 @@ private:
     template <typename T>
     void resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
                cudaStream_t s_);
-    void record_iteration();
+    void record_iteration(int m);
     int warm_start(double bnorm, double* rn, gbp_stats* stats);
-    int run_iteration();
+    void drop_graphs();
+    int run_iteration(int m);
     int build_bottom();
 
     gbp_options opt{};
@@ -113,7 +116,7 @@ private:
     double scale32 = 1.0;
     // result buffer of each level's V-cycle (ping-pong aware)
     void* xres[kMaxLevels] = {};
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec[kMaxInner + 1] = {};  // one refinement-step graph per inner-cycle count
     int gexec_prec = -1;
     double gexec_scale = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
@@ -126,13 +129,16 @@ private:
     int launch_rc = 0;           // first failure while issuing a sweep (tensor-map encoding)
     bool use_tma = true;
     long long nk = 0;            // kernels issued (or replayed through graphs) since reset_count()
-    long long step_kernels = 0;  // kernels in one refinement step
+    long long step_kernels = 0;  // kernels in one refinement step (the last one recorded)
+    long long step_kernels_m[kMaxInner + 1] = {};
     nn::UNet* net = nullptr;     // warm-start network (not owned)
     int net_level = 1, net_mode = 0;
     __nv_bfloat16* net_x0 = nullptr;  // network input tensor
     size_t net_x0_bytes = 0;
     double* net_scr = nullptr;   // 8 device doubles: input statistics, Galerkin dot products
     cudaEvent_t evw = nullptr;
+    int warm_streak = 0;         // consecutive bypassed warm starts
+    int warm_skip = 0;           // solves left before the next attempt after a streak
 };
 
 }  // namespace gbp

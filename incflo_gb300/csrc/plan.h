@@ -17,4 +17,6 @@ struct gbp_plan {
     // device staging for the host-buffer entry point
     double* hbuf = nullptr;
     size_t hbuf_bytes = 0;
+    double* dflux = nullptr;  // 2 device doubles: inflow / outflow of the solvability fix
+    double* ccbuf = nullptr;  // cell-centred projection scratch (unprojected face velocities, phi)
 };

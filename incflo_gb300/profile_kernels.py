@@ -2,9 +2,15 @@
 
   python -m incflo_gb300.profile_kernels --n 256 --which 1 --reps 3
 
-which: 0 FP64 Jacobi sweep, 1 FP32 Jacobi sweep, 2 FP64 residual, 3 FP32 residual. The plan holds the
-256^3 variable-density workload's sigma (periodic x/y, walls z); the only launches of the selected
-kernel are the level-0 ones, so `ncu -k regex:<kernel>` captures exactly those.
+which: 0 FP64 Jacobi sweep, 1 FP32 Jacobi sweep, 2 FP64 residual, 3 FP32 residual, 4 streaming triad
+over the same arrays. The plan holds the 256^3 variable-density workload's sigma (periodic x/y,
+walls z); the only launches of the selected kernel are the level-0 ones, so `ncu -k regex:<kernel>`
+captures exactly those.
+
+  python -m incflo_gb300.profile_kernels --unet 128 --reps 5
+
+times the warm-start U-Net's forward pass (tensor-core convolutions) on a 128 x 128 x 136 network
+grid (the multigrid level 1 of a 256^3 projection) and reports the convolution FLOP rate.
 """
 from __future__ import annotations
 
@@ -30,11 +36,14 @@ def main():
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--which", type=int, default=1)
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--unet", type=int, default=0, help="time the U-Net forward on an n x n x (n+8) grid")
     args = ap.parse_args()
     from incflo_gb300.build import build
 
     build()
     lib = _abi.load()
+    if args.unet:
+        return unet_forward(args.unet, args.reps)
     n = args.n
     rho = synth.variable_density_rt(n)["rho"]
     geom = Geometry((n, n, n))
@@ -45,6 +54,33 @@ def main():
     _abi.check(lib.gbp_plan_time_kernel(plan.ptr, args.which, args.reps, ctypes.byref(ms), ctypes.byref(by)), "time")
     print(json.dumps({"which": args.which, "n": n, "ms_per_launch": ms.value, "bytes_per_launch": by.value,
                       "GBps": by.value / ms.value / 1e6}))
+
+
+def unet_forward(n, reps):
+    from incflo_gb300.surrogate import Surrogate
+    from oracle import unet as U  # layer shapes only (for the FLOP count)
+
+    dims = (n, n, n + 8)
+    rows = (dims[0] + 2) * (dims[1] + 2) * (dims[2] + 2)
+    s = Surrogate(seed=0)
+    x0 = torch.zeros((rows, 16), dtype=torch.bfloat16, device="cuda")
+    x0[:, :3] = torch.randn((rows, 3), device="cuda").to(torch.bfloat16)
+    s.predict(x0, dims)  # workspace, weights, warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        s.predict(x0, dims)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    # conv FLOPs: 2 x voxels x taps x cin x cout per layer on its level's grid
+    flops, vox = 0.0, dims[0] * dims[1] * dims[2]
+    spec = U.layer_specs()
+    lv = [0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0, 0]
+    for (nin, c0, c1, co, t), l in zip(spec, lv):
+        flops += 2.0 * vox / 8 ** l * t * (c0 + c1) * co
+    print(json.dumps({"unet_forward_ms": ms, "dims": dims, "gflop": flops / 1e9, "tflops": flops / ms / 1e9}))
 
 
 if __name__ == "__main__":

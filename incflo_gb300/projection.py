@@ -230,12 +230,25 @@ class NodalProjector:
     def getGradPhi(self):  # noqa: N802
         return self.gradphi
 
+    def enforceInOutSolvability(self, dd_lo, dd_hi):  # noqa: N802
+        """HydroUtils::enforceInOutSolvability on this projector's velocity (whose boundary ghost
+        cells hold the boundary values) for the direction_dependent faces marked in dd_lo / dd_hi
+        (incflo_apply_nodal_projection.cpp:166-179). Returns (inflow, outflow) before scaling."""
+        plan = self._plan()
+        io = (ctypes.c_double * 2)()
+        A.check(A.load().gbp_enforce_inout_solvability(plan.ptr, _ref(array4(self.vel, self.ng)),
+                                                       (ctypes.c_int * 3)(*dd_lo), (ctypes.c_int * 3)(*dd_hi), io),
+                "gbp_enforce_inout_solvability")
+        return io[0], io[1]
+
 
 def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd, *, time=0.0, dt=1.0,
                            prev_dt=1.0, scaling_factor=1.0, incremental=False, set_inflow_bc=True,
                            vel_old=None, rho0=1.0, ng=1, options: A.Options | None = None, stream=None,
-                           constant_density=False):
-    """incflo::ApplyNodalProjection for one level, fused on the device; returns the stats dict."""
+                           constant_density=False, surrogate=None, surrogate_level=1):
+    """incflo::ApplyNodalProjection for one level, fused on the device; returns the stats dict.
+    ``surrogate`` (incflo_gb300.surrogate.Surrogate) enables the learned warm start on multigrid level
+    ``surrogate_level``."""
     options = options or A.default_options(A.GBP_NODAL)
     key = (tuple(geom.n_cell), tuple(geom.prob_lo), tuple(geom.prob_hi), tuple(bc_lo), tuple(bc_hi),
            options.max_coarsening_level, torch.cuda.current_device())
@@ -245,6 +258,9 @@ def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd,
         NodalProjector._plans[key] = plan
     else:
         plan.set_options(options)
+    A.check(A.load().gbp_plan_set_surrogate(plan.ptr, surrogate.ptr if surrogate is not None else None,
+                                            int(surrogate_level), int(surrogate is not None)),
+            "gbp_plan_set_surrogate")
     st = A.Stats()
     rho_a = None if constant_density else array4(density, 0)
     A.check(A.load().gbp_apply_nodal_projection(
@@ -252,6 +268,32 @@ def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd,
         float(rho0), _ref(array4(gp)), _ref(array4(p_nd)) if p_nd is not None else None, float(time), float(dt),
         float(prev_dt), float(scaling_factor), int(incremental), int(set_inflow_bc), ctypes.byref(st)),
         "gbp_apply_nodal_projection")
+    return st.as_dict()
+
+
+def apply_cc_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_cc, umac, *, time=0.0, dt=1.0,
+                        prev_dt=1.0, scaling_factor=1.0, incremental=False, set_inflow_bc=True, vel_old=None,
+                        rho0=1.0, ng=1, ng_rho=1, options: A.Options | None = None, stream=None,
+                        constant_density=False):
+    """incflo::ApplyCCProjection for one level (non-EB), on the device; umac = [ux, uy, uz] face tensors
+    receive the projected face velocities. density has ``ng_rho`` ghost layers. Returns the stats dict."""
+    options = options or A.default_options(A.GBP_MAC)
+    key = ("cc", tuple(geom.n_cell), tuple(geom.prob_lo), tuple(geom.prob_hi), tuple(bc_lo), tuple(bc_hi),
+           options.max_coarsening_level, torch.cuda.current_device())
+    plan = MacProjector._cc_plans.get(key)
+    if plan is None:
+        plan = _Plan(geom, A.GBP_MAC, bc_lo, bc_hi, options, stream)
+        MacProjector._cc_plans[key] = plan
+    else:
+        plan.set_options(options)
+    st = A.Stats()
+    rho_a = None if constant_density else array4(density, ng_rho)
+    u = [array4(x) for x in umac]
+    A.check(A.load().gbp_apply_cc_projection(
+        plan.ptr, _ref(array4(vel, ng)), _ref(array4(vel_old, 0)) if vel_old is not None else None, _ref(rho_a),
+        float(rho0), _ref(array4(gp)), _ref(array4(p_cc)) if p_cc is not None else None, _ref(u[0]), _ref(u[1]),
+        _ref(u[2]), float(time), float(dt), float(prev_dt), float(scaling_factor), int(incremental),
+        int(set_inflow_bc), ctypes.byref(st)), "gbp_apply_cc_projection")
     return st.as_dict()
 
 
@@ -276,6 +318,8 @@ def nodal_divergence(geom: Geometry, bc_lo, bc_hi, vel, ng=1, use_inflow=True, o
 # ------------------------------------------------------------------------------------ MAC
 class MacProjector:
     """Hydro::MacProjector(geom) for one level: initProjector / updateCoeffs / setUMAC / project."""
+
+    _cc_plans: dict = {}
 
     def __init__(self, geom: Geometry, options: A.Options | None = None, stream=None):
         self.geom = geom
@@ -312,6 +356,17 @@ class MacProjector:
 
     def setUMAC(self, umac):  # noqa: N802
         self.umac = list(umac)
+
+    def enforceInOutSolvability(self, dd_lo, dd_hi):  # noqa: N802
+        """HydroUtils::enforceInOutSolvability on the face velocities given to setUMAC
+        (incflo_compute_MAC_projected_velocities.cpp:266-270). Returns (inflow, outflow)."""
+        self._ensure()
+        u = [array4(x) for x in self.umac]
+        io = (ctypes.c_double * 2)()
+        A.check(A.load().gbp_mac_enforce_inout_solvability(self.plan.ptr, _ref(u[0]), _ref(u[1]), _ref(u[2]),
+                                                           (ctypes.c_int * 3)(*dd_lo), (ctypes.c_int * 3)(*dd_hi),
+                                                           io), "gbp_mac_enforce_inout_solvability")
+        return io[0], io[1]
 
     def _ensure(self):
         if self.plan is None:

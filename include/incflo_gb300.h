@@ -93,7 +93,9 @@ typedef struct {
     int nu1;                     /* num_pre_smooth  (2) */
     int nu2;                     /* num_post_smooth (2) */
     double omega;                /* Jacobi weight of the nodal smoother (0.85) */
-    int ir_inner_cycles;         /* mixed form: FP32 V-cycles per FP64 refinement step (4) */
+    int ir_inner_cycles;         /* mixed form: at most this many FP32 V-cycles per FP64
+                                    refinement step (5); fewer when the observed contraction
+                                    says fewer reach the tolerance */
     int use_graphs;              /* capture each V-cycle as a CUDA graph (1) */
     int always_use_bnorm;        /* relative tolerance against |b| (1) or |r0| (0) */
 } gbp_options;
@@ -109,7 +111,9 @@ typedef struct {
     double ms_total;             /* device time of the whole call, CUDA events */
     double ms_solve;             /* device time of the solve alone */
     long long kernel_launches;   /* kernels this call ran on the device (graph nodes included) */
-    int warm_start;              /* learned warm start: 0 not attached, 1 used, 2 bypassed */
+    int warm_start;              /* learned warm start: 0 not attached, 1 used, 2 bypassed,
+                                    3 skipped (the two attempts before were bypassed; the plan
+                                    retries after 16 skipped solves) */
     double warm_rel_resid;       /* residual of the scaled prediction / rhs_norm (when attempted) */
     double ms_warm;              /* device time of the warm start (network + scaling + residual) */
 } gbp_stats;
@@ -225,6 +229,39 @@ int gbp_apply_nodal_projection_host(gbp_plan* plan, double* vel, const double* r
  * which: 0 = FP64 Jacobi sweep, 1 = FP32 Jacobi sweep, 2 = FP64 residual, 3 = FP32 residual. */
 int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_launch,
                          double* bytes_per_launch);
+
+/* incflo::ApplyCCProjection(density, umac, time, scaling_factor, incremental) for one level,
+ * non-EB (src/projection/incflo_apply_cc_projection.cpp:199-487; option incflo.use_cc_proj):
+ * gp add-back (:214-238), U^n subtraction for incremental / small-dt projections (:241-249),
+ * method-of-lines face velocities (MOL::ExtrapVelToFaces, :350-353: monotonised-central slopes,
+ * upwinded by the face-state average; wall faces 0, inflow faces the ghost value, outflow faces
+ * the adjacent cell), the MAC solve with beta = scaling_factor / rho_face (arithmetic mean of the
+ * two cells; rho == NULL: scaling_factor / rho0) (:276-366), fluxes -beta grad phi averaged to
+ * cells (:383-399), u += gphi, p_cc = phi (+= when incremental), gp = -gphi rho / s (-=)
+ * (:401-463), U^n added back (:471-477). plan: a MAC plan. umac_x/y/z receive the projected face
+ * velocities (they are the reference's u_mac/v_mac/w_mac arguments). */
+int gbp_apply_cc_projection(gbp_plan* plan, gbp_array4* vel, const gbp_array4* vel_old,
+                            const gbp_array4* rho, double rho0, gbp_array4* gp, gbp_array4* p_cc,
+                            gbp_array4* umac_x, gbp_array4* umac_y, gbp_array4* umac_z, double time,
+                            double dt, double prev_dt, double scaling_factor, int incremental,
+                            int set_inflow_bc, gbp_stats* stats);
+
+/* ---- inflow / outflow solvability -----------------------------------------------------
+ * HydroUtils::enforceInOutSolvability as incflo calls it before the nodal projection
+ * (incflo_apply_nodal_projection.cpp:166-179; has_inout_bndry && set_inflow_bc): vel is the
+ * cell-centred velocity (3 comps, one ghost layer whose boundary ghost cells hold the boundary
+ * values); dd_lo / dd_hi mark the direction_dependent faces. The flux into the domain through
+ * those faces (face area x normal velocity) is split into inflow and outflow and every outflow
+ * normal velocity is multiplied by inflow / outflow, so the net flux is zero (no change when
+ * there is no outflow). inflow_outflow (host, 2 doubles, may be NULL) receives the two fluxes
+ * before scaling. */
+int gbp_enforce_inout_solvability(gbp_plan* plan, gbp_array4* vel, const int dd_lo[3],
+                                  const int dd_hi[3], double* inflow_outflow);
+/* The same on the MAC face velocities' boundary faces 0 and n
+ * (incflo_compute_MAC_projected_velocities.cpp:266-270). */
+int gbp_mac_enforce_inout_solvability(gbp_plan* plan, gbp_array4* ux, gbp_array4* uy,
+                                      gbp_array4* uz, const int dd_lo[3], const int dd_hi[3],
+                                      double* inflow_outflow);
 
 /* ---- warm-start network building blocks (no reference counterpart) -------------------
  * Activations are channels-last BF16 matrices [R][C] over a grid of dims[0] x dims[1] x

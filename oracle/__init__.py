@@ -222,3 +222,177 @@ def mac_project(g: Grid, beta, umac, phi0=None, rtol=1e-13, atol=0.0, maxiter=40
                               _p(phi), int(phi0 is not None), rtol, atol, maxiter, _p(stats))
     return u, phi, {"status": st, "iters": int(stats[0]), "rel_resid": stats[1],
                     "rhs_norm": stats[2]}
+
+
+def _inout_faces(g: Grid, dd_lo, dd_hi, getter):
+    """Yield (d, side, view) for every marked face; view is a writable array of normal velocities."""
+    for d in range(3):
+        for side, on in ((0, dd_lo[d]), (1, dd_hi[d])):
+            if on:
+                yield d, side, getter(d, side)
+
+
+def _inout_scale(g: Grid, faces):
+    """HydroUtils::enforceInOutSolvability (AMReX-Hydro, not vendored; called by incflo at
+    src/projection/incflo_apply_nodal_projection.cpp:166-179 and
+    src/convection/incflo_compute_MAC_projected_velocities.cpp:266-270): the flux into the domain
+    over the marked faces (area x normal velocity, positive = inflow) is split into inflow and
+    outflow; every outflow velocity is multiplied by inflow / outflow so the net flux is zero."""
+    faces = list(faces)
+    inflow = outflow = 0.0
+    for d, side, v in faces:
+        area = g.h[(d + 1) % 3] * g.h[(d + 2) % 3]
+        into = -v if side else v
+        inflow += area * into[into > 0].sum()
+        outflow -= area * into[into < 0].sum()
+    if outflow > 0.0:
+        alpha = inflow / outflow
+        for d, side, v in faces:
+            into = -v if side else v
+            v[into < 0] *= alpha
+    return inflow, outflow
+
+
+def enforce_inout_solvability(g: Grid, vel, dd_lo, dd_hi):
+    """Cell velocity (3, nz+2, ny+2, nx+2) whose boundary ghost cells hold the boundary values;
+    returns (scaled copy, inflow, outflow)."""
+    v = np.array(vel, dtype=np.float64, copy=True)
+
+    def getter(d, side):
+        sl = [slice(1, -1)] * 3
+        sl[2 - d] = -1 if side else 0
+        return v[(d,) + tuple(sl)]
+
+    # views share memory with v, so scaling them scales v
+    inflow, outflow = _inout_scale(g, _inout_faces(g, dd_lo, dd_hi, getter))
+    return v, inflow, outflow
+
+
+def mac_enforce_inout_solvability(g: Grid, umac, dd_lo, dd_hi):
+    """Face velocities (x: (nz, ny, nx+1), ...): scales the boundary faces 0 / n; returns
+    (scaled copies, inflow, outflow)."""
+    u = [np.array(x, dtype=np.float64, copy=True) for x in umac]
+
+    def getter(d, side):
+        sl = [slice(None)] * 3
+        sl[2 - d] = -1 if side else 0
+        return u[d][tuple(sl)]
+
+    inflow, outflow = _inout_scale(g, _inout_faces(g, dd_lo, dd_hi, getter))
+    return u, inflow, outflow
+
+
+def mol_extrap_to_faces(g: Grid, vel, use_inflow=True):
+    """Normal velocity on faces from cell velocity, the method-of-lines face extrapolation incflo's
+    ApplyCCProjection uses (MOL::ExtrapVelToFaces, AMReX-Hydro, not vendored; called at
+    src/projection/incflo_apply_cc_projection.cpp:350-353), restated: each cell's value is
+    extrapolated to its faces with a monotonised-central slope, the two face states are upwinded by
+    their average (zero when they diverge or the average is below 1e-10 in magnitude). Boundaries:
+    periodic faces wrap; wall (Neumann) faces carry 0; inflow faces carry the ghost-cell value
+    (0 when use_inflow is false); outflow (Dirichlet) faces take the adjacent interior value; cells
+    next to a non-periodic boundary use a zero slope.
+
+    vel: (3, nz+2, ny+2, nx+2); returns [ux (nz, ny, nx+1), uy (nz, ny+1, nx), uz (nz+1, ny, nx)]."""
+    small = 1e-10
+    out = []
+    for d in range(3):
+        ax = 2 - d
+        n = g.n[d]
+        q = np.moveaxis(vel[d][1:-1, 1:-1, 1:-1], ax, -1)  # (..., n) interior values along d
+        if g.periodic(d):
+            qm, qp = np.roll(q, 1, axis=-1), np.roll(q, -1, axis=-1)
+        else:
+            qm = np.concatenate([q[..., :1], q[..., :-1]], axis=-1)
+            qp = np.concatenate([q[..., 1:], q[..., -1:]], axis=-1)
+        dl, dr, dc = 2.0 * (q - qm), 2.0 * (qp - q), 0.5 * (qp - qm)
+        slope = np.minimum(np.minimum(np.abs(dl), np.abs(dr)), np.abs(dc))
+        slope = np.where(dl * dr > 0.0, np.where(dc > 0.0, slope, -slope), 0.0)
+        if not g.periodic(d):
+            slope[..., 0] = 0.0
+            slope[..., -1] = 0.0
+        right_of_face = q - 0.5 * slope   # state just right of face i (cell i)
+        left_of_face = q + 0.5 * slope    # state just left of face i+1 (cell i)
+        f = np.zeros(q.shape[:-1] + (n + 1,))
+        # interior faces 1..n-1 (and the periodic face 0 == n)
+        um = left_of_face[..., :-1]
+        up = right_of_face[..., 1:]
+        avg = 0.5 * (um + up)
+        val = np.where(avg >= small, um, np.where(avg <= -small, up, 0.0))
+        val = np.where((um < 0.0) & (up > 0.0), 0.0, val)
+        f[..., 1:n] = val
+        if g.periodic(d):
+            um, up = left_of_face[..., -1], right_of_face[..., 0]
+            avg = 0.5 * (um + up)
+            v = np.where(avg >= small, um, np.where(avg <= -small, up, 0.0))
+            v = np.where((um < 0.0) & (up > 0.0), 0.0, v)
+            f[..., 0] = v
+            f[..., n] = v
+        else:
+            for side, bc in ((0, g.bclo[d]), (1, g.bchi[d])):
+                k = n if side else 0
+                if bc == DIRICHLET:
+                    f[..., k] = q[..., -1 if side else 0]
+                elif bc == INFLOW and use_inflow:
+                    gsl = [slice(1, -1)] * 3
+                    gsl[ax] = -1 if side else 0
+                    f[..., k] = vel[d][tuple(gsl)]  # the boundary ghost cell holds the inflow value
+                else:
+                    f[..., k] = 0.0
+        out.append(np.ascontiguousarray(np.moveaxis(f, -1, ax)))
+    return out
+
+
+def cc_projection(g: Grid, vel, rho, gp, p_cc, *, vel_old=None, rho0=1.0, constant_density=False, time=0.0,
+                  dt=1.0, prev_dt=1.0, scaling_factor=1.0, incremental=False, use_inflow=True, rtol=1e-13):
+    """incflo::ApplyCCProjection for one level, non-EB (src/projection/incflo_apply_cc_projection.cpp:199-487):
+    gp add-back (:214-238), U^n subtraction for incremental / small-dt (:241-249), MOL face velocities
+    (:350-353), MAC projection with beta = s / rho_face, rho_face the arithmetic mean of the two cells
+    (:276-323, :366), fluxes -beta grad phi averaged to cells (:392-399), then u += gphi, p_cc = phi
+    (+= when incremental), gp = -gphi rho / s (-= when incremental) (:401-463), U^n added back (:471-477).
+
+    vel (3, nz+2, ny+2, nx+2) with inflow ghosts; rho (nz+2, ny+2, nx+2) with ghosts (the ghost across
+    a Dirichlet face is used); gp (3, nz, ny, nx); p_cc (nz, ny, nx). Returns new copies
+    (vel, gp, p_cc, umac, phi, stats)."""
+    v = np.array(vel, dtype=np.float64, copy=True)
+    gp = np.array(gp, dtype=np.float64, copy=True)
+    p_cc = np.array(p_cc, dtype=np.float64, copy=True)
+    s = scaling_factor
+    small_dt = time > 0.0 and dt < 0.1 * prev_dt
+    sub_old = small_dt or incremental
+    rc = np.full(g.cell_shape, rho0) if constant_density else rho[1:-1, 1:-1, 1:-1]
+    inner = (slice(None), slice(1, -1), slice(1, -1), slice(1, -1))
+    if not incremental:
+        v[inner] += gp * (s / rc)
+    if sub_old:
+        v[inner] -= vel_old
+    umac = mol_extrap_to_faces(g, v, use_inflow=use_inflow and not sub_old)
+    if constant_density:
+        beta = [np.full(g.face_shape(d), s / rho0) for d in range(3)]
+    else:
+        beta = []
+        for d in range(3):
+            ax = 2 - d
+            core = [slice(1, -1)] * 3
+            core[ax] = slice(None)
+            r = np.moveaxis(rho[tuple(core)], ax, -1)  # (..., n+2) with both ghosts along d
+            if g.periodic(d):
+                rr = r[..., 1:-1]
+                r = np.concatenate([rr[..., -1:], rr, rr[..., :1]], axis=-1)
+            rf = 0.5 * (r[..., :-1] + r[..., 1:])
+            beta.append(np.ascontiguousarray(np.moveaxis(s / rf, -1, ax)))
+    unew, phi, st = mac_project(g, beta, umac, rtol=rtol)
+    gphi = np.empty((3,) + g.cell_shape)
+    for d in range(3):
+        ax = 2 - d
+        F = np.moveaxis(unew[d] - umac[d], ax, -1)
+        gphi[d] = np.moveaxis(0.5 * (F[..., :-1] + F[..., 1:]), -1, ax)
+    v[inner] += gphi
+    if incremental:
+        p_cc += phi
+        gp -= gphi * rc / s
+    else:
+        p_cc = phi.copy()
+        gp = -gphi * rc / s
+    if sub_old:
+        v[inner] += vel_old
+    return v, gp, p_cc, unew, phi, st
