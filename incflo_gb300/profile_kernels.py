@@ -58,7 +58,6 @@ def main():
 
 def unet_forward(n, reps):
     from incflo_gb300.surrogate import Surrogate
-    from oracle import unet as U  # layer shapes only (for the FLOP count)
 
     dims = (n, n, n + 8)
     rows = (dims[0] + 2) * (dims[1] + 2) * (dims[2] + 2)
@@ -75,11 +74,18 @@ def unet_forward(n, reps):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     # conv FLOPs: 2 x voxels x taps x cin x cout per layer on its level's grid
+    # (level, taps, input channels, output channels) of the 15 layers: encoder a/b per level, decoder
+    # a (upsampled + skip) / b for levels 2, 1, 0, and the 1x1x1 head
+    c = [16, 32, 64, 128]
+    layers = []
+    for lvl in range(4):
+        layers += [(lvl, 27, 16 if lvl == 0 else c[lvl - 1], c[lvl]), (lvl, 27, c[lvl], c[lvl])]
+    for lvl in (2, 1, 0):
+        layers += [(lvl, 27, c[lvl + 1] + c[lvl], c[lvl]), (lvl, 27, c[lvl], c[lvl])]
+    layers.append((0, 1, 16, 16))
     flops, vox = 0.0, dims[0] * dims[1] * dims[2]
-    spec = U.layer_specs()
-    lv = [0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0, 0]
-    for (nin, c0, c1, co, t), l in zip(spec, lv):
-        flops += 2.0 * vox / 8 ** l * t * (c0 + c1) * co
+    for lvl, t, ci, co in layers:
+        flops += 2.0 * vox / 8 ** lvl * t * ci * co
     print(json.dumps({"unet_forward_ms": ms, "dims": dims, "gflop": flops / 1e9, "tflops": flops / ms / 1e9}))
 
 
