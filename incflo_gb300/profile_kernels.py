@@ -9,8 +9,15 @@ captures exactly those.
 
   python -m incflo_gb300.profile_kernels --unet 128 --reps 5
 
-times the warm-start U-Net's forward pass (tensor-core convolutions) on a 128 x 128 x 136 network
-grid (the multigrid level 1 of a 256^3 projection) and reports the convolution FLOP rate.
+times the warm-start U-Net's forward pass, and
+
+  python -m incflo_gb300.profile_kernels --project mixed --n 256 --reps 1
+
+runs whole projections of the 256^3 variable-density workload in one form (mixed | fp64), so that an
+ncu launch list covers exactly one form.
+
+The U-Net mode runs the tensor-core convolutions on a 128 x 128 x 136 network grid (the multigrid
+level 1 of a 256^3 projection) and reports the convolution FLOP rate.
 """
 from __future__ import annotations
 
@@ -37,6 +44,7 @@ def main():
     ap.add_argument("--which", type=int, default=1)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--unet", type=int, default=0, help="time the U-Net forward on an n x n x (n+8) grid")
+    ap.add_argument("--project", default="", choices=["", "mixed", "fp64"])
     args = ap.parse_args()
     from incflo_gb300.build import build
 
@@ -44,6 +52,8 @@ def main():
     lib = _abi.load()
     if args.unet:
         return unet_forward(args.unet, args.reps)
+    if args.project:
+        return projections(args.n, args.project, args.reps)
     n = args.n
     rho = synth.variable_density_rt(n)["rho"]
     geom = Geometry((n, n, n))
@@ -54,6 +64,27 @@ def main():
     _abi.check(lib.gbp_plan_time_kernel(plan.ptr, args.which, args.reps, ctypes.byref(ms), ctypes.byref(by)), "time")
     print(json.dumps({"which": args.which, "n": n, "ms_per_launch": ms.value, "bytes_per_launch": by.value,
                       "GBps": by.value / ms.value / 1e6}))
+
+
+def projections(n, form, reps):
+    from incflo_gb300 import apply_nodal_projection, make_options
+
+    w = synth.variable_density_rt(n)
+    geom = Geometry(w["n"], w["lo"], w["hi"])
+    vel0 = torch.from_numpy(synth.with_ghosts(w["vel"], 1)).cuda()
+    rho = torch.from_numpy(np.ascontiguousarray(w["rho"])).cuda()
+    vel = vel0.clone()
+    gp = torch.zeros((3,) + rho.shape, dtype=torch.float64, device="cuda")
+    p_nd = torch.zeros((n + 1, n + 1, n + 1), dtype=torch.float64, device="cuda")
+    opts = make_options(0, precision=form, mg_rtol=1e-10, mg_atol=0.0)
+    out = []
+    for _ in range(reps):
+        vel.copy_(vel0)
+        gp.zero_()
+        st = apply_nodal_projection(geom, w["bclo"], w["bchi"], vel, rho, gp, p_nd, set_inflow_bc=False,
+                                    options=opts)
+        out.append({k: st[k] for k in ("status", "vcycles", "outer_iters", "final_rel_resid", "ms_total")})
+    print(json.dumps({"form": form, "n": n, "runs": out}))
 
 
 def unet_forward(n, reps):
