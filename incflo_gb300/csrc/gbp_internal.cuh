@@ -106,6 +106,14 @@ __device__ __forceinline__ int node_alias_cand(int i, int n, int per, int c)
 template <typename T>
 __device__ __forceinline__ void store_node(T* a, const NodalGeom& g, int i, int j, int k, T v)
 {
+    // nodes away from a periodic seam (all but a few planes) have no alias: one store
+    const bool ax = g.per[0] && (i <= 1 || i >= g.n[0] - 1);
+    const bool ay = g.per[1] && (j <= 1 || j >= g.n[1] - 1);
+    const bool az = g.per[2] && (k <= 1 || k >= g.n[2] - 1);
+    if (!(ax || ay || az)) {
+        a[pidx(g.sy, g.sz, i, j, k)] = v;
+        return;
+    }
 #pragma unroll 1
     for (int c = 0; c < 4; ++c) {
         const int kk = node_alias_cand(k, g.n[2], g.per[2], c);

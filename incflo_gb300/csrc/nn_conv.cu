@@ -37,7 +37,7 @@ namespace {
 
 constexpr int kBM = 128;       // output rows per tile (MMA M)
 constexpr int kThreads = 192;  // warp 0 TMA producer, warp 1 MMA issuer, warps 2..5 epilogue
-constexpr int kMaxStages = 8;
+constexpr int kMaxStages = 32;
 constexpr int kWgradRows = 64;  // K rows per pipeline stage of the weight-gradient kernel
 
 struct ConvParams {
@@ -45,6 +45,12 @@ struct ConvParams {
     CUtensorMap wmap[2];
     int nin, ntaps, N, ntiles;
     int cb[2], nchunk[2], wc0[2];
+    // K steps walk tap groups: a 3x3x3 convolution has 9 groups (dz, dy), each one activation box of
+    // kBM + 2 rows shared by its 3 dx taps (tap q starts tap_row[q] rows into the box); a 1x1x1 one
+    // has one group of one tap
+    int ngroups, gtaps, a_rows, wbox_rows;
+    int goff[9];
+    int tap_row[3];
     int off[27];
     int X, Y, Z;
     long long PX, PXY, R;
@@ -146,17 +152,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv(const __grid_constant__ Co
                 const int p0 = tile * kBM;
                 for (int i = 0; i < P.nin; ++i)
                     for (int j = 0; j < P.nchunk[i]; ++j)
-                        for (int t = 0; t < P.ntaps; ++t) {
+                        for (int gq = 0; gq < P.ngroups; ++gq) {
                             const uint32_t s = it % P.ns;
                             if (it >= (uint32_t)P.ns && !mbar_wait_bounded(&empty[s], ((it / P.ns) + 1) & 1, P.err)) {
                                 abort_flag = 1;
                                 goto produced;
                             }
-                            const uint32_t bytes = (uint32_t)(kBM + P.N) * P.cb[i] * 2u;
+                            const uint32_t bytes = (uint32_t)(P.a_rows + P.gtaps * P.N) * P.cb[i] * 2u;
                             mbar_arrive_expect_tx(&full[s], bytes);
                             unsigned char* a = sgen + s * P.stage_bytes;
-                            tma_load_2d(a, &P.amap[i], &full[s], j * P.cb[i], p0 + P.off[t]);
-                            tma_load_2d(a + P.a_bytes, &P.wmap[i], &full[s], P.wc0[i] + j * P.cb[i], t * P.N);
+                            tma_load_2d(a, &P.amap[i], &full[s], j * P.cb[i], p0 + P.goff[gq]);
+                            const int wrow0 = gq * P.gtaps * P.N;
+                            for (int r = 0; r < P.gtaps * P.N; r += P.wbox_rows)
+                                tma_load_2d(a + P.a_bytes + (uint32_t)r * P.cb[i] * 2u, &P.wmap[i], &full[s],
+                                            P.wc0[i] + j * P.cb[i], wrow0 + r);
                             ++it;
                         }
             }
@@ -183,7 +192,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv(const __grid_constant__ Co
                     const uint32_t rowb = P.cb[i] * 2u;
                     const int swz = tc::swizzle_code((int)rowb);
                     for (int j = 0; j < P.nchunk[i]; ++j)
-                        for (int t = 0; t < P.ntaps; ++t) {
+                        for (int gq = 0; gq < P.ngroups; ++gq) {
                             const uint32_t s = it % P.ns;
                             if (!mbar_wait_bounded(&full[s], (it / P.ns) & 1, P.err)) {
                                 abort_flag = 1;
@@ -191,10 +200,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv(const __grid_constant__ Co
                             }
                             tc::fence_after_sync();
                             const uint32_t a = sbase + s * P.stage_bytes, b = a + P.a_bytes;
-                            for (uint32_t kk = 0; kk < rowb / 32u; ++kk) {
-                                tc::mma_bf16(d, tc::sdesc(a + 32u * kk, 16, 8 * rowb, swz),
-                                             tc::sdesc(b + 32u * kk, 16, 8 * rowb, swz), P.idesc, acc);
-                                acc = 1;
+                            for (int q = 0; q < P.gtaps; ++q) {
+                                // the tap's 128 rows start tap_row[q] rows into the shared box; the
+                                // swizzle follows the absolute shared-memory address, so a start on
+                                // any row of the 8-row pattern reads the rows TMA wrote there
+                                const uint32_t aq = a + (uint32_t)P.tap_row[q] * rowb;
+                                const uint32_t bq = b + (uint32_t)(q * P.N) * rowb;
+                                for (uint32_t kk = 0; kk < rowb / 32u; ++kk) {
+                                    tc::mma_bf16(d, tc::sdesc(aq + 32u * kk, 16, 8 * rowb, swz),
+                                                 tc::sdesc(bq + 32u * kk, 16, 8 * rowb, swz), P.idesc, acc);
+                                    acc = 1;
+                                }
                             }
                             tc::mma_commit(&empty[s]);
                             ++it;
@@ -491,16 +507,31 @@ int conv3d(const ConvLaunch& L, cudaStream_t st)
         set_error("conv3d: output segments must cover N channels");
         return GBP_BAD_ARG;
     }
-    for (int i = 0; i < L.nin; ++i) {
-        int rc = encode_rows(L.in[i], L.cin[i], L.g.R, P.cb[i], kBM, &P.amap[i]);
-        if (!rc) rc = encode_rows(L.w, cin_tot, (long long)L.ntaps * L.N, P.cb[i], L.N, &P.wmap[i]);
-        if (rc) return rc;
-    }
     P.nin = L.nin;
     P.ntaps = L.ntaps;
     P.N = L.N;
     P.ntiles = (int)((L.g.R + kBM - 1) / kBM);
     tap_offsets(L.g, L.ntaps, L.flip, P.off);
+    if (L.ntaps == 27) {
+        P.ngroups = 9;
+        P.gtaps = 3;
+        P.a_rows = kBM + 2;
+        for (int gq = 0; gq < 9; ++gq) P.goff[gq] = std::min(P.off[3 * gq], P.off[3 * gq + 2]);
+        // dx = -1, 0, +1 of a group sit at rows +0, +1, +2 of the box (+2, +1, +0 for flipped taps)
+        for (int q = 0; q < 3; ++q) P.tap_row[q] = P.off[q] - P.goff[0];
+    } else {
+        P.ngroups = 1;
+        P.gtaps = 1;
+        P.a_rows = kBM;
+        P.goff[0] = P.off[0];
+        P.tap_row[0] = 0;
+    }
+    P.wbox_rows = P.gtaps * L.N <= 256 ? P.gtaps * L.N : L.N;
+    for (int i = 0; i < L.nin; ++i) {
+        int rc = encode_rows(L.in[i], L.cin[i], L.g.R, P.cb[i], P.a_rows, &P.amap[i]);
+        if (!rc) rc = encode_rows(L.w, cin_tot, (long long)L.ntaps * L.N, P.cb[i], P.wbox_rows, &P.wmap[i]);
+        if (rc) return rc;
+    }
     P.X = L.g.X;
     P.Y = L.g.Y;
     P.Z = L.g.Z;
@@ -511,8 +542,8 @@ int conv3d(const ConvLaunch& L, cudaStream_t st)
     P.flags = L.flags;
     P.bias = L.bias;
     P.err = L.err;
-    P.a_bytes = (uint32_t)kBM * cbmax * 2u;
-    P.stage_bytes = P.a_bytes + (((uint32_t)L.N * cbmax * 2u + 1023u) & ~1023u);
+    P.a_bytes = ((uint32_t)P.a_rows * cbmax * 2u + 1023u) & ~1023u;
+    P.stage_bytes = P.a_bytes + (((uint32_t)(P.gtaps * L.N) * cbmax * 2u + 1023u) & ~1023u);
     P.tmem_cols = pow2_cols(L.N);
     P.idesc = tc::idesc_bf16(kBM, L.N, 0, 0);
     const int max_smem = 200 * 1024;

@@ -239,7 +239,8 @@ __global__ void __launch_bounds__(256) k_prolong_add(NodalGeom gf, NodalGeom gc,
             }
         }
     }
-    const T w = T(1) / T(1 << (oi + oj + ok));
+    const int sh = oi + oj + ok;
+    const T w = sh == 0 ? T(1) : (sh == 1 ? T(0.5) : (sh == 2 ? T(0.25) : T(0.125)));
     const long long p = pidx(gf.sy, gf.sz, i, j, k);
     store_node(xf, gf, i, j, k, xf[p] + w * acc);
 }

@@ -207,6 +207,9 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
     }
     const NodalGeom& G0 = L[0].g;
     for (int q = 0; q < 3; ++q) add(G0.count, 8);
+    use_qsweep = qsweep_supported(G0);
+    if (use_qsweep)
+        for (int q = 0; q < 4; ++q) add(G0.count, 8);
     add(nodal_partials_needed(G0) + 64, 8);
     add(5 * B.g.count, 8);
     add(16, 4);
@@ -233,6 +236,12 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
     phi = pool.take<double>(G0.count);
     rhs0 = pool.take<double>(G0.count);
     res = pool.take<double>(G0.count);
+    if (use_qsweep) {
+        qw.wsum = pool.take<double>(G0.count);
+        qw.wx = pool.take<double>(G0.count);
+        qw.wy = pool.take<double>(G0.count);
+        qw.wz = pool.take<double>(G0.count);
+    }
     partials = pool.take<double>(nodal_partials_needed(G0) + 64);
     bscr = pool.take<double>(5 * B.g.count);
     dinfo = pool.take<int>(16);
@@ -280,6 +289,7 @@ int NodalSolver::set_sigma(const gbp_array4* sigma, double cval)
 // face) use (A + c 1 1^T)^-1, which solves A x = b exactly for consistent b (sum b = 0).
 int NodalSolver::build_bottom()
 {
+    if (use_qsweep) nodal_qweights64(L[0].g, L[0].s64, qw, st);
     if (!dense_bottom) return GBP_OK;
     const NodalLevel& B = L.back();
     const NodalGeom& g = B.g;
@@ -427,7 +437,10 @@ struct LevelBufs<float> {
 template <typename T>
 void NodalSolver::jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, cudaStream_t s_)
 {
-    if (use_tma && sweep_supported(g, (int)sizeof(T))) {
+    if (sizeof(T) == 8 && use_qsweep && &g == &L[0].g) {
+        nodal_qsweep64(g, 0, reinterpret_cast<const double*>(s), qw, reinterpret_cast<const double*>(x),
+                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(out), opt.omega, nullptr, s_);
+    } else if (use_tma && sweep_supported(g, (int)sizeof(T))) {
         int rc = nodal_sweep<T>(g, 0, s, x, b, out, opt.omega, derr, nullptr, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else {
@@ -439,7 +452,10 @@ template <typename T>
 void NodalSolver::resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
                         cudaStream_t s_)
 {
-    if (use_tma && sweep_supported(g, (int)sizeof(T))) {
+    if (sizeof(T) == 8 && use_qsweep && &g == &L[0].g) {
+        nodal_qsweep64(g, 1, reinterpret_cast<const double*>(s), qw, reinterpret_cast<const double*>(x),
+                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(r), opt.omega, norm, s_);
+    } else if (use_tma && sweep_supported(g, (int)sizeof(T))) {
         int rc = nodal_sweep<T>(g, 1, s, x, b, r, opt.omega, derr, norm, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else {
@@ -845,8 +861,8 @@ namespace gbp {
 
 int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
 {
-    if (which < 0 || which > 5 || reps < 1 || !sigma_ready) {
-        set_error("time_kernel: which must be 0..5, reps >= 1, and sigma must be set");
+    if (which < 0 || which > 7 || reps < 1 || !sigma_ready || (which >= 6 && L.size() < 2)) {
+        set_error("time_kernel: which must be 0..7 (6, 7 need two levels), reps >= 1, and sigma must be set");
         return GBP_BAD_ARG;
     }
     const NodalLevel& l0 = L[0];
@@ -858,6 +874,10 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
     // Jacobi: x, b read + x written per node, sigma read per cell; residual: x, b read, r written;
     // triad (which 4): three padded arrays read, one written
     *bytes = which == 4 ? 4.0 * 4.0 * (double)g.count : w * (3.0 * nn + nc);
+    // prolongation (which 6): fine x read and written, coarse x read; restriction (7): fine r read,
+    // coarse b written
+    if (which == 6) *bytes = 4.0 * (2.0 * nn + nn / 8.0);
+    if (which == 7) *bytes = 4.0 * (nn + nn / 8.0);
     if (f32) nodal_to_f32(g, res, l0.b32, scale32, st);
     GBP_CUDA(cudaEventRecord(ev0, st));
     for (int r = 0; r < reps; ++r) {
@@ -867,6 +887,8 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
         case 2: resid<double>(g, l0.s64, phi, rhs0, l0.r64, nullptr, st); break;
         case 3: resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st); break;
         case 4: stream_triad(l0.x32, l0.s32, l0.b32, l0.r32, g.count, st); break;
+        case 6: nodal_prolong_add<float>(g, L[1].g, L[1].x32, l0.x32, st); break;
+        case 7: nodal_restrict<float>(g, L[1].g, l0.r32, L[1].b32, st); break;
         default:
             nodal_jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, opt.omega,
                                 false, st);

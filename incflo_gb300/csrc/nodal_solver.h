@@ -9,6 +9,7 @@
 
 #include "gbp_internal.cuh"
 #include "nodal_kernels.h"
+#include "nodal_sweep.h"
 
 namespace gbp {
 
@@ -137,6 +138,8 @@ private:
     size_t net_x0_bytes = 0;
     double* net_scr = nullptr;   // 8 device doubles: input statistics, Galerkin dot products
     cudaEvent_t evw = nullptr;
+    QWeights qw{};               // level-0 sigma sums of the shared-sum FP64 sweep (isotropic levels)
+    bool use_qsweep = false;
     int warm_streak = 0;         // consecutive bypassed warm starts
     int warm_skip = 0;           // solves left before the next attempt after a streak
 };

@@ -15,6 +15,18 @@ namespace gbp {
 template <typename T>
 int nodal_sweep(const NodalGeom& g, int mode, const T* s, const T* x, const T* b, T* out, double omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st);
+// Precomputed sigma sums of the shared-sum FP64 sweep (nodal_qsweep64.cu), one value per padded node:
+// wsum = the 8 cells around the node; wx / wy / wz = the 4 cells around the edge to the +x / +y / +z
+// neighbour.
+struct QWeights {
+    double *wsum, *wx, *wy, *wz;
+};
+bool qsweep_supported(const NodalGeom& g);
+void nodal_qweights64(const NodalGeom& g, const double* s64, const QWeights& w, cudaStream_t st);
+// mode 0: Jacobi sweep, 1: residual (+ strong-form max norm into *norm when norm != nullptr)
+void nodal_qsweep64(const NodalGeom& g, int mode, const double* s64, const QWeights& w, const double* x,
+                    const double* b, double* out, double omega, unsigned long long* norm, cudaStream_t st);
+
 // whether the TMA sweep handles this level for elements of esize bytes (else the plain kernels do)
 bool sweep_supported(const NodalGeom& g, int esize);
 void sweep_forget_maps(const void* pool_base, size_t pool_bytes);

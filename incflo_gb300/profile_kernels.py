@@ -3,7 +3,8 @@
   python -m incflo_gb300.profile_kernels --n 256 --which 1 --reps 3
 
 which: 0 FP64 Jacobi sweep, 1 FP32 Jacobi sweep, 2 FP64 residual, 3 FP32 residual, 4 streaming triad
-over the same arrays. The plan holds the 256^3 variable-density workload's sigma (periodic x/y,
+over the same arrays, 5 FP32 Jacobi through the plain kernel, 6 FP32 prolongation level 1 -> 0,
+7 FP32 restriction level 0 -> 1. The plan holds the 256^3 variable-density workload's sigma (periodic x/y,
 walls z); the only launches of the selected kernel are the level-0 ones, so `ncu -k regex:<kernel>`
 captures exactly those.
 

@@ -226,7 +226,9 @@ int gbp_apply_nodal_projection_host(gbp_plan* plan, double* vel, const double* r
  * No counterpart in the reference (its MLMG has only TINY_PROFILE timers). Times `reps`
  * back-to-back launches of one level-0 kernel of a nodal plan on the plan's stream with CUDA
  * events, on the arrays of the last solve, and reports the kernel's algorithmic bytes per launch.
- * which: 0 = FP64 Jacobi sweep, 1 = FP32 Jacobi sweep, 2 = FP64 residual, 3 = FP32 residual. */
+ * which: 0 = FP64 Jacobi sweep, 1 = FP32 Jacobi sweep, 2 = FP64 residual, 3 = FP32 residual,
+ * 4 = streaming triad over three level arrays (an HBM reference), 5 = FP32 Jacobi through the
+ * plain kernel, 6 = FP32 prolongation level 1 -> 0, 7 = FP32 restriction level 0 -> 1. */
 int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_launch,
                          double* bytes_per_launch);
 
