@@ -25,7 +25,7 @@ EXPORTS = (
     "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
     "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel",
     "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc",
-    "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
+    "gbp_mac_set_robin", "gbp_average_down", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
     "gbp_nn_conv3d", "gbp_nn_conv3d_wgrad",
     "gbp_surrogate_create", "gbp_surrogate_destroy", "gbp_surrogate_num_params", "gbp_surrogate_get_params",
     "gbp_surrogate_set_params", "gbp_surrogate_get_grads", "gbp_surrogate_save", "gbp_surrogate_load",
@@ -138,6 +138,9 @@ def load(path: str = LIB_PATH):
         "gbp_nodal_divergence_noalloc": (i, [ctypes.POINTER(Geometry), ctypes.POINTER(ctypes.c_int),
                                              ctypes.POINTER(ctypes.c_int), A4, i, A4,
                                              ctypes.POINTER(ctypes.c_double), P]),
+        "gbp_mac_set_robin": (i, [P, A4, A4, A4]),
+        "gbp_average_down": (i, [A4, A4, ctypes.POINTER(ctypes.c_int), i, ctypes.POINTER(ctypes.c_int),
+                                 ctypes.POINTER(ctypes.c_int), P]),
         "gbp_apply_cc_projection": (i, [P, A4, A4, A4, d, A4, A4, A4, A4, A4, d, d, d, d, i, i,
                                         ctypes.POINTER(Stats)]),
         "gbp_enforce_inout_solvability": (i, [P, A4, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),

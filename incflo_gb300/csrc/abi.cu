@@ -503,6 +503,27 @@ int gbp_mac_set_beta_from_density(gbp_plan* p, const gbp_array4* rho, double dt)
     return p->mac->set_beta(2, src, dt);
 }
 
+int gbp_mac_set_robin(gbp_plan* p, const gbp_array4* robin_a, const gbp_array4* robin_b, const gbp_array4* robin_f)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_mac_set_robin: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    const int lo[3] = {-1, -1, -1};
+    const int hi[3] = {p->geom.n_cell[0], p->geom.n_cell[1], p->geom.n_cell[2]};
+    for (const gbp_array4* a : {robin_a, robin_b}) {
+        if (!valid_array(a, 1) || !covers(a, lo, hi)) {
+            set_error("gbp_mac_set_robin: robin_a and robin_b must be cell arrays with one ghost layer");
+            return GBP_BAD_ARG;
+        }
+    }
+    if (robin_f && robin_f->data && !(valid_array(robin_f, 1) && covers(robin_f, lo, hi))) {
+        set_error("gbp_mac_set_robin: robin_f must be a cell array with one ghost layer");
+        return GBP_BAD_ARG;
+    }
+    return p->mac->set_robin(robin_a, robin_b, (robin_f && robin_f->data) ? robin_f : nullptr);
+}
+
 int gbp_mac_project(gbp_plan* p, gbp_array4* ux, gbp_array4* uy, gbp_array4* uz, gbp_array4* phi, int phi_guess,
                     gbp_stats* stats)
 {
@@ -645,6 +666,30 @@ int gbp_mac_enforce_inout_solvability(gbp_plan* p, gbp_array4* ux, gbp_array4* u
         GBP_CUDA(cudaStreamSynchronize(p->stream));
     }
     return rc;
+}
+
+int gbp_average_down(const gbp_array4* fine, gbp_array4* crse, const int ratio[3], int ncomp, const int crse_lo[3],
+                     const int crse_hi[3], void* stream)
+{
+    if (!fine || !crse || !ratio || !crse_lo || !crse_hi || ncomp < 1 || !valid_array(fine, ncomp) ||
+        !valid_array(crse, ncomp)) {
+        set_error("gbp_average_down: fine / coarse arrays with ncomp components and the coarse box are required");
+        return GBP_BAD_ARG;
+    }
+    int flo[3], fhi[3];
+    for (int d = 0; d < 3; ++d) {
+        if (ratio[d] < 1 || crse_hi[d] < crse_lo[d]) {
+            set_error("gbp_average_down: ratio must be >= 1 and the coarse box non-empty");
+            return GBP_BAD_ARG;
+        }
+        flo[d] = crse_lo[d] * ratio[d];
+        fhi[d] = crse_hi[d] * ratio[d] + ratio[d] - 1;
+    }
+    if (!covers(crse, crse_lo, crse_hi) || !covers(fine, flo, fhi)) {
+        set_error("gbp_average_down: the arrays do not cover the coarse box / its refinement");
+        return GBP_BAD_ARG;
+    }
+    return average_down(*fine, *crse, ratio, ncomp, crse_lo, crse_hi, static_cast<cudaStream_t>(stream));
 }
 
 int gbp_plan_time_kernel(gbp_plan* p, int which, int reps, double* ms_per_launch, double* bytes_per_launch)

@@ -226,7 +226,7 @@ __device__ __forceinline__ double* a4p(const gbp_array4& a, int i, int j, int k,
 // Effective face beta of direction d for faces 0..n[d]: source 0 = array, 1 = constant,
 // 2 = dt / (0.5 (rho_lo + rho_hi)) (incflo: average_cellcenter_to_face then invert(dt)).
 __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double cval, int bclo, int bchi,
-                           double* __restrict__ b64, float* __restrict__ b32)
+                           double* __restrict__ b64, float* __restrict__ b32, RobinFaces rb)
 {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int fn[3] = {g.n[0], g.n[1], g.n[2]};
@@ -241,7 +241,8 @@ __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double
     const int fd = f[d];
     const bool per = g.per[d];
     const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
-    if (!per && (fd == 0 || fd == g.n[d]) && (fd == 0 ? bclo : bchi) != GBP_BC_DIRICHLET) {
+    const int bside = fd == 0 ? bclo : bchi;
+    if (!per && (fd == 0 || fd == g.n[d]) && bside != GBP_BC_DIRICHLET && bside != GBP_BC_ROBIN) {
         // wall / inflow face: no flux through it, and no ghost value is read
         b64[p] = 0.0;
         b32[p] = 0.f;
@@ -260,8 +261,20 @@ __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double
         if (per && lo[d] < 0) lo[d] += g.n[d];
         beta = cval / (0.5 * (a4(src, lo[0], lo[1], lo[2], 0) + a4(src, q[0], q[1], q[2], 0)));
     }
-    // Dirichlet face: the ghost value sits half a cell out, so the face weight doubles
-    const double eff = (!per && (fd == 0 || fd == g.n[d])) ? 2.0 * beta : beta;
+    // Dirichlet face: the ghost value sits half a cell out, so the face weight doubles; Robin face
+    // (a phi + b dphi/dn = 0): weight beta a h / (a h / 2 + b), with the raw beta kept for later factors
+    double eff = beta;
+    if (!per && (fd == 0 || fd == g.n[d])) {
+        if (bside == GBP_BC_ROBIN) {
+            const int q = 2 * d + (fd == 0 ? 0 : 1);
+            const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+            const long long fi = f[d1] + (long long)g.n[d1] * f[d2];
+            rb.braw[q][fi] = beta;
+            eff = beta * rb.rfac[q][fi];
+        } else {
+            eff = 2.0 * beta;
+        }
+    }
     b64[p] = eff;
     b32[p] = (float)eff;
 }
@@ -445,11 +458,67 @@ GBP_MAC_INST(double)
 GBP_MAC_INST(float)
 
 void mac_set_beta(const CellGeom& g, int d, int source, const gbp_array4* src, double cval, int bclo, int bchi,
-                  double* b64, float* b32, cudaStream_t st)
+                  double* b64, float* b32, cudaStream_t st, const RobinFaces* rb)
 {
     gbp_array4 a{};
     if (src) a = *src;
-    k_mac_beta<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, source, a, cval, bclo, bchi, b64, b32);
+    RobinFaces r{};
+    if (rb) r = *rb;
+    k_mac_beta<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, source, a, cval, bclo, bchi, b64, b32, r);
+}
+
+__global__ void k_mac_robin_factors(CellGeom g, int d, int hi, gbp_array4 a, gbp_array4 b, gbp_array4 f, int has_f,
+                                    double* __restrict__ rfac, unsigned* flags)
+{
+    const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)g.n[d1] * g.n[d2]) return;
+    int c[3];
+    c[d1] = (int)(t % g.n[d1]);
+    c[d2] = (int)(t / g.n[d1]);
+    c[d] = hi ? g.n[d] : -1;  // the ghost cell next to the face holds the Robin data
+    const double av = a4(a, c[0], c[1], c[2], 0), bv = a4(b, c[0], c[1], c[2], 0);
+    const double fv = has_f ? a4(f, c[0], c[1], c[2], 0) : 0.0;
+    const double den = av * 0.5 * g.h[d] + bv;
+    unsigned fl = 0;
+    if (!(av >= 0.0) || !(bv >= 0.0) || !(den > 0.0) || fv != 0.0) fl |= 2u;
+    if (av > 0.0) fl |= 1u;
+    rfac[t] = den > 0.0 ? av * g.h[d] / den : 0.0;
+    if (fl) atomicOr(flags, fl);
+}
+
+void mac_robin_factors(const CellGeom& g, int d, int hi, const gbp_array4& a, const gbp_array4& b,
+                       const gbp_array4* f, double* rfac, unsigned* flags, cudaStream_t st)
+{
+    const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    const long long n = (long long)g.n[d1] * g.n[d2];
+    gbp_array4 fz{};
+    if (f) fz = *f;
+    k_mac_robin_factors<<<nblk(n, 256), 256, 0, st>>>(g, d, hi, a, b, fz, f ? 1 : 0, rfac, flags);
+}
+
+__global__ void k_mac_robin_apply(CellGeom g, int d, int hi, const double* __restrict__ braw,
+                                  const double* __restrict__ rfac, double* __restrict__ b64, float* __restrict__ b32)
+{
+    const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)g.n[d1] * g.n[d2]) return;
+    int f[3];
+    f[d1] = (int)(t % g.n[d1]);
+    f[d2] = (int)(t / g.n[d1]);
+    f[d] = hi ? g.n[d] : 0;
+    const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
+    const double eff = braw[t] * rfac[t];
+    b64[p] = eff;
+    b32[p] = (float)eff;
+}
+
+void mac_robin_apply(const CellGeom& g, int d, int hi, const double* braw, const double* rfac, double* b64,
+                     float* b32, cudaStream_t st)
+{
+    const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    const long long n = (long long)g.n[d1] * g.n[d2];
+    k_mac_robin_apply<<<nblk(n, 256), 256, 0, st>>>(g, d, hi, braw, rfac, b64, b32);
 }
 void mac_coarsen_beta(const CellGeom& gf, const CellGeom& gc, int d, const double* bf, double* bc64, float* bc32,
                       cudaStream_t st)

@@ -91,11 +91,7 @@ int MacSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_h
         }
         for (int s = 0; s < 2; ++s) {
             int b = s ? bc_hi[d] : bc_lo[d];
-            if (b == GBP_BC_ROBIN) {
-                set_error("mac plan: Robin (mixed) boundaries are not supported yet");
-                return GBP_BAD_ARG;
-            }
-            if (b < GBP_BC_PERIODIC || b > GBP_BC_INFLOW) {
+            if (b < GBP_BC_PERIODIC || b > GBP_BC_ROBIN) {
                 set_error("mac plan: unknown boundary type");
                 return GBP_BAD_ARG;
             }
@@ -109,6 +105,10 @@ int MacSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_h
         dhi[d] = bc_hi[d] == GBP_BC_DIRICHLET;
         if (dlo[d] || dhi[d]) singular = false;
     }
+    any_dirichlet = !singular;
+    robin_ready = true;
+    for (int d = 0; d < 3; ++d)
+        if (bc_lo[d] == GBP_BC_ROBIN || bc_hi[d] == GBP_BC_ROBIN) robin_ready = false;
     int rc = set_options(o);
     if (rc) return rc;
     opt.max_coarsening_level = o.max_coarsening_level;
@@ -143,6 +143,14 @@ int MacSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_h
     add(mac_partials_needed(G0) + 64, 8);
     add(5 * B.g.count, 8);
     add(8, 8);
+    add(8, 4);
+    for (int q = 0; q < 6; ++q) {
+        const int d = q >> 1, d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+        if ((q & 1 ? bc_hi[d] : bc_lo[d]) == GBP_BC_ROBIN) {
+            add((size_t)n[d1] * n[d2], 8);
+            add((size_t)n[d1] * n[d2], 8);
+        }
+    }
     need += 4096;
     rc = pool.reserve(need);
     if (rc) return rc;
@@ -162,6 +170,15 @@ int MacSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_h
     partials = pool.take<double>(mac_partials_needed(G0) + 64);
     bscr = pool.take<double>(5 * B.g.count);
     dnorm = pool.take<unsigned long long>(8);
+    dflags = pool.take<unsigned>(8);
+    rb = RobinFaces{};
+    for (int q = 0; q < 6; ++q) {
+        const int d = q >> 1, d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+        if ((q & 1 ? bc_hi[d] : bc_lo[d]) == GBP_BC_ROBIN) {
+            rb.rfac[q] = pool.take<double>((size_t)n[d1] * n[d2]);
+            rb.braw[q] = pool.take<double>((size_t)n[d1] * n[d2]);
+        }
+    }
     GBP_CUDA(cudaMallocHost(&hnorm, 8 * sizeof(unsigned long long)));
     memset(hnorm, 0, 8 * sizeof(unsigned long long));
     GBP_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -175,13 +192,55 @@ int MacSolver::set_beta(int source, const gbp_array4* src[3], double cval)
 {
     for (int d = 0; d < 3; ++d) {
         const gbp_array4* s = source == 0 ? src[d] : (source == 2 ? src[0] : nullptr);
-        mac_set_beta(L[0].g, d, source, s, cval, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st);
+        mac_set_beta(L[0].g, d, source, s, cval, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st, &rb);
     }
     for (size_t l = 1; l < L.size(); ++l)
         for (int d = 0; d < 3; ++d)
             mac_coarsen_beta(L[l - 1].g, L[l].g, d, L[l - 1].b64[d], L[l].b64[d], L[l].b32[d], st);
     GBP_CUDA(cudaGetLastError());
     beta_ready = true;
+    return GBP_OK;
+}
+
+int MacSolver::set_robin(const gbp_array4* a, const gbp_array4* b, const gbp_array4* f)
+{
+    bool any = false;
+    for (int q = 0; q < 6; ++q) any = any || rb.rfac[q];
+    if (!any) {
+        set_error("mac_set_robin: the plan has no Robin (GBP_BC_ROBIN) side");
+        return GBP_BAD_ARG;
+    }
+    GBP_CUDA(cudaMemsetAsync(dflags, 0, sizeof(unsigned), st));
+    for (int q = 0; q < 6; ++q)
+        if (rb.rfac[q])
+            mac_robin_factors(L[0].g, q >> 1, q & 1, *a, *b, f, const_cast<double*>(rb.rfac[q]), dflags, st);
+    unsigned fl = 0;
+    GBP_CUDA(cudaMemcpyAsync(&fl, dflags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    if (fl & 2u) {
+        set_error("mac_set_robin: Robin data needs a >= 0, b >= 0, a h / 2 + b > 0 and f = 0 on every Robin face");
+        robin_ready = false;
+        return GBP_BAD_ARG;
+    }
+    robin_ready = true;
+    if (beta_ready) {
+        for (int q = 0; q < 6; ++q)
+            if (rb.rfac[q]) {
+                const int d = q >> 1;
+                mac_robin_apply(L[0].g, d, q & 1, rb.braw[q], rb.rfac[q], L[0].b64[d], L[0].b32[d], st);
+            }
+        for (size_t l = 1; l < L.size(); ++l)
+            for (int d = 0; d < 3; ++d)
+                mac_coarsen_beta(L[l - 1].g, L[l].g, d, L[l - 1].b64[d], L[l].b64[d], L[l].b32[d], st);
+        GBP_CUDA(cudaGetLastError());
+    }
+    // a Robin face with a > 0 pins phi like a Dirichlet face
+    const bool sing = !(any_dirichlet || (fl & 1u));
+    if (sing != singular) {
+        singular = sing;
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
     return GBP_OK;
 }
 
@@ -355,8 +414,9 @@ int MacSolver::solve(bool have_guess, gbp_stats* stats)
 
 int MacSolver::project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats)
 {
-    if (!beta_ready) {
-        set_error("mac project: beta was never set on this plan");
+    if (!beta_ready || !robin_ready) {
+        set_error(beta_ready ? "mac project: the plan has Robin sides but no Robin data (mac_set_robin)"
+                             : "mac project: beta was never set on this plan");
         return GBP_BAD_ARG;
     }
     const MacLevel& l0 = L[0];

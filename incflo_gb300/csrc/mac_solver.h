@@ -28,6 +28,9 @@ public:
     int set_options(const gbp_options& opt);
     // source: 0 = arrays, 1 = constant, 2 = dt / face average of rho
     int set_beta(int source, const gbp_array4* src[3], double cval);
+    // Robin data of the ROBIN sides (MacProjector::setLevelBC(lev, nullptr, robin_a, robin_b,
+    // robin_f)): cell arrays with one ghost layer, read in the ghost cells next to the Robin faces
+    int set_robin(const gbp_array4* a, const gbp_array4* b, const gbp_array4* f);
     int project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats);
     size_t device_bytes() const { return pool.bytes; }
 
@@ -53,6 +56,10 @@ private:
     int gexec_prec = -1;
     double gexec_scale = 0.0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr;
+    RobinFaces rb{};             // finest-level Robin faces (sides with GBP_BC_ROBIN)
+    bool any_dirichlet = false;  // a Dirichlet side exists (the system is nonsingular)
+    bool robin_ready = false;
+    unsigned* dflags = nullptr;
 };
 
 }  // namespace gbp

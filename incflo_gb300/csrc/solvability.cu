@@ -174,3 +174,40 @@ int enforce_inout_faces(const gbp_geometry& geom, const int dd_lo[3], const int 
 }
 
 }  // namespace gbp
+
+// ------------------------------------------------------------------------------------------------
+// amrex::average_down of a cell field (incflo_apply_nodal_projection.cpp:258-266 for gp): each coarse
+// cell of the region the fine level covers takes the mean of its ratio[0] x ratio[1] x ratio[2] fine
+// cells, component by component.
+namespace gbp {
+namespace {
+__global__ void k_average_down(gbp_array4 f, gbp_array4 c, int r0, int r1, int r2, int ncomp, int lo0, int lo1,
+                               int lo2, int nx, int ny, int nz)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nx * ny * nz * ncomp) return;
+    const int i = lo0 + (int)(t % nx);
+    const int j = lo1 + (int)((t / nx) % ny);
+    const long long r = t / ((long long)nx * ny);
+    const int k = lo2 + (int)(r % nz);
+    const int n = (int)(r / nz);
+    double acc = 0.0;
+    for (int c2 = 0; c2 < r2; ++c2)
+        for (int c1 = 0; c1 < r1; ++c1)
+            for (int c0 = 0; c0 < r0; ++c0) acc += *at(f, i * r0 + c0, j * r1 + c1, k * r2 + c2, n);
+    *at(c, i, j, k, n) = acc / (double)(r0 * r1 * r2);
+}
+}  // namespace
+
+int average_down(const gbp_array4& fine, const gbp_array4& crse, const int ratio[3], int ncomp, const int lo[3],
+                 const int hi[3], cudaStream_t st)
+{
+    const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+    const long long n = (long long)nx * ny * nz * ncomp;
+    if (n <= 0) return GBP_OK;
+    k_average_down<<<(unsigned)((n + kT - 1) / kT), kT, 0, st>>>(fine, crse, ratio[0], ratio[1], ratio[2], ncomp,
+                                                                 lo[0], lo[1], lo[2], nx, ny, nz);
+    GBP_CUDA(cudaGetLastError());
+    return GBP_OK;
+}
+}  // namespace gbp

@@ -14,4 +14,8 @@ int enforce_inout_cell(const gbp_geometry& geom, const int dd_lo[3], const int d
 int enforce_inout_faces(const gbp_geometry& geom, const int dd_lo[3], const int dd_hi[3], const gbp_array4* u,
                         double* flux, cudaStream_t st);
 
+// amrex::average_down of ncomp cell components over the coarse box [lo, hi]
+int average_down(const gbp_array4& fine, const gbp_array4& crse, const int ratio[3], int ncomp, const int lo[3],
+                 const int hi[3], cudaStream_t st);
+
 }  // namespace gbp

@@ -297,6 +297,22 @@ def apply_cc_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_cc, um
     return st.as_dict()
 
 
+def average_down(fine: torch.Tensor, crse: torch.Tensor, ratio=(2, 2, 2), crse_lo=None, crse_hi=None, stream=None,
+                 fine_lo=(0, 0, 0), crse_box_lo=(0, 0, 0)):
+    """amrex::average_down of a cell field (components first, or one component): crse[box] = mean of its
+    fine cells. Index spaces: fine_lo / crse_box_lo are the global indices of each tensor's first
+    element; the coarse box defaults to the coarsened fine extent."""
+    fa = array4(fine, 0, lo=fine_lo)
+    ca = array4(crse, 0, lo=crse_box_lo)
+    nc = fine.shape[0] if fine.dim() == 4 else 1
+    if crse_lo is None:
+        crse_lo = [fa.lo[d] // ratio[d] for d in range(3)]
+        crse_hi = [(fa.hi[d] + 1) // ratio[d] - 1 for d in range(3)]
+    A.check(A.load().gbp_average_down(_ref(fa), _ref(ca), (ctypes.c_int * 3)(*ratio), nc,
+                                      (ctypes.c_int * 3)(*crse_lo), (ctypes.c_int * 3)(*crse_hi), _stream_ptr(stream)),
+            "gbp_average_down")
+
+
 def nodal_divergence(geom: Geometry, bc_lo, bc_hi, vel, ng=1, use_inflow=True, out=None, stream=None):
     """Nodal divergence of vel as the projection sees it (strong form, consistent for singular
     boundary sets). Returns (max |div|, out) with out a nodal (nz+1, ny+1, nx+1) tensor."""
@@ -330,6 +346,7 @@ class MacProjector:
         self.beta = None
         self.umac = None
         self.stats = None
+        self.robin = None
 
     def needInitialization(self):  # noqa: N802
         return self.plan is None
@@ -345,6 +362,21 @@ class MacProjector:
         self.bc_lo = tuple(LinOpBCType.get(b, b) for b in lo)
         self.bc_hi = tuple(LinOpBCType.get(b, b) for b in hi)
         self.plan = None
+
+    def setLevelBC(self, lev, levelbcdata=None, robinbc_a=None, robinbc_b=None, robinbc_f=None):  # noqa: N802
+        """Robin data of the Robin sides: cell tensors (nz+2, ny+2, nx+2) with one ghost layer, read in
+        the ghost cells next to each Robin face (a phi + b dphi/dn = f, f = 0)."""
+        if lev != 0 or levelbcdata is not None:
+            raise ValueError("single level only; Dirichlet values are zero")
+        self.robin = (robinbc_a, robinbc_b, robinbc_f)
+        self._push_robin()
+
+    def _push_robin(self):
+        if self.plan is None or self.robin is None:
+            return
+        a, b, f = self.robin
+        A.check(A.load().gbp_mac_set_robin(self.plan.ptr, _ref(array4(a, 1)), _ref(array4(b, 1)),
+                                           _ref(array4(f, 1)) if f is not None else None), "gbp_mac_set_robin")
 
     def updateCoeffs(self, beta):  # noqa: N802
         self.beta = beta
@@ -374,6 +406,7 @@ class MacProjector:
                 raise RuntimeError("setDomainBC must be called before project")
             self.plan = _Plan(self.geom, A.GBP_MAC, self.bc_lo, self.bc_hi, self.options, self.stream)
             self._push_beta()
+            self._push_robin()
         else:
             self.plan.set_options(self.options)
 

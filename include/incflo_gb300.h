@@ -55,7 +55,8 @@ typedef enum {
     GBP_BC_NEUMANN = 2,   /* slip / no-slip wall */
     GBP_BC_INFLOW = 3,    /* mass_inflow / direction_dependent (nodal): Neumann for phi, the
                              normal inflow velocity from the ghost cells enters the RHS */
-    GBP_BC_ROBIN = 4      /* mixed (MAC only); not supported yet: GBP_BAD_ARG */
+    GBP_BC_ROBIN = 4      /* mixed (MAC plans): a phi + b dphi/dn = 0 per boundary face, data
+                             from gbp_mac_set_robin; nodal plans reject it */
 } gbp_bc;
 
 typedef enum { GBP_PREC_FP64 = 0, GBP_PREC_MIXED = 1 } gbp_precision;
@@ -232,6 +233,16 @@ int gbp_apply_nodal_projection_host(gbp_plan* plan, double* vel, const double* r
 int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_launch,
                          double* bytes_per_launch);
 
+/* MacProjector::setLevelBC(lev, nullptr, robin_a, robin_b, robin_f) for the GBP_BC_ROBIN sides
+ * (incflo_compute_MAC_projected_velocities.cpp:116-123; data from incflo::make_robinBC_MFs,
+ * src/boundary_conditions/incflo_set_bcs.cpp:121-192): cell arrays with one ghost layer whose
+ * ghost cells next to a Robin face hold a, b, f of a phi + b dphi/dn = f on that face. The face
+ * enters the operator with weight beta a h / (a h / 2 + b) (phi at the face = mean of the ghost and
+ * interior values): b = 0 gives the Dirichlet face, a = 0 the Neumann one. f must be 0 (incflo's
+ * MAC Robin data, prob_set_MAC_robinBCs, always has f = 0); robin_f may be NULL. */
+int gbp_mac_set_robin(gbp_plan* plan, const gbp_array4* robin_a, const gbp_array4* robin_b,
+                      const gbp_array4* robin_f);
+
 /* incflo::ApplyCCProjection(density, umac, time, scaling_factor, incremental) for one level,
  * non-EB (src/projection/incflo_apply_cc_projection.cpp:199-487; option incflo.use_cc_proj):
  * gp add-back (:214-238), U^n subtraction for incremental / small-dt projections (:241-249),
@@ -247,6 +258,13 @@ int gbp_apply_cc_projection(gbp_plan* plan, gbp_array4* vel, const gbp_array4* v
                             gbp_array4* umac_x, gbp_array4* umac_y, gbp_array4* umac_z, double time,
                             double dt, double prev_dt, double scaling_factor, int incremental,
                             int set_inflow_bc, gbp_stats* stats);
+
+/* amrex::average_down(fine, crse, 0, ncomp, ratio) as incflo applies it to gp after the nodal
+ * projection on an AMR hierarchy (incflo_apply_nodal_projection.cpp:258-266): every coarse cell
+ * of [crse_lo, crse_hi] (the coarsened fine region, coarse-level indices) becomes the mean of its
+ * ratio[0] x ratio[1] x ratio[2] fine cells, for components 0..ncomp-1. stream: cudaStream_t. */
+int gbp_average_down(const gbp_array4* fine, gbp_array4* crse, const int ratio[3], int ncomp,
+                     const int crse_lo[3], const int crse_hi[3], void* stream);
 
 /* ---- inflow / outflow solvability -----------------------------------------------------
  * HydroUtils::enforceInOutSolvability as incflo calls it before the nodal projection

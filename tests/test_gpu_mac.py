@@ -64,3 +64,54 @@ def test_mac_phi_initial_guess_and_constant_beta(gpu_lib):
     assert rel_l2(phi.cpu().numpy(), phi_or) <= 1e-9
     for d in range(3):
         np.testing.assert_allclose(ut[d].cpu().numpy(), un_or[d], rtol=0, atol=1e-9 * np.abs(un_or[d]).max())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mac_robin_faces_match_oracle(gpu_lib, precision):
+    """Robin sides (incflo's mixed BC: Neumann where a = 0, Dirichlet where b = 0, in between for
+    a, b > 0) against the oracle, where a Robin face with f = 0 is a zero-value Dirichlet face of
+    half its effective weight beta a h / (a h / 2 + b)."""
+    n, ext = (16, 12, 10), (1.0, 0.75, 0.625)
+    bclo, bchi = (O.NEUMANN, P, 4), (4, P, O.NEUMANN)
+    rng = np.random.default_rng(7)
+    g_or = O.Grid(n, hi=ext, bclo=(O.NEUMANN, P, D), bchi=(D, P, O.NEUMANN))
+    beta = [np.abs(b) + 0.2 for b in face_fields(g_or, rng, zero_neumann=False)]
+    umac = face_fields(g_or, rng)
+    ra = np.zeros((n[2] + 2, n[1] + 2, n[0] + 2))
+    rb = np.zeros_like(ra)
+    # high-x side: outflow half (Dirichlet), inflow half (Neumann); low-z side: a, b > 0 both
+    ra[1:-1, 1:-1, -1] = np.where(np.arange(n[1])[None, :] < n[1] // 2, 1.0, 0.0)
+    rb[1:-1, 1:-1, -1] = 1.0 - ra[1:-1, 1:-1, -1]
+    ra[0, 1:-1, 1:-1] = rng.uniform(0.5, 2.0, (n[1], n[0]))
+    rb[0, 1:-1, 1:-1] = rng.uniform(0.01, 0.1, (n[1], n[0]))
+    h = [ext[d] / n[d] for d in range(3)]
+    beta_or = [b.copy() for b in beta]
+    a_x, b_x = ra[1:-1, 1:-1, -1], rb[1:-1, 1:-1, -1]
+    beta_or[0][:, :, -1] = beta[0][:, :, -1] * (a_x * h[0] / (a_x * h[0] / 2 + b_x)) / 2
+    a_z, b_z = ra[0, 1:-1, 1:-1], rb[0, 1:-1, 1:-1]
+    beta_or[2][0, :, :] = beta[2][0, :, :] * (a_z * h[2] / (a_z * h[2] / 2 + b_z)) / 2
+    un_or, phi_or, st_or = O.mac_project(g_or, beta_or, umac, rtol=1e-13)
+    assert st_or["status"] == 0
+    mp = MacProjector(Geometry(n, (0, 0, 0), ext), options=make_options(1, precision=precision))
+    mp.initProjector(beta=[cuda(b) for b in beta])
+    mp.setDomainBC(bclo, bchi)
+    mp.setLevelBC(0, None, cuda(ra), cuda(rb), None)
+    ut = [cuda(u) for u in umac]
+    mp.setUMAC(ut)
+    phi = cuda(np.zeros(g_or.cell_shape))
+    st = mp.project(rtol=1e-12, atol=0.0, phi=phi, phi_guess=False)
+    assert st["status"] == 0 and st["final_rel_resid"] <= 1e-12
+    assert rel_l2(phi.cpu().numpy(), phi_or) <= 1e-9
+    for d in range(3):
+        np.testing.assert_allclose(ut[d].cpu().numpy(), un_or[d], rtol=0, atol=1e-9 * np.abs(un_or[d]).max())
+
+
+def test_mac_robin_rejects_bad_data(gpu_lib):
+    n = (8, 8, 8)
+    mp = MacProjector(Geometry(n))
+    mp.initProjector(beta=1.0)
+    mp.setDomainBC((4, O.NEUMANN, O.NEUMANN), (O.NEUMANN, O.NEUMANN, O.NEUMANN))
+    z = cuda(np.zeros((10, 10, 10)))
+    with pytest.raises(Exception):
+        mp.setLevelBC(0, None, z, z, None)  # a = b = 0: no boundary condition
+        mp._ensure()

@@ -41,3 +41,19 @@ def test_face_form_matches_oracle(gpu_lib):
     assert abs(fi - inflow) <= 1e-12 * abs(inflow) and abs(fo - outflow) <= 1e-12 * abs(outflow)
     for d in range(3):
         np.testing.assert_allclose(ut[d].cpu().numpy(), ref[d], rtol=1e-14, atol=1e-15)
+
+
+def test_average_down_matches_numpy(gpu_lib):
+    """amrex::average_down of gp (3 components) over a refined region, ratio 2, into a larger
+    coarse array (cells outside the region untouched)."""
+    from incflo_gb300.projection import average_down
+
+    rng = np.random.default_rng(8)
+    fine = rng.standard_normal((3, 8, 12, 16))       # fine cells (z, y, x), global fine index lo (4, 6, 2)
+    crse = rng.standard_normal((3, 10, 10, 12))      # coarse cells, global coarse index lo (0, 0, 0)
+    ref = crse.copy()
+    f = fine.reshape(3, 4, 2, 6, 2, 8, 2).mean(axis=(2, 4, 6))
+    ref[:, 1:5, 3:9, 2:10] = f                       # fine lo (x4, y6, z2) -> coarse (2, 3, 1)
+    ft, ct = torch.from_numpy(fine).cuda(), torch.from_numpy(crse).cuda()
+    average_down(ft, ct, ratio=(2, 2, 2), fine_lo=(4, 6, 2), crse_box_lo=(0, 0, 0))
+    np.testing.assert_allclose(ct.cpu().numpy(), ref, rtol=1e-15, atol=1e-15)
