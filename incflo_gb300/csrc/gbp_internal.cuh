@@ -114,23 +114,24 @@ __device__ __forceinline__ void store_node(T* a, const NodalGeom& g, int i, int 
         a[pidx(g.sy, g.sz, i, j, k)] = v;
         return;
     }
-    // candidate positions per direction at fixed list slots (the node, then its aliases 0<->n,
-    // 1<->n+1, n-1<->-1); fully unrolled with compile-time indices, so the lists stay in registers
-    int xs[4], ys[4], zs[4];
-#pragma unroll
+    // a node on a periodic seam: every combination of its per-direction aliases (kept as rolled
+    // loops: this path is rare, and inlining it unrolled bloats every kernel that stores nodes)
+#pragma unroll 1
     for (int c = 0; c < 4; ++c) {
-        xs[c] = node_alias_cand(i, g.n[0], g.per[0], c);
-        ys[c] = node_alias_cand(j, g.n[1], g.per[1], c);
-        zs[c] = node_alias_cand(k, g.n[2], g.per[2], c);
+        const int kk = node_alias_cand(k, g.n[2], g.per[2], c);
+        if (kk == kNoAlias) continue;
+#pragma unroll 1
+        for (int b = 0; b < 4; ++b) {
+            const int jj = node_alias_cand(j, g.n[1], g.per[1], b);
+            if (jj == kNoAlias) continue;
+#pragma unroll 1
+            for (int q = 0; q < 4; ++q) {
+                const int ii = node_alias_cand(i, g.n[0], g.per[0], q);
+                if (ii == kNoAlias) continue;
+                a[pidx(g.sy, g.sz, ii, jj, kk)] = v;
+            }
+        }
     }
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (xs[q] != kNoAlias && ys[b] != kNoAlias && zs[c] != kNoAlias)
-                    a[pidx(g.sy, g.sz, xs[q], ys[b], zs[c])] = v;
 }
 
 template <typename T>

@@ -118,6 +118,15 @@ __device__ __forceinline__ bool decode_node(const NodalGeom& g, long long t, int
 {
     const long long nxy = (long long)g.nu[0] * g.nu[1];
     if (t >= nxy * g.nu[2]) return false;
+    if (t < 0x7fffffffll) {
+        // 32-bit division where it fits (all levels below about 2^31 nodes): several times cheaper
+        const unsigned u = (unsigned)t, uxy = (unsigned)nxy;
+        k = (int)(u / uxy);
+        const unsigned r = u - (unsigned)k * uxy;
+        j = (int)(r / (unsigned)g.nu[0]);
+        i = (int)(r - (unsigned)j * (unsigned)g.nu[0]);
+        return true;
+    }
     k = (int)(t / nxy);
     long long r = t - (long long)k * nxy;
     j = (int)(r / g.nu[0]);
@@ -243,6 +252,80 @@ __global__ void __launch_bounds__(256) k_prolong_add(NodalGeom gf, NodalGeom gc,
     const T w = sh == 0 ? T(1) : (sh == 1 ? T(0.5) : (sh == 2 ? T(0.25) : T(0.125)));
     const long long p = pidx(gf.sy, gf.sz, i, j, k);
     store_node(xf, gf, i, j, k, xf[p] + w * acc);
+}
+
+// fine += P xc with one thread per coarse node (I, J, K): it reads the 8 coarse nodes of the cell
+// (I..I+1, J..J+1, K..K+1) once and updates the fine block (2I..2I+1, 2J..2J+1, 2K..2K+1), x pairs
+// as one vector access. Fine Dirichlet nodes lie on coarse Dirichlet faces, whose coarse values are
+// 0, so they receive 0 without a test.
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+    using type = float2;
+};
+template <>
+struct Vec2<double> {
+    using type = double2;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong_block(NodalGeom gf, NodalGeom gc, const T* __restrict__ xc,
+                                                       T* __restrict__ xf)
+{
+    int I, J, K;
+    if (!grid3_node(gc, I, J, K)) return;
+    const bool vx = 2 * I + 1 < gf.nu[0], vy = 2 * J + 1 < gf.nu[1], vz = 2 * K + 1 < gf.nu[2];
+    const long long pc = pidx(gc.sy, gc.sz, I, J, K);
+    T c[2][2][2];
+#pragma unroll
+    for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+        for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+            for (int cx = 0; cx < 2; ++cx) {
+                const bool need = (!cx || vx) && (!cy || vy) && (!cz || vz);
+                c[cz][cy][cx] = need ? xc[pc + cx + cy * gc.sy + cz * gc.sz] : T(0);
+            }
+    const bool seam = (gf.per[0] && (2 * I <= 1 || 2 * I + 1 >= gf.n[0] - 1)) ||
+                      (gf.per[1] && (2 * J <= 1 || 2 * J + 1 >= gf.n[1] - 1)) ||
+                      (gf.per[2] && (2 * K <= 1 || 2 * K + 1 >= gf.n[2] - 1));
+#pragma unroll
+    for (int oz = 0; oz < 2; ++oz) {
+        if (oz && !vz) break;
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy) {
+            if (oy && !vy) break;
+            // coarse values interpolated to (., 2J+oy, 2K+oz) at x = I and I+1
+            T e0 = c[0][0][0], e1 = c[0][0][1];
+            if (oy) {
+                e0 = T(0.5) * (e0 + c[0][1][0]);
+                e1 = T(0.5) * (e1 + c[0][1][1]);
+            }
+            if (oz) {
+                T f0 = c[1][0][0], f1 = c[1][0][1];
+                if (oy) {
+                    f0 = T(0.5) * (f0 + c[1][1][0]);
+                    f1 = T(0.5) * (f1 + c[1][1][1]);
+                }
+                e0 = T(0.5) * (e0 + f0);
+                e1 = T(0.5) * (e1 + f1);
+            }
+            const T a0 = e0, a1 = T(0.5) * (e0 + e1);  // fine x = 2I, 2I+1
+            const int i = 2 * I, j = 2 * J + oy, k = 2 * K + oz;
+            const long long p = pidx(gf.sy, gf.sz, i, j, k);
+            if (!seam && vx) {
+                using V = typename Vec2<T>::type;
+                V v = *reinterpret_cast<const V*>(xf + p);
+                v.x += a0;
+                v.y += a1;
+                *reinterpret_cast<V*>(xf + p) = v;
+            } else {
+                store_node(xf, gf, i, j, k, xf[p] + a0);
+                if (vx) store_node(xf, gf, i + 1, j, k, xf[p + 1] + a1);
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -659,13 +742,11 @@ __global__ void __launch_bounds__(256) k_to_f32(NodalGeom g, const double* __res
 __global__ void __launch_bounds__(256) k_nodal_correct(NodalGeom g, CorrArgs a, const double* __restrict__ s64,
                                                        const double* __restrict__ phi)
 {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long nxy = (long long)g.n[0] * g.n[1];
-    if (t >= nxy * g.n[2]) return;
-    const int k = (int)(t / nxy);
-    const long long rem = t - (long long)k * nxy;
-    const int j = (int)(rem / g.n[0]);
-    const int i = (int)(rem - (long long)j * g.n[0]);
+    // 3-D launch over the cells (block 32 x 4 x 2): no index division
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= g.n[0] || j >= g.n[1] || k >= g.n[2]) return;
     const long long c = pidx(g.sy, g.sz, i, j, k);
     const long long sy = g.sy, sz = g.sz;
     const double p000 = phi[c], p100 = phi[c + 1], p010 = phi[c + sy], p110 = phi[c + 1 + sy];
@@ -799,7 +880,7 @@ void nodal_restrict(const NodalGeom& gf, const NodalGeom& gc, const T* rf, T* bc
 template <typename T>
 void nodal_prolong_add(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T* xf, cudaStream_t st)
 {
-    k_prolong_add<T><<<grid3(gf), kBlock3, 0, st>>>(gf, gc, xc, xf);
+    k_prolong_block<T><<<grid3(gc), kBlock3, 0, st>>>(gf, gc, xc, xf);
 }
 
 template <typename T>
@@ -906,7 +987,7 @@ void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale,
 
 void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st)
 {
-    k_nodal_correct<<<nblocks(ncells(g), 256), 256, 0, st>>>(g, a, s64, phi);
+    k_nodal_correct<<<dim3((g.n[0] + 31) / 32, (g.n[1] + 3) / 4, (g.n[2] + 1) / 2), kBlock3, 0, st>>>(g, a, s64, phi);
 }
 
 void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* phi, int accumulate, cudaStream_t st)

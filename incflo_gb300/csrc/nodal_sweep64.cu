@@ -441,8 +441,15 @@ void sweep_forget_maps(const void* pool_base, size_t pool_bytes)
     }
 }
 
+// The z-marching sweeps need a long z range per CTA to amortise their pipeline; on levels below a few
+// million nodes the one-node-per-thread kernels (nodal_kernels.cu) are faster (measured: 128^3 and
+// smaller levels of the 256^3 hierarchy).
+constexpr long long kSweepMinNodes = 4ll << 20;
+
 bool sweep_supported(const NodalGeom& g, int esize)
 {
+    const long long nodes = (long long)g.nu[0] * g.nu[1] * g.nu[2];
+    if (nodes < kSweepMinNodes) return false;
     if (esize == 4) return g.iso && g.nu[0] >= 32 && g.nu[1] >= 4 && g.nu[2] >= 4;
     return g.nu[0] >= 16 && g.nu[1] >= 4 && g.nu[2] >= 4;
 }
