@@ -24,8 +24,8 @@ EXPORTS = (
     "gbp_nodal_set_sigma_from_density", "gbp_nodal_set_sigma", "gbp_nodal_project",
     "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
     "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel",
-    "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc",
-    "gbp_mac_set_robin", "gbp_average_down", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
+    "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc", "gbp_nodal_set_overset_mask",
+    "gbp_mac_set_robin", "gbp_mac_set_eb", "gbp_average_down", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
     "gbp_nn_conv3d", "gbp_nn_conv3d_wgrad",
     "gbp_surrogate_create", "gbp_surrogate_destroy", "gbp_surrogate_num_params", "gbp_surrogate_get_params",
     "gbp_surrogate_set_params", "gbp_surrogate_get_grads", "gbp_surrogate_save", "gbp_surrogate_load",
@@ -43,6 +43,16 @@ class Array4(ctypes.Structure):
         ("jstride", ctypes.c_longlong),
         ("kstride", ctypes.c_longlong),
         ("nstride", ctypes.c_longlong),
+    ]
+
+
+class IArray4(ctypes.Structure):
+    _fields_ = [
+        ("data", ctypes.c_void_p),
+        ("lo", ctypes.c_int * 3),
+        ("hi", ctypes.c_int * 3),
+        ("jstride", ctypes.c_longlong),
+        ("kstride", ctypes.c_longlong),
     ]
 
 
@@ -139,6 +149,8 @@ def load(path: str = LIB_PATH):
                                              ctypes.POINTER(ctypes.c_int), A4, i, A4,
                                              ctypes.POINTER(ctypes.c_double), P]),
         "gbp_mac_set_robin": (i, [P, A4, A4, A4]),
+        "gbp_mac_set_eb": (i, [P, A4, A4, A4, A4, A4, A4, A4]),
+        "gbp_nodal_set_overset_mask": (i, [P, ctypes.POINTER(IArray4)]),
         "gbp_average_down": (i, [A4, A4, ctypes.POINTER(ctypes.c_int), i, ctypes.POINTER(ctypes.c_int),
                                  ctypes.POINTER(ctypes.c_int), P]),
         "gbp_apply_cc_projection": (i, [P, A4, A4, A4, d, A4, A4, A4, A4, A4, d, d, d, d, i, i,

@@ -400,6 +400,22 @@ int gbp_nodal_project(gbp_plan* p, gbp_array4* vel, gbp_array4* phi, gbp_array4*
     return p->nodal->project(ra, ca, phi, 0, phi_guess ? phi : nullptr, stats);
 }
 
+int gbp_nodal_set_overset_mask(gbp_plan* p, const gbp_iarray4* m)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_nodal_set_overset_mask: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    if (m && m->data) {
+        for (int d = 0; d < 3; ++d)
+            if (m->lo[d] > 0 || m->hi[d] < p->geom.n_cell[d] || m->jstride <= 0 || m->kstride <= 0) {
+                set_error("gbp_nodal_set_overset_mask: the mask must cover nodes 0..n");
+                return GBP_BAD_ARG;
+            }
+    }
+    return p->nodal->set_mask(m);
+}
+
 int gbp_nodal_divergence(gbp_plan* p, const gbp_array4* vel, int use_inflow, gbp_array4* div_out, double* max_norm)
 {
     if (!p || !p->nodal) {
@@ -522,6 +538,28 @@ int gbp_mac_set_robin(gbp_plan* p, const gbp_array4* robin_a, const gbp_array4* 
         return GBP_BAD_ARG;
     }
     return p->mac->set_robin(robin_a, robin_b, (robin_f && robin_f->data) ? robin_f : nullptr);
+}
+
+int gbp_mac_set_eb(gbp_plan* p, const gbp_array4* vfrac, const gbp_array4* ax, const gbp_array4* ay,
+                   const gbp_array4* az, const gbp_array4* fx, const gbp_array4* fy, const gbp_array4* fz)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_mac_set_eb: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    if (!vfrac || !vfrac->data) return p->mac->set_eb(nullptr, nullptr, nullptr);
+    const gbp_array4* area[3] = {ax, ay, az};
+    const gbp_array4* fc[3] = {fx, fy, fz};
+    if (!valid_array(vfrac, 1)) {
+        set_error("gbp_mac_set_eb: bad volume-fraction array");
+        return GBP_BAD_ARG;
+    }
+    for (int d = 0; d < 3; ++d)
+        if (!valid_array(area[d], 1) || !valid_array(fc[d], 2)) {
+            set_error("gbp_mac_set_eb: need 3 area-fraction arrays and 3 face-centroid arrays with 2 components");
+            return GBP_BAD_ARG;
+        }
+    return p->mac->set_eb(vfrac, area, fc);
 }
 
 int gbp_mac_project(gbp_plan* p, gbp_array4* ux, gbp_array4* uy, gbp_array4* uz, gbp_array4* phi, int phi_guess,

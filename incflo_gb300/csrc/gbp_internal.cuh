@@ -42,6 +42,7 @@ struct NodalGeom {
     double ivol;   // 1 / vol
     double h[3];
     int iso;       // hx == hy == hz: K[1] = K[2] = K[4] = 0 and K[3..7] equal
+    const unsigned char* mask;  // overset mask over the padded nodes (0 = phi held at 0), or null
 };
 
 // Geometry of one cell-centred (MAC) level.
@@ -162,7 +163,8 @@ __device__ __forceinline__ void store_sigma_cell(T* a, const NodalGeom& g, int i
 __device__ __forceinline__ bool node_is_dirichlet(const NodalGeom& g, int i, int j, int k)
 {
     return (g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) ||
-           (g.dhi[1] && j == g.n[1]) || (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+           (g.dhi[1] && j == g.n[1]) || (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]) ||
+           (g.mask && !g.mask[pidx(g.sy, g.sz, i, j, k)]);
 }
 
 // Control volume of a node: h per direction, h/2 on a non-periodic boundary.

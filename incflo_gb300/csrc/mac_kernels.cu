@@ -125,24 +125,31 @@ __global__ void __launch_bounds__(1024) k_mac_bottom(CellGeom g, const double* _
     const long long N = (long long)g.n[0] * g.n[1] * g.n[2];
     for (long long t = threadIdx.x; t < 5 * P; t += blockDim.x) scr[t] = 0.0;
     __syncthreads();
-    double bs = 0.0;
+    double bs = 0.0, nf = 0.0;
     for (long long t = threadIdx.x; t < N; t += blockDim.x) {
         int i, j, k;
         decode_cell(g, t, i, j, k);
         const long long c = pidx(g.sy, g.sz, i, j, k);
         const double bv = (double)bin[c];
         r[c] = bv;
-        bs += bv;
         double d, off;
         (void)mac_Ax<double>(g, x, bx, by, bz, c, d, off);
         dg[c] = d;
+        if (d != 0.0) {  // cells fully covered by an embedded boundary have no equation
+            bs += bv;
+            nf += 1.0;
+        }
     }
     if (singular) {
-        const double mean = mac_block_sum(bs, red) / (double)N;
+        bs = mac_block_sum(bs, red);
+        nf = mac_block_sum(nf, red);
+        const double mean = nf > 0.0 ? bs / nf : 0.0;
+        __syncthreads();
         for (long long t = threadIdx.x; t < N; t += blockDim.x) {
             int i, j, k;
             decode_cell(g, t, i, j, k);
-            r[pidx(g.sy, g.sz, i, j, k)] -= mean;
+            const long long c = pidx(g.sy, g.sz, i, j, k);
+            r[c] = dg[c] != 0.0 ? r[c] - mean : 0.0;
         }
     }
     __syncthreads();
@@ -226,7 +233,8 @@ __device__ __forceinline__ double* a4p(const gbp_array4& a, int i, int j, int k,
 // Effective face beta of direction d for faces 0..n[d]: source 0 = array, 1 = constant,
 // 2 = dt / (0.5 (rho_lo + rho_hi)) (incflo: average_cellcenter_to_face then invert(dt)).
 __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double cval, int bclo, int bchi,
-                           double* __restrict__ b64, float* __restrict__ b32, RobinFaces rb)
+                           double* __restrict__ b64, float* __restrict__ b32, RobinFaces rb,
+                           const double* __restrict__ ap)
 {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int fn[3] = {g.n[0], g.n[1], g.n[2]};
@@ -275,6 +283,7 @@ __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double
             eff = 2.0 * beta;
         }
     }
+    if (ap) eff = ap[p] > 0.0 ? eff * ap[p] : 0.0;  // cut cells: the open fraction scales the flux
     b64[p] = eff;
     b32[p] = (float)eff;
 }
@@ -302,21 +311,32 @@ __global__ void k_mac_beta_coarsen(CellGeom gf, CellGeom gc, int d, const double
 }
 
 __global__ void __launch_bounds__(256) k_mac_rhs(CellGeom g, gbp_array4 ux, gbp_array4 uy, gbp_array4 uz,
-                                                 double* __restrict__ b)
+                                                 double* __restrict__ b, MacEB eb)
 {
     int i, j, k;
     if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
     const int ip = (g.per[0] && i + 1 == g.n[0]) ? 0 : i + 1;
     const int jp = (g.per[1] && j + 1 == g.n[1]) ? 0 : j + 1;
     const int kp = (g.per[2] && k + 1 == g.n[2]) ? 0 : k + 1;
-    const double dv = (a4(ux, ip, j, k, 0) - a4(ux, i, j, k, 0)) / g.h[0] +
-                      (a4(uy, i, jp, k, 0) - a4(uy, i, j, k, 0)) / g.h[1] +
-                      (a4(uz, i, j, kp, 0) - a4(uz, i, j, k, 0)) / g.h[2];
-    b[pidx(g.sy, g.sz, i, j, k)] = -g.vol * dv;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    double fx0 = a4(ux, i, j, k, 0), fx1 = a4(ux, ip, j, k, 0);
+    double fy0 = a4(uy, i, j, k, 0), fy1 = a4(uy, i, jp, k, 0);
+    double fz0 = a4(uz, i, j, k, 0), fz1 = a4(uz, i, j, kp, 0);
+    if (eb.ap[0]) {
+        // cut cells: fluxes through the open part of each face only (no flow through the EB)
+        fx0 *= eb.ap[0][p];
+        fx1 *= eb.ap[0][p + 1];
+        fy0 *= eb.ap[1][p];
+        fy1 *= eb.ap[1][p + g.sy];
+        fz0 *= eb.ap[2][p];
+        fz1 *= eb.ap[2][p + g.sz];
+    }
+    const double dv = (fx1 - fx0) / g.h[0] + (fy1 - fy0) / g.h[1] + (fz1 - fz0) / g.h[2];
+    b[p] = -g.vol * dv;
 }
 
 __global__ void __launch_bounds__(256) k_mac_correct(CellGeom g, int d, gbp_array4 u, const double* __restrict__ beta,
-                                                     const double* __restrict__ phi)
+                                                     const double* __restrict__ phi, const double* __restrict__ ap)
 {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int fn[3] = {g.n[0], g.n[1], g.n[2]};
@@ -330,8 +350,9 @@ __global__ void __launch_bounds__(256) k_mac_correct(CellGeom g, int d, gbp_arra
     f[0] = (int)(rem - (long long)f[1] * fn[0]);
     const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
     const long long s = d == 0 ? 1 : (d == 1 ? g.sy : g.sz);
-    const double be = beta[p];
+    double be = beta[p];
     if (be == 0.0) return;
+    if (ap) be /= ap[p];  // beta here is ap x beta (be != 0 implies ap > 0)
     double* up = a4p(u, f[0], f[1], f[2], 0);
     *up -= be * (phi[p] - phi[p - s]) / g.h[d];
 }
@@ -350,43 +371,57 @@ __global__ void k_mac_store_phi(CellGeom g, gbp_array4 out, const double* __rest
     *a4p(out, i, j, k, 0) = phi[pidx(g.sy, g.sz, i, j, k)];
 }
 
-__global__ void __launch_bounds__(256) k_mac_norm(CellGeom g, const double* __restrict__ v, unsigned long long* norm)
+__global__ void __launch_bounds__(256) k_mac_norm(CellGeom g, const double* __restrict__ v, unsigned long long* norm,
+                                                  const double* __restrict__ kap)
 {
     int i, j, k;
     double nv = 0.0;
-    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k))
-        nv = fabs(v[pidx(g.sy, g.sz, i, j, k)]) / g.vol;
+    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        if (!kap)
+            nv = fabs(v[p]) / g.vol;
+        else if (kap[p] > 0.0)
+            nv = fabs(v[p]) / (kap[p] * g.vol);  // the cut-cell operator divides by the volume fraction
+    }
     nv = block_max(nv);
     if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
 }
 
-__global__ void k_mac_sums(CellGeom g, const double* __restrict__ v, double* __restrict__ part)
+// per-block sums of v (kap != null and weighted: of kap * v)
+__global__ void k_mac_sums(CellGeom g, const double* __restrict__ v, double* __restrict__ part,
+                           const double* __restrict__ kap, int weighted)
 {
     __shared__ double red[32];
     int i, j, k;
     double acc = 0.0;
-    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) acc = v[pidx(g.sy, g.sz, i, j, k)];
+    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        acc = (kap && weighted) ? kap[p] * v[p] : v[p];
+    }
     acc = mac_block_sum(acc, red);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-// mode 0: b -= mean(b); mode 1: x -= mean(x) with periodic aliases
+// mode 0: b_c -= kappa_c sum(b) / sum(kappa), so that sum(b) = 0 (the range of the operator);
+// mode 1: x -= its volume-weighted mean, with periodic aliases, and 0 in covered cells. Without cut
+// cells kappa = 1 and nfluid = the cell count.
 __global__ void k_mac_remove_mean(CellGeom g, double* __restrict__ v, const double* __restrict__ part, int nparts,
-                                  int mode)
+                                  int mode, const double* __restrict__ kap, double nfluid)
 {
     __shared__ double red[32];
     double acc = 0.0;
     for (int t = threadIdx.x; t < nparts; t += blockDim.x) acc += part[t];
     acc = mac_block_sum(acc, red);
-    const double c = acc / ((double)g.n[0] * g.n[1] * g.n[2]);
+    const double c = acc / nfluid;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         if (!decode_cell(g, t, i, j, k)) break;
         const long long p = pidx(g.sy, g.sz, i, j, k);
+        const double kc = kap ? kap[p] : 1.0;
         if (mode == 0)
-            v[p] -= c * g.vol;
+            v[p] -= c * kc;
         else
-            store_cell(v, g, i, j, k, v[p] - c);
+            store_cell(v, g, i, j, k, kc > 0.0 ? v[p] - c : 0.0);
     }
 }
 
@@ -458,13 +493,44 @@ GBP_MAC_INST(double)
 GBP_MAC_INST(float)
 
 void mac_set_beta(const CellGeom& g, int d, int source, const gbp_array4* src, double cval, int bclo, int bchi,
-                  double* b64, float* b32, cudaStream_t st, const RobinFaces* rb)
+                  double* b64, float* b32, cudaStream_t st, const RobinFaces* rb, const double* ap)
 {
     gbp_array4 a{};
     if (src) a = *src;
     RobinFaces r{};
     if (rb) r = *rb;
-    k_mac_beta<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, source, a, cval, bclo, bchi, b64, b32, r);
+    k_mac_beta<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, source, a, cval, bclo, bchi, b64, b32, r, ap);
+}
+
+__global__ void k_mac_load_kappa(CellGeom g, gbp_array4 in, double* __restrict__ kap)
+{
+    int i, j, k;
+    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k))
+        store_cell(kap, g, i, j, k, a4(in, i, j, k, 0));
+}
+
+__global__ void k_mac_load_aperture(CellGeom g, int d, gbp_array4 in, double* __restrict__ ap)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int fn[3] = {g.n[0], g.n[1], g.n[2]};
+    fn[d] += 1;
+    if (t >= (long long)fn[0] * fn[1] * fn[2]) return;
+    int f[3];
+    f[0] = (int)(t % fn[0]);
+    f[1] = (int)((t / fn[0]) % fn[1]);
+    f[2] = (int)(t / ((long long)fn[0] * fn[1]));
+    ap[pidx(g.sy, g.sz, f[0], f[1], f[2])] = a4(in, f[0], f[1], f[2], 0);
+}
+
+void mac_load_eb(const CellGeom& g, const gbp_array4& vfrac, const gbp_array4* const apf[3], const MacEB& eb,
+                 cudaStream_t st)
+{
+    cudaMemsetAsync(eb.kap, 0, sizeof(double) * g.count, st);
+    k_mac_load_kappa<<<nblk(ncell(g), 256), 256, 0, st>>>(g, vfrac, eb.kap);
+    for (int d = 0; d < 3; ++d) {
+        cudaMemsetAsync(eb.ap[d], 0, sizeof(double) * g.count, st);
+        k_mac_load_aperture<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, *apf[d], eb.ap[d]);
+    }
 }
 
 __global__ void k_mac_robin_factors(CellGeom g, int d, int hi, gbp_array4 a, gbp_array4 b, gbp_array4 f, int has_f,
@@ -498,7 +564,8 @@ void mac_robin_factors(const CellGeom& g, int d, int hi, const gbp_array4& a, co
 }
 
 __global__ void k_mac_robin_apply(CellGeom g, int d, int hi, const double* __restrict__ braw,
-                                  const double* __restrict__ rfac, double* __restrict__ b64, float* __restrict__ b32)
+                                  const double* __restrict__ rfac, double* __restrict__ b64, float* __restrict__ b32,
+                                  const double* __restrict__ ap)
 {
     const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -508,17 +575,18 @@ __global__ void k_mac_robin_apply(CellGeom g, int d, int hi, const double* __res
     f[d2] = (int)(t / g.n[d1]);
     f[d] = hi ? g.n[d] : 0;
     const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
-    const double eff = braw[t] * rfac[t];
+    double eff = braw[t] * rfac[t];
+    if (ap) eff = ap[p] > 0.0 ? eff * ap[p] : 0.0;
     b64[p] = eff;
     b32[p] = (float)eff;
 }
 
 void mac_robin_apply(const CellGeom& g, int d, int hi, const double* braw, const double* rfac, double* b64,
-                     float* b32, cudaStream_t st)
+                     float* b32, cudaStream_t st, const double* ap)
 {
     const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
     const long long n = (long long)g.n[d1] * g.n[d2];
-    k_mac_robin_apply<<<nblk(n, 256), 256, 0, st>>>(g, d, hi, braw, rfac, b64, b32);
+    k_mac_robin_apply<<<nblk(n, 256), 256, 0, st>>>(g, d, hi, braw, rfac, b64, b32, ap);
 }
 void mac_coarsen_beta(const CellGeom& gf, const CellGeom& gc, int d, const double* bf, double* bc64, float* bc32,
                       cudaStream_t st)
@@ -526,14 +594,16 @@ void mac_coarsen_beta(const CellGeom& gf, const CellGeom& gc, int d, const doubl
     k_mac_beta_coarsen<<<nblk(nface(gc, d), 256), 256, 0, st>>>(gf, gc, d, bf, bc64, bc32);
 }
 void mac_rhs(const CellGeom& g, const gbp_array4& ux, const gbp_array4& uy, const gbp_array4& uz, double* b,
-             cudaStream_t st)
+             cudaStream_t st, const MacEB* eb)
 {
-    k_mac_rhs<<<nblk(ncell(g), 256), 256, 0, st>>>(g, ux, uy, uz, b);
+    MacEB e{};
+    if (eb) e = *eb;
+    k_mac_rhs<<<nblk(ncell(g), 256), 256, 0, st>>>(g, ux, uy, uz, b, e);
 }
 void mac_correct(const CellGeom& g, int d, const gbp_array4& u, const double* beta, const double* phi,
-                 cudaStream_t st)
+                 cudaStream_t st, const double* ap)
 {
-    k_mac_correct<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, u, beta, phi);
+    k_mac_correct<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, u, beta, phi, ap);
 }
 void mac_load_phi(const CellGeom& g, const gbp_array4& in, double* phi, cudaStream_t st)
 {
@@ -543,16 +613,159 @@ void mac_store_phi(const CellGeom& g, const gbp_array4& out, const double* phi, 
 {
     k_mac_store_phi<<<nblk(ncell(g), 256), 256, 0, st>>>(g, out, phi);
 }
-void mac_norm(const CellGeom& g, const double* v, unsigned long long* norm, cudaStream_t st)
+void mac_norm(const CellGeom& g, const double* v, unsigned long long* norm, cudaStream_t st, const double* kap)
 {
-    k_mac_norm<<<nblk(ncell(g), 256), 256, 0, st>>>(g, v, norm);
+    k_mac_norm<<<nblk(ncell(g), 256), 256, 0, st>>>(g, v, norm, kap);
 }
 int mac_partials_needed(const CellGeom& g) { return (int)nblk(ncell(g), 256); }
-void mac_remove_mean(const CellGeom& g, double* v, double* partials, int mode, cudaStream_t st)
+void mac_remove_mean(const CellGeom& g, double* v, double* partials, int mode, cudaStream_t st, const double* kap,
+                     double nfluid)
 {
     const unsigned nb = nblk(ncell(g), 256);
-    k_mac_sums<<<nb, 256, 0, st>>>(g, v, partials);
-    k_mac_remove_mean<<<nb < 1024 ? nb : 1024, 256, 0, st>>>(g, v, partials, (int)nb, mode);
+    if (!kap) nfluid = (double)g.n[0] * g.n[1] * g.n[2];
+    k_mac_sums<<<nb, 256, 0, st>>>(g, v, partials, kap, mode);
+    k_mac_remove_mean<<<nb < 1024 ? nb : 1024, 256, 0, st>>>(g, v, partials, (int)nb, mode, kap, nfluid);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Cut cells (embedded boundary) on the finest level. The 7-point part of the operator carries the
+// apertures in its face betas; the kernels below add the difference between the centroid and the
+// face-centre normal derivative on the few cut faces, from a table built once per geometry.
+__global__ void k_mac_pack_faces(CellGeom g, int d, gbp_array4 in, int c, double* __restrict__ out)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int fn[3] = {g.n[0], g.n[1], g.n[2]};
+    if (d >= 0) fn[d] += 1;
+    if (t >= (long long)fn[0] * fn[1] * fn[2]) return;
+    const int i = (int)(t % fn[0]);
+    const int j = (int)((t / fn[0]) % fn[1]);
+    const int k = (int)(t / ((long long)fn[0] * fn[1]));
+    out[t] = a4(in, i, j, k, c);
+}
+
+void mac_pack_faces(const CellGeom& g, int d, const gbp_array4& in, int c, double* out, cudaStream_t st)
+{
+    k_mac_pack_faces<<<nblk(d >= 0 ? nface(g, d) : ncell(g), 256), 256, 0, st>>>(g, d, in, c, out);
+}
+
+struct EbPtrs {
+    const double* b[3];
+    const double* ap[3];
+};
+
+__global__ void k_eb_table_beta(const EbFace* __restrict__ F, int nf, EbPtrs P, double* __restrict__ cb64,
+                                float* __restrict__ cb32)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nf) return;
+    const EbFace& f = F[e];
+    for (int m = 0; m < 4; ++m) {
+        double v = 0.0;
+        if (m < f.nm) {
+            const long long q = f.pf[m];
+            v = f.coef[m] * (P.b[f.d][q] / P.ap[f.d][q]);
+        }
+        cb64[4 * e + m] = v;
+        cb32[4 * e + m] = (float)v;
+    }
+}
+
+void eb_table_beta(const EbFace* F, int nf, const double* const b64[3], const double* const ap[3], double* cb64,
+                   float* cb32, cudaStream_t st)
+{
+    if (nf <= 0) return;
+    EbPtrs P;
+    for (int d = 0; d < 3; ++d) {
+        P.b[d] = b64[d];
+        P.ap[d] = ap[d];
+    }
+    k_eb_table_beta<<<nblk(nf, 128), 128, 0, st>>>(F, nf, P, cb64, cb32);
+}
+
+template <typename T>
+__device__ __forceinline__ T eb_dflux(const EbFace& f, const T* __restrict__ cb, int e, const T* __restrict__ x,
+                                      long long sd)
+{
+    T acc = T(0);
+    for (int m = 0; m < f.nm; ++m) acc += cb[4 * e + m] * (x[f.pf[m]] - x[f.pf[m] - sd]);
+    return acc;
+}
+
+template <typename T>
+__global__ void k_eb_cells(CellGeom g, const EbCell* __restrict__ C, int nc, const EbFace* __restrict__ F,
+                           const T* __restrict__ cb, const T* __restrict__ x, const T* in, T* out)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nc) return;
+    const EbCell c = C[e];
+    const long long sd[3] = {1, g.sy, g.sz};
+    T corr = T(0);
+    for (int s = 0; s < 6; ++s) {
+        const int q = c.slot[s];
+        if (q < 0) continue;
+        const EbFace& f = F[q];
+        const T df = eb_dflux<T>(f, cb, q, x, sd[f.d]);
+        // (A phi)_c = -(F_high - F_low) summed over the directions
+        corr += (s & 1) ? -df : df;
+    }
+    out[c.p] = in[c.p] - corr;
+}
+
+template <typename T>
+void eb_cells(const CellGeom& g, const EbCell* C, int nc, const EbFace* F, const T* cb, const T* x, const T* in,
+              T* out, cudaStream_t st)
+{
+    if (nc <= 0) return;
+    k_eb_cells<T><<<nblk(nc, 128), 128, 0, st>>>(g, C, nc, F, cb, x, in, out);
+}
+template void eb_cells<double>(const CellGeom&, const EbCell*, int, const EbFace*, const double*, const double*,
+                               const double*, double*, cudaStream_t);
+template void eb_cells<float>(const CellGeom&, const EbCell*, int, const EbFace*, const float*, const float*,
+                              const float*, float*, cudaStream_t);
+
+struct EbU {
+    gbp_array4 u[3];
+};
+
+__global__ void k_eb_correct_u(CellGeom g, const EbFace* __restrict__ F, int nf, EbPtrs P,
+                               const double* __restrict__ phi, EbU U)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nf) return;
+    const EbFace& f = F[e];
+    const long long sd = f.d == 0 ? 1 : (f.d == 1 ? g.sy : g.sz);
+    double acc = 0.0;
+    for (int m = 0; m < f.nm; ++m) {
+        const long long q = f.pf[m];
+        acc += f.vcoef[m] * (P.b[f.d][q] / P.ap[f.d][q]) * (phi[q] - phi[q - sd]);
+    }
+    *a4p(U.u[f.d], f.f[0], f.f[1], f.f[2], 0) -= acc;
+}
+
+void eb_correct_u(const CellGeom& g, const EbFace* F, int nf, const double* const b64[3], const double* const ap[3],
+                  const double* phi, gbp_array4* const u[3], cudaStream_t st)
+{
+    if (nf <= 0) return;
+    EbPtrs P;
+    EbU U;
+    for (int d = 0; d < 3; ++d) {
+        P.b[d] = b64[d];
+        P.ap[d] = ap[d];
+        U.u[d] = *u[d];
+    }
+    k_eb_correct_u<<<nblk(nf, 128), 128, 0, st>>>(g, F, nf, P, phi, U);
+}
+
+__global__ void k_eb_zero_covered(CellGeom g, const double* __restrict__ kap, double* phi)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    if (!(kap[pidx(g.sy, g.sz, i, j, k)] > 0.0)) store_cell(phi, g, i, j, k, 0.0);
+}
+
+void eb_zero_covered(const CellGeom& g, const double* kap, double* phi, cudaStream_t st)
+{
+    k_eb_zero_covered<<<nblk(ncell(g), 256), 256, 0, st>>>(g, kap, phi);
 }
 template <typename TE>
 void mac_add_correction(const CellGeom& g, double* x, const TE* e, double inv_scale, cudaStream_t st)

@@ -5,6 +5,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <unordered_map>
+#include <vector>
 
 #include "mac_solver.h"
 
@@ -43,6 +45,8 @@ void MacSolver::destroy()
     if (ev2) cudaEventDestroy(ev2);
     ev0 = ev1 = ev2 = nullptr;
     pool.release();
+    eb.pool.release();
+    eb = EbState{};
     L.clear();
     beta_ready = false;
 }
@@ -192,13 +196,242 @@ int MacSolver::set_beta(int source, const gbp_array4* src[3], double cval)
 {
     for (int d = 0; d < 3; ++d) {
         const gbp_array4* s = source == 0 ? src[d] : (source == 2 ? src[0] : nullptr);
-        mac_set_beta(L[0].g, d, source, s, cval, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st, &rb);
+        mac_set_beta(L[0].g, d, source, s, cval, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st, &rb,
+                     eb.on ? eb.m.ap[d] : nullptr);
     }
     for (size_t l = 1; l < L.size(); ++l)
         for (int d = 0; d < 3; ++d)
             mac_coarsen_beta(L[l - 1].g, L[l].g, d, L[l - 1].b64[d], L[l].b64[d], L[l].b32[d], st);
+    eb_refresh_beta();
     GBP_CUDA(cudaGetLastError());
     beta_ready = true;
+    return GBP_OK;
+}
+
+void MacSolver::eb_refresh_beta()
+{
+    if (!eb.on) return;
+    const double* b[3] = {L[0].b64[0], L[0].b64[1], L[0].b64[2]};
+    const double* a[3] = {eb.m.ap[0], eb.m.ap[1], eb.m.ap[2]};
+    eb_table_beta(eb.faces, eb.nfaces, b, a, eb.cb64, eb.cb32, st);
+}
+
+// Cut-face table of the finest level. For a cut face (0 < ap < 1) off the non-periodic domain sides,
+// the normal derivative at its centroid is the bilinear blend of the face-centre differences of the face
+// and of its neighbours f1, f2, f12 one cell towards the centroid in the two tangential directions
+// (weights |offset|); a neighbour enters only if open, the corner only with both f1 and f2 (else the
+// second weight drops). This is the face-centroid gradient of the cut-cell finite-volume method that
+// AMReX's MLEBABecLap uses for the MAC projection (Location::FaceCentroid, src/incflo.cpp:286-292).
+int MacSolver::set_eb(const gbp_array4* vfrac, const gbp_array4* const area[3], const gbp_array4* const fcent[3])
+{
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    beta_ready = false;
+    GBP_CUDA(cudaStreamSynchronize(st));
+    eb.pool.release();
+    eb = EbState{};
+    if (!vfrac) return GBP_OK;
+    for (int d = 0; d < 3; ++d)
+        if (!area || !fcent || !area[d] || !fcent[d] || !area[d]->data || !fcent[d]->data || fcent[d]->ncomp < 2) {
+            set_error("mac_set_eb: need the volume fractions, 3 area-fraction arrays and 3 face-centroid arrays "
+                      "(2 components)");
+            return GBP_BAD_ARG;
+        }
+    if (!vfrac->data) {
+        set_error("mac_set_eb: null volume-fraction data");
+        return GBP_BAD_ARG;
+    }
+    const CellGeom& g = L[0].g;
+    const int* n = g.n;
+    // every array must cover its index space
+    auto covers = [&](const gbp_array4& a, int d) {
+        for (int e = 0; e < 3; ++e) {
+            const int hi = n[e] - 1 + (e == d ? 1 : 0);
+            if (a.lo[e] > 0 || a.hi[e] < hi) return false;
+        }
+        return true;
+    };
+    bool ok = covers(*vfrac, -1);
+    for (int d = 0; d < 3; ++d) ok = ok && covers(*area[d], d) && covers(*fcent[d], d);
+    if (!ok) {
+        set_error("mac_set_eb: an EB array does not cover the cells / faces of the level");
+        return GBP_BAD_ARG;
+    }
+    // host copies (dense, x fastest)
+    long long fnum[3];
+    int fn[3][3];
+    for (int d = 0; d < 3; ++d) {
+        for (int e = 0; e < 3; ++e) fn[d][e] = n[e] + (e == d ? 1 : 0);
+        fnum[d] = (long long)fn[d][0] * fn[d][1] * fn[d][2];
+    }
+    const long long ncell = (long long)n[0] * n[1] * n[2];
+    long long mx = ncell;
+    for (int d = 0; d < 3; ++d) mx = std::max(mx, fnum[d]);
+    double* tmp = nullptr;
+    GBP_CUDA(cudaMalloc(&tmp, sizeof(double) * (size_t)mx));
+    std::vector<double> kapH((size_t)ncell), apH[3], fcH[3][2];
+    auto fetch = [&](const gbp_array4& a, int d, int c, std::vector<double>& out) -> int {
+        const long long cnt = d < 0 ? ncell : fnum[d];
+        out.resize((size_t)cnt);
+        mac_pack_faces(g, d, a, c, tmp, st);
+        cudaError_t e = cudaMemcpyAsync(out.data(), tmp, sizeof(double) * (size_t)cnt, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        return e == cudaSuccess ? GBP_OK : cuda_fail(e, "mac_set_eb: copy of the EB arrays");
+    };
+    int rc = fetch(*vfrac, -1, 0, kapH);
+    for (int d = 0; d < 3 && !rc; ++d) {
+        rc = fetch(*area[d], d, 0, apH[d]);
+        for (int c = 0; c < 2 && !rc; ++c) rc = fetch(*fcent[d], d, c, fcH[d][c]);
+    }
+    cudaFree(tmp);
+    if (rc) return rc;
+    auto cid = [&](int i, int j, int k) { return i + (long long)n[0] * (j + (long long)n[1] * k); };
+    auto fid = [&](int d, int i, int j, int k) { return i + (long long)fn[d][0] * (j + (long long)fn[d][1] * k); };
+    double ksum = 0.0;
+    for (long long c = 0; c < ncell; ++c) {
+        const double v = kapH[(size_t)c];
+        if (!(v >= 0.0 && v <= 1.0)) {
+            set_error("mac_set_eb: volume fractions must lie in [0, 1]");
+            return GBP_BAD_ARG;
+        }
+        ksum += v;
+    }
+    if (!(ksum > 0.0)) {
+        set_error("mac_set_eb: every cell is covered");
+        return GBP_BAD_ARG;
+    }
+    for (int d = 0; d < 3; ++d)
+        for (int k = 0; k < fn[d][2]; ++k)
+            for (int j = 0; j < fn[d][1]; ++j)
+                for (int i = 0; i < fn[d][0]; ++i) {
+                    const long long q = fid(d, i, j, k);
+                    const double a = apH[d][(size_t)q];
+                    const double o0 = fcH[d][0][(size_t)q], o1 = fcH[d][1][(size_t)q];
+                    if (!(a >= 0.0 && a <= 1.0) || !(fabs(o0) <= 0.5 + 1e-12) || !(fabs(o1) <= 0.5 + 1e-12)) {
+                        set_error("mac_set_eb: area fractions must lie in [0, 1] and centroid offsets in [-0.5, 0.5]");
+                        return GBP_BAD_ARG;
+                    }
+                    if (a > 0.0) {
+                        int c[3] = {i, j, k};
+                        const int fd = c[d];
+                        for (int side = 0; side < 2; ++side) {
+                            int cc[3] = {c[0], c[1], c[2]};
+                            cc[d] = fd - 1 + side;
+                            if (g.per[d]) cc[d] = (cc[d] + n[d]) % n[d];
+                            if (cc[d] < 0 || cc[d] >= n[d]) continue;
+                            if (!(kapH[(size_t)cid(cc[0], cc[1], cc[2])] > 0.0)) {
+                                set_error("mac_set_eb: an open face (area fraction > 0) touches a covered cell");
+                                return GBP_BAD_ARG;
+                            }
+                        }
+                    }
+                }
+    // cut-face table
+    std::vector<EbFace> F;
+    std::unordered_map<long long, int> cell_of;
+    std::vector<EbCell> C;
+    const long long sd[3] = {1, g.sy, g.sz};
+    auto add_slot = [&](int i, int j, int k, int slot, int e) {
+        const long long key = cid(i, j, k);
+        auto it = cell_of.find(key);
+        int ci;
+        if (it == cell_of.end()) {
+            EbCell ec;
+            ec.p = pidx(g.sy, g.sz, i, j, k);
+            for (int s = 0; s < 6; ++s) ec.slot[s] = -1;
+            ci = (int)C.size();
+            C.push_back(ec);
+            cell_of.emplace(key, ci);
+        } else {
+            ci = it->second;
+        }
+        C[(size_t)ci].slot[slot] = e;
+    };
+    for (int d = 0; d < 3; ++d) {
+        const int t1 = d == 0 ? 1 : 0, t2 = d == 2 ? 1 : 2;
+        for (int k = 0; k < fn[d][2]; ++k)
+            for (int j = 0; j < fn[d][1]; ++j)
+                for (int i = 0; i < fn[d][0]; ++i) {
+                    const long long q = fid(d, i, j, k);
+                    const double a = apH[d][(size_t)q];
+                    if (!(a > 0.0 && a < 1.0)) continue;
+                    int f[3] = {i, j, k};
+                    const int fd = f[d];
+                    if (!g.per[d] && (fd == 0 || fd == n[d])) continue;  // no blend on domain sides
+                    const double o[2] = {fcH[d][0][(size_t)q], fcH[d][1][(size_t)q]};
+                    const int s1 = o[0] >= 0.0 ? 1 : -1, s2 = o[1] >= 0.0 ? 1 : -1;
+                    auto shift = [&](const int* in, int t, int s, int* out) {
+                        for (int e = 0; e < 3; ++e) out[e] = in[e];
+                        out[t] += s;
+                        if (g.per[t]) out[t] = (out[t] + n[t]) % n[t];
+                        return out[t] >= 0 && out[t] < n[t];
+                    };
+                    auto open = [&](const int* ff) { return apH[d][(size_t)fid(d, ff[0], ff[1], ff[2])] > 0.0; };
+                    int f1[3], f2[3], f12[3];
+                    const bool h1 = shift(f, t1, s1, f1) && open(f1);
+                    const bool h2 = shift(f, t2, s2, f2) && open(f2);
+                    double w1 = h1 ? fabs(o[0]) : 0.0, w2 = h2 ? fabs(o[1]) : 0.0;
+                    bool h12 = false;
+                    if (w1 > 0.0 && w2 > 0.0) {
+                        h12 = shift(f1, t2, s2, f12) && open(f12);
+                        if (!h12) w2 = 0.0;
+                    }
+                    if (w1 == 0.0 && w2 == 0.0) continue;
+                    EbFace e{};
+                    e.d = d;
+                    for (int c = 0; c < 3; ++c) e.f[c] = f[c];
+                    const double wd = g.w[d], hd = g.h[d];
+                    auto put = [&](const int* ff, double wt) {
+                        const int m = e.nm++;
+                        e.pf[m] = pidx(g.sy, g.sz, ff[0], ff[1], ff[2]);
+                        e.coef[m] = a * wd * wt;
+                        e.vcoef[m] = wt / hd;
+                    };
+                    put(f, (1.0 - w1) * (1.0 - w2) - 1.0);
+                    if (w1 > 0.0) put(f1, w1 * (1.0 - w2));
+                    if (w2 > 0.0) put(f2, (1.0 - w1) * w2);
+                    if (w1 > 0.0 && w2 > 0.0) put(f12, w1 * w2);
+                    (void)sd;
+                    const int ei = (int)F.size();
+                    F.push_back(e);
+                    // the face is the low face of cell f (if inside) and the high face of cell f - e_d
+                    if (fd < n[d]) add_slot(f[0], f[1], f[2], 2 * d, ei);
+                    if (fd >= 1) {
+                        int c[3] = {f[0], f[1], f[2]};
+                        c[d] -= 1;
+                        add_slot(c[0], c[1], c[2], 2 * d + 1, ei);
+                    }
+                }
+    }
+    // device storage
+    size_t need = 0;
+    auto add = [&](size_t cnt, size_t sz) { need = ((need + 255) & ~size_t(255)) + cnt * sz; };
+    for (int q = 0; q < 5; ++q) add(g.count, 8);
+    add(g.count, 4);
+    add(F.size() + 1, sizeof(EbFace));
+    add(C.size() + 1, sizeof(EbCell));
+    add(4 * F.size() + 4, 8);
+    add(4 * F.size() + 4, 4);
+    need += 4096;
+    rc = eb.pool.reserve(need);
+    if (rc) return rc;
+    eb.m.kap = eb.pool.take<double>(g.count);
+    for (int d = 0; d < 3; ++d) eb.m.ap[d] = eb.pool.take<double>(g.count);
+    eb.beff64 = eb.pool.take<double>(g.count);
+    eb.beff32 = eb.pool.take<float>(g.count);
+    eb.faces = eb.pool.take<EbFace>(F.size() + 1);
+    eb.cells = eb.pool.take<EbCell>(C.size() + 1);
+    eb.cb64 = eb.pool.take<double>(4 * F.size() + 4);
+    eb.cb32 = eb.pool.take<float>(4 * F.size() + 4);
+    eb.nfaces = (int)F.size();
+    eb.ncells = (int)C.size();
+    eb.kap_sum = ksum;
+    if (!F.empty()) GBP_CUDA(cudaMemcpyAsync(eb.faces, F.data(), sizeof(EbFace) * F.size(), cudaMemcpyHostToDevice, st));
+    if (!C.empty()) GBP_CUDA(cudaMemcpyAsync(eb.cells, C.data(), sizeof(EbCell) * C.size(), cudaMemcpyHostToDevice, st));
+    mac_load_eb(g, *vfrac, area, eb.m, st);
+    GBP_CUDA(cudaGetLastError());
+    GBP_CUDA(cudaStreamSynchronize(st));  // the host tables go out of scope
+    eb.on = true;
     return GBP_OK;
 }
 
@@ -227,11 +460,13 @@ int MacSolver::set_robin(const gbp_array4* a, const gbp_array4* b, const gbp_arr
         for (int q = 0; q < 6; ++q)
             if (rb.rfac[q]) {
                 const int d = q >> 1;
-                mac_robin_apply(L[0].g, d, q & 1, rb.braw[q], rb.rfac[q], L[0].b64[d], L[0].b32[d], st);
+                mac_robin_apply(L[0].g, d, q & 1, rb.braw[q], rb.rfac[q], L[0].b64[d], L[0].b32[d], st,
+                                eb.on ? eb.m.ap[d] : nullptr);
             }
         for (size_t l = 1; l < L.size(); ++l)
             for (int d = 0; d < 3; ++d)
                 mac_coarsen_beta(L[l - 1].g, L[l].g, d, L[l - 1].b64[d], L[l].b64[d], L[l].b32[d], st);
+        eb_refresh_beta();
         GBP_CUDA(cudaGetLastError());
     }
     // a Robin face with a > 0 pins phi like a Dirichlet face
@@ -248,6 +483,10 @@ template <typename T>
 struct MacBufs;
 template <>
 struct MacBufs<double> {
+    template <typename E>
+    static double* beff(const E& e) { return e.beff64; }
+    template <typename E>
+    static const double* cb(const E& e) { return e.cb64; }
     static double* const* b(const MacLevel& l) { return l.b64; }
     static double* x(const MacLevel& l) { return l.x64; }
     static double* rhs(const MacLevel& l) { return l.rhs64; }
@@ -255,6 +494,10 @@ struct MacBufs<double> {
 };
 template <>
 struct MacBufs<float> {
+    template <typename E>
+    static float* beff(const E& e) { return e.beff32; }
+    template <typename E>
+    static const float* cb(const E& e) { return e.cb32; }
     static float* const* b(const MacLevel& l) { return l.b32; }
     static float* x(const MacLevel& l) { return l.x32; }
     static float* rhs(const MacLevel& l) { return l.rhs32; }
@@ -275,19 +518,46 @@ void MacSolver::vcycle(int l, const T* b, bool zero)
     }
     T* const* be = B::b(lv);
     if (zero) cudaMemsetAsync(x, 0, sizeof(T) * lv.g.count, s);
+    // cut cells on the finest level: the smoother sees b minus the cut-face terms of the current x
+    // (lagged by one red-black pair), the residual carries them exactly
+    const bool cut = l == 0 && eb.on;
+    const T* bs = b;
+    if (cut) {
+        T* beff = B::beff(eb);
+        cudaMemcpyAsync(beff, b, sizeof(T) * lv.g.count, cudaMemcpyDeviceToDevice, s);
+        bs = beff;
+    }
+    auto lag = [&]() {
+        if (cut) eb_cells<T>(lv.g, eb.cells, eb.ncells, eb.faces, B::cb(eb), x, b, B::beff(eb), s);
+    };
     for (int q = 0; q < opt.nu1; ++q) {
-        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 0, s);
-        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 1, s);
+        lag();
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], bs, x, 0, s);
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], bs, x, 1, s);
     }
     mac_resid<T>(lv.g, be[0], be[1], be[2], x, b, B::r(lv), nullptr, s);
+    if (cut) eb_cells<T>(lv.g, eb.cells, eb.ncells, eb.faces, B::cb(eb), x, B::r(lv), B::r(lv), s);
     const MacLevel& cv = L[l + 1];
     mac_restrict<T>(lv.g, cv.g, B::r(lv), B::rhs(cv), s);
     vcycle<T>(l + 1, B::rhs(cv), true);
     mac_prolong_add<T>(lv.g, cv.g, B::x(cv), x, s);
     for (int q = 0; q < opt.nu2; ++q) {
-        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 1, s);
-        mac_rbgs<T>(lv.g, be[0], be[1], be[2], b, x, 0, s);
+        lag();
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], bs, x, 1, s);
+        mac_rbgs<T>(lv.g, be[0], be[1], be[2], bs, x, 0, s);
     }
+}
+
+void MacSolver::resid64(const double* x, const double* b, double* r, unsigned long long* norm, cudaStream_t s)
+{
+    const MacLevel& l0 = L[0];
+    if (!eb.on) {
+        mac_resid<double>(l0.g, l0.b64[0], l0.b64[1], l0.b64[2], x, b, r, norm, s);
+        return;
+    }
+    mac_resid<double>(l0.g, l0.b64[0], l0.b64[1], l0.b64[2], x, b, r, nullptr, s);
+    eb_cells<double>(l0.g, eb.cells, eb.ncells, eb.faces, eb.cb64, x, r, r, s);
+    mac_norm(l0.g, r, norm, s, eb.m.kap);
 }
 
 void MacSolver::record_iteration()
@@ -304,7 +574,7 @@ void MacSolver::record_iteration()
         mac_add_correction<double>(l0.g, phi, l0.x64, 1.0, s);
     }
     cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), s);
-    mac_resid<double>(l0.g, l0.b64[0], l0.b64[1], l0.b64[2], phi, rhs0, res, dnorm + 1, s);
+    resid64(phi, rhs0, res, dnorm + 1, s);
     cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
 }
 
@@ -353,8 +623,8 @@ int MacSolver::solve(bool have_guess, gbp_stats* stats)
     GBP_CUDA(cudaEventRecord(ev1, st));
     if (!have_guess) GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
     GBP_CUDA(cudaMemsetAsync(dnorm, 0, 4 * sizeof(unsigned long long), st));
-    mac_norm(l0.g, rhs0, dnorm, st);
-    mac_resid<double>(l0.g, l0.b64[0], l0.b64[1], l0.b64[2], phi, rhs0, res, dnorm + 1, st);
+    mac_norm(l0.g, rhs0, dnorm, st, eb.on ? eb.m.kap : nullptr);
+    resid64(phi, rhs0, res, dnorm + 1, st);
     GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     GBP_CUDA(cudaStreamSynchronize(st));
     const double bnorm = bits_to_double(hnorm[0]);
@@ -376,6 +646,7 @@ int MacSolver::solve(bool have_guess, gbp_stats* stats)
     while (rn > target) {
         if (it >= opt.maxiter) {
             status = GBP_NOT_CONVERGED;
+            set_error("solve: maxiter reached before the tolerance");
             break;
         }
         int rc = run_iteration();
@@ -390,7 +661,10 @@ int MacSolver::solve(bool have_guess, gbp_stats* stats)
             break;
         }
     }
-    if (singular) mac_remove_mean(l0.g, phi, partials, 1, st);
+    if (singular)
+        mac_remove_mean(l0.g, phi, partials, 1, st, eb.on ? eb.m.kap : nullptr, eb.kap_sum);
+    else if (eb.on)
+        eb_zero_covered(l0.g, eb.m.kap, phi, st);
     GBP_CUDA(cudaEventRecord(ev2, st));
     GBP_CUDA(cudaGetLastError());
     if (stats) {
@@ -421,14 +695,19 @@ int MacSolver::project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_
     }
     const MacLevel& l0 = L[0];
     GBP_CUDA(cudaEventRecord(ev0, st));
-    mac_rhs(l0.g, *u[0], *u[1], *u[2], rhs0, st);
-    if (singular) mac_remove_mean(l0.g, rhs0, partials, 0, st);
+    mac_rhs(l0.g, *u[0], *u[1], *u[2], rhs0, st, eb.on ? &eb.m : nullptr);
+    if (singular) mac_remove_mean(l0.g, rhs0, partials, 0, st, eb.on ? eb.m.kap : nullptr, eb.kap_sum);
     const bool guess = phi_guess && phi_io && phi_io->data;
     if (guess) mac_load_phi(l0.g, *phi_io, phi, st);
     GBP_CUDA(cudaGetLastError());
     int status = solve(guess, stats);
     if (status != GBP_OK && status != GBP_NOT_CONVERGED) return status;
-    for (int d = 0; d < 3; ++d) mac_correct(l0.g, d, *u[d], l0.b64[d], phi, st);
+    for (int d = 0; d < 3; ++d) mac_correct(l0.g, d, *u[d], l0.b64[d], phi, st, eb.on ? eb.m.ap[d] : nullptr);
+    if (eb.on) {
+        const double* b[3] = {l0.b64[0], l0.b64[1], l0.b64[2]};
+        const double* a[3] = {eb.m.ap[0], eb.m.ap[1], eb.m.ap[2]};
+        eb_correct_u(l0.g, eb.faces, eb.nfaces, b, a, phi, u, st);
+    }
     if (phi_io && phi_io->data) mac_store_phi(l0.g, *phi_io, phi, st);
     GBP_CUDA(cudaEventRecord(ev2, st));
     GBP_CUDA(cudaGetLastError());
@@ -439,12 +718,15 @@ int MacSolver::project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_
         stats->ms_total = ms;
         // kernels per V-cycle: 2 sweeps (red, black) per smoothing step, residual, restriction and
         // prolongation on every level above the bottom, one bottom solve
-        const long long per_v = (long long)(L.size() - 1) * (2LL * (opt.nu1 + opt.nu2) + 3) + 1;
+        const int cut = eb.on ? 1 : 0;
+        // with cut cells the finest level adds one cut-cell pass per smoothing step and one for its residual
+        const long long per_v =
+            (long long)(L.size() - 1) * (2LL * (opt.nu1 + opt.nu2) + 3) + 1 + cut * (opt.nu1 + opt.nu2 + 1);
         const int mixed = opt.precision == GBP_PREC_MIXED;
-        const long long per_step = (mixed ? opt.ir_inner_cycles : 1) * per_v + 2 + mixed;
+        const long long per_step = (mixed ? opt.ir_inner_cycles : 1) * per_v + 2 + mixed + 2 * cut;
         const int steps = stats->outer_iters - 1;
-        stats->kernel_launches = 1 + (singular ? 4 : 0) + (guess ? 1 : 0) + 2 + steps * per_step + 3 +
-                                 ((phi_io && phi_io->data) ? 1 : 0);
+        stats->kernel_launches = 1 + (singular ? 4 : 0) + (guess ? 1 : 0) + 2 + 2 * cut + steps * per_step + 3 +
+                                 2 * cut + ((phi_io && phi_io->data) ? 1 : 0);
     }
     return status;
 }

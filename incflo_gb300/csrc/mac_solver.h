@@ -31,12 +31,20 @@ public:
     // Robin data of the ROBIN sides (MacProjector::setLevelBC(lev, nullptr, robin_a, robin_b,
     // robin_f)): cell arrays with one ghost layer, read in the ghost cells next to the Robin faces
     int set_robin(const gbp_array4* a, const gbp_array4* b, const gbp_array4* f);
+    // cut cells of an embedded boundary (vfrac == nullptr removes them): volume fractions, area
+    // fractions and face centroids (2 components, AMReX's fcx / fcy / fcz) of the finest level. The
+    // face betas must be set again afterwards.
+    int set_eb(const gbp_array4* vfrac, const gbp_array4* const area[3], const gbp_array4* const fcent[3]);
+    bool has_eb() const { return eb.on; }
     int project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats);
     size_t device_bytes() const { return pool.bytes; }
 
 private:
     template <typename T>
     void vcycle(int l, const T* b, bool zero);
+    // r = b - A x on the finest level in FP64 (with the cut-face terms), norm = max |r| / (kap V)
+    void resid64(const double* x, const double* b, double* r, unsigned long long* norm, cudaStream_t s);
+    void eb_refresh_beta();
     void record_iteration();
     int run_iteration();
     int solve(bool have_guess, gbp_stats* stats);
@@ -60,6 +68,19 @@ private:
     bool any_dirichlet = false;  // a Dirichlet side exists (the system is nonsingular)
     bool robin_ready = false;
     unsigned* dflags = nullptr;
+    struct EbState {
+        DevicePool pool;
+        MacEB m{};
+        EbFace* faces = nullptr;
+        EbCell* cells = nullptr;
+        int nfaces = 0, ncells = 0;
+        double* cb64 = nullptr;
+        float* cb32 = nullptr;
+        double* beff64 = nullptr;  // finest-level right-hand side with the lagged cut-face terms
+        float* beff32 = nullptr;
+        double kap_sum = 0.0;
+        bool on = false;
+    } eb;
 };
 
 }  // namespace gbp

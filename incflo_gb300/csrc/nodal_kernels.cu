@@ -256,8 +256,9 @@ __global__ void __launch_bounds__(256) k_prolong_add(NodalGeom gf, NodalGeom gc,
 
 // fine += P xc with one thread per coarse node (I, J, K): it reads the 8 coarse nodes of the cell
 // (I..I+1, J..J+1, K..K+1) once and updates the fine block (2I..2I+1, 2J..2J+1, 2K..2K+1), x pairs
-// as one vector access. Fine Dirichlet nodes lie on coarse Dirichlet faces, whose coarse values are
-// 0, so they receive 0 without a test.
+// as one vector access. Fine nodes on Dirichlet faces lie on coarse Dirichlet faces, whose coarse
+// values are 0, so they receive 0 without a test; with an overset mask every fine node is tested
+// (a masked node with an odd index interpolates unmasked coarse nodes).
 template <typename T>
 struct Vec2;
 template <>
@@ -314,18 +315,36 @@ __global__ void __launch_bounds__(256) k_prolong_block(NodalGeom gf, NodalGeom g
             const T a0 = e0, a1 = T(0.5) * (e0 + e1);  // fine x = 2I, 2I+1
             const int i = 2 * I, j = 2 * J + oy, k = 2 * K + oz;
             const long long p = pidx(gf.sy, gf.sz, i, j, k);
-            if (!seam && vx) {
+            if (!seam && vx && !gf.mask) {
                 using V = typename Vec2<T>::type;
                 V v = *reinterpret_cast<const V*>(xf + p);
                 v.x += a0;
                 v.y += a1;
                 *reinterpret_cast<V*>(xf + p) = v;
             } else {
-                store_node(xf, gf, i, j, k, xf[p] + a0);
-                if (vx) store_node(xf, gf, i + 1, j, k, xf[p + 1] + a1);
+                if (!(gf.mask && !gf.mask[p])) store_node(xf, gf, i, j, k, xf[p] + a0);
+                if (vx && !(gf.mask && !gf.mask[p + 1])) store_node(xf, gf, i + 1, j, k, xf[p + 1] + a1);
             }
         }
     }
+}
+
+__global__ void k_mask_load(NodalGeom g, gbp_iarray4 m, unsigned char* __restrict__ out, unsigned* zeros)
+{
+    int i, j, k;
+    if (!grid3_node(g, i, j, k)) return;
+    const int v = m.data[(long long)(i - m.lo[0]) + (long long)(j - m.lo[1]) * m.jstride +
+                         (long long)(k - m.lo[2]) * m.kstride];
+    store_node(out, g, i, j, k, (unsigned char)(v != 0));
+    if (!v) atomicAdd(zeros, 1u);
+}
+
+__global__ void k_mask_coarsen(NodalGeom gf, NodalGeom gc, const unsigned char* __restrict__ mf,
+                               unsigned char* __restrict__ mc)
+{
+    int I, J, K;
+    if (!grid3_node(gc, I, J, K)) return;
+    store_node(mc, gc, I, J, K, mf[pidx(gf.sy, gf.sz, 2 * I, 2 * J, 2 * K)]);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -347,7 +366,8 @@ __global__ void __launch_bounds__(1024) k_bottom_cg(NodalGeom g, const double* _
     double* q = scr + 3 * P;
     double* dg = scr + 4 * P;
     const long long N = (long long)g.nu[0] * g.nu[1] * g.nu[2];
-    const bool singular = !(g.dlo[0] || g.dhi[0] || g.dlo[1] || g.dhi[1] || g.dlo[2] || g.dhi[2]);
+    // an overset mask (set only when it holds at least one 0) pins phi like a Dirichlet face
+    const bool singular = !(g.dlo[0] || g.dhi[0] || g.dlo[1] || g.dhi[1] || g.dlo[2] || g.dhi[2]) && !g.mask;
 
     // clear the scratch (padding must hold zeros for the stencil)
     for (long long t = threadIdx.x; t < 5 * P; t += blockDim.x) scr[t] = 0.0;
@@ -999,6 +1019,17 @@ void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* ph
 void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaStream_t st)
 {
     k_nodal_load_phi<<<grid3(g), kBlock3, 0, st>>>(g, in, phi);
+}
+
+void nodal_mask_load(const NodalGeom& g, const gbp_iarray4& m, unsigned char* out, unsigned* zeros, cudaStream_t st)
+{
+    k_mask_load<<<grid3(g), kBlock3, 0, st>>>(g, m, out, zeros);
+}
+
+void nodal_mask_coarsen(const NodalGeom& gf, const NodalGeom& gc, const unsigned char* mf, unsigned char* mc,
+                        cudaStream_t st)
+{
+    k_mask_coarsen<<<grid3(gc), kBlock3, 0, st>>>(gf, gc, mf, mc);
 }
 
 }  // namespace gbp

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(QTX * QTY) k_qsweep64(NodalGeom g, const doubl
                 const long long pn = pc;
                 const double xp = x[pn + sz];
                 double v = 0.0;
-                if (!(dxy || (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]))) {
+                if (!(dxy || (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]) || (g.mask && !g.mask[pn]))) {
                     const double ssum = w.wsum[pn];
                     const double wzp = w.wz[pn];
                     double e = x[pn + 1] * w.wx[pn];

@@ -204,6 +204,7 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
     for (auto& lv : L) {
         for (int q = 0; q < 5; ++q) add(lv.g.count, 8);
         for (int q = 0; q < 5; ++q) add(lv.g.count, 4);
+        add(lv.g.count, 1);
     }
     const NodalGeom& G0 = L[0].g;
     for (int q = 0; q < 3; ++q) add(G0.count, 8);
@@ -232,7 +233,9 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
         lv.t32 = pool.take<float>(lv.g.count);
         lv.b32 = pool.take<float>(lv.g.count);
         lv.r32 = pool.take<float>(lv.g.count);
+        lv.mask8 = pool.take<unsigned char>(lv.g.count);
     }
+    singular_faces = singular;
     phi = pool.take<double>(G0.count);
     rhs0 = pool.take<double>(G0.count);
     res = pool.take<double>(G0.count);
@@ -299,9 +302,16 @@ int NodalSolver::build_bottom()
     const int N = nbottom;
     std::vector<double> A((size_t)N * N, 0.0);
     auto wrapn = [&](int i, int d) { return g.per[d] ? ((i % g.n[d]) + g.n[d]) % g.n[d] : i; };
+    std::vector<unsigned char> hm;
+    if (g.mask) {
+        hm.resize((size_t)g.count);
+        GBP_CUDA(cudaMemcpyAsync(hm.data(), g.mask, g.count, cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+    }
     auto dir = [&](int i, int j, int k) {
         return (g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) || (g.dhi[1] && j == g.n[1]) ||
-               (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+               (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]) ||
+               (g.mask && !hm[(size_t)pidx(g.sy, g.sz, i, j, k)]);
     };
     for (int k = 0; k < g.nu[2]; ++k)
         for (int j = 0; j < g.nu[1]; ++j)
@@ -648,6 +658,7 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
     while (rn > target) {
         if (it >= opt.maxiter) {
             status = GBP_NOT_CONVERGED;
+            set_error("solve: maxiter reached before the tolerance");
             break;
         }
         int rc = run_iteration(m);
@@ -706,6 +717,29 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
         fprintf(stderr, "gbp nodal: %s after %d steps, rel resid %.3e\n", status == GBP_OK ? "converged" : "stopped",
                 it, bnorm > 0 ? rn / bnorm : rn);
     return status;
+}
+
+int NodalSolver::set_mask(const gbp_iarray4* m)
+{
+    unsigned zeros = 0;
+    if (m && m->data) {
+        unsigned* dz = reinterpret_cast<unsigned*>(dscal + 7);
+        GBP_CUDA(cudaMemsetAsync(dz, 0, sizeof(unsigned), st));
+        nodal_mask_load(L[0].g, *m, L[0].mask8, dz, st);
+        L[0].g.mask = L[0].mask8;
+        for (size_t l = 1; l < L.size(); ++l) {
+            nodal_mask_coarsen(L[l - 1].g, L[l].g, L[l - 1].mask8, L[l].mask8, st);
+            L[l].g.mask = L[l].mask8;
+        }
+        GBP_CUDA(cudaMemcpyAsync(&zeros, dz, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+    }
+    if (zeros == 0)  // no masked node: the plain operator (and its null space) stays
+        for (auto& lv : L) lv.g.mask = nullptr;
+    // the level geometries (captured by value in the graphs) changed, and a masked node pins phi
+    singular = singular_faces && zeros == 0;
+    drop_graphs();
+    return sigma_ready ? build_bottom() : GBP_OK;
 }
 
 int NodalSolver::set_surrogate(nn::UNet* n, int level, int mode)

@@ -36,6 +36,7 @@ struct NodalLevel {
     NodalGeom g;
     double *s64 = nullptr, *x64 = nullptr, *t64 = nullptr, *b64 = nullptr, *r64 = nullptr;
     float *s32 = nullptr, *x32 = nullptr, *t32 = nullptr, *b32 = nullptr, *r32 = nullptr;
+    unsigned char* mask8 = nullptr;  // overset mask storage (active when g.mask is set)
 };
 
 class NodalSolver {
@@ -50,6 +51,8 @@ public:
     int set_options(const gbp_options& opt);
     int set_sigma_from_density(const gbp_array4* rho, double scale, double rho0);
     int set_sigma(const gbp_array4* sigma, double cval);
+    // overset mask (0 = phi held at 0) over nodes 0..n; nullptr removes it
+    int set_mask(const gbp_iarray4* mask);
 
     // full projection: rhs from vel (+ fused add-back / U^n subtraction), solve, correct
     int project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
@@ -113,6 +116,7 @@ private:
     unsigned long long* dnorm = nullptr;  // [0] rhs norm, [1] residual norm
     unsigned long long* hnorm = nullptr;  // pinned mirror
     bool singular = false;
+    bool singular_faces = false;  // singular from the boundary types alone (no overset mask)
     bool sigma_ready = false;
     double scale32 = 1.0;
     // result buffer of each level's V-cycle (ping-pong aware)

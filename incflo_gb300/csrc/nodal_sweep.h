@@ -41,6 +41,6 @@ int sm_count_cached();
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st);
 int sweep32_tma1_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out,
-                     float omega, unsigned* err, unsigned long long* norm, cudaStream_t st);
+                     float omega, unsigned* err, unsigned long long* norm, cudaStream_t st, bool packed);
 
 }  // namespace gbp

@@ -787,11 +787,12 @@ int sweep_variant()
     static int v = -1;
     if (v < 0) {
         const char* e = getenv("GBP_SWEEP32");
-        // 3: register-blocked 2x4 (default), 4: register-blocked 2x2, 2: packed pair,
-        // 0: scalar z-march, 1: TMA producer/consumer
+        // 5: k_sweep32t (default), 6: k_sweep32p (packed FP32x2), 3: register-blocked 2x4,
+        // 4: register-blocked 2x2, 2: packed pair, 0: scalar z-march, 1: TMA producer/consumer
         v = 5;
         if (e) {
-            if (e[0] == 'b') v = 3;
+            if (e[0] == 'q') v = 6;  // k_sweep32p, packed FP32x2 (measured 7 % slower)
+            else if (e[0] == 'b') v = 3;
             else if (e[0] == 't') v = 1;
             else if (e[0] == 's') v = 0;
             else if (e[0] == 'p') v = 2;
@@ -806,7 +807,7 @@ int sweep_variant()
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
-    if (sweep_variant() == 5) return sweep32_tma1_run(g, mode, s, x, b, out, omega, err, norm, st);
+    if (sweep_variant() >= 5) return sweep32_tma1_run(g, mode, s, x, b, out, omega, err, norm, st, sweep_variant() == 6);
     if (sweep_variant() == 3)
         return mode == 0 ? launch_zblock<0, 4>(g, s, x, b, out, omega, norm, st)
                          : launch_zblock<1, 4>(g, s, x, b, out, omega, norm, st);

@@ -1,0 +1,173 @@
+"""Cut-cell geometry of an embedded boundary from an implicit surface (the role of AMReX's EB2::Build
+for incflo's cylinder, src/embedded_boundaries/eb_cylinder.cpp:15-64, which is not available here).
+
+For a cylinder along one axis the fluid is outside the circle (EB2::CylinderIF with fluid outside):
+  - a face normal to a direction in the circle's plane is a rectangle crossed by the cylinder along
+    a chord; its aperture is the fraction of the face outside [c - s, c + s], s = sqrt(r^2 - d^2);
+  - a face normal to the axis, and a cell's volume fraction, are the fraction of a rectangle outside
+    the circle. The covered part is integrated exactly: between the break points (the circle's extreme
+    points and where it crosses the rectangle's sides) its height is a + b s(u), u = x - cx, and the
+    integrals of 1, u, s, u s and s^2 have closed forms.
+Arrays follow incflo_gb300.projection: cells (nz, ny, nx), x faces (nz, ny, nx+1), ... (last axis x).
+Face centroids follow AMReX's fcx / fcy / fcz: the offset of the open part's centroid from the face
+centre in units of the cell size, in [-0.5, 0.5], for the two tangential directions in increasing
+order (x faces: (y, z); y faces: (x, z); z faces: (x, y)); last axis of size 2.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _outside_fraction_1d(a, b, c, s):
+    """Fraction of the interval [a, b] outside [c - s, c + s] (s <= 0: no overlap)."""
+    lo = np.maximum(a, c - np.maximum(s, 0.0))
+    hi = np.minimum(b, c + np.maximum(s, 0.0))
+    covered = np.clip(hi - lo, 0.0, None)
+    covered = np.where(s > 0.0, covered, 0.0)
+    return 1.0 - covered / (b - a)
+
+
+def _outside_moment_1d(a, b, c, s):
+    """First moment of the part of [a, b] outside [c - s, c + s] (s <= 0: no overlap)."""
+    lo = np.maximum(a, c - np.maximum(s, 0.0))
+    hi = np.minimum(b, c + np.maximum(s, 0.0))
+    cov = np.where((s > 0.0) & (hi > lo), 0.5 * (hi * hi - lo * lo), 0.0)
+    return 0.5 * (b * b - a * a) - cov
+
+
+def _rect_disk(x0, x1, y0, y1, cx, cy, r):
+    """Area and first moments (int x, int y) of the rectangle's part inside the circle, exactly."""
+    ua, ub = max(x0 - cx, -r), min(x1 - cx, r)
+    if ub <= ua:
+        return 0.0, 0.0, 0.0
+    r2 = r * r
+
+    def s(u):
+        return math.sqrt(max(r2 - u * u, 0.0))
+
+    def i_s(u):  # int s du
+        return 0.5 * (u * s(u) + r2 * math.asin(max(-1.0, min(1.0, u / r))))
+
+    def i_s2(u):  # int s^2 du
+        return r2 * u - u ** 3 / 3.0
+
+    def i_us(u):  # int u s du
+        return -s(u) ** 3 / 3.0
+
+    cuts = [ua, ub]
+    for yb in (y0, y1):
+        d = yb - cy
+        if abs(d) < r:
+            w = math.sqrt(r2 - d * d)
+            cuts += [w, -w]
+    cuts = sorted(c for c in cuts if ua <= c <= ub)
+    area = mx = my = 0.0
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        if b <= a:
+            continue
+        sm = s(0.5 * (a + b))
+        if min(y1, cy + sm) <= max(y0, cy - sm):
+            continue
+        # upper bound y1 or the circle (cy + s), lower bound y0 or the circle (cy - s)
+        h0, h1 = (cy, 1.0) if cy + sm < y1 else (y1, 0.0)
+        l0, l1 = (cy, -1.0) if cy - sm > y0 else (y0, 0.0)
+        du = b - a
+        ds = i_s(b) - i_s(a)
+        area_p = (h0 - l0) * du + (h1 - l1) * ds
+        area += area_p
+        mx += cx * area_p + (h0 - l0) * 0.5 * (b * b - a * a) + (h1 - l1) * (i_us(b) - i_us(a))
+        my += 0.5 * ((h0 * h0 - l0 * l0) * du + 2.0 * (h0 * h1 - l0 * l1) * ds
+                     + (h1 * h1 - l1 * l1) * (i_s2(b) - i_s2(a)))
+    return area, mx, my
+
+
+def _outside_rect(x0, x1, y0, y1, cx, cy, r):
+    """Fraction of the rectangle outside the circle and the centroid (x, y) of that part."""
+    full = (x1 - x0) * (y1 - y0)
+    ca, cmx, cmy = _rect_disk(x0, x1, y0, y1, cx, cy, r)
+    area = full - ca
+    if area <= 1e-15 * full:
+        return 0.0, 0.5 * (x0 + x1), 0.5 * (y0 + y1)
+    mx = 0.5 * (x1 * x1 - x0 * x0) * (y1 - y0) - cmx
+    my = 0.5 * (y1 * y1 - y0 * y0) * (x1 - x0) - cmy
+    return min(1.0, area / full), mx / area, my / area
+
+
+def cylinder(n, lo, hi, center, radius, axis=2):
+    """Volume fractions, face apertures and face centroids of the region outside a cylinder along
+    `axis`. Returns dict(vfrac, apx, apy, apz, fcx, fcy, fcz) as float64 arrays."""
+    n = tuple(int(v) for v in n)
+    h = [(hi[d] - lo[d]) / n[d] for d in range(3)]
+    edges = [lo[d] + h[d] * np.arange(n[d] + 1) for d in range(3)]
+    p, q = [d for d in range(3) if d != axis]  # the circle's plane, p < q
+    cp, cq = center[p], center[q]
+    shape_cells = (n[2], n[1], n[0])
+
+    def grid(d, faces):
+        """coordinates along d broadcast to the (z, y, x) array of cells or d-faces"""
+        e = edges[d]
+        v = e if faces else 0.5 * (e[:-1] + e[1:])
+        sh = [1, 1, 1]
+        sh[2 - d] = v.size
+        return v.reshape(sh)
+
+    def lohi(d):
+        e = edges[d]
+        sh = [1, 1, 1]
+        sh[2 - d] = n[d]
+        return e[:-1].reshape(sh), e[1:].reshape(sh)
+
+    # cells (and axis-normal faces): rectangles of the (p, q) cross-section, indexed [q, p]
+    frac = np.ones((n[q], n[p]))
+    offp = np.zeros((n[q], n[p]))
+    offq = np.zeros((n[q], n[p]))
+    ep, eq = edges[p], edges[q]
+    for b in range(n[q]):
+        if abs(0.5 * (eq[b] + eq[b + 1]) - cq) > radius + h[q]:
+            continue
+        for a in range(n[p]):
+            if abs(0.5 * (ep[a] + ep[a + 1]) - cp) > radius + h[p]:
+                continue
+            f, xc, yc = _outside_rect(ep[a], ep[a + 1], eq[b], eq[b + 1], cp, cq, radius)
+            frac[b, a] = f
+            if 0.0 < f < 1.0:
+                offp[b, a] = (xc - 0.5 * (ep[a] + ep[a + 1])) / h[p]
+                offq[b, a] = (yc - 0.5 * (eq[b] + eq[b + 1])) / h[q]
+
+    def to_cells(a2, extra_axis=None):
+        """[q, p] cross-section -> (z, y, x) array (the axis direction extended by one if asked);
+        array axes run z, y, x, so q (the larger direction) comes first as in a2"""
+        sh = [1, 1, 1]
+        sh[2 - q] = n[q]
+        sh[2 - p] = n[p]
+        fs = list(shape_cells)
+        if extra_axis is not None:
+            fs[2 - extra_axis] += 1
+        return np.broadcast_to(a2.reshape(sh), tuple(fs)).copy()
+
+    vfrac = to_cells(frac)
+    ap = [None, None, None]
+    fc = [None, None, None]
+    ap[axis] = to_cells(frac, axis)
+    off = {p: to_cells(offp, axis), q: to_cells(offq, axis)}
+    fc[axis] = np.stack([off[t] for t in range(3) if t != axis], axis=-1)
+    # faces normal to p (and q): chord at the face position, fraction of the other extent
+    for d, o in ((p, q), (q, p)):
+        xd = grid(d, True)
+        cd = center[d]
+        s = np.where((xd - cd) ** 2 < radius * radius, np.sqrt(np.clip(radius ** 2 - (xd - cd) ** 2, 0, None)), -1.0)
+        o0, o1 = lohi(o)
+        f = _outside_fraction_1d(o0, o1, center[o], s)
+        length = (o1 - o0) * f
+        mom = _outside_moment_1d(o0, o1, center[o], s)
+        cen = np.where(length > 0.0, mom / np.where(length > 0.0, length, 1.0), 0.5 * (o0 + o1))
+        fs = list(shape_cells)
+        fs[2 - d] += 1
+        ap[d] = np.broadcast_to(f, tuple(fs)).copy()
+        cut = (ap[d] > 0.0) & (ap[d] < 1.0)
+        offo = np.where(cut, np.broadcast_to((cen - 0.5 * (o0 + o1)) / h[o], tuple(fs)), 0.0)
+        comps = [offo if t == o else np.zeros(tuple(fs)) for t in range(3) if t != d]
+        fc[d] = np.stack(comps, axis=-1)
+    return dict(vfrac=vfrac, apx=ap[0], apy=ap[1], apz=ap[2], fcx=fc[0], fcy=fc[1], fcz=fc[2])

@@ -170,10 +170,16 @@ class NodalProjector:
         self.stats = None
         self.surrogate = None
         self.surrogate_level = 1
+        self.mask = None
 
     def setDomainBC(self, lo, hi):  # noqa: N802 (reference name)
         self.bc_lo = tuple(LinOpBCType.get(b, b) for b in lo)
         self.bc_hi = tuple(LinOpBCType.get(b, b) for b in hi)
+
+    def setOversetMask(self, mask):  # noqa: N802 (getLinOp().setOversetMask(lev, mask))
+        """Nodal int32 tensor (nz+1, ny+1, nx+1): 0 = phi held at 0 (the Dirichlet part of a mixed
+        boundary, incflo::make_nodalBC_mask), nonzero = solve. None removes it."""
+        self.mask = mask
 
     def setSurrogate(self, surrogate, level: int = 1):  # noqa: N802 (no reference counterpart)
         """Learned warm start for zero-guess solves (incflo_gb300.surrogate.Surrogate), evaluated on
@@ -205,7 +211,21 @@ class NodalProjector:
             A.check(L.gbp_nodal_set_sigma(plan.ptr, _ref(array4(self.sigma)), 0.0), "gbp_nodal_set_sigma")
         else:
             A.check(L.gbp_nodal_set_sigma(plan.ptr, None, float(self.sigma)), "gbp_nodal_set_sigma")
-        # plans are shared between projectors of one geometry: (re)state the warm start every call
+        # plans are shared between projectors of one geometry: (re)state the mask (when it changed)
+        # and the warm start every call
+        m = self.mask
+        if getattr(plan, "mask_ref", None) is not m:
+            if m is not None:
+                if m.dtype != torch.int32 or not m.is_cuda or m.stride(-1) != 1:
+                    raise TypeError("the overset mask is a CUDA int32 tensor, x contiguous")
+                ia = A.IArray4()
+                ia.data = m.data_ptr()
+                ia.hi[0], ia.hi[1], ia.hi[2] = m.shape[2] - 1, m.shape[1] - 1, m.shape[0] - 1
+                ia.jstride, ia.kstride = m.stride(1), m.stride(0)
+                A.check(L.gbp_nodal_set_overset_mask(plan.ptr, ctypes.byref(ia)), "gbp_nodal_set_overset_mask")
+            else:
+                A.check(L.gbp_nodal_set_overset_mask(plan.ptr, None), "gbp_nodal_set_overset_mask")
+            plan.mask_ref = m
         s = self.surrogate
         A.check(L.gbp_plan_set_surrogate(plan.ptr, s.ptr if s is not None else None, self.surrogate_level,
                                          int(s is not None)), "gbp_plan_set_surrogate")
@@ -347,6 +367,7 @@ class MacProjector:
         self.umac = None
         self.stats = None
         self.robin = None
+        self.eb = None
 
     def needInitialization(self):  # noqa: N802
         return self.plan is None
@@ -378,6 +399,29 @@ class MacProjector:
         A.check(A.load().gbp_mac_set_robin(self.plan.ptr, _ref(array4(a, 1)), _ref(array4(b, 1)),
                                            _ref(array4(f, 1)) if f is not None else None), "gbp_mac_set_robin")
 
+    def setEB(self, vfrac, areafrac, facecent):  # noqa: N802
+        """Cut cells of an embedded boundary (what the reference takes from the EB factory of its
+        MultiFabs): vfrac (nz, ny, nx); areafrac = [x (nz, ny, nx+1), y, z] face tensors; facecent =
+        [x (2, nz, ny, nx+1), y, z]: centroid offsets in cell widths along the two tangential
+        directions in increasing order (AMReX's fcx / fcy / fcz). vfrac None removes the EB."""
+        self.eb = None if vfrac is None else (vfrac, list(areafrac), list(facecent))
+        self._push_eb()
+        self._push_beta()
+        self._push_robin()
+
+    def _push_eb(self):
+        if self.plan is None:
+            return
+        L = A.load()
+        if self.eb is None:
+            A.check(L.gbp_mac_set_eb(self.plan.ptr, None, None, None, None, None, None, None), "gbp_mac_set_eb")
+            return
+        v, ap, fc = self.eb
+        a = [array4(x) for x in ap]
+        f = [array4(x) for x in fc]
+        A.check(L.gbp_mac_set_eb(self.plan.ptr, _ref(array4(v)), _ref(a[0]), _ref(a[1]), _ref(a[2]), _ref(f[0]),
+                                 _ref(f[1]), _ref(f[2])), "gbp_mac_set_eb")
+
     def updateCoeffs(self, beta):  # noqa: N802
         self.beta = beta
         self._push_beta()
@@ -405,6 +449,7 @@ class MacProjector:
             if self.bc_lo is None:
                 raise RuntimeError("setDomainBC must be called before project")
             self.plan = _Plan(self.geom, A.GBP_MAC, self.bc_lo, self.bc_hi, self.options, self.stream)
+            self._push_eb()
             self._push_beta()
             self._push_robin()
         else:

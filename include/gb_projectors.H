@@ -127,6 +127,12 @@ public:
         phi_ = phi;
         gradphi_ = gradphi;
     }
+    // getLinOp().setOversetMask(lev, mask): 0 = phi held at 0 (incflo::make_nodalBC_mask)
+    void setOversetMask(gbp_iarray4 mask)
+    {
+        if (!plan_) throw Error(GBP_BAD_ARG, "NodalProjector::setOversetMask before setDomainBC");
+        check(gbp_nodal_set_overset_mask(plan_.get(), &mask), "gbp_nodal_set_overset_mask");
+    }
 
     gbp_stats project(double rtol, double atol)
     {
@@ -205,6 +211,23 @@ public:
     void setUMAC(const gbp_array4 umac[3])
     {
         for (int d = 0; d < 3; ++d) umac_[d] = umac[d];
+    }
+    // setLevelBC(lev, nullptr, robin_a, robin_b, robin_f) for the Robin sides (f = 0)
+    void setLevelBC(int lev, const gbp_array4* levelbcdata, const gbp_array4* robin_a, const gbp_array4* robin_b,
+                    const gbp_array4* robin_f)
+    {
+        if (lev != 0 || levelbcdata) throw Error(GBP_BAD_ARG, "MacProjector::setLevelBC: single level, zero Dirichlet");
+        if (!plan_) throw Error(GBP_BAD_ARG, "MacProjector::setLevelBC before setDomainBC");
+        check(gbp_mac_set_robin(plan_.get(), robin_a, robin_b, robin_f), "gbp_mac_set_robin");
+    }
+    // the EB factory's volume fractions, area fractions and face centroids (what the reference's
+    // MacProjector reads from the factory of its MultiFabs); beta is pushed again afterwards
+    void setEB(const gbp_array4& vfrac, const gbp_array4 area[3], const gbp_array4 fcent[3])
+    {
+        if (!plan_) throw Error(GBP_BAD_ARG, "MacProjector::setEB before setDomainBC");
+        check(gbp_mac_set_eb(plan_.get(), &vfrac, &area[0], &area[1], &area[2], &fcent[0], &fcent[1], &fcent[2]),
+              "gbp_mac_set_eb");
+        push_beta();
     }
     gbp_stats project(double rtol, double atol) { return run(nullptr, rtol, atol); }
     gbp_stats project(gbp_array4 phi, double rtol, double atol) { return run(&phi, rtol, atol); }

@@ -71,6 +71,15 @@ typedef struct {
     long long nstride;
 } gbp_array4;
 
+/* Integer mirror of amrex::Array4<int> (one component): the overset mask. */
+typedef struct {
+    const int* data;
+    int lo[3];
+    int hi[3];
+    long long jstride;
+    long long kstride;
+} gbp_iarray4;
+
 typedef struct {
     int n_cell[3];       /* cells of the (single-box) level */
     double prob_lo[3];
@@ -163,6 +172,12 @@ int gbp_nodal_set_sigma(gbp_plan* plan, const gbp_array4* sigma, double const_si
 int gbp_nodal_project(gbp_plan* plan, gbp_array4* vel, gbp_array4* phi, gbp_array4* gradphi,
                       int phi_guess, gbp_stats* stats);
 
+/* getLinOp().setOversetMask(lev, mask) (incflo_apply_nodal_projection.cpp:203-210, mask from
+ * incflo::make_nodalBC_mask, src/boundary_conditions/incflo_set_bcs.cpp:10-53): nodal integer
+ * mask over nodes 0..n, 0 = phi is held at 0 there (the Dirichlet part of a mixed boundary), nonzero
+ * = solve. Coarse levels take the mask by injection. NULL (or data == NULL) removes the mask. */
+int gbp_nodal_set_overset_mask(gbp_plan* plan, const gbp_iarray4* mask);
+
 /* The nodal divergence of vel as the projection sees it: the right-hand side of the nodal solve
  * (div_i = weak divergence / control volume, inflow normal velocity from the ghost cells when
  * use_inflow != 0, 0 on Dirichlet nodes), made consistent for singular boundary sets. div_out
@@ -242,6 +257,22 @@ int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_lau
  * MAC Robin data, prob_set_MAC_robinBCs, always has f = 0); robin_f may be NULL. */
 int gbp_mac_set_robin(gbp_plan* plan, const gbp_array4* robin_a, const gbp_array4* robin_b,
                       const gbp_array4* robin_f);
+
+/* Embedded-boundary cut cells of a MAC plan: what the reference's MacProjector takes from the
+ * EBFArrayBoxFactory of its beta MultiFabs (incflo's EB factory, src/incflo.H:743-752; the projector
+ * is built with MLMG::Location::FaceCentroid for umac and beta, src/incflo.cpp:286-292, and
+ * MLEBABecLap, src/convection/incflo_compute_MAC_projected_velocities.cpp:82-90). vfrac: volume
+ * fractions (cells); area_x/y/z: area fractions (faces 0..n of each direction); fcent_x/y/z: face
+ * centroids, 2 components = offsets of the open part's centroid from the face centre in cell widths
+ * ([-0.5, 0.5]) along the two tangential directions in increasing order (AMReX's fcx / fcy / fcz).
+ * The operator becomes the cut-cell one: flux = area fraction x beta x the normal derivative at the
+ * face centroid (bilinear blend of neighbouring face-centre differences), no flux through the EB,
+ * RHS = area-weighted divergence of the face-centroid velocities, stopping norm max |r| / vfrac,
+ * singular systems made consistent and gauged with vfrac weights, covered cells phi = 0. Beta must
+ * be set again after this call. vfrac == NULL removes the EB. */
+int gbp_mac_set_eb(gbp_plan* plan, const gbp_array4* vfrac, const gbp_array4* area_x, const gbp_array4* area_y,
+                   const gbp_array4* area_z, const gbp_array4* fcent_x, const gbp_array4* fcent_y,
+                   const gbp_array4* fcent_z);
 
 /* incflo::ApplyCCProjection(density, umac, time, scaling_factor, incremental) for one level,
  * non-EB (src/projection/incflo_apply_cc_projection.cpp:199-487; option incflo.use_cc_proj):

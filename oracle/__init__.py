@@ -35,6 +35,7 @@ class _Grid(ctypes.Structure):
         ("h", ctypes.c_double * 3),
         ("bclo", ctypes.c_int * 3),
         ("bchi", ctypes.c_int * 3),
+        ("mask", ctypes.c_void_p),
     ]
 
 
@@ -82,7 +83,7 @@ def _p(a: np.ndarray):
 class Grid:
     """Single-box domain: n cells, extent [lo, hi], boundary codes per side."""
 
-    def __init__(self, n, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), bclo=(0, 0, 0), bchi=None):
+    def __init__(self, n, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), bclo=(0, 0, 0), bchi=None, mask=None):
         self.n = tuple(int(v) for v in n)
         self.lo = tuple(float(v) for v in lo)
         self.hi = tuple(float(v) for v in hi)
@@ -92,8 +93,13 @@ class Grid:
         for d in range(3):
             if (self.bclo[d] == PERIODIC) != (self.bchi[d] == PERIODIC):
                 raise ValueError("periodic must be set on both sides")
+        # overset mask (nodal): unique nodes (node_shape), 0 = phi fixed at 0 (incflo's mixed BCs)
+        self.mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        if self.mask is not None and self.mask.shape != self.node_shape:
+            raise ValueError("mask must have the unique-node shape")
         self._c = _Grid((ctypes.c_int * 3)(*self.n), (ctypes.c_double * 3)(*self.h),
-                        (ctypes.c_int * 3)(*self.bclo), (ctypes.c_int * 3)(*self.bchi))
+                        (ctypes.c_int * 3)(*self.bclo), (ctypes.c_int * 3)(*self.bchi),
+                        self.mask.ctypes.data if self.mask is not None else None)
 
     def periodic(self, d):
         return self.bclo[d] == PERIODIC

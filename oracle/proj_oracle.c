@@ -288,6 +288,13 @@ static void q1_element(const double h[3], double K[8])
 static int node_fixed(const or_grid* g, int i, int j, int k)
 {
     int idx[3] = {i, j, k};
+    if (g->mask) {
+        /* incflo's mixed boundaries: the solver's overset mask marks nodes whose phi is known (0),
+           src/boundary_conditions/incflo_set_bcs.cpp:10-53 */
+        int nn[3];
+        or_nodal_dims(g, nn);
+        if (!g->mask[i + (long)nn[0] * (j + (long)nn[1] * k)]) return 1;
+    }
     for (int d = 0; d < 3; ++d) {
         if (is_per(g, d)) continue;
         if (idx[d] == 0 && g->bclo[d] == OR_DIRICHLET) return 1;
@@ -596,6 +603,7 @@ typedef struct {
     double* b[MAXLEV];
     double* r[MAXLEV];
     int nu;
+    unsigned char* owned_mask[MAXLEV]; /* coarse overset masks built by injection */
 } mg_t;
 
 static int can_coarsen(const or_grid* g)
@@ -641,6 +649,20 @@ static void mg_build_nodal(mg_t* mg, const or_grid* g, const double* sigma)
         or_grid* f = &mg->grid[l];
         or_grid* c = &mg->grid[l + 1];
         coarse_grid(f, c);
+        if (f->mask) {
+            /* coarse mask by injection: coarse node I is fixed iff fine node 2I is */
+            int fn[3], cn[3];
+            or_nodal_dims(f, fn);
+            or_nodal_dims(c, cn);
+            unsigned char* cm = (unsigned char*)malloc((size_t)cn[0] * cn[1] * cn[2]);
+            for (int k = 0; k < cn[2]; ++k)
+                for (int j = 0; j < cn[1]; ++j)
+                    for (int i = 0; i < cn[0]; ++i)
+                        cm[i + (long)cn[0] * (j + (long)cn[1] * k)] =
+                            f->mask[2 * i + (long)fn[0] * (2 * j + (long)fn[1] * 2 * k)];
+            c->mask = cm;
+            mg->owned_mask[l + 1] = cm;
+        }
         double* cs = (double*)malloc(sizeof(double) * (size_t)c->n[0] * c->n[1] * c->n[2]);
         for (int k = 0; k < c->n[2]; ++k)
             for (int j = 0; j < c->n[1]; ++j)
@@ -726,6 +748,10 @@ static void mg_free(mg_t* mg)
         free(mg->x[l]);
         free(mg->b[l]);
         free(mg->r[l]);
+    }
+    for (int l = 0; l < MAXLEV; ++l) {
+        free(mg->owned_mask[l]);
+        mg->owned_mask[l] = NULL;
     }
     mg->nlev = 0;
 }

@@ -39,6 +39,7 @@ typedef struct {
     double h[3];     /* cell size */
     int bclo[3];     /* OR_* per direction, low side */
     int bchi[3];     /* OR_* per direction, high side */
+    const unsigned char* mask; /* nodal: unique-node overset mask, 0 = phi fixed at 0 (NULL: none) */
 } or_grid;
 
 /* ---- nodal ---------------------------------------------------------------------------

@@ -115,3 +115,27 @@ def test_mac_robin_rejects_bad_data(gpu_lib):
     with pytest.raises(Exception):
         mp.setLevelBC(0, None, z, z, None)  # a = b = 0: no boundary condition
         mp._ensure()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mac_all_neumann_inconsistent_rhs(gpu_lib, precision):
+    """Walls all round with non-zero wall-normal velocities: the divergence has a non-zero sum, the
+    singular system is made consistent by removing its mean (as the oracle does) before the solve."""
+    n, ext, bc = (16, 12, 8), (2.0, 1.5, 1.0), (N, N, N)
+    g = O.Grid(n, hi=ext, bclo=bc, bchi=bc)
+    rng = np.random.default_rng(11)
+    beta = [np.abs(b) + 0.2 for b in face_fields(g, rng, zero_neumann=False)]
+    umac = face_fields(g, rng, zero_neumann=False)
+    un_or, phi_or, st_or = O.mac_project(g, beta, umac, rtol=1e-13)
+    assert st_or["status"] == 0
+    mp = MacProjector(Geometry(n, (0, 0, 0), ext), options=make_options(1, precision=precision))
+    mp.initProjector(beta=[cuda(b) for b in beta])
+    mp.setDomainBC(bc, bc)
+    ut = [cuda(u) for u in umac]
+    mp.setUMAC(ut)
+    phi = cuda(np.zeros(g.cell_shape))
+    st = mp.project(rtol=1e-12, atol=0.0, phi=phi, phi_guess=False)
+    assert st["status"] == 0
+    assert rel_l2(phi.cpu().numpy(), phi_or) <= 1e-9
+    for d in range(3):
+        np.testing.assert_allclose(ut[d].cpu().numpy(), un_or[d], rtol=0, atol=1e-9 * np.abs(un_or[d]).max())

@@ -182,3 +182,35 @@ def test_nan_rhs_reported(gpu_lib):
         proj.project()
     assert e.value.status == 2
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_overset_mask_matches_oracle(gpu_lib, precision):
+    """incflo's mixed boundaries on the nodal side: an overset mask (0 = phi held at 0) over part of
+    the high-x face and a patch of the low-z face of an otherwise all-Neumann box (which the mask
+    makes nonsingular), against the oracle with the same mask."""
+    n, ext, bclo, bchi = (16, 12, 10), (1.0, 0.75, 0.625), (N, N, N), (I, N, N)
+    g0, sigma, vel = nodal_case(n, ext, bclo, bchi, seed=4)
+    nn = g0.node_shape
+    mask = np.ones(nn, np.int32)
+    mask[:, : nn[1] // 2, -1] = 0          # outflow part of the high-x face
+    mask[0, 2:6, 3:9] = 0                  # a patch on the low-z face
+    g = O.Grid(n, hi=ext, bclo=bclo, bchi=bchi, mask=mask.astype(np.uint8))
+    vel_or, phi_or, grad_or, st_or = O.nodal_project(g, sigma, vel, rtol=1e-13)
+    assert st_or["status"] == 0
+    vt = cuda(vel)
+    proj = NodalProjector(vt, cuda(sigma), Geometry(n, (0, 0, 0), ext),
+                          options=make_options(0, precision=precision))
+    proj.setDomainBC(bclo, bchi)
+    full = np.ones((n[2] + 1, n[1] + 1, n[0] + 1), np.int32)
+    full[: nn[0], : nn[1], : nn[2]] = mask
+    proj.setOversetMask(torch.from_numpy(full).cuda())
+    st = proj.project(rtol=1e-12, atol=0.0)
+    assert st["status"] == 0 and st["final_rel_resid"] <= 1e-12
+    phi = unique_nodes(g, proj.getPhi().cpu().numpy())
+    assert np.abs(phi[mask == 0]).max() == 0.0
+    assert rel_l2(phi, phi_or) <= 1e-9
+    inner = (slice(None), slice(1, -1), slice(1, -1), slice(1, -1))
+    got = vt.cpu().numpy()
+    np.testing.assert_allclose(got[inner], vel_or[inner], rtol=0, atol=1e-9 * np.abs(vel_or[inner]).max())
+    proj.setOversetMask(None)  # the shared plan goes back to the unmasked operator
