@@ -25,7 +25,9 @@ EXPORTS = (
     "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
     "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel",
     "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc", "gbp_nodal_set_overset_mask",
-    "gbp_mac_set_robin", "gbp_mac_set_eb", "gbp_average_down", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
+    "gbp_mac_set_robin", "gbp_mac_set_eb", "gbp_average_down",
+    "gbp_amr_create", "gbp_amr_destroy", "gbp_amr_set_options", "gbp_amr_device_bytes",
+    "gbp_amr_apply_nodal_projection", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
     "gbp_nn_conv3d", "gbp_nn_conv3d_wgrad",
     "gbp_surrogate_create", "gbp_surrogate_destroy", "gbp_surrogate_num_params", "gbp_surrogate_get_params",
     "gbp_surrogate_set_params", "gbp_surrogate_get_grads", "gbp_surrogate_save", "gbp_surrogate_load",
@@ -150,6 +152,14 @@ def load(path: str = LIB_PATH):
                                              ctypes.POINTER(ctypes.c_double), P]),
         "gbp_mac_set_robin": (i, [P, A4, A4, A4]),
         "gbp_mac_set_eb": (i, [P, A4, A4, A4, A4, A4, A4, A4]),
+        "gbp_amr_create": (i, [ctypes.POINTER(Geometry), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                               ctypes.POINTER(ctypes.c_int), i, ctypes.POINTER(Options), P, ctypes.POINTER(P)]),
+        "gbp_amr_destroy": (i, [P]),
+        "gbp_amr_set_options": (i, [P, ctypes.POINTER(Options)]),
+        "gbp_amr_device_bytes": (ctypes.c_size_t, [P]),
+        "gbp_amr_apply_nodal_projection": (i, [P, A4, A4, A4, A4, A4, ctypes.POINTER(A4), ctypes.POINTER(A4),
+                                               ctypes.POINTER(A4), ctypes.POINTER(A4), ctypes.POINTER(A4), d, d, i,
+                                               ctypes.POINTER(Stats)]),
         "gbp_nodal_set_overset_mask": (i, [P, ctypes.POINTER(IArray4)]),
         "gbp_average_down": (i, [A4, A4, ctypes.POINTER(ctypes.c_int), i, ctypes.POINTER(ctypes.c_int),
                                  ctypes.POINTER(ctypes.c_int), P]),

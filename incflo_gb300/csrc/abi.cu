@@ -13,6 +13,7 @@
 #include "mac_solver.h"
 #include "nodal_solver.h"
 #include "plan.h"
+#include "amr.h"
 #include "cc_projection.h"
 #include "solvability.h"
 
@@ -268,6 +269,13 @@ int gbp_plan_destroy(gbp_plan* p)
     delete p->nodal;
     delete p->mac;
     if (p->hbuf) cudaFree(p->hbuf);
+    if (p->copy_stream) {
+        cudaStreamSynchronize(p->copy_stream);
+        cudaStreamDestroy(p->copy_stream);
+    }
+    if (p->ev_in) cudaEventDestroy(p->ev_in);
+    if (p->ev_phi) cudaEventDestroy(p->ev_phi);
+    if (p->ev_out) cudaEventDestroy(p->ev_out);
     if (p->dflux) cudaFree(p->dflux);
     if (p->ccbuf) cudaFree(p->ccbuf);
     delete p;
@@ -434,9 +442,25 @@ int gbp_nodal_divergence(gbp_plan* p, const gbp_array4* vel, int use_inflow, gbp
     return p->nodal->divergence(ra, div_out, max_norm);
 }
 
+static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
+                            double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
+                            double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats,
+                            cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy);
+
 int gbp_apply_nodal_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
                                double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
                                double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats)
+{
+    return apply_nodal_impl(p, vel, vel_old, rho, rho0, gp, p_nd, time, dt, prev_dt, scaling_factor, incremental,
+                            set_inflow_bc, stats, nullptr, nullptr);
+}
+
+// wait_before_rhs: an event the plan's stream waits on after sigma is set and before the right-hand
+// side (the host path uploads the velocities meanwhile); phi_copy: a copy issued once p_nd is stored
+static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
+                            double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
+                            double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats,
+                            cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy)
 {
     if (!p || !p->nodal) {
         set_error("gbp_apply_nodal_projection: not a nodal plan");
@@ -472,7 +496,8 @@ int gbp_apply_nodal_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* v
     ca.add_gp = !incremental;
     ca.incremental = incremental;
     if (stats) memset(stats, 0, sizeof(*stats));
-    return p->nodal->project(ra, ca, p_nd, incremental, nullptr, stats);
+    if (wait_before_rhs) GBP_CUDA(cudaStreamWaitEvent(p->stream, wait_before_rhs, 0));
+    return p->nodal->project(ra, ca, p_nd, incremental, nullptr, stats, phi_copy);
 }
 
 int gbp_mac_set_beta(gbp_plan* p, const gbp_array4* bx, const gbp_array4* by, const gbp_array4* bz,
@@ -739,6 +764,111 @@ int gbp_plan_time_kernel(gbp_plan* p, int which, int reps, double* ms_per_launch
     return p->nodal->time_kernel(which, reps, ms_per_launch, bytes_per_launch);
 }
 
+struct gbp_amr {
+    gbp::CompositeNodal* c = nullptr;
+    gbp_geometry geom{};
+};
+
+int gbp_amr_create(const gbp_geometry* coarse, const int bc_lo[3], const int bc_hi[3], const int* fine_boxes,
+                   int nbox, const gbp_options* opt, void* stream, gbp_amr** amr)
+{
+    if (!coarse || !bc_lo || !bc_hi || !fine_boxes || nbox < 1 || !amr) {
+        set_error("gbp_amr_create: geometry, boundary types, fine boxes and the output handle are required");
+        return GBP_BAD_ARG;
+    }
+    *amr = nullptr;
+    gbp_options o;
+    if (opt)
+        o = *opt;
+    else
+        gbp_options_default(GBP_NODAL, &o);
+    gbp_amr* a = new (std::nothrow) gbp_amr;
+    if (!a) return GBP_BAD_ARG;
+    a->geom = *coarse;
+    a->c = new (std::nothrow) gbp::CompositeNodal;
+    if (!a->c) {
+        delete a;
+        return GBP_BAD_ARG;
+    }
+    int rc = a->c->init(*coarse, bc_lo, bc_hi, fine_boxes, nbox, o, static_cast<cudaStream_t>(stream));
+    if (rc) {
+        gbp_amr_destroy(a);
+        return rc;
+    }
+    *amr = a;
+    return GBP_OK;
+}
+
+int gbp_amr_destroy(gbp_amr* a)
+{
+    if (!a) return GBP_OK;
+    delete a->c;
+    delete a;
+    return GBP_OK;
+}
+
+int gbp_amr_set_options(gbp_amr* a, const gbp_options* opt)
+{
+    if (!a || !opt) return GBP_BAD_ARG;
+    return a->c->set_options(*opt);
+}
+
+size_t gbp_amr_device_bytes(const gbp_amr* a) { return a ? a->c->device_bytes() : 0; }
+
+int gbp_amr_apply_nodal_projection(gbp_amr* a, gbp_array4* vel_c, const gbp_array4* vel_old_c,
+                                   const gbp_array4* rho_c, gbp_array4* gp_c, gbp_array4* p_c,
+                                   gbp_array4* const* vel_f, const gbp_array4* const* vel_old_f,
+                                   const gbp_array4* const* rho_f, gbp_array4* const* gp_f, gbp_array4* const* p_f,
+                                   double rho0, double scaling_factor, int incremental, gbp_stats* stats)
+{
+    if (!a) {
+        set_error("gbp_amr_apply_nodal_projection: null handle");
+        return GBP_BAD_ARG;
+    }
+    const int lo[3] = {0, 0, 0};
+    const int hic[3] = {a->geom.n_cell[0] - 1, a->geom.n_cell[1] - 1, a->geom.n_cell[2] - 1};
+    const int hin[3] = {a->geom.n_cell[0], a->geom.n_cell[1], a->geom.n_cell[2]};
+    if (!valid_array(vel_c, 3) || !covers(vel_c, lo, hic) || !valid_array(gp_c, 3) || !covers(gp_c, lo, hic)) {
+        set_error("gbp_amr_apply_nodal_projection: coarse vel and gp must cover the cells with 3 components");
+        return GBP_BAD_ARG;
+    }
+    if (rho_c && !(valid_array(rho_c, 1) && covers(rho_c, lo, hic))) {
+        set_error("gbp_amr_apply_nodal_projection: coarse rho must cover the cells");
+        return GBP_BAD_ARG;
+    }
+    if (p_c && p_c->data && !(valid_array(p_c, 1) && covers(p_c, lo, hin))) {
+        set_error("gbp_amr_apply_nodal_projection: coarse p_nd must cover the nodes");
+        return GBP_BAD_ARG;
+    }
+    if ((rho_c == nullptr) != (rho_f == nullptr)) {
+        set_error("gbp_amr_apply_nodal_projection: rho must be given on both levels or on neither");
+        return GBP_BAD_ARG;
+    }
+    if (incremental && ((vel_old_c == nullptr) != (vel_old_f == nullptr))) {
+        set_error("gbp_amr_apply_nodal_projection: vel_old must be given on both levels or on neither");
+        return GBP_BAD_ARG;
+    }
+    if (vel_old_c && !(valid_array(vel_old_c, 3) && covers(vel_old_c, lo, hic))) {
+        set_error("gbp_amr_apply_nodal_projection: coarse vel_old must cover the cells with 3 components");
+        return GBP_BAD_ARG;
+    }
+    gbp::AmrFields f{};
+    f.vel_c = vel_c;
+    f.vel_old_c = incremental ? vel_old_c : nullptr;
+    f.rho_c = rho_c;
+    f.gp_c = gp_c;
+    f.p_c = (p_c && p_c->data) ? p_c : nullptr;
+    f.vel_f = vel_f;
+    f.vel_old_f = incremental ? vel_old_f : nullptr;
+    f.rho_f = rho_f;
+    f.gp_f = gp_f;
+    f.p_f = p_f;
+    f.rho0 = rho0;
+    f.scale = scaling_factor;
+    f.incremental = incremental;
+    return a->c->project(f, stats);
+}
+
 int gbp_apply_nodal_projection_host(gbp_plan* p, double* vel, const double* rho, double rho0, double* gp,
                                     double* p_nd, double scaling_factor, int incremental, gbp_stats* stats)
 {
@@ -757,15 +887,28 @@ int gbp_apply_nodal_projection_host(gbp_plan* p, double* vel, const double* rho,
         GBP_CUDA(cudaMalloc(&p->hbuf, need));
         p->hbuf_bytes = need;
     }
+    if (!p->copy_stream) {
+        GBP_CUDA(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
+        GBP_CUDA(cudaEventCreateWithFlags(&p->ev_in, cudaEventDisableTiming));
+        GBP_CUDA(cudaEventCreateWithFlags(&p->ev_phi, cudaEventDisableTiming));
+        GBP_CUDA(cudaEventCreateWithFlags(&p->ev_out, cudaEventDisableTiming));
+    }
     double* dvel = p->hbuf;
     double* dgp = dvel + 3 * nc;
     double* drho = dgp + 3 * nc;
     double* dp = drho + (rho ? nc : 0);
-    const cudaStream_t s = p->stream;
-    GBP_CUDA(cudaMemcpyAsync(dvel, vel, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, s));
-    GBP_CUDA(cudaMemcpyAsync(dgp, gp, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, s));
+    const cudaStream_t s = p->stream, c = p->copy_stream;
+    // the copy stream starts after the work already queued on the plan's stream (earlier users of
+    // the staging buffers)
+    GBP_CUDA(cudaEventRecord(p->ev_out, s));
+    GBP_CUDA(cudaStreamWaitEvent(c, p->ev_out, 0));
+    // density first on the plan's stream (sigma and its edge weights are computed from it while the
+    // velocities and gp upload on the copy stream)
     if (rho) GBP_CUDA(cudaMemcpyAsync(drho, rho, nc * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (p_nd && incremental) GBP_CUDA(cudaMemcpyAsync(dp, p_nd, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    GBP_CUDA(cudaMemcpyAsync(dvel, vel, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, c));
+    GBP_CUDA(cudaMemcpyAsync(dgp, gp, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, c));
+    if (p_nd && incremental) GBP_CUDA(cudaMemcpyAsync(dp, p_nd, nn * sizeof(double), cudaMemcpyHostToDevice, c));
+    GBP_CUDA(cudaEventRecord(p->ev_in, c));
     auto cells = [&](double* d, int nc_) {
         gbp_array4 a{};
         a.data = d;
@@ -788,13 +931,18 @@ int gbp_apply_nodal_projection_host(gbp_plan* p, double* vel, const double* rho,
     ap.jstride = nx + 1;
     ap.kstride = (long long)(nx + 1) * (ny + 1);
     ap.nstride = (long long)nn;
-    int rc = gbp_apply_nodal_projection(p, &av, nullptr, rho ? &ar : nullptr, rho0, &ag, p_nd ? &ap : nullptr, 0.0,
-                                        1.0, 1.0, scaling_factor, incremental, 0, stats);
-    if (rc != GBP_OK && rc != GBP_NOT_CONVERGED) return rc;
+    // p_nd goes back on the copy stream as soon as it is stored, while the velocity correction runs
+    gbp::HostCopy pc{p_nd, dp, nn * sizeof(double), c, p->ev_phi};
+    int rc = apply_nodal_impl(p, &av, nullptr, rho ? &ar : nullptr, rho0, &ag, p_nd ? &ap : nullptr, 0.0, 1.0, 1.0,
+                              scaling_factor, incremental, 0, stats, p->ev_in, p_nd ? &pc : nullptr);
+    if (rc != GBP_OK && rc != GBP_NOT_CONVERGED) {
+        cudaStreamSynchronize(c);
+        return rc;
+    }
     GBP_CUDA(cudaMemcpyAsync(vel, dvel, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, s));
     GBP_CUDA(cudaMemcpyAsync(gp, dgp, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, s));
-    if (p_nd) GBP_CUDA(cudaMemcpyAsync(p_nd, dp, nn * sizeof(double), cudaMemcpyDeviceToHost, s));
     GBP_CUDA(cudaStreamSynchronize(s));
+    GBP_CUDA(cudaStreamSynchronize(c));
     return rc;
 }
 

@@ -1,0 +1,1002 @@
+// Two-level (AMR) composite nodal projection (see amr.h).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+
+#include "amr.h"
+#include "gbp_internal.cuh"
+#include "nodal_kernels.h"
+
+namespace gbp {
+
+namespace {
+
+constexpr int kT = 256;
+
+// fine node classes (unique nodes of the fine bounding box)
+enum : unsigned char { F_OUT = 0, F_DOF = 1, F_ALIGNED = 2, F_HANGING = 3, F_FIXED = 4 };
+// coarse node classes
+enum : unsigned char { C_DOF = 0, C_COVERED = 1, C_IFACE = 2, C_FIXED = 3 };
+
+__device__ __forceinline__ double* at4(const gbp_array4& a, int i, int j, int k, int n)
+{
+    return a.data + (long long)(i - a.lo[0]) + (long long)(j - a.lo[1]) * a.jstride + (long long)(k - a.lo[2]) * a.kstride +
+           (long long)n * a.nstride;
+}
+
+struct BoxEntry {
+    int lo[3], hi[3];  // fine cells (global)
+    gbp_array4 a;      // the box's array (or data == nullptr)
+};
+
+// ------------------------------------------------------------------------------------------ set-up
+// fine leaf-cell mask over the bounding box (padded cell layout, periodic aliases)
+__global__ void k_amr_cmask_fine(NodalGeom gf, const BoxEntry* __restrict__ bx, int off0, int off1, int off2,
+                                 unsigned char* __restrict__ m)
+{
+    const BoxEntry b = bx[blockIdx.y];
+    const int ex = b.hi[0] - b.lo[0] + 1, ey = b.hi[1] - b.lo[1] + 1, ez = b.hi[2] - b.lo[2] + 1;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = b.lo[0] + (int)(t % ex) - off0;
+        const int j = b.lo[1] + (int)((t / ex) % ey) - off1;
+        const int k = b.lo[2] + (int)(t / ((long long)ex * ey)) - off2;
+        store_sigma_cell(m, gf, i, j, k, (unsigned char)1);
+    }
+}
+
+// coarse leaf-cell mask: a coarse cell is covered when its first fine child is a fine cell
+__global__ void k_amr_cmask_coarse(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ mf, int off0,
+                                   int off1, int off2, unsigned char* __restrict__ mc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.n[0] || j >= gc.n[1] || k >= gc.n[2]) return;
+    const int fi = 2 * i - off0, fj = 2 * j - off1, fk = 2 * k - off2;
+    const bool in = fi >= 0 && fj >= 0 && fk >= 0 && fi < gf.n[0] && fj < gf.n[1] && fk < gf.n[2] &&
+                    mf[pidx(gf.sy, gf.sz, fi, fj, fk)];
+    store_sigma_cell(mc, gc, i, j, k, (unsigned char)(in ? 0 : 1));
+}
+
+// fine node class: in (all in-domain fine cells around it are fine cells), aligned interface,
+// hanging interface, or outside; nodes of the region on a Dirichlet side are fixed
+__global__ void k_amr_classify_fine(NodalGeom gf, const unsigned char* __restrict__ mf, int off0, int off1, int off2,
+                                    int nd0, int nd1, int nd2, int dper0, int dper1, int dper2,
+                                    unsigned char* __restrict__ cls)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const int off[3] = {off0, off1, off2}, nd[3] = {nd0, nd1, nd2}, dper[3] = {dper0, dper1, dper2};
+    const int node[3] = {i, j, k};
+    int tot = 0, in = 0;
+    for (int c = 0; c < 8; ++c) {
+        int cl[3];
+        bool dom = true;
+        for (int d = 0; d < 3; ++d) {
+            int v = node[d] - 1 + ((c >> d) & 1);  // local cell index
+            int gv = v + off[d];                   // global fine cell index
+            if (dper[d]) {
+                gv = (gv % nd[d] + nd[d]) % nd[d];
+            } else if (gv < 0 || gv >= nd[d]) {
+                dom = false;
+            }
+            if (gf.per[d]) v = (v % gf.n[d] + gf.n[d]) % gf.n[d];
+            cl[d] = v;
+        }
+        if (!dom) continue;
+        ++tot;
+        if (cl[0] >= 0 && cl[1] >= 0 && cl[2] >= 0 && cl[0] < gf.n[0] && cl[1] < gf.n[1] && cl[2] < gf.n[2] &&
+            mf[pidx(gf.sy, gf.sz, cl[0], cl[1], cl[2])])
+            ++in;
+    }
+    unsigned char c = F_OUT;
+    if (in > 0) {
+        if (in == tot) {
+            c = node_is_dirichlet(gf, i, j, k) ? F_FIXED : F_DOF;
+        } else {
+            const bool even = ((i + off0) % 2 == 0) && ((j + off1) % 2 == 0) && ((k + off2) % 2 == 0);
+            c = even ? F_ALIGNED : F_HANGING;
+        }
+    }
+    cls[pidx(gf.sy, gf.sz, i, j, k)] = c;
+}
+
+// local fine node of global fine node position g (periodic wrap in the fine box), or false
+__device__ __forceinline__ bool fine_local(const NodalGeom& gf, const int off[3], const int gpos[3], int out[3])
+{
+    for (int d = 0; d < 3; ++d) {
+        int v = gpos[d] - off[d];
+        if (gf.per[d]) {
+            v = (v % gf.n[d] + gf.n[d]) % gf.n[d];
+        } else if (v < 0 || v >= gf.nu[d]) {
+            return false;
+        }
+        out[d] = v;
+    }
+    return true;
+}
+
+__global__ void k_amr_classify_coarse(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0,
+                                      int off1, int off2, unsigned char* __restrict__ ccls)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const int off[3] = {off0, off1, off2};
+    const int gpos[3] = {2 * i, 2 * j, 2 * k};
+    int m[3];
+    unsigned char fc = F_OUT;
+    if (fine_local(gf, off, gpos, m)) fc = fcls[pidx(gf.sy, gf.sz, m[0], m[1], m[2])];
+    unsigned char c;
+    if (fc == F_DOF || fc == F_FIXED)
+        c = C_COVERED;
+    else if (node_is_dirichlet(gc, i, j, k))
+        c = C_FIXED;
+    else
+        c = fc == F_ALIGNED ? C_IFACE : C_DOF;
+    ccls[pidx(gc.sy, gc.sz, i, j, k)] = c;
+}
+
+// overset mask of the fine solver: 1 on the fine unknowns only (int nodes 0..n of the bounding box)
+__global__ void k_amr_fine_mask(NodalGeom gf, const unsigned char* __restrict__ fcls, int* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > gf.n[0] || j > gf.n[1] || k > gf.n[2]) return;
+    const int iu = gf.per[0] && i == gf.n[0] ? 0 : i;
+    const int ju = gf.per[1] && j == gf.n[1] ? 0 : j;
+    const int ku = gf.per[2] && k == gf.n[2] ? 0 : k;
+    out[i + (long long)(gf.n[0] + 1) * (j + (long long)(gf.n[1] + 1) * k)] =
+        fcls[pidx(gf.sy, gf.sz, iu, ju, ku)] == F_DOF;
+}
+
+// ------------------------------------------------------------------------------ fine data in / out
+// bounding-box dense cell arrays <- per-box arrays (ncomp components), batched over the boxes
+__global__ void k_amr_gather(const BoxEntry* __restrict__ bx, int off0, int off1, int off2, int nb0, int nb1, int nb2,
+                             int ncomp, double* __restrict__ dst)
+{
+    const BoxEntry b = bx[blockIdx.y];
+    if (!b.a.data) return;
+    const int ex = b.hi[0] - b.lo[0] + 1, ey = b.hi[1] - b.lo[1] + 1, ez = b.hi[2] - b.lo[2] + 1;
+    const long long ncell = (long long)nb0 * nb1 * nb2;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int gi = b.lo[0] + (int)(t % ex), gj = b.lo[1] + (int)((t / ex) % ey),
+                  gk = b.lo[2] + (int)(t / ((long long)ex * ey));
+        const long long q = (gi - off0) + (long long)nb0 * ((gj - off1) + (long long)nb1 * (gk - off2));
+        for (int c = 0; c < ncomp; ++c) dst[q + c * ncell] = *at4(b.a, gi, gj, gk, c);
+    }
+}
+
+__global__ void k_amr_scatter(const BoxEntry* __restrict__ bx, int off0, int off1, int off2, int nb0, int nb1, int nb2,
+                              int ncomp, const double* __restrict__ src)
+{
+    const BoxEntry b = bx[blockIdx.y];
+    if (!b.a.data) return;
+    const int ex = b.hi[0] - b.lo[0] + 1, ey = b.hi[1] - b.lo[1] + 1, ez = b.hi[2] - b.lo[2] + 1;
+    const long long ncell = (long long)nb0 * nb1 * nb2;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int gi = b.lo[0] + (int)(t % ex), gj = b.lo[1] + (int)((t / ex) % ey),
+                  gk = b.lo[2] + (int)(t / ((long long)ex * ey));
+        const long long q = (gi - off0) + (long long)nb0 * ((gj - off1) + (long long)nb1 * (gk - off2));
+        for (int c = 0; c < ncomp; ++c) *at4(b.a, gi, gj, gk, c) = src[q + c * ncell];
+    }
+}
+
+// per-box nodal arrays (nodes lo..hi+1) <- fine phi on all bounding-box nodes (dense, 0..n)
+__global__ void k_amr_scatter_nodes(const BoxEntry* __restrict__ bx, int off0, int off1, int off2, int nb0, int nb1,
+                                    const double* __restrict__ src, int accumulate)
+{
+    const BoxEntry b = bx[blockIdx.y];
+    if (!b.a.data) return;
+    const int ex = b.hi[0] - b.lo[0] + 2, ey = b.hi[1] - b.lo[1] + 2, ez = b.hi[2] - b.lo[2] + 2;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int gi = b.lo[0] + (int)(t % ex), gj = b.lo[1] + (int)((t / ex) % ey),
+                  gk = b.lo[2] + (int)(t / ((long long)ex * ey));
+        const long long q = (gi - off0) + (long long)(nb0 + 1) * ((gj - off1) + (long long)(nb1 + 1) * (gk - off2));
+        double* p = at4(b.a, gi, gj, gk, 0);
+        *p = accumulate ? *p + src[q] : src[q];
+    }
+}
+
+// fine sigma on the bounding box cells (dense): scale / rho on fine cells, 0 elsewhere
+__global__ void k_amr_sigma_fine(NodalGeom gf, const unsigned char* __restrict__ mf, const double* __restrict__ rho,
+                                 int have_rho, double scale, double rho0, double* __restrict__ sig)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.n[0] || j >= gf.n[1] || k >= gf.n[2]) return;
+    const long long q = i + (long long)gf.n[0] * (j + (long long)gf.n[1] * k);
+    double v = 0.0;
+    if (mf[pidx(gf.sy, gf.sz, i, j, k)]) v = have_rho ? scale / rho[q] : scale / rho0;
+    sig[q] = v;
+}
+
+// coarse sigma with covered cells zeroed (whole padded arrays, aliases included)
+__global__ void k_amr_mask_sigma(long long count, const double* __restrict__ s, const unsigned char* __restrict__ m,
+                                 double* __restrict__ out)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < count) out[t] = m[t] ? s[t] : 0.0;
+}
+
+// ------------------------------------------------------------------------------ composite operator
+__device__ __forceinline__ int cwrap(const NodalGeom& gc, int d, int v)
+{
+    return gc.per[d] ? (v % gc.n[d] + gc.n[d]) % gc.n[d] : v;
+}
+
+// interface values of the fine level from the coarse one: aligned nodes copy, hanging nodes
+// interpolate along the coarse face they lie on
+__global__ void k_amr_fill_fine(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0, int off1,
+                                int off2, const double* __restrict__ pc, double* pf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const unsigned char c = fcls[pidx(gf.sy, gf.sz, i, j, k)];
+    if (c != F_ALIGNED && c != F_HANGING) return;
+    const int gpos[3] = {i + off0, j + off1, k + off2};
+    double acc = 0.0;
+    int nodd = 0;
+    for (int d = 0; d < 3; ++d) nodd += gpos[d] & 1;
+    const double w = nodd == 0 ? 1.0 : (nodd == 1 ? 0.5 : 0.25);
+    for (int q = 0; q < 8; ++q) {
+        int I[3];
+        bool use = true;
+        for (int d = 0; d < 3; ++d) {
+            const int sel = (q >> d) & 1;
+            if (gpos[d] & 1) {
+                I[d] = cwrap(gc, d, (gpos[d] - 1) / 2 + sel);
+            } else {
+                if (sel) use = false;
+                I[d] = cwrap(gc, d, gpos[d] / 2);
+            }
+        }
+        if (use) acc += pc[pidx(gc.sy, gc.sz, I[0], I[1], I[2])];
+    }
+    store_node(pf, gf, i, j, k, w * acc);
+}
+
+// v_c[I] += sum of the interface fine values that map to the coarse interface node I (the aligned
+// node with weight 1, hanging nodes 2I + delta with weight 2^-|delta|)
+__global__ void k_amr_sync(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ ccls,
+                           const unsigned char* __restrict__ fcls, int off0, int off1, int off2,
+                           const double* __restrict__ vf, double* __restrict__ vc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const long long p = pidx(gc.sy, gc.sz, i, j, k);
+    if (ccls[p] != C_IFACE) return;
+    const int off[3] = {off0, off1, off2};
+    double acc = 0.0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int gpos[3] = {2 * i + dx, 2 * j + dy, 2 * k + dz};
+                int m[3];
+                if (!fine_local(gf, off, gpos, m)) continue;
+                const long long q = pidx(gf.sy, gf.sz, m[0], m[1], m[2]);
+                const unsigned char c = fcls[q];
+                const int nz = (dx != 0) + (dy != 0) + (dz != 0);
+                if ((nz == 0 && c == F_ALIGNED) || (nz > 0 && c == F_HANGING))
+                    acc += (nz == 0 ? 1.0 : (nz == 1 ? 0.5 : 0.25)) * vf[q];
+            }
+    vc[p] += acc;
+}
+
+// zero the entries that are not unknowns (both levels)
+__global__ void k_amr_zero_nondof(NodalGeom gc, const unsigned char* __restrict__ ccls, double* __restrict__ vc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const long long p = pidx(gc.sy, gc.sz, i, j, k);
+    const unsigned char c = ccls[p];
+    if (c == C_COVERED || c == C_FIXED) vc[p] = 0.0;
+}
+__global__ void k_amr_zero_nondof_fine(NodalGeom gf, const unsigned char* __restrict__ fcls, double* __restrict__ vf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const long long p = pidx(gf.sy, gf.sz, i, j, k);
+    if (fcls[p] != F_DOF) vf[p] = 0.0;
+}
+
+// composite max norm |v| / V over the unknowns of both levels (per-level node volumes)
+__global__ void k_amr_norm_c(NodalGeom gc, const unsigned char* __restrict__ ccls, const double* __restrict__ v,
+                             unsigned long long* norm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    double nv = 0.0;
+    if (i < gc.nu[0] && j < gc.nu[1] && k < gc.nu[2]) {
+        const long long p = pidx(gc.sy, gc.sz, i, j, k);
+        const unsigned char c = ccls[p];
+        if (c == C_DOF || c == C_IFACE) nv = fabs(v[p]) * node_inv_volume(gc, i, j, k);
+        if (v[p] != v[p] && (c == C_DOF || c == C_IFACE)) nv = v[p];
+    }
+    nv = block_max(nv);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, nv);
+}
+__global__ void k_amr_norm_f(NodalGeom gf, const unsigned char* __restrict__ fcls, const double* __restrict__ v,
+                             unsigned long long* norm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    double nv = 0.0;
+    if (i < gf.nu[0] && j < gf.nu[1] && k < gf.nu[2]) {
+        const long long p = pidx(gf.sy, gf.sz, i, j, k);
+        if (fcls[p] == F_DOF) nv = v[p] != v[p] ? v[p] : fabs(v[p]) * node_inv_volume(gf, i, j, k);
+    }
+    nv = block_max(nv);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, nv);
+}
+
+// restriction of the composite residual to the whole coarse level: the coarse unknowns' own residual
+// plus the trilinear (full-weighting) transpose of the fine unknowns' residuals
+__global__ void k_amr_restrict(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ ccls,
+                               const unsigned char* __restrict__ fcls, int off0, int off1, int off2,
+                               const double* __restrict__ rc, const double* __restrict__ rf, double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const long long p = pidx(gc.sy, gc.sz, i, j, k);
+    const unsigned char c = ccls[p];
+    double acc = (c == C_DOF || c == C_IFACE) ? rc[p] : 0.0;
+    if (c != C_FIXED) {
+        const int off[3] = {off0, off1, off2};
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int gpos[3] = {2 * i + dx, 2 * j + dy, 2 * k + dz};
+                    int m[3];
+                    if (!fine_local(gf, off, gpos, m)) continue;
+                    const long long q = pidx(gf.sy, gf.sz, m[0], m[1], m[2]);
+                    if (fcls[q] != F_DOF) continue;
+                    const int nz = (dx != 0) + (dy != 0) + (dz != 0);
+                    acc += (nz == 0 ? 1.0 : (nz == 1 ? 0.5 : (nz == 2 ? 0.25 : 0.125))) * rf[q];
+                }
+    }
+    store_node(out, gc, i, j, k, acc);
+}
+
+// phi_c += e_c on the coarse unknowns; phi_f += (trilinear e_c) on the fine unknowns
+__global__ void k_amr_prolong_c(NodalGeom gc, const unsigned char* __restrict__ ccls, const double* __restrict__ e,
+                                double* pc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const long long p = pidx(gc.sy, gc.sz, i, j, k);
+    const unsigned char c = ccls[p];
+    if (c == C_DOF || c == C_IFACE) store_node(pc, gc, i, j, k, pc[p] + e[p]);
+}
+__global__ void k_amr_prolong_f(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0, int off1,
+                                int off2, const double* __restrict__ e, double* pf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const long long q = pidx(gf.sy, gf.sz, i, j, k);
+    if (fcls[q] != F_DOF) return;
+    const int gpos[3] = {i + off0, j + off1, k + off2};
+    double acc = 0.0;
+    for (int s = 0; s < 8; ++s) {
+        int I[3];
+        double w = 1.0;
+        bool use = true;
+        for (int d = 0; d < 3; ++d) {
+            const int sel = (s >> d) & 1;
+            if (gpos[d] & 1) {
+                I[d] = cwrap(gc, d, (gpos[d] - 1) / 2 + sel);
+                w *= 0.5;
+            } else {
+                if (sel) use = false;
+                I[d] = cwrap(gc, d, gpos[d] / 2);
+            }
+        }
+        if (use) acc += w * e[pidx(gc.sy, gc.sz, I[0], I[1], I[2])];
+    }
+    store_node(pf, gf, i, j, k, pf[q] + acc);
+}
+
+// covered coarse nodes take the fine value at their position (output and coarse gradient)
+__global__ void k_amr_inject(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ ccls, int off0, int off1,
+                             int off2, const double* __restrict__ pf, double* pc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    if (ccls[pidx(gc.sy, gc.sz, i, j, k)] != C_COVERED) return;
+    const int off[3] = {off0, off1, off2};
+    const int gpos[3] = {2 * i, 2 * j, 2 * k};
+    int m[3];
+    if (!fine_local(gf, off, gpos, m)) return;
+    store_node(pc, gc, i, j, k, pf[pidx(gf.sy, gf.sz, m[0], m[1], m[2])]);
+}
+
+// sums over the unknowns of v and of the node volumes (consistency of a singular system)
+__global__ void k_amr_sums_c(NodalGeom gc, const unsigned char* __restrict__ ccls, const double* __restrict__ v,
+                             double* __restrict__ part)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    double a = 0.0, b = 0.0;
+    if (i < gc.nu[0] && j < gc.nu[1] && k < gc.nu[2]) {
+        const long long p = pidx(gc.sy, gc.sz, i, j, k);
+        const unsigned char c = ccls[p];
+        if (c == C_DOF || c == C_IFACE) {
+            a = v[p];
+            b = node_volume(gc, i, j, k);
+        }
+    }
+    a = block_sum_all(a);
+    b = block_sum_all(b);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+        const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        atomicAdd(part, a);
+        atomicAdd(part + 1, b);
+        (void)bid;
+    }
+}
+__global__ void k_amr_sums_f(NodalGeom gf, const unsigned char* __restrict__ fcls, const double* __restrict__ v,
+                             double* __restrict__ part)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    double a = 0.0, b = 0.0;
+    if (i < gf.nu[0] && j < gf.nu[1] && k < gf.nu[2]) {
+        const long long p = pidx(gf.sy, gf.sz, i, j, k);
+        if (fcls[p] == F_DOF) {
+            a = v[p];
+            b = node_volume(gf, i, j, k);
+        }
+    }
+    a = block_sum_all(a);
+    b = block_sum_all(b);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+        atomicAdd(part, a);
+        atomicAdd(part + 1, b);
+    }
+}
+// v -= V_node * (sum v / sum V) on the unknowns
+__global__ void k_amr_consistent_c(NodalGeom gc, const unsigned char* __restrict__ ccls, const double* __restrict__ part,
+                                   double* __restrict__ v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const long long p = pidx(gc.sy, gc.sz, i, j, k);
+    const unsigned char c = ccls[p];
+    if (c == C_DOF || c == C_IFACE) v[p] -= node_volume(gc, i, j, k) * (part[0] / part[1]);
+}
+__global__ void k_amr_consistent_f(NodalGeom gf, const unsigned char* __restrict__ fcls, const double* __restrict__ part,
+                                   double* __restrict__ v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const long long p = pidx(gf.sy, gf.sz, i, j, k);
+    if (fcls[p] == F_DOF) v[p] -= node_volume(gf, i, j, k) * (part[0] / part[1]);
+}
+// fine phi -= c on the region's nodes (the gauge shift of the coarse level)
+__global__ void k_amr_shift_f(NodalGeom gf, const unsigned char* __restrict__ fcls, const double* __restrict__ scal,
+                              double* pf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const long long p = pidx(gf.sy, gf.sz, i, j, k);
+    if (fcls[p] != F_OUT && fcls[p] != F_FIXED) store_node(pf, gf, i, j, k, pf[p] - *scal);
+}
+
+// dense copy of phi on all bounding-box nodes 0..n (periodic duplicates from the aliases)
+__global__ void k_amr_fine_nodes(NodalGeom gf, const double* __restrict__ pf, double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > gf.n[0] || j > gf.n[1] || k > gf.n[2]) return;
+    out[i + (long long)(gf.n[0] + 1) * (j + (long long)(gf.n[1] + 1) * k)] = pf[pidx(gf.sy, gf.sz, i, j, k)];
+}
+
+inline dim3 g3(int a, int b, int c) { return dim3((a + 31) / 32, (b + 3) / 4, (c + 1) / 2); }
+const dim3 kB3(32, 4, 2);
+inline dim3 gnodes(const NodalGeom& g) { return g3(g.nu[0], g.nu[1], g.nu[2]); }
+inline double bits_to_double(unsigned long long b)
+{
+    double v;
+    memcpy(&v, &b, sizeof(v));
+    return v;
+}
+
+}  // namespace
+
+CompositeNodal::~CompositeNodal()
+{
+    if (st) cudaStreamSynchronize(st);
+    if (hnorm) cudaFreeHost(hnorm);
+    if (dboxes) cudaFree(dboxes);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    pool.release();
+}
+
+size_t CompositeNodal::device_bytes() const { return pool.bytes + crs.device_bytes() + fin.device_bytes(); }
+
+int CompositeNodal::set_options(const gbp_options& o)
+{
+    int rc = crs.set_options(o);
+    if (!rc) rc = fin.set_options(o);
+    if (!rc) opt = o;
+    return rc;
+}
+
+int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const int bc_hi[3], const int* bxs, int nbox,
+                         const gbp_options& o, cudaStream_t stream)
+{
+    opt = o;
+    st = stream;
+    geom_c = coarse;
+    if (nbox < 1 || !bxs) {
+        set_error("amr plan: at least one fine box is needed");
+        return GBP_BAD_ARG;
+    }
+    int nd[3];
+    bool per[3];
+    singular = true;
+    for (int d = 0; d < 3; ++d) {
+        bclo[d] = bc_lo[d];
+        bchi[d] = bc_hi[d];
+        nd[d] = 2 * coarse.n_cell[d];
+        per[d] = bc_lo[d] == GBP_BC_PERIODIC;
+        for (int b : {bc_lo[d], bc_hi[d]}) {
+            if (b == GBP_BC_INFLOW || b == GBP_BC_ROBIN) {
+                set_error("amr plan: inflow and Robin sides are not supported by the composite solve");
+                return GBP_BAD_ARG;
+            }
+            if (b == GBP_BC_DIRICHLET) singular = false;
+        }
+    }
+    boxes.assign(nbox, AmrBox{});
+    int blo[3] = {1 << 30, 1 << 30, 1 << 30}, bhi[3] = {-1, -1, -1};
+    for (int b = 0; b < nbox; ++b) {
+        for (int d = 0; d < 3; ++d) {
+            boxes[b].lo[d] = bxs[6 * b + d];
+            boxes[b].hi[d] = bxs[6 * b + 3 + d];
+            const int lo = boxes[b].lo[d], hi = boxes[b].hi[d];
+            if (lo < 0 || hi >= nd[d] || hi < lo || (lo & 1) || !(hi & 1)) {
+                set_error("amr plan: fine boxes must lie in the domain and cover whole coarse cells (even lo, odd hi)");
+                return GBP_BAD_ARG;
+            }
+            blo[d] = std::min(blo[d], lo);
+            bhi[d] = std::max(bhi[d], hi);
+        }
+    }
+    // overlap check (disjoint boxes, as in an AMReX BoxArray)
+    for (int a = 0; a < nbox; ++a)
+        for (int b = a + 1; b < nbox; ++b) {
+            bool ov = true;
+            for (int d = 0; d < 3; ++d)
+                ov = ov && !(boxes[a].hi[d] < boxes[b].lo[d] || boxes[b].hi[d] < boxes[a].lo[d]);
+            if (ov) {
+                set_error("amr plan: fine boxes overlap");
+                return GBP_BAD_ARG;
+            }
+        }
+    // bounding box; in a periodic direction that it touches at either end it spans the whole domain
+    // (the region may then continue across the periodic seam)
+    int fbclo[3], fbchi[3];
+    for (int d = 0; d < 3; ++d) {
+        if (per[d] && (blo[d] == 0 || bhi[d] == nd[d] - 1)) {
+            blo[d] = 0;
+            bhi[d] = nd[d] - 1;
+        }
+        off[d] = blo[d];
+        nfb[d] = bhi[d] - blo[d] + 1;
+        if (per[d] && nfb[d] == nd[d]) {
+            fbclo[d] = fbchi[d] = GBP_BC_PERIODIC;
+        } else {
+            fbclo[d] = (blo[d] == 0) ? (per[d] ? GBP_BC_NEUMANN : bc_lo[d]) : GBP_BC_NEUMANN;
+            fbchi[d] = (bhi[d] == nd[d] - 1) ? (per[d] ? GBP_BC_NEUMANN : bc_hi[d]) : GBP_BC_NEUMANN;
+        }
+    }
+    gbp_geometry gfine{};
+    for (int d = 0; d < 3; ++d) {
+        const double hf = (coarse.prob_hi[d] - coarse.prob_lo[d]) / nd[d];
+        gfine.n_cell[d] = nfb[d];
+        gfine.prob_lo[d] = coarse.prob_lo[d] + off[d] * hf;
+        gfine.prob_hi[d] = gfine.prob_lo[d] + nfb[d] * hf;
+    }
+    int rc = crs.init(coarse, bc_lo, bc_hi, o, stream);
+    if (rc) return rc;
+    rc = fin.init(gfine, fbclo, fbchi, o, stream);
+    if (rc) return rc;
+    gc = crs.geom0();
+    gf = fin.geom0();
+    gf_nomask = gf;
+    gf_nomask.mask = nullptr;
+    // device storage
+    size_t need = 0;
+    auto add = [&](size_t cnt, size_t sz) { need = ((need + 255) & ~size_t(255)) + cnt * sz; };
+    const size_t ncf = (size_t)nfb[0] * nfb[1] * nfb[2];
+    const size_t nnf = (size_t)(nfb[0] + 1) * (nfb[1] + 1) * (nfb[2] + 1);
+    add(gc.count, 1);
+    add(gf.count, 1);
+    add(gc.count, 1);
+    add(gf.count, 1);
+    for (int q = 0; q < 6; ++q) add(gc.count, 8);  // sc_m, phi_c, b_c, r_c, rc_full, e_c
+    for (int q = 0; q < 3; ++q) add(gf.count, 8);  // phi_f, b_f, r_f
+    add(3 * ncf, 8);                               // vel_f
+    add(3 * ncf, 8);                               // gp_f
+    add(ncf, 8);                                   // rho_f
+    add(3 * ncf, 8);                               // velo_f
+    add(ncf, 8);                                   // sig_f
+    add(nnf, 8);                                   // p_fb
+    nparts = std::max(nodal_partials_needed(gc), 1184);
+    add(nparts + 64, 8);
+    add(8, 8);
+    add(8, 8);
+    need += 4096;
+    rc = pool.reserve(need);
+    if (rc) return rc;
+    cmask_c = pool.take<unsigned char>(gc.count);
+    cmask_f = pool.take<unsigned char>(gf.count);
+    ccls = pool.take<unsigned char>(gc.count);
+    fcls = pool.take<unsigned char>(gf.count);
+    sc_m = pool.take<double>(gc.count);
+    phi_c = pool.take<double>(gc.count);
+    b_c = pool.take<double>(gc.count);
+    r_c = pool.take<double>(gc.count);
+    rc_full = pool.take<double>(gc.count);
+    e_c = pool.take<double>(gc.count);
+    phi_f = pool.take<double>(gf.count);
+    b_f = pool.take<double>(gf.count);
+    r_f = pool.take<double>(gf.count);
+    vel_f = pool.take<double>(3 * ncf);
+    gp_f = pool.take<double>(3 * ncf);
+    rho_f = pool.take<double>(ncf);
+    velo_f = pool.take<double>(3 * ncf);
+    sig_f = pool.take<double>(ncf);
+    p_fb = pool.take<double>(nnf);
+    part = pool.take<double>(nparts + 64);
+    scal = pool.take<double>(8);
+    dnorm = pool.take<unsigned long long>(8);
+    GBP_CUDA(cudaMallocHost(&hnorm, 8 * sizeof(unsigned long long)));
+    GBP_CUDA(cudaEventCreate(&ev0));
+    GBP_CUDA(cudaEventCreate(&ev1));
+    dboxes_bytes = sizeof(BoxEntry) * (size_t)nbox;
+    GBP_CUDA(cudaMalloc(&dboxes, dboxes_bytes));
+    // masks and classes
+    std::vector<BoxEntry> tab(nbox);
+    for (int b = 0; b < nbox; ++b) {
+        memset(&tab[b], 0, sizeof(BoxEntry));
+        for (int d = 0; d < 3; ++d) {
+            tab[b].lo[d] = boxes[b].lo[d];
+            tab[b].hi[d] = boxes[b].hi[d];
+        }
+    }
+    GBP_CUDA(cudaMemcpyAsync(dboxes, tab.data(), dboxes_bytes, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemsetAsync(cmask_f, 0, gf.count, st));
+    GBP_CUDA(cudaMemsetAsync(cmask_c, 0, gc.count, st));
+    GBP_CUDA(cudaMemsetAsync(fcls, 0, gf.count, st));
+    GBP_CUDA(cudaMemsetAsync(ccls, C_FIXED, gc.count, st));
+    k_amr_cmask_fine<<<dim3(64, nbox), kT, 0, st>>>(gf, (const BoxEntry*)dboxes, off[0], off[1], off[2], cmask_f);
+    k_amr_cmask_coarse<<<g3(gc.n[0], gc.n[1], gc.n[2]), kB3, 0, st>>>(gc, gf, cmask_f, off[0], off[1], off[2], cmask_c);
+    k_amr_classify_fine<<<gnodes(gf), kB3, 0, st>>>(gf, cmask_f, off[0], off[1], off[2], nd[0], nd[1], nd[2], per[0],
+                                                  per[1], per[2], fcls);
+    k_amr_classify_coarse<<<gnodes(gc), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], ccls);
+    GBP_CUDA(cudaGetLastError());
+    // the fine solver's overset mask: the fine unknowns
+    int* im = nullptr;
+    GBP_CUDA(cudaMalloc(&im, sizeof(int) * nnf));
+    k_amr_fine_mask<<<g3(gf.n[0] + 1, gf.n[1] + 1, gf.n[2] + 1), kB3, 0, st>>>(gf, fcls, im);
+    gbp_iarray4 ma{};
+    ma.data = im;
+    for (int d = 0; d < 3; ++d) ma.hi[d] = nfb[d];
+    ma.jstride = nfb[0] + 1;
+    ma.kstride = (long long)(nfb[0] + 1) * (nfb[1] + 1);
+    rc = fin.set_mask(&ma);
+    cudaStreamSynchronize(st);
+    cudaFree(im);
+    if (rc) return rc;
+    gf = fin.geom0();  // now carries the mask
+    return GBP_OK;
+}
+
+int CompositeNodal::check_fields(const AmrFields& f)
+{
+    if (!f.vel_c || !f.vel_f || !f.gp_c || !f.gp_f) {
+        set_error("amr project: velocity and gp are required on both levels");
+        return GBP_BAD_ARG;
+    }
+    for (size_t b = 0; b < boxes.size(); ++b) {
+        if (!f.vel_f[b] || !f.vel_f[b]->data || !f.gp_f[b] || !f.gp_f[b]->data) {
+            set_error("amr project: every fine box needs its velocity and gp");
+            return GBP_BAD_ARG;
+        }
+        const gbp_array4* arr[4] = {f.vel_f[b], f.gp_f[b], f.rho_f ? f.rho_f[b] : nullptr,
+                                    f.vel_old_f ? f.vel_old_f[b] : nullptr};
+        for (const gbp_array4* a : arr) {
+            if (!a || !a->data) continue;
+            for (int d = 0; d < 3; ++d)
+                if (a->lo[d] > boxes[b].lo[d] || a->hi[d] < boxes[b].hi[d]) {
+                    set_error("amr project: a fine array does not cover its box");
+                    return GBP_BAD_ARG;
+                }
+        }
+        if (f.p_f && f.p_f[b] && f.p_f[b]->data)
+            for (int d = 0; d < 3; ++d)
+                if (f.p_f[b]->lo[d] > boxes[b].lo[d] || f.p_f[b]->hi[d] < boxes[b].hi[d] + 1) {
+                    set_error("amr project: a fine p_nd array does not cover its box's nodes");
+                    return GBP_BAD_ARG;
+                }
+    }
+    return GBP_OK;
+}
+
+// v_c (coarse interface nodes) += the restricted interface values of v_f
+void CompositeNodal::sync(double* vc, const double* vf)
+{
+    k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], vf, vc);
+}
+
+// r = b - A phi on both levels (fine interface values filled first), with the fine interface
+// residuals restricted into the coarse interface nodes; norm (if given) = composite max norm
+void CompositeNodal::composite_residual(const double* bc, const double* bf, unsigned long long* norm)
+{
+    k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], phi_c, phi_f);
+    nodal_resid<double>(gf_nomask, fin.sigma64(), phi_f, bf, r_f, nullptr, st);
+    nodal_resid<double>(gc, sc_m, phi_c, bc, r_c, nullptr, st);
+    sync(r_c, r_f);
+    if (norm) {
+        k_amr_norm_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, r_c, norm);
+        k_amr_norm_f<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, r_f, norm);
+    }
+}
+
+int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
+{
+    int rc = check_fields(f);
+    if (rc) return rc;
+    const int nbox = (int)boxes.size();
+    const size_t ncf = (size_t)nfb[0] * nfb[1] * nfb[2];
+    GBP_CUDA(cudaEventRecord(ev0, st));
+    // fine inputs into the bounding box (cells outside the fine boxes: zero)
+    std::vector<BoxEntry> tab(nbox);
+    auto gather = [&](const gbp_array4* const* arr, int ncomp, double* dst) -> int {
+        GBP_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * ncomp * ncf, st));
+        if (!arr) return GBP_OK;
+        for (int b = 0; b < nbox; ++b) {
+            memset(&tab[b], 0, sizeof(BoxEntry));
+            for (int d = 0; d < 3; ++d) {
+                tab[b].lo[d] = boxes[b].lo[d];
+                tab[b].hi[d] = boxes[b].hi[d];
+            }
+            if (arr[b]) tab[b].a = *arr[b];
+        }
+        GBP_CUDA(cudaMemcpyAsync(dboxes, tab.data(), dboxes_bytes, cudaMemcpyHostToDevice, st));
+        k_amr_gather<<<dim3(64, nbox), kT, 0, st>>>((const BoxEntry*)dboxes, off[0], off[1], off[2], nfb[0], nfb[1],
+                                                    nfb[2], ncomp, dst);
+        // the table is reused by the next gather: let this one finish reading it
+        GBP_CUDA(cudaStreamSynchronize(st));
+        return GBP_OK;
+    };
+    if ((rc = gather((const gbp_array4* const*)f.vel_f, 3, vel_f))) return rc;
+    if ((rc = gather((const gbp_array4* const*)f.gp_f, 3, gp_f))) return rc;
+    if ((rc = gather(f.rho_f, 1, rho_f))) return rc;
+    if ((rc = gather(f.vel_old_f, 3, velo_f))) return rc;
+    // sigma on both levels (coarse: whole level for the V-cycles, covered cells zeroed for the
+    // composite operator; fine: zero outside the fine cells)
+    rc = crs.set_sigma_from_density(f.rho_c, f.scale, f.rho0);
+    if (rc) return rc;
+    k_amr_mask_sigma<<<(unsigned)((gc.count + kT - 1) / kT), kT, 0, st>>>(gc.count, crs.sigma64(), cmask_c, sc_m);
+    k_amr_sigma_fine<<<g3(nfb[0], nfb[1], nfb[2]), kB3, 0, st>>>(gf, cmask_f, rho_f, f.rho_f != nullptr, f.scale,
+                                                                 f.rho0, sig_f);
+    gbp_array4 sa{};
+    sa.data = sig_f;
+    for (int d = 0; d < 3; ++d) sa.hi[d] = nfb[d] - 1;
+    sa.ncomp = 1;
+    sa.jstride = nfb[0];
+    sa.kstride = (long long)nfb[0] * nfb[1];
+    sa.nstride = (long long)ncf;
+    rc = fin.set_sigma(&sa, 0.0);
+    if (rc) return rc;
+    // right-hand sides: leaf cells of each level, then the fine interface into the coarse interface
+    const bool sub_old = f.incremental && f.vel_old_c;
+    auto cellsf = [&](double* d, int nc_) {
+        gbp_array4 a{};
+        a.data = d;
+        for (int q = 0; q < 3; ++q) a.hi[q] = nfb[q] - 1;
+        a.ncomp = nc_;
+        a.jstride = nfb[0];
+        a.kstride = (long long)nfb[0] * nfb[1];
+        a.nstride = (long long)ncf;
+        return a;
+    };
+    RhsArgs rac{}, raf{};
+    for (int d = 0; d < 3; ++d) {
+        const double hc[3] = {gc.h[0], gc.h[1], gc.h[2]};
+        const int e = d == 0 ? 1 : 0, q = d == 2 ? 1 : 2;
+        rac.cf[d] = hc[e] * hc[q] / 4.0;
+        raf.cf[d] = gf.h[e] * gf.h[q] / 4.0;
+    }
+    rac.vel = *f.vel_c;
+    rac.gp = *f.gp_c;
+    rac.add_gp = !f.incremental;
+    rac.sub_old = sub_old;
+    if (sub_old) rac.vel_old = *f.vel_old_c;
+    rac.cmask = cmask_c;
+    raf.vel = cellsf(vel_f, 3);
+    raf.gp = cellsf(gp_f, 3);
+    raf.add_gp = !f.incremental;
+    raf.sub_old = sub_old;
+    if (sub_old) raf.vel_old = cellsf(velo_f, 3);
+    raf.cmask = cmask_f;
+    nodal_rhs(gc, rac, crs.sigma64(), b_c, nullptr, st);
+    nodal_rhs(gf_nomask, raf, fin.sigma64(), b_f, nullptr, st);
+    sync(b_c, b_f);
+    k_amr_zero_nondof<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, b_c);
+    k_amr_zero_nondof_fine<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, b_f);
+    if (singular) {
+        GBP_CUDA(cudaMemsetAsync(part, 0, 2 * sizeof(double), st));
+        k_amr_sums_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, b_c, part);
+        k_amr_sums_f<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, b_f, part);
+        k_amr_consistent_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, part, b_c);
+        k_amr_consistent_f<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, part, b_f);
+    }
+    GBP_CUDA(cudaMemsetAsync(dnorm, 0, 2 * sizeof(unsigned long long), st));
+    k_amr_norm_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, b_c, dnorm);
+    k_amr_norm_f<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, b_f, dnorm);
+    GBP_CUDA(cudaMemsetAsync(phi_c, 0, sizeof(double) * gc.count, st));
+    GBP_CUDA(cudaMemsetAsync(phi_f, 0, sizeof(double) * gf.count, st));
+    composite_residual(b_c, b_f, dnorm + 1);
+    GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    GBP_CUDA(cudaGetLastError());
+    const double bnorm = bits_to_double(hnorm[0]);
+    double rn = bits_to_double(hnorm[1]);
+    if (!isfinite(bnorm) || !isfinite(rn)) {
+        set_error("amr solve: right-hand side is not finite");
+        return GBP_NAN;
+    }
+    const double target = std::max(opt.rtol * (opt.always_use_bnorm ? bnorm : rn), opt.atol);
+    double scale32 = 1.0;
+    if (bnorm > 0.0) {
+        int ex = 0;
+        frexp(bnorm * gc.vol, &ex);
+        scale32 = ldexp(1.0, -ex);
+    }
+    const int m = 2;  // V-cycles per level per step
+    int it = 0, status = GBP_OK;
+    const double r0 = rn;
+    while (rn > target) {
+        if (it >= opt.maxiter) {
+            status = GBP_NOT_CONVERGED;
+            set_error("amr solve: maxiter reached before the tolerance");
+            break;
+        }
+        // coarse correction on the restricted composite residual
+        k_amr_restrict<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], r_c, r_f, rc_full);
+        GBP_CUDA(cudaMemsetAsync(e_c, 0, sizeof(double) * gc.count, st));
+        crs.apply_vcycles(rc_full, e_c, m, scale32, st);
+        k_amr_prolong_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, e_c, phi_c);
+        k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], e_c, phi_f);
+        // fine correction on the fresh fine residual, interface held
+        k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], phi_c, phi_f);
+        nodal_resid<double>(gf_nomask, fin.sigma64(), phi_f, b_f, r_f, nullptr, st);
+        fin.apply_vcycles(r_f, phi_f, m, scale32, st);
+        // composite residual and its norm
+        GBP_CUDA(cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st));
+        composite_residual(b_c, b_f, dnorm + 1);
+        GBP_CUDA(cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+        GBP_CUDA(cudaGetLastError());
+        rn = bits_to_double(hnorm[1]);
+        ++it;
+        if (opt.verbose > 1) fprintf(stderr, "gbp amr: iter %d rel resid %.3e\n", it, bnorm > 0 ? rn / bnorm : rn);
+        if (!isfinite(rn)) {
+            status = GBP_NAN;
+            set_error("amr solve: residual became NaN/Inf");
+            break;
+        }
+    }
+    // outputs: interface values, covered coarse nodes from the fine level, gauge of a singular system
+    k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], phi_c, phi_f);
+    k_amr_inject<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, off[0], off[1], off[2], phi_f, phi_c);
+    if (singular) {
+        nodal_remove_mean(gc, phi_c, part, scal, 1, 0, 0, nullptr, st);
+        k_amr_shift_f<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, scal, phi_f);
+    }
+    // corrections per level
+    CorrArgs cac{}, caf{};
+    for (int d = 0; d < 3; ++d) {
+        cac.inv4h[d] = 1.0 / (4.0 * gc.h[d]);
+        caf.inv4h[d] = 1.0 / (4.0 * gf.h[d]);
+    }
+    cac.vel = *f.vel_c;
+    cac.gp = *f.gp_c;
+    cac.add_gp = !f.incremental;
+    cac.incremental = f.incremental;
+    caf.vel = cellsf(vel_f, 3);
+    caf.gp = cellsf(gp_f, 3);
+    caf.add_gp = !f.incremental;
+    caf.incremental = f.incremental;
+    if (f.p_c && f.p_c->data) nodal_store_phi(gc, *f.p_c, phi_c, f.incremental, st);
+    nodal_correct(gc, cac, crs.sigma64(), phi_c, st);
+    nodal_correct(gf_nomask, caf, fin.sigma64(), phi_f, st);
+    k_amr_fine_nodes<<<g3(nfb[0] + 1, nfb[1] + 1, nfb[2] + 1), kB3, 0, st>>>(gf, phi_f, p_fb);
+    // fine outputs back into the boxes
+    auto scatter = [&](gbp_array4* const* arr, int ncomp, const double* src, bool nodes) -> int {
+        if (!arr) return GBP_OK;
+        for (int b = 0; b < nbox; ++b) {
+            memset(&tab[b], 0, sizeof(BoxEntry));
+            for (int d = 0; d < 3; ++d) {
+                tab[b].lo[d] = boxes[b].lo[d];
+                tab[b].hi[d] = boxes[b].hi[d];
+            }
+            if (arr[b]) tab[b].a = *arr[b];
+        }
+        GBP_CUDA(cudaMemcpyAsync(dboxes, tab.data(), dboxes_bytes, cudaMemcpyHostToDevice, st));
+        if (nodes)
+            k_amr_scatter_nodes<<<dim3(64, nbox), kT, 0, st>>>((const BoxEntry*)dboxes, off[0], off[1], off[2], nfb[0],
+                                                               nfb[1], src, f.incremental);
+        else
+            k_amr_scatter<<<dim3(64, nbox), kT, 0, st>>>((const BoxEntry*)dboxes, off[0], off[1], off[2], nfb[0], nfb[1],
+                                                         nfb[2], ncomp, src);
+        GBP_CUDA(cudaStreamSynchronize(st));
+        return GBP_OK;
+    };
+    if ((rc = scatter(f.vel_f, 3, vel_f, false))) return rc;
+    if ((rc = scatter(f.gp_f, 3, gp_f, false))) return rc;
+    if ((rc = scatter(f.p_f, 1, p_fb, true))) return rc;
+    GBP_CUDA(cudaEventRecord(ev1, st));
+    GBP_CUDA(cudaEventSynchronize(ev1));
+    GBP_CUDA(cudaGetLastError());
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->status = status;
+        stats->outer_iters = it + 1;
+        stats->vcycles = 2 * m * it;
+        stats->num_levels = 2;
+        stats->rhs_norm = bnorm;
+        stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;
+        stats->final_rel_resid = bnorm > 0 ? rn / bnorm : rn;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        stats->ms_total = ms;
+    }
+    return status;
+}
+
+}  // namespace gbp

@@ -1,0 +1,87 @@
+// Two-level (AMR) composite nodal projection: incflo::ApplyNodalProjection over finest_level = 1
+// (src/projection/incflo_apply_nodal_projection.cpp:95-267) with one NodalProjector over both levels
+// (:187-192) and MLNodeLaplacian's composite solve (:215).
+//
+// Discretisation: conforming Q1 elements on the composite mesh. Leaf cells are the fine cells of the
+// fine boxes (ratio 2) and the coarse cells they do not cover; unknowns are the uncovered coarse nodes
+// and the fine nodes strictly inside the fine region; fine nodes on the coarse-fine interface at coarse
+// positions are those coarse nodes, the others hang (linear / bilinear interpolation along the coarse
+// face). A = P^T (sum over leaf cells) P, b = P^T (sum over leaf cells of int u . grad N).
+//
+// Data: the coarse level as one box (a NodalSolver over the domain); the fine level on the bounding box
+// of its boxes (a second NodalSolver, sigma zero outside the fine cells, its overset mask holding every
+// node but the fine unknowns). Solver: FP64 composite residual (fine residual with the interface values
+// filled from the coarse level, coarse residual with sigma zero on covered cells, plus the fine interface
+// residuals restricted to their coarse nodes), then one two-level correction per step: coarse V-cycles
+// on the restricted composite residual (prolonged trilinearly to the fine unknowns), a fresh fine
+// residual, fine V-cycles on the fine unknowns with the interface held.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "incflo_gb300.h"
+#include "nodal_solver.h"
+
+namespace gbp {
+
+struct AmrBox {
+    int lo[3], hi[3];  // fine cells, inclusive, in the fine index space of the whole domain
+};
+
+struct AmrFields {
+    gbp_array4* vel_c;
+    const gbp_array4* vel_old_c;
+    const gbp_array4* rho_c;
+    gbp_array4* gp_c;
+    gbp_array4* p_c;
+    gbp_array4* const* vel_f;       // nbox entries each; NULL arrays allowed where optional
+    const gbp_array4* const* vel_old_f;
+    const gbp_array4* const* rho_f;
+    gbp_array4* const* gp_f;
+    gbp_array4* const* p_f;
+    double rho0, scale;
+    int incremental;
+};
+
+class CompositeNodal {
+public:
+    int init(const gbp_geometry& coarse, const int bc_lo[3], const int bc_hi[3], const int* boxes, int nbox,
+             const gbp_options& opt, cudaStream_t stream);
+    ~CompositeNodal();
+    int project(const AmrFields& f, gbp_stats* stats);
+    size_t device_bytes() const;
+    int set_options(const gbp_options& o);
+
+private:
+    int check_fields(const AmrFields& f);
+    void composite_residual(const double* bc, const double* bf, unsigned long long* norm);
+    void sync(double* vc, const double* vf);
+
+    gbp_options opt{};
+    cudaStream_t st = nullptr;
+    gbp_geometry geom_c{};
+    int bclo[3] = {}, bchi[3] = {};
+    std::vector<AmrBox> boxes;
+    int off[3] = {};   // fine bounding box origin (fine cells)
+    int nfb[3] = {};   // fine bounding box extent (fine cells)
+    NodalSolver crs, fin;
+    NodalGeom gc{}, gf{}, gf_nomask{};
+    bool singular = false;
+    DevicePool pool;
+    unsigned char *cmask_c = nullptr, *cmask_f = nullptr, *ccls = nullptr, *fcls = nullptr;
+    double *sc_m = nullptr;                                       // coarse sigma, covered cells 0
+    double *phi_c = nullptr, *b_c = nullptr, *r_c = nullptr, *rc_full = nullptr, *e_c = nullptr;
+    double *phi_f = nullptr, *b_f = nullptr, *r_f = nullptr;
+    double *vel_f = nullptr, *gp_f = nullptr, *rho_f = nullptr, *velo_f = nullptr, *sig_f = nullptr;
+    double *p_fb = nullptr;                                       // fine phi on all bbox nodes 0..n
+    double *scal = nullptr, *part = nullptr;
+    int nparts = 0;
+    unsigned long long *dnorm = nullptr, *hnorm = nullptr;
+    void* dboxes = nullptr;  // device table for the batched box kernels
+    size_t dboxes_bytes = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+}  // namespace gbp

@@ -188,37 +188,115 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, doubl
     atomicMax(dst, bits);
 }
 
+// |v| as an order-preserving integer key: for non-negative doubles the IEEE bit pattern orders like
+// the value and every NaN pattern (sign cleared) lies above +inf, so an integer max over keys is a
+// NaN-propagating max of |v| that costs no FP64 instruction.
+__device__ __forceinline__ unsigned long long abs_key(double v)
+{
+    return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ double key_value(unsigned long long k)
+{
+    return k > 0x7ff0000000000000ull ? __longlong_as_double(0x7ff8000000000000ll) : __longlong_as_double((long long)k);
+}
+
+// 1/x by Newton's iteration r <- r + r (1 - x r) from the single-precision reciprocal: each step
+// doubles the correct bits (24 -> 48 -> the double's 53), within an ulp or two of the correctly
+// rounded quotient, in 4 FP64 instructions instead of a full IEEE division. Outside the float range
+// the IEEE division is used.
+__device__ __forceinline__ double recip_newton(double x)
+{
+    const double ax = fabs(x);
+    if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
+    double r = (double)__frcp_rn((float)x);
+    r = fma(r, fma(-x, r, 1.0), r);
+    r = fma(r, fma(-x, r, 1.0), r);
+    return r;
+}
+
+// Warp reductions over the lanes that exist: a block whose size is not a multiple of 32 has a
+// partial last warp, whose missing lanes must neither be named in the shuffle mask nor read.
+// Results are valid in lane 0; the order of the additions is fixed (deterministic).
+__device__ __forceinline__ unsigned lanes_mask(int nl) { return nl >= 32 ? 0xffffffffu : ((1u << nl) - 1u); }
+__device__ __forceinline__ double warp_sum0(double v, int lane, int nl)
+{
+    const unsigned m = lanes_mask(nl);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_down_sync(m, v, o);
+        if (lane + o < nl) v += w;
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_max0(double v, int lane, int nl)
+{
+    const unsigned m = lanes_mask(nl);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_down_sync(m, v, o);
+        if (lane + o < nl) v = nanmax(v, w);
+    }
+    return v;
+}
+
 __device__ __forceinline__ double block_max(double v)
 {
     __shared__ double red[32];
-    for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    const int nw = (nt + 31) >> 5;
     const int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int lane = lin & 31, wid = lin >> 5;
+    v = warp_max0(v, lane, min(32, nt - (wid << 5)));
     __syncthreads();
     if (lane == 0) red[wid] = v;
     __syncthreads();
     if (wid == 0) {
         v = lane < nw ? red[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        v = warp_max0(v, lane, min(32, nt));
     }
     return v;  // valid in thread 0
 }
 
-// Deterministic block sum (fixed shuffle tree), the result valid in every thread.
+// block max of integer keys (valid in thread 0), partial warps allowed
+__device__ __forceinline__ unsigned long long block_max_key(unsigned long long v)
+{
+    __shared__ unsigned long long redk[32];
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    const int nw = (nt + 31) >> 5;
+    const int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = lin & 31, wid = lin >> 5;
+    int nl = min(32, nt - (wid << 5));
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(lanes_mask(nl), v, o);
+        if (lane + o < nl && w > v) v = w;
+    }
+    __syncthreads();
+    if (lane == 0) redk[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < nw ? redk[lane] : 0ull;
+        nl = min(32, nt);
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_down_sync(lanes_mask(nl), v, o);
+            if (lane + o < nl && w > v) v = w;
+        }
+    }
+    return v;
+}
+
+// Deterministic block sum (fixed reduction tree), the result valid in every thread.
 __device__ __forceinline__ double block_sum_all(double v)
 {
     __shared__ double red[33];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+    const int nw = (nt + 31) >> 5;
     const int lin = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int lane = lin & 31, wid = lin >> 5;
+    v = warp_sum0(v, lane, min(32, nt - (wid << 5)));
     __syncthreads();
     if (lane == 0) red[wid] = v;
     __syncthreads();
     if (wid == 0) {
         double t = lane < nw ? red[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        t = warp_sum0(t, lane, min(32, nt));
         if (lane == 0) red[32] = t;
     }
     __syncthreads();

@@ -17,6 +17,7 @@
 
 #include "gbp_internal.cuh"
 #include "nodal_kernels.h"
+#include "nodal_sweep.h"
 
 namespace gbp {
 
@@ -543,34 +544,47 @@ __device__ __forceinline__ double* a4p(const gbp_array4& a, int i, int j, int k,
            (long long)(k - a.lo[2]) * a.kstride + (long long)n * a.nstride;
 }
 
-__global__ void k_sigma_from_rho(NodalGeom g, gbp_array4 rho, int have_rho, double scale, double rho0,
-                                 double* __restrict__ s64, float* __restrict__ s32)
+// cells away from a periodic seam have no alias: one store
+__device__ __forceinline__ bool cell_alias_free(const NodalGeom& g, int i, int j, int k)
 {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long nxy = (long long)g.n[0] * g.n[1];
-    if (t >= nxy * g.n[2]) return;
-    const int k = (int)(t / nxy);
-    const long long rem = t - (long long)k * nxy;
-    const int j = (int)(rem / g.n[0]);
-    const int i = (int)(rem - (long long)j * g.n[0]);
-    const double v = have_rho ? scale / a4(rho, i, j, k, 0) : scale / rho0;
-    store_sigma_cell(s64, g, i, j, k, v);
-    if (s32) store_sigma_cell(s32, g, i, j, k, (float)v);
+    return !((g.per[0] && (i == 0 || i == g.n[0] - 1)) || (g.per[1] && (j == 0 || j == g.n[1] - 1)) ||
+             (g.per[2] && (k == 0 || k == g.n[2] - 1)));
 }
 
-__global__ void k_sigma_copy(NodalGeom g, gbp_array4 sig, int have_sig, double cval, double* __restrict__ s64,
-                             float* __restrict__ s32)
+template <typename T>
+__device__ __forceinline__ void put_sigma_cell(T* a, const NodalGeom& g, int i, int j, int k, T v)
 {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long nxy = (long long)g.n[0] * g.n[1];
-    if (t >= nxy * g.n[2]) return;
-    const int k = (int)(t / nxy);
-    const long long rem = t - (long long)k * nxy;
-    const int j = (int)(rem / g.n[0]);
-    const int i = (int)(rem - (long long)j * g.n[0]);
+    if (cell_alias_free(g, i, j, k))
+        a[pidx(g.sy, g.sz, i, j, k)] = v;
+    else
+        store_sigma_cell(a, g, i, j, k, v);
+}
+
+// 3-D launch over the cells (block 32 x 4 x 2): no index division
+__global__ void __launch_bounds__(256) k_sigma_from_rho(NodalGeom g, gbp_array4 rho, int have_rho, double scale,
+                                                        double rho0, double* __restrict__ s64, float* __restrict__ s32)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= g.n[0] || j >= g.n[1] || k >= g.n[2]) return;
+    // sigma = s / rho with a Newton reciprocal: the IEEE FP64 division would bound this kernel by the
+    // FP64 pipe
+    const double v = have_rho ? scale * recip_newton(a4(rho, i, j, k, 0)) : scale / rho0;
+    put_sigma_cell(s64, g, i, j, k, v);
+    if (s32) put_sigma_cell(s32, g, i, j, k, (float)v);
+}
+
+__global__ void __launch_bounds__(256) k_sigma_copy(NodalGeom g, gbp_array4 sig, int have_sig, double cval,
+                                                    double* __restrict__ s64, float* __restrict__ s32)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= g.n[0] || j >= g.n[1] || k >= g.n[2]) return;
     const double v = have_sig ? a4(sig, i, j, k, 0) : cval;
-    store_sigma_cell(s64, g, i, j, k, v);
-    if (s32) store_sigma_cell(s32, g, i, j, k, (float)v);
+    put_sigma_cell(s64, g, i, j, k, v);
+    if (s32) put_sigma_cell(s32, g, i, j, k, (float)v);
 }
 
 __global__ void k_sigma_coarsen(NodalGeom gf, NodalGeom gc, const double* __restrict__ sf,
@@ -592,85 +606,129 @@ __global__ void k_sigma_coarsen(NodalGeom gf, NodalGeom gc, const double* __rest
     if (sc32) store_sigma_cell(sc32, gc, i, j, k, (float)v);
 }
 
-// g = -(weak divergence) of u' = u + (add_gp ? sigma*gp : 0) - (sub_old ? u_old : 0).
-// A CTA covers a 32x4x4 box of nodes. Its 33x5x5 surrounding cells are read once (coalesced along
-// x) into shared memory as the per-cell weak fluxes F_d = (h_e h_f / 4) u'_d; every node then sums
-// +-F over its 8 cells. Ghost cells carry F only across an inflow face, and only the normal
-// component (the inflow velocity); every other ghost carries 0 (the wall / outflow case).
-// part: per-block sums of g for the consistency correction of singular systems.
-constexpr int RX = 32, RY = 4, RZ = 4;
-__global__ void __launch_bounds__(RX* RY* RZ) k_nodal_rhs(NodalGeom g, RhsArgs a, const double* __restrict__ s64,
-                                                          double* __restrict__ b, double* __restrict__ part)
+// Tiles of the z-marching FP64 kernels: a CTA of 33 x 9 threads covers 32 x 8 node columns; thread
+// (tx, ty) owns cell column and node column (x0 - 1 + tx, y0 - 1 + ty) (a cell is named by its low
+// node), the threads with tx, ty >= 1 own nodes, and the CTA walks a z range one layer at a time.
+constexpr int ZX = 32, ZY = 8, ZTX = ZX + 1, ZTY = ZY + 1;
+
+// z chunk length for a bx x by tile grid over nz planes: about 4 waves of CTAs
+static int zchunk(int bx, int by, int nz)
 {
-    __shared__ double F[3][RZ + 1][RY + 1][RX + 1];
-    const int x0 = blockIdx.x * RX, y0 = blockIdx.y * RY, z0 = blockIdx.z * RZ;
-    const int tid = threadIdx.x + RX * (threadIdx.y + RY * threadIdx.z);
-    constexpr int NC = (RX + 1) * (RY + 1) * (RZ + 1);
-    for (int q = tid; q < NC; q += RX * RY * RZ) {
-        const int cx = q % (RX + 1), cy = (q / (RX + 1)) % (RY + 1), cz = q / ((RX + 1) * (RY + 1));
-        int cell[3] = {x0 - 1 + cx, y0 - 1 + cy, z0 - 1 + cz};
-        int nout = 0, dout = -1;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            int ci = cell[d];
-            if (g.per[d]) {
-                if (ci < 0) ci += g.n[d];
-                if (ci >= g.n[d]) ci -= g.n[d];
-            } else if (ci < 0 || ci >= g.n[d]) {
-                ++nout;
-                dout = d;
-            }
-            cell[d] = ci;
-        }
-        double f[3] = {0.0, 0.0, 0.0};
-        if (nout == 0 && cell[0] < g.n[0] + 1 && cell[1] < g.n[1] + 1 && cell[2] < g.n[2] + 1) {
-            const long long off = (long long)(cell[0] - a.vel.lo[0]) + (long long)(cell[1] - a.vel.lo[1]) * a.vel.jstride +
-                                  (long long)(cell[2] - a.vel.lo[2]) * a.vel.kstride;
-            const double sg = a.add_gp ? s64[pidx(g.sy, g.sz, cell[0], cell[1], cell[2])] : 0.0;
-            long long og = 0, oo = 0;
-            if (a.add_gp)
-                og = (long long)(cell[0] - a.gp.lo[0]) + (long long)(cell[1] - a.gp.lo[1]) * a.gp.jstride +
-                     (long long)(cell[2] - a.gp.lo[2]) * a.gp.kstride;
-            if (a.sub_old)
-                oo = (long long)(cell[0] - a.vel_old.lo[0]) + (long long)(cell[1] - a.vel_old.lo[1]) * a.vel_old.jstride +
-                     (long long)(cell[2] - a.vel_old.lo[2]) * a.vel_old.kstride;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                double u = a.vel.data[off + d * a.vel.nstride];
-                if (a.add_gp) u = fma(a.gp.data[og + d * a.gp.nstride], sg, u);
-                if (a.sub_old) u -= a.vel_old.data[oo + d * a.vel_old.nstride];
-                f[d] = a.cf[d] * u;
-            }
-        } else if (nout == 1) {
-            const int inflow = cell[dout] < 0 ? a.inflow_lo[dout] : a.inflow_hi[dout];
-            if (inflow) f[dout] = a.cf[dout] * a4(a.vel, cell[0], cell[1], cell[2], dout);
-        }
-        F[0][cz][cy][cx] = f[0];
-        F[1][cz][cy][cx] = f[1];
-        F[2][cz][cy][cx] = f[2];
+    const int want = std::max(1, 4 * sm_count_cached() * 6 / std::max(1, bx * by));
+    return std::max(4, (nz + want - 1) / want);
+}
+
+// g = -(weak divergence) of u' = u + (add_gp ? sigma*gp : 0) - (sub_old ? u_old : 0), for the nodes.
+// Each cell of a layer computes its weak fluxes F_d = (h_e h_f / 4) u'_d once (ghost cells carry F
+// only across an inflow face, and only the normal component; other ghosts carry 0); a node sums +-F
+// over its 8 cells in separable form: per layer the x difference of y-pair sums of F_x, the y
+// difference of x-pair sums of F_y and the 4-cell sum of F_z, then layers k-1 and k.
+// part: per-CTA sums of g (consistency correction of singular systems).
+__global__ void __launch_bounds__(ZTX* ZTY) k_nodal_rhs(NodalGeom g, RhsArgs a, const double* __restrict__ s64,
+                                                        double* __restrict__ b, double* __restrict__ part, int kchunk)
+{
+    __shared__ double F[2][3][ZTY][ZTX];
+    const int tx = threadIdx.x % ZTX, ty = threadIdx.x / ZTX;
+    const int ci = blockIdx.x * ZX - 1 + tx, cj = blockIdx.y * ZY - 1 + ty;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(kbeg + kchunk, g.nu[2]);
+    const bool owner = tx >= 1 && ty >= 1 && ci < g.nu[0] && cj < g.nu[1];
+    // cells beyond the last node column are never read by an owner
+    const bool used = ci < g.nu[0] && cj < g.nu[1];
+    // x / y part of this cell column: periodic wrap, or out of the domain (ghost)
+    int c0 = ci, c1 = cj, nout_xy = 0, dout_xy = -1;
+    if (g.per[0]) {
+        if (c0 < 0) c0 += g.n[0];
+        if (c0 >= g.n[0]) c0 -= g.n[0];
+    } else if (c0 < 0 || c0 >= g.n[0]) {
+        ++nout_xy;
+        dout_xy = 0;
     }
-    __syncthreads();
-    const int tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
-    const int i = x0 + tx, j = y0 + ty, k = z0 + tz;
-    double gv = 0.0;
-    if (i < g.nu[0] && j < g.nu[1] && k < g.nu[2]) {
-        if (!node_is_dirichlet(g, i, j, k)) {
-            double dx = 0.0, dy = 0.0, dz = 0.0;
-#pragma unroll
-            for (int c = 0; c < 2; ++c)
-#pragma unroll
-                for (int bq = 0; bq < 2; ++bq) {
-                    dx += F[0][tz + c][ty + bq][tx + 1] - F[0][tz + c][ty + bq][tx];
-                    dy += F[1][tz + c][ty + 1][tx + bq] - F[1][tz + c][ty][tx + bq];
-                    dz += F[2][tz + 1][ty + c][tx + bq] - F[2][tz][ty + c][tx + bq];
+    if (g.per[1]) {
+        if (c1 < 0) c1 += g.n[1];
+        if (c1 >= g.n[1]) c1 -= g.n[1];
+    } else if (c1 < 0 || c1 >= g.n[1]) {
+        ++nout_xy;
+        dout_xy = 1;
+    }
+    double A0p = 0.0, A1p = 0.0, Q2p = 0.0, acc = 0.0;
+    for (int L = kbeg - 1; L < kend; ++L) {
+        const int buf = (L - kbeg + 1) & 1;
+        double f0 = 0.0, f1 = 0.0, f2 = 0.0;
+        if (used) {
+            int c2 = L, nout = nout_xy, dout = dout_xy;
+            if (g.per[2]) {
+                if (c2 < 0) c2 += g.n[2];
+                if (c2 >= g.n[2]) c2 -= g.n[2];
+            } else if (c2 < 0 || c2 >= g.n[2]) {
+                ++nout;
+                dout = 2;
+            }
+            if (nout == 0 && a.cmask && !a.cmask[pidx(g.sy, g.sz, c0, c1, c2)]) {
+                // not a leaf cell of this level: no flux
+            } else if (nout == 0) {
+                const long long off = (long long)(c0 - a.vel.lo[0]) + (long long)(c1 - a.vel.lo[1]) * a.vel.jstride +
+                                      (long long)(c2 - a.vel.lo[2]) * a.vel.kstride;
+                double u0 = a.vel.data[off], u1 = a.vel.data[off + a.vel.nstride],
+                       u2 = a.vel.data[off + 2 * a.vel.nstride];
+                if (a.add_gp) {
+                    const double sg = s64[pidx(g.sy, g.sz, c0, c1, c2)];
+                    const long long og = (long long)(c0 - a.gp.lo[0]) + (long long)(c1 - a.gp.lo[1]) * a.gp.jstride +
+                                         (long long)(c2 - a.gp.lo[2]) * a.gp.kstride;
+                    u0 = fma(a.gp.data[og], sg, u0);
+                    u1 = fma(a.gp.data[og + a.gp.nstride], sg, u1);
+                    u2 = fma(a.gp.data[og + 2 * a.gp.nstride], sg, u2);
                 }
-            gv = -((dx + dy) + dz);
+                if (a.sub_old) {
+                    const long long oo = (long long)(c0 - a.vel_old.lo[0]) +
+                                         (long long)(c1 - a.vel_old.lo[1]) * a.vel_old.jstride +
+                                         (long long)(c2 - a.vel_old.lo[2]) * a.vel_old.kstride;
+                    u0 -= a.vel_old.data[oo];
+                    u1 -= a.vel_old.data[oo + a.vel_old.nstride];
+                    u2 -= a.vel_old.data[oo + 2 * a.vel_old.nstride];
+                }
+                f0 = a.cf[0] * u0;
+                f1 = a.cf[1] * u1;
+                f2 = a.cf[2] * u2;
+            } else if (nout == 1) {
+                // the ghost cell across one face: its raw (unwrapped) index in that direction
+                int q[3] = {c0, c1, c2};
+                q[dout] = dout == 0 ? ci : (dout == 1 ? cj : L);
+                const int inflow = q[dout] < 0 ? a.inflow_lo[dout] : a.inflow_hi[dout];
+                if (inflow) {
+                    const double fv = a.cf[dout] * a4(a.vel, q[0], q[1], q[2], dout);
+                    if (dout == 0) f0 = fv;
+                    else if (dout == 1) f1 = fv;
+                    else f2 = fv;
+                }
+            }
         }
-        b[pidx(g.sy, g.sz, i, j, k)] = gv;
+        F[buf][0][ty][tx] = f0;
+        F[buf][1][ty][tx] = f1;
+        F[buf][2][ty][tx] = f2;
+        __syncthreads();
+        if (owner) {
+            const double(*F0)[ZTX] = F[buf][0];
+            const double(*F1)[ZTX] = F[buf][1];
+            const double(*F2)[ZTX] = F[buf][2];
+            const double A0 = (F0[ty - 1][tx] + F0[ty][tx]) - (F0[ty - 1][tx - 1] + F0[ty][tx - 1]);
+            const double A1 = (F1[ty][tx - 1] + F1[ty][tx]) - (F1[ty - 1][tx - 1] + F1[ty - 1][tx]);
+            const double Q2 = (F2[ty - 1][tx - 1] + F2[ty - 1][tx]) + (F2[ty][tx - 1] + F2[ty][tx]);
+            if (L >= kbeg) {
+                // node (ci, cj, L): layers L-1 and L
+                double gv = 0.0;
+                if (!node_is_dirichlet(g, ci, cj, L)) gv = -(((A0p + A0) + (A1p + A1)) + (Q2 - Q2p));
+                b[pidx(g.sy, g.sz, ci, cj, L)] = gv;
+                acc += gv;
+            }
+            A0p = A0;
+            A1p = A1;
+            Q2p = Q2;
+        }
     }
     if (part) {
-        const double t = block_sum_all(gv);
-        if (tid == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = t;
+        const double t = block_sum_all(acc);
+        if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = t;
     }
 }
 
@@ -689,18 +747,21 @@ __global__ void __launch_bounds__(256) k_node_norm(NodalGeom g, const double* __
 }
 
 // Per-block partial sums (weighted: sum V_i v_i), grid-stride over the unique nodes.
+// Tiled launches over the unique nodes without index division: block (32, 8), each thread walks
+// a z chunk of its node column.
 __global__ void __launch_bounds__(256) k_node_sums(NodalGeom g, const double* __restrict__ v, int weighted,
-                                                   double* __restrict__ part)
+                                                   double* __restrict__ part, int kchunk)
 {
+    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    const int kbeg = blockIdx.z * kchunk, kend = min(kbeg + kchunk, g.nu[2]);
     double acc = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        if (!decode_node(g, t, i, j, k)) break;
-        const double x = v[pidx(g.sy, g.sz, i, j, k)];
-        acc += weighted ? x * node_volume(g, i, j, k) : x;
-    }
+    if (i < g.nu[0] && j < g.nu[1])
+        for (int k = kbeg; k < kend; ++k) {
+            const double x = v[pidx(g.sy, g.sz, i, j, k)];
+            acc += weighted ? x * node_volume(g, i, j, k) : x;
+        }
     acc = block_sum_all(acc);
-    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+    if (threadIdx.x == 0 && threadIdx.y == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = acc;
 }
 
 // One block folds the partials in a fixed order: scal = sum / vtot.
@@ -717,25 +778,34 @@ __global__ void __launch_bounds__(1024) k_fold(const double* __restrict__ part, 
 //         max norm of the corrected b into *norm
 // mode 1: x_i -= c (gauge: volume-weighted mean zero), with periodic aliases
 __global__ void __launch_bounds__(256) k_remove_mean(NodalGeom g, double* __restrict__ v, const double* __restrict__ scal,
-                                                     int mode, unsigned long long* norm)
+                                                     int mode, unsigned long long* norm, int kchunk)
 {
     const double c = *scal;
-    double nv = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        if (!decode_node(g, t, i, j, k)) break;
-        const long long p = pidx(g.sy, g.sz, i, j, k);
-        if (mode == 0) {
-            const double bv = v[p] - c * node_volume(g, i, j, k);
-            v[p] = bv;
-            nv = nanmax(nv, fabs(bv) * node_inv_volume(g, i, j, k));
-        } else {
-            store_node(v, g, i, j, k, v[p] - c);
+    const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+    const int kbeg = blockIdx.z * kchunk, kend = min(kbeg + kchunk, g.nu[2]);
+    // node volume = V / 2^(boundary count): the x / y part is fixed along the column; the norm keeps
+    // the max of |b| 2^e as an integer key and multiplies by 1/V once (FP64 instructions are the
+    // bound of this kernel on GB300)
+    const int exy = (!g.per[0] && (i == 0 || i == g.n[0])) + (!g.per[1] && (j == 0 || j == g.n[1]));
+    const double cv = c * (exy == 0 ? g.vol : (exy == 1 ? 0.5 * g.vol : 0.25 * g.vol));
+    const double cvz = 0.5 * cv;  // on a z boundary plane
+    unsigned long long key = 0;
+    if (i < g.nu[0] && j < g.nu[1])
+        for (int k = kbeg; k < kend; ++k) {
+            const long long p = pidx(g.sy, g.sz, i, j, k);
+            if (mode == 0) {
+                const int e = exy + (!g.per[2] && (k == 0 || k == g.n[2]));
+                const double bv = v[p] - (e == exy ? cv : cvz);
+                v[p] = bv;
+                const unsigned long long kb = e == 0 ? abs_key(bv) : abs_key(bv * (double)(1 << e));
+                key = kb > key ? kb : key;
+            } else {
+                store_node(v, g, i, j, k, v[p] - c);
+            }
         }
-    }
     if (mode == 0 && norm) {
-        nv = block_max(nv);
-        if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+        key = block_max_key(key);
+        if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(norm, key_value(key) * g.ivol);
     }
 }
 
@@ -758,48 +828,72 @@ __global__ void __launch_bounds__(256) k_to_f32(NodalGeom g, const double* __res
     r32[p] = (float)(r[p] * scale);
 }
 
-// u <- u + (add_gp ? sigma*gp : 0) - sigma*G phi; gradphi <- G phi; gp <- G phi (+= if incremental)
-__global__ void __launch_bounds__(256) k_nodal_correct(NodalGeom g, CorrArgs a, const double* __restrict__ s64,
-                                                       const double* __restrict__ phi)
+// u <- u + (add_gp ? sigma*gp : 0) - sigma*G phi; gradphi <- G phi; gp <- G phi (+= if incremental).
+// z-marching tile (33 x 9 node columns for 32 x 8 cell columns): each node column forms the z-pair sum
+// S and difference D of its two planes once; a cell's gradient is then
+//   4h G_x = (S10 + S11) - (S00 + S01), 4h G_y = (S01 + S11) - (S00 + S10), 4h G_z = (D00 + D10) + (D01 + D11)
+// (Sab = node column (i+a, j+b)), 9 additions instead of 21.
+__global__ void __launch_bounds__(ZTX* ZTY) k_nodal_correct(NodalGeom g, CorrArgs a, const double* __restrict__ s64,
+                                                            const double* __restrict__ phi, int kchunk)
 {
-    // 3-D launch over the cells (block 32 x 4 x 2): no index division
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    if (i >= g.n[0] || j >= g.n[1] || k >= g.n[2]) return;
-    const long long c = pidx(g.sy, g.sz, i, j, k);
-    const long long sy = g.sy, sz = g.sz;
-    const double p000 = phi[c], p100 = phi[c + 1], p010 = phi[c + sy], p110 = phi[c + 1 + sy];
-    const double p001 = phi[c + sz], p101 = phi[c + 1 + sz], p011 = phi[c + sy + sz], p111 = phi[c + 1 + sy + sz];
-    double G[3];
-    G[0] = ((p100 - p000) + (p110 - p010) + (p101 - p001) + (p111 - p011)) * a.inv4h[0];
-    G[1] = ((p010 - p000) + (p110 - p100) + (p011 - p001) + (p111 - p101)) * a.inv4h[1];
-    G[2] = ((p001 - p000) + (p101 - p100) + (p011 - p010) + (p111 - p110)) * a.inv4h[2];
-    const double sg = s64[c];
+    __shared__ double S[2][ZTY][ZTX], D[2][ZTY][ZTX];
+    const int tx = threadIdx.x % ZTX, ty = threadIdx.x / ZTX;
+    const int ni = blockIdx.x * ZX + tx, nj = blockIdx.y * ZY + ty;  // node column; cell column = same
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(kbeg + kchunk, g.n[2]);
+    // node columns 0..n (index n: the periodic alias or the high boundary node)
+    const bool has_node = ni <= g.n[0] && nj <= g.n[1];
+    const bool cell = tx < ZX && ty < ZY && ni < g.n[0] && nj < g.n[1];
+    const long long pc = pidx(g.sy, g.sz, ni, nj, kbeg);
+    double plo = has_node ? phi[pc] : 0.0;
+    for (int k = kbeg; k < kend; ++k) {
+        const int buf = (k - kbeg) & 1;
+        const long long pk = pc + (long long)(k - kbeg) * g.sz;
+        const double phi_hi = has_node ? phi[pk + g.sz] : 0.0;
+        S[buf][ty][tx] = plo + phi_hi;
+        D[buf][ty][tx] = phi_hi - plo;
+        plo = phi_hi;
+        __syncthreads();
+        if (cell) {
+            const double S00 = S[buf][ty][tx], S10 = S[buf][ty][tx + 1], S01 = S[buf][ty + 1][tx],
+                         S11 = S[buf][ty + 1][tx + 1];
+            const double D00 = D[buf][ty][tx], D10 = D[buf][ty][tx + 1], D01 = D[buf][ty + 1][tx],
+                         D11 = D[buf][ty + 1][tx + 1];
+            double G[3];
+            G[0] = ((S10 + S11) - (S00 + S01)) * a.inv4h[0];
+            G[1] = ((S01 + S11) - (S00 + S10)) * a.inv4h[1];
+            G[2] = ((D00 + D10) + (D01 + D11)) * a.inv4h[2];
+            const double sg = s64[pk];
+            const long long ov = (long long)(ni - a.vel.lo[0]) + (long long)(nj - a.vel.lo[1]) * a.vel.jstride +
+                                 (long long)(k - a.vel.lo[2]) * a.vel.kstride;
+            long long og = 0;
+            if (a.gp.data)
+                og = (long long)(ni - a.gp.lo[0]) + (long long)(nj - a.gp.lo[1]) * a.gp.jstride +
+                     (long long)(k - a.gp.lo[2]) * a.gp.kstride;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        double* up = a4p(a.vel, i, j, k, d);
-        double u = *up;
-        double gpo = 0.0;
-        if (a.gp.data) gpo = a4(a.gp, i, j, k, d);
-        if (a.add_gp) u += gpo * sg;
-        *up = u - sg * G[d];
-        if (a.gradphi.data) *a4p(a.gradphi, i, j, k, d) = G[d];
-        if (a.gp.data) *a4p(a.gp, i, j, k, d) = a.incremental ? gpo + G[d] : G[d];
+            for (int d = 0; d < 3; ++d) {
+                double* up = a.vel.data + ov + d * a.vel.nstride;
+                double u = *up;
+                double gpo = 0.0;
+                if (a.gp.data) gpo = a.gp.data[og + d * a.gp.nstride];
+                if (a.add_gp) u = fma(gpo, sg, u);
+                *up = fma(-sg, G[d], u);
+                if (a.gradphi.data) *a4p(a.gradphi, ni, nj, k, d) = G[d];
+                if (a.gp.data) a.gp.data[og + d * a.gp.nstride] = a.incremental ? gpo + G[d] : G[d];
+            }
+        }
     }
 }
 
 // p_nd (nodal, all nodes 0..n) <- phi (+= if incremental)
-__global__ void k_nodal_store_phi(NodalGeom g, gbp_array4 out, const double* __restrict__ phi, int accumulate)
+__global__ void __launch_bounds__(256) k_nodal_store_phi(NodalGeom g, gbp_array4 out, const double* __restrict__ phi,
+                                                         int accumulate)
 {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const int n0 = g.n[0] + 1, n1 = g.n[1] + 1, n2 = g.n[2] + 1;
-    const long long nxy = (long long)n0 * n1;
-    if (t >= nxy * n2) return;
-    const int k = (int)(t / nxy);
-    const long long rem = t - (long long)k * nxy;
-    const int j = (int)(rem / n0);
-    const int i = (int)(rem - (long long)j * n0);
+    // 3-D launch over all nodes 0..n (block 32 x 4 x 2)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > g.n[0] || j > g.n[1] || k > g.n[2]) return;
     const double v = phi[pidx(g.sy, g.sz, i, j, k)];
     double* p = a4p(out, i, j, k, 0);
     *p = accumulate ? *p + v : v;
@@ -863,6 +957,10 @@ static inline long long nunique(const NodalGeom& g) { return (long long)g.nu[0] 
 static inline long long ncells(const NodalGeom& g) { return (long long)g.n[0] * g.n[1] * g.n[2]; }
 
 static const dim3 kBlock3(32, 4, 2);
+static inline dim3 grid3c(const NodalGeom& g)
+{
+    return dim3((g.n[0] + 31) / 32, (g.n[1] + 3) / 4, (g.n[2] + 1) / 2);
+}
 static inline dim3 grid3(const NodalGeom& g)
 {
     return dim3((g.nu[0] + 31) / 32, (g.nu[1] + 3) / 4, (g.nu[2] + 1) / 2);
@@ -932,7 +1030,7 @@ void nodal_sigma_from_rho(const NodalGeom& g, const gbp_array4* rho, double scal
 {
     gbp_array4 r{};
     if (rho) r = *rho;
-    k_sigma_from_rho<<<nblocks(ncells(g), 256), 256, 0, st>>>(g, r, rho != nullptr, scale, rho0, s64, s32);
+    k_sigma_from_rho<<<grid3c(g), kBlock3, 0, st>>>(g, r, rho != nullptr, scale, rho0, s64, s32);
 }
 
 void nodal_sigma_copy(const NodalGeom& g, const gbp_array4* sig, double cval, double* s64, float* s32,
@@ -940,7 +1038,7 @@ void nodal_sigma_copy(const NodalGeom& g, const gbp_array4* sig, double cval, do
 {
     gbp_array4 r{};
     if (sig) r = *sig;
-    k_sigma_copy<<<nblocks(ncells(g), 256), 256, 0, st>>>(g, r, sig != nullptr, cval, s64, s32);
+    k_sigma_copy<<<grid3c(g), kBlock3, 0, st>>>(g, r, sig != nullptr, cval, s64, s32);
 }
 
 void nodal_sigma_coarsen(const NodalGeom& gf, const NodalGeom& gc, const double* sf, double* sc64, float* sc32,
@@ -949,15 +1047,35 @@ void nodal_sigma_coarsen(const NodalGeom& gf, const NodalGeom& gc, const double*
     k_sigma_coarsen<<<nblocks(ncells(gc), 256), 256, 0, st>>>(gf, gc, sf, sc64, sc32);
 }
 
+static dim3 rhs_grid(const NodalGeom& g, int& kchunk)
+{
+    const int bx = (g.nu[0] + ZX - 1) / ZX, by = (g.nu[1] + ZY - 1) / ZY;
+    kchunk = zchunk(bx, by, g.nu[2]);
+    return dim3(bx, by, (g.nu[2] + kchunk - 1) / kchunk);
+}
+
 void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, double* part, cudaStream_t st)
 {
-    dim3 grid((g.nu[0] + RX - 1) / RX, (g.nu[1] + RY - 1) / RY, (g.nu[2] + RZ - 1) / RZ);
-    k_nodal_rhs<<<grid, dim3(RX, RY, RZ), 0, st>>>(g, a, s64, b, part);
+    int kchunk;
+    const dim3 grid = rhs_grid(g, kchunk);
+    k_nodal_rhs<<<grid, ZTX * ZTY, 0, st>>>(g, a, s64, b, part, kchunk);
 }
 
 int nodal_rhs_partials(const NodalGeom& g)
 {
-    return ((g.nu[0] + RX - 1) / RX) * ((g.nu[1] + RY - 1) / RY) * ((g.nu[2] + RZ - 1) / RZ);
+    int kchunk;
+    const dim3 grid = rhs_grid(g, kchunk);
+    return (int)(grid.x * grid.y * grid.z);
+}
+
+// node-column launches (block 32 x 8, z chunks) with at most `cap` blocks
+static dim3 column_grid(const NodalGeom& g, int cap, int& kchunk)
+{
+    const int bx = (g.nu[0] + 31) / 32, by = (g.nu[1] + 7) / 8;
+    int gz = std::max(1, std::min(cap / std::max(1, bx * by), (g.nu[2] + 7) / 8));
+    kchunk = (g.nu[2] + gz - 1) / gz;
+    gz = (g.nu[2] + kchunk - 1) / kchunk;
+    return dim3(bx, by, gz);
 }
 
 static inline unsigned stride_blocks(long long n) { return (unsigned)std::min<long long>(nblocks(n, 256), 1184); }
@@ -976,13 +1094,15 @@ void nodal_fold(const NodalGeom& g, const double* part, int nparts, double* scal
 void nodal_remove_mean(const NodalGeom& g, double* v, double* partials, double* scal, int mode, int have_partials,
                        int nparts, unsigned long long* norm, cudaStream_t st)
 {
+    const int cap = nodal_partials_needed(g);
+    int kchunk;
+    const dim3 grid = column_grid(g, cap, kchunk);
     if (!have_partials) {
-        const unsigned nb = stride_blocks(nunique(g));
-        k_node_sums<<<nb, 256, 0, st>>>(g, v, mode == 1, partials);
-        nparts = (int)nb;
+        k_node_sums<<<grid, dim3(32, 8), 0, st>>>(g, v, mode == 1, partials, kchunk);
+        nparts = (int)(grid.x * grid.y * grid.z);
     }
     k_fold<<<1, 1024, 0, st>>>(partials, nparts, domain_volume(g), scal);
-    k_remove_mean<<<stride_blocks(nunique(g)), 256, 0, st>>>(g, v, scal, mode, norm);
+    k_remove_mean<<<grid, dim3(32, 8), 0, st>>>(g, v, scal, mode, norm, kchunk);
 }
 
 void nodal_norm(const NodalGeom& g, const double* v, unsigned long long* norm, cudaStream_t st)
@@ -1007,13 +1127,15 @@ void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale,
 
 void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st)
 {
-    k_nodal_correct<<<dim3((g.n[0] + 31) / 32, (g.n[1] + 3) / 4, (g.n[2] + 1) / 2), kBlock3, 0, st>>>(g, a, s64, phi);
+    const int bx = (g.n[0] + ZX - 1) / ZX, by = (g.n[1] + ZY - 1) / ZY;
+    const int kchunk = zchunk(bx, by, g.n[2]);
+    k_nodal_correct<<<dim3(bx, by, (g.n[2] + kchunk - 1) / kchunk), ZTX * ZTY, 0, st>>>(g, a, s64, phi, kchunk);
 }
 
 void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* phi, int accumulate, cudaStream_t st)
 {
-    const long long n = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.n[2] + 1);
-    k_nodal_store_phi<<<nblocks(n, 256), 256, 0, st>>>(g, out, phi, accumulate);
+    k_nodal_store_phi<<<dim3((g.n[0] + 32) / 32, (g.n[1] + 4) / 4, (g.n[2] + 2) / 2), kBlock3, 0, st>>>(g, out, phi,
+                                                                                                   accumulate);
 }
 
 void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaStream_t st)

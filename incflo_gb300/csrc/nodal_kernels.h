@@ -17,6 +17,9 @@ struct RhsArgs {
     int inflow_lo[3];
     int inflow_hi[3];
     double cf[3];  // h_e h_f / 4: integral of dN/dx_d over one cell, up to sign
+    // cells that take part (padded cell layout, periodic aliases filled; nullptr = all): the leaf
+    // cells of a level in a composite (AMR) projection
+    const unsigned char* cmask;
 };
 
 // Outputs of the fused correction kernel.

@@ -34,27 +34,52 @@ __device__ __forceinline__ bool q_alias(const NodalGeom& g, int i, int j, int k)
 // wsum = sum of the 8 cells around each node; wx / wy / wz = sigma sum of the 4 cells around the edge
 // from node (i,j,k) to (i+1,j,k) / (i,j+1,k) / (i,j,k+1). Written over index ranges -1..nu so that the
 // sweep can read the edge to a node's low neighbour; padding cells are 0, periodic ones aliased.
-__global__ void k_qweights64(NodalGeom g, const double* __restrict__ s, double* __restrict__ wsum,
-                             double* __restrict__ wx, double* __restrict__ wy, double* __restrict__ wz)
+// z-marching tile (33 x 9 threads: node columns x0-1 .. x0+31, y0-1 .. y0+7 and the cell columns one
+// lower), separable sums per cell layer: Px = x pair, Q = Px + Px(j-1) (4 cells around a z edge),
+// Y = y pair; then wsum = Q(k-1) + Q(k), wz = Q(k), wx = Y(k-1) + Y(k), wy = Px(k-1) + Px(k).
+__global__ void __launch_bounds__(QTX* QTY) k_qweights64(NodalGeom g, const double* __restrict__ s,
+                                                         double* __restrict__ wsum, double* __restrict__ wx,
+                                                         double* __restrict__ wy, double* __restrict__ wz, int kchunk)
 {
-    const int ex = g.nu[0] + 1, ey = g.nu[1] + 1, ez = g.nu[2] + 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)ex * ey * ez) return;
-    const int i = (int)(t % ex) - 1;
-    const int j = (int)((t / ex) % ey) - 1;
-    const int k = (int)(t / ((long long)ex * ey)) - 1;
-    auto S = [&](int a, int b, int c) { return s[pidx(g.sy, g.sz, a, b, c)]; };
-    const long long p = pidx(g.sy, g.sz, i, j, k);
-    if (i >= 0 && j >= 0 && k >= 0) {
-        double a = 0.0;
-        for (int c = -1; c <= 0; ++c)
-            for (int b = -1; b <= 0; ++b)
-                for (int q = -1; q <= 0; ++q) a += S(i + q, j + b, k + c);
-        wsum[p] = a;
+    __shared__ double T[2][QTY + 1][QTX + 1];
+    const int tx = threadIdx.x % QTX, ty = threadIdx.x / QTX;
+    // node column of this thread: (i, j) = (x0 - 1 + tx, y0 - 1 + ty); its cells are i-1..i, j-1..j
+    const int i = blockIdx.x * QX - 1 + tx, j = blockIdx.y * QY - 1 + ty;
+    const int kbeg = blockIdx.z * kchunk - 1;  // node planes -1 .. nu-1
+    const int kend = min(kbeg + kchunk, g.nu[2]);
+    // neighbouring tiles share their edge column / row: the lower tile writes it
+    const bool node = (tx >= 1 || blockIdx.x == 0) && (ty >= 1 || blockIdx.y == 0) && i < g.nu[0] && j < g.nu[1];
+    double Qp = 0.0, Yp = 0.0, Pp = 0.0;
+    for (int L = kbeg - 1; L < kend; ++L) {
+        const int buf = (L - kbeg + 1) & 1;
+        // stage cells (x0-2 .. x0+31, y0-2 .. y0+7) of layer L: tile (tx, ty) = cell (i - 1, j - 1),
+        // plus the extra high column / row; cells below -1 are never read (zero)
+        for (int q = threadIdx.x; q < (QTX + 1) * (QTY + 1); q += QTX * QTY) {
+            const int cx = q % (QTX + 1), cy = q / (QTX + 1);
+            const int a = blockIdx.x * QX - 2 + cx, b = blockIdx.y * QY - 2 + cy;
+            double v = 0.0;
+            if (L >= -1 && a >= -1 && b >= -1 && a <= g.nu[0] - 1 && b <= g.nu[1] - 1) v = s[pidx(g.sy, g.sz, a, b, L)];
+            T[buf][cy][cx] = v;
+        }
+        __syncthreads();
+        // this node's cells in the tile: (i-1, j-1) = (tx, ty), (i, j-1) = (tx+1, ty), (i-1, j) = (tx, ty+1), (i, j) = (tx+1, ty+1)
+        const double Px = T[buf][ty + 1][tx] + T[buf][ty + 1][tx + 1];   // cells (i-1..i, j)
+        const double Pxm = T[buf][ty][tx] + T[buf][ty][tx + 1];          // cells (i-1..i, j-1)
+        const double Q = Px + Pxm;
+        const double Y = T[buf][ty][tx + 1] + T[buf][ty + 1][tx + 1];    // cells (i, j-1..j)
+        if (node && L >= kbeg) {
+            // node (i, j, L): layers L-1 (previous) and L
+            const int k = L;
+            const long long p = pidx(g.sy, g.sz, i, j, k);
+            if (i >= 0 && j >= 0 && k >= 0) wsum[p] = Qp + Q;
+            if (j >= 0 && k >= 0) wx[p] = Yp + Y;
+            if (i >= 0 && k >= 0) wy[p] = Pp + Px;
+            if (i >= 0 && j >= 0) wz[p] = Q;
+        }
+        Qp = Q;
+        Yp = Y;
+        Pp = Px;
     }
-    if (j >= 0 && k >= 0) wx[p] = S(i, j - 1, k - 1) + S(i, j, k - 1) + S(i, j - 1, k) + S(i, j, k);
-    if (i >= 0 && k >= 0) wy[p] = S(i - 1, j, k - 1) + S(i, j, k - 1) + S(i - 1, j, k) + S(i, j, k);
-    if (i >= 0 && j >= 0) wz[p] = S(i - 1, j - 1, k) + S(i, j - 1, k) + S(i - 1, j, k) + S(i, j, k);
 }
 
 template <int MODE>
@@ -80,7 +105,7 @@ __global__ void __launch_bounds__(QTX * QTY) k_qsweep64(NodalGeom g, const doubl
     auto qsum = [&](long long pp) { return (x[pp] + x[pp + 1]) + (x[pp + sy] + x[pp + sy + 1]); };
     double q_lo = inbox ? qsum(p) : 0.0;  // plane kbeg-1
     double u_lo = 0.0;                    // layer kbeg-1 sum around the node
-    double nmax = 0.0;
+    unsigned long long nkey = 0;
     double xm = 0.0, xc = 0.0, wzm = 0.0;
     if (owner) {
         xm = x[p];
@@ -120,7 +145,13 @@ __global__ void __launch_bounds__(QTX * QTY) k_qsweep64(NodalGeom g, const doubl
                         v = xc + omega * (bv - ax) * rd;
                     } else {
                         v = bv - ax;
-                        if (norm) nmax = nanmax(nmax, fabs(v) * node_inv_volume(g, i, j, k));
+                        if (norm) {
+                            // |v| / V_node as an integer key (boundary nodes: V / 2^e, exact scaling)
+                            const int e = (!g.per[0] && (i == 0 || i == g.n[0])) + (!g.per[1] && (j == 0 || j == g.n[1])) +
+                                          (!g.per[2] && (k == 0 || k == g.n[2]));
+                            const unsigned long long kb = e == 0 ? abs_key(v) : abs_key(v * (double)(1 << e));
+                            nkey = kb > nkey ? kb : nkey;
+                        }
                     }
                     wzm = wzp;
                 } else {
@@ -137,8 +168,8 @@ __global__ void __launch_bounds__(QTX * QTY) k_qsweep64(NodalGeom g, const doubl
         }
     }
     if (MODE == 1 && norm) {
-        nmax = block_max(nmax);
-        if (threadIdx.x == 0) atomic_max_nonneg(norm, nmax);
+        nkey = block_max_key(nkey);
+        if (threadIdx.x == 0) atomic_max_nonneg(norm, key_value(nkey) * g.ivol);
     }
 }
 
@@ -148,8 +179,13 @@ bool qsweep_supported(const NodalGeom& g) { return g.iso != 0; }
 
 void nodal_qweights64(const NodalGeom& g, const double* s64, const QWeights& w, cudaStream_t st)
 {
-    const long long n = (long long)(g.nu[0] + 1) * (g.nu[1] + 1) * (g.nu[2] + 1);
-    k_qweights64<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, s64, w.wsum, w.wx, w.wy, w.wz);
+    // node columns -1 .. nu-1 in tiles of 32 x 8 (tile origin x0 - 1), node planes -1 .. nu-1
+    const int bx = (g.nu[0] + QX - 1) / QX, by = (g.nu[1] + QY - 1) / QY;
+    const int nz = g.nu[2] + 1;
+    const int want = std::max(1, 4 * sm_count_cached() * 6 / std::max(1, bx * by));
+    const int kchunk = std::max(4, (nz + want - 1) / want);
+    k_qweights64<<<dim3(bx, by, (nz + kchunk - 1) / kchunk), QTX * QTY, 0, st>>>(g, s64, w.wsum, w.wx, w.wy, w.wz,
+                                                                                kchunk);
 }
 
 void nodal_qsweep64(const NodalGeom& g, int mode, const double* s64, const QWeights& w, const double* x,

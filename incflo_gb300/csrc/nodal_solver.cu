@@ -549,6 +549,23 @@ void NodalSolver::record_iteration(int m)
     step_kernels = nk - nk0;
 }
 
+void NodalSolver::apply_vcycles(const double* r, double* x, int m, double scale, cudaStream_t s)
+{
+    const NodalLevel& l0 = L[0];
+    cap_or_st = s;
+    if (opt.precision == GBP_PREC_MIXED) {
+        nodal_to_f32(l0.g, r, l0.b32, scale, s);
+        vcycle<float>(0, l0.b32, true);
+        for (int c = 1; c < m; ++c) vcycle<float>(0, l0.b32, false);
+        nodal_add_correction<float>(l0.g, x, (const float*)xres[0], 1.0 / scale, s);
+    } else {
+        vcycle<double>(0, r, true);
+        for (int c = 1; c < m; ++c) vcycle<double>(0, r, false);
+        nodal_add_correction<double>(l0.g, x, (const double*)xres[0], 1.0, s);
+    }
+    cap_or_st = st;
+}
+
 int NodalSolver::run_iteration(int m)
 {
     if (!opt.use_graphs) {
@@ -845,7 +862,7 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
 }
 
 int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
-                         const gbp_array4* phi_guess, gbp_stats* stats)
+                         const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy)
 {
     if (!sigma_ready) {
         set_error("nodal project: sigma was never set on this plan");
@@ -871,12 +888,19 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
     GBP_CUDA(cudaGetLastError());
     int status = solve(phi_guess != nullptr, stats);
     if (status != GBP_OK && status != GBP_NOT_CONVERGED) return status;
-    nodal_correct(l0.g, corr, l0.s64, phi, st);
-    ++nk;
+    // p_nd first: its copy-out can then overlap the velocity correction
     if (phi_out && phi_out->data) {
         nodal_store_phi(l0.g, *phi_out, phi, phi_accumulate, st);
         ++nk;
+        if (phi_copy && phi_copy->dst) {
+            GBP_CUDA(cudaEventRecord(phi_copy->ev, st));
+            GBP_CUDA(cudaStreamWaitEvent(phi_copy->stream, phi_copy->ev, 0));
+            GBP_CUDA(cudaMemcpyAsync(phi_copy->dst, phi_copy->src, phi_copy->bytes, cudaMemcpyDeviceToHost,
+                                     phi_copy->stream));
+        }
     }
+    nodal_correct(l0.g, corr, l0.s64, phi, st);
+    ++nk;
     GBP_CUDA(cudaEventRecord(ev2, st));
     GBP_CUDA(cudaGetLastError());
     if (stats) {

@@ -17,6 +17,15 @@ namespace nn {
 class UNet;
 }
 
+// an asynchronous copy to issue on `stream` after `ev` (recorded by the issuer) completes
+struct HostCopy {
+    void* dst;
+    const void* src;
+    size_t bytes;
+    cudaStream_t stream;
+    cudaEvent_t ev;
+};
+
 struct DevicePool {
     char* base = nullptr;
     size_t bytes = 0;
@@ -54,9 +63,11 @@ public:
     // overset mask (0 = phi held at 0) over nodes 0..n; nullptr removes it
     int set_mask(const gbp_iarray4* mask);
 
-    // full projection: rhs from vel (+ fused add-back / U^n subtraction), solve, correct
+    // full projection: rhs from vel (+ fused add-back / U^n subtraction), solve, correct.
+    // phi_copy: a copy (e.g. p_nd to the host) issued on its own stream once phi_out is stored,
+    // overlapping the velocity correction
     int project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
-                const gbp_array4* phi_guess, gbp_stats* stats);
+                const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy = nullptr);
 
     // nodal divergence of vel as the projection sees it (consistent for singular systems), strong form
     int divergence(const RhsArgs& rhs, const gbp_array4* out, double* max_norm);
@@ -66,6 +77,11 @@ public:
     cudaStream_t stream() const { return st; }
     // solve A phi = g on the level-0 arrays already in place (used by project and tests)
     int solve(bool have_guess, gbp_stats* stats);
+
+    // Preconditioner for a composite (two-level) driver: x += m V-cycles from zero on the FP64 level-0
+    // residual r, in the plan's precision (FP32 V-cycles on r * scale in the mixed form). r and x are
+    // level-0 arrays in the padded layout; r is not modified.
+    void apply_vcycles(const double* r, double* x, int m, double scale, cudaStream_t s);
 
     void reset_count() { nk = 0; }
     long long kernel_count() const { return nk; }

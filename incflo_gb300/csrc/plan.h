@@ -14,9 +14,12 @@ struct gbp_plan {
     int bc_lo[3], bc_hi[3];
     gbp::NodalSolver* nodal = nullptr;
     gbp::MacSolver* mac = nullptr;
-    // device staging for the host-buffer entry point
+    // device staging for the host-buffer entry point, and the stream / events that overlap its
+    // copies with the solve
     double* hbuf = nullptr;
     size_t hbuf_bytes = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_phi = nullptr, ev_out = nullptr;
     double* dflux = nullptr;  // 2 device doubles: inflow / outflow of the solvability fix
     double* ccbuf = nullptr;  // cell-centred projection scratch (unprojected face velocities, phi)
 };

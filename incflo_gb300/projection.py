@@ -291,6 +291,67 @@ def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd,
     return st.as_dict()
 
 
+class AmrNodalProjector:
+    """incflo::ApplyNodalProjection over two levels (finest_level = 1, refinement ratio 2): the composite
+    nodal solve of one NodalProjector over both levels. ``fine_boxes``: the fine level's BoxArray as
+    [(lo, hi)] of fine cells (inclusive, whole coarse cells). Fields per level: the coarse ones as
+    tensors over the coarse cells (nodes for p_nd), the fine ones as lists of per-box tensors over each
+    box's cells (nodes lo..hi+1 for p_nd); components first for velocities and gp."""
+
+    def __init__(self, geom: Geometry, bc_lo, bc_hi, fine_boxes, options: A.Options | None = None, stream=None):
+        L = A.load()
+        self.geom = geom
+        self.boxes = [(tuple(int(v) for v in lo), tuple(int(v) for v in hi)) for lo, hi in fine_boxes]
+        self.options = options or A.default_options(A.GBP_NODAL)
+        flat = (ctypes.c_int * (6 * len(self.boxes)))(*[v for lo, hi in self.boxes for v in (*lo, *hi)])
+        self.ptr = ctypes.c_void_p()
+        A.check(L.gbp_amr_create(ctypes.byref(geom.c()), (ctypes.c_int * 3)(*[int(v) for v in bc_lo]),
+                                 (ctypes.c_int * 3)(*[int(v) for v in bc_hi]), flat, len(self.boxes),
+                                 ctypes.byref(self.options), _stream_ptr(stream), ctypes.byref(self.ptr)),
+                "gbp_amr_create")
+
+    def set_options(self, options: A.Options):
+        self.options = options
+        A.check(A.load().gbp_amr_set_options(self.ptr, ctypes.byref(options)), "gbp_amr_set_options")
+
+    def device_bytes(self) -> int:
+        return int(A.load().gbp_amr_device_bytes(self.ptr))
+
+    def _boxes4(self, tensors, nodal=False):
+        if tensors is None:
+            return None, None
+        arr = (A.Array4 * len(self.boxes))()
+        for b, t in enumerate(tensors):
+            arr[b] = array4(t, 0, lo=self.boxes[b][0])
+        return arr, ctypes.cast(arr, ctypes.POINTER(A.Array4))
+
+    def apply(self, vel_c, density_c, gp_c, p_c, vel_f, density_f, gp_f, p_f, *, scaling_factor=1.0,
+              incremental=False, vel_old_c=None, vel_old_f=None, rho0=1.0, constant_density=False):
+        keep = []
+
+        def bx(t):
+            a, p = self._boxes4(t)
+            keep.append(a)
+            return p
+
+        st = A.Stats()
+        rho_c = None if constant_density else array4(density_c, 0)
+        A.check(A.load().gbp_amr_apply_nodal_projection(
+            self.ptr, _ref(array4(vel_c)), _ref(array4(vel_old_c)) if vel_old_c is not None else None, _ref(rho_c),
+            _ref(array4(gp_c)), _ref(array4(p_c)) if p_c is not None else None, bx(vel_f), bx(vel_old_f),
+            None if constant_density else bx(density_f), bx(gp_f), bx(p_f), float(rho0), float(scaling_factor),
+            int(incremental), ctypes.byref(st)), "gbp_amr_apply_nodal_projection")
+        return st.as_dict()
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                A.load().gbp_amr_destroy(self.ptr)
+                self.ptr = ctypes.c_void_p()
+        except Exception:
+            pass
+
+
 def apply_cc_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_cc, umac, *, time=0.0, dt=1.0,
                         prev_dt=1.0, scaling_factor=1.0, incremental=False, set_inflow_bc=True, vel_old=None,
                         rho0=1.0, ng=1, ng_rho=1, options: A.Options | None = None, stream=None,

@@ -230,6 +230,33 @@ int gbp_mac_set_beta_from_density(gbp_plan* plan, const gbp_array4* rho, double 
 int gbp_mac_project(gbp_plan* plan, gbp_array4* umac_x, gbp_array4* umac_y, gbp_array4* umac_z,
                     gbp_array4* phi, int phi_guess, gbp_stats* stats);
 
+/* ---- two-level (AMR) composite nodal projection ----------------------------------------
+ * incflo::ApplyNodalProjection(density, time, scaling_factor, incremental) over finest_level = 1
+ * (src/projection/incflo_apply_nodal_projection.cpp:95-267): one NodalProjector over both levels
+ * (:187-192) and MLNodeLaplacian's composite solve (:215), the levels' phi / grad phi (:218-219),
+ * gp and p_nd per level (:221-257). Composite discretisation: conforming Q1 elements on the leaf cells
+ * (fine cells of the fine boxes, coarse cells they do not cover); fine nodes on the coarse-fine
+ * interface that are not coarse nodes hang (linear along the coarse face). Refinement ratio 2.
+ * fine_boxes: nbox boxes of fine cells (lo[3], hi[3] inclusive, 6 ints each, in the fine index
+ * space of the whole domain; disjoint, whole coarse cells: lo even, hi odd) — the fine level's
+ * BoxArray. Boundaries: periodic, Dirichlet (outflow) and Neumann (walls); inflow is rejected. */
+typedef struct gbp_amr gbp_amr;
+int gbp_amr_create(const gbp_geometry* coarse, const int bc_lo[3], const int bc_hi[3], const int* fine_boxes,
+                   int nbox, const gbp_options* opt, void* stream, gbp_amr** amr);
+int gbp_amr_destroy(gbp_amr* amr);
+int gbp_amr_set_options(gbp_amr* amr, const gbp_options* opt);
+size_t gbp_amr_device_bytes(const gbp_amr* amr);
+/* Coarse level: vel (3 comps), gp (3), rho (NULL: rho0), vel_old (incremental only, else NULL) cell
+ * arrays, p_nd nodal (NULL: not written). Fine level: arrays of nbox pointers (the fine MultiFab's
+ * FABs, in box order) with the same meaning; p_f covers each box's nodes. Non-incremental: u += s gp /
+ * rho before the solve and gp = grad phi, p_nd = phi after; incremental: u -= vel_old before, gp +=,
+ * p_nd += after, with vel_old added back. */
+int gbp_amr_apply_nodal_projection(gbp_amr* amr, gbp_array4* vel_c, const gbp_array4* vel_old_c,
+                                   const gbp_array4* rho_c, gbp_array4* gp_c, gbp_array4* p_c,
+                                   gbp_array4* const* vel_f, const gbp_array4* const* vel_old_f,
+                                   const gbp_array4* const* rho_f, gbp_array4* const* gp_f, gbp_array4* const* p_f,
+                                   double rho0, double scaling_factor, int incremental, gbp_stats* stats);
+
 /* ---- host-buffer convenience (end-to-end path) ----------------------------------------
  * Same as gbp_apply_nodal_projection with contiguous HOST arrays (no ghost cells):
  * vel [3][nz][ny][nx], rho [nz][ny][nx], gp [3][nz][ny][nx], p_nd nodal [nz+1][ny+1][nx+1].
