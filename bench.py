@@ -181,6 +181,106 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_amr(args, dev, steps=3, warmup=1):
+    """ms per two-level composite projection (mixed form): base n^3 + a ratio-2 band z in [3/8, 5/8)
+    in 64^3 fine boxes; inputs restored before each call (outside the timed region)."""
+    import numpy as np
+    import torch
+
+    from incflo_gb300 import AmrNodalProjector, Geometry, make_options, synth
+
+    w = synth.variable_density_rt_amr(args.n)
+    b = w["base"]
+    n = b["n"]
+    geom = Geometry(n, b["lo"], b["hi"])
+    proj = AmrNodalProjector(geom, b["bclo"], b["bchi"], w["boxes"],
+                             options=make_options(0, precision="mixed", mg_rtol=args.rtol, mg_atol=0.0))
+    vel0 = torch.from_numpy(np.ascontiguousarray(b["vel"])).to(dev)
+    rho_c = torch.from_numpy(np.ascontiguousarray(b["rho"])).to(dev)
+    vel_c = vel0.clone()
+    gp_c = torch.zeros_like(vel0)
+    p_c = torch.zeros((n[2] + 1, n[1] + 1, n[0] + 1), dtype=torch.float64, device=dev)
+    zlo = w["zlo"]
+    vf0 = torch.from_numpy(w["vel_f"]).to(dev)
+    rf = torch.from_numpy(np.ascontiguousarray(w["rho_f"])).to(dev)
+
+    def sl(t, lo, hi, e=0):
+        return t[..., lo[2] - zlo:hi[2] - zlo + 1 + e, lo[1]:hi[1] + 1 + e, lo[0]:hi[0] + 1 + e]
+
+    vel_f = [sl(vf0, lo, hi).clone() for lo, hi in w["boxes"]]
+    vel_f0 = [v.clone() for v in vel_f]
+    rho_f = [sl(rf, lo, hi).contiguous() for lo, hi in w["boxes"]]
+    gp_f = [torch.zeros_like(v) for v in vel_f]
+    p_f = [torch.zeros((hi[2] - lo[2] + 2, hi[1] - lo[1] + 2, hi[0] - lo[0] + 2), dtype=torch.float64, device=dev)
+           for lo, hi in w["boxes"]]
+    times, st = [], None
+    for i in range(warmup + steps):
+        vel_c.copy_(vel0)
+        gp_c.zero_()
+        for v, v0, g in zip(vel_f, vel_f0, gp_f):
+            v.copy_(v0)
+            g.zero_()
+        torch.cuda.synchronize()
+        st = proj.apply(vel_c, rho_c, gp_c, p_c, vel_f, rho_f, gp_f, p_f, scaling_factor=1.0)
+        if st["status"] != 0:
+            raise RuntimeError(f"amr projection failed: {st}")
+        if i >= warmup:
+            times.append(st["ms_total"])
+    fine_cells = sum((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) for lo, hi in w["boxes"])
+    return {"workload": f"{args.n}^3 base + ratio-2 band z in [3/8, 5/8) of the whole x/y extent "
+                        f"({len(w['boxes'])} fine boxes of 64^3, {fine_cells} fine cells), composite nodal "
+                        f"projection, FP32 V-cycles inside FP64 refinement, rtol {args.rtol:g}",
+            "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
+            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"],
+            "device_bytes": proj.device_bytes()}
+
+
+def run_eb_mac(args, dev, steps=5, warmup=3):
+    """ms per cut-cell MAC projection on the cylinder channel: [0,4]x[0,1]^2 at 256x64x64, cylinder
+    r = 0.125 at (1, 0.5) along z, inflow u = 1 + 1e-3 noise at x = 0, outflow x = 4, walls y,
+    periodic z, rho = 1 (beta = dt = 1), mixed form, rtol 1e-10 (the cfg4 geometry)."""
+    import numpy as np
+    import torch
+
+    from incflo_gb300 import Geometry, MacProjector, eb, make_options
+
+    n, ext = (256, 64, 64), (4.0, 1.0, 1.0)
+    P, D, N, I = 0, 1, 2, 3
+    geo = eb.cylinder(n, (0, 0, 0), ext, (1.0, 0.5, 0.0), 0.125)
+    rng = np.random.Generator(np.random.PCG64(4))
+    shapes = [(n[2], n[1], n[0] + 1), (n[2], n[1] + 1, n[0]), (n[2] + 1, n[1], n[0])]
+    u = [1e-3 * rng.uniform(-1.0, 1.0, sh) for sh in shapes]
+    u[0] += 1.0
+    u[0][:, :, 0] = 1.0
+    u[1][:, 0, :] = 0.0
+    u[1][:, -1, :] = 0.0
+    u[2][-1] = u[2][0]
+    u0 = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in u]
+    ut = [x.clone() for x in u0]
+    mp = MacProjector(Geometry(n, (0, 0, 0), ext),
+                      options=make_options(1, precision="mixed", mg_rtol=args.rtol, mg_atol=0.0))
+    mp.initProjector(beta=1.0)
+    mp.setDomainBC((I, N, P), (D, N, P))
+    mp.setEB(torch.from_numpy(geo["vfrac"]).to(dev), [torch.from_numpy(geo[k]).to(dev) for k in ("apx", "apy", "apz")],
+             [torch.from_numpy(np.ascontiguousarray(np.moveaxis(geo[k], -1, 0))).to(dev) for k in ("fcx", "fcy", "fcz")])
+    mp.setUMAC(ut)
+    times, st = [], None
+    for i in range(warmup + steps):
+        for a, b in zip(ut, u0):
+            a.copy_(b)
+        torch.cuda.synchronize()
+        st = mp.project(rtol=args.rtol, atol=0.0)
+        if st["status"] != 0:
+            raise RuntimeError(f"EB MAC projection failed: {st}")
+        if i >= warmup:
+            times.append(st["ms_total"])
+    cut = int(((geo["vfrac"] > 0) & (geo["vfrac"] < 1)).sum())
+    return {"workload": f"cut-cell MAC projection, cylinder channel 256x64x64 ({cut} cut cells), inflow / outflow "
+                        f"/ walls / periodic, FP32 V-cycles inside FP64 refinement, rtol {args.rtol:g}",
+            "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
+            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"]}
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -310,6 +410,14 @@ def run_ours(args, ws, rank, local):
                "d2h_bytes_per_step": 6 * nc * 8 + (n + 1) ** 3 * 8}
         del hplan
 
+    # two-level (AMR) composite projection: the 256^3 base plus a refined interface band (cfg5-like)
+    amr = None
+    if not args.no_amr:
+        amr = run_amr(args, dev)
+    eb_mac = None
+    if not args.no_eb:
+        eb_mac = run_eb_mac(args, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         ns = max(16, n // 2)
@@ -345,6 +453,8 @@ def run_ours(args, ws, rank, local):
                                  "ms_per_launch": round(ms64.value, 5)},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "amr": amr,
+        "eb_mac": eb_mac,
         "gpu_launches": launches,
         "clocks": clocks,
     }
@@ -364,6 +474,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-amr", action="store_true")
+    ap.add_argument("--no-eb", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm-start", action="store_true")
     ap.add_argument("--warm-level", type=int, default=1)

@@ -764,6 +764,72 @@ int gbp_plan_time_kernel(gbp_plan* p, int which, int reps, double* ms_per_launch
     return p->nodal->time_kernel(which, reps, ms_per_launch, bytes_per_launch);
 }
 
+int gbp_abec_set_coeffs(gbp_plan* p, double alpha, const gbp_array4* a, double a0, double beta,
+                        const gbp_array4* bx, const gbp_array4* by, const gbp_array4* bz, double b0)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_abec_set_coeffs: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    const int lo[3] = {0, 0, 0};
+    const int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+    if (a && !(valid_array(a, 1) && covers(a, lo, hi))) {
+        set_error("gbp_abec_set_coeffs: a must cover the cells");
+        return GBP_BAD_ARG;
+    }
+    const gbp_array4* b[3] = {bx, by, bz};
+    if (bx || by || bz)
+        for (int d = 0; d < 3; ++d) {
+            int fhi[3] = {hi[0], hi[1], hi[2]};
+            fhi[d] += 1;
+            if (!valid_array(b[d], 1) || !covers(b[d], lo, fhi)) {
+                set_error("gbp_abec_set_coeffs: each b array must cover its faces 0..n");
+                return GBP_BAD_ARG;
+            }
+        }
+    return p->mac->set_abec(alpha, a, a0, beta, (bx || by || bz) ? b : nullptr, b0);
+}
+
+int gbp_abec_set_coeffs_eta(gbp_plan* p, double alpha, const gbp_array4* a, double a0, double beta,
+                            const gbp_array4* eta)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_abec_set_coeffs_eta: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    const int lo[3] = {0, 0, 0};
+    const int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+    if ((a && !(valid_array(a, 1) && covers(a, lo, hi))) || !valid_array(eta, 1) || !covers(eta, lo, hi)) {
+        set_error("gbp_abec_set_coeffs_eta: a and eta must cover the cells");
+        return GBP_BAD_ARG;
+    }
+    return p->mac->set_abec(alpha, a, a0, beta, nullptr, 0.0, eta);
+}
+
+int gbp_abec_solve(gbp_plan* p, const gbp_array4* rhs, gbp_array4* phi, gbp_stats* stats)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_abec_solve: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    int lo[3] = {0, 0, 0};
+    int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+    if (!valid_array(rhs, 1) || !covers(rhs, lo, hi)) {
+        set_error("gbp_abec_solve: rhs must cover the cells");
+        return GBP_BAD_ARG;
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (p->bc_lo[d] == GBP_BC_DIRICHLET) lo[d] = -1;
+        if (p->bc_hi[d] == GBP_BC_DIRICHLET) hi[d] += 1;
+    }
+    if (!valid_array(phi, 1) || !covers(phi, lo, hi)) {
+        set_error("gbp_abec_solve: phi must cover the cells and one ghost layer on the Dirichlet sides");
+        return GBP_BAD_ARG;
+    }
+    if (stats) memset(stats, 0, sizeof(*stats));
+    return p->mac->abec_solve(rhs, phi, stats);
+}
+
 struct gbp_amr {
     gbp::CompositeNodal* c = nullptr;
     gbp_geometry geom{};

@@ -223,6 +223,31 @@ __global__ void k_amr_sigma_fine(NodalGeom gf, const unsigned char* __restrict__
     sig[q] = v;
 }
 
+// sigma of the coarse level's V-cycles (dense cells): scale / rho on uncovered cells, the mean of the 8
+// fine sigma on covered ones (those cells are not part of the composite system; the fine average makes
+// the coarse correction match the fine operator there)
+__global__ void k_amr_sigma_coarse(NodalGeom gc, const unsigned char* __restrict__ mc, gbp_array4 rho, int have_rho,
+                                   double scale, double rho0, const double* __restrict__ sig_f, int off0, int off1,
+                                   int off2, int nb0, int nb1, double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.n[0] || j >= gc.n[1] || k >= gc.n[2]) return;
+    double v;
+    if (mc[pidx(gc.sy, gc.sz, i, j, k)]) {
+        v = have_rho ? scale / *at4(rho, i, j, k, 0) : scale / rho0;
+    } else {
+        v = 0.0;
+        for (int q = 0; q < 8; ++q) {
+            const int fi = 2 * i - off0 + (q & 1), fj = 2 * j - off1 + ((q >> 1) & 1), fk = 2 * k - off2 + (q >> 2);
+            v += sig_f[fi + (long long)nb0 * (fj + (long long)nb1 * fk)];
+        }
+        v *= 0.125;
+    }
+    out[i + (long long)gc.n[0] * (j + (long long)gc.n[1] * k)] = v;
+}
+
 // coarse sigma with covered cells zeroed (whole padded arrays, aliases included)
 __global__ void k_amr_mask_sigma(long long count, const double* __restrict__ s, const unsigned char* __restrict__ m,
                                  double* __restrict__ out)
@@ -655,7 +680,7 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     add(gf.count, 1);
     add(gc.count, 1);
     add(gf.count, 1);
-    for (int q = 0; q < 6; ++q) add(gc.count, 8);  // sc_m, phi_c, b_c, r_c, rc_full, e_c
+    for (int q = 0; q < 7; ++q) add(gc.count, 8);  // sc_m, sc_t, phi_c, b_c, r_c, rc_full, e_c
     for (int q = 0; q < 3; ++q) add(gf.count, 8);  // phi_f, b_f, r_f
     add(3 * ncf, 8);                               // vel_f
     add(3 * ncf, 8);                               // gp_f
@@ -675,6 +700,7 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     ccls = pool.take<unsigned char>(gc.count);
     fcls = pool.take<unsigned char>(gf.count);
     sc_m = pool.take<double>(gc.count);
+    sc_t = pool.take<double>(gc.count);
     phi_c = pool.take<double>(gc.count);
     b_c = pool.take<double>(gc.count);
     r_c = pool.take<double>(gc.count);
@@ -818,11 +844,29 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     if ((rc = gather(f.vel_old_f, 3, velo_f))) return rc;
     // sigma on both levels (coarse: whole level for the V-cycles, covered cells zeroed for the
     // composite operator; fine: zero outside the fine cells)
-    rc = crs.set_sigma_from_density(f.rho_c, f.scale, f.rho0);
-    if (rc) return rc;
-    k_amr_mask_sigma<<<(unsigned)((gc.count + kT - 1) / kT), kT, 0, st>>>(gc.count, crs.sigma64(), cmask_c, sc_m);
     k_amr_sigma_fine<<<g3(nfb[0], nfb[1], nfb[2]), kB3, 0, st>>>(gf, cmask_f, rho_f, f.rho_f != nullptr, f.scale,
                                                                  f.rho0, sig_f);
+    {
+        gbp_array4 rc_a{};
+        if (f.rho_c) rc_a = *f.rho_c;
+        k_amr_sigma_coarse<<<g3(gc.n[0], gc.n[1], gc.n[2]), kB3, 0, st>>>(gc, cmask_c, rc_a, f.rho_c != nullptr,
+                                                                          f.scale, f.rho0, sig_f, off[0], off[1],
+                                                                          off[2], nfb[0], nfb[1], rc_full);
+        gbp_array4 ca{};
+        ca.data = rc_full;  // scratch until the solve starts
+        for (int d = 0; d < 3; ++d) ca.hi[d] = gc.n[d] - 1;
+        ca.ncomp = 1;
+        ca.jstride = gc.n[0];
+        ca.kstride = (long long)gc.n[0] * gc.n[1];
+        ca.nstride = (long long)gc.n[0] * gc.n[1] * gc.n[2];
+        rc = crs.set_sigma(&ca, 0.0);
+        if (rc) return rc;
+    }
+    // s / rho on every coarse cell: the gp add-back and the velocity correction of the coarse level;
+    // covered cells zeroed: the coarse part of the composite operator
+    GBP_CUDA(cudaMemsetAsync(sc_t, 0, sizeof(double) * gc.count, st));
+    nodal_sigma_from_rho(gc, f.rho_c, f.scale, f.rho0, sc_t, nullptr, st);
+    k_amr_mask_sigma<<<(unsigned)((gc.count + kT - 1) / kT), kT, 0, st>>>(gc.count, sc_t, cmask_c, sc_m);
     gbp_array4 sa{};
     sa.data = sig_f;
     for (int d = 0; d < 3; ++d) sa.hi[d] = nfb[d] - 1;
@@ -863,7 +907,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     raf.sub_old = sub_old;
     if (sub_old) raf.vel_old = cellsf(velo_f, 3);
     raf.cmask = cmask_f;
-    nodal_rhs(gc, rac, crs.sigma64(), b_c, nullptr, st);
+    nodal_rhs(gc, rac, sc_t, b_c, nullptr, st);
     nodal_rhs(gf_nomask, raf, fin.sigma64(), b_f, nullptr, st);
     sync(b_c, b_f);
     k_amr_zero_nondof<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, b_c);
@@ -953,7 +997,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     caf.add_gp = !f.incremental;
     caf.incremental = f.incremental;
     if (f.p_c && f.p_c->data) nodal_store_phi(gc, *f.p_c, phi_c, f.incremental, st);
-    nodal_correct(gc, cac, crs.sigma64(), phi_c, st);
+    nodal_correct(gc, cac, sc_t, phi_c, st);
     nodal_correct(gf_nomask, caf, fin.sigma64(), phi_f, st);
     k_amr_fine_nodes<<<g3(nfb[0] + 1, nfb[1] + 1, nfb[2] + 1), kB3, 0, st>>>(gf, phi_f, p_fb);
     // fine outputs back into the boxes

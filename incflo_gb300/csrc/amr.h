@@ -72,6 +72,7 @@ private:
     DevicePool pool;
     unsigned char *cmask_c = nullptr, *cmask_f = nullptr, *ccls = nullptr, *fcls = nullptr;
     double *sc_m = nullptr;                                       // coarse sigma, covered cells 0
+    double *sc_t = nullptr;                                       // coarse sigma s / rho on every cell
     double *phi_c = nullptr, *b_c = nullptr, *r_c = nullptr, *rc_full = nullptr, *e_c = nullptr;
     double *phi_f = nullptr, *b_f = nullptr, *r_f = nullptr;
     double *vel_f = nullptr, *gp_f = nullptr, *rho_f = nullptr, *velo_f = nullptr, *sig_f = nullptr;

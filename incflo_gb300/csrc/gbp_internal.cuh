@@ -55,6 +55,9 @@ struct CellGeom {
     double w[3];   // V / h_d^2: face weight per unit beta
     double vol;
     double h[3];
+    // diagonal term alpha a V per cell (the ABecLaplacian's alpha a), or null (the Poisson operator)
+    const double* a64;
+    const float* a32;
 };
 
 // x position of index 0 in a padded row: 4 elements, so that node/cell 0 starts a 16-byte (FP32) /
@@ -198,20 +201,6 @@ __device__ __forceinline__ unsigned long long abs_key(double v)
 __device__ __forceinline__ double key_value(unsigned long long k)
 {
     return k > 0x7ff0000000000000ull ? __longlong_as_double(0x7ff8000000000000ll) : __longlong_as_double((long long)k);
-}
-
-// 1/x by Newton's iteration r <- r + r (1 - x r) from the single-precision reciprocal: each step
-// doubles the correct bits (24 -> 48 -> the double's 53), within an ulp or two of the correctly
-// rounded quotient, in 4 FP64 instructions instead of a full IEEE division. Outside the float range
-// the IEEE division is used.
-__device__ __forceinline__ double recip_newton(double x)
-{
-    const double ax = fabs(x);
-    if (!(ax > 1e-30 && ax < 1e30)) return 1.0 / x;
-    double r = (double)__frcp_rn((float)x);
-    r = fma(r, fma(-x, r, 1.0), r);
-    r = fma(r, fma(-x, r, 1.0), r);
-    return r;
 }
 
 // Warp reductions over the lanes that exist: a block whose size is not a multiple of 32 has a

@@ -27,6 +27,15 @@ __device__ __forceinline__ bool decode_cell(const CellGeom& g, long long t, int&
 }
 
 template <typename T>
+__device__ __forceinline__ const T* mac_acoef(const CellGeom& g);
+template <>
+__device__ __forceinline__ const double* mac_acoef<double>(const CellGeom& g) { return g.a64; }
+template <>
+__device__ __forceinline__ const float* mac_acoef<float>(const CellGeom& g) { return g.a32; }
+
+// (A x)_p = sum over faces of w beta (x_p - x_nb) [+ alpha a V x_p]; diag and the neighbour sum for
+// the Gauss-Seidel update x_p = (b_p + offsum) / diag
+template <typename T>
 __device__ __forceinline__ T mac_Ax(const CellGeom& g, const T* __restrict__ x, const T* __restrict__ bx,
                                     const T* __restrict__ by, const T* __restrict__ bz, long long p, T& diag,
                                     T& offsum)
@@ -39,8 +48,14 @@ __device__ __forceinline__ T mac_Ax(const CellGeom& g, const T* __restrict__ x, 
     diag = ((b0 + b1) + (b2 + b3)) + (b4 + b5);
     offsum = ((b0 * x[p - 1] + b1 * x[p + 1]) + (b2 * x[p - g.sy] + b3 * x[p + g.sy])) +
              (b4 * x[p - g.sz] + b5 * x[p + g.sz]);
-    return ((b0 * (xc - x[p - 1]) + b1 * (xc - x[p + 1])) + (b2 * (xc - x[p - g.sy]) + b3 * (xc - x[p + g.sy]))) +
+    T ax = ((b0 * (xc - x[p - 1]) + b1 * (xc - x[p + 1])) + (b2 * (xc - x[p - g.sy]) + b3 * (xc - x[p + g.sy]))) +
            (b4 * (xc - x[p - g.sz]) + b5 * (xc - x[p + g.sz]));
+    const T* ac = mac_acoef<T>(g);
+    if (ac) {
+        diag += ac[p];
+        ax += ac[p] * xc;
+    }
+    return ax;
 }
 
 template <typename T>
@@ -234,7 +249,7 @@ __device__ __forceinline__ double* a4p(const gbp_array4& a, int i, int j, int k,
 // 2 = dt / (0.5 (rho_lo + rho_hi)) (incflo: average_cellcenter_to_face then invert(dt)).
 __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double cval, int bclo, int bchi,
                            double* __restrict__ b64, float* __restrict__ b32, RobinFaces rb,
-                           const double* __restrict__ ap)
+                           const double* __restrict__ ap, double mult)
 {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int fn[3] = {g.n[0], g.n[1], g.n[2]};
@@ -263,12 +278,25 @@ __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double
         beta = a4(src, q[0], q[1], q[2], 0);
     } else if (source == 1) {
         beta = cval;
+    } else if (source == 3) {
+        // face average of a cell field (amrex::average_cellcenter_to_face), the adjacent cell on a
+        // non-periodic domain side (incflo::fixup_eta_on_domain_faces)
+        int lo[3] = {q[0], q[1], q[2]};
+        lo[d] -= 1;
+        if (per && lo[d] < 0) lo[d] += g.n[d];
+        if (!per && fd == 0)
+            beta = a4(src, q[0], q[1], q[2], 0);
+        else if (!per && fd == g.n[d])
+            beta = a4(src, lo[0], lo[1], lo[2], 0);
+        else
+            beta = 0.5 * (a4(src, lo[0], lo[1], lo[2], 0) + a4(src, q[0], q[1], q[2], 0));
     } else {
         int lo[3] = {q[0], q[1], q[2]};
         lo[d] -= 1;
         if (per && lo[d] < 0) lo[d] += g.n[d];
         beta = cval / (0.5 * (a4(src, lo[0], lo[1], lo[2], 0) + a4(src, q[0], q[1], q[2], 0)));
     }
+    beta *= mult;  // the ABecLaplacian's beta scalar times b (1 for the projections)
     // Dirichlet face: the ghost value sits half a cell out, so the face weight doubles; Robin face
     // (a phi + b dphi/dn = 0): weight beta a h / (a h / 2 + b), with the raw beta kept for later factors
     double eff = beta;
@@ -493,13 +521,89 @@ GBP_MAC_INST(double)
 GBP_MAC_INST(float)
 
 void mac_set_beta(const CellGeom& g, int d, int source, const gbp_array4* src, double cval, int bclo, int bchi,
-                  double* b64, float* b32, cudaStream_t st, const RobinFaces* rb, const double* ap)
+                  double* b64, float* b32, cudaStream_t st, const RobinFaces* rb, const double* ap, double mult)
 {
     gbp_array4 a{};
     if (src) a = *src;
     RobinFaces r{};
     if (rb) r = *rb;
-    k_mac_beta<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, source, a, cval, bclo, bchi, b64, b32, r, ap);
+    k_mac_beta<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, source, a, cval, bclo, bchi, b64, b32, r, ap, mult);
+}
+
+// ------------------------------------------------------------------------------------------------
+// ABecLaplacian extras: the diagonal alpha a V per cell on every level, the right-hand side V rhs with
+// the Dirichlet boundary values moved onto it
+__global__ void k_abec_acoef(CellGeom g, gbp_array4 a, int have_a, double alpha, double a0, double* __restrict__ a64,
+                             float* __restrict__ a32)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const double v = alpha * (have_a ? a4(a, i, j, k, 0) : a0) * g.vol;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    a64[p] = v;
+    a32[p] = (float)v;
+}
+
+__global__ void k_abec_acoarsen(CellGeom gf, CellGeom gc, const double* __restrict__ af, double* __restrict__ ac64,
+                                float* __restrict__ ac32)
+{
+    int I, J, K;
+    if (!decode_cell(gc, blockIdx.x * (long long)blockDim.x + threadIdx.x, I, J, K)) return;
+    const long long f = pidx(gf.sy, gf.sz, 2 * I, 2 * J, 2 * K);
+    const double v = ((af[f] + af[f + 1]) + (af[f + gf.sy] + af[f + 1 + gf.sy])) +
+                     ((af[f + gf.sz] + af[f + 1 + gf.sz]) + (af[f + gf.sy + gf.sz] + af[f + 1 + gf.sy + gf.sz]));
+    const long long p = pidx(gc.sy, gc.sz, I, J, K);
+    ac64[p] = v;
+    ac32[p] = (float)v;
+}
+
+__global__ void k_abec_rhs(CellGeom g, gbp_array4 rhs, double* __restrict__ b)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    b[pidx(g.sy, g.sz, i, j, k)] = g.vol * a4(rhs, i, j, k, 0);
+}
+
+// b += w eff_face phi_b on the cells next to a Dirichlet side (phi_b: the ghost cell of phi, which holds
+// the value on the face)
+__global__ void k_abec_dirichlet(CellGeom g, int d, int hi, const double* __restrict__ beta, gbp_array4 phi,
+                                 double* __restrict__ b)
+{
+    const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)g.n[d1] * g.n[d2]) return;
+    int c[3], f[3];
+    c[d1] = f[d1] = (int)(t % g.n[d1]);
+    c[d2] = f[d2] = (int)(t / g.n[d1]);
+    c[d] = hi ? g.n[d] - 1 : 0;
+    f[d] = hi ? g.n[d] : 0;
+    int gh[3] = {c[0], c[1], c[2]};
+    gh[d] = hi ? g.n[d] : -1;
+    const double eff = beta[pidx(g.sy, g.sz, f[0], f[1], f[2])];
+    b[pidx(g.sy, g.sz, c[0], c[1], c[2])] += g.w[d] * eff * a4(phi, gh[0], gh[1], gh[2], 0);
+}
+
+void abec_acoef(const CellGeom& g, const gbp_array4* a, double alpha, double a0, double* a64, float* a32,
+                cudaStream_t st)
+{
+    gbp_array4 aa{};
+    if (a) aa = *a;
+    k_abec_acoef<<<nblk(ncell(g), 256), 256, 0, st>>>(g, aa, a != nullptr, alpha, a0, a64, a32);
+}
+void abec_acoarsen(const CellGeom& gf, const CellGeom& gc, const double* af, double* ac64, float* ac32,
+                   cudaStream_t st)
+{
+    k_abec_acoarsen<<<nblk(ncell(gc), 256), 256, 0, st>>>(gf, gc, af, ac64, ac32);
+}
+void abec_rhs(const CellGeom& g, const gbp_array4& rhs, double* b, cudaStream_t st)
+{
+    k_abec_rhs<<<nblk(ncell(g), 256), 256, 0, st>>>(g, rhs, b);
+}
+void abec_dirichlet(const CellGeom& g, int d, int hi, const double* beta, const gbp_array4& phi, double* b,
+                    cudaStream_t st)
+{
+    const int d1 = d == 0 ? 1 : 0, d2 = d == 2 ? 1 : 2;
+    k_abec_dirichlet<<<nblk((long long)g.n[d1] * g.n[d2], 256), 256, 0, st>>>(g, d, hi, beta, phi, b);
 }
 
 __global__ void k_mac_load_kappa(CellGeom g, gbp_array4 in, double* __restrict__ kap)

@@ -46,7 +46,8 @@ struct EbCell {
     int slot[6];
 };
 
-// source: 0 = face array, 1 = constant, 2 = dt / face average of rho (src = rho, cval = dt)
+// source: 0 = face array, 1 = constant, 2 = dt / face average of rho (src = rho, cval = dt),
+// 3 = face average of a cell field (the adjacent cell on non-periodic sides); mult scales the result
 // Robin boundary faces of the finest level (side q = 2 d + hi): rfac = a h / (a h / 2 + b) per face,
 // braw = the face beta before that factor; nullptr for the other sides
 struct RobinFaces {
@@ -63,7 +64,17 @@ void mac_robin_apply(const CellGeom& g, int d, int hi, const double* braw, const
 // ap (cut cells): the face's aperture multiplies its beta
 void mac_set_beta(const CellGeom& g, int d, int source, const gbp_array4* src, double cval, int bclo, int bchi,
                   double* b64, float* b32, cudaStream_t st, const RobinFaces* rb = nullptr,
-                  const double* ap = nullptr);
+                  const double* ap = nullptr, double mult = 1.0);
+// ABecLaplacian (alpha a phi - beta div(b grad phi) = rhs on the same levels): a64 / a32 = alpha a V per
+// cell (a == nullptr: the constant a0), coarse levels the sum of their 8 fine cells; b = V rhs; the
+// Dirichlet boundary values (ghost cells of phi) moved onto b
+void abec_acoef(const CellGeom& g, const gbp_array4* a, double alpha, double a0, double* a64, float* a32,
+                cudaStream_t st);
+void abec_acoarsen(const CellGeom& gf, const CellGeom& gc, const double* af, double* ac64, float* ac32,
+                   cudaStream_t st);
+void abec_rhs(const CellGeom& g, const gbp_array4& rhs, double* b, cudaStream_t st);
+void abec_dirichlet(const CellGeom& g, int d, int hi, const double* beta, const gbp_array4& phi, double* b,
+                    cudaStream_t st);
 // copy the EB arrays into the padded layouts of eb (other padded positions 0)
 void mac_load_eb(const CellGeom& g, const gbp_array4& vfrac, const gbp_array4* const apf[3], const MacEB& eb,
                  cudaStream_t st);

@@ -45,6 +45,8 @@ void MacSolver::destroy()
     if (ev2) cudaEventDestroy(ev2);
     ev0 = ev1 = ev2 = nullptr;
     pool.release();
+    apool.release();
+    abec = false;
     eb.pool.release();
     eb = EbState{};
     L.clear();
@@ -206,6 +208,97 @@ int MacSolver::set_beta(int source, const gbp_array4* src[3], double cval)
     GBP_CUDA(cudaGetLastError());
     beta_ready = true;
     return GBP_OK;
+}
+
+int MacSolver::set_abec(double alpha, const gbp_array4* a, double a0, double beta, const gbp_array4* const b[3],
+                        double b0, const gbp_array4* eta_cc)
+{
+    if (eb.on) {
+        set_error("abec: cut cells are not supported by the ABecLaplacian form");
+        return GBP_BAD_ARG;
+    }
+    for (int d = 0; d < 3; ++d)
+        if (bclo[d] == GBP_BC_ROBIN || bchi[d] == GBP_BC_ROBIN) {
+            set_error("abec: Robin sides are not supported by the ABecLaplacian form");
+            return GBP_BAD_ARG;
+        }
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    if (alpha != 0.0) {
+        if (!apool.base) {
+            size_t need = 0;
+            for (auto& lv : L) need += ((lv.g.count * 12 + 255) & ~size_t(255)) + 512;
+            int rc = apool.reserve(need + 4096);
+            if (rc) return rc;
+            for (auto& lv : L) {
+                double* p64 = apool.take<double>(lv.g.count);
+                float* p32 = apool.take<float>(lv.g.count);
+                GBP_CUDA(cudaMemsetAsync(p64, 0, sizeof(double) * lv.g.count, st));
+                GBP_CUDA(cudaMemsetAsync(p32, 0, sizeof(float) * lv.g.count, st));
+                lv.g.a64 = p64;
+                lv.g.a32 = p32;
+            }
+        }
+        abec_acoef(L[0].g, a, alpha, a0, const_cast<double*>(L[0].g.a64), const_cast<float*>(L[0].g.a32), st);
+        for (size_t l = 1; l < L.size(); ++l)
+            abec_acoarsen(L[l - 1].g, L[l].g, L[l - 1].g.a64, const_cast<double*>(L[l].g.a64),
+                          const_cast<float*>(L[l].g.a32), st);
+        abec = true;
+    } else {
+        for (auto& lv : L) {
+            lv.g.a64 = nullptr;
+            lv.g.a32 = nullptr;
+        }
+        apool.release();
+        abec = false;
+    }
+    // face coefficients beta b (b arrays or the constant b0)
+    const bool arrays = b && b[0];
+    for (int d = 0; d < 3; ++d) {
+        if (eta_cc)
+            mac_set_beta(L[0].g, d, 3, eta_cc, 0.0, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st, &rb, nullptr, beta);
+        else
+            mac_set_beta(L[0].g, d, arrays ? 0 : 1, arrays ? b[d] : nullptr, arrays ? 0.0 : beta * b0, bclo[d],
+                         bchi[d], L[0].b64[d], L[0].b32[d], st, &rb, nullptr, arrays ? beta : 1.0);
+    }
+    for (size_t l = 1; l < L.size(); ++l)
+        for (int d = 0; d < 3; ++d)
+            mac_coarsen_beta(L[l - 1].g, L[l].g, d, L[l - 1].b64[d], L[l].b64[d], L[l].b32[d], st);
+    GBP_CUDA(cudaGetLastError());
+    beta_ready = true;
+    singular = !any_dirichlet && !abec;
+    return GBP_OK;
+}
+
+int MacSolver::abec_solve(const gbp_array4* rhs, gbp_array4* phi_io, gbp_stats* stats)
+{
+    if (!beta_ready) {
+        set_error("abec solve: coefficients were never set on this plan");
+        return GBP_BAD_ARG;
+    }
+    const MacLevel& l0 = L[0];
+    GBP_CUDA(cudaEventRecord(ev0, st));
+    abec_rhs(l0.g, *rhs, rhs0, st);
+    for (int d = 0; d < 3; ++d) {
+        if (bclo[d] == GBP_BC_DIRICHLET) abec_dirichlet(l0.g, d, 0, l0.b64[d], *phi_io, rhs0, st);
+        if (bchi[d] == GBP_BC_DIRICHLET) abec_dirichlet(l0.g, d, 1, l0.b64[d], *phi_io, rhs0, st);
+    }
+    if (singular) mac_remove_mean(l0.g, rhs0, partials, 0, st);
+    GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
+    mac_load_phi(l0.g, *phi_io, phi, st);
+    GBP_CUDA(cudaGetLastError());
+    int status = solve(true, stats);
+    if (status != GBP_OK && status != GBP_NOT_CONVERGED) return status;
+    mac_store_phi(l0.g, *phi_io, phi, st);
+    GBP_CUDA(cudaEventRecord(ev2, st));
+    GBP_CUDA(cudaGetLastError());
+    if (stats) {
+        GBP_CUDA(cudaEventSynchronize(ev2));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev0, ev2);
+        stats->ms_total = ms;
+    }
+    return status;
 }
 
 void MacSolver::eb_refresh_beta()

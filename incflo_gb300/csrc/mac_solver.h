@@ -36,6 +36,16 @@ public:
     // face betas must be set again afterwards.
     int set_eb(const gbp_array4* vfrac, const gbp_array4* const area[3], const gbp_array4* const fcent[3]);
     bool has_eb() const { return eb.on; }
+    // ABecLaplacian on the same levels (MLABecLaplacian::setScalars / setACoeffs / setBCoeffs):
+    // alpha a phi - beta div(b grad phi) = rhs; a == nullptr: the constant a0; b == nullptr: the
+    // constant b0. alpha = 0 gives back the plain Poisson operator of the projections.
+    // eta_cc (instead of b): b = the face average of this cell field (incflo's
+    // average_scalar_eta_to_faces)
+    int set_abec(double alpha, const gbp_array4* a, double a0, double beta, const gbp_array4* const b[3], double b0,
+                 const gbp_array4* eta_cc = nullptr);
+    // MLMG::solve(phi, rhs, rtol, atol) with setLevelBC(0, &phi): phi (cells, one ghost layer on the
+    // Dirichlet sides, whose ghost cells hold the boundary values) is the initial guess and the result
+    int abec_solve(const gbp_array4* rhs, gbp_array4* phi, gbp_stats* stats);
     int project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats);
     size_t device_bytes() const { return pool.bytes; }
 
@@ -68,6 +78,8 @@ private:
     bool any_dirichlet = false;  // a Dirichlet side exists (the system is nonsingular)
     bool robin_ready = false;
     unsigned* dflags = nullptr;
+    DevicePool apool;  // alpha a V per level (ABecLaplacian)
+    bool abec = false;
     struct EbState {
         DevicePool pool;
         MacEB m{};

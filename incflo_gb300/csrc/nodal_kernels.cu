@@ -568,9 +568,7 @@ __global__ void __launch_bounds__(256) k_sigma_from_rho(NodalGeom g, gbp_array4 
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
     if (i >= g.n[0] || j >= g.n[1] || k >= g.n[2]) return;
-    // sigma = s / rho with a Newton reciprocal: the IEEE FP64 division would bound this kernel by the
-    // FP64 pipe
-    const double v = have_rho ? scale * recip_newton(a4(rho, i, j, k, 0)) : scale / rho0;
+    const double v = have_rho ? scale / a4(rho, i, j, k, 0) : scale / rho0;
     put_sigma_cell(s64, g, i, j, k, v);
     if (s32) put_sigma_cell(s32, g, i, j, k, (float)v);
 }

@@ -46,6 +46,7 @@ def main():
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--unet", type=int, default=0, help="time the U-Net forward on an n x n x (n+8) grid")
     ap.add_argument("--project", default="", choices=["", "mixed", "fp64"])
+    ap.add_argument("--opt", action="append", default=[], help="option override key=value (projection mode)")
     args = ap.parse_args()
     from incflo_gb300.build import build
 
@@ -54,7 +55,7 @@ def main():
     if args.unet:
         return unet_forward(args.unet, args.reps)
     if args.project:
-        return projections(args.n, args.project, args.reps)
+        return projections(args.n, args.project, args.reps, args.opt)
     n = args.n
     rho = synth.variable_density_rt(n)["rho"]
     geom = Geometry((n, n, n))
@@ -67,7 +68,7 @@ def main():
                       "GBps": by.value / ms.value / 1e6}))
 
 
-def projections(n, form, reps):
+def projections(n, form, reps, extra=()):
     from incflo_gb300 import apply_nodal_projection, make_options
 
     w = synth.variable_density_rt(n)
@@ -77,7 +78,7 @@ def projections(n, form, reps):
     vel = vel0.clone()
     gp = torch.zeros((3,) + rho.shape, dtype=torch.float64, device="cuda")
     p_nd = torch.zeros((n + 1, n + 1, n + 1), dtype=torch.float64, device="cuda")
-    opts = make_options(0, precision=form, mg_rtol=1e-10, mg_atol=0.0)
+    opts = make_options(0, precision=form, mg_rtol=1e-10, mg_atol=0.0, **dict(kv.split("=", 1) for kv in extra))
     out = []
     for _ in range(reps):
         vel.copy_(vel0)

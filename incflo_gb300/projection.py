@@ -317,13 +317,17 @@ class AmrNodalProjector:
     def device_bytes(self) -> int:
         return int(A.load().gbp_amr_device_bytes(self.ptr))
 
-    def _boxes4(self, tensors, nodal=False):
+    def _boxes4(self, tensors):
+        """(keep-alive, argument): the C ABI takes an array of nbox pointers to gbp_array4."""
         if tensors is None:
             return None, None
+        if len(tensors) != len(self.boxes):
+            raise ValueError("one tensor per fine box is required")
         arr = (A.Array4 * len(self.boxes))()
         for b, t in enumerate(tensors):
             arr[b] = array4(t, 0, lo=self.boxes[b][0])
-        return arr, ctypes.cast(arr, ctypes.POINTER(A.Array4))
+        ptrs = (ctypes.POINTER(A.Array4) * len(self.boxes))(*[ctypes.pointer(arr[b]) for b in range(len(self.boxes))])
+        return (arr, ptrs), ptrs
 
     def apply(self, vel_c, density_c, gp_c, p_c, vel_f, density_f, gp_f, p_f, *, scaling_factor=1.0,
               incremental=False, vel_old_c=None, vel_old_f=None, rho0=1.0, constant_density=False):

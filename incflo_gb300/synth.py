@@ -104,3 +104,28 @@ def double_shear_layer(n=128, seed=None, amp_noise=0.0):
 def with_ghosts(vel, ng=1):
     """Pad a (3, nz, ny, nx) cell field with ng zero ghost layers (the state after setBndry(0))."""
     return np.pad(vel, ((0, 0),) + ((ng, ng),) * 3)
+
+
+def variable_density_rt_amr(n=256, band=(0.375, 0.625), box=64, seed_h=2, seed_u=3, rho_lo=1.0, rho_hi=3.0):
+    """Two-level form of variable_density_rt: the base level as above plus a refined (ratio 2) band of
+    whole-domain x/y extent around the interface, z in `band`, split into box^3 fine boxes (the fine
+    BoxArray, max_grid_size = box). Fine density from the same interface at the fine resolution; fine
+    velocity injected from the base level (a freshly regridded level). Returns the base fields, the
+    fine boxes [(lo, hi)] and the fine band arrays (band origin at fine z index zlo)."""
+    base = variable_density_rt(n, seed_h, seed_u, rho_lo, rho_hi)
+    nn = base["n"]
+    nf = tuple(2 * v for v in nn)
+    zlo = int(round(band[0] * nf[2])) // box * box
+    zhi = int(round(band[1] * nf[2])) // box * box
+    dz = 1.0 / nf[2]
+    z = (np.arange(zlo, zhi) + 0.5) * dz
+    hxy = interface_height(nf, seed_h)
+    rho_f = rho_lo + (rho_hi - rho_lo) * 0.5 * (1.0 + np.tanh((z[:, None, None] - hxy[None, :, :]) / (2.0 * dz)))
+    vc = base["vel"][:, zlo // 2:zhi // 2]
+    vel_f = np.repeat(np.repeat(np.repeat(vc, 2, axis=1), 2, axis=2), 2, axis=3)
+    boxes = []
+    for k in range(zlo, zhi, box):
+        for j in range(0, nf[1], box):
+            for i in range(0, nf[0], box):
+                boxes.append(((i, j, k), (i + box - 1, j + box - 1, k + box - 1)))
+    return dict(base=base, boxes=boxes, zlo=zlo, rho_f=rho_f, vel_f=np.ascontiguousarray(vel_f))

@@ -230,6 +230,26 @@ int gbp_mac_set_beta_from_density(gbp_plan* plan, const gbp_array4* rho, double 
 int gbp_mac_project(gbp_plan* plan, gbp_array4* umac_x, gbp_array4* umac_y, gbp_array4* umac_z,
                     gbp_array4* phi, int phi_guess, gbp_stats* stats);
 
+/* ---- cell-centred ABecLaplacian solve (scalar diffusion) ---------------------------------
+ * The implicit scalar diffusion of DiffusionScalarOp::diffuse_scalar
+ * (src/diffusion/DiffusionScalarOp.cpp:150-327): MLABecLaplacian alpha a phi - beta div(b grad phi) =
+ * rhs (setScalars :193-195, setACoeffs :197-202, setBCoeffs with the face-averaged eta :251-252,
+ * setLevelBC(lev, &phi) :295) solved by MLMG (:306-326), on a MAC plan (same levels, boundary types,
+ * options: mg_rtol / mg_atol / maxiter / precision). Dirichlet sides take their boundary values from
+ * the ghost cells of phi (the value on the face, linear extrapolation: maxorder 2 as incflo sets it);
+ * Neumann sides are homogeneous; Robin sides and cut cells are rejected.
+ * gbp_abec_set_coeffs: a (cells) or the constant a0 when a == NULL; b (face arrays of each direction)
+ * or the constant b0 when bx == NULL; alpha = 0 restores the plan's Poisson operator.
+ * gbp_abec_solve: rhs (cells); phi (cells, one ghost layer on Dirichlet sides) is the initial guess and
+ * receives the solution. */
+int gbp_abec_set_coeffs(gbp_plan* plan, double alpha, const gbp_array4* a, double a0, double beta,
+                        const gbp_array4* bx, const gbp_array4* by, const gbp_array4* bz, double b0);
+int gbp_abec_solve(gbp_plan* plan, const gbp_array4* rhs, gbp_array4* phi, gbp_stats* stats);
+/* setBCoeffs(incflo::average_scalar_eta_to_faces(eta)) (src/diffusion/incflo_diffusion.cpp:289-343):
+ * b = the face average of the cell field eta, the adjacent cell's eta on non-periodic domain sides. */
+int gbp_abec_set_coeffs_eta(gbp_plan* plan, double alpha, const gbp_array4* a, double a0, double beta,
+                            const gbp_array4* eta);
+
 /* ---- two-level (AMR) composite nodal projection ----------------------------------------
  * incflo::ApplyNodalProjection(density, time, scaling_factor, incremental) over finest_level = 1
  * (src/projection/incflo_apply_nodal_projection.cpp:95-267): one NodalProjector over both levels
