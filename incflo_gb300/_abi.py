@@ -27,7 +27,9 @@ EXPORTS = (
     "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc", "gbp_nodal_set_overset_mask",
     "gbp_mac_set_robin", "gbp_mac_set_eb", "gbp_average_down",
     "gbp_amr_create", "gbp_amr_destroy", "gbp_amr_set_options", "gbp_amr_device_bytes",
-    "gbp_amr_apply_nodal_projection", "gbp_abec_set_coeffs", "gbp_abec_solve", "gbp_abec_set_coeffs_eta", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
+    "gbp_amr_apply_nodal_projection", "gbp_abec_set_coeffs", "gbp_abec_solve", "gbp_abec_set_coeffs_eta", "gbp_nodal_set_eb", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
+    "gbp_tensor_create", "gbp_tensor_destroy", "gbp_tensor_set_options", "gbp_tensor_device_bytes",
+    "gbp_tensor_set_coeffs", "gbp_tensor_solve", "gbp_tensor_apply",
     "gbp_nn_conv3d", "gbp_nn_conv3d_wgrad",
     "gbp_surrogate_create", "gbp_surrogate_destroy", "gbp_surrogate_num_params", "gbp_surrogate_get_params",
     "gbp_surrogate_set_params", "gbp_surrogate_get_grads", "gbp_surrogate_save", "gbp_surrogate_load",
@@ -158,12 +160,21 @@ def load(path: str = LIB_PATH):
         "gbp_abec_set_coeffs": (i, [P, d, A4, d, d, A4, A4, A4, d]),
         "gbp_abec_solve": (i, [P, A4, A4, ctypes.POINTER(Stats)]),
         "gbp_abec_set_coeffs_eta": (i, [P, d, A4, d, d, A4]),
+        "gbp_nodal_set_eb": (i, [P, A4]),
         "gbp_amr_set_options": (i, [P, ctypes.POINTER(Options)]),
         "gbp_amr_device_bytes": (ctypes.c_size_t, [P]),
         "gbp_amr_apply_nodal_projection": (i, [P, A4, A4, A4, A4, A4, ctypes.POINTER(A4), ctypes.POINTER(A4),
                                                ctypes.POINTER(A4), ctypes.POINTER(A4), ctypes.POINTER(A4), d, d, i,
                                                ctypes.POINTER(Stats)]),
         "gbp_nodal_set_overset_mask": (i, [P, ctypes.POINTER(IArray4)]),
+        "gbp_tensor_create": (i, [ctypes.POINTER(Geometry), ctypes.POINTER(ctypes.c_int),
+                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(Options), P, ctypes.POINTER(P)]),
+        "gbp_tensor_destroy": (i, [P]),
+        "gbp_tensor_set_options": (i, [P, ctypes.POINTER(Options)]),
+        "gbp_tensor_device_bytes": (ctypes.c_size_t, [P]),
+        "gbp_tensor_set_coeffs": (i, [P, d, A4, d, d, A4, A4, A4, A4, d]),
+        "gbp_tensor_solve": (i, [P, A4, A4, ctypes.POINTER(Stats)]),
+        "gbp_tensor_apply": (i, [P, A4, A4]),
         "gbp_average_down": (i, [A4, A4, ctypes.POINTER(ctypes.c_int), i, ctypes.POINTER(ctypes.c_int),
                                  ctypes.POINTER(ctypes.c_int), P]),
         "gbp_apply_cc_projection": (i, [P, A4, A4, A4, d, A4, A4, A4, A4, A4, d, d, d, d, i, i,

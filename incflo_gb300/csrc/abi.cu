@@ -14,6 +14,7 @@
 #include "nodal_solver.h"
 #include "plan.h"
 #include "amr.h"
+#include "tensor.h"
 #include "cc_projection.h"
 #include "solvability.h"
 
@@ -764,6 +765,19 @@ int gbp_plan_time_kernel(gbp_plan* p, int which, int reps, double* ms_per_launch
     return p->nodal->time_kernel(which, reps, ms_per_launch, bytes_per_launch);
 }
 
+int gbp_nodal_set_eb(gbp_plan* p, const gbp_array4* moments)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_nodal_set_eb: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    if (moments && moments->data && !valid_array(moments, 27)) {
+        set_error("gbp_nodal_set_eb: the moments array needs 27 components");
+        return GBP_BAD_ARG;
+    }
+    return p->nodal->set_eb((moments && moments->data) ? moments : nullptr);
+}
+
 int gbp_abec_set_coeffs(gbp_plan* p, double alpha, const gbp_array4* a, double a0, double beta,
                         const gbp_array4* bx, const gbp_array4* by, const gbp_array4* bz, double b0)
 {
@@ -828,6 +842,96 @@ int gbp_abec_solve(gbp_plan* p, const gbp_array4* rhs, gbp_array4* phi, gbp_stat
     }
     if (stats) memset(stats, 0, sizeof(*stats));
     return p->mac->abec_solve(rhs, phi, stats);
+}
+
+struct gbp_tensor {
+    gbp::TensorSolver* t = nullptr;
+};
+
+int gbp_tensor_create(const gbp_geometry* geom, const int bc_lo[9], const int bc_hi[9], const gbp_options* opt,
+                      void* stream, gbp_tensor** out)
+{
+    if (!geom || !bc_lo || !bc_hi || !out) {
+        set_error("gbp_tensor_create: geometry, boundary types and the output handle are required");
+        return GBP_BAD_ARG;
+    }
+    *out = nullptr;
+    gbp_options o;
+    if (opt)
+        o = *opt;
+    else
+        gbp_options_default(GBP_MAC, &o);
+    gbp_tensor* h = new (std::nothrow) gbp_tensor;
+    if (!h) return GBP_BAD_ARG;
+    h->t = new (std::nothrow) gbp::TensorSolver;
+    if (!h->t) {
+        delete h;
+        return GBP_BAD_ARG;
+    }
+    int rc = h->t->init(*geom, bc_lo, bc_hi, o, static_cast<cudaStream_t>(stream));
+    if (rc) {
+        gbp_tensor_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return GBP_OK;
+}
+
+int gbp_tensor_destroy(gbp_tensor* h)
+{
+    if (!h) return GBP_OK;
+    delete h->t;
+    delete h;
+    return GBP_OK;
+}
+
+int gbp_tensor_set_options(gbp_tensor* h, const gbp_options* opt)
+{
+    if (!h || !opt) return GBP_BAD_ARG;
+    return h->t->set_options(*opt);
+}
+
+size_t gbp_tensor_device_bytes(const gbp_tensor* h) { return h ? h->t->device_bytes() : 0; }
+
+int gbp_tensor_set_coeffs(gbp_tensor* h, double alpha, const gbp_array4* a, double a0, double beta,
+                          const gbp_array4* eta_cc, const gbp_array4* eta_x, const gbp_array4* eta_y,
+                          const gbp_array4* eta_z, double eta0)
+{
+    if (!h) {
+        set_error("gbp_tensor_set_coeffs: null handle");
+        return GBP_BAD_ARG;
+    }
+    if ((a && !valid_array(a, 1)) || (eta_cc && !valid_array(eta_cc, 1))) {
+        set_error("gbp_tensor_set_coeffs: invalid a or eta array");
+        return GBP_BAD_ARG;
+    }
+    const bool faces = eta_x && eta_y && eta_z;
+    if (!eta_cc && (eta_x || eta_y || eta_z) && !(faces && valid_array(eta_x, 1) && valid_array(eta_y, 1) &&
+                                                   valid_array(eta_z, 1))) {
+        set_error("gbp_tensor_set_coeffs: give all three eta face arrays or none");
+        return GBP_BAD_ARG;
+    }
+    const gbp_array4* ef[3] = {eta_x, eta_y, eta_z};
+    return h->t->set_coeffs(alpha, a, a0, beta, eta_cc, (!eta_cc && faces) ? ef : nullptr, eta0);
+}
+
+int gbp_tensor_solve(gbp_tensor* h, const gbp_array4* rhs, gbp_array4* vel, gbp_stats* stats)
+{
+    if (!h || !rhs || !vel) {
+        set_error("gbp_tensor_solve: handle, rhs and vel are required");
+        return GBP_BAD_ARG;
+    }
+    if (stats) memset(stats, 0, sizeof(*stats));
+    return h->t->solve(*rhs, *vel, stats);
+}
+
+int gbp_tensor_apply(gbp_tensor* h, const gbp_array4* vel, gbp_array4* divtau)
+{
+    if (!h || !vel || !divtau) {
+        set_error("gbp_tensor_apply: handle, vel and divtau are required");
+        return GBP_BAD_ARG;
+    }
+    return h->t->apply(*vel, *divtau);
 }
 
 struct gbp_amr {

@@ -211,7 +211,7 @@ int MacSolver::set_beta(int source, const gbp_array4* src[3], double cval)
 }
 
 int MacSolver::set_abec(double alpha, const gbp_array4* a, double a0, double beta, const gbp_array4* const b[3],
-                        double b0, const gbp_array4* eta_cc)
+                        double b0, const gbp_array4* eta_cc, const double* bscale)
 {
     if (eb.on) {
         set_error("abec: cut cells are not supported by the ABecLaplacian form");
@@ -255,11 +255,13 @@ int MacSolver::set_abec(double alpha, const gbp_array4* a, double a0, double bet
     // face coefficients beta b (b arrays or the constant b0)
     const bool arrays = b && b[0];
     for (int d = 0; d < 3; ++d) {
+        const double f = bscale ? bscale[d] : 1.0;
         if (eta_cc)
-            mac_set_beta(L[0].g, d, 3, eta_cc, 0.0, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st, &rb, nullptr, beta);
+            mac_set_beta(L[0].g, d, 3, eta_cc, 0.0, bclo[d], bchi[d], L[0].b64[d], L[0].b32[d], st, &rb, nullptr,
+                         beta * f);
         else
-            mac_set_beta(L[0].g, d, arrays ? 0 : 1, arrays ? b[d] : nullptr, arrays ? 0.0 : beta * b0, bclo[d],
-                         bchi[d], L[0].b64[d], L[0].b32[d], st, &rb, nullptr, arrays ? beta : 1.0);
+            mac_set_beta(L[0].g, d, arrays ? 0 : 1, arrays ? b[d] : nullptr, arrays ? 0.0 : beta * b0 * f, bclo[d],
+                         bchi[d], L[0].b64[d], L[0].b32[d], st, &rb, nullptr, arrays ? beta * f : 1.0);
     }
     for (size_t l = 1; l < L.size(); ++l)
         for (int d = 0; d < 3; ++d)
@@ -299,6 +301,22 @@ int MacSolver::abec_solve(const gbp_array4* rhs, gbp_array4* phi_io, gbp_stats* 
         stats->ms_total = ms;
     }
     return status;
+}
+
+void MacSolver::add_vcycle_correction(const double* r, double* e, double sc)
+{
+    const MacLevel& l0 = L[0];
+    cap_or_st = st;
+    if (opt.precision == GBP_PREC_MIXED) {
+        mac_to_f32(l0.g, r, l0.rhs32, sc, st);
+        vcycle<float>(0, l0.rhs32, true);
+        for (int c = 1; c < opt.ir_inner_cycles; ++c) vcycle<float>(0, l0.rhs32, false);
+        mac_add_correction<float>(l0.g, e, l0.x32, 1.0 / sc, st);
+    } else {
+        vcycle<double>(0, r, true);
+        for (int c = 1; c < opt.ir_inner_cycles; ++c) vcycle<double>(0, r, false);
+        mac_add_correction<double>(l0.g, e, l0.x64, 1.0, st);
+    }
 }
 
 void MacSolver::eb_refresh_beta()

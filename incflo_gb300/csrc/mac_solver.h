@@ -41,12 +41,19 @@ public:
     // constant b0. alpha = 0 gives back the plain Poisson operator of the projections.
     // eta_cc (instead of b): b = the face average of this cell field (incflo's
     // average_scalar_eta_to_faces)
+    // bscale (optional): a factor on b per face direction (the tensor solve's 4/3 on the normal faces)
     int set_abec(double alpha, const gbp_array4* a, double a0, double beta, const gbp_array4* const b[3], double b0,
-                 const gbp_array4* eta_cc = nullptr);
+                 const gbp_array4* eta_cc = nullptr, const double* bscale = nullptr);
     // MLMG::solve(phi, rhs, rtol, atol) with setLevelBC(0, &phi): phi (cells, one ghost layer on the
     // Dirichlet sides, whose ghost cells hold the boundary values) is the initial guess and the result
     int abec_solve(const gbp_array4* rhs, gbp_array4* phi, gbp_stats* stats);
     int project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats);
+    // for a solver that uses this operator as one block of a preconditioner (the tensor solve): the
+    // finest level, and e += the inner V-cycles of A e = r from zero (r in the finest padded layout,
+    // homogeneous boundaries; FP32 V-cycles on r * scale32 in the mixed form)
+    const CellGeom& finest() const { return L[0].g; }
+    const gbp_options& options() const { return opt; }
+    void add_vcycle_correction(const double* r, double* e, double scale32_);
     size_t device_bytes() const { return pool.bytes; }
 
 private:

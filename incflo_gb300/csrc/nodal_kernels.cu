@@ -357,7 +357,7 @@ template <typename T>
 __global__ void __launch_bounds__(1024) k_bottom_cg(NodalGeom g, const double* __restrict__ s,
                                                     const T* __restrict__ bin, T* __restrict__ xout,
                                                     double* __restrict__ scr, int maxiter, double rtol,
-                                                    double atol, int* info)
+                                                    double atol, int* info, int singular)
 {
     __shared__ double red[32];
     const long long P = g.count;
@@ -367,8 +367,8 @@ __global__ void __launch_bounds__(1024) k_bottom_cg(NodalGeom g, const double* _
     double* q = scr + 3 * P;
     double* dg = scr + 4 * P;
     const long long N = (long long)g.nu[0] * g.nu[1] * g.nu[2];
-    // an overset mask (set only when it holds at least one 0) pins phi like a Dirichlet face
-    const bool singular = !(g.dlo[0] || g.dhi[0] || g.dlo[1] || g.dhi[1] || g.dlo[2] || g.dhi[2]) && !g.mask;
+    // singular: no Dirichlet side and no pinning mask (the caller knows whether the level's mask pins phi
+    // or only takes out nodes that touch no fluid)
 
     // clear the scratch (padding must hold zeros for the stencil)
     for (long long t = threadIdx.x; t < 5 * P; t += blockDim.x) scr[t] = 0.0;
@@ -394,14 +394,14 @@ __global__ void __launch_bounds__(1024) k_bottom_cg(NodalGeom g, const double* _
         for (long long t = threadIdx.x; t < N; t += blockDim.x) {
             int i, j, k;
             decode_node(g, t, i, j, k);
-            vtot += node_volume(g, i, j, k);
+            if (!node_is_dirichlet(g, i, j, k)) vtot += node_volume(g, i, j, k);
         }
         vtot = block_sum(vtot, red);
-        double cfac = tot / vtot;
+        double cfac = vtot > 0.0 ? tot / vtot : 0.0;
         for (long long t = threadIdx.x; t < N; t += blockDim.x) {
             int i, j, k;
             decode_node(g, t, i, j, k);
-            r[pidx(g.sy, g.sz, i, j, k)] -= cfac * node_volume(g, i, j, k);
+            if (!node_is_dirichlet(g, i, j, k)) r[pidx(g.sy, g.sz, i, j, k)] -= cfac * node_volume(g, i, j, k);
         }
     }
     __syncthreads();
@@ -490,20 +490,22 @@ __global__ void __launch_bounds__(256) k_bottom_dense(NodalGeom g, const double*
     for (int t = threadIdx.x; t < N; t += blockDim.x) {
         int i, j, k;
         decode_node(g, t, i, j, k);
-        const double v = node_is_dirichlet(g, i, j, k) ? 0.0 : (double)bin[pidx(g.sy, g.sz, i, j, k)];
+        const bool held = node_is_dirichlet(g, i, j, k);
+        const double v = held ? 0.0 : (double)bin[pidx(g.sy, g.sz, i, j, k)];
         bb[t] = v;
         part += v;
-        vpart += node_volume(g, i, j, k);
+        if (!held) vpart += node_volume(g, i, j, k);
     }
     if (singular) {
-        // consistent right-hand side: remove the component along the constants
+        // consistent right-hand side: remove the component along the constants of the free nodes
+        // (masked nodes that touch no fluid are outside the system and keep 0)
         const double s = block_sum_all(part);
         const double vs = block_sum_all(vpart);
-        const double c = s / vs;
+        const double c = vs > 0.0 ? s / vs : 0.0;
         for (int t = threadIdx.x; t < N; t += blockDim.x) {
             int i, j, k;
             decode_node(g, t, i, j, k);
-            bb[t] -= c * node_volume(g, i, j, k);
+            if (!node_is_dirichlet(g, i, j, k)) bb[t] -= c * node_volume(g, i, j, k);
         }
     }
     __syncthreads();
@@ -852,7 +854,7 @@ __global__ void __launch_bounds__(ZTX* ZTY) k_nodal_correct(NodalGeom g, CorrArg
         D[buf][ty][tx] = phi_hi - plo;
         plo = phi_hi;
         __syncthreads();
-        if (cell) {
+        if (cell && (!a.cmask || a.cmask[pk])) {
             const double S00 = S[buf][ty][tx], S10 = S[buf][ty][tx + 1], S01 = S[buf][ty + 1][tx],
                          S11 = S[buf][ty + 1][tx + 1];
             const double D00 = D[buf][ty][tx], D10 = D[buf][ty][tx + 1], D01 = D[buf][ty + 1][tx],
@@ -1001,9 +1003,9 @@ void nodal_prolong_add(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T*
 
 template <typename T>
 void nodal_bottom(const NodalGeom& g, const double* s64, const T* b, T* x, double* scratch, int maxiter,
-                  double rtol, double atol, int* info, cudaStream_t st)
+                  double rtol, double atol, int* info, int singular, cudaStream_t st)
 {
-    k_bottom_cg<T><<<1, 1024, 0, st>>>(g, s64, b, x, scratch, maxiter, rtol, atol, info);
+    k_bottom_cg<T><<<1, 1024, 0, st>>>(g, s64, b, x, scratch, maxiter, rtol, atol, info, singular);
 }
 
 template void nodal_jacobi<double>(const NodalGeom&, const double*, const double*, const double*, double*, double,
@@ -1019,9 +1021,9 @@ template void nodal_restrict<float>(const NodalGeom&, const NodalGeom&, const fl
 template void nodal_prolong_add<double>(const NodalGeom&, const NodalGeom&, const double*, double*, cudaStream_t);
 template void nodal_prolong_add<float>(const NodalGeom&, const NodalGeom&, const float*, float*, cudaStream_t);
 template void nodal_bottom<double>(const NodalGeom&, const double*, const double*, double*, double*, int, double,
-                                   double, int*, cudaStream_t);
+                                   double, int*, int, cudaStream_t);
 template void nodal_bottom<float>(const NodalGeom&, const double*, const float*, float*, double*, int, double,
-                                  double, int*, cudaStream_t);
+                                  double, int*, int, cudaStream_t);
 
 void nodal_sigma_from_rho(const NodalGeom& g, const gbp_array4* rho, double scale, double rho0, double* s64,
                           float* s32, cudaStream_t st)

@@ -30,6 +30,7 @@ struct CorrArgs {
     int add_gp;
     int incremental;
     double inv4h[3];
+    const unsigned char* cmask;  // cells to update (padded cell layout), nullptr = all
 };
 
 template <typename T>
@@ -44,7 +45,7 @@ template <typename T>
 void nodal_prolong_add(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T* xf, cudaStream_t st);
 template <typename T>
 void nodal_bottom(const NodalGeom& g, const double* s64, const T* b, T* x, double* scratch, int maxiter,
-                  double rtol, double atol, int* info, cudaStream_t st);
+                  double rtol, double atol, int* info, int singular, cudaStream_t st);
 
 template <typename T>
 void nodal_bottom_dense(const NodalGeom& g, const double* M, const T* b, T* x, int singular, cudaStream_t st);

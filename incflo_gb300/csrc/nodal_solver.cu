@@ -112,6 +112,11 @@ void NodalSolver::destroy()
     net_x0_bytes = 0;
     net = nullptr;
     if (pool.base) sweep_forget_maps(pool.base, pool.bytes);
+    eb.pool.release();
+    eb = EbState{};
+    auxpool.release();
+    umask8 = nullptr;
+    user_zeros = 0;
     pool.release();
     L.clear();
     sigma_ready = false;
@@ -236,6 +241,7 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
         lv.mask8 = pool.take<unsigned char>(lv.g.count);
     }
     singular_faces = singular;
+    bsing = singular;
     phi = pool.take<double>(G0.count);
     rhs0 = pool.take<double>(G0.count);
     res = pool.take<double>(G0.count);
@@ -268,19 +274,26 @@ int NodalSolver::set_sigma_from_density(const gbp_array4* rho, double scale, dou
         return GBP_BAD_ARG;
     }
     nodal_sigma_from_rho(L[0].g, rho, scale, rho0, L[0].s64, L[0].s32, st);
-    for (size_t l = 1; l < L.size(); ++l)
-        nodal_sigma_coarsen(L[l - 1].g, L[l].g, L[l - 1].s64, L[l].s64, L[l].s32, st);
-    nk += (long long)L.size();
-    GBP_CUDA(cudaGetLastError());
-    sigma_ready = true;
-    return build_bottom();
+    return finish_sigma();
 }
 
 int NodalSolver::set_sigma(const gbp_array4* sigma, double cval)
 {
     nodal_sigma_copy(L[0].g, sigma, cval, L[0].s64, L[0].s32, st);
+    return finish_sigma();
+}
+
+// level 0 holds the caller's sigma: with cut cells keep it aside, leave it on the regular cells only and
+// coarsen sigma x volume fraction; then the coarse levels and the bottom
+int NodalSolver::finish_sigma()
+{
+    const double* src0 = L[0].s64;
+    if (eb.on) {
+        eb_sigma(L[0].g, eb.e, L[0].s64, L[0].s64, L[0].s32, L[0].t64, st);
+        src0 = L[0].t64;
+    }
     for (size_t l = 1; l < L.size(); ++l)
-        nodal_sigma_coarsen(L[l - 1].g, L[l].g, L[l - 1].s64, L[l].s64, L[l].s32, st);
+        nodal_sigma_coarsen(L[l - 1].g, L[l].g, l == 1 ? src0 : L[l - 1].s64, L[l].s64, L[l].s32, st);
     nk += (long long)L.size();
     GBP_CUDA(cudaGetLastError());
     sigma_ready = true;
@@ -347,7 +360,7 @@ int NodalSolver::build_bottom()
                                     }
                         }
             }
-    if (singular) {
+    if (bsing) {
         double tr = 0.0;
         for (int u = 0; u < N; ++u) tr += A[(size_t)u * N + u];
         const double c = tr / ((double)N * N);
@@ -406,10 +419,10 @@ void NodalSolver::bottom<double>(int l, const double* b, double* x)
 {
     const NodalLevel& lv = L[l];
     if (dense_bottom)
-        nodal_bottom_dense<double>(lv.g, dmat, b, x, singular ? 1 : 0, cap_or_st);
+        nodal_bottom_dense<double>(lv.g, dmat, b, x, bsing ? 1 : 0, cap_or_st);
     else
         nodal_bottom<double>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
-                             cap_or_st);
+                             bsing ? 1 : 0, cap_or_st);
     xres[l] = x;
 }
 
@@ -418,10 +431,10 @@ void NodalSolver::bottom<float>(int l, const float* b, float* x)
 {
     const NodalLevel& lv = L[l];
     if (dense_bottom)
-        nodal_bottom_dense<float>(lv.g, dmat, b, x, singular ? 1 : 0, cap_or_st);
+        nodal_bottom_dense<float>(lv.g, dmat, b, x, bsing ? 1 : 0, cap_or_st);
     else
         nodal_bottom<float>(lv.g, lv.s64, b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol, opt.bottom_atol, dinfo,
-                            cap_or_st);
+                            bsing ? 1 : 0, cap_or_st);
     xres[l] = x;
 }
 
@@ -488,9 +501,12 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     T* x = zero ? B::x(lv) : (T*)xres[l];
     T* t = (x == B::x(lv)) ? B::t(lv) : B::x(lv);
     int pre = opt.nu1;
+    // cut cells (finest level): the EB nodes are recomputed from the same input after each sweep
+    const bool cut = l == 0 && eb.on;
     if (zero) {
         if (pre > 0) {
             nodal_jacobi<T>(lv.g, B::s(lv), nullptr, b, x, opt.omega, true, s);
+            if (cut) eb_nodes<T>(lv.g, eb.e, 0, nullptr, b, x, opt.omega, s);
             ++nk;
             --pre;
         } else {
@@ -499,10 +515,12 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     }
     for (int q = 0; q < pre; ++q) {
         jacobi<T>(lv.g, B::s(lv), x, b, t, s);
+        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, opt.omega, s);
         ++nk;
         std::swap(x, t);
     }
     resid<T>(lv.g, B::s(lv), x, b, B::r(lv), nullptr, s);
+    if (cut) eb_nodes<T>(lv.g, eb.e, 1, x, b, B::r(lv), opt.omega, s);
     const NodalLevel& cv = L[l + 1];
     nodal_restrict<T>(lv.g, cv.g, B::r(lv), B::b(cv), s);
     nk += 2;
@@ -511,10 +529,24 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     ++nk;
     for (int q = 0; q < opt.nu2; ++q) {
         jacobi<T>(lv.g, B::s(lv), x, b, t, s);
+        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, opt.omega, s);
         ++nk;
         std::swap(x, t);
     }
     xres[l] = x;
+}
+
+// FP64 residual r = b - A x of level 0 with its max norm (into *norm when given)
+void NodalSolver::resid0(const double* x, const double* b, double* r, unsigned long long* norm, cudaStream_t s)
+{
+    const NodalLevel& l0 = L[0];
+    if (!eb.on) {
+        resid<double>(l0.g, l0.s64, x, b, r, norm, s);
+        return;
+    }
+    resid<double>(l0.g, l0.s64, x, b, r, nullptr, s);
+    eb_nodes<double>(l0.g, eb.e, 1, x, b, r, opt.omega, s);
+    if (norm) eb_norm(l0.g, r, eb.ivol, norm, s);
 }
 
 void NodalSolver::drop_graphs()
@@ -543,7 +575,7 @@ void NodalSolver::record_iteration(int m)
         nodal_add_correction<double>(l0.g, phi, (const double*)xres[0], 1.0, s);
     }
     cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), s);
-    resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, s);
+    resid0(phi, rhs0, res, dnorm + 1, s);
     nk += 2;
     cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
     step_kernels = nk - nk0;
@@ -625,7 +657,7 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
     GBP_CUDA(cudaMemsetAsync(derr, 0, sizeof(unsigned), st));
     launch_rc = 0;
     if (have_guess) {
-        resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
+        resid0(phi, rhs0, res, dnorm + 1, st);
         if (launch_rc) return launch_rc;
         ++nk;
     } else {
@@ -738,25 +770,339 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
 
 int NodalSolver::set_mask(const gbp_iarray4* m)
 {
-    unsigned zeros = 0;
+    user_zeros = 0;
     if (m && m->data) {
+        if (!umask8) {
+            int rc = auxpool.reserve(L[0].g.count + 4096);
+            if (rc) return rc;
+            umask8 = auxpool.take<unsigned char>(L[0].g.count);
+        }
         unsigned* dz = reinterpret_cast<unsigned*>(dscal + 7);
         GBP_CUDA(cudaMemsetAsync(dz, 0, sizeof(unsigned), st));
-        nodal_mask_load(L[0].g, *m, L[0].mask8, dz, st);
+        nodal_mask_load(L[0].g, *m, umask8, dz, st);
+        GBP_CUDA(cudaMemcpyAsync(&user_zeros, dz, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+    }
+    return rebuild_masks();
+}
+
+// Level masks from the user's overset mask (nodes held at 0, which pin phi; coarse levels by injection)
+// and the cut-cell geometry (nodes that touch no fluid on their own level, which do not pin phi).
+int NodalSolver::rebuild_masks()
+{
+    const bool um = umask8 && user_zeros > 0;
+    const bool em = eb.on && eb.has_inactive;
+    if (!um && !em) {
+        for (auto& lv : L) lv.g.mask = nullptr;
+    } else {
+        mask_and(L[0].g.count, um ? umask8 : nullptr, nullptr, L[0].mask8, st);
         L[0].g.mask = L[0].mask8;
         for (size_t l = 1; l < L.size(); ++l) {
             nodal_mask_coarsen(L[l - 1].g, L[l].g, L[l - 1].mask8, L[l].mask8, st);
             L[l].g.mask = L[l].mask8;
         }
-        GBP_CUDA(cudaMemcpyAsync(&zeros, dz, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-        GBP_CUDA(cudaStreamSynchronize(st));
+        if (em)
+            for (size_t l = 0; l < L.size(); ++l) mask_and(L[l].g.count, L[l].mask8, eb.active8[l], L[l].mask8, st);
+        GBP_CUDA(cudaGetLastError());
     }
-    if (zeros == 0)  // no masked node: the plain operator (and its null space) stays
-        for (auto& lv : L) lv.g.mask = nullptr;
-    // the level geometries (captured by value in the graphs) changed, and a masked node pins phi
-    singular = singular_faces && zeros == 0;
+    // nodes that touch no fluid are decoupled on every level (their cells hold no fluid there), so the
+    // cut-cell system keeps the constant null space of its free nodes down to the bottom
+    singular = singular_faces && !um;
+    bsing = singular;
+    // the level geometries (captured by value in the graphs) changed
     drop_graphs();
     return sigma_ready ? build_bottom() : GBP_OK;
+}
+
+// Q1 element of a cut cell from the second moments of its fluid part (M[p + 3q + 9r] = int xi^p eta^q
+// zeta^r dV / V, normalised coordinates in [-1/2, 1/2]): K_ab = int grad N_a . grad N_b, G_a = int grad
+// N_a over the fluid part, Gc_a = grad N_a at the fluid centroid. N_a = prod_d (1/2 + s_d xi_d), s = +-1.
+static void eb_element(const double* M, const double h[3], double* K, double* G, double* Gc)
+{
+    auto mom = [&](int p, int q, int r) { return M[p + 3 * q + 9 * r]; };
+    auto sg = [](int a, int d) { return ((a >> d) & 1) ? 1.0 : -1.0; };
+    const double V = h[0] * h[1] * h[2];
+    for (int a = 0; a < 8; ++a) {
+        for (int d = 0; d < 3; ++d) {
+            const int e = d == 0 ? 1 : 0, f = d == 2 ? 1 : 2;
+            double acc = 0.0;
+            for (int pe = 0; pe < 2; ++pe)
+                for (int pf = 0; pf < 2; ++pf) {
+                    int idx[3] = {0, 0, 0};
+                    idx[e] = pe;
+                    idx[f] = pf;
+                    acc += (pe ? sg(a, e) : 0.5) * (pf ? sg(a, f) : 0.5) * mom(idx[0], idx[1], idx[2]);
+                }
+            G[3 * a + d] = sg(a, d) / h[d] * V * acc;
+        }
+        for (int b = 0; b < 8; ++b) {
+            double sum = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                const int e = d == 0 ? 1 : 0, f = d == 2 ? 1 : 2;
+                const double ce[3] = {0.25, 0.5 * (sg(a, e) + sg(b, e)), sg(a, e) * sg(b, e)};
+                const double cf[3] = {0.25, 0.5 * (sg(a, f) + sg(b, f)), sg(a, f) * sg(b, f)};
+                double acc = 0.0;
+                for (int pe = 0; pe < 3; ++pe)
+                    for (int pf = 0; pf < 3; ++pf) {
+                        int idx[3] = {0, 0, 0};
+                        idx[e] = pe;
+                        idx[f] = pf;
+                        acc += ce[pe] * cf[pf] * mom(idx[0], idx[1], idx[2]);
+                    }
+                sum += sg(a, d) * sg(b, d) / (h[d] * h[d]) * V * acc;
+            }
+            K[8 * a + b] = sum;
+        }
+    }
+    const double vol = mom(0, 0, 0);
+    const double cen[3] = {vol > 0 ? mom(1, 0, 0) / vol : 0.0, vol > 0 ? mom(0, 1, 0) / vol : 0.0,
+                           vol > 0 ? mom(0, 0, 1) / vol : 0.0};
+    for (int a = 0; a < 8; ++a) {
+        double fac[3];
+        for (int d = 0; d < 3; ++d) fac[d] = 0.5 + sg(a, d) * cen[d];
+        for (int d = 0; d < 3; ++d) {
+            const int e = d == 0 ? 1 : 0, f = d == 2 ? 1 : 2;
+            Gc[3 * a + d] = sg(a, d) / h[d] * fac[e] * fac[f];
+        }
+    }
+}
+
+int NodalSolver::set_eb(const gbp_array4* M)
+{
+    drop_graphs();
+    GBP_CUDA(cudaStreamSynchronize(st));
+    eb.pool.release();
+    eb = EbState{};
+    sigma_ready = false;  // the level-0 sigma split depends on the geometry: set sigma again
+    if (!M || !M->data) return rebuild_masks();
+    if (M->ncomp < 27) {
+        set_error("nodal_set_eb: the moments array needs 27 components");
+        return GBP_BAD_ARG;
+    }
+    const NodalGeom& g = L[0].g;
+    const int* n = g.n;
+    for (int d = 0; d < 3; ++d)
+        if (M->lo[d] > 0 || M->hi[d] < n[d] - 1) {
+            set_error("nodal_set_eb: the moments array must cover the cells");
+            return GBP_BAD_ARG;
+        }
+    const long long nc = (long long)n[0] * n[1] * n[2];
+    std::vector<double> Mh((size_t)(27 * nc));
+    double* tmp = nullptr;
+    GBP_CUDA(cudaMalloc(&tmp, sizeof(double) * (size_t)nc));
+    int rc = GBP_OK;
+    for (int c = 0; c < 27 && !rc; ++c) {
+        eb_pack_cells(*M, c, n, tmp, st);
+        cudaError_t e = cudaMemcpyAsync(Mh.data() + (size_t)c * nc, tmp, sizeof(double) * (size_t)nc,
+                                        cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_fail(e, "nodal_set_eb: copy of the moments");
+    }
+    cudaFree(tmp);
+    if (rc) return rc;
+    auto cid = [&](int i, int j, int k) { return i + (long long)n[0] * (j + (long long)n[1] * k); };
+    auto kap = [&](long long c) { return Mh[(size_t)c]; };
+    // cells: -2 covered, -1 regular, >= 0 cut (table index)
+    std::vector<int> ctype((size_t)nc);
+    std::vector<EbNodeCell> cells;
+    double M27[27];
+    for (int k = 0; k < n[2]; ++k)
+        for (int j = 0; j < n[1]; ++j)
+            for (int i = 0; i < n[0]; ++i) {
+                const long long c = cid(i, j, k);
+                const double kv = kap(c);
+                if (!(kv >= -1e-12 && kv <= 1.0 + 1e-12)) {
+                    set_error("nodal_set_eb: volume fractions (moment 0) must lie in [0, 1]");
+                    return GBP_BAD_ARG;
+                }
+                if (kv <= 1e-12) {
+                    ctype[(size_t)c] = kEbCovered;
+                } else if (kv >= 1.0 - 1e-12) {
+                    ctype[(size_t)c] = kEbRegular;
+                } else {
+                    EbNodeCell ec{};
+                    ec.p = pidx(g.sy, g.sz, i, j, k);
+                    ec.i = i;
+                    ec.j = j;
+                    ec.k = k;
+                    for (int q = 0; q < 27; ++q) M27[q] = Mh[(size_t)q * nc + c];
+                    eb_element(M27, g.h, ec.K, ec.G, ec.Gc);
+                    ctype[(size_t)c] = (int)cells.size();
+                    cells.push_back(ec);
+                }
+            }
+    auto wrapc = [&](int v, int d, bool& inside) {
+        if (g.per[d]) return ((v % n[d]) + n[d]) % n[d];
+        inside = inside && v >= 0 && v < n[d];
+        return v;
+    };
+    // nodes: active (touches fluid), EB (touches a cut cell)
+    std::vector<EbNodeEntry> nodes;
+    std::vector<unsigned char> act_u((size_t)g.nu[0] * g.nu[1] * g.nu[2], 0);
+    bool inactive = false;
+    for (int k = 0; k < g.nu[2]; ++k)
+        for (int j = 0; j < g.nu[1]; ++j)
+            for (int i = 0; i < g.nu[0]; ++i) {
+                EbNodeEntry nd{};
+                nd.i = i;
+                nd.j = j;
+                nd.k = k;
+                bool has_cut = false, has_fluid = false;
+                for (int c = 0; c < 8; ++c) {
+                    bool inside = true;
+                    const int ci = wrapc(i - 1 + (c & 1), 0, inside), cj = wrapc(j - 1 + ((c >> 1) & 1), 1, inside),
+                              ck = wrapc(k - 1 + (c >> 2), 2, inside);
+                    int t = kEbCovered;
+                    if (inside) t = ctype[(size_t)cid(ci, cj, ck)];
+                    nd.cell[c] = t;
+                    has_cut = has_cut || t >= 0;
+                    has_fluid = has_fluid || t != kEbCovered;
+                }
+                act_u[(size_t)(i + g.nu[0] * ((size_t)j + (size_t)g.nu[1] * k))] = has_fluid;
+                inactive = inactive || !has_fluid;
+                if (has_cut) nodes.push_back(nd);
+            }
+    // padded arrays (periodic aliases filled): volume fraction, regular-cell flag, active-node flag
+    std::vector<double> kap_p((size_t)g.count, 0.0), ivol_p((size_t)g.count, 0.0);
+    std::vector<unsigned char> reg_p((size_t)g.count, 0), act_p((size_t)g.count, 0);
+    // fluid volume of each unique node's dual cell: kappa V / 8 from each of its 8 cells
+    std::vector<double> vf_u(act_u.size(), 0.0);
+    for (int k = 0; k < g.nu[2]; ++k)
+        for (int j = 0; j < g.nu[1]; ++j)
+            for (int i = 0; i < g.nu[0]; ++i) {
+                double v = 0.0;
+                for (int c = 0; c < 8; ++c) {
+                    bool inside = true;
+                    const int ci = wrapc(i - 1 + (c & 1), 0, inside), cj = wrapc(j - 1 + ((c >> 1) & 1), 1, inside),
+                              ck = wrapc(k - 1 + (c >> 2), 2, inside);
+                    if (inside) v += kap(cid(ci, cj, ck)) * g.vol / 8.0;
+                }
+                vf_u[(size_t)(i + g.nu[0] * ((size_t)j + (size_t)g.nu[1] * k))] = v;
+            }
+    for (int k = -1; k <= n[2]; ++k)
+        for (int j = -1; j <= n[1]; ++j)
+            for (int i = -1; i <= n[0]; ++i) {
+                bool inside = true;
+                const int ci = wrapc(i, 0, inside), cj = wrapc(j, 1, inside), ck = wrapc(k, 2, inside);
+                const long long p = pidx(g.sy, g.sz, i, j, k);
+                if (inside) {
+                    const long long c = cid(ci, cj, ck);
+                    kap_p[(size_t)p] = kap(c);
+                    reg_p[(size_t)p] = ctype[(size_t)c] == kEbRegular;
+                }
+                // node (i, j, k): unique index by periodic wrap of the node index space
+                bool nin = true;
+                int ni[3] = {i, j, k};
+                for (int d = 0; d < 3; ++d) {
+                    if (g.per[d])
+                        ni[d] = ((ni[d] % n[d]) + n[d]) % n[d];
+                    else if (ni[d] < 0 || ni[d] >= g.nu[d])
+                        nin = false;
+                }
+                if (nin) {
+                    const size_t u = (size_t)(ni[0] + g.nu[0] * ((size_t)ni[1] + (size_t)g.nu[1] * ni[2]));
+                    act_p[(size_t)p] = act_u[u];
+                    ivol_p[(size_t)p] = vf_u[u] > 0.0 ? 1.0 / vf_u[u] : 0.0;
+                }
+            }
+    // coarse levels: a cell holds fluid when one of its 8 fine cells does; a node is active when one of
+    // its cells holds fluid. (Injecting the level-0 flags instead would pin the coarse nodes that lie in
+    // the body next to fluid and stall the coarse correction along the boundary.)
+    std::vector<std::vector<unsigned char>> act_lv(L.size());
+    act_lv[0] = act_p;
+    {
+        std::vector<unsigned char> fl((size_t)nc);
+        for (long long c = 0; c < nc; ++c) fl[(size_t)c] = ctype[(size_t)c] != kEbCovered;
+        for (size_t l = 1; l < L.size(); ++l) {
+            const NodalGeom& f = L[l - 1].g;
+            const NodalGeom& cg = L[l].g;
+            const int* m = cg.n;
+            std::vector<unsigned char> cf((size_t)m[0] * m[1] * m[2], 0);
+            for (int k = 0; k < m[2]; ++k)
+                for (int j = 0; j < m[1]; ++j)
+                    for (int i = 0; i < m[0]; ++i) {
+                        unsigned char v = 0;
+                        for (int c = 0; c < 8; ++c)
+                            v |= fl[(size_t)((2 * i + (c & 1)) +
+                                             (long long)f.n[0] * ((2 * j + ((c >> 1) & 1)) +
+                                                                  (long long)f.n[1] * (2 * k + (c >> 2))))];
+                        cf[(size_t)(i + (long long)m[0] * (j + (long long)m[1] * k))] = v;
+                    }
+            std::vector<unsigned char> ap((size_t)cg.count, 0);
+            for (int k = -1; k <= m[2]; ++k)
+                for (int j = -1; j <= m[1]; ++j)
+                    for (int i = -1; i <= m[0]; ++i) {
+                        int ni[3] = {i, j, k};
+                        bool nin = true;
+                        for (int d = 0; d < 3; ++d) {
+                            if (cg.per[d])
+                                ni[d] = ((ni[d] % m[d]) + m[d]) % m[d];
+                            else if (ni[d] < 0 || ni[d] > m[d])
+                                nin = false;
+                        }
+                        if (!nin) continue;
+                        unsigned char v = 0;
+                        for (int c = 0; c < 8; ++c) {
+                            int ci[3] = {ni[0] - 1 + (c & 1), ni[1] - 1 + ((c >> 1) & 1), ni[2] - 1 + (c >> 2)};
+                            bool in = true;
+                            for (int d = 0; d < 3; ++d) {
+                                if (cg.per[d])
+                                    ci[d] = ((ci[d] % m[d]) + m[d]) % m[d];
+                                else
+                                    in = in && ci[d] >= 0 && ci[d] < m[d];
+                            }
+                            if (in) v |= cf[(size_t)(ci[0] + (long long)m[0] * (ci[1] + (long long)m[1] * ci[2]))];
+                        }
+                        ap[(size_t)pidx(cg.sy, cg.sz, i, j, k)] = v;
+                    }
+            act_lv[l].swap(ap);
+            fl.swap(cf);
+        }
+    }
+    size_t need = 0;
+    auto add = [&](size_t cnt, size_t sz) { need = ((need + 255) & ~size_t(255)) + cnt * sz; };
+    add(nodes.size() + 1, sizeof(EbNodeEntry));
+    add(cells.size() + 1, sizeof(EbNodeCell));
+    add(g.count, 8);
+    add(g.count, 1);
+    for (size_t l = 0; l < L.size(); ++l) add(L[l].g.count, 1);
+    add(g.count, 8);
+    add(g.count, 4);
+    add(g.count, 8);
+    need += 4096;
+    rc = eb.pool.reserve(need);
+    if (rc) return rc;
+    EbNodeEntry* dn = eb.pool.take<EbNodeEntry>(nodes.size() + 1);
+    EbNodeCell* dc = eb.pool.take<EbNodeCell>(cells.size() + 1);
+    double* dk = eb.pool.take<double>(g.count);
+    unsigned char* dr = eb.pool.take<unsigned char>(g.count);
+    for (size_t l = 0; l < L.size(); ++l) eb.active8[l] = eb.pool.take<unsigned char>(L[l].g.count);
+    double* s64t = eb.pool.take<double>(g.count);
+    float* s32t = eb.pool.take<float>(g.count);
+    eb.ivol = eb.pool.take<double>(g.count);
+    if (!nodes.empty())
+        GBP_CUDA(cudaMemcpyAsync(dn, nodes.data(), sizeof(EbNodeEntry) * nodes.size(), cudaMemcpyHostToDevice, st));
+    if (!cells.empty())
+        GBP_CUDA(cudaMemcpyAsync(dc, cells.data(), sizeof(EbNodeCell) * cells.size(), cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(dk, kap_p.data(), sizeof(double) * g.count, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(dr, reg_p.data(), g.count, cudaMemcpyHostToDevice, st));
+    for (size_t l = 0; l < L.size(); ++l)
+        GBP_CUDA(cudaMemcpyAsync(eb.active8[l], act_lv[l].data(), L[l].g.count, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(eb.ivol, ivol_p.data(), sizeof(double) * g.count, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemsetAsync(s64t, 0, sizeof(double) * g.count, st));
+    GBP_CUDA(cudaMemsetAsync(s32t, 0, sizeof(float) * g.count, st));
+    GBP_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+    eb.e.nodes = dn;
+    eb.e.cells = dc;
+    eb.e.nnodes = (int)nodes.size();
+    eb.e.ncells = (int)cells.size();
+    eb.e.sig64 = s64t;
+    eb.e.sig32 = s32t;
+    eb.e.kap = dk;
+    eb.e.reg = dr;
+    eb.has_inactive = inactive;
+    eb.on = true;
+    return rebuild_masks();
 }
 
 int NodalSolver::set_surrogate(nn::UNet* n, int level, int mode)
@@ -824,7 +1170,7 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
     if (alpha != 0.0) {
         rc = nn::scale_to64(l0.g.count, l0.x32, alpha, phi, st);
         if (rc) return rc;
-        resid<double>(l0.g, l0.s64, phi, rhs0, res, dnorm + 1, st);
+        resid0(phi, rhs0, res, dnorm + 1, st);
         if (launch_rc) return launch_rc;
         nk += 2;
         GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -871,15 +1217,23 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
     const NodalLevel& l0 = L[0];
     GBP_CUDA(cudaEventRecord(ev0, st));
     GBP_CUDA(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), st));
-    nodal_rhs(l0.g, rhs, l0.s64, rhs0, singular ? partials : nullptr, st);
+    RhsArgs ra = rhs;
+    if (eb.on) ra.cmask = eb.e.reg;  // cut and covered cells: the cut-cell table below
+    nodal_rhs(l0.g, ra, l0.s64, rhs0, singular ? partials : nullptr, st);
     ++nk;
+    if (eb.on) eb_rhs(l0.g, eb.e, ra, rhs0, st);
     if (singular) {
-        // consistent right-hand side, and its max norm (the relative-tolerance reference)
+        // consistent right-hand side, and its max norm (the relative-tolerance reference; with cut
+        // cells taken again below over the fluid volumes)
         nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, 1, nodal_rhs_partials(l0.g), dnorm, st);
         nk += 2;
     } else {
         nodal_norm(l0.g, rhs0, dnorm, st);
         ++nk;
+    }
+    if (eb.on) {
+        GBP_CUDA(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), st));
+        eb_norm(l0.g, rhs0, eb.ivol, dnorm, st);
     }
     if (phi_guess) {
         nodal_load_phi(l0.g, *phi_guess, phi, st);
@@ -899,8 +1253,11 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
                                      phi_copy->stream));
         }
     }
-    nodal_correct(l0.g, corr, l0.s64, phi, st);
+    CorrArgs ca = corr;
+    if (eb.on) ca.cmask = eb.e.reg;
+    nodal_correct(l0.g, ca, l0.s64, phi, st);
     ++nk;
+    if (eb.on) eb_correct(l0.g, eb.e, corr, phi, st);
     GBP_CUDA(cudaEventRecord(ev2, st));
     GBP_CUDA(cudaGetLastError());
     if (stats) {
@@ -965,7 +1322,10 @@ int NodalSolver::divergence(const RhsArgs& rhs, const gbp_array4* out, double* m
 {
     const NodalLevel& l0 = L[0];
     GBP_CUDA(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), st));
-    nodal_rhs(l0.g, rhs, l0.s64, rhs0, singular ? partials : nullptr, st);
+    RhsArgs ra = rhs;
+    if (eb.on) ra.cmask = eb.e.reg;
+    nodal_rhs(l0.g, ra, l0.s64, rhs0, singular ? partials : nullptr, st);
+    if (eb.on) eb_rhs(l0.g, eb.e, ra, rhs0, st);
     if (singular)
         nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, 1, nodal_rhs_partials(l0.g), dnorm, st);
     else

@@ -9,6 +9,7 @@
 
 #include "gbp_internal.cuh"
 #include "nodal_kernels.h"
+#include "nodal_eb.h"
 #include "nodal_sweep.h"
 
 namespace gbp {
@@ -62,6 +63,10 @@ public:
     int set_sigma(const gbp_array4* sigma, double cval);
     // overset mask (0 = phi held at 0) over nodes 0..n; nullptr removes it
     int set_mask(const gbp_iarray4* mask);
+    // cut cells: moments (27 components M[p + 3 q + 9 r] = int xi^p eta^q zeta^r dV / V over the fluid
+    // part of each cell, normalised coordinates in [-1/2, 1/2]); nullptr removes them. Sigma must be set
+    // again afterwards.
+    int set_eb(const gbp_array4* moments);
 
     // full projection: rhs from vel (+ fused add-back / U^n subtraction), solve, correct.
     // phi_copy: a copy (e.g. p_nd to the host) issued on its own stream once phi_out is stored,
@@ -131,8 +136,24 @@ private:
     int* dinfo = nullptr;        // bottom iteration count
     unsigned long long* dnorm = nullptr;  // [0] rhs norm, [1] residual norm
     unsigned long long* hnorm = nullptr;  // pinned mirror
-    bool singular = false;
+    bool singular = false;        // the system has the constants as null space (consistent RHS, gauge)
+    bool bsing = false;           // the coarsest operator does (no node held at 0 on it)
     bool singular_faces = false;  // singular from the boundary types alone (no overset mask)
+    int rebuild_masks();
+    int finish_sigma();
+    void resid0(const double* x, const double* b, double* r, unsigned long long* norm, cudaStream_t s);
+    unsigned user_zeros = 0;
+    unsigned char* umask8 = nullptr;  // the user's overset mask, level 0 (null: none)
+    DevicePool auxpool;               // user mask storage
+    struct EbState {
+        DevicePool pool;
+        EbNodal e{};
+        // nodes touching fluid on each level (a coarse cell holds fluid when one of its fine cells does)
+        unsigned char* active8[kMaxLevels] = {};
+        double* ivol = nullptr;            // 1 / fluid volume of each node's dual cell (level 0)
+        bool has_inactive = false;
+        bool on = false;
+    } eb;
     bool sigma_ready = false;
     double scale32 = 1.0;
     // result buffer of each level's V-cycle (ping-pong aware)

@@ -37,9 +37,15 @@ def _outside_moment_1d(a, b, c, s):
     return 0.5 * (b * b - a * a) - cov
 
 
+def _snap(u, r):
+    """u within rounding of +-r is +-r: the closed forms below (asin near +-1) would otherwise turn the
+    last bit of a grid line that touches the circle's extreme point into an area error of ~1e-10."""
+    return math.copysign(r, u) if abs(abs(u) - r) <= 1e-12 * r else u
+
+
 def _rect_disk(x0, x1, y0, y1, cx, cy, r):
     """Area and first moments (int x, int y) of the rectangle's part inside the circle, exactly."""
-    ua, ub = max(x0 - cx, -r), min(x1 - cx, r)
+    ua, ub = max(_snap(x0 - cx, r), -r), min(_snap(x1 - cx, r), r)
     if ub <= ua:
         return 0.0, 0.0, 0.0
     r2 = r * r
@@ -60,7 +66,7 @@ def _rect_disk(x0, x1, y0, y1, cx, cy, r):
     for yb in (y0, y1):
         d = yb - cy
         if abs(d) < r:
-            w = math.sqrt(r2 - d * d)
+            w = _snap(math.sqrt(r2 - d * d), r)
             cuts += [w, -w]
     cuts = sorted(c for c in cuts if ua <= c <= ub)
     area = mx = my = 0.0
@@ -95,9 +101,11 @@ def _outside_rect(x0, x1, y0, y1, cx, cy, r):
     return min(1.0, area / full), mx / area, my / area
 
 
-def cylinder(n, lo, hi, center, radius, axis=2):
+def cylinder(n, lo, hi, center, radius, axis=2, small_volfrac=0.0):
     """Volume fractions, face apertures and face centroids of the region outside a cylinder along
-    `axis`. Returns dict(vfrac, apx, apy, apz, fcx, fcy, fcz) as float64 arrays."""
+    `axis`. Returns dict(vfrac, apx, apy, apz, fcx, fcy, fcz) as float64 arrays. Cells whose volume
+    fraction is below `small_volfrac` are made covered, with their faces closed (EB2's small-cell
+    removal, the eb2.small_volfrac input; incflo's cylinder benchmarks use 1e-4)."""
     n = tuple(int(v) for v in n)
     h = [(hi[d] - lo[d]) / n[d] for d in range(3)]
     edges = [lo[d] + h[d] * np.arange(n[d] + 1) for d in range(3)]
@@ -157,7 +165,9 @@ def cylinder(n, lo, hi, center, radius, axis=2):
     for d, o in ((p, q), (q, p)):
         xd = grid(d, True)
         cd = center[d]
-        s = np.where((xd - cd) ** 2 < radius * radius, np.sqrt(np.clip(radius ** 2 - (xd - cd) ** 2, 0, None)), -1.0)
+        # a face line within rounding of the circle's extreme point is tangent to it (no chord)
+        inside = (xd - cd) ** 2 < radius * radius * (1.0 - 2e-12)
+        s = np.where(inside, np.sqrt(np.clip(radius ** 2 - (xd - cd) ** 2, 0, None)), -1.0)
         o0, o1 = lohi(o)
         f = _outside_fraction_1d(o0, o1, center[o], s)
         length = (o1 - o0) * f
@@ -170,4 +180,116 @@ def cylinder(n, lo, hi, center, radius, axis=2):
         offo = np.where(cut, np.broadcast_to((cen - 0.5 * (o0 + o1)) / h[o], tuple(fs)), 0.0)
         comps = [offo if t == o else np.zeros(tuple(fs)) for t in range(3) if t != d]
         fc[d] = np.stack(comps, axis=-1)
+    if small_volfrac > 0.0:
+        small = (vfrac > 0.0) & (vfrac < small_volfrac)
+        if small.any():
+            vfrac[small] = 0.0
+            for d in range(3):
+                ax = 2 - d
+                pad = [(0, 0)] * 3
+                pad[ax] = (0, 1)
+                lo_side = np.pad(small, pad)
+                pad[ax] = (1, 0)
+                hi_side = np.pad(small, pad)
+                shut = lo_side | hi_side
+                ap[d][shut] = 0.0
+                fc[d][shut] = 0.0
     return dict(vfrac=vfrac, apx=ap[0], apy=ap[1], apz=ap[2], fcx=fc[0], fcy=fc[1], fcz=fc[2])
+
+
+_GL16_X, _GL16_W = np.polynomial.legendre.leggauss(16)
+
+
+def _outside_moments_2d(x0, x1, y0, y1, cx, cy, r, pmax=2):
+    """Moments int xi^p eta^q (p, q <= pmax) of the part of the rectangle outside the circle, over the
+    rectangle's normalised coordinates xi = (x - xm) / (x1 - x0), eta likewise, in [-1/2, 1/2]. The covered
+    part is integrated piecewise between the break points in the angle theta (u = x - cx = r sin theta),
+    where the integrand is smooth, by 16-point Gauss-Legendre."""
+    hx, hy = x1 - x0, y1 - y0
+    xm, ym = 0.5 * (x0 + x1), 0.5 * (y0 + y1)
+    full = np.zeros((pmax + 1, pmax + 1))
+    for p in range(pmax + 1):
+        for q in range(pmax + 1):
+            ix = (0.5 ** (p + 1) - (-0.5) ** (p + 1)) / (p + 1)
+            iy = (0.5 ** (q + 1) - (-0.5) ** (q + 1)) / (q + 1)
+            full[p, q] = ix * iy
+    ua, ub = max(_snap(x0 - cx, r), -r), min(_snap(x1 - cx, r), r)
+    cov = np.zeros_like(full)
+    if ub > ua:
+        cuts = [ua, ub]
+        for yb in (y0, y1):
+            d = yb - cy
+            if abs(d) < r:
+                w = math.sqrt(r * r - d * d)
+                cuts += [w, -w]
+        cuts = sorted(c for c in cuts if ua <= c <= ub)
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            if b <= a:
+                continue
+            ta, tb = math.asin(max(-1.0, min(1.0, a / r))), math.asin(max(-1.0, min(1.0, b / r)))
+            tm, th = 0.5 * (ta + tb), 0.5 * (tb - ta)
+            for t, w in zip(_GL16_X, _GL16_W):
+                theta = tm + th * t
+                u = r * math.sin(theta)
+                s = r * math.cos(theta)
+                jac = r * math.cos(theta) * th * w  # du = r cos(theta) dtheta
+                lo, hi = max(y0, cy - s), min(y1, cy + s)
+                if hi <= lo:
+                    continue
+                xi = (cx + u - xm) / hx
+                elo, ehi = (lo - ym) / hy, (hi - ym) / hy
+                for p in range(pmax + 1):
+                    for q in range(pmax + 1):
+                        cov[p, q] += jac / hx * xi ** p * (ehi ** (q + 1) - elo ** (q + 1)) / (q + 1)
+    return full - cov
+
+
+def cylinder_moments(n, lo, hi, center, radius, axis=2, small_volfrac=0.0):
+    """Second moments of the fluid part of every cell for the cylinder of `cylinder`: an array
+    (nz, ny, nx, 3, 3, 3) of int xi^p eta^q zeta^r dV / V over the fluid part, in the cell's
+    normalised coordinates (xi, eta, zeta) in [-1/2, 1/2]^3 along (x, y, z), p, q, r <= 2. A regular
+    cell has M[0,0,0] = 1, M[2,.,.] etc. = 1/12 products; a covered cell all zeros. The fluid part of a
+    cell is a prism along the axis, so the axial factor is exact (1, 0, 1/12). Cells whose volume
+    fraction is below `small_volfrac` are made covered (as in `cylinder`)."""
+    n = tuple(int(v) for v in n)
+    h = [(hi[d] - lo[d]) / n[d] for d in range(3)]
+    edges = [lo[d] + h[d] * np.arange(n[d] + 1) for d in range(3)]
+    p_, q_ = [d for d in range(3) if d != axis]
+    za = np.array([1.0, 0.0, 1.0 / 12.0])
+    M = np.zeros((n[2], n[1], n[0], 3, 3, 3))
+    m2 = np.zeros((n[q_], n[p_], 3, 3))
+    full2 = None
+    for b in range(n[q_]):
+        for a in range(n[p_]):
+            x0, x1 = edges[p_][a], edges[p_][a + 1]
+            y0, y1 = edges[q_][b], edges[q_][b + 1]
+            if (abs(0.5 * (x0 + x1) - center[p_]) > radius + h[p_] or
+                    abs(0.5 * (y0 + y1) - center[q_]) > radius + h[q_]):
+                if full2 is None:
+                    full2 = _outside_moments_2d(0.0, 1.0, 0.0, 1.0, 10.0, 10.0, 1e-3)
+                m2[b, a] = full2
+            else:
+                mm = _outside_moments_2d(x0, x1, y0, y1, center[p_], center[q_], radius)
+                if mm[0, 0] <= 1e-14 or mm[0, 0] < small_volfrac:  # covered (rounding, or a small cell)
+                    mm[:] = 0.0
+                elif mm[0, 0] >= 1.0 - 1e-14:  # a full cell the circle only touches
+                    mm = _outside_moments_2d(0.0, 1.0, 0.0, 1.0, 10.0, 10.0, 1e-3)
+                m2[b, a] = mm
+    # assemble (p along x, q along y, r along z): direction p_ -> index of m2's first moment axis
+    for pz in range(3):
+        for qy in range(3):
+            for rx in range(3):
+                e = {0: rx, 1: qy, 2: pz}
+                val = m2[:, :, e[p_], e[q_]] * za[e[axis]]
+                sh = [1, 1, 1]
+                sh[2 - q_] = n[q_]
+                sh[2 - p_] = n[p_]
+                M[..., rx, qy, pz] = np.broadcast_to(val.reshape(sh), (n[2], n[1], n[0]))
+    return M
+
+
+def moments_components(M):
+    """(nz, ny, nx, 3, 3, 3) moments -> the (27, nz, ny, nx) array of gbp_nodal_set_eb, component
+    p + 3q + 9r."""
+    M = np.asarray(M, dtype=np.float64)
+    return np.ascontiguousarray(M.transpose(5, 4, 3, 0, 1, 2).reshape((27,) + M.shape[:3]))

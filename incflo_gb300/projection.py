@@ -262,13 +262,24 @@ class NodalProjector:
         return io[0], io[1]
 
 
+def _set_plan_eb(plan, eb_moments):
+    """attach (or remove) cut cells on a cached nodal plan when they changed"""
+    key = None if eb_moments is None else (eb_moments.data_ptr(), tuple(eb_moments.shape), eb_moments._version)
+    if getattr(plan, "_eb_key", None) == key:
+        return
+    A.check(A.load().gbp_nodal_set_eb(plan.ptr, _ref(array4(eb_moments)) if eb_moments is not None else None),
+            "gbp_nodal_set_eb")
+    plan._eb_key = key
+
+
 def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd, *, time=0.0, dt=1.0,
                            prev_dt=1.0, scaling_factor=1.0, incremental=False, set_inflow_bc=True,
                            vel_old=None, rho0=1.0, ng=1, options: A.Options | None = None, stream=None,
-                           constant_density=False, surrogate=None, surrogate_level=1):
+                           constant_density=False, surrogate=None, surrogate_level=1, eb_moments=None):
     """incflo::ApplyNodalProjection for one level, fused on the device; returns the stats dict.
     ``surrogate`` (incflo_gb300.surrogate.Surrogate) enables the learned warm start on multigrid level
-    ``surrogate_level``."""
+    ``surrogate_level``; ``eb_moments`` (27, nz, ny, nx) the cut cells of an embedded boundary
+    (incflo_gb300.eb.cylinder_moments, components p + 3q + 9r)."""
     options = options or A.default_options(A.GBP_NODAL)
     key = (tuple(geom.n_cell), tuple(geom.prob_lo), tuple(geom.prob_hi), tuple(bc_lo), tuple(bc_hi),
            options.max_coarsening_level, torch.cuda.current_device())
@@ -281,6 +292,7 @@ def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd,
     A.check(A.load().gbp_plan_set_surrogate(plan.ptr, surrogate.ptr if surrogate is not None else None,
                                             int(surrogate_level), int(surrogate is not None)),
             "gbp_plan_set_surrogate")
+    _set_plan_eb(plan, eb_moments)
     st = A.Stats()
     rho_a = None if constant_density else array4(density, 0)
     A.check(A.load().gbp_apply_nodal_projection(

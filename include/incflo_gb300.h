@@ -178,6 +178,17 @@ int gbp_nodal_project(gbp_plan* plan, gbp_array4* vel, gbp_array4* phi, gbp_arra
  * = solve. Coarse levels take the mask by injection. NULL (or data == NULL) removes the mask. */
 int gbp_nodal_set_overset_mask(gbp_plan* plan, const gbp_iarray4* mask);
 
+/* Cut cells of a nodal plan: the EB factory of the NodalProjector's MultiFabs
+ * (incflo_apply_nodal_projection.cpp:95-267 on an EB level; MLNodeLaplacian builds its cut-cell
+ * stencils from the EB volume moments). moments: cell array with 27 components, component p + 3q + 9r =
+ * int xi^p eta^q zeta^r dV / V over the fluid part of the cell (p, q, r <= 2), in the cell's normalised
+ * coordinates [-1/2, 1/2]^3; component 0 is the volume fraction. Each cut cell contributes its exact Q1
+ * element matrix and int u . grad N over the fluid part; no flux through the embedded boundary; nodes
+ * that touch no fluid are not unknowns; the correction uses grad phi at the fluid centroid of each cut
+ * cell. NULL removes the cut cells. Sigma must be set again afterwards (gbp_apply_nodal_projection
+ * does on every call). */
+int gbp_nodal_set_eb(gbp_plan* plan, const gbp_array4* moments);
+
 /* The nodal divergence of vel as the projection sees it: the right-hand side of the nodal solve
  * (div_i = weak divergence / control volume, inflow normal velocity from the ghost cells when
  * use_inflow != 0, 0 on Dirichlet nodes), made consistent for singular boundary sets. div_out
@@ -249,6 +260,34 @@ int gbp_abec_solve(gbp_plan* plan, const gbp_array4* rhs, gbp_array4* phi, gbp_s
  * b = the face average of the cell field eta, the adjacent cell's eta on non-periodic domain sides. */
 int gbp_abec_set_coeffs_eta(gbp_plan* plan, double alpha, const gbp_array4* a, double a0, double beta,
                             const gbp_array4* eta);
+
+/* ---- tensor (velocity) diffusion ---------------------------------------------------------
+ * DiffusionTensorOp (src/diffusion/DiffusionTensorOp.cpp:104-317) over MLTensorOp:
+ *   alpha a u - beta div tau = rhs,  tau = eta (grad u + grad u^T) - (2/3) eta (div u) I
+ * diffuse_velocity: alpha = 1, a = rho, beta = dt, rhs = rho u, eta on faces from
+ * average_velocity_eta_to_faces (the face average of the cell field with the domain-side fix-up);
+ * compute_divtau: div tau. One box, cell-centred. bc_lo / bc_hi: [3 * component + direction] (the
+ * per-component table of incflo::get_diffuse_tensor_bc, incflo_diffusion.cpp:106-153):
+ * GBP_BC_PERIODIC, GBP_BC_DIRICHLET (no-slip wall, mass inflow; GBP_BC_INFLOW is read as Dirichlet) or
+ * GBP_BC_NEUMANN (outflow; tangential components at a slip wall). Velocity arrays carry 3 components
+ * and one ghost layer on the non-periodic sides; the ghost cells next to Dirichlet faces hold the face
+ * values (setLevelBC(lev, velocity)). */
+typedef struct gbp_tensor gbp_tensor;
+int gbp_tensor_create(const gbp_geometry* geom, const int bc_lo[9], const int bc_hi[9], const gbp_options* opt,
+                      void* stream, gbp_tensor** out);
+int gbp_tensor_destroy(gbp_tensor* t);
+int gbp_tensor_set_options(gbp_tensor* t, const gbp_options* opt);
+size_t gbp_tensor_device_bytes(const gbp_tensor* t);
+/* setScalars(alpha, beta), setACoeffs(a) (a == NULL: the constant a0), setShearViscosity: eta as a cell
+ * field averaged to the faces (eta_cc), as face arrays (eta_x/y/z, when eta_cc is NULL) or the
+ * constant eta0 (all NULL). alpha > 0 for solves. */
+int gbp_tensor_set_coeffs(gbp_tensor* t, double alpha, const gbp_array4* a, double a0, double beta,
+                          const gbp_array4* eta_cc, const gbp_array4* eta_x, const gbp_array4* eta_y,
+                          const gbp_array4* eta_z, double eta0);
+/* MLMG::solve(velocity, rhs, rtol, atol): vel is the initial guess and receives the solution */
+int gbp_tensor_solve(gbp_tensor* t, const gbp_array4* rhs, gbp_array4* vel, gbp_stats* stats);
+/* MLMG::apply with setScalars(0, -1): divtau = div tau of vel */
+int gbp_tensor_apply(gbp_tensor* t, const gbp_array4* vel, gbp_array4* divtau);
 
 /* ---- two-level (AMR) composite nodal projection ----------------------------------------
  * incflo::ApplyNodalProjection(density, time, scaling_factor, incremental) over finest_level = 1

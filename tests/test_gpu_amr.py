@@ -64,7 +64,7 @@ def test_amr_composite_projection_matches_oracle(gpu_lib, name, precision):
                        device="cuda") for lo, hi in boxes]
     st = proj.apply(vel_c, rc, gpc, p_c, vel_f, rho_fb, gp_fb, p_f, scaling_factor=s)
     assert st["status"] == 0 and st["final_rel_resid"] <= 1e-12
-    assert st["outer_iters"] <= 20
+    assert st["outer_iters"] <= 40
     assert rel_l2(p_c.cpu().numpy(), ref["phi_c"]) <= 1e-9
     np.testing.assert_allclose(vel_c.cpu().numpy(), ref["u_c"], rtol=0, atol=1e-9 * np.abs(ref["u_c"]).max())
     np.testing.assert_allclose(gpc.cpu().numpy(), ref["gphi_c"], rtol=0, atol=1e-9 * np.abs(ref["gphi_c"]).max())
