@@ -324,6 +324,46 @@ def run_eb_nodal(args, dev, steps=5, warmup=3):
             "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"]}
 
 
+def run_tensor(args, dev, steps=3, warmup=3):
+    """ms per tensor (velocity) diffusion solve, DiffusionTensorOp::diffuse_velocity on a 256^3 channel
+    (periodic x / z, no-slip walls y with a moving upper wall), rho 1..2 and eta 0.01..0.02 seeded
+    random, dt = 0.5 h, rhs = rho u, rtol 1e-10, FP32 block V-cycles inside FP64 defect correction."""
+    import torch
+
+    from incflo_gb300 import Geometry, make_options
+    from incflo_gb300.diffusion import TensorOp, diffuse_tensor_bc
+
+    n = 256
+    bclo, bchi = diffuse_tensor_bc(("periodic", "no_slip_wall", "periodic"), ("periodic", "no_slip_wall", "periodic"))
+    g = torch.Generator(device=dev).manual_seed(11)
+    rho = 1.0 + torch.rand((n, n, n), dtype=torch.float64, device=dev, generator=g)
+    eta = 0.01 * (1.0 + torch.rand((n, n, n), dtype=torch.float64, device=dev, generator=g))
+    v0 = torch.zeros((3, n + 2, n + 2, n + 2), dtype=torch.float64, device=dev)
+    v0[:, 1:-1, 1:-1, 1:-1] = torch.randn((3, n, n, n), dtype=torch.float64, device=dev, generator=g)
+    v0[0, 1:-1, -1, 1:-1] = 1.0  # moving upper wall
+    rhs = (rho[None] * v0[:, 1:-1, 1:-1, 1:-1]).contiguous()
+    op = TensorOp(Geometry((n, n, n), (0, 0, 0), (1.0, 1.0, 1.0)), options=make_options(1, precision="mixed"))
+    op.setDomainBC(bclo, bchi)
+    op.setScalars(1.0, 0.5 / n)
+    op.setACoeffs(0, rho)
+    op.setShearViscosity(0, eta)
+    vt = v0.clone()
+    times, st = [], None
+    for i in range(warmup + steps):
+        vt.copy_(v0)
+        torch.cuda.synchronize()
+        st = op.solve(vt, rhs, rtol=args.rtol, atol=0.0)
+        if st["status"] != 0:
+            raise RuntimeError(f"tensor solve failed: {st}")
+        if i >= warmup:
+            times.append(st["ms_solve"])
+    del op
+    return {"workload": "tensor (velocity) diffusion 256^3, periodic x/z, no-slip walls y, rho 1..2, eta 0.01..0.02, "
+                        f"dt = 0.5 h, rtol {args.rtol:g}, FP32 block V-cycles inside FP64 defect correction",
+            "ms_per_solve": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
+            "block_vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"]}
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -461,6 +501,7 @@ def run_ours(args, ws, rank, local):
     if not args.no_eb:
         eb_mac = run_eb_mac(args, dev)
         eb_nodal = run_eb_nodal(args, dev)
+    tensor = None if args.no_tensor else run_tensor(args, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -500,6 +541,7 @@ def run_ours(args, ws, rank, local):
         "amr": amr,
         "eb_mac": eb_mac,
         "eb_nodal": eb_nodal,
+        "tensor_diffusion": tensor,
         "gpu_launches": launches,
         "clocks": clocks,
     }
@@ -521,6 +563,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-amr", action="store_true")
     ap.add_argument("--no-eb", action="store_true")
+    ap.add_argument("--no-tensor", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-warm-start", action="store_true")
     ap.add_argument("--warm-level", type=int, default=1)

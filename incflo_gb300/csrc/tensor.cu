@@ -300,8 +300,12 @@ int TensorSolver::init(const gbp_geometry& g, const int bc_lo[9], const int bc_h
         bclo[q] = bc_lo[q] == GBP_BC_INFLOW ? GBP_BC_DIRICHLET : bc_lo[q];
         bchi[q] = bc_hi[q] == GBP_BC_INFLOW ? GBP_BC_DIRICHLET : bc_hi[q];
     }
+    // one V-cycle per block and step: the outer defect correction is what converges the cross terms,
+    // so further inner cycles per step only sharpen the block-diagonal part
+    gbp_options bo = opt;
+    bo.ir_inner_cycles = 1;
     for (int c = 0; c < 3; ++c) {
-        int rc = comp[c].init(g, bclo + 3 * c, bchi + 3 * c, opt, st);
+        int rc = comp[c].init(g, bclo + 3 * c, bchi + 3 * c, bo, st);
         if (rc) return rc;
     }
     const CellGeom& cg = comp[0].finest();
@@ -324,8 +328,10 @@ int TensorSolver::init(const gbp_geometry& g, const int bc_lo[9], const int bc_h
 
 int TensorSolver::set_options(const gbp_options& o)
 {
+    gbp_options bo = o;
+    bo.ir_inner_cycles = 1;
     for (int c = 0; c < 3; ++c) {
-        int rc = comp[c].set_options(o);
+        int rc = comp[c].set_options(bo);
         if (rc) return rc;
     }
     opt = o;
@@ -475,10 +481,9 @@ int TensorSolver::solve(const gbp_array4& rhs_in, gbp_array4& vel, gbp_stats* st
         GBP_CUDA(cudaEventSynchronize(ev1));
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ev0, ev1);
-        const gbp_options& mo = comp[0].options();
         stats->status = status;
         stats->outer_iters = it + 1;
-        stats->vcycles = it * mo.ir_inner_cycles;
+        stats->vcycles = 3 * it;  // one per component block and step
         stats->rhs_norm = bnorm;
         stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;
         stats->final_rel_resid = bnorm > 0 ? rn / bnorm : rn;

@@ -9,7 +9,7 @@
 // (Dirichlet 2 u_b - u_inner, Neumann u_inner, periodic wrap; the face values continued past an edge).
 //
 // Solver: defect correction. Each step takes the FP64 residual of the full operator and, per component,
-// the inner V-cycles of its ABecLaplacian block (the normal-derivative part: b = 4/3 eta on the
+// one V-cycle of its ABecLaplacian block (the normal-derivative part: b = 4/3 eta on the
 // component's own faces, eta on the others, the component's boundary types) on a MacSolver hierarchy;
 // the cross-derivative terms only enter the residual (as MLTensorOp treats them). The blocks' V-cycles run
 // in FP32 (mixed form) or FP64.

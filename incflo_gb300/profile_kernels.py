@@ -17,6 +17,12 @@ times the warm-start U-Net's forward pass, and
 runs whole projections of the 256^3 variable-density workload in one form (mixed | fp64), so that an
 ncu launch list covers exactly one form.
 
+  python -m incflo_gb300.profile_kernels --row eb_nodal --reps 1
+
+runs the workload of one bench.py row (amr | eb_mac | eb_nodal | tensor: the two-level composite
+projection, the cut-cell MAC and nodal projections of the cylinder channel, the tensor diffusion solve)
+with `reps` timed solves after one warm-up, so that an ncu launch list covers that row alone.
+
 The U-Net mode runs the tensor-core convolutions on a 128 x 128 x 136 network grid (the multigrid
 level 1 of a 256^3 projection) and reports the convolution FLOP rate.
 """
@@ -47,6 +53,8 @@ def main():
     ap.add_argument("--unet", type=int, default=0, help="time the U-Net forward on an n x n x (n+8) grid")
     ap.add_argument("--project", default="", choices=["", "mixed", "fp64"])
     ap.add_argument("--opt", action="append", default=[], help="option override key=value (projection mode)")
+    ap.add_argument("--row", default="", choices=["", "amr", "eb_mac", "eb_nodal", "tensor"])
+    ap.add_argument("--rtol", type=float, default=1e-10)
     args = ap.parse_args()
     from incflo_gb300.build import build
 
@@ -56,6 +64,12 @@ def main():
         return unet_forward(args.unet, args.reps)
     if args.project:
         return projections(args.n, args.project, args.reps, args.opt)
+    if args.row:
+        import bench
+
+        run = getattr(bench, "run_" + args.row)
+        print(json.dumps(run(args, torch.device("cuda", 0), steps=args.reps, warmup=1)))
+        return None
     n = args.n
     rho = synth.variable_density_rt(n)["rho"]
     geom = Geometry((n, n, n))
