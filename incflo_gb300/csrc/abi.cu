@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <new>
 #include <string>
 
@@ -277,6 +278,8 @@ int gbp_plan_destroy(gbp_plan* p)
     if (p->ev_in) cudaEventDestroy(p->ev_in);
     if (p->ev_phi) cudaEventDestroy(p->ev_phi);
     if (p->ev_out) cudaEventDestroy(p->ev_out);
+    for (auto e : p->ev_slab)
+        if (e) cudaEventDestroy(e);
     if (p->dflux) cudaFree(p->dflux);
     if (p->ccbuf) cudaFree(p->ccbuf);
     delete p;
@@ -446,7 +449,8 @@ int gbp_nodal_divergence(gbp_plan* p, const gbp_array4* vel, int use_inflow, gbp
 static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
                             double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
                             double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats,
-                            cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy);
+                            cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy,
+                            const gbp::HostSlabs* out_slabs = nullptr);
 
 int gbp_apply_nodal_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
                                double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
@@ -457,11 +461,13 @@ int gbp_apply_nodal_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* v
 }
 
 // wait_before_rhs: an event the plan's stream waits on after sigma is set and before the right-hand
-// side (the host path uploads the velocities meanwhile); phi_copy: a copy issued once p_nd is stored
+// side (the host path uploads the velocities meanwhile); phi_copy: a copy issued once p_nd is stored;
+// out_slabs: the corrected velocity and gp copied out slab by slab behind the correction
 static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
                             double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
                             double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats,
-                            cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy)
+                            cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy,
+                            const gbp::HostSlabs* out_slabs)
 {
     if (!p || !p->nodal) {
         set_error("gbp_apply_nodal_projection: not a nodal plan");
@@ -498,7 +504,7 @@ static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_
     ca.incremental = incremental;
     if (stats) memset(stats, 0, sizeof(*stats));
     if (wait_before_rhs) GBP_CUDA(cudaStreamWaitEvent(p->stream, wait_before_rhs, 0));
-    return p->nodal->project(ra, ca, p_nd, incremental, nullptr, stats, phi_copy);
+    return p->nodal->project(ra, ca, p_nd, incremental, nullptr, stats, phi_copy, out_slabs);
 }
 
 int gbp_mac_set_beta(gbp_plan* p, const gbp_array4* bx, const gbp_array4* by, const gbp_array4* bz,
@@ -1101,16 +1107,19 @@ int gbp_apply_nodal_projection_host(gbp_plan* p, double* vel, const double* rho,
     ap.jstride = nx + 1;
     ap.kstride = (long long)(nx + 1) * (ny + 1);
     ap.nstride = (long long)nn;
-    // p_nd goes back on the copy stream as soon as it is stored, while the velocity correction runs
+    // p_nd goes back on the copy stream as soon as it is stored, then the velocity and gp slab by slab
+    // while the correction of the next slab runs
     gbp::HostCopy pc{p_nd, dp, nn * sizeof(double), c, p->ev_phi};
+    if (!p->ev_slab[0])
+        for (auto& e : p->ev_slab) GBP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    const int nslabs = std::min(kHostSlabs, std::max(1, nz / 16));
+    gbp::HostSlabs os{vel, gp, dvel, dgp, (size_t)nx * ny, nc, nslabs, c, p->ev_slab};
     int rc = apply_nodal_impl(p, &av, nullptr, rho ? &ar : nullptr, rho0, &ag, p_nd ? &ap : nullptr, 0.0, 1.0, 1.0,
-                              scaling_factor, incremental, 0, stats, p->ev_in, p_nd ? &pc : nullptr);
+                              scaling_factor, incremental, 0, stats, p->ev_in, p_nd ? &pc : nullptr, &os);
     if (rc != GBP_OK && rc != GBP_NOT_CONVERGED) {
         cudaStreamSynchronize(c);
         return rc;
     }
-    GBP_CUDA(cudaMemcpyAsync(vel, dvel, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, s));
-    GBP_CUDA(cudaMemcpyAsync(gp, dgp, 3 * nc * sizeof(double), cudaMemcpyDeviceToHost, s));
     GBP_CUDA(cudaStreamSynchronize(s));
     GBP_CUDA(cudaStreamSynchronize(c));
     return rc;

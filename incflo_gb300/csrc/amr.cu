@@ -109,12 +109,20 @@ __global__ void k_amr_classify_fine(NodalGeom gf, const unsigned char* __restric
 }
 
 // local fine node of global fine node position g (periodic wrap in the fine box), or false
+// v into [0, n) for arguments a few periods out at most (integer division is slow on the GPU)
+__device__ __forceinline__ int wrap_period(int v, int n)
+{
+    while (v < 0) v += n;
+    while (v >= n) v -= n;
+    return v;
+}
+
 __device__ __forceinline__ bool fine_local(const NodalGeom& gf, const int off[3], const int gpos[3], int out[3])
 {
     for (int d = 0; d < 3; ++d) {
         int v = gpos[d] - off[d];
         if (gf.per[d]) {
-            v = (v % gf.n[d] + gf.n[d]) % gf.n[d];
+            v = wrap_period(v, gf.n[d]);
         } else if (v < 0 || v >= gf.nu[d]) {
             return false;
         }
@@ -260,7 +268,7 @@ __global__ void k_amr_mask_sigma(long long count, const double* __restrict__ s, 
 // ------------------------------------------------------------------------------ composite operator
 __device__ __forceinline__ int cwrap(const NodalGeom& gc, int d, int v)
 {
-    return gc.per[d] ? (v % gc.n[d] + gc.n[d]) % gc.n[d] : v;
+    return gc.per[d] ? wrap_period(v, gc.n[d]) : v;
 }
 
 // interface values of the fine level from the coarse one: aligned nodes copy, hanging nodes
@@ -353,15 +361,18 @@ __global__ void k_amr_norm_c(NodalGeom gc, const unsigned char* __restrict__ ccl
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    double nv = 0.0;
+    unsigned long long key = 0;  // as in k_amr_norm_f
     if (i < gc.nu[0] && j < gc.nu[1] && k < gc.nu[2]) {
         const long long p = pidx(gc.sy, gc.sz, i, j, k);
         const unsigned char c = ccls[p];
-        if (c == C_DOF || c == C_IFACE) nv = fabs(v[p]) * node_inv_volume(gc, i, j, k);
-        if (v[p] != v[p] && (c == C_DOF || c == C_IFACE)) nv = v[p];
+        if (c == C_DOF || c == C_IFACE) {
+            const int e = (!gc.per[0] && (i == 0 || i == gc.n[0])) + (!gc.per[1] && (j == 0 || j == gc.n[1])) +
+                          (!gc.per[2] && (k == 0 || k == gc.n[2]));
+            key = e == 0 ? abs_key(v[p]) : abs_key(v[p] * (double)(1 << e));
+        }
     }
-    nv = block_max(nv);
-    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, nv);
+    key = block_max_key(key);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, key_value(key) * gc.ivol);
 }
 __global__ void k_amr_norm_f(NodalGeom gf, const unsigned char* __restrict__ fcls, const double* __restrict__ v,
                              unsigned long long* norm)
@@ -369,13 +380,19 @@ __global__ void k_amr_norm_f(NodalGeom gf, const unsigned char* __restrict__ fcl
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    double nv = 0.0;
+    // max |v| / node volume as an integer key of |v| 2^e (volume V / 2^e on e non-periodic boundary
+    // planes): no FP64 instruction on interior nodes, one multiplication by 1/V per block
+    unsigned long long key = 0;
     if (i < gf.nu[0] && j < gf.nu[1] && k < gf.nu[2]) {
         const long long p = pidx(gf.sy, gf.sz, i, j, k);
-        if (fcls[p] == F_DOF) nv = v[p] != v[p] ? v[p] : fabs(v[p]) * node_inv_volume(gf, i, j, k);
+        if (fcls[p] == F_DOF) {
+            const int e = (!gf.per[0] && (i == 0 || i == gf.n[0])) + (!gf.per[1] && (j == 0 || j == gf.n[1])) +
+                          (!gf.per[2] && (k == 0 || k == gf.n[2]));
+            key = e == 0 ? abs_key(v[p]) : abs_key(v[p] * (double)(1 << e));
+        }
     }
-    nv = block_max(nv);
-    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, nv);
+    key = block_max_key(key);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, key_value(key) * gf.ivol);
 }
 
 // restriction of the composite residual to the whole coarse level: the coarse unknowns' own residual

@@ -834,13 +834,13 @@ __global__ void __launch_bounds__(256) k_to_f32(NodalGeom g, const double* __res
 //   4h G_x = (S10 + S11) - (S00 + S01), 4h G_y = (S01 + S11) - (S00 + S10), 4h G_z = (D00 + D10) + (D01 + D11)
 // (Sab = node column (i+a, j+b)), 9 additions instead of 21.
 __global__ void __launch_bounds__(ZTX* ZTY) k_nodal_correct(NodalGeom g, CorrArgs a, const double* __restrict__ s64,
-                                                            const double* __restrict__ phi, int kchunk)
+                                                            const double* __restrict__ phi, int kchunk, int k0, int k1)
 {
     __shared__ double S[2][ZTY][ZTX], D[2][ZTY][ZTX];
     const int tx = threadIdx.x % ZTX, ty = threadIdx.x / ZTX;
     const int ni = blockIdx.x * ZX + tx, nj = blockIdx.y * ZY + ty;  // node column; cell column = same
-    const int kbeg = blockIdx.z * kchunk;
-    const int kend = min(kbeg + kchunk, g.n[2]);
+    const int kbeg = k0 + blockIdx.z * kchunk;
+    const int kend = min(kbeg + kchunk, k1);
     // node columns 0..n (index n: the periodic alias or the high boundary node)
     const bool has_node = ni <= g.n[0] && nj <= g.n[1];
     const bool cell = tx < ZX && ty < ZY && ni < g.n[0] && nj < g.n[1];
@@ -1125,11 +1125,15 @@ void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale,
     k_to_f32<<<grid3(g), kBlock3, 0, st>>>(g, r, r32, scale);
 }
 
-void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st)
+void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st,
+                   int k0, int k1)
 {
+    if (k1 < 0) k1 = g.n[2];
+    if (k1 <= k0) return;
     const int bx = (g.n[0] + ZX - 1) / ZX, by = (g.n[1] + ZY - 1) / ZY;
-    const int kchunk = zchunk(bx, by, g.n[2]);
-    k_nodal_correct<<<dim3(bx, by, (g.n[2] + kchunk - 1) / kchunk), ZTX * ZTY, 0, st>>>(g, a, s64, phi, kchunk);
+    const int kchunk = zchunk(bx, by, k1 - k0);
+    k_nodal_correct<<<dim3(bx, by, (k1 - k0 + kchunk - 1) / kchunk), ZTX * ZTY, 0, st>>>(g, a, s64, phi, kchunk, k0,
+                                                                                         k1);
 }
 
 void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* phi, int accumulate, cudaStream_t st)

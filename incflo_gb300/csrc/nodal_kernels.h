@@ -69,7 +69,9 @@ void nodal_norm(const NodalGeom& g, const double* v, unsigned long long* norm, c
 template <typename TE>
 void nodal_add_correction(const NodalGeom& g, double* x, const TE* e, double inv_scale, cudaStream_t st);
 void nodal_to_f32(const NodalGeom& g, const double* r, float* r32, double scale, cudaStream_t st);
-void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st);
+// cell planes k0 .. k1-1 (k1 < 0: to the last plane)
+void nodal_correct(const NodalGeom& g, const CorrArgs& a, const double* s64, const double* phi, cudaStream_t st,
+                   int k0 = 0, int k1 = -1);
 void nodal_store_phi(const NodalGeom& g, const gbp_array4& out, const double* phi, int accumulate, cudaStream_t st);
 void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaStream_t st);
 // streaming reference: out = a + b + c over n floats (n a multiple of 4, 16-byte aligned arrays)

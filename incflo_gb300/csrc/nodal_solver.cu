@@ -1208,7 +1208,8 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
 }
 
 int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
-                         const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy)
+                         const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy,
+                         const HostSlabs* out_slabs)
 {
     if (!sigma_ready) {
         set_error("nodal project: sigma was never set on this plan");
@@ -1255,9 +1256,38 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
     }
     CorrArgs ca = corr;
     if (eb.on) ca.cmask = eb.e.reg;
-    nodal_correct(l0.g, ca, l0.s64, phi, st);
-    ++nk;
-    if (eb.on) eb_correct(l0.g, eb.e, corr, phi, st);
+    if (out_slabs && out_slabs->nslabs > 0 && !eb.on) {
+        // correction by z-slabs, each slab's velocity and gp copied out while the next is corrected
+        const HostSlabs& o = *out_slabs;
+        const int nz = l0.g.n[2];
+        for (int q = 0; q < o.nslabs; ++q) {
+            const int k0 = (int)((long long)nz * q / o.nslabs), k1 = (int)((long long)nz * (q + 1) / o.nslabs);
+            if (k1 <= k0) continue;
+            nodal_correct(l0.g, ca, l0.s64, phi, st, k0, k1);
+            ++nk;
+            GBP_CUDA(cudaEventRecord(o.ev[q], st));
+            GBP_CUDA(cudaStreamWaitEvent(o.stream, o.ev[q], 0));
+            const size_t off = (size_t)k0 * o.plane, cnt = (size_t)(k1 - k0) * o.plane;
+            for (int c = 0; c < 3; ++c) {
+                GBP_CUDA(cudaMemcpyAsync(o.hvel + c * o.ncell + off, o.dvel + c * o.ncell + off, cnt * sizeof(double),
+                                         cudaMemcpyDeviceToHost, o.stream));
+                GBP_CUDA(cudaMemcpyAsync(o.hgp + c * o.ncell + off, o.dgp + c * o.ncell + off, cnt * sizeof(double),
+                                         cudaMemcpyDeviceToHost, o.stream));
+            }
+        }
+    } else {
+        nodal_correct(l0.g, ca, l0.s64, phi, st);
+        ++nk;
+        if (eb.on) eb_correct(l0.g, eb.e, corr, phi, st);
+        if (out_slabs && out_slabs->nslabs > 0) {
+            // cut cells: one copy after the whole correction
+            const HostSlabs& o = *out_slabs;
+            GBP_CUDA(cudaEventRecord(o.ev[0], st));
+            GBP_CUDA(cudaStreamWaitEvent(o.stream, o.ev[0], 0));
+            GBP_CUDA(cudaMemcpyAsync(o.hvel, o.dvel, 3 * o.ncell * sizeof(double), cudaMemcpyDeviceToHost, o.stream));
+            GBP_CUDA(cudaMemcpyAsync(o.hgp, o.dgp, 3 * o.ncell * sizeof(double), cudaMemcpyDeviceToHost, o.stream));
+        }
+    }
     GBP_CUDA(cudaEventRecord(ev2, st));
     GBP_CUDA(cudaGetLastError());
     if (stats) {

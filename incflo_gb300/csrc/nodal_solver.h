@@ -27,6 +27,20 @@ struct HostCopy {
     cudaEvent_t ev;
 };
 
+// The corrected cell fields copied back by z-slabs, each slab's copies issued on `stream` as soon as its
+// correction is done (velocity and gp, 3 components each, component-major without ghost cells:
+// component c of cell plane k starts at c * ncell + k * plane).
+struct HostSlabs {
+    double* hvel;
+    double* hgp;
+    const double* dvel;
+    const double* dgp;
+    size_t plane, ncell;
+    int nslabs;
+    cudaStream_t stream;
+    cudaEvent_t* ev;  // nslabs events
+};
+
 struct DevicePool {
     char* base = nullptr;
     size_t bytes = 0;
@@ -72,7 +86,8 @@ public:
     // phi_copy: a copy (e.g. p_nd to the host) issued on its own stream once phi_out is stored,
     // overlapping the velocity correction
     int project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
-                const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy = nullptr);
+                const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy = nullptr,
+                const HostSlabs* out_slabs = nullptr);
 
     // nodal divergence of vel as the projection sees it (consistent for singular systems), strong form
     int divergence(const RhsArgs& rhs, const gbp_array4* out, double* max_norm);

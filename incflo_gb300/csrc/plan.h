@@ -7,6 +7,8 @@
 #include "mac_solver.h"
 #include "nodal_solver.h"
 
+constexpr int kHostSlabs = 8;
+
 struct gbp_plan {
     int kind;
     cudaStream_t stream;
@@ -20,6 +22,7 @@ struct gbp_plan {
     size_t hbuf_bytes = 0;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_in = nullptr, ev_phi = nullptr, ev_out = nullptr;
+    cudaEvent_t ev_slab[kHostSlabs] = {};  // one per z-slab of the copy-out
     double* dflux = nullptr;  // 2 device doubles: inflow / outflow of the solvability fix
     double* ccbuf = nullptr;  // cell-centred projection scratch (unprojected face velocities, phi)
 };

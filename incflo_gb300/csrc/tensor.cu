@@ -15,7 +15,6 @@ namespace gbp {
 namespace {
 
 constexpr double kFourThirds = 4.0 / 3.0;
-constexpr double kTwoThirds = 2.0 / 3.0;
 
 __device__ __forceinline__ double at(const gbp_array4& a, int i, int j, int k, int n)
 {
@@ -189,53 +188,84 @@ __global__ void k_tensor_ghost(CellGeom g, int d, int bl0, int bl1, int bl2, int
     }
 }
 
-// tau_{c,d} (c = 0..2) on the face between cells L and R of direction d
-__device__ __forceinline__ void face_tau(const CU3& u, int d, long long L, long long R, const long long s[3],
-                                         const double ih[3], double eta, double tau[3])
+// Host-computed scale factors (FP64 division and most FP64 arithmetic are kept out of the kernels: GB300
+// issues FP64 at 1/64 of the FP32 rate, and these kernels are bound by it)
+struct FaceK {
+    double ih[3];   // 1 / h_d
+    double q[3];    // 1 / (4 h_e): tangential derivative from the four-cell difference sum
+    double n43[3];  // (4/3) / h_d
+    double t23[3];  // (2/3) / (4 h_e)
+};
+
+// tau_{c,d} / h_d (c = 0..2) on the face between cells L and R of direction d
+template <int d>
+__device__ __forceinline__ void face_tau(const CU3& u, long long L, long long R, const long long s[3], const FaceK& K,
+                                         double eta, double tau[3])
 {
-    double N[3];
-#pragma unroll
-    for (int m = 0; m < 3; ++m) N[m] = (u.c[m][R] - u.c[m][L]) * ih[d];
-    // T[m][e]: tangential derivative of component m along e (e != d)
-    auto T = [&](int m, int e) {
-        const double* x = u.c[m];
-        return ((x[R + s[e]] - x[R - s[e]]) + (x[L + s[e]] - x[L - s[e]])) * (0.25 * ih[e]);
-    };
-    const int e1 = d == 0 ? 1 : 0, e2 = d == 2 ? 1 : 2;
-    tau[d] = eta * (kFourThirds * N[d] - kTwoThirds * (T(e1, e1) + T(e2, e2)));
-    tau[e1] = eta * (N[e1] + T(d, e1));
-    tau[e2] = eta * (N[e2] + T(d, e2));
+    constexpr int e1 = d == 0 ? 1 : 0, e2 = d == 2 ? 1 : 2;
+    const double* u0 = u.c[d];
+    const double* u1 = u.c[e1];
+    const double* u2 = u.c[e2];
+    // four-cell difference sums (tangential derivatives times 4 h_e)
+    const double Tdd1 = (u0[R + s[e1]] - u0[R - s[e1]]) + (u0[L + s[e1]] - u0[L - s[e1]]);
+    const double Tdd2 = (u0[R + s[e2]] - u0[R - s[e2]]) + (u0[L + s[e2]] - u0[L - s[e2]]);
+    const double T11 = (u1[R + s[e1]] - u1[R - s[e1]]) + (u1[L + s[e1]] - u1[L - s[e1]]);
+    const double T22 = (u2[R + s[e2]] - u2[R - s[e2]]) + (u2[L + s[e2]] - u2[L - s[e2]]);
+    const double a = eta * K.ih[d];
+    double t = K.n43[d] * (u0[R] - u0[L]);
+    t = fma(-K.t23[e1], T11, t);
+    t = fma(-K.t23[e2], T22, t);
+    tau[d] = a * t;
+    tau[e1] = a * fma(K.q[e1], Tdd1, K.ih[d] * (u1[R] - u1[L]));
+    tau[e2] = a * fma(K.q[e2], Tdd2, K.ih[d] * (u2[R] - u2[L]));
 }
 
-// MODE 0: r = b - (alpha a V u - beta V div tau) per component, max |r| / V into *norm.
+// tau_{c,d} / h_d of every face of direction d (faces 0 .. n_d), once per face: fl[c] at the face's
+// padded index
+template <int d>
+__global__ void __launch_bounds__(256) k_tensor_flux(CellGeom g, CU3 u, const double* __restrict__ eta, U3 fl, FaceK K)
+{
+    int f[3] = {(int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(blockIdx.y * blockDim.y + threadIdx.y),
+                (int)(blockIdx.z * blockDim.z + threadIdx.z)};
+    for (int e = 0; e < 3; ++e)
+        if (f[e] >= g.n[e] + (e == d ? 1 : 0)) return;
+    const long long s[3] = {1, g.sy, g.sz};
+    const long long R = pidx(g.sy, g.sz, f[0], f[1], f[2]);
+    double tau[3];
+    face_tau<d>(u, R - s[d], R, s, K, eta[R], tau);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fl.c[c][R] = tau[c];
+}
+
+struct Fl9 {
+    const double* f[3][3];  // [direction][component]
+};
+
+// MODE 0: r = b - (alpha a V u - beta V div tau) per component, max |r| / V into *norm (bvol = beta V).
 // MODE 1: out(i, j, k, c) = div tau.
 template <int MODE>
-__global__ void __launch_bounds__(256) k_tensor_resid(CellGeom g, CU3 u, CU3 eta, const double* __restrict__ a64,
-                                                      double beta, CU3 b, U3 r, unsigned long long* norm,
-                                                      gbp_array4 out)
+__global__ void __launch_bounds__(256) k_tensor_div(CellGeom g, Fl9 fl, CU3 u, const double* __restrict__ a64,
+                                                    double bvol, double ivol, CU3 b, U3 r, unsigned long long* norm,
+                                                    gbp_array4 out)
 {
     int i, j, k;
-    double nv = 0.0;
+    unsigned long long key = 0;
     if (cell3(g, i, j, k)) {
         const long long p = pidx(g.sy, g.sz, i, j, k);
         const long long s[3] = {1, g.sy, g.sz};
-        const double ih[3] = {1.0 / g.h[0], 1.0 / g.h[1], 1.0 / g.h[2]};
-        double div[3] = {0.0, 0.0, 0.0};
+        double div[3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            double tl[3], th[3];
-            face_tau(u, d, p - s[d], p, s, ih, eta.c[d][p], tl);
-            face_tau(u, d, p, p + s[d], s, ih, eta.c[d][p + s[d]], th);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) div[c] += (th[c] - tl[c]) * ih[d];
-        }
+        for (int c = 0; c < 3; ++c)
+            div[c] = ((fl.f[0][c][p + s[0]] - fl.f[0][c][p]) + (fl.f[1][c][p + s[1]] - fl.f[1][c][p])) +
+                     (fl.f[2][c][p + s[2]] - fl.f[2][c][p]);
         if (MODE == 0) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const double ax = (a64 ? a64[p] * u.c[c][p] : 0.0) - beta * g.vol * div[c];
+                const double ax = a64 ? fma(a64[p], u.c[c][p], -bvol * div[c]) : -bvol * div[c];
                 const double v = b.c[c][p] - ax;
                 r.c[c][p] = v;
-                nv = fmax(nv, v != v ? v : fabs(v) / g.vol);
+                const unsigned long long kv = abs_key(v);
+                key = kv > key ? kv : key;
             }
         } else {
 #pragma unroll
@@ -243,8 +273,8 @@ __global__ void __launch_bounds__(256) k_tensor_resid(CellGeom g, CU3 u, CU3 eta
         }
     }
     if (MODE == 0) {
-        nv = block_max(nv);
-        if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, nv);
+        key = block_max_key(key);
+        if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, key_value(key) * ivol);
     }
 }
 
@@ -262,6 +292,14 @@ inline double bits_to_double(unsigned long long b)
 }
 
 }  // namespace
+
+static Fl9 make_fl9(double* const fl[3][3])
+{
+    Fl9 t{};
+    for (int d = 0; d < 3; ++d)
+        for (int c = 0; c < 3; ++c) t.f[d][c] = fl[d][c];
+    return t;
+}
 
 TensorSolver::~TensorSolver()
 {
@@ -310,7 +348,7 @@ int TensorSolver::init(const gbp_geometry& g, const int bc_lo[9], const int bc_h
     }
     const CellGeom& cg = comp[0].finest();
     const size_t cnt = (size_t)cg.count;
-    int rc = pool.reserve(12 * (cnt * sizeof(double) + 256) + 4096);
+    int rc = pool.reserve(21 * (cnt * sizeof(double) + 256) + 4096);
     if (rc) return rc;
     for (int c = 0; c < 3; ++c) {
         u[c] = pool.take<double>(cnt);
@@ -319,6 +357,11 @@ int TensorSolver::init(const gbp_geometry& g, const int bc_lo[9], const int bc_h
         eta[c] = pool.take<double>(cnt);
         for (double* q : {u[c], rhs[c], r[c], eta[c]}) GBP_CUDA(cudaMemsetAsync(q, 0, sizeof(double) * cnt, st));
     }
+    for (int d = 0; d < 3; ++d)
+        for (int c = 0; c < 3; ++c) {
+            fl[d][c] = pool.take<double>(cnt);
+            GBP_CUDA(cudaMemsetAsync(fl[d][c], 0, sizeof(double) * cnt, st));
+        }
     dnorm = pool.take<unsigned long long>(4);
     GBP_CUDA(cudaMallocHost(&hnorm, 4 * sizeof(unsigned long long)));
     GBP_CUDA(cudaEventCreate(&ev0));
@@ -398,6 +441,31 @@ void TensorSolver::load(const gbp_array4& vel)
     k_tensor_load<<<cells_grid(g), kBlk, 0, st>>>(g, vel, U3{{u[0], u[1], u[2]}});
 }
 
+void TensorSolver::fluxes()
+{
+    const CellGeom& g = comp[0].finest();
+    const CU3 uc{{u[0], u[1], u[2]}};
+    FaceK K;
+    for (int d = 0; d < 3; ++d) {
+        K.ih[d] = 1.0 / g.h[d];
+        K.q[d] = 0.25 / g.h[d];
+        K.n43[d] = (4.0 / 3.0) / g.h[d];
+        K.t23[d] = (2.0 / 3.0) * 0.25 / g.h[d];
+    }
+    for (int d = 0; d < 3; ++d) {
+        int fn[3] = {g.n[0], g.n[1], g.n[2]};
+        fn[d] += 1;
+        dim3 grid((unsigned)((fn[0] + 31) / 32), (unsigned)((fn[1] + 3) / 4), (unsigned)((fn[2] + 1) / 2));
+        const U3 out{{fl[d][0], fl[d][1], fl[d][2]}};
+        if (d == 0)
+            k_tensor_flux<0><<<grid, kBlk, 0, st>>>(g, uc, eta[0], out, K);
+        else if (d == 1)
+            k_tensor_flux<1><<<grid, kBlk, 0, st>>>(g, uc, eta[1], out, K);
+        else
+            k_tensor_flux<2><<<grid, kBlk, 0, st>>>(g, uc, eta[2], out, K);
+    }
+}
+
 void TensorSolver::fill_ghosts(const gbp_array4& vel)
 {
     const CellGeom& g = comp[0].finest();
@@ -425,14 +493,17 @@ int TensorSolver::solve(const gbp_array4& rhs_in, gbp_array4& vel, gbp_stats* st
         return GBP_BAD_ARG;
     }
     const CellGeom& g = comp[0].finest();
-    const CU3 uc{{u[0], u[1], u[2]}}, ec{{eta[0], eta[1], eta[2]}}, bc{{rhs[0], rhs[1], rhs[2]}};
+    const CU3 uc{{u[0], u[1], u[2]}}, bc{{rhs[0], rhs[1], rhs[2]}};
     const U3 rr{{r[0], r[1], r[2]}};
+    const Fl9 f9 = make_fl9(fl);
     GBP_CUDA(cudaEventRecord(ev0, st));
     GBP_CUDA(cudaMemsetAsync(dnorm, 0, 4 * sizeof(unsigned long long), st));
     k_tensor_rhs<<<cells_grid(g), kBlk, 0, st>>>(g, rhs_in, U3{{rhs[0], rhs[1], rhs[2]}}, dnorm);
     load(vel);
     fill_ghosts(vel);
-    k_tensor_resid<0><<<cells_grid(g), kBlk, 0, st>>>(g, uc, ec, g.a64, beta, bc, rr, dnorm + 1, gbp_array4{});
+    fluxes();
+    k_tensor_div<0><<<cells_grid(g), kBlk, 0, st>>>(g, f9, uc, g.a64, beta * g.vol, 1.0 / g.vol, bc, rr, dnorm + 1,
+                                                    gbp_array4{});
     GBP_CUDA(cudaGetLastError());
     GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     GBP_CUDA(cudaStreamSynchronize(st));
@@ -461,7 +532,9 @@ int TensorSolver::solve(const gbp_array4& rhs_in, gbp_array4& vel, gbp_stats* st
         for (int c = 0; c < 3; ++c) comp[c].add_vcycle_correction(r[c], u[c], scale32);
         fill_ghosts(vel);
         GBP_CUDA(cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st));
-        k_tensor_resid<0><<<cells_grid(g), kBlk, 0, st>>>(g, uc, ec, g.a64, beta, bc, rr, dnorm + 1, gbp_array4{});
+        fluxes();
+        k_tensor_div<0><<<cells_grid(g), kBlk, 0, st>>>(g, f9, uc, g.a64, beta * g.vol, 1.0 / g.vol, bc, rr, dnorm + 1,
+                                                        gbp_array4{});
         GBP_CUDA(cudaGetLastError());
         GBP_CUDA(cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         GBP_CUDA(cudaStreamSynchronize(st));
@@ -506,9 +579,10 @@ int TensorSolver::apply(const gbp_array4& vel, gbp_array4& out)
     const CellGeom& g = comp[0].finest();
     load(vel);
     fill_ghosts(vel);
-    k_tensor_resid<1><<<cells_grid(g), kBlk, 0, st>>>(g, CU3{{u[0], u[1], u[2]}}, CU3{{eta[0], eta[1], eta[2]}},
-                                                      nullptr, 0.0, CU3{{nullptr, nullptr, nullptr}},
-                                                      U3{{nullptr, nullptr, nullptr}}, nullptr, out);
+    fluxes();
+    k_tensor_div<1><<<cells_grid(g), kBlk, 0, st>>>(g, make_fl9(fl), CU3{{u[0], u[1], u[2]}}, nullptr, 0.0, 0.0,
+                                                    CU3{{nullptr, nullptr, nullptr}}, U3{{nullptr, nullptr, nullptr}},
+                                                    nullptr, out);
     GBP_CUDA(cudaGetLastError());
     GBP_CUDA(cudaStreamSynchronize(st));
     return GBP_OK;

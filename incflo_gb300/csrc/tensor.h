@@ -44,6 +44,7 @@ private:
     int check_vel(const gbp_array4& v, bool need_ghosts) const;
     void load(const gbp_array4& vel);
     void fill_ghosts(const gbp_array4& vel);
+    void fluxes();  // tau on every face, once per face
 
     gbp_options opt{};
     cudaStream_t st = nullptr;
@@ -55,6 +56,7 @@ private:
     double* rhs[3] = {};
     double* r[3] = {};
     double* eta[3] = {};
+    double* fl[3][3] = {};  // [face direction][component]: tau_{c,d} on the faces of direction d
     double alpha = 0.0, beta = 0.0;
     bool ready = false;
     unsigned long long *dnorm = nullptr, *hnorm = nullptr;
