@@ -706,6 +706,12 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     add(3 * ncf, 8);                               // velo_f
     add(ncf, 8);                                   // sig_f
     add(nnf, 8);                                   // p_fb
+    // the shared-sum FP64 residual on both levels (isotropic cells): four edge-weight arrays each
+    qsw = qsweep_supported(gf_nomask) && qsweep_supported(gc);
+    if (qsw) {
+        for (int q = 0; q < 4; ++q) add(gf.count, 8);
+        for (int q = 0; q < 4; ++q) add(gc.count, 8);
+    }
     nparts = std::max(nodal_partials_needed(gc), 1184);
     add(nparts + 64, 8);
     add(8, 8);
@@ -717,6 +723,12 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     cmask_f = pool.take<unsigned char>(gf.count);
     ccls = pool.take<unsigned char>(gc.count);
     fcls = pool.take<unsigned char>(gf.count);
+    if (qsw) {
+        double** wf[4] = {&qwf.wsum, &qwf.wx, &qwf.wy, &qwf.wz};
+        double** wc[4] = {&qwc.wsum, &qwc.wx, &qwc.wy, &qwc.wz};
+        for (int q = 0; q < 4; ++q) *wf[q] = pool.take<double>(gf.count);
+        for (int q = 0; q < 4; ++q) *wc[q] = pool.take<double>(gc.count);
+    }
     sc_m = pool.take<double>(gc.count);
     sc_t = pool.take<double>(gc.count);
     phi_c = pool.take<double>(gc.count);
@@ -809,6 +821,23 @@ int CompositeNodal::check_fields(const AmrFields& f)
     return GBP_OK;
 }
 
+// FP64 residuals of the composite operator's two parts (fine bounding box without the overset mask,
+// coarse level with covered cells' sigma zeroed): the shared-sum form when the cells are isotropic
+void CompositeNodal::resid_f(const double* x, const double* b, double* r)
+{
+    if (qsw)
+        nodal_qsweep64(gf_nomask, 1, fin.sigma64(), qwf, x, b, r, 1.0, nullptr, st);
+    else
+        nodal_resid<double>(gf_nomask, fin.sigma64(), x, b, r, nullptr, st);
+}
+void CompositeNodal::resid_c(const double* x, const double* b, double* r)
+{
+    if (qsw)
+        nodal_qsweep64(gc, 1, sc_m, qwc, x, b, r, 1.0, nullptr, st);
+    else
+        nodal_resid<double>(gc, sc_m, x, b, r, nullptr, st);
+}
+
 // v_c (coarse interface nodes) += the restricted interface values of v_f
 void CompositeNodal::sync(double* vc, const double* vf)
 {
@@ -820,8 +849,8 @@ void CompositeNodal::sync(double* vc, const double* vf)
 void CompositeNodal::composite_residual(const double* bc, const double* bf, unsigned long long* norm)
 {
     k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], phi_c, phi_f);
-    nodal_resid<double>(gf_nomask, fin.sigma64(), phi_f, bf, r_f, nullptr, st);
-    nodal_resid<double>(gc, sc_m, phi_c, bc, r_c, nullptr, st);
+    resid_f(phi_f, bf, r_f);
+    resid_c(phi_c, bc, r_c);
     sync(r_c, r_f);
     if (norm) {
         k_amr_norm_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, r_c, norm);
@@ -894,6 +923,10 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     sa.nstride = (long long)ncf;
     rc = fin.set_sigma(&sa, 0.0);
     if (rc) return rc;
+    if (qsw) {
+        nodal_qweights64(gf_nomask, fin.sigma64(), qwf, st);
+        nodal_qweights64(gc, sc_m, qwc, st);
+    }
     // right-hand sides: leaf cells of each level, then the fine interface into the coarse interface
     const bool sub_old = f.incremental && f.vel_old_c;
     auto cellsf = [&](double* d, int nc_) {
@@ -979,7 +1012,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
         k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], e_c, phi_f);
         // fine correction on the fresh fine residual, interface held
         k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], phi_c, phi_f);
-        nodal_resid<double>(gf_nomask, fin.sigma64(), phi_f, b_f, r_f, nullptr, st);
+        resid_f(phi_f, b_f, r_f);
         fin.apply_vcycles(r_f, phi_f, m, scale32, st);
         // composite residual and its norm
         GBP_CUDA(cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st));

@@ -23,6 +23,7 @@
 
 #include "incflo_gb300.h"
 #include "nodal_solver.h"
+#include "nodal_sweep.h"
 
 namespace gbp {
 
@@ -58,6 +59,8 @@ private:
     int check_fields(const AmrFields& f);
     void composite_residual(const double* bc, const double* bf, unsigned long long* norm);
     void sync(double* vc, const double* vf);
+    void resid_f(const double* x, const double* b, double* r);
+    void resid_c(const double* x, const double* b, double* r);
 
     gbp_options opt{};
     cudaStream_t st = nullptr;
@@ -80,6 +83,8 @@ private:
     double *scal = nullptr, *part = nullptr;
     int nparts = 0;
     unsigned long long *dnorm = nullptr, *hnorm = nullptr;
+    bool qsw = false;      // shared-sum FP64 residuals (isotropic cells)
+    QWeights qwf{}, qwc{};  // their edge weights, fine and coarse
     void* dboxes = nullptr;  // device table for the batched box kernels
     size_t dboxes_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -136,10 +136,26 @@ int NodalSolver::set_options(const gbp_options& o)
     const int maxc = opt.max_coarsening_level;
     opt = o;
     opt.max_coarsening_level = maxc;  // hierarchy depth is fixed at plan creation
+    set_omega();
     if (regraph) {
         drop_graphs();
     }
     return GBP_OK;
+}
+
+// The smoother's weight: the requested omega, capped by the Gershgorin bound of the Jacobi-scaled
+// operator, lambda_max(D^-1 A) <= 1 + sum_{q != 0} |K_q| / K_0 per element (every cell's row of a node has
+// that ratio, so the sigma-weighted sum does too). Cubic cells give 1 + 1 and keep omega = 0.85; cells
+// stretched beyond an aspect ratio of about 2 have positive couplings, a larger bound, and a damped
+// Jacobi at 0.85 that would diverge. All levels share the ratio (every direction coarsens by 2).
+void NodalSolver::set_omega()
+{
+    omega_eff = opt.omega;
+    if (L.empty()) return;
+    const double* K = L[0].g.K;
+    double off = 0.0;
+    for (int q = 1; q < 8; ++q) off += fabs(K[q]);
+    if (K[0] > 0.0) omega_eff = std::min(opt.omega, 0.85 * 2.0 / (1.0 + off / K[0]));
 }
 
 int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_hi[3], const gbp_options& o,
@@ -197,6 +213,7 @@ int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc
             ch[d] *= 2.0;
         }
     }
+    set_omega();
     const NodalLevel& B = L.back();
     if ((long long)B.g.nu[0] * B.g.nu[1] * B.g.nu[2] > 200000) {
         set_error("nodal plan: the coarsest level is too large for the single-CTA bottom solver "
@@ -462,12 +479,12 @@ void NodalSolver::jacobi(const NodalGeom& g, const T* s, const T* x, const T* b,
 {
     if (sizeof(T) == 8 && use_qsweep && &g == &L[0].g) {
         nodal_qsweep64(g, 0, reinterpret_cast<const double*>(s), qw, reinterpret_cast<const double*>(x),
-                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(out), opt.omega, nullptr, s_);
+                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(out), omega_eff, nullptr, s_);
     } else if (use_tma && sweep_supported(g, (int)sizeof(T))) {
-        int rc = nodal_sweep<T>(g, 0, s, x, b, out, opt.omega, derr, nullptr, s_);
+        int rc = nodal_sweep<T>(g, 0, s, x, b, out, omega_eff, derr, nullptr, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else {
-        nodal_jacobi<T>(g, s, x, b, out, opt.omega, false, s_);
+        nodal_jacobi<T>(g, s, x, b, out, omega_eff, false, s_);
     }
 }
 
@@ -477,9 +494,9 @@ void NodalSolver::resid(const NodalGeom& g, const T* s, const T* x, const T* b, 
 {
     if (sizeof(T) == 8 && use_qsweep && &g == &L[0].g) {
         nodal_qsweep64(g, 1, reinterpret_cast<const double*>(s), qw, reinterpret_cast<const double*>(x),
-                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(r), opt.omega, norm, s_);
+                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(r), omega_eff, norm, s_);
     } else if (use_tma && sweep_supported(g, (int)sizeof(T))) {
-        int rc = nodal_sweep<T>(g, 1, s, x, b, r, opt.omega, derr, norm, s_);
+        int rc = nodal_sweep<T>(g, 1, s, x, b, r, omega_eff, derr, norm, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else {
         nodal_resid<T>(g, s, x, b, r, norm, s_);
@@ -505,8 +522,8 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     const bool cut = l == 0 && eb.on;
     if (zero) {
         if (pre > 0) {
-            nodal_jacobi<T>(lv.g, B::s(lv), nullptr, b, x, opt.omega, true, s);
-            if (cut) eb_nodes<T>(lv.g, eb.e, 0, nullptr, b, x, opt.omega, s);
+            nodal_jacobi<T>(lv.g, B::s(lv), nullptr, b, x, omega_eff, true, s);
+            if (cut) eb_nodes<T>(lv.g, eb.e, 0, nullptr, b, x, omega_eff, s);
             ++nk;
             --pre;
         } else {
@@ -515,12 +532,12 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     }
     for (int q = 0; q < pre; ++q) {
         jacobi<T>(lv.g, B::s(lv), x, b, t, s);
-        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, opt.omega, s);
+        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, omega_eff, s);
         ++nk;
         std::swap(x, t);
     }
     resid<T>(lv.g, B::s(lv), x, b, B::r(lv), nullptr, s);
-    if (cut) eb_nodes<T>(lv.g, eb.e, 1, x, b, B::r(lv), opt.omega, s);
+    if (cut) eb_nodes<T>(lv.g, eb.e, 1, x, b, B::r(lv), omega_eff, s);
     const NodalLevel& cv = L[l + 1];
     nodal_restrict<T>(lv.g, cv.g, B::r(lv), B::b(cv), s);
     nk += 2;
@@ -529,7 +546,7 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     ++nk;
     for (int q = 0; q < opt.nu2; ++q) {
         jacobi<T>(lv.g, B::s(lv), x, b, t, s);
-        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, opt.omega, s);
+        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, omega_eff, s);
         ++nk;
         std::swap(x, t);
     }
@@ -545,7 +562,7 @@ void NodalSolver::resid0(const double* x, const double* b, double* r, unsigned l
         return;
     }
     resid<double>(l0.g, l0.s64, x, b, r, nullptr, s);
-    eb_nodes<double>(l0.g, eb.e, 1, x, b, r, opt.omega, s);
+    eb_nodes<double>(l0.g, eb.e, 1, x, b, r, omega_eff, s);
     if (norm) eb_norm(l0.g, r, eb.ivol, norm, s);
 }
 
@@ -1335,7 +1352,7 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
         case 6: nodal_prolong_add<float>(g, L[1].g, L[1].x32, l0.x32, st); break;
         case 7: nodal_restrict<float>(g, L[1].g, l0.r32, L[1].b32, st); break;
         default:
-            nodal_jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, opt.omega,
+            nodal_jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, omega_eff,
                                 false, st);
             break;
         }

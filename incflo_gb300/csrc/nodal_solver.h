@@ -152,6 +152,8 @@ private:
     unsigned long long* dnorm = nullptr;  // [0] rhs norm, [1] residual norm
     unsigned long long* hnorm = nullptr;  // pinned mirror
     bool singular = false;        // the system has the constants as null space (consistent RHS, gauge)
+    double omega_eff = 0.85;  // the smoother weight in use (see set_omega)
+    void set_omega();
     bool bsing = false;           // the coarsest operator does (no node held at 0 on it)
     bool singular_faces = false;  // singular from the boundary types alone (no overset mask)
     int rebuild_masks();

@@ -20,6 +20,7 @@ CASES = [
     ((16, 12, 20), (1.0, 0.75, 1.25), (P, P, N), (P, P, N)),
     ((12, 16, 8), (1.5, 2.0, 1.0), (N, D, P), (I, N, P)),
     ((16, 8, 8), (1.0, 1.0, 0.5), (D, N, N), (D, I, D)),   # anisotropic spacing
+    ((24, 20, 32), (1.0, 0.8, 0.4), (P, N, N), (P, N, D)),  # aspect ratio 3.3: the smoother weight is capped
     ((10, 12, 14), (1.0, 1.2, 1.4), (N, N, N), (N, N, N)),  # odd coarse sizes
     ((2, 2, 2), (1.0, 1.0, 1.0), (P, N, N), (P, N, N)),     # bottom-only hierarchy
     ((32, 32, 32), (1.0, 1.0, 1.0), (P, P, N), (P, P, N)),
