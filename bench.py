@@ -325,7 +325,7 @@ def run_eb_nodal(args, dev, steps=5, warmup=3):
 
 
 def run_tensor(args, dev, steps=3, warmup=3):
-    """ms per tensor (velocity) diffusion solve, DiffusionTensorOp::diffuse_velocity on a 256^3 channel
+    """ms per tensor (velocity) diffusion solve, DiffusionTensorOp::diffuse_velocity on an n^3 channel (256^3)
     (periodic x / z, no-slip walls y with a moving upper wall), rho 1..2 and eta 0.01..0.02 seeded
     random, dt = 0.5 h, rhs = rho u, rtol 1e-10, FP32 block V-cycles inside FP64 defect correction."""
     import torch
@@ -333,7 +333,7 @@ def run_tensor(args, dev, steps=3, warmup=3):
     from incflo_gb300 import Geometry, make_options
     from incflo_gb300.diffusion import TensorOp, diffuse_tensor_bc
 
-    n = 256
+    n = args.n
     bclo, bchi = diffuse_tensor_bc(("periodic", "no_slip_wall", "periodic"), ("periodic", "no_slip_wall", "periodic"))
     g = torch.Generator(device=dev).manual_seed(11)
     rho = 1.0 + torch.rand((n, n, n), dtype=torch.float64, device=dev, generator=g)
@@ -358,7 +358,7 @@ def run_tensor(args, dev, steps=3, warmup=3):
         if i >= warmup:
             times.append(st["ms_solve"])
     del op
-    return {"workload": "tensor (velocity) diffusion 256^3, periodic x/z, no-slip walls y, rho 1..2, eta 0.01..0.02, "
+    return {"workload": f"tensor (velocity) diffusion {n}^3, periodic x/z, no-slip walls y, rho 1..2, eta 0.01..0.02, "
                         f"dt = 0.5 h, rtol {args.rtol:g}, FP32 block V-cycles inside FP64 defect correction",
             "ms_per_solve": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
             "block_vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"]}
