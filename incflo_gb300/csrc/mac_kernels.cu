@@ -520,6 +520,54 @@ void mac_bottom(const CellGeom& g, const double* bx, const double* by, const dou
 GBP_MAC_INST(double)
 GBP_MAC_INST(float)
 
+// Dense bottom solve: x = M b with M the FP64 inverse of the coarsest operator, precomputed on the host
+// whenever the face coefficients change (singular systems: the inverse of A + c 1 1^T over the cells
+// that carry an equation, exact for a right-hand side of zero mean over them). One CTA; N <= 128.
+template <typename T>
+__global__ void __launch_bounds__(128) k_mac_bottom_dense(CellGeom g, const double* __restrict__ M,
+                                                          const unsigned char* __restrict__ act,
+                                                          const T* __restrict__ bin, T* __restrict__ xout, int singular)
+{
+    __shared__ double bb[128];
+    __shared__ double red[32];
+    const int N = g.n[0] * g.n[1] * g.n[2];
+    double s = 0.0, na = 0.0;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_cell(g, t, i, j, k);
+        const double v = act[t] ? (double)bin[pidx(g.sy, g.sz, i, j, k)] : 0.0;
+        bb[t] = v;
+        s += v;
+        na += act[t] ? 1.0 : 0.0;
+    }
+    if (singular) {
+        s = mac_block_sum(s, red);
+        na = mac_block_sum(na, red);
+        const double mean = na > 0.0 ? s / na : 0.0;
+        for (int t = threadIdx.x; t < N; t += blockDim.x)
+            if (act[t]) bb[t] -= mean;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        double a0 = 0.0;
+        for (int v = 0; v < N; ++v) a0 = fma(M[(size_t)v * N + t], bb[v], a0);
+        int i, j, k;
+        decode_cell(g, t, i, j, k);
+        store_cell(xout, g, i, j, k, (T)a0);
+    }
+}
+
+template <typename T>
+void mac_bottom_dense(const CellGeom& g, const double* M, const unsigned char* act, const T* b, T* x, int singular,
+                      cudaStream_t st)
+{
+    k_mac_bottom_dense<T><<<1, 128, 0, st>>>(g, M, act, b, x, singular);
+}
+template void mac_bottom_dense<double>(const CellGeom&, const double*, const unsigned char*, const double*, double*,
+                                       int, cudaStream_t);
+template void mac_bottom_dense<float>(const CellGeom&, const double*, const unsigned char*, const float*, float*, int,
+                                      cudaStream_t);
+
 void mac_set_beta(const CellGeom& g, int d, int source, const gbp_array4* src, double cval, int bclo, int bchi,
                   double* b64, float* b32, cudaStream_t st, const RobinFaces* rb, const double* ap, double mult)
 {

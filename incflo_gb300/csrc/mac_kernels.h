@@ -19,6 +19,11 @@ void mac_prolong_add(const CellGeom& gf, const CellGeom& gc, const T* xc, T* xf,
 template <typename T>
 void mac_bottom(const CellGeom& g, const double* bx, const double* by, const double* bz, const T* b, T* x,
                 double* scratch, int maxiter, double rtol, double atol, int singular, cudaStream_t st);
+// x = M b on the coarsest level (M: the precomputed dense inverse, act: cells with an equation)
+constexpr int kMacDenseBottomMax = 128;
+template <typename T>
+void mac_bottom_dense(const CellGeom& g, const double* M, const unsigned char* act, const T* b, T* x, int singular,
+                      cudaStream_t st);
 
 // Cut cells of an embedded boundary on the finest level (all nullptr: no EB). Padded layouts: kap like a
 // cell array, ap[d] like the face array of direction d (face (i,j,k) at pidx(i,j,k)).

@@ -46,6 +46,10 @@ void MacSolver::destroy()
     ev0 = ev1 = ev2 = nullptr;
     pool.release();
     apool.release();
+    dpool.release();
+    dmat = nullptr;
+    dact = nullptr;
+    dense_bottom = false;
     abec = false;
     eb.pool.release();
     eb = EbState{};
@@ -207,7 +211,7 @@ int MacSolver::set_beta(int source, const gbp_array4* src[3], double cval)
     eb_refresh_beta();
     GBP_CUDA(cudaGetLastError());
     beta_ready = true;
-    return GBP_OK;
+    return build_dense_bottom();
 }
 
 int MacSolver::set_abec(double alpha, const gbp_array4* a, double a0, double beta, const gbp_array4* const b[3],
@@ -269,7 +273,7 @@ int MacSolver::set_abec(double alpha, const gbp_array4* a, double a0, double bet
     GBP_CUDA(cudaGetLastError());
     beta_ready = true;
     singular = !any_dirichlet && !abec;
-    return GBP_OK;
+    return build_dense_bottom();
 }
 
 int MacSolver::abec_solve(const gbp_array4* rhs, gbp_array4* phi_io, gbp_stats* stats)
@@ -301,6 +305,132 @@ int MacSolver::abec_solve(const gbp_array4* rhs, gbp_array4* phi_io, gbp_stats* 
         stats->ms_total = ms;
     }
     return status;
+}
+
+// Dense inverse of the coarsest level's operator, assembled on the host from its face coefficients
+// (boundary factors included: 0 on walls, doubled on Dirichlet faces) and alpha a V: the same matrix the
+// smoother and the CG see. Cells whose row is empty (covered by an embedded boundary) carry no
+// equation and stay 0; a singular system is regularised with c 1 1^T over the other cells.
+int MacSolver::build_dense_bottom()
+{
+    const MacLevel& B = L.back();
+    const CellGeom& g = B.g;
+    const int N = g.n[0] * g.n[1] * g.n[2];
+    const bool was = dense_bottom;
+    dense_bottom = false;
+    // (a one-level hierarchy with cut cells has terms outside the face coefficients: keep the CG)
+    if (N > kMacDenseBottomMax || (L.size() == 1 && eb.on)) {
+        if (was && gexec) {
+            cudaGraphExecDestroy(gexec);
+            gexec = nullptr;
+        }
+        return GBP_OK;
+    }
+    if (!dmat) {
+        int rc = dpool.reserve(sizeof(double) * (size_t)N * N + (size_t)N + 1024);
+        if (rc) return rc;
+        dmat = dpool.take<double>((size_t)N * N);
+        dact = dpool.take<unsigned char>((size_t)N);
+    }
+    std::vector<double> bf[3], av;
+    for (int d = 0; d < 3; ++d) {
+        bf[d].resize((size_t)g.count);
+        GBP_CUDA(cudaMemcpyAsync(bf[d].data(), B.b64[d], sizeof(double) * g.count, cudaMemcpyDeviceToHost, st));
+    }
+    if (g.a64) {
+        av.resize((size_t)g.count);
+        GBP_CUDA(cudaMemcpyAsync(av.data(), g.a64, sizeof(double) * g.count, cudaMemcpyDeviceToHost, st));
+    }
+    GBP_CUDA(cudaStreamSynchronize(st));
+    auto cid = [&](int i, int j, int k) { return i + g.n[0] * (j + g.n[1] * k); };
+    std::vector<double> A((size_t)N * N, 0.0);
+    const long long sd[3] = {1, g.sy, g.sz};
+    for (int k = 0; k < g.n[2]; ++k)
+        for (int j = 0; j < g.n[1]; ++j)
+            for (int i = 0; i < g.n[0]; ++i) {
+                const int c = cid(i, j, k);
+                const long long p = pidx(g.sy, g.sz, i, j, k);
+                double diag = av.empty() ? 0.0 : av[(size_t)p];
+                const int ijk[3] = {i, j, k};
+                for (int d = 0; d < 3; ++d)
+                    for (int side = 0; side < 2; ++side) {
+                        const double coef = g.w[d] * bf[d][(size_t)(side ? p + sd[d] : p)];
+                        diag += coef;
+                        int nb[3] = {ijk[0], ijk[1], ijk[2]};
+                        nb[d] += side ? 1 : -1;
+                        if (nb[d] < 0 || nb[d] >= g.n[d]) {
+                            if (!g.per[d]) continue;  // ghost value 0 (Dirichlet) or no flux
+                            nb[d] = (nb[d] + g.n[d]) % g.n[d];
+                        }
+                        A[(size_t)c * N + cid(nb[0], nb[1], nb[2])] -= coef;
+                    }
+                A[(size_t)c * N + c] += diag;
+            }
+    std::vector<unsigned char> act((size_t)N);
+    int na = 0;
+    double tr = 0.0;
+    for (int c = 0; c < N; ++c) {
+        act[(size_t)c] = A[(size_t)c * N + c] != 0.0;
+        na += act[(size_t)c];
+        tr += A[(size_t)c * N + c];
+    }
+    if (singular && na > 0) {
+        const double cr = tr / ((double)na * na);
+        for (int u = 0; u < N; ++u)
+            for (int v = 0; v < N; ++v)
+                if (act[(size_t)u] && act[(size_t)v]) A[(size_t)u * N + v] += cr;
+    }
+    for (int c = 0; c < N; ++c)
+        if (!act[(size_t)c]) A[(size_t)c * N + c] = 1.0;
+    // Gauss-Jordan inverse with partial pivoting
+    std::vector<double> M((size_t)N * N, 0.0);
+    for (int u = 0; u < N; ++u) M[(size_t)u * N + u] = 1.0;
+    for (int col = 0; col < N; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < N; ++r)
+            if (fabs(A[(size_t)r * N + col]) > fabs(A[(size_t)piv * N + col])) piv = r;
+        if (A[(size_t)piv * N + col] == 0.0) {  // not invertible: keep the CG bottom
+            if (was && gexec) {
+                cudaGraphExecDestroy(gexec);
+                gexec = nullptr;
+            }
+            return GBP_OK;
+        }
+        if (piv != col)
+            for (int q = 0; q < N; ++q) {
+                std::swap(A[(size_t)piv * N + q], A[(size_t)col * N + q]);
+                std::swap(M[(size_t)piv * N + q], M[(size_t)col * N + q]);
+            }
+        const double inv = 1.0 / A[(size_t)col * N + col];
+        for (int q = 0; q < N; ++q) {
+            A[(size_t)col * N + q] *= inv;
+            M[(size_t)col * N + q] *= inv;
+        }
+        for (int r = 0; r < N; ++r) {
+            if (r == col) continue;
+            const double f = A[(size_t)r * N + col];
+            if (f == 0.0) continue;
+            for (int q = 0; q < N; ++q) {
+                A[(size_t)r * N + q] -= f * A[(size_t)col * N + q];
+                M[(size_t)r * N + q] -= f * M[(size_t)col * N + q];
+            }
+        }
+    }
+    for (int u = 0; u < N; ++u)
+        if (!act[(size_t)u])
+            for (int q = 0; q < N; ++q) M[(size_t)u * N + q] = M[(size_t)q * N + u] = 0.0;
+    std::vector<double> Mt((size_t)N * N);
+    for (int u = 0; u < N; ++u)
+        for (int v = 0; v < N; ++v) Mt[(size_t)v * N + u] = M[(size_t)u * N + v];
+    GBP_CUDA(cudaMemcpyAsync(dmat, Mt.data(), sizeof(double) * Mt.size(), cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaMemcpyAsync(dact, act.data(), (size_t)N, cudaMemcpyHostToDevice, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    dense_bottom = true;
+    if (!was && gexec) {  // a captured step holds the other bottom kernel
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    return GBP_OK;
 }
 
 void MacSolver::add_vcycle_correction(const double* r, double* e, double sc)
@@ -587,7 +717,7 @@ int MacSolver::set_robin(const gbp_array4* a, const gbp_array4* b, const gbp_arr
         if (gexec) cudaGraphExecDestroy(gexec);
         gexec = nullptr;
     }
-    return GBP_OK;
+    return beta_ready ? build_dense_bottom() : GBP_OK;
 }
 
 template <typename T>
@@ -623,8 +753,11 @@ void MacSolver::vcycle(int l, const T* b, bool zero)
     const cudaStream_t s = cap_or_st;
     T* x = B::x(lv);
     if (l == (int)L.size() - 1) {
-        mac_bottom<T>(lv.g, lv.b64[0], lv.b64[1], lv.b64[2], b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol,
-                      opt.bottom_atol, singular ? 1 : 0, s);
+        if (dense_bottom)
+            mac_bottom_dense<T>(lv.g, dmat, dact, b, x, singular ? 1 : 0, s);
+        else
+            mac_bottom<T>(lv.g, lv.b64[0], lv.b64[1], lv.b64[2], b, x, bscr, opt.bottom_maxiter, opt.bottom_rtol,
+                          opt.bottom_atol, singular ? 1 : 0, s);
         return;
     }
     T* const* be = B::b(lv);

@@ -62,6 +62,7 @@ private:
     // r = b - A x on the finest level in FP64 (with the cut-face terms), norm = max |r| / (kap V)
     void resid64(const double* x, const double* b, double* r, unsigned long long* norm, cudaStream_t s);
     void eb_refresh_beta();
+    int build_dense_bottom();
     void record_iteration();
     int run_iteration();
     int solve(bool have_guess, gbp_stats* stats);
@@ -86,6 +87,12 @@ private:
     bool robin_ready = false;
     unsigned* dflags = nullptr;
     DevicePool apool;  // alpha a V per level (ABecLaplacian)
+    // dense inverse of the coarsest operator (at most kMacDenseBottomMax cells), rebuilt with the face
+    // coefficients; the single-CTA CG otherwise
+    DevicePool dpool;
+    double* dmat = nullptr;
+    unsigned char* dact = nullptr;
+    bool dense_bottom = false;
     bool abec = false;
     struct EbState {
         DevicePool pool;
