@@ -116,3 +116,19 @@ def test_solve_then_apply_gives_back_the_rhs():
     full = vel.copy()
     full[:, 1:-1, 1:-1, 1:-1] = u
     np.testing.assert_allclose(T.apply(full, h, bclo, bchi, 1.0, rho, 0.5, eta), rhs, rtol=0, atol=1e-10)
+
+
+def test_diffuse_tensor_bc_table():
+    """incflo::get_diffuse_tensor_bc: walls and mass inflow Dirichlet, pressure sides Neumann, a slip
+    wall Dirichlet for the normal component only, periodic kept; [component][direction] per side."""
+    from incflo_gb300.diffusion import diffuse_tensor_bc
+
+    lo, hi = diffuse_tensor_bc(("mass_inflow", "slip_wall", "periodic"), ("pressure_outflow", "no_slip_wall", "periodic"))
+    for c in range(3):
+        assert lo[c][0] == T.DIRICHLET and hi[c][0] == T.NEUMANN
+        assert lo[c][1] == (T.DIRICHLET if c == 1 else T.NEUMANN) and hi[c][1] == T.DIRICHLET
+        assert lo[c][2] == T.PERIODIC and hi[c][2] == T.PERIODIC
+    import pytest
+
+    with pytest.raises(ValueError):
+        diffuse_tensor_bc(("mixed", "periodic", "periodic"), ("periodic", "periodic", "periodic"))
