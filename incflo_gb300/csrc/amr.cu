@@ -397,14 +397,31 @@ __global__ void k_amr_norm_f(NodalGeom gf, const unsigned char* __restrict__ fcl
 
 // restriction of the composite residual to the whole coarse level: the coarse unknowns' own residual
 // plus the trilinear (full-weighting) transpose of the fine unknowns' residuals
-__global__ void k_amr_restrict(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ ccls,
-                               const unsigned char* __restrict__ fcls, int off0, int off1, int off2,
-                               const double* __restrict__ rc, const double* __restrict__ rf, double* __restrict__ out)
+// coarse nodes away from the fine region: their own residual only
+__global__ void k_amr_restrict_copy(NodalGeom gc, const unsigned char* __restrict__ ccls, const double* __restrict__ rc,
+                                    double* __restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
     if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const long long p = pidx(gc.sy, gc.sz, i, j, k);
+    const unsigned char c = ccls[p];
+    store_node(out, gc, i, j, k, (c == C_DOF || c == C_IFACE) ? rc[p] : 0.0);
+}
+
+// the coarse nodes whose 3 x 3 x 3 fine neighbourhood meets the fine bounding box (origin c0, extent
+// ce): own residual plus the fine contributions
+__global__ void k_amr_restrict(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ ccls,
+                               const unsigned char* __restrict__ fcls, int off0, int off1, int off2,
+                               const double* __restrict__ rc, const double* __restrict__ rf, double* __restrict__ out,
+                               int3 c0, int3 ce)
+{
+    const int ti = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tj = blockIdx.y * blockDim.y + threadIdx.y;
+    const int tk = blockIdx.z * blockDim.z + threadIdx.z;
+    if (ti >= ce.x || tj >= ce.y || tk >= ce.z) return;
+    const int i = c0.x + ti, j = c0.y + tj, k = c0.z + tk;
     const long long p = pidx(gc.sy, gc.sz, i, j, k);
     const unsigned char c = ccls[p];
     double acc = (c == C_DOF || c == C_IFACE) ? rc[p] : 0.0;
@@ -447,24 +464,23 @@ __global__ void k_amr_prolong_f(NodalGeom gc, NodalGeom gf, const unsigned char*
     const long long q = pidx(gf.sy, gf.sz, i, j, k);
     if (fcls[q] != F_DOF) return;
     const int gpos[3] = {i + off0, j + off1, k + off2};
+    // trilinear weights are 2^-(odd directions) for every coarse node used: sum the values, scale once
+    // (FP64 instructions are the bound here)
+    int lo[3], hi[3], nodd = 0;
+    for (int d = 0; d < 3; ++d) {
+        const int odd = gpos[d] & 1;
+        nodd += odd;
+        lo[d] = cwrap(gc, d, (gpos[d] - odd) / 2);
+        hi[d] = odd ? cwrap(gc, d, (gpos[d] - 1) / 2 + 1) : lo[d];
+    }
     double acc = 0.0;
     for (int s = 0; s < 8; ++s) {
-        int I[3];
-        double w = 1.0;
-        bool use = true;
-        for (int d = 0; d < 3; ++d) {
-            const int sel = (s >> d) & 1;
-            if (gpos[d] & 1) {
-                I[d] = cwrap(gc, d, (gpos[d] - 1) / 2 + sel);
-                w *= 0.5;
-            } else {
-                if (sel) use = false;
-                I[d] = cwrap(gc, d, gpos[d] / 2);
-            }
-        }
-        if (use) acc += w * e[pidx(gc.sy, gc.sz, I[0], I[1], I[2])];
+        const int sx = s & 1, sy = (s >> 1) & 1, sz = s >> 2;
+        if ((sx && !(gpos[0] & 1)) || (sy && !(gpos[1] & 1)) || (sz && !(gpos[2] & 1))) continue;
+        acc += e[pidx(gc.sy, gc.sz, sx ? hi[0] : lo[0], sy ? hi[1] : lo[1], sz ? hi[2] : lo[2])];
     }
-    store_node(pf, gf, i, j, k, pf[q] + acc);
+    const double scale = nodd == 0 ? 1.0 : (nodd == 1 ? 0.5 : (nodd == 2 ? 0.25 : 0.125));
+    store_node(pf, gf, i, j, k, fma(scale, acc, pf[q]));
 }
 
 // covered coarse nodes take the fine value at their position (output and coarse gradient)
@@ -1005,7 +1021,27 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
             break;
         }
         // coarse correction on the restricted composite residual
-        k_amr_restrict<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], r_c, r_f, rc_full);
+        k_amr_restrict_copy<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, r_c, rc_full);
+        {
+            int lo[3], ext[3];
+            for (int d = 0; d < 3; ++d) {
+                // fine global node positions 2i-1 .. 2i+1 against the box's off .. off + nfb
+                lo[d] = std::max(0, (off[d] - 1) / 2);
+                const int hi = std::min(gc.nu[d] - 1, (off[d] + nfb[d] + 1) / 2 + 1);
+                if (gf.per[d]) {
+                    lo[d] = 0;
+                    ext[d] = gc.nu[d];
+                } else {
+                    ext[d] = std::max(0, hi - lo[d] + 1);
+                }
+            }
+            if (ext[0] > 0 && ext[1] > 0 && ext[2] > 0) {
+                const dim3 grid((unsigned)((ext[0] + kB3.x - 1) / kB3.x), (unsigned)((ext[1] + kB3.y - 1) / kB3.y),
+                                (unsigned)((ext[2] + kB3.z - 1) / kB3.z));
+                k_amr_restrict<<<grid, kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], r_c, r_f, rc_full,
+                                                     make_int3(lo[0], lo[1], lo[2]), make_int3(ext[0], ext[1], ext[2]));
+            }
+        }
         GBP_CUDA(cudaMemsetAsync(e_c, 0, sizeof(double) * gc.count, st));
         crs.apply_vcycles(rc_full, e_c, m, scale32, st);
         k_amr_prolong_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, e_c, phi_c);
