@@ -280,6 +280,8 @@ int gbp_plan_destroy(gbp_plan* p)
     if (p->ev_out) cudaEventDestroy(p->ev_out);
     for (auto e : p->ev_slab)
         if (e) cudaEventDestroy(e);
+    for (auto e : p->ev_rhs)
+        if (e) cudaEventDestroy(e);
     if (p->dflux) cudaFree(p->dflux);
     if (p->ccbuf) cudaFree(p->ccbuf);
     delete p;
@@ -450,7 +452,7 @@ static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_
                             double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
                             double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats,
                             cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy,
-                            const gbp::HostSlabs* out_slabs = nullptr);
+                            const gbp::HostSlabs* out_slabs = nullptr, const gbp::RhsGroups* rhs_groups = nullptr);
 
 int gbp_apply_nodal_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
                                double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
@@ -467,7 +469,7 @@ static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_
                             double rho0, gbp_array4* gp, gbp_array4* p_nd, double time, double dt, double prev_dt,
                             double scaling_factor, int incremental, int set_inflow_bc, gbp_stats* stats,
                             cudaEvent_t wait_before_rhs, const gbp::HostCopy* phi_copy,
-                            const gbp::HostSlabs* out_slabs)
+                            const gbp::HostSlabs* out_slabs, const gbp::RhsGroups* rhs_groups)
 {
     if (!p || !p->nodal) {
         set_error("gbp_apply_nodal_projection: not a nodal plan");
@@ -504,7 +506,7 @@ static int apply_nodal_impl(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_
     ca.incremental = incremental;
     if (stats) memset(stats, 0, sizeof(*stats));
     if (wait_before_rhs) GBP_CUDA(cudaStreamWaitEvent(p->stream, wait_before_rhs, 0));
-    return p->nodal->project(ra, ca, p_nd, incremental, nullptr, stats, phi_copy, out_slabs);
+    return p->nodal->project(ra, ca, p_nd, incremental, nullptr, stats, phi_copy, out_slabs, rhs_groups);
 }
 
 int gbp_mac_set_beta(gbp_plan* p, const gbp_array4* bx, const gbp_array4* by, const gbp_array4* bz,
@@ -1081,8 +1083,36 @@ int gbp_apply_nodal_projection_host(gbp_plan* p, double* vel, const double* rho,
     // density first on the plan's stream (sigma and its edge weights are computed from it while the
     // velocities and gp upload on the copy stream)
     if (rho) GBP_CUDA(cudaMemcpyAsync(drho, rho, nc * sizeof(double), cudaMemcpyHostToDevice, s));
-    GBP_CUDA(cudaMemcpyAsync(dvel, vel, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, c));
-    GBP_CUDA(cudaMemcpyAsync(dgp, gp, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, c));
+    // velocity and gp by z-slabs matched to the right-hand side's z chunks: each group of chunks starts
+    // as soon as the cells it reads have arrived (not with a p_nd to upload: the incremental form)
+    const bool grouped = !(p_nd && incremental) && !p->nodal->has_eb();
+    gbp::RhsGroups rg{};
+    if (grouped) {
+        if (!p->ev_rhs[0])
+            for (auto& e : p->ev_rhs) GBP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        int kc = 1;
+        const int nzc = gbp::nodal_rhs_zchunks(p->nodal->geom0(), &kc);
+        rg.n = std::min(gbp::kRhsGroups, nzc);
+        const size_t plane = (size_t)nx * ny;
+        int cs = 0;
+        for (int q = 0; q < rg.n; ++q) {
+            rg.zb[q] = (int)((long long)nzc * q / rg.n);
+            rg.zb[q + 1] = (int)((long long)nzc * (q + 1) / rg.n);
+            const int ce = q == rg.n - 1 ? nz : std::min(nz, rg.zb[q + 1] * kc);
+            if (ce > cs)
+                for (int comp = 0; comp < 3; ++comp) {
+                    const size_t off = comp * nc + (size_t)cs * plane, cnt = (size_t)(ce - cs) * plane;
+                    GBP_CUDA(cudaMemcpyAsync(dvel + off, vel + off, cnt * sizeof(double), cudaMemcpyHostToDevice, c));
+                    GBP_CUDA(cudaMemcpyAsync(dgp + off, gp + off, cnt * sizeof(double), cudaMemcpyHostToDevice, c));
+                }
+            cs = std::max(cs, ce);
+            rg.ev[q] = p->ev_rhs[q];
+            GBP_CUDA(cudaEventRecord(rg.ev[q], c));
+        }
+    } else {
+        GBP_CUDA(cudaMemcpyAsync(dvel, vel, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, c));
+        GBP_CUDA(cudaMemcpyAsync(dgp, gp, 3 * nc * sizeof(double), cudaMemcpyHostToDevice, c));
+    }
     if (p_nd && incremental) GBP_CUDA(cudaMemcpyAsync(dp, p_nd, nn * sizeof(double), cudaMemcpyHostToDevice, c));
     GBP_CUDA(cudaEventRecord(p->ev_in, c));
     auto cells = [&](double* d, int nc_) {
@@ -1115,7 +1145,8 @@ int gbp_apply_nodal_projection_host(gbp_plan* p, double* vel, const double* rho,
     const int nslabs = std::min(kHostSlabs, std::max(1, nz / 16));
     gbp::HostSlabs os{vel, gp, dvel, dgp, (size_t)nx * ny, nc, nslabs, c, p->ev_slab};
     int rc = apply_nodal_impl(p, &av, nullptr, rho ? &ar : nullptr, rho0, &ag, p_nd ? &ap : nullptr, 0.0, 1.0, 1.0,
-                              scaling_factor, incremental, 0, stats, p->ev_in, p_nd ? &pc : nullptr, &os);
+                              scaling_factor, incremental, 0, stats, grouped ? nullptr : p->ev_in,
+                              p_nd ? &pc : nullptr, &os, grouped ? &rg : nullptr);
     if (rc != GBP_OK && rc != GBP_NOT_CONVERGED) {
         cudaStreamSynchronize(c);
         return rc;

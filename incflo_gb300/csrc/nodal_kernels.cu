@@ -625,12 +625,14 @@ static int zchunk(int bx, int by, int nz)
 // difference of x-pair sums of F_y and the 4-cell sum of F_z, then layers k-1 and k.
 // part: per-CTA sums of g (consistency correction of singular systems).
 __global__ void __launch_bounds__(ZTX* ZTY) k_nodal_rhs(NodalGeom g, RhsArgs a, const double* __restrict__ s64,
-                                                        double* __restrict__ b, double* __restrict__ part, int kchunk)
+                                                        double* __restrict__ b, double* __restrict__ part, int kchunk,
+                                                        int zb0, int nzb)
 {
     __shared__ double F[2][3][ZTY][ZTX];
     const int tx = threadIdx.x % ZTX, ty = threadIdx.x / ZTX;
     const int ci = blockIdx.x * ZX - 1 + tx, cj = blockIdx.y * ZY - 1 + ty;
-    const int kbeg = blockIdx.z * kchunk;
+    const int zb = zb0 + blockIdx.z;  // z chunk (a launch may cover a subset of them)
+    const int kbeg = zb * kchunk;
     const int kend = min(kbeg + kchunk, g.nu[2]);
     const bool owner = tx >= 1 && ty >= 1 && ci < g.nu[0] && cj < g.nu[1];
     // cells beyond the last node column are never read by an owner
@@ -728,8 +730,9 @@ __global__ void __launch_bounds__(ZTX* ZTY) k_nodal_rhs(NodalGeom g, RhsArgs a, 
     }
     if (part) {
         const double t = block_sum_all(acc);
-        if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = t;
+        if (threadIdx.x == 0) part[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * zb)] = t;
     }
+    (void)nzb;
 }
 
 // strong-form max norm max_i |v_i| / V_i over the unique non-Dirichlet nodes
@@ -1054,11 +1057,22 @@ static dim3 rhs_grid(const NodalGeom& g, int& kchunk)
     return dim3(bx, by, (g.nu[2] + kchunk - 1) / kchunk);
 }
 
-void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, double* part, cudaStream_t st)
+void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, double* part, cudaStream_t st,
+               int zb0, int zb1)
 {
     int kchunk;
     const dim3 grid = rhs_grid(g, kchunk);
-    k_nodal_rhs<<<grid, ZTX * ZTY, 0, st>>>(g, a, s64, b, part, kchunk);
+    if (zb1 < 0) zb1 = (int)grid.z;
+    if (zb1 <= zb0) return;
+    k_nodal_rhs<<<dim3(grid.x, grid.y, zb1 - zb0), ZTX * ZTY, 0, st>>>(g, a, s64, b, part, kchunk, zb0, (int)grid.z);
+}
+
+int nodal_rhs_zchunks(const NodalGeom& g, int* kchunk)
+{
+    int kc;
+    const dim3 grid = rhs_grid(g, kc);
+    if (kchunk) *kchunk = kc;
+    return (int)grid.z;
 }
 
 int nodal_rhs_partials(const NodalGeom& g)

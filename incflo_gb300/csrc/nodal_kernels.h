@@ -57,7 +57,11 @@ void nodal_sigma_copy(const NodalGeom& g, const gbp_array4* sig, double cval, do
 void nodal_sigma_coarsen(const NodalGeom& gf, const NodalGeom& gc, const double* sf, double* sc64, float* sc32,
                          cudaStream_t st);
 // part: per-block sums of the right-hand side (nodal_rhs_partials(g) of them), or nullptr
-void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, double* part, cudaStream_t st);
+// z chunks zb0 .. zb1-1 of the launch grid (zb1 < 0: all); the partial sums keep their full-grid slots
+void nodal_rhs(const NodalGeom& g, const RhsArgs& a, const double* s64, double* b, double* part, cudaStream_t st,
+               int zb0 = 0, int zb1 = -1);
+// number of z chunks of the right-hand-side launch and the node planes per chunk
+int nodal_rhs_zchunks(const NodalGeom& g, int* kchunk);
 int nodal_rhs_partials(const NodalGeom& g);
 // mode 0: make b consistent (remove V-weighted mean; max norm of the result into *norm);
 // mode 1: gauge x to zero V-weighted mean. have_partials: `partials` already holds nparts sums of v.

@@ -1226,7 +1226,7 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
 
 int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
                          const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy,
-                         const HostSlabs* out_slabs)
+                         const HostSlabs* out_slabs, const RhsGroups* rhs_groups)
 {
     if (!sigma_ready) {
         set_error("nodal project: sigma was never set on this plan");
@@ -1237,8 +1237,19 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
     GBP_CUDA(cudaMemsetAsync(dnorm, 0, sizeof(unsigned long long), st));
     RhsArgs ra = rhs;
     if (eb.on) ra.cmask = eb.e.reg;  // cut and covered cells: the cut-cell table below
-    nodal_rhs(l0.g, ra, l0.s64, rhs0, singular ? partials : nullptr, st);
-    ++nk;
+    if (rhs_groups && rhs_groups->n > 0 && !eb.on) {
+        // each group of z chunks as soon as the cells it reads are on the device
+        const RhsGroups& G = *rhs_groups;
+        for (int q = 0; q < G.n; ++q) {
+            GBP_CUDA(cudaStreamWaitEvent(st, G.ev[q], 0));
+            if (q == 0 && l0.g.per[2]) GBP_CUDA(cudaStreamWaitEvent(st, G.ev[G.n - 1], 0));
+            nodal_rhs(l0.g, ra, l0.s64, rhs0, singular ? partials : nullptr, st, G.zb[q], G.zb[q + 1]);
+            ++nk;
+        }
+    } else {
+        nodal_rhs(l0.g, ra, l0.s64, rhs0, singular ? partials : nullptr, st);
+        ++nk;
+    }
     if (eb.on) eb_rhs(l0.g, eb.e, ra, rhs0, st);
     if (singular) {
         // consistent right-hand side, and its max norm (the relative-tolerance reference; with cut

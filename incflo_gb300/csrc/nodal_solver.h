@@ -41,6 +41,15 @@ struct HostSlabs {
     cudaEvent_t* ev;  // nslabs events
 };
 
+// The right-hand side launched by groups of its z chunks, group q after event ev[q] (its cells uploaded);
+// with a periodic z direction group 0 also waits for the last event (node plane 0 reads the top cells).
+constexpr int kRhsGroups = 8;
+struct RhsGroups {
+    int n;
+    int zb[kRhsGroups + 1];
+    cudaEvent_t ev[kRhsGroups];
+};
+
 struct DevicePool {
     char* base = nullptr;
     size_t bytes = 0;
@@ -87,12 +96,13 @@ public:
     // overlapping the velocity correction
     int project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* phi_out, int phi_accumulate,
                 const gbp_array4* phi_guess, gbp_stats* stats, const HostCopy* phi_copy = nullptr,
-                const HostSlabs* out_slabs = nullptr);
+                const HostSlabs* out_slabs = nullptr, const RhsGroups* rhs_groups = nullptr);
 
     // nodal divergence of vel as the projection sees it (consistent for singular systems), strong form
     int divergence(const RhsArgs& rhs, const gbp_array4* out, double* max_norm);
 
     const NodalGeom& geom0() const { return L[0].g; }
+    bool has_eb() const { return eb.on; }
     size_t device_bytes() const { return pool.bytes; }
     cudaStream_t stream() const { return st; }
     // solve A phi = g on the level-0 arrays already in place (used by project and tests)

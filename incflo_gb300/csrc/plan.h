@@ -23,6 +23,7 @@ struct gbp_plan {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_in = nullptr, ev_phi = nullptr, ev_out = nullptr;
     cudaEvent_t ev_slab[kHostSlabs] = {};  // one per z-slab of the copy-out
+    cudaEvent_t ev_rhs[gbp::kRhsGroups] = {};  // one per z-slab of the upload
     double* dflux = nullptr;  // 2 device doubles: inflow / outflow of the solvability fix
     double* ccbuf = nullptr;  // cell-centred projection scratch (unprojected face velocities, phi)
 };
