@@ -19,6 +19,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -74,7 +75,9 @@ class ClockSampler:
     def __init__(self, device_index=0):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # the raw samples (a few KB) go to BENCH_CLOCKS_DIR when set, else the system temp directory
+        out_dir = os.environ.get("BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, f"clocks_bench_{os.getpid()}.csv")
 
     def start(self):
         try:

@@ -3,7 +3,7 @@
 Parity bar: phi relative L2 <= 1e-9 (gauge: zero volume-weighted mean on singular systems),
 projected velocity and grad(phi) within 1e-9 of the oracle's scale, final relative residual
 <= the requested tolerance. Both the plain FP64 form and the mixed form (FP32 V-cycles inside
-FP64 iterative refinement) must meet it: the FP64 outer residual is the judge.
+FP64 iterative refinement) must meet it: the FP64 outer residual decides convergence.
 """
 import numpy as np
 import pytest
