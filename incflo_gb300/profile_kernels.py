@@ -19,8 +19,9 @@ ncu launch list covers exactly one form.
 
   python -m incflo_gb300.profile_kernels --row eb_nodal --reps 1
 
-runs the workload of one bench.py row (amr | eb_mac | eb_nodal | tensor: the two-level composite
-projection, the cut-cell MAC and nodal projections of the cylinder channel, the tensor diffusion solve)
+runs the workload of one bench.py row (amr | mac | eb_mac | eb_nodal | tensor: the two-level composite
+projection, the MAC projection of the headline grid, the cut-cell MAC and nodal projections of the
+cylinder channel, the tensor diffusion solve)
 with `reps` timed solves after one warm-up, so that an ncu launch list covers that row alone.
 
 The U-Net mode runs the tensor-core convolutions on a 128 x 128 x 136 network grid (the multigrid
@@ -53,7 +54,7 @@ def main():
     ap.add_argument("--unet", type=int, default=0, help="time the U-Net forward on an n x n x (n+8) grid")
     ap.add_argument("--project", default="", choices=["", "mixed", "fp64"])
     ap.add_argument("--opt", action="append", default=[], help="option override key=value (projection mode)")
-    ap.add_argument("--row", default="", choices=["", "amr", "eb_mac", "eb_nodal", "tensor"])
+    ap.add_argument("--row", default="", choices=["", "amr", "mac", "eb_mac", "eb_nodal", "tensor"])
     ap.add_argument("--rtol", type=float, default=1e-10)
     args = ap.parse_args()
     from incflo_gb300.build import build
