@@ -804,14 +804,14 @@ void MacSolver::resid64(const double* x, const double* b, double* r, unsigned lo
     mac_norm(l0.g, r, norm, s, eb.m.kap);
 }
 
-void MacSolver::record_iteration()
+void MacSolver::record_iteration(int m)
 {
     const MacLevel& l0 = L[0];
     const cudaStream_t s = cap_or_st;
     if (opt.precision == GBP_PREC_MIXED) {
         mac_to_f32(l0.g, res, l0.rhs32, scale32, s);
         vcycle<float>(0, l0.rhs32, true);
-        for (int c = 1; c < opt.ir_inner_cycles; ++c) vcycle<float>(0, l0.rhs32, false);
+        for (int c = 1; c < m; ++c) vcycle<float>(0, l0.rhs32, false);
         mac_add_correction<float>(l0.g, phi, l0.x32, 1.0 / scale32, s);
     } else {
         vcycle<double>(0, res, true);
@@ -822,11 +822,12 @@ void MacSolver::record_iteration()
     cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
 }
 
-int MacSolver::run_iteration()
+int MacSolver::run_iteration(int m)
 {
-    if (!opt.use_graphs) {
+    // the captured step holds ir_inner_cycles V-cycles; a shortened last step is launched directly
+    if (!opt.use_graphs || m != opt.ir_inner_cycles) {
         cap_or_st = st;
-        record_iteration();
+        record_iteration(m);
         GBP_CUDA(cudaGetLastError());
         return GBP_OK;
     }
@@ -836,7 +837,7 @@ int MacSolver::run_iteration()
         cudaGraph_t graph = nullptr;
         cap_or_st = cap;
         GBP_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-        record_iteration();
+        record_iteration(opt.ir_inner_cycles);
         cudaError_t e = cudaStreamEndCapture(cap, &graph);
         cap_or_st = st;
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(mac refinement step)");
@@ -885,19 +886,31 @@ int MacSolver::solve(bool have_guess, gbp_stats* stats)
         frexp(bnorm * l0.g.vol, &ex);
         scale32 = ldexp(1.0, -ex);
     }
-    int it = 0, status = GBP_OK;
+    int it = 0, status = GBP_OK, vcycles = 0;
     const double r0 = rn;
+    const bool mixed = opt.precision == GBP_PREC_MIXED;
+    int m = mixed ? opt.ir_inner_cycles : 1;
     while (rn > target) {
         if (it >= opt.maxiter) {
             status = GBP_NOT_CONVERGED;
             set_error("solve: maxiter reached before the tolerance");
             break;
         }
-        int rc = run_iteration();
+        int rc = run_iteration(m);
         if (rc) return rc;
         GBP_CUDA(cudaStreamSynchronize(st));
+        const double rprev = rn;
         rn = bits_to_double(hnorm[1]);
         ++it;
+        vcycles += m;
+        if (mixed && rn > target && rn < rprev && rn > 0.0) {
+            // next inner solve: the V-cycles the observed per-cycle contraction says the remaining
+            // reduction needs (+1/4 cycle of margin), capped by ir_inner_cycles and by what an FP32
+            // inner solve delivers (about 1e-6 of its right-hand side)
+            const double rho = std::min(0.9, std::max(1e-3, pow(rn / rprev, 1.0 / m)));
+            const double need = log(std::max(target / rn, 1e-6)) / log(rho);
+            m = std::max(1, std::min(opt.ir_inner_cycles, (int)ceil(need + 0.25)));
+        }
         if (opt.verbose > 1) fprintf(stderr, "gbp mac: iter %d rel resid %.3e\n", it, bnorm > 0 ? rn / bnorm : rn);
         if (!isfinite(rn)) {
             status = GBP_NAN;
@@ -914,7 +927,7 @@ int MacSolver::solve(bool have_guess, gbp_stats* stats)
     if (stats) {
         stats->status = status;
         stats->outer_iters = it + 1;
-        stats->vcycles = it * (opt.precision == GBP_PREC_MIXED ? opt.ir_inner_cycles : 1);
+        stats->vcycles = vcycles;
         stats->num_levels = (int)L.size();
         stats->rhs_norm = bnorm;
         stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;

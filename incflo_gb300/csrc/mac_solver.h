@@ -63,8 +63,8 @@ private:
     void resid64(const double* x, const double* b, double* r, unsigned long long* norm, cudaStream_t s);
     void eb_refresh_beta();
     int build_dense_bottom();
-    void record_iteration();
-    int run_iteration();
+    void record_iteration(int m);  // m V-cycles per refinement step
+    int run_iteration(int m);
     int solve(bool have_guess, gbp_stats* stats);
 
     gbp_options opt{};
