@@ -136,38 +136,36 @@ def ncu_traffic(summary_name):
     return None
 
 
-def cpu_sample(n_sample, rtol, n_full):
-    """The oracle's FP64 multigrid (C, OpenMP, all host threads) on one projection of the same
-    workload at n_sample^3, scaled by the unknown count to n_full^3."""
-    import numpy as np
-
+def cpu_projection(n, rtol):
+    """The oracle's FP64 PCG-multigrid (C, OpenMP, all host threads) on one full projection of the
+    benchmark workload at n^3: returns (ms, threads, stats, phi, projected velocity)."""
     import oracle as O
     from incflo_gb300 import synth
 
-    w = synth.variable_density_rt(n_sample)
+    w = synth.variable_density_rt(n)
     g = O.Grid(w["n"], lo=w["lo"], hi=w["hi"], bclo=w["bclo"], bchi=w["bchi"])
     vel = synth.with_ghosts(w["vel"], 1)
     sigma = 1.0 / w["rho"]
     t0 = time.perf_counter()
-    _, _, _, st = O.nodal_project(g, sigma, vel, rtol=rtol, atol=0.0)
+    vel_new, phi, _, st = O.nodal_project(g, sigma, vel, rtol=rtol, atol=0.0)
     dt = time.perf_counter() - t0
-    scale = (n_full / n_sample) ** 3
-    return dt * 1e3 * scale, O.num_threads(), st, dt
+    return dt * 1e3, O.num_threads(), st, phi, vel_new
 
 
 def run_reference(args, ws, rank):
+    """The CPU reference arm: one full n^3 projection of the workload per timed step (warm-up steps at
+    32^3, untimed: they only page the code and the OpenMP pool in)."""
     if rank != 0:
         return
-    n_sample = max(16, args.n // 2)
     vals = []
     st = None
     for i in range(args.warmup + args.steps):
-        ms, cores, st, _ = cpu_sample(n_sample, args.rtol, args.n)
+        ms, cores, st, _, _ = cpu_projection(args.n if i >= args.warmup else min(32, args.n), args.rtol)
         if i >= args.warmup:
             vals.append(ms)
     v = sum(vals) / len(vals)
-    sample = (f"one projection of the same workload at {n_sample}^3 per step (CPU oracle FP64 PCG-multigrid, "
-              f"{cores} OpenMP threads), time x{(args.n // n_sample) ** 3} for {args.n}^3")
+    sample = (f"one full {args.n}^3 projection of the same workload per step (CPU oracle FP64 PCG-multigrid, "
+              f"{cores} OpenMP threads)")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "ms/projection", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 3), "higher_is_better": False,
@@ -182,6 +180,56 @@ def run_reference(args, ws, rank):
         "oracle_iters": st["iters"] if st else None,
     }
     print(json.dumps(line), flush=True)
+
+
+def rel_l2(a, b):
+    import numpy as np
+
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def parity_cfg1(dev):
+    """cfg1 (64^3 Taylor-Green + noise, triply periodic, rho = 1): nodal and MAC projections in both
+    forms at incflo's tolerances (rtol 1e-11, atol 1e-14), phi error against the oracle (1e-13)."""
+    import numpy as np
+    import torch
+
+    import oracle as O
+    from incflo_gb300 import Geometry, MacProjector, NodalProjector, make_options, synth
+
+    c = synth.taylor_green_noise(64)
+    g = O.Grid(c["n"], c["lo"], c["hi"], c["bclo"], c["bchi"])
+    vel = synth.with_ghosts(c["vel"])
+    sigma = np.ones(g.cell_shape)
+    _, phi_or, _, _ = O.nodal_project(g, sigma, vel, rtol=1e-13)
+    n = c["n"]
+    umac = []
+    for d in range(3):
+        u, ax = c["vel"][d], 2 - d
+        m = u.shape[ax]
+        umac.append(np.ascontiguousarray(0.5 * (np.take(u, np.arange(-1, m), axis=ax, mode="wrap") +
+                                                np.take(u, np.arange(0, m + 1), axis=ax, mode="wrap"))))
+    beta = [np.ones(x.shape) for x in umac]
+    _, mphi_or, _ = O.mac_project(g, beta, umac, rtol=1e-13)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        vt = torch.from_numpy(vel).to(dev)
+        proj = NodalProjector(vt, torch.from_numpy(sigma).to(dev), Geometry(n, c["lo"], c["hi"]),
+                              options=make_options(0, precision=prec))
+        proj.setDomainBC(c["bclo"], c["bchi"])
+        st = proj.project(rtol=1e-11, atol=1e-14)
+        nz, ny, nx = g.node_shape
+        out[f"nodal_{prec}"] = rel_l2(proj.getPhi().cpu().numpy()[:nz, :ny, :nx], phi_or)
+        mp = MacProjector(Geometry(n, c["lo"], c["hi"]), options=make_options(1, precision=prec))
+        mp.initProjector(beta=1.0)
+        mp.setDomainBC(c["bclo"], c["bchi"])
+        mp.setUMAC([torch.from_numpy(u).to(dev) for u in umac])
+        ph = torch.zeros(g.cell_shape, dtype=torch.float64, device=dev)
+        st2 = mp.project(rtol=1e-11, atol=1e-14, phi=ph, phi_guess=False)
+        if st["status"] or st2["status"]:
+            raise RuntimeError(f"cfg1 projection failed: {st} {st2}")
+        out[f"mac_{prec}"] = rel_l2(ph.cpu().numpy(), mphi_or)
+    return {k: float(f"{v:.3e}") for k, v in out.items()}
 
 
 def run_amr(args, dev, steps=3, warmup=1):
@@ -284,10 +332,22 @@ def run_mac(args, dev, steps=5, warmup=3):
             raise RuntimeError(f"MAC projection failed: {st}")
         if i >= warmup:
             times.append(st["ms_total"])
+    parity = None
+    if not args.no_parity:
+        import oracle as O
+
+        for a, b in zip(ut, u0):
+            a.copy_(b)
+        ph = torch.zeros((n[2], n[1], n[0]), dtype=torch.float64, device=dev)
+        mp.project(rtol=args.rtol, atol=0.0, phi=ph, phi_guess=False)
+        g = O.Grid(n, w["lo"], w["hi"], (P, P, N), (P, P, N))
+        _, phi_or, st_or = O.mac_project(g, beta, u, rtol=1e-12)
+        parity = {"phi_rel_l2_chosen": float(f"{rel_l2(ph.cpu().numpy(), phi_or):.3e}"),
+                  "oracle": f"CPU FP64 PCG-multigrid to rtol 1e-12 ({st_or['iters']} iterations)"}
     return {"workload": f"MAC projection {args.n}^3, variable density (rho 1->3 tanh interface, beta = 1/rho_face), "
                         f"periodic x/y, walls z, FP32 V-cycles inside FP64 refinement, rtol {args.rtol:g}",
             "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
-            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"]}
+            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"], "parity": parity}
 
 
 def run_eb_mac(args, dev, steps=5, warmup=3):
@@ -330,10 +390,23 @@ def run_eb_mac(args, dev, steps=5, warmup=3):
         if i >= warmup:
             times.append(st["ms_total"])
     cut = int(((geo["vfrac"] > 0) & (geo["vfrac"] < 1)).sum())
+    parity = None
+    if not args.no_parity:
+        # too large for the direct cut-cell oracle: the oracle's own divergence of the projected faces
+        from oracle.eb_mac import EBMac
+
+        ap = [geo["apx"], geo["apy"], geo["apz"]]
+        fc = [geo["fcx"], geo["fcy"], geo["fcz"]]
+        m = EBMac(n, [ext[d] / n[d] for d in range(3)], (I, N, P), (D, N, P), geo["vfrac"], ap, fc,
+                  [np.ones(a.shape) for a in ap])
+        d0, d1 = m.divergence(u), m.divergence([x.cpu().numpy() for x in ut])
+        parity = {"oracle_divergence_ratio": float(f"{d1 / d0:.3e}"),
+                  "check": "max |cut-cell divergence| / (kappa V) of the projected face velocities in the oracle's "
+                           "operator, relative to the input's (the direct oracle solve does not fit this size)"}
     return {"workload": f"cut-cell MAC projection, cylinder channel 256x64x64 ({cut} cut cells), inflow / outflow "
                         f"/ walls / periodic, FP32 V-cycles inside FP64 refinement, rtol {args.rtol:g}",
             "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
-            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"]}
+            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"], "parity": parity}
 
 
 def run_eb_nodal(args, dev, steps=5, warmup=3):
@@ -372,11 +445,23 @@ def run_eb_nodal(args, dev, steps=5, warmup=3):
         if i >= warmup:
             times.append(st["ms_total"])
     kap = M[0]
+    parity = None
+    if not args.no_parity:
+        # the GPU phi's residual in the oracle's cut-cell operator (the direct solve does not fit this size)
+        from oracle.eb_nodal import EBNodal
+
+        Mfull = eb.cylinder_moments(n, (0, 0, 0), ext, (1.0, 0.5, 0.0), 0.125, small_volfrac=1e-4)
+        o = EBNodal(n, [ext[d] / n[d] for d in range(3)], (I, N, P), (D, N, P), Mfull)
+        r = o.residual_norm(np.ones((n[2], n[1], n[0])), np.ascontiguousarray(vel[:, 1:-1, 1:-1, 1:-1]),
+                            pnd.cpu().numpy(), vel)
+        parity = {"oracle_rel_resid": float(f"{r:.3e}"),
+                  "check": "max |b - A phi| / (fluid dual volume) of the GPU phi in the oracle's cut-cell operator, "
+                           "relative to |b| (the direct oracle solve does not fit this size)"}
     return {"workload": f"cut-cell nodal projection, cylinder channel 256x64x64 ({int(((kap > 0) & (kap < 1)).sum())} "
                         f"cut cells), inflow / outflow / walls / periodic, FP32 V-cycles inside FP64 refinement, "
                         f"rtol {args.rtol:g}",
             "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
-            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"]}
+            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"], "parity": parity}
 
 
 def run_tensor(args, dev, steps=3, warmup=3):
@@ -430,6 +515,8 @@ def run_ours(args, ws, rank, local):
     build()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if rank != 0:
+        args.no_parity = True  # the oracle checks run once, on rank 0
     n = args.n
     w = synth.variable_density_rt(n)
     geom = Geometry(w["n"], w["lo"], w["hi"])
@@ -484,6 +571,9 @@ def run_ours(args, ws, rank, local):
     sampler.start()
     ms_mixed, st_mixed, wall_mixed = run_form("mixed", args.steps, args.warmup, surrogate)
     clocks = sampler.stop()
+    # the last timed step's outputs, for the error against the oracle (checked after all timing)
+    phi_mixed_out = p_nd.cpu().numpy()
+    vel_mixed_out = vel.cpu().numpy()
     warm = None
     if surrogate is not None:
         codes = [s_["warm_start"] for s_ in st_mixed]
@@ -496,6 +586,7 @@ def run_ours(args, ws, rank, local):
                 "mixed_without_warm_start_ms": round(sum(ms_plain_mixed) / len(ms_plain_mixed), 4),
                 "mixed_without_warm_start_vcycles": st_plain_mixed[0]["vcycles"]}
     ms_fp64, st_fp64, wall_fp64 = run_form("fp64", max(1, min(args.steps, args.fp64_steps)), 1)
+    phi_fp64_out = p_nd.cpu().numpy()
 
     tot_mixed = allreduce_max(ws, sum(ms_mixed))
     per_step = tot_mixed / len(ms_mixed)
@@ -560,12 +651,33 @@ def run_ours(args, ws, rank, local):
     mac = None if args.no_mac else run_mac(args, dev)
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
-        ns = max(16, n // 2)
-        ms_cpu, cores, st_cpu, dt_cpu = cpu_sample(ns, args.rtol, n)
+        ms_cpu, cores, st_cpu, _, _ = cpu_projection(n, args.rtol)
         cpu = {"value": round(ms_cpu, 1), "unit": "ms/projection", "cores": cores, "kind": "port",
-               "sample": f"one projection at {ns}^3 ({dt_cpu:.1f} s, CPU oracle FP64 PCG-multigrid), "
-                         f"time x{(n // ns) ** 3} for {n}^3"}
+               "sample": f"one full {n}^3 projection of the same workload (CPU oracle FP64 PCG-multigrid, "
+                         f"{st_cpu['iters']} iterations to rtol {args.rtol:g})"}
+    if rank == 0 and not args.no_parity:
+        # error of each form against the FP64 oracle solved to 1e-12 (outside every timed region)
+        import oracle as O
+
+        _, _, st_ref, phi_ref, vel_ref = cpu_projection(n, 1e-12)
+        gref = O.Grid(w["n"], lo=w["lo"], hi=w["hi"], bclo=bclo, bchi=bchi)
+        nz, ny, nx = gref.node_shape
+        div_ref = float(np.abs(O.nodal_rhs(gref, vel_ref)).max())
+        parity = {"oracle": f"CPU FP64 PCG-multigrid to rtol 1e-12 ({st_ref['iters']} iterations)",
+                  "cfg2_nodal_256": {
+                      "phi_rel_l2_chosen": float(f"{rel_l2(phi_mixed_out[:nz, :ny, :nx], phi_ref):.3e}"),
+                      "phi_rel_l2_plain_fp64": float(f"{rel_l2(phi_fp64_out[:nz, :ny, :nx], phi_ref):.3e}"),
+                      "max_div_after_chosen": float(f"{np.abs(O.nodal_rhs(gref, vel_mixed_out)).max():.6e}"),
+                      "max_div_after_oracle": float(f"{div_ref:.6e}")}}
+        del phi_ref, vel_ref
+        if mac is not None:
+            parity["cfg2_mac_256"] = mac.pop("parity", None)
+        parity["cfg1_tg_64"] = parity_cfg1(dev)
+        for row, key in ((eb_mac, "cfg4_eb_mac"), (eb_nodal, "cfg4_eb_nodal")):
+            if row is not None and "parity" in row:
+                parity[key] = row.pop("parity")
 
     launches = int(sum(s["kernel_launches"] for s in st_mixed))
     line = {
@@ -593,6 +705,7 @@ def run_ours(args, ws, rank, local):
         "roofline_fp64_jacobi": {"achieved_gbs": round(ach64, 1), "frac_hbm": round(ach64 / peak, 4),
                                  "ms_per_launch": round(ms64.value, 5)},
         "cpu_baseline": cpu,
+        "parity": parity,
         "e2e": e2e,
         "amr": amr,
         "mac": mac,
@@ -623,6 +736,7 @@ def main():
     ap.add_argument("--no-tensor", action="store_true")
     ap.add_argument("--no-mac", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-warm-start", action="store_true")
     ap.add_argument("--warm-level", type=int, default=1)
     args = ap.parse_args()

@@ -1008,10 +1008,9 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
         frexp(bnorm * gc.vol, &ex);
         scale32 = ldexp(1.0, -ex);
     }
-    // V-cycles per level per refinement step (GBP_AMR_CYCLES overrides, 1..4); one is the fastest on the
-    // 256^3 + band workload (186 ms against 205 ms with two)
-    int m = 1;
-    if (const char* e = getenv("GBP_AMR_CYCLES")) m = std::max(1, std::min(4, atoi(e)));
+    // V-cycles per level per refinement step: one is the fastest on the 256^3 + band workload (186 ms
+    // against 205 ms with two)
+    const int m = 1;
     int it = 0, status = GBP_OK;
     const double r0 = rn;
     while (rn > target) {

@@ -1,7 +1,7 @@
 // gbp_nodal_divergence_noalloc: the nodal divergence of gbp_nodal_divergence for callers that cannot
-// allocate device memory -- code running inside a CUDA stream capture that must not add allocation
-// nodes, a host application whose device memory is owned by another framework's allocator, or an
-// embedding (e.g. a solver plugin) that may not create a plan. It needs no plan: it reads the
+// allocate device memory: a host application whose device memory belongs to another framework's
+// allocator (which may own the whole memory pool, or forbid cudaMalloc / cudaFree while it runs), or an
+// embedding such as a solver plugin that may not create a plan. It needs no plan: it reads the
 // caller's velocity, writes the caller's output, and keeps its only scratch (per-block partial sums
 // and two scalars) in the file-scope device array below, which every GPU that loads this library
 // holds until the process exits.
@@ -9,10 +9,14 @@
 // Limits and rules:
 //  - scratch holds kMaxBlocks per-block partial sums: at most 65536 blocks of 32 x 4 x 4 nodes, i.e.
 //    about 33.5 million nodes (256^3 fits; larger grids are rejected with GBP_BAD_ARG);
-//  - the first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
-//    device current; make that first call before any stream capture;
+//  - the first call on a device (and the first call after that device's context was reset) looks up
+//    the array's device address (cudaGetSymbolAddress) with that device current; make that first call
+//    before any stream capture;
 //  - every call shares the one array: calls that overlap on the GPU (different streams, or another
-//    host thread) race on it; serialise them.
+//    host thread) race on it; serialise them;
+//  - each call ends by reading the max norm back to the host, so it synchronises the stream it is
+//    given.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -31,8 +35,26 @@ constexpr int BX = 32, BY = 4, BZ = 4;
 // shift; [kMaxBlocks + 1]: the max norm (as ordered bits)
 static __device__ __align__(256) double g_noalloc_scratch[kMaxBlocks + 8];
 
+// the scratch address per device, with the context it was looked up in: a device reset creates a new
+// context (and reloads this module), after which the address is looked up again
 std::mutex g_mu;
 double* g_dev_scratch[kMaxDevices] = {};
+CUcontext g_dev_ctx[kMaxDevices] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+CtxGetCurrentFn ctx_get_current()
+{
+    static CtxGetCurrentFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrentFn>(p);
+    });
+    return fn;
+}
 
 __device__ __forceinline__ double a4v(const gbp_array4& a, int i, int j, int k, int n)
 {
@@ -68,7 +90,9 @@ __global__ void __launch_bounds__(BX* BY* BZ) k_div_noalloc(NodalGeom g, DivArgs
             int ci = cell[d];
             if (g.per[d]) {
                 ci = ((ci % g.n[d]) + g.n[d]) % g.n[d];
-            } else if (ci < 0 || ci >= g.n[d]) {
+            } else if (ci < -1 || ci > g.n[d]) {
+                nout += 2;  // beyond the one ghost layer: no flux, and never read
+            } else if (ci == -1 || ci == g.n[d]) {
                 ++nout;
                 dout = d;
             }
@@ -187,11 +211,13 @@ extern "C" int gbp_nodal_divergence_noalloc(const gbp_geometry* geom, const int 
     g.ivol = 1.0 / g.vol;
     // argument layout: velocity over the valid cells (+1 ghost across inflow faces), output nodes 0..n
     for (int d = 0; d < 3; ++d) {
-        const int gh = (use_inflow && (bc_lo[d] == GBP_BC_INFLOW || bc_hi[d] == GBP_BC_INFLOW)) ? 1 : 0;
-        if (vel->ncomp < 3 || vel->lo[d] > -gh || vel->hi[d] < g.n[d] - 1 + gh || div_out->lo[d] > 0 ||
+        // one ghost cell on each side that is an inflow face (read only when use_inflow is set)
+        const int glo = (use_inflow && bc_lo[d] == GBP_BC_INFLOW) ? 1 : 0;
+        const int ghi = (use_inflow && bc_hi[d] == GBP_BC_INFLOW) ? 1 : 0;
+        if (vel->ncomp < 3 || vel->lo[d] > -glo || vel->hi[d] < g.n[d] - 1 + ghi || div_out->lo[d] > 0 ||
             div_out->hi[d] < g.n[d]) {
             set_error("gbp_nodal_divergence_noalloc: vel must cover the valid cells (3 components, one ghost cell "
-                      "across inflow faces) and div_out nodes 0..n");
+                      "across each inflow face) and div_out nodes 0..n");
             return GBP_BAD_ARG;
         }
     }
@@ -210,14 +236,23 @@ extern "C" int gbp_nodal_divergence_noalloc(const gbp_geometry* geom, const int 
         set_error("gbp_nodal_divergence_noalloc: device ordinal out of range");
         return GBP_BAD_ARG;
     }
+    // cudaFree(0) makes the device's primary context current without allocating, so that the context
+    // key below is the one the launches use
+    e = cudaFree(nullptr);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFree(nullptr) (context initialisation)");
+    CUcontext ctx = nullptr;
+    if (auto fn = ctx_get_current()) {
+        if (fn(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+    }
     double* scr = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_dev_scratch[dev]) {
+        if (!g_dev_scratch[dev] || g_dev_ctx[dev] != ctx) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
             g_dev_scratch[dev] = static_cast<double*>(p);
+            g_dev_ctx[dev] = ctx;
         }
         scr = g_dev_scratch[dev];
     }

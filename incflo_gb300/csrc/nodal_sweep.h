@@ -1,5 +1,5 @@
-// TMA-staged level sweeps of the nodal operator (nodal_sweep64.cu: FP64 sweep, tensor maps and launch
-// helpers; nodal_sweep32.cu: FP32 producer/consumer sweep).
+// TMA-staged level sweeps of the nodal operator (nodal_sweep64.cu: FP64 and FP32 sweeps, tensor maps and
+// launch helpers).
 #pragma once
 
 #include <cuda.h>
@@ -40,7 +40,5 @@ int sweep_z_chunks(const NodalGeom& g, int xy_tiles, int resident);
 int sm_count_cached();
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st);
-int sweep32_tma1_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out,
-                     float omega, unsigned* err, unsigned long long* norm, cudaStream_t st, bool packed);
 
 }  // namespace gbp

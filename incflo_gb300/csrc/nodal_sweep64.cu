@@ -8,7 +8,7 @@
 // per sweep (halos come from L2) and each node reads only plane k+1 from shared memory.
 //
 // This file holds the FP64 sweep (FP64-issue-bound on GB300: one node per thread, 32 x 8 nodes per
-// CTA, 3 slots), the tensor-map cache and the launch helpers; the FP32 sweep is in nodal_sweep32.cu.
+// CTA, 3 slots), the FP32 sweep of the same design, the tensor-map cache and the launch helpers.
 //
 // Padded layout (gbp_internal.cuh): node / cell q of a row sits at position q + 4. Every x box
 // starts at position x0 (node x0 - 4), a multiple of 32 elements, so it is 16-byte aligned; a box
@@ -243,159 +243,6 @@ __global__ void __launch_bounds__(SweepShape<float>::THREADS)
             fence_proxy_async();
             issue(s + NS);
         }
-    }
-    if (abort_flag && tid == 0)
-        for (int q = 0; q < NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
-    if (MODE == 1 && norm) {
-        const double m = block_max((double)nmax);
-        if (tid == 0) atomic_max_nonneg(norm, m);
-    }
-}
-
-// Packed variant of k_sweep32t: the same tiles, TMA ring and arithmetic order per cell, but (1) the
-// two cells of a row of a cell layer are evaluated as one FP32x2 lane pair (__fadd2_rn /
-// __ffma2_rn: one instruction for both), and (2) the z loop is unrolled six ways so the plane and
-// sigma-layer registers rotate roles instead of being copied every plane.
-struct Plane32 {
-    float2 e[3];  // (x-1, x+1) of rows y-1, y, y+1
-    float m[3];   // x of rows y-1, y, y+1
-};
-
-__device__ __forceinline__ void layer32p(const Plane32& Pn, const Plane32& Pd, const float2 (&sg)[2], float xc,
-                                         float2& acc, float2& ssum)
-{
-    const float2 nx = make_float2(-xc, -xc);
-#pragma unroll
-    for (int cy = 0; cy < 2; ++cy) {
-        const int oy = cy ? 2 : 0;
-        const float2 a = __fadd2_rn(Pn.e[oy], nx);
-        const float2 b = __fadd2_rn(Pd.e[1], nx);
-        const float c = Pd.m[oy] - xc;
-        const float2 d = __fadd2_rn(Pd.e[oy], nx);
-        const float2 S = __fadd2_rn(__fadd2_rn(a, b), __fadd2_rn(make_float2(c, c), d));
-        acc = __ffma2_rn(sg[cy], S, acc);
-        ssum = __fadd2_rn(ssum, sg[cy]);
-    }
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(SweepShape<float>::THREADS)
-    k_sweep32p(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
-               const __grid_constant__ CUtensorMap mb, NodalGeom g, float* __restrict__ out, float k0, float k3,
-               float omega, int kchunk, unsigned* err, unsigned long long* norm)
-{
-    using S = SweepShape<float>;
-    constexpr int NS = S::NS;
-    extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t bar[NS];
-    __shared__ int abort_flag;
-
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = tx + 32 * ty;
-    const int x0 = blockIdx.x * S::NX, y0 = blockIdx.y * S::TY;
-    const int kbeg = blockIdx.z * kchunk;
-    const int kend = min(kbeg + kchunk, g.nu[2]);
-    const int nsteps = kend - kbeg + 2;
-    const int i = x0 + tx, j = y0 + ty;
-    const bool active = i < g.nu[0] && j < g.nu[1];
-    const bool dxy = dir_xy(g, i, j), axy = alias_xy(g, i, j);
-    float* op = out + pidx(g.sy, g.sz, i, j, kbeg);
-
-    auto issue = [&](int st) {
-        const int slot = st % NS;
-        unsigned char* base = smem + slot * S::STAGE;
-        const int k = kbeg - 2 + st;
-        mbar_arrive_expect_tx(&bar[slot], S::TX_BYTES);
-        tma_load_3d(base + S::XO, &mx, &bar[slot], x0, y0, k + 2);
-        tma_load_3d(base + S::SO, &ms, &bar[slot], x0, y0, k + 1);
-        tma_load_3d(base + S::BO, &mb, &bar[slot], x0 + kOX, y0 + 1, k + 1);
-    };
-    if (tid == 0) {
-        for (int q = 0; q < NS; ++q) mbar_init(&bar[q], 1);
-        mbar_fence_init();
-        abort_flag = 0;
-    }
-    __syncthreads();
-    if (tid == 0)
-        for (int st = 0; st < NS && st < nsteps; ++st) issue(st);
-
-    Plane32 P0, P1, P2;
-    float2 S0[2], S1[2];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        P0.e[a] = P1.e[a] = P2.e[a] = make_float2(0.f, 0.f);
-        P0.m[a] = P1.m[a] = P2.m[a] = 0.f;
-    }
-    S0[0] = S0[1] = S1[0] = S1[1] = make_float2(0.f, 0.f);
-    float nmax = 0.f;
-    bool stop = false;
-
-    // one plane step: load plane k+1 into Pn and cell layer k into Sn, finish node (i, j, k)
-    auto step = [&](int st, const Plane32& Pm, const Plane32& Pc, Plane32& Pn, const float2 (&Sm)[2],
-                    float2 (&Sn)[2]) {
-        const int slot = st % NS;
-        const unsigned char* base = smem + slot * S::STAGE;
-        if (!mbar_wait_bounded(&bar[slot], (uint32_t)((st / NS) & 1), err)) abort_flag = 1;
-        __syncthreads();
-        if (abort_flag) {
-            stop = true;
-            return;
-        }
-        const float* sx = reinterpret_cast<const float*>(base + S::XO) + tx + 3;
-        const float* ss = reinterpret_cast<const float*>(base + S::SO) + tx + 3;
-        const float* sb = reinterpret_cast<const float*>(base + S::BO) + tx;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            Pn.e[a] = make_float2(sx[(ty + a) * S::BXX], sx[(ty + a) * S::BXX + 2]);
-            Pn.m[a] = sx[(ty + a) * S::BXX + 1];
-        }
-#pragma unroll
-        for (int a = 0; a < 2; ++a) Sn[a] = make_float2(ss[(ty + a) * S::BXS], ss[(ty + a) * S::BXS + 1]);
-        const float bv = sb[ty * S::BXB];
-        const int k = kbeg - 2 + st;
-        if (st >= 2 && active) {
-            float v = 0.f;
-            if (!(dxy || dir_k(g, k))) {
-                const float xc = Pc.m[1];
-                float2 acc = make_float2(0.f, 0.f), ss2 = make_float2(0.f, 0.f);
-                layer32p(Pc, Pm, Sm, xc, acc, ss2);
-                layer32p(Pc, Pn, Sn, xc, acc, ss2);
-                const float ax = k3 * (acc.x + acc.y);
-                const float ssum = ss2.x + ss2.y;
-                if (MODE == 0) {
-                    v = fmaf(omega * (bv - ax), __frcp_rn(k0 * ssum), xc);
-                } else {
-                    v = bv - ax;
-                    if (norm)
-                        nmax = (v != v || nmax != nmax) ? __int_as_float(0x7fc00000)
-                                                        : fmaxf(nmax, fabsf(v) * (float)node_inv_volume(g, i, j, k));
-                }
-            }
-            if (axy || alias_k(g, k))
-                store_node(out, g, i, j, k, v);
-            else
-                *op = v;
-            op += g.sz;
-        }
-        __syncthreads();
-        if (tid == 0 && st + NS < nsteps) {
-            fence_proxy_async();
-            issue(st + NS);
-        }
-    };
-
-    for (int st = 0; st < nsteps && !stop; st += 6) {
-        step(st, P0, P1, P2, S0, S1);
-        if (st + 1 >= nsteps || stop) break;
-        step(st + 1, P1, P2, P0, S1, S0);
-        if (st + 2 >= nsteps || stop) break;
-        step(st + 2, P2, P0, P1, S0, S1);
-        if (st + 3 >= nsteps || stop) break;
-        step(st + 3, P0, P1, P2, S1, S0);
-        if (st + 4 >= nsteps || stop) break;
-        step(st + 4, P1, P2, P0, S0, S1);
-        if (st + 5 >= nsteps || stop) break;
-        step(st + 5, P2, P0, P1, S1, S0);
     }
     if (abort_flag && tid == 0)
         for (int q = 0; q < NS; ++q) (void)mbar_wait_bounded(&bar[q], 0, nullptr);
@@ -671,12 +518,12 @@ static int launch_sweep(const CUtensorMap& mx, const CUtensorMap& ms, const CUte
     return GBP_OK;
 }
 
-template <int MODE, bool PK>
+template <int MODE>
 static int launch_sweep32t(const CUtensorMap& mx, const CUtensorMap& ms, const CUtensorMap& mb, const NodalGeom& g,
                            float* out, float omega, unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
     using S = SweepShape<float>;
-    auto kern = PK ? k_sweep32p<MODE> : k_sweep32t<MODE>;
+    auto kern = k_sweep32t<MODE>;
     static int resident = 0;
     if (!resident) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM);
@@ -693,8 +540,8 @@ static int launch_sweep32t(const CUtensorMap& mx, const CUtensorMap& ms, const C
     return GBP_OK;
 }
 
-int sweep32_tma1_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out,
-                     float omega, unsigned* err, unsigned long long* norm, cudaStream_t st, bool packed)
+int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
+                unsigned* err, unsigned long long* norm, cudaStream_t st)
 {
     using S = SweepShape<float>;
     CUtensorMap mx, ms, mb;
@@ -702,11 +549,8 @@ int sweep32_tma1_run(const NodalGeom& g, int mode, const float* s, const float* 
     if (!rc) rc = make_tensor_map(s, 4, g.sy, g.sz, g.count, S::BXS, S::TY + 1, &ms);
     if (!rc) rc = make_tensor_map(b, 4, g.sy, g.sz, g.count, S::BXB, S::TY, &mb);
     if (rc) return rc;
-    if (packed)
-        return mode == 0 ? launch_sweep32t<0, true>(mx, ms, mb, g, out, omega, err, norm, st)
-                         : launch_sweep32t<1, true>(mx, ms, mb, g, out, omega, err, norm, st);
-    return mode == 0 ? launch_sweep32t<0, false>(mx, ms, mb, g, out, omega, err, norm, st)
-                     : launch_sweep32t<1, false>(mx, ms, mb, g, out, omega, err, norm, st);
+    return mode == 0 ? launch_sweep32t<0>(mx, ms, mb, g, out, omega, err, norm, st)
+                     : launch_sweep32t<1>(mx, ms, mb, g, out, omega, err, norm, st);
 }
 
 template <>

@@ -199,14 +199,17 @@ int gbp_nodal_divergence(gbp_plan* plan, const gbp_array4* vel, int use_inflow, 
                          double* max_norm);
 
 /* Allocation-free gbp_nodal_divergence. No counterpart in the reference. For callers that cannot
- * allocate device memory: code inside a CUDA stream capture that must not add allocation nodes, or
- * a host program whose device memory belongs to another allocator. Needs no plan; the only scratch
- * is a static device array built into the library (512 KB per GPU, held until the process exits),
- * which caps the grid at 65536 blocks of 32x4x4 nodes (about 33.5 million nodes; larger grids return
- * GBP_BAD_ARG). The first call on a device looks up that array's address with the device current,
- * so make it before any stream capture. All calls share the array: calls that overlap on the GPU
- * race, so serialise them. Arguments as gbp_nodal_divergence, plus the level geometry, boundary
- * types and stream that a plan would otherwise hold; *max_norm is written on return. */
+ * allocate device memory: a host program whose device memory belongs to another framework's
+ * allocator (which may hold the whole pool or forbid cudaMalloc while it runs), or a plugin that may
+ * not create a plan. Needs no plan; the only scratch is a static device array built into the library
+ * (512 KB per GPU, held until the process exits), which caps the grid at 65536 blocks of 32x4x4
+ * nodes (about 33.5 million nodes; larger grids return GBP_BAD_ARG). The first call on a device
+ * (and the first after a reset of its context) looks up that array's address with the device
+ * current, so make it before any stream capture. All calls share the array: calls that overlap on
+ * the GPU race, so serialise them. Arguments as gbp_nodal_divergence, plus the level geometry,
+ * boundary types and stream that a plan would otherwise hold; vel needs one ghost cell only across
+ * the sides that are inflow faces. *max_norm is read back to the host before the call returns, so
+ * the call synchronises the stream. */
 int gbp_nodal_divergence_noalloc(const gbp_geometry* geom, const int bc_lo[3], const int bc_hi[3],
                                  const gbp_array4* vel, int use_inflow, gbp_array4* div_out,
                                  double* max_norm, void* stream);

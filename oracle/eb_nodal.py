@@ -24,7 +24,7 @@ import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
-PERIODIC, DIRICHLET, NEUMANN = 0, 1, 2
+PERIODIC, DIRICHLET, NEUMANN, INFLOW = 0, 1, 2, 3
 
 
 def _sgn(a, d):
@@ -74,6 +74,11 @@ def element(M, h):
 
 
 class EBNodal:
+    """The cut-cell nodal system of one box. Inflow sides (code 3) are natural boundaries like Neumann
+    sides; their right-hand-side term comes from the ghost cells of the velocity passed to project()
+    (regular ghost cells across the face, normal component only, as the plain oracle's or_nodal_rhs
+    takes them)."""
+
     def __init__(self, n, h, bclo, bchi, moments):
         self.n = [int(v) for v in n]
         self.h = [float(v) for v in h]
@@ -87,68 +92,137 @@ class EBNodal:
         self._elements()
 
     def _node(self, i, j, k):
-        v = [i, j, k]
+        """Unknown index of node (i, j, k) (scalars or integer arrays; periodic positions wrapped)."""
+        v = [np.asarray(i), np.asarray(j), np.asarray(k)]
         for d in range(3):
             if self.per[d]:
-                v[d] %= self.n[d]
+                v[d] = v[d] % self.n[d]
         return v[0] + self.nu[0] * (v[1] + self.nu[1] * v[2])
 
     def _fixed(self, i, j, k):
-        for d, v in enumerate((i, j, k)):
+        """Whether node (i, j, k) sits on a Dirichlet side (arrays accepted)."""
+        out = np.zeros(np.broadcast(np.asarray(i), np.asarray(j), np.asarray(k)).shape, bool)
+        for d, v in enumerate((np.asarray(i), np.asarray(j), np.asarray(k))):
             if self.per[d]:
                 continue
-            if (v == 0 and self.bclo[d] == DIRICHLET) or (v == self.n[d] and self.bchi[d] == DIRICHLET):
-                return True
-        return False
+            if self.bclo[d] == DIRICHLET:
+                out |= v == 0
+            if self.bchi[d] == DIRICHLET:
+                out |= v == self.n[d]
+        return out
 
     def _elements(self):
-        cache = {}
-        self.cells = []
         n = self.n
-        for k, j, i in itertools.product(range(n[2]), range(n[1]), range(n[0])):
-            if self.kap[k, j, i] <= 0.0:
-                continue
-            key = self.M[k, j, i].tobytes()
-            if key not in cache:
-                cache[key] = element(self.M[k, j, i], self.h)
-            nodes = [self._node(i + (a & 1), j + ((a >> 1) & 1), k + (a >> 2)) for a in range(8)]
-            fixed = [self._fixed(i + (a & 1), j + ((a >> 1) & 1), k + (a >> 2)) for a in range(8)]
-            self.cells.append(((i, j, k), nodes, fixed, cache[key]))
+        kk, jj, ii = np.nonzero(self.kap > 0.0)
+        self.cell_k, self.cell_j, self.cell_i = kk, jj, ii
+        Mc = self.M[kk, jj, ii].reshape(len(kk), 27)
+        keys, inv = np.unique(Mc, axis=0, return_inverse=True)
+        els = [element(key.reshape(3, 3, 3), self.h) for key in keys]
+        self.Ku = np.array([e[0] for e in els]).reshape(-1, 8, 8)
+        self.Gu = np.array([e[1] for e in els]).reshape(-1, 8, 3)
+        self.Gcu = np.array([e[2] for e in els]).reshape(-1, 8, 3)
+        self.inv = np.asarray(inv).reshape(-1)
+        a = np.arange(8)
+        ci, cj, ck = ii[:, None] + (a & 1), jj[:, None] + ((a >> 1) & 1), kk[:, None] + (a >> 2)
+        self.ids = self._node(ci, cj, ck)
+        fixed_c = self._fixed(ci, cj, ck)
         N = self.nu[0] * self.nu[1] * self.nu[2]
         self.active = np.zeros(N, bool)
+        self.active[self.ids.reshape(-1)] = True
         self.fixed = np.zeros(N, bool)
-        for _, nodes, fixed, _ in self.cells:
-            for a in range(8):
-                self.active[nodes[a]] = True
-                self.fixed[nodes[a]] |= fixed[a]
+        self.fixed[self.ids[fixed_c]] = True
 
-    def assemble(self, sigma, u):
+    def _inflow_rhs(self, b, u_ghost):
+        """Inflow sides: each ghost cell across the face adds its normal velocity times the regular
+        element's int dN/dn (+-h_e h_f / 4) to the four face nodes it touches (or_nodal_rhs's term)."""
+        n, h = self.n, self.h
+        for d in range(3):
+            for side, bc in ((0, self.bclo[d]), (1, self.bchi[d])):
+                if bc != INFLOW:
+                    continue
+                e, f = [q for q in range(3) if q != d]  # e < f, so the slice's array axes are (f, e)
+                sl = [slice(1, -1)] * 3
+                sl[2 - d] = 0 if side == 0 else n[d] + 1
+                vals = u_ghost[(d,) + tuple(sl)]
+                tf, te = np.meshgrid(np.arange(n[f]), np.arange(n[e]), indexing="ij")
+                w = (1.0 if side == 0 else -1.0) * h[e] * h[f] / 4.0
+                for de in (0, 1):
+                    for df in (0, 1):
+                        idx = [None, None, None]
+                        idx[d] = np.full(te.shape, 0 if side == 0 else n[d])
+                        idx[e] = te + de
+                        idx[f] = tf + df
+                        node = self._node(idx[0], idx[1], idx[2])
+                        np.add.at(b, node.reshape(-1), (w * vals).reshape(-1))
+
+    def assemble(self, sigma, u, u_ghost=None):
+        """Sparse operator A (all node positions, unknowns and not) and right-hand side b."""
         N = self.nu[0] * self.nu[1] * self.nu[2]
-        rows, cols, vals = [], [], []
-        b = np.zeros(N)
-        for (i, j, k), nodes, fixed, (K, G, _) in self.cells:
-            s = sigma[k, j, i]
-            for a in range(8):
-                b[nodes[a]] += float(G[a] @ u[:, k, j, i])
-                for c in range(8):
-                    rows.append(nodes[a])
-                    cols.append(nodes[c])
-                    vals.append(s * K[a, c])
+        s = sigma[self.cell_k, self.cell_j, self.cell_i]
+        rows = np.repeat(self.ids, 8, axis=1).reshape(-1)
+        cols = np.tile(self.ids, (1, 8)).reshape(-1)
+        vals = (s[:, None, None] * self.Ku[self.inv]).reshape(-1)
         A = sp.csr_matrix((vals, (rows, cols)), shape=(N, N))
+        b = self.rhs(u, u_ghost)
         return A, b
 
-    def project(self, sigma, u):
+    def rhs(self, u, u_ghost=None):
+        N = self.nu[0] * self.nu[1] * self.nu[2]
+        uc = u[:, self.cell_k, self.cell_j, self.cell_i]  # (3, ncell)
+        contrib = np.einsum("cad,dc->ca", self.Gu[self.inv], uc)
+        b = np.bincount(self.ids.reshape(-1), weights=contrib.reshape(-1), minlength=N)
+        if u_ghost is not None:
+            self._inflow_rhs(b, u_ghost)
+        return b
+
+    def apply(self, sigma, phi_u, chunk=1 << 17):
+        """A phi over all node positions, matrix-free (phi_u indexed like the unknowns)."""
+        N = self.nu[0] * self.nu[1] * self.nu[2]
+        y = np.zeros(N)
+        s = sigma[self.cell_k, self.cell_j, self.cell_i]
+        for c0 in range(0, len(s), chunk):
+            sl = slice(c0, c0 + chunk)
+            ids = self.ids[sl]
+            kx = np.einsum("cab,cb->ca", self.Ku[self.inv[sl]], phi_u[ids]) * s[sl, None]
+            y += np.bincount(ids.reshape(-1), weights=kx.reshape(-1), minlength=N)
+        return y
+
+    def dual_volume(self):
+        """Fluid volume of each node's dual cell (kappa V / 8 from every cell around it)."""
+        N = self.nu[0] * self.nu[1] * self.nu[2]
+        V = self.h[0] * self.h[1] * self.h[2]
+        w = self.kap[self.cell_k, self.cell_j, self.cell_i] * V / 8.0
+        return np.bincount(self.ids.reshape(-1), weights=np.repeat(w, 8), minlength=N)
+
+    def to_unknowns(self, phi_all):
+        """A node array over all positions (nz+1, ny+1, nx+1) as the unknown-indexed vector."""
+        n = self.n
+        out = np.zeros(self.nu[0] * self.nu[1] * self.nu[2])
+        k, j, i = np.meshgrid(np.arange(self.nu[2]), np.arange(self.nu[1]), np.arange(self.nu[0]), indexing="ij")
+        out[self._node(i, j, k).reshape(-1)] = phi_all[:self.nu[2], :self.nu[1], :self.nu[0]].reshape(-1)
+        del n
+        return out
+
+    def residual_norm(self, sigma, u, phi_all, u_ghost=None):
+        """max |b - A phi| / (fluid dual volume) over the unknowns, relative to the same norm of b
+        (after the consistency shift on singular systems): a check of a solution at any size."""
+        b = self.rhs(u, u_ghost)
+        w = self.dual_volume()
+        unk = self.active & ~self.fixed
+        if self.singular:
+            b[unk] -= w[unk] * b[unk].sum() / w[unk].sum()
+        r = b - self.apply(sigma, self.to_unknowns(phi_all))
+        bn = np.max(np.abs(b[unk]) / w[unk])
+        return float(np.max(np.abs(r[unk]) / w[unk]) / bn) if bn > 0 else 0.0
+
+    def project(self, sigma, u, u_ghost=None):
         """Returns dict(phi (all node positions), u (projected), grad (3, nz, ny, nx), b)."""
-        A, b = self.assemble(sigma, u)
+        A, b = self.assemble(sigma, u, u_ghost)
         unk = np.nonzero(self.active & ~self.fixed)[0]
         Aa = A[unk][:, unk].tocsc()
         ba = b[unk]
         if self.singular:
-            w = np.zeros(len(self.active))
-            for (i, j, k), nodes, fixed, _ in self.cells:
-                for a in range(8):
-                    w[nodes[a]] += self.kap[k, j, i] / 8.0
-            wu = w[unk]
+            wu = (self.dual_volume() / (self.h[0] * self.h[1] * self.h[2]))[unk]
             ba = ba - wu * ba.sum() / wu.sum()
             Ab = sp.bmat([[Aa, sp.csc_matrix(wu.reshape(-1, 1))], [sp.csc_matrix(wu.reshape(1, -1)), None]]).tocsc()
             x = spla.spsolve(Ab, np.concatenate([ba, [0.0]]))[:len(unk)]
@@ -157,13 +231,13 @@ class EBNodal:
         phi_u = np.zeros(len(self.active))
         phi_u[unk] = x
         n = self.n
-        phi = np.zeros((n[2] + 1, n[1] + 1, n[0] + 1))
-        for k, j, i in itertools.product(range(n[2] + 1), range(n[1] + 1), range(n[0] + 1)):
-            phi[k, j, i] = phi_u[self._node(i, j, k)]
+        k, j, i = np.meshgrid(np.arange(n[2] + 1), np.arange(n[1] + 1), np.arange(n[0] + 1), indexing="ij")
+        phi = phi_u[self._node(i, j, k)]
         grad = np.zeros((3, n[2], n[1], n[0]))
         un = np.array(u, dtype=np.float64, copy=True)
-        for (i, j, k), nodes, fixed, (_, _, Gc) in self.cells:
-            g = Gc.T @ phi_u[nodes]
-            grad[:, k, j, i] = g
-            un[:, k, j, i] -= sigma[k, j, i] * g
+        g = np.einsum("cad,ca->dc", self.Gcu[self.inv], phi_u[self.ids])
+        s = sigma[self.cell_k, self.cell_j, self.cell_i]
+        for d in range(3):
+            grad[d, self.cell_k, self.cell_j, self.cell_i] = g[d]
+            un[d, self.cell_k, self.cell_j, self.cell_i] -= s * g[d]
         return {"phi": phi, "u": un, "grad": grad, "b": b, "unknowns": unk}

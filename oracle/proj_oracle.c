@@ -40,6 +40,7 @@ typedef struct {
     int per[3];
     int nst;
     int off[27][3];
+    long loff[27]; /* linear offset of each stencil entry (nodes away from every side need no wrap) */
     long n;
     double* st;
     double* vol;
@@ -105,6 +106,8 @@ static void lvl_alloc(lvl* L, const int dims[3], const int per[3], int nst)
                                      {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
         memcpy(L->off, o7, sizeof(o7));
     }
+    for (int m = 0; m < nst; ++m)
+        L->loff[m] = (long)L->off[m][0] + (long)dims[0] * ((long)L->off[m][1] + (long)dims[1] * L->off[m][2]);
     for (int k = 0; k < dims[2]; ++k)
         for (int j = 0; j < dims[1]; ++j)
             for (int i = 0; i < dims[0]; ++i)
@@ -124,6 +127,25 @@ static void lvl_free(lvl* L)
 
 static int center_index(const lvl* L) { return L->nst == 27 ? 13 : 0; }
 
+/* sum over the stencil row of node u = (i, j, k): nodes away from every side take the linear offsets,
+ * the others wrap (periodic) or drop (outside) each neighbour; zero coefficients are skipped either way */
+static inline double row_dot(const lvl* L, int i, int j, int k, long u, const double* x)
+{
+    const double* s = L->st + u * L->nst;
+    double acc = 0.0;
+    if (i >= 1 && i < L->dims[0] - 1 && j >= 1 && j < L->dims[1] - 1 && k >= 1 && k < L->dims[2] - 1) {
+        for (int m = 0; m < L->nst; ++m)
+            if (s[m] != 0.0) acc += s[m] * x[u + L->loff[m]];
+    } else {
+        for (int m = 0; m < L->nst; ++m) {
+            if (s[m] == 0.0) continue;
+            long v = nb(L, i, j, k, m);
+            if (v >= 0) acc += s[m] * x[v];
+        }
+    }
+    return acc;
+}
+
 static void lvl_apply(const lvl* L, const double* x, double* y)
 {
 #pragma omp parallel for schedule(static)
@@ -131,18 +153,7 @@ static void lvl_apply(const lvl* L, const double* x, double* y)
         for (int j = 0; j < L->dims[1]; ++j)
             for (int i = 0; i < L->dims[0]; ++i) {
                 long u = lid(L, i, j, k);
-                if (L->fixed[u]) {
-                    y[u] = 0.0;
-                    continue;
-                }
-                const double* s = L->st + u * L->nst;
-                double acc = 0.0;
-                for (int m = 0; m < L->nst; ++m) {
-                    if (s[m] == 0.0) continue;
-                    long v = nb(L, i, j, k, m);
-                    if (v >= 0) acc += s[m] * x[v];
-                }
-                y[u] = acc;
+                y[u] = L->fixed[u] ? 0.0 : row_dot(L, i, j, k, u, x);
             }
 }
 
@@ -153,26 +164,22 @@ static void lvl_resid(const lvl* L, const double* b, const double* x, double* r)
     for (long u = 0; u < L->n; ++u) r[u] = L->fixed[u] ? 0.0 : b[u] - r[u];
 }
 
-/* one colour-ordered Gauss-Seidel pass; dir=+1 colours 0..7, dir=-1 colours 7..0 */
+/* one colour-ordered Gauss-Seidel pass; dir=+1 colours 0..7, dir=-1 colours 7..0. Colour
+ * (i&1) | (j&1)<<1 | (k&1)<<2: the nodes of one colour are visited with stride 2 in each direction */
 static void lvl_gs(const lvl* L, const double* b, double* x, int dir)
 {
     int c0 = dir > 0 ? 0 : 7;
     for (int cc = 0; cc < 8; ++cc) {
         int col = c0 + dir * cc;
+        const int i0 = col & 1, j0 = (col >> 1) & 1, k0 = (col >> 2) & 1;
 #pragma omp parallel for schedule(static)
-        for (int k = 0; k < L->dims[2]; ++k)
-            for (int j = 0; j < L->dims[1]; ++j)
-                for (int i = 0; i < L->dims[0]; ++i) {
+        for (int k = k0; k < L->dims[2]; k += 2)
+            for (int j = j0; j < L->dims[1]; j += 2)
+                for (int i = i0; i < L->dims[0]; i += 2) {
                     long u = lid(L, i, j, k);
-                    if (L->color[u] != col || L->fixed[u]) continue;
-                    const double* s = L->st + u * L->nst;
-                    double acc = 0.0;
-                    for (int m = 0; m < L->nst; ++m) {
-                        if (s[m] == 0.0) continue;
-                        long v = nb(L, i, j, k, m);
-                        if (v >= 0) acc += s[m] * x[v];
-                    }
-                    double dg = s[center_index(L)];
+                    if (L->fixed[u]) continue;
+                    double acc = row_dot(L, i, j, k, u, x);
+                    double dg = L->st[u * L->nst + center_index(L)];
                     if (dg != 0.0) x[u] += (b[u] - acc) / dg;
                 }
     }
@@ -889,6 +896,7 @@ static void vcycle(mg_t* mg, int l)
         prolong_nodal_add(mg, l, mg->x[l + 1], x);
     else
         prolong_mac_add(mg, l, mg->x[l + 1], x);
+#pragma omp parallel for schedule(static)
     for (long u = 0; u < L->n; ++u)
         if (L->fixed[u]) x[u] = 0.0;
     for (int s = 0; s < mg->nu; ++s) lvl_gs(L, b, x, -1);
@@ -961,6 +969,7 @@ static int pcg(mg_t* mg, const double* rhs_in, double* phi, double rtol, double 
             double pq = dot(L, p, q);
             if (pq == 0.0) break;
             double alpha = rz / pq;
+#pragma omp parallel for schedule(static)
             for (long u = 0; u < n; ++u) {
                 phi[u] += alpha * p[u];
                 r[u] -= alpha * q[u];
@@ -975,6 +984,7 @@ static int pcg(mg_t* mg, const double* rhs_in, double* phi, double rtol, double 
             double rz2 = dot(L, r, z);
             double beta = rz2 / rz;
             rz = rz2;
+#pragma omp parallel for schedule(static)
             for (long u = 0; u < n; ++u) p[u] = z[u] + beta * p[u];
         }
         if (it > maxiter) status = 1;

@@ -99,3 +99,47 @@ def test_small_cell_removal_consistent_and_conditions_the_system():
         w = np.linalg.eigvalsh(A[ui][:, ui].toarray())
         conds.append(w[-1] / w[1])
     assert conds[0] > 1e8 and conds[1] < 1e6
+
+
+def test_inflow_sides_match_single_level_oracle():
+    """Inflow sides (ghost-cell normal velocity on the face) on a regular geometry reduce to the
+    single-level oracle's inflow term, on both the low and the high side."""
+    I = O.INFLOW
+    n, ext, bclo, bchi = (8, 6, 4), (1.0, 0.75, 0.5), (I, N, P), (D, I, P)
+    h = [ext[d] / n[d] for d in range(3)]
+    rng = np.random.default_rng(1)
+    sig = rng.uniform(0.5, 2.0, (n[2], n[1], n[0]))
+    vg = np.zeros((3, n[2] + 2, n[1] + 2, n[0] + 2))
+    vg[:, 1:-1, 1:-1, 1:-1] = rng.standard_normal((3, n[2], n[1], n[0]))
+    vg[0, 1:-1, 1:-1, 0] = rng.uniform(0.5, 1.5, (n[2], n[1]))   # x-low inflow ghosts
+    vg[1, 1:-1, -1, 1:-1] = rng.uniform(-1.5, -0.5, (n[2], n[0]))  # y-high inflow ghosts
+    g = O.Grid(n, hi=ext, bclo=bclo, bchi=bchi)
+    vn, phi, _, _ = O.nodal_project(g, sig, vg, rtol=1e-14)
+    M = np.broadcast_to(_full_moments(), (n[2], n[1], n[0], 3, 3, 3))
+    o = EBNodal(n, h, bclo, bchi, M)
+    u = np.ascontiguousarray(vg[:, 1:-1, 1:-1, 1:-1])
+    unk = o.active & ~o.fixed  # the C oracle writes 0 on Dirichlet nodes, which are not unknowns
+    np.testing.assert_allclose(o.rhs(u, vg)[unk], O.nodal_rhs(g, vg).reshape(-1)[unk], rtol=0, atol=1e-14)
+    r = o.project(sig, u, vg)
+    assert rel_l2(unique_nodes(g, r["phi"]), phi) <= 1e-11
+    np.testing.assert_allclose(r["u"], vn[:, 1:-1, 1:-1, 1:-1], rtol=0, atol=1e-11)
+
+
+def test_residual_norm_checks_a_solution():
+    """residual_norm (the full-size check of a GPU solution) is at round-off for the oracle's own
+    solution of a cut-cell channel with inflow and large for a perturbed one."""
+    I = O.INFLOW
+    n, ext = (32, 8, 4), (4.0, 1.0, 0.5)
+    h = [ext[d] / n[d] for d in range(3)]
+    M = eb.cylinder_moments(n, (0, 0, 0), ext, (1.0, 0.5, 0.0), 0.125, small_volfrac=1e-4)
+    rng = np.random.default_rng(2)
+    sig = np.ones((n[2], n[1], n[0]))
+    vg = np.zeros((3, n[2] + 2, n[1] + 2, n[0] + 2))
+    vg[:, 1:-1, 1:-1, 1:-1] = 1e-3 * rng.uniform(-1, 1, (3, n[2], n[1], n[0]))
+    vg[0] += 1.0
+    o = EBNodal(n, h, (I, N, P), (D, N, P), M)
+    u = np.ascontiguousarray(vg[:, 1:-1, 1:-1, 1:-1])
+    r = o.project(sig, u, vg)
+    assert o.residual_norm(sig, u, r["phi"], vg) <= 1e-11
+    bad = r["phi"] * (1 + 1e-6)
+    assert o.residual_norm(sig, u, bad, vg) >= 1e-8
