@@ -773,6 +773,15 @@ int gbp_plan_time_kernel(gbp_plan* p, int which, int reps, double* ms_per_launch
     return p->nodal->time_kernel(which, reps, ms_per_launch, bytes_per_launch);
 }
 
+int gbp_plan_check_level_kernels(gbp_plan* p, double diff[4])
+{
+    if (!p || !p->nodal || !diff) {
+        set_error("gbp_plan_check_level_kernels: needs a nodal plan and an output array");
+        return GBP_BAD_ARG;
+    }
+    return p->nodal->check_level_kernels(diff);
+}
+
 int gbp_nodal_set_eb(gbp_plan* p, const gbp_array4* moments)
 {
     if (!p || !p->nodal) {

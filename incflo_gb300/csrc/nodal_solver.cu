@@ -111,7 +111,10 @@ void NodalSolver::destroy()
     net_scr = nullptr;
     net_x0_bytes = 0;
     net = nullptr;
-    if (pool.base) sweep_forget_maps(pool.base, pool.bytes);
+    if (pool.base) {
+        sweep_forget_maps(pool.base, pool.bytes);
+        vsweep32_forget_maps(pool.base, pool.bytes);
+    }
     eb.pool.release();
     eb = EbState{};
     auxpool.release();
@@ -480,6 +483,10 @@ void NodalSolver::jacobi(const NodalGeom& g, const T* s, const T* x, const T* b,
     if (sizeof(T) == 8 && use_qsweep && &g == &L[0].g) {
         nodal_qsweep64(g, 0, reinterpret_cast<const double*>(s), qw, reinterpret_cast<const double*>(x),
                        reinterpret_cast<const double*>(b), reinterpret_cast<double*>(out), omega_eff, nullptr, s_);
+    } else if (sizeof(T) == 4 && use_tma && vsweep32_supported(g)) {
+        int rc = vsweep32(g, 0, reinterpret_cast<const float*>(s), reinterpret_cast<const float*>(x),
+                          reinterpret_cast<const float*>(b), reinterpret_cast<float*>(out), (float)omega_eff, derr, s_);
+        if (rc && !launch_rc) launch_rc = rc;
     } else if (use_tma && sweep_supported(g, (int)sizeof(T))) {
         int rc = nodal_sweep<T>(g, 0, s, x, b, out, omega_eff, derr, nullptr, s_);
         if (rc && !launch_rc) launch_rc = rc;
@@ -495,6 +502,10 @@ void NodalSolver::resid(const NodalGeom& g, const T* s, const T* x, const T* b, 
     if (sizeof(T) == 8 && use_qsweep && &g == &L[0].g) {
         nodal_qsweep64(g, 1, reinterpret_cast<const double*>(s), qw, reinterpret_cast<const double*>(x),
                        reinterpret_cast<const double*>(b), reinterpret_cast<double*>(r), omega_eff, norm, s_);
+    } else if (sizeof(T) == 4 && !norm && use_tma && vsweep32_supported(g)) {
+        int rc = vsweep32(g, 1, reinterpret_cast<const float*>(s), reinterpret_cast<const float*>(x),
+                          reinterpret_cast<const float*>(b), reinterpret_cast<float*>(r), 0.f, derr, s_);
+        if (rc && !launch_rc) launch_rc = rc;
     } else if (use_tma && sweep_supported(g, (int)sizeof(T))) {
         int rc = nodal_sweep<T>(g, 1, s, x, b, r, omega_eff, derr, norm, s_);
         if (rc && !launch_rc) launch_rc = rc;
@@ -536,9 +547,32 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
         ++nk;
         std::swap(x, t);
     }
+    const NodalLevel& cv = L[l + 1];
+    // FP32 levels with whole-row sweeps: residual + restriction in one pass, and the prolongation fused
+    // into the first post-smoothing sweep (the coarse level must not be the bottom: the sweeps read the
+    // coarse correction's periodic aliases, which the level sweeps write)
+    if constexpr (sizeof(T) == 4) {
+        if (!cut && use_tma && opt.nu2 >= 1 && l + 2 < (int)L.size() && vsweep32_transfer_supported(lv.g, cv.g)) {
+            int rc = vsweep32_resid_restrict(lv.g, cv.g, B::s(lv), x, b, B::b(cv), derr, s);
+            if (rc && !launch_rc) launch_rc = rc;
+            ++nk;
+            vcycle<T>(l + 1, B::b(cv), true);
+            rc = vsweep32_prolong_jacobi(lv.g, cv.g, B::s(lv), x, (const T*)xres[l + 1], b, t, (float)omega_eff, derr,
+                                         s);
+            if (rc && !launch_rc) launch_rc = rc;
+            ++nk;
+            std::swap(x, t);
+            for (int q = 1; q < opt.nu2; ++q) {
+                jacobi<T>(lv.g, B::s(lv), x, b, t, s);
+                ++nk;
+                std::swap(x, t);
+            }
+            xres[l] = x;
+            return;
+        }
+    }
     resid<T>(lv.g, B::s(lv), x, b, B::r(lv), nullptr, s);
     if (cut) eb_nodes<T>(lv.g, eb.e, 1, x, b, B::r(lv), omega_eff, s);
-    const NodalLevel& cv = L[l + 1];
     nodal_restrict<T>(lv.g, cv.g, B::r(lv), B::b(cv), s);
     nk += 2;
     vcycle<T>(l + 1, B::b(cv), true);
@@ -1334,8 +1368,12 @@ namespace gbp {
 
 int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
 {
-    if (which < 0 || which > 7 || reps < 1 || !sigma_ready || (which >= 6 && L.size() < 2)) {
-        set_error("time_kernel: which must be 0..7 (6, 7 need two levels), reps >= 1, and sigma must be set");
+    if (which < 0 || which > 9 || reps < 1 || !sigma_ready || (which >= 6 && L.size() < 2)) {
+        set_error("time_kernel: which must be 0..9 (6..9 need two levels), reps >= 1, and sigma must be set");
+        return GBP_BAD_ARG;
+    }
+    if (which >= 8 && !(use_tma && vsweep32_transfer_supported(L[0].g, L[1].g))) {
+        set_error("time_kernel: the fused transfer sweeps (8, 9) do not apply to this level");
         return GBP_BAD_ARG;
     }
     const NodalLevel& l0 = L[0];
@@ -1351,6 +1389,10 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
     // coarse b written
     if (which == 6) *bytes = 4.0 * (2.0 * nn + nn / 8.0);
     if (which == 7) *bytes = 4.0 * (nn + nn / 8.0);
+    // fused residual + restriction (8): x, b read per node, sigma per cell, coarse b written; fused
+    // prolongation + Jacobi (9): x, b read and the result written per node, sigma per cell, coarse x read
+    if (which == 8) *bytes = 4.0 * (2.0 * nn + nc + nn / 8.0);
+    if (which == 9) *bytes = 4.0 * (3.0 * nn + nc + nn / 8.0);
     if (f32) nodal_to_f32(g, res, l0.b32, scale32, st);
     GBP_CUDA(cudaEventRecord(ev0, st));
     for (int r = 0; r < reps; ++r) {
@@ -1362,6 +1404,17 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
         case 4: stream_triad(l0.x32, l0.s32, l0.b32, l0.r32, g.count, st); break;
         case 6: nodal_prolong_add<float>(g, L[1].g, L[1].x32, l0.x32, st); break;
         case 7: nodal_restrict<float>(g, L[1].g, l0.r32, L[1].b32, st); break;
+        case 8: {
+            int rc = vsweep32_resid_restrict(g, L[1].g, l0.s32, l0.x32, l0.b32, L[1].b32, derr, st);
+            if (rc) return rc;
+            break;
+        }
+        case 9: {
+            int rc = vsweep32_prolong_jacobi(g, L[1].g, l0.s32, l0.x32, L[1].x32, l0.b32, l0.t32, (float)omega_eff,
+                                             derr, st);
+            if (rc) return rc;
+            break;
+        }
         default:
             nodal_jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, omega_eff,
                                 false, st);
@@ -1393,6 +1446,125 @@ int NodalSolver::divergence(const RhsArgs& rhs, const gbp_array4* out, double* m
     GBP_CUDA(cudaStreamSynchronize(st));
     GBP_CUDA(cudaGetLastError());
     if (max_norm) *max_norm = bits_to_double(hnorm[0]);
+    return GBP_OK;
+}
+
+}  // namespace gbp
+
+namespace gbp {
+
+namespace {
+
+__global__ void k_maxdiff(const float* __restrict__ a, const float* __restrict__ ref, long long n,
+                          unsigned long long* out)
+{
+    double d = 0.0, m = 0.0;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+        d = nanmax(d, fabs((double)a[p] - (double)ref[p]));
+        m = nanmax(m, fabs((double)ref[p]));
+    }
+    d = block_max(d);
+    __syncthreads();
+    m = block_max(m);
+    if (threadIdx.x == 0) {
+        atomic_max_nonneg(out, d);
+        atomic_max_nonneg(out + 1, m);
+    }
+}
+
+// seeded values in [-1, 1) on the unique nodes (with their periodic aliases when `aliases`)
+__global__ void k_fill_seeded(NodalGeom g, float* __restrict__ a, unsigned seed, int aliases)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i >= g.nu[0]) return;
+    unsigned h = (unsigned)(i + 7919 * j + 104729 * k) * 2654435761u ^ seed;
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    const float v = (float)(h & 0xffffff) * (2.0f / 16777216.0f) - 1.0f;
+    if (aliases)
+        store_node(a, g, i, j, k, v);
+    else
+        a[pidx(g.sy, g.sz, i, j, k)] = v;
+}
+
+}  // namespace
+
+int NodalSolver::check_level_kernels(double diff[4])
+{
+    if (L.size() < 3 || !sigma_ready || !vsweep32_transfer_supported(L[0].g, L[1].g)) {
+        set_error("check_level_kernels: needs a level that the whole-row FP32 sweeps handle, and sigma");
+        return GBP_BAD_ARG;
+    }
+    const NodalLevel& l0 = L[0];
+    const NodalLevel& l1 = L[1];
+    const NodalGeom& g = l0.g;
+    float* A = reinterpret_cast<float*>(l0.t64);  // scratch: the FP64 arrays hold twice the FP32 count
+    float* C = reinterpret_cast<float*>(l0.r64);
+    unsigned long long* dm = reinterpret_cast<unsigned long long*>(dscal + 4);
+    auto compare = [&](const float* a, const float* ref, long long n, double* out) -> int {
+        GBP_CUDA(cudaMemsetAsync(dm, 0, 2 * sizeof(unsigned long long), st));
+        k_maxdiff<<<592, 256, 0, st>>>(a, ref, n, dm);
+        unsigned long long h[2];
+        GBP_CUDA(cudaMemcpyAsync(h, dm, sizeof(h), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+        double d, m;
+        memcpy(&d, &h[0], 8);
+        memcpy(&m, &h[1], 8);
+        *out = m > 0 ? d / m : d;
+        return GBP_OK;
+    };
+    const size_t f0 = sizeof(float) * g.count, f1 = sizeof(float) * l1.g.count;
+    GBP_CUDA(cudaMemsetAsync(derr, 0, sizeof(unsigned), st));
+    // seeded inputs, so that residuals are of the size of their terms: x and the coarse correction
+    // with their periodic aliases (as the level sweeps write them), b on the unique nodes only
+    GBP_CUDA(cudaMemsetAsync(l0.x32, 0, f0, st));
+    GBP_CUDA(cudaMemsetAsync(l0.b32, 0, f0, st));
+    GBP_CUDA(cudaMemsetAsync(l1.x32, 0, f1, st));
+    k_fill_seeded<<<dim3((g.nu[0] + 127) / 128, g.nu[1], g.nu[2]), 128, 0, st>>>(g, l0.x32, 17u, 1);
+    k_fill_seeded<<<dim3((g.nu[0] + 127) / 128, g.nu[1], g.nu[2]), 128, 0, st>>>(g, l0.b32, 29u, 0);
+    k_fill_seeded<<<dim3((l1.g.nu[0] + 127) / 128, l1.g.nu[1], l1.g.nu[2]), 128, 0, st>>>(l1.g, l1.x32, 41u, 1);
+    // [0] Jacobi
+    GBP_CUDA(cudaMemsetAsync(l0.t32, 0, f0, st));
+    GBP_CUDA(cudaMemsetAsync(A, 0, f0, st));
+    nodal_jacobi<float>(g, l0.s32, l0.x32, l0.b32, l0.t32, omega_eff, false, st);
+    int rc = vsweep32(g, 0, l0.s32, l0.x32, l0.b32, A, (float)omega_eff, derr, st);
+    if (!rc) rc = compare(A, l0.t32, g.count, &diff[0]);
+    // [1] residual
+    if (!rc) {
+        GBP_CUDA(cudaMemsetAsync(l0.r32, 0, f0, st));
+        GBP_CUDA(cudaMemsetAsync(A, 0, f0, st));
+        nodal_resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st);
+        rc = vsweep32(g, 1, l0.s32, l0.x32, l0.b32, A, 0.f, derr, st);
+    }
+    if (!rc) rc = compare(A, l0.r32, g.count, &diff[1]);
+    // [2] residual + restriction (l0.r32 holds the reference residual)
+    if (!rc) {
+        GBP_CUDA(cudaMemsetAsync(l1.b32, 0, f1, st));
+        GBP_CUDA(cudaMemsetAsync(l1.r32, 0, f1, st));
+        nodal_restrict<float>(g, l1.g, l0.r32, l1.b32, st);
+        rc = vsweep32_resid_restrict(g, l1.g, l0.s32, l0.x32, l0.b32, l1.r32, derr, st);
+    }
+    if (!rc) rc = compare(l1.r32, l1.b32, l1.g.count, &diff[2]);
+    // [3] prolongation + Jacobi: reference x' = x + P e in C, then a Jacobi sweep
+    if (!rc) {
+        GBP_CUDA(cudaMemcpyAsync(C, l0.x32, f0, cudaMemcpyDeviceToDevice, st));
+        nodal_prolong_add<float>(g, l1.g, l1.x32, C, st);
+        GBP_CUDA(cudaMemsetAsync(l0.t32, 0, f0, st));
+        GBP_CUDA(cudaMemsetAsync(A, 0, f0, st));
+        nodal_jacobi<float>(g, l0.s32, C, l0.b32, l0.t32, omega_eff, false, st);
+        rc = vsweep32_prolong_jacobi(g, l1.g, l0.s32, l0.x32, l1.x32, l0.b32, A, (float)omega_eff, derr, st);
+    }
+    if (!rc) rc = compare(A, l0.t32, g.count, &diff[3]);
+    if (rc) return rc;
+    unsigned herr = 0;
+    GBP_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    GBP_CUDA(cudaGetLastError());
+    if (herr) {
+        set_error("check_level_kernels: a bounded device wait ran out");
+        return GBP_TIMEOUT;
+    }
     return GBP_OK;
 }
 

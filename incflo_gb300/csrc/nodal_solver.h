@@ -117,6 +117,11 @@ public:
     long long kernel_count() const { return nk; }
     // time `reps` launches of one level-0 kernel (0/1: FP64/FP32 Jacobi, 2/3: FP64/FP32 residual)
     int time_kernel(int which, int reps, double* ms, double* bytes);
+    // Test hook: the level-0 FP32 whole-row sweeps against the one-node-per-thread kernels on seeded
+    // level-0 / level-1 data (the plan's sigma): max |new - reference| / max |reference| over every
+    // padded position for [0] Jacobi, [1] residual, [2] residual + restriction (coarse level), [3]
+    // prolongation + Jacobi. Overwrites solver scratch (the next solve refills it).
+    int check_level_kernels(double diff[4]);
 
     // Learned warm start for zero-guess solves: the network runs on multigrid level `level` (its
     // prediction is prolonged to level 0 and scaled by the Galerkin factor x.b / x.Ax); mode 0 off,

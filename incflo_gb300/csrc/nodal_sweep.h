@@ -41,4 +41,20 @@ int sm_count_cached();
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st);
 
+// FP32 whole-row sweeps with fused grid transfers (nodal_vsweep32.cu), isotropic levels without an
+// overset mask whose rows hold at most 512 nodes.
+bool vsweep32_supported(const NodalGeom& g);
+// ... and whose coarse level is the standard coarsening by 2 (residual + restriction, prolongation + sweep)
+bool vsweep32_transfer_supported(const NodalGeom& g, const NodalGeom& gc);
+// mode 0: Jacobi sweep, 1: residual
+int vsweep32(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
+             unsigned* err, cudaStream_t st);
+// bc (the coarse right-hand side) = full-weighting restriction of b - A x
+int vsweep32_resid_restrict(const NodalGeom& g, const NodalGeom& gc, const float* s, const float* x, const float* b,
+                            float* bc, unsigned* err, cudaStream_t st);
+// out = one Jacobi sweep from x + P ec (ec: the coarse correction)
+int vsweep32_prolong_jacobi(const NodalGeom& g, const NodalGeom& gc, const float* s, const float* x, const float* ec,
+                            const float* b, float* out, float omega, unsigned* err, cudaStream_t st);
+void vsweep32_forget_maps(const void* pool_base, size_t pool_bytes);
+
 }  // namespace gbp

@@ -333,9 +333,17 @@ int gbp_apply_nodal_projection_host(gbp_plan* plan, double* vel, const double* r
  * events, on the arrays of the last solve, and reports the kernel's algorithmic bytes per launch.
  * which: 0 = FP64 Jacobi sweep, 1 = FP32 Jacobi sweep, 2 = FP64 residual, 3 = FP32 residual,
  * 4 = streaming triad over three level arrays (an HBM reference), 5 = FP32 Jacobi through the
- * plain kernel, 6 = FP32 prolongation level 1 -> 0, 7 = FP32 restriction level 0 -> 1. */
+ * plain kernel, 6 = FP32 prolongation level 1 -> 0, 7 = FP32 restriction level 0 -> 1,
+ * 8 = fused FP32 residual + restriction 0 -> 1, 9 = fused FP32 prolongation 1 -> 0 + Jacobi. */
 int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_launch,
                          double* bytes_per_launch);
+
+/* No counterpart in the reference: a test hook. On seeded level-0 / level-1 data of a nodal plan (its
+ * sigma), runs the FP32 whole-row level kernels and the one-node-per-thread kernels they replace and
+ * writes max |new - reference| / max |reference| over every padded position (periodic aliases
+ * included) for diff[0] Jacobi, diff[1] residual, diff[2] residual + restriction, diff[3]
+ * prolongation + Jacobi. GBP_BAD_ARG when the whole-row kernels do not apply to the plan's level 0. */
+int gbp_plan_check_level_kernels(gbp_plan* plan, double diff[4]);
 
 /* MacProjector::setLevelBC(lev, nullptr, robin_a, robin_b, robin_f) for the GBP_BC_ROBIN sides
  * (incflo_compute_MAC_projected_velocities.cpp:116-123; data from incflo::make_robinBC_MFs,

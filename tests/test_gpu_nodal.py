@@ -61,11 +61,17 @@ def test_nodal_project_matches_oracle(gpu_lib, case, precision):
     np.testing.assert_array_equal(vel[:, 0], vel_or[:, 0])
 
 
+LARGE = [((176, 176, 168), (1.0, 1.0, 168 / 176), (P, P, N), (P, P, N)),
+         ((192, 136, 100), (1.0, 136 / 192, 100 / 192), (P, D, N), (P, I, D))]
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_large_level_tma_sweeps_match_oracle(gpu_lib, precision):
-    """A level above the size where the TMA-staged z-marching sweeps take over from the
-    one-node-per-thread kernels (176^2 x 168 cells: 5.4 M nodes), periodic x/y, walls in z."""
-    case = ((176, 176, 168), (1.0, 1.0, 168 / 176), (P, P, N), (P, P, N))
+@pytest.mark.parametrize("case", LARGE, ids=["periodic-xy", "dirichlet-inflow"])
+def test_large_level_tma_sweeps_match_oracle(gpu_lib, precision, case):
+    """Levels above the size where the TMA-staged z-marching sweeps take over from the
+    one-node-per-thread kernels (5.4 M and 2.7 M nodes; the mixed form runs the whole-row FP32
+    sweeps with the fused residual + restriction and prolongation + sweep on its two finest levels),
+    periodic, wall, Dirichlet and inflow sides."""
     g, st, st_or, phi, phi_or, vel, vel_or, grad, grad_or = _run(case, precision)
     assert st["status"] == 0 and st["final_rel_resid"] <= 1e-12
     assert rel_l2(phi, phi_or) <= 1e-9
@@ -215,3 +221,28 @@ def test_overset_mask_matches_oracle(gpu_lib, precision):
     got = vt.cpu().numpy()
     np.testing.assert_allclose(got[inner], vel_or[inner], rtol=0, atol=1e-9 * np.abs(vel_or[inner]).max())
     proj.setOversetMask(None)  # the shared plan goes back to the unmasked operator
+
+
+@pytest.mark.parametrize("case", [((256, 256, 256), (1.0, 1.0, 1.0), (P, P, N), (P, P, N)), LARGE[1]],
+                         ids=["256-periodic-xy", "192-dirichlet-inflow"])
+def test_whole_row_level_kernels_match_plain_kernels(gpu_lib, case):
+    """The FP32 whole-row sweeps (Jacobi, residual, fused residual + restriction, fused prolongation +
+    Jacobi) against the one-node-per-thread kernels on seeded level data (the plan's sigma), over every
+    padded position including the periodic aliases. Both compute in FP32 with different association, so
+    they agree to FP32 rounding; an indexing fault would differ by O(1)."""
+    import ctypes
+
+    from incflo_gb300 import _abi
+
+    n, ext, bclo, bchi = case
+    g, sigma, vel = nodal_case(n, ext, bclo, bchi, seed=9)
+    proj = NodalProjector(cuda(vel), cuda(sigma), Geometry(n, (0, 0, 0), ext),
+                          options=make_options(0, precision="mixed"))
+    proj.setDomainBC(bclo, bchi)
+    st = proj.project(rtol=1e-10, atol=0.0)
+    assert st["status"] == 0
+    diff = (ctypes.c_double * 4)()
+    _abi.check(_abi.load().gbp_plan_check_level_kernels(proj._plan().ptr, diff), "check_level_kernels")
+    print(f"\n{n}: jacobi {diff[0]:.2e} resid {diff[1]:.2e} resid+restrict {diff[2]:.2e} "
+          f"prolong+jacobi {diff[3]:.2e}")
+    assert max(diff) <= 1e-5
