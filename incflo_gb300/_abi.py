@@ -23,7 +23,7 @@ EXPORTS = (
     "gbp_plan_create", "gbp_plan_destroy", "gbp_plan_set_options", "gbp_plan_device_bytes",
     "gbp_nodal_set_sigma_from_density", "gbp_nodal_set_sigma", "gbp_nodal_project",
     "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
-    "gbp_mac_project", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel", "gbp_plan_check_level_kernels",
+    "gbp_mac_project", "gbp_mac_get_fluxes", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel", "gbp_plan_check_level_kernels",
     "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc", "gbp_nodal_set_overset_mask",
     "gbp_mac_set_robin", "gbp_mac_set_eb", "gbp_average_down",
     "gbp_amr_create", "gbp_amr_destroy", "gbp_amr_set_options", "gbp_amr_device_bytes",
@@ -146,6 +146,7 @@ def load(path: str = LIB_PATH):
         "gbp_mac_set_beta": (i, [P, A4, A4, A4, d]),
         "gbp_mac_set_beta_from_density": (i, [P, A4, d]),
         "gbp_mac_project": (i, [P, A4, A4, A4, A4, i, ctypes.POINTER(Stats)]),
+        "gbp_mac_get_fluxes": (i, [P, A4, A4, A4, A4]),
         "gbp_apply_nodal_projection_host": (i, [P, P, P, d, P, P, d, i, ctypes.POINTER(Stats)]),
         "gbp_plan_time_kernel": (i, [P, i, i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "gbp_plan_check_level_kernels": (i, [P, ctypes.POINTER(ctypes.c_double)]),

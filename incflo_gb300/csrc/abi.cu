@@ -621,6 +621,27 @@ int gbp_mac_project(gbp_plan* p, gbp_array4* ux, gbp_array4* uy, gbp_array4* uz,
     return p->mac->project(u, phi, phi_guess, stats);
 }
 
+int gbp_mac_get_fluxes(gbp_plan* p, const gbp_array4* phi, gbp_array4* fx, gbp_array4* fy, gbp_array4* fz)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_mac_get_fluxes: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    gbp_array4* f[3] = {fx, fy, fz};
+    for (int d = 0; d < 3; ++d) {
+        int lo[3] = {0, 0, 0};
+        int hi[3] = {p->geom.n_cell[0] - 1, p->geom.n_cell[1] - 1, p->geom.n_cell[2] - 1};
+        hi[d] += 1;
+        if (!valid_array(f[d], 1) || !covers(f[d], lo, hi)) {
+            set_error("gbp_mac_get_fluxes: each flux array must cover its faces 0..n");
+            return GBP_BAD_ARG;
+        }
+    }
+    int rc = check_cells(p, phi, 1, "phi");
+    if (rc) return rc;
+    return p->mac->get_fluxes(*phi, f);
+}
+
 int gbp_apply_cc_projection(gbp_plan* p, gbp_array4* vel, const gbp_array4* vel_old, const gbp_array4* rho,
                             double rho0, gbp_array4* gp, gbp_array4* p_cc, gbp_array4* umac_x, gbp_array4* umac_y,
                             gbp_array4* umac_z, double time, double dt, double prev_dt, double scaling_factor,

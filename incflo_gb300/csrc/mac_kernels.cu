@@ -385,6 +385,21 @@ __global__ void __launch_bounds__(256) k_mac_correct(CellGeom g, int d, gbp_arra
     *up -= be * (phi[p] - phi[p - s]) / g.h[d];
 }
 
+// zero the faces 0..n (direction d) of a caller face array
+__global__ void __launch_bounds__(256) k_mac_zero_faces(CellGeom g, int d, gbp_array4 u)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int fn[3] = {g.n[0], g.n[1], g.n[2]};
+    fn[d] += 1;
+    const long long nxy = (long long)fn[0] * fn[1];
+    if (t >= nxy * fn[2]) return;
+    const int k = (int)(t / nxy);
+    const long long rem = t - (long long)k * nxy;
+    const int j = (int)(rem / fn[0]);
+    const int i = (int)(rem - (long long)j * fn[0]);
+    *a4p(u, i, j, k, 0) = 0.0;
+}
+
 __global__ void k_mac_load_phi(CellGeom g, gbp_array4 in, double* __restrict__ phi)
 {
     int i, j, k;
@@ -752,6 +767,11 @@ void mac_rhs(const CellGeom& g, const gbp_array4& ux, const gbp_array4& uy, cons
     if (eb) e = *eb;
     k_mac_rhs<<<nblk(ncell(g), 256), 256, 0, st>>>(g, ux, uy, uz, b, e);
 }
+void mac_zero_faces(const CellGeom& g, int d, const gbp_array4& u, cudaStream_t st)
+{
+    k_mac_zero_faces<<<nblk(nface(g, d), 256), 256, 0, st>>>(g, d, u);
+}
+
 void mac_correct(const CellGeom& g, int d, const gbp_array4& u, const double* beta, const double* phi,
                  cudaStream_t st, const double* ap)
 {

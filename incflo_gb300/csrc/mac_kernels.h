@@ -105,6 +105,7 @@ void mac_rhs(const CellGeom& g, const gbp_array4& ux, const gbp_array4& uy, cons
 void mac_correct(const CellGeom& g, int d, const gbp_array4& u, const double* beta, const double* phi,
                  cudaStream_t st, const double* ap = nullptr);
 void mac_load_phi(const CellGeom& g, const gbp_array4& in, double* phi, cudaStream_t st);
+void mac_zero_faces(const CellGeom& g, int d, const gbp_array4& u, cudaStream_t st);
 void mac_store_phi(const CellGeom& g, const gbp_array4& out, const double* phi, cudaStream_t st);
 // max |v| / (kap V) over the cells (kap == nullptr: kap = 1; cells with kap == 0 skipped)
 void mac_norm(const CellGeom& g, const double* v, unsigned long long* norm, cudaStream_t st,

@@ -943,6 +943,26 @@ int MacSolver::solve(bool have_guess, gbp_stats* stats)
     return status;
 }
 
+int MacSolver::get_fluxes(const gbp_array4& phi_in, gbp_array4* flux[3])
+{
+    if (!beta_ready || !robin_ready) {
+        set_error("mac get_fluxes: beta (and Robin data on Robin sides) must be set on the plan");
+        return GBP_BAD_ARG;
+    }
+    const MacLevel& l0 = L[0];
+    mac_load_phi(l0.g, phi_in, phi, st);
+    // the correction of project() applied to zero face values: 0 - beta grad phi
+    for (int d = 0; d < 3; ++d) mac_zero_faces(l0.g, d, *flux[d], st);
+    for (int d = 0; d < 3; ++d) mac_correct(l0.g, d, *flux[d], l0.b64[d], phi, st, eb.on ? eb.m.ap[d] : nullptr);
+    if (eb.on) {
+        const double* b[3] = {l0.b64[0], l0.b64[1], l0.b64[2]};
+        const double* a[3] = {eb.m.ap[0], eb.m.ap[1], eb.m.ap[2]};
+        eb_correct_u(l0.g, eb.faces, eb.nfaces, b, a, phi, flux, st);
+    }
+    GBP_CUDA(cudaGetLastError());
+    return GBP_OK;
+}
+
 int MacSolver::project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats)
 {
     if (!beta_ready || !robin_ready) {

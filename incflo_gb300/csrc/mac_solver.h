@@ -48,6 +48,9 @@ public:
     // Dirichlet sides, whose ghost cells hold the boundary values) is the initial guess and the result
     int abec_solve(const gbp_array4* rhs, gbp_array4* phi, gbp_stats* stats);
     int project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_stats* stats);
+    // MacProjector::getFluxes: flux[d] = -beta grad phi on the faces 0..n of direction d, the correction
+    // project() subtracts from umac (face centroids on cut faces), for a given phi (cells)
+    int get_fluxes(const gbp_array4& phi_in, gbp_array4* flux[3]);
     // for a solver that uses this operator as one block of a preconditioner (the tensor solve): the
     // finest level, and e += the inner V-cycles of A e = r from zero (r in the finest padded layout,
     // homogeneous boundaries; FP32 V-cycles on r * scale32 in the mixed form)

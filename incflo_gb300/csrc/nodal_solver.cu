@@ -1499,8 +1499,31 @@ int NodalSolver::check_level_kernels(double diff[4])
     const NodalLevel& l0 = L[0];
     const NodalLevel& l1 = L[1];
     const NodalGeom& g = l0.g;
-    float* A = reinterpret_cast<float*>(l0.t64);  // scratch: the FP64 arrays hold twice the FP32 count
-    float* C = reinterpret_cast<float*>(l0.r64);
+    // scratch of its own (a test hook may allocate): the plan's FP64 arrays must keep their zero padding
+    float *A = nullptr, *C = nullptr;
+    GBP_CUDA(cudaMalloc(&A, sizeof(float) * g.count));
+    if (cudaMalloc(&C, sizeof(float) * g.count) != cudaSuccess) {
+        cudaFree(A);
+        set_error("check_level_kernels: cudaMalloc failed");
+        return GBP_CUDA_ERROR;
+    }
+    int rc = check_level_kernels_on(A, C, diff);
+    cudaStreamSynchronize(st);
+    cudaFree(A);
+    cudaFree(C);
+    // leave the FP32 level arrays as a fresh plan has them (the next solve refills what it reads)
+    const size_t f0 = sizeof(float) * g.count, f1 = sizeof(float) * l1.g.count;
+    for (float* p : {l0.x32, l0.t32, l0.b32, l0.r32}) GBP_CUDA(cudaMemsetAsync(p, 0, f0, st));
+    for (float* p : {l1.x32, l1.b32, l1.r32}) GBP_CUDA(cudaMemsetAsync(p, 0, f1, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+int NodalSolver::check_level_kernels_on(float* A, float* C, double diff[4])
+{
+    const NodalLevel& l0 = L[0];
+    const NodalLevel& l1 = L[1];
+    const NodalGeom& g = l0.g;
     unsigned long long* dm = reinterpret_cast<unsigned long long*>(dscal + 4);
     auto compare = [&](const float* a, const float* ref, long long n, double* out) -> int {
         GBP_CUDA(cudaMemsetAsync(dm, 0, 2 * sizeof(unsigned long long), st));
@@ -1515,6 +1538,7 @@ int NodalSolver::check_level_kernels(double diff[4])
         return GBP_OK;
     };
     const size_t f0 = sizeof(float) * g.count, f1 = sizeof(float) * l1.g.count;
+    int rc = GBP_OK;
     GBP_CUDA(cudaMemsetAsync(derr, 0, sizeof(unsigned), st));
     // seeded inputs, so that residuals are of the size of their terms: x and the coarse correction
     // with their periodic aliases (as the level sweeps write them), b on the unique nodes only
@@ -1528,7 +1552,7 @@ int NodalSolver::check_level_kernels(double diff[4])
     GBP_CUDA(cudaMemsetAsync(l0.t32, 0, f0, st));
     GBP_CUDA(cudaMemsetAsync(A, 0, f0, st));
     nodal_jacobi<float>(g, l0.s32, l0.x32, l0.b32, l0.t32, omega_eff, false, st);
-    int rc = vsweep32(g, 0, l0.s32, l0.x32, l0.b32, A, (float)omega_eff, derr, st);
+    rc = vsweep32(g, 0, l0.s32, l0.x32, l0.b32, A, (float)omega_eff, derr, st);
     if (!rc) rc = compare(A, l0.t32, g.count, &diff[0]);
     // [1] residual
     if (!rc) {

@@ -122,6 +122,7 @@ public:
     // padded position for [0] Jacobi, [1] residual, [2] residual + restriction (coarse level), [3]
     // prolongation + Jacobi. Overwrites solver scratch (the next solve refills it).
     int check_level_kernels(double diff[4]);
+    int check_level_kernels_on(float* A, float* C, double diff[4]);
 
     // Learned warm start for zero-guess solves: the network runs on multigrid level `level` (its
     // prediction is prolonged to level 0 and scaled by the Galerkin factor x.b / x.Ax); mode 0 off,

@@ -50,8 +50,31 @@ namespace gbp {
 
 namespace {
 
-constexpr int kNS = 3;       // pipeline stages
+// Launch shape. Pipeline stages (TMA prefetch distance = stages - 1) for the plain sweeps (modes 0, 1)
+// and the transfer sweeps (modes 2, 3, which stage more per plane), resident CTAs per SM they are
+// compiled for, and the rows per CTA of 256-node rows.
+#ifndef GBP_VS_STAGES_PLAIN
+#define GBP_VS_STAGES_PLAIN 3
+#endif
+#ifndef GBP_VS_STAGES_XFER
+#define GBP_VS_STAGES_XFER 3
+#endif
+#ifndef GBP_VS_MINB_PLAIN
+#define GBP_VS_MINB_PLAIN 3
+#endif
+#ifndef GBP_VS_MINB_XFER
+#define GBP_VS_MINB_XFER 2
+#endif
+#ifndef GBP_VS_TY_256
+#define GBP_VS_TY_256 4
+#endif
 constexpr int kMaxTX = 128;  // threads per row: 4 * 128 = 512 nodes per row at most
+// CTA shapes: TY rows per CTA by the row width (TX threads of 4 nodes): 8 rows for rows of <= 128
+// nodes (TX <= 32), GBP_VS_TY_256 for <= 256 (TX <= 64), 2 for <= 512 (TX <= 128)
+template <int MODE>
+struct Stages {
+    static constexpr int N = MODE <= 1 ? GBP_VS_STAGES_PLAIN : GBP_VS_STAGES_XFER;
+};
 
 __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z,
                                             int w)
@@ -83,9 +106,10 @@ struct VsShape {
     static constexpr int SR = TYR + 1;     // sigma cell rows: first node row - 1 .. last
     static constexpr int BR = TYR;         // b rows
     static constexpr int CR = TY / 2 + 3;  // coarse rows (mode 3)
-    // scratch rows: mode 2 the residual rows, mode 3 the blended coarse rows
-    static constexpr int RR = MODE == 2 ? TYR : (MODE == 3 ? XR : 0);
-    static constexpr int MAXT = TY == 8 ? 288 : 640;  // launch bound (TX <= 32 with TY 8, <= 128 with 4)
+    // scratch rows: mode 2 the residual rows of two planes (the restriction of a plane runs one step later)
+    static constexpr int RR = MODE == 2 ? 2 * TYR : 0;
+    // resident CTAs per SM the kernel is compiled for (launch bounds)
+    static constexpr int MINB = MODE <= 1 ? GBP_VS_MINB_PLAIN : (MODE == 2 ? GBP_VS_MINB_XFER : GBP_VS_MINB_PLAIN);
 };
 
 __host__ __device__ constexpr int al128(int b) { return (b + 127) / 128 * 128; }
@@ -121,23 +145,33 @@ __host__ __device__ inline StageLayout stage_layout(int rowlen, int crowlen)
 template <int MODE, int TY>
 inline int smem_bytes(int rowlen, int crowlen, int rstride)
 {
-    return kNS * stage_layout<MODE, TY>(rowlen, crowlen).bytes + VsShape<MODE, TY>::RR * rstride * 4;
+    return Stages<MODE>::N * stage_layout<MODE, TY>(rowlen, crowlen).bytes + VsShape<MODE, TY>::RR * rstride * 4;
 }
 
 // positions below -1 do not exist in the padded layout; periodic ones map to their alias
 __device__ __forceinline__ int wrapz(const NodalGeom& g, int p) { return (p < -1 && g.per[2]) ? p + g.n[2] : p; }
 
 // Store the 4 node values of a thread with the periodic aliases of x (node 0 -> n, 1 -> n+1,
-// n-1 -> -1), y and z.
+// n-1 -> -1), y and z. Away from the periodic seams (all but a few rows and planes): one vector store.
 __device__ __forceinline__ void store4(float* out, const NodalGeom& g, int i0, int j, int k, const float (&v)[4],
                                        int nact)
 {
-    int ys[3], zs[3];
-    const int ny = node_aliases(j, g.n[1], g.per[1], ys);
-    const int nz = node_aliases(k, g.n[2], g.per[2], zs);
-    for (int c = 0; c < nz; ++c)
-        for (int b = 0; b < ny; ++b) {
-            float* row = out + pidx(g.sy, g.sz, 0, ys[b], zs[c]);
+    const bool ax = g.per[0] && (i0 == 0 || i0 + 3 == g.n[0] - 1);
+    const bool ay = g.per[1] && (j <= 1 || j == g.n[1] - 1);
+    const bool az = g.per[2] && (k <= 1 || k == g.n[2] - 1);
+    if (!(ax || ay || az) && nact == 4) {
+        *reinterpret_cast<float4*>(out + pidx(g.sy, g.sz, i0, j, k)) = make_float4(v[0], v[1], v[2], v[3]);
+        return;
+    }
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        const int kk = node_alias_cand(k, g.n[2], g.per[2], c);
+        if (kk == kNoAlias) continue;
+#pragma unroll 1
+        for (int b = 0; b < 4; ++b) {
+            const int jj = node_alias_cand(j, g.n[1], g.per[1], b);
+            if (jj == kNoAlias) continue;
+            float* row = out + pidx(g.sy, g.sz, 0, jj, kk);
             if (nact == 4) {
                 *reinterpret_cast<float4*>(row + i0) = make_float4(v[0], v[1], v[2], v[3]);
             } else {
@@ -151,6 +185,7 @@ __device__ __forceinline__ void store4(float* out, const NodalGeom& g, int i0, i
                 if (i0 + 3 == g.n[0] - 1) row[-1] = v[3];
             }
         }
+    }
 }
 
 // Approximate reciprocal (one MUFU operation): the Jacobi smoother only scales its update by it.
@@ -166,24 +201,25 @@ __device__ __forceinline__ float rcp_approx(float d)
 __device__ __forceinline__ float layer_side(const float (&A)[3][6], const float (&B)[3][6], const float (&S)[2][5],
                                             const float (&SY)[5], const float (&SX)[2][4], int q)
 {
+    // two partial sums (rows below / above the node): two independent chains of four
     const float c = A[1][q + 1];
-    float t = S[0][q] * ((A[0][q] - c) + (B[0][q] - c));
-    t = fmaf(S[0][q + 1], (A[0][q + 2] - c) + (B[0][q + 2] - c), t);
-    t = fmaf(S[1][q], (A[2][q] - c) + (B[2][q] - c), t);
-    t = fmaf(S[1][q + 1], (A[2][q + 2] - c) + (B[2][q + 2] - c), t);
-    t = fmaf(SY[q], B[1][q] - c, t);
-    t = fmaf(SY[q + 1], B[1][q + 2] - c, t);
-    t = fmaf(SX[0][q], B[0][q + 1] - c, t);
-    t = fmaf(SX[1][q], B[2][q + 1] - c, t);
-    return t;
+    float t0 = S[0][q] * ((A[0][q] - c) + (B[0][q] - c));
+    float t1 = S[1][q] * ((A[2][q] - c) + (B[2][q] - c));
+    t0 = fmaf(S[0][q + 1], (A[0][q + 2] - c) + (B[0][q + 2] - c), t0);
+    t1 = fmaf(S[1][q + 1], (A[2][q + 2] - c) + (B[2][q + 2] - c), t1);
+    t0 = fmaf(SY[q], B[1][q] - c, t0);
+    t1 = fmaf(SY[q + 1], B[1][q + 2] - c, t1);
+    t0 = fmaf(SX[0][q], B[0][q + 1] - c, t0);
+    t1 = fmaf(SX[1][q], B[2][q + 1] - c, t1);
+    return t0 + t1;
 }
 
 // MODE 0: Jacobi  out = x + omega (b - A x) / diag(A)
 // MODE 1: residual out = b - A x
 // MODE 2: residual + restriction: out (the coarse b) = full weighting of b - A x
 // MODE 3: prolongation + Jacobi: x' = x + P e (e = the coarse correction), out = x' + omega (b - A x') / diag
-template <int MODE, int TY>
-__global__ void __launch_bounds__(VsShape<MODE, TY>::MAXT)
+template <int MODE, int TY, int TXM>
+__global__ void __launch_bounds__(TXM * VsShape<MODE, TY>::TYR, VsShape<MODE, TY>::MINB)
     k_vsweep32(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
                const __grid_constant__ CUtensorMap mb, const __grid_constant__ CUtensorMap mc,
                const __grid_constant__ CUtensorMap mx1, const __grid_constant__ CUtensorMap ms1,
@@ -191,11 +227,12 @@ __global__ void __launch_bounds__(VsShape<MODE, TY>::MAXT)
 {
     using Sh = VsShape<MODE, TY>;
     extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int kNS = Stages<MODE>::N;
     __shared__ uint64_t bar[kNS];
     __shared__ int abort_flag;
     const NodalGeom& g = a.g;
     const StageLayout L = stage_layout<MODE, TY>(a.rowlen, a.crowlen);
-    float* R = reinterpret_cast<float*>(smem + kNS * L.bytes);  // scratch rows (modes 2, 3)
+    float* R = reinterpret_cast<float*>(smem + kNS * L.bytes);  // mode 2: residual rows of two planes
 
     const int t = threadIdx.x, jr = threadIdx.y;
     const int TX = blockDim.x;
@@ -274,35 +311,65 @@ __global__ void __launch_bounds__(VsShape<MODE, TY>::MAXT)
 #pragma unroll
     for (int q = 0; q < 4; ++q) acc[q] = ss[q] = 0.f;
 
+    // Mode 2: restrict residual plane k (staged in scratch buffer rb): x and y full weighting of the
+    // thread's coarse row, z weights carried in registers; a coarse plane is stored once complete.
+    auto restrict_plane = [&](int k, int rb) {
+        if (MODE != 2 || cJ < 0) return;
+        // coarse (2t, cJ), (2t+1, cJ): fine x 4t-1 .. 4t+3 of scratch rows 2 jr .. 2 jr + 2
+        float c2[2] = {0.f, 0.f};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const float* rr = R + (rb * Sh::TYR + 2 * jr + r) * a.rstride + 3 + i0;
+            const float w = r == 1 ? 1.f : 0.5f;
+            const float x0 = rr[0], x1 = rr[1], x2 = rr[2], x3 = rr[3], x4 = rr[4];
+            c2[0] = fmaf(w, fmaf(0.5f, x0 + x2, x1), c2[0]);
+            c2[1] = fmaf(w, fmaf(0.5f, x2 + x4, x3), c2[1]);
+        }
+        int Kst = -1;
+        float o0 = 0.f, o1 = 0.f;
+        if (k & 1) {
+            // an odd plane completes coarse plane (k-1)/2, unless it is the chunk's extra plane
+            if (k > kfirst) {
+                Kst = (k - 1) >> 1;
+                o0 = carry0 + 0.5f * c2[0];
+                o1 = carry1 + 0.5f * c2[1];
+            }
+            carry0 = 0.5f * c2[0];
+            carry1 = 0.5f * c2[1];
+        } else {
+            carry0 += c2[0];
+            carry1 += c2[1];
+            if (!g.per[2] && k == g.nu[2] - 1) {  // the last plane of a non-periodic direction
+                Kst = k >> 1;
+                o0 = carry0;
+                o1 = carry1;
+            }
+        }
+        if (Kst >= 0 && cJ < a.gc.nu[1] && Kst < a.gc.nu[2]) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int I = 2 * t + h;
+                if (I < a.gc.nu[0])
+                    a.out[pidx(a.gc.sy, a.gc.sz, I, cJ, Kst)] =
+                        node_is_dirichlet(a.gc, I, cJ, Kst) ? 0.f : (h ? o1 : o0);
+            }
+        }
+    };
+
+    // consumer position in the ring: the stage of step s and its mbarrier phase parity
+    int cslot = 0;
+    uint32_t cphase = 0;
     // One z step: Bn receives plane P (prolongated in mode 3); Ao holds plane P-1.
     auto step = [&](int s, const float (&Ao)[3][6], float (&Bn)[3][6]) {
-        const unsigned char* base = smem + (s % kNS) * L.bytes;
-        if (!mbar_wait_bounded(&bar[s % kNS], (uint32_t)((s / kNS) & 1), a.err)) abort_flag = 1;
-        const int P = kfirst - 1 + s;
-        if (MODE == 3) {
-            // blend the two coarse planes in z and the coarse rows in y, for every staged fine row
-            const float* C0 = reinterpret_cast<const float*>(base + L.co);
-            const float* C1 = reinterpret_cast<const float*>(base + L.co1);
-            const int oz = P & 1;
-            const int J0 = (y0 - 1) >> 1;
-            const int cend = 2 * TX + 7;  // coarse nodes -1 .. 2TX+2 at positions 3 .. 2TX+6
-            for (int r = jr; r < Sh::XR; r += Sh::TYR) {
-                const int jf = y0 - 1 + r;
-                const float* c0 = C0 + ((jf >> 1) - J0) * a.crowlen;
-                const float* c1 = C1 + ((jf >> 1) - J0) * a.crowlen;
-                const int oj = (jf & 1) * a.crowlen;
-                float* dst = R + r * a.rstride;
-                for (int cc = 3 + t; cc < cend; cc += TX) {
-                    float v0 = c0[cc], v1 = c0[cc + oj];
-                    if (oz) {
-                        v0 = 0.5f * (v0 + c1[cc]);
-                        v1 = 0.5f * (v1 + c1[cc + oj]);
-                    }
-                    dst[cc] = 0.5f * (v0 + v1);  // oj = 0: v1 == v0
-                }
-            }
-            __syncthreads();
+        const unsigned char* base = smem + cslot * L.bytes;
+        if (!mbar_wait_bounded(&bar[cslot], cphase, a.err)) abort_flag = 1;
+        if (++cslot == kNS) {
+            cslot = 0;
+            cphase ^= 1u;
         }
+        const int P = kfirst - 1 + s;
+        // the residual plane staged at the previous step (its rows are complete: a barrier lies between)
+        if (MODE == 2 && s >= 3) restrict_plane(P - 2, (s - 1) & 1);
         // staged row r of an array: mode 2 keeps row 0 (the row below the tile) in its own area
         auto srow = [&](int area, int main, int r) -> const float* {
             if (MODE == 2)
@@ -323,11 +390,32 @@ __global__ void __launch_bounds__(VsShape<MODE, TY>::MAXT)
             Bn[r][5] = row[5];
         }
         if (MODE == 3) {
-            // x' = x + P e: fine node i0-1+c from the blended coarse nodes 2t-1 .. 2t+2
+            // x' = x + P e. The thread's fine rows j-1 .. j+1 lie between coarse rows jc .. jc+2
+            // (jc = (j-1) >> 1); their coarse nodes 2t-1 .. 2t+2 sit at positions 2t+3 .. 2t+6. Blend the
+            // two staged coarse planes in z (odd P), then the coarse rows in y (odd fine rows), then x.
+            const float* C0 = reinterpret_cast<const float*>(base + L.co);
+            const float* C1 = reinterpret_cast<const float*>(base + L.co1);
+            const int cr = ((j - 1) >> 1) - ((y0 - 1) >> 1);
+            const bool oz = P & 1;
+            float Cz[3][4];
+#pragma unroll
+            for (int rr = 0; rr < 3; ++rr) {
+                const float* p0 = C0 + (cr + rr) * a.crowlen + 2 * t + 3;
+                const float* p1 = C1 + (cr + rr) * a.crowlen + 2 * t + 3;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) Cz[rr][c] = oz ? 0.5f * (p0[c] + p1[c]) : p0[c];
+            }
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
-                const float* cy = R + (jr + r) * a.rstride + 2 * t + 3;
-                const float c0 = cy[0], c1 = cy[1], c2 = cy[2], c3 = cy[3];
+                const int jf = j - 1 + r;
+                const int b0 = (jf >> 1) - ((j - 1) >> 1);  // 0 or 1
+                const bool oj = jf & 1;
+                float cyv[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    cyv[c] = oj ? 0.5f * ((b0 ? Cz[1][c] : Cz[0][c]) + (b0 ? Cz[2][c] : Cz[1][c]))
+                                : (b0 ? Cz[1][c] : Cz[0][c]);
+                const float c0 = cyv[0], c1 = cyv[1], c2 = cyv[2], c3 = cyv[3];
                 Bn[r][0] += 0.5f * (c0 + c1);
                 Bn[r][1] += c1;
                 Bn[r][2] += 0.5f * (c1 + c2);
@@ -374,52 +462,10 @@ __global__ void __launch_bounds__(VsShape<MODE, TY>::MAXT)
                 v[q] = (dxy[q] || dk) ? 0.f : val;
             }
             if (MODE == 2) {
-                // stage the residual row (the x restriction needs the neighbours of other threads)
-                float* Rr = R + jr * a.rstride;
+                // stage the residual row; the plane is restricted at the next step, after its barrier
+                float* Rr = R + ((s & 1) * Sh::TYR + jr) * a.rstride;
                 *reinterpret_cast<float4*>(Rr + 4 + i0) = make_float4(v[0], v[1], v[2], v[3]);
                 if (t == TX - 1) Rr[3] = g.per[0] ? v[3] : 0.f;  // node -1 (periodic: n-1 = 4 TX - 1)
-                __syncthreads();
-                if (cJ >= 0) {
-                    // coarse (2t, cJ), (2t+1, cJ): fine x 4t-1 .. 4t+3 of scratch rows 2 jr .. 2 jr + 2
-                    float c2[2] = {0.f, 0.f};
-#pragma unroll
-                    for (int r = 0; r < 3; ++r) {
-                        const float* rr = R + (2 * jr + r) * a.rstride + 3 + i0;
-                        const float w = r == 1 ? 1.f : 0.5f;
-                        const float x0 = rr[0], x1 = rr[1], x2 = rr[2], x3 = rr[3], x4 = rr[4];
-                        c2[0] = fmaf(w, fmaf(0.5f, x0 + x2, x1), c2[0]);
-                        c2[1] = fmaf(w, fmaf(0.5f, x2 + x4, x3), c2[1]);
-                    }
-                    int Kst = -1;
-                    float o0 = 0.f, o1 = 0.f;
-                    if (k & 1) {
-                        // an odd plane completes coarse plane (k-1)/2, unless it is the chunk's extra plane
-                        if (k > kfirst) {
-                            Kst = (k - 1) >> 1;
-                            o0 = carry0 + 0.5f * c2[0];
-                            o1 = carry1 + 0.5f * c2[1];
-                        }
-                        carry0 = 0.5f * c2[0];
-                        carry1 = 0.5f * c2[1];
-                    } else {
-                        carry0 += c2[0];
-                        carry1 += c2[1];
-                        if (!g.per[2] && k == g.nu[2] - 1) {  // the last plane of a non-periodic direction
-                            Kst = k >> 1;
-                            o0 = carry0;
-                            o1 = carry1;
-                        }
-                    }
-                    if (Kst >= 0 && cJ < a.gc.nu[1] && Kst < a.gc.nu[2]) {
-#pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const int I = 2 * t + h;
-                            if (I < a.gc.nu[0])
-                                a.out[pidx(a.gc.sy, a.gc.sz, I, cJ, Kst)] =
-                                    node_is_dirichlet(a.gc, I, cJ, Kst) ? 0.f : (h ? o1 : o0);
-                        }
-                    }
-                }
             } else if (j < g.nu[1] && nact > 0) {
                 store4(a.out, g, i0, j, k, v, nact);
             }
@@ -458,6 +504,7 @@ __global__ void __launch_bounds__(VsShape<MODE, TY>::MAXT)
         consumed = s + 2;
     }
     __syncthreads();
+    if (MODE == 2 && !abort_flag && nsteps >= 3) restrict_plane(kend - 1, (nsteps - 1) & 1);
     if (abort_flag && tid == 0) {
         // copies still in flight: steps consumed .. issued-1 (bounded waits)
         for (uint32_t s = (uint32_t)consumed; s < issued; ++s)
@@ -527,7 +574,7 @@ int make_map4(const void* base, long long sy, long long sz, long long count, int
     return GBP_OK;
 }
 
-template <int MODE, int TY>
+template <int MODE, int TY, int TXM>
 int launch(const NodalGeom& g, const NodalGeom* gc, const float* s, const float* x, const float* b,
            const float* e, float* out, float omega, unsigned* err, cudaStream_t st)
 {
@@ -542,7 +589,7 @@ int launch(const NodalGeom& g, const NodalGeom* gc, const float* s, const float*
     a.omega = omega;
     a.rowlen = (int)g.sy;
     a.crowlen = gc ? (int)gc->sy : 4;
-    a.rstride = MODE == 2 ? 4 * TX + 8 : 2 * TX + 8;
+    a.rstride = 4 * TX + 8;
     a.err = err;
     // mode 2 stages the row below the tile through one-row maps (x1, s1, b1)
     CUtensorMap mx, ms, mb, mc, mx1, ms1, mb1;
@@ -558,10 +605,11 @@ int launch(const NodalGeom& g, const NodalGeom* gc, const float* s, const float*
     if (MODE != 3) mc = mb;
     if (MODE != 2) mx1 = mx, ms1 = ms, mb1 = mb;
     const int smem = smem_bytes<MODE, TY>(a.rowlen, a.crowlen, a.rstride);
-    auto kern = k_vsweep32<MODE, TY>;
+    auto kern = k_vsweep32<MODE, TY, TXM>;
     static int configured = 0, resident = 1;
     if (configured < smem) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         int r = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, TX * Sh::TYR, smem) == cudaSuccess && r > 0)
             resident = r;
@@ -571,7 +619,7 @@ int launch(const NodalGeom& g, const NodalGeom* gc, const float* s, const float*
     // z chunks: whole waves of resident CTAs; an even chunk length in mode 2 (the restriction pairs planes)
     int nz = sweep_z_chunks(g, ty, resident);
     int kchunk = (g.nu[2] + nz - 1) / nz;
-    if (MODE == 2 && (kchunk & 1)) ++kchunk;
+    if ((MODE == 2 || MODE == 3) && (kchunk & 1)) ++kchunk;
     a.kchunk = kchunk;
     dim3 grid(1, ty, (g.nu[2] + kchunk - 1) / kchunk);
     kern<<<grid, dim3(TX, Sh::TYR), smem, st>>>(mx, ms, mb, mc, mx1, ms1, mb1, a);
@@ -606,30 +654,34 @@ bool vsweep32_transfer_supported(const NodalGeom& g, const NodalGeom& gc)
            2 * TX + 7 <= (int)gc.sy;
 }
 
-static inline bool wide(const NodalGeom& g) { return (g.nu[0] + 3) / 4 > 32; }
+// rows per CTA by the row width: 8 (<= 128 nodes), GBP_VS_TY_256 (<= 256), 2 (<= 512)
+template <int MODE>
+static int launch_any(const NodalGeom& g, const NodalGeom* gc, const float* s, const float* x, const float* b,
+                      const float* e, float* out, float omega, unsigned* err, cudaStream_t st)
+{
+    const int TX = (g.nu[0] + 3) / 4;
+    if (TX <= 32) return launch<MODE, 8, 32>(g, gc, s, x, b, e, out, omega, err, st);
+    if (TX <= 64) return launch<MODE, GBP_VS_TY_256, 64>(g, gc, s, x, b, e, out, omega, err, st);
+    return launch<MODE, 2, 128>(g, gc, s, x, b, e, out, omega, err, st);
+}
 
 int vsweep32(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
              unsigned* err, cudaStream_t st)
 {
-    if (mode == 0)
-        return wide(g) ? launch<0, 4>(g, nullptr, s, x, b, nullptr, out, omega, err, st)
-                       : launch<0, 8>(g, nullptr, s, x, b, nullptr, out, omega, err, st);
-    return wide(g) ? launch<1, 4>(g, nullptr, s, x, b, nullptr, out, omega, err, st)
-                   : launch<1, 8>(g, nullptr, s, x, b, nullptr, out, omega, err, st);
+    return mode == 0 ? launch_any<0>(g, nullptr, s, x, b, nullptr, out, omega, err, st)
+                     : launch_any<1>(g, nullptr, s, x, b, nullptr, out, omega, err, st);
 }
 
 int vsweep32_resid_restrict(const NodalGeom& g, const NodalGeom& gc, const float* s, const float* x, const float* b,
                             float* bc, unsigned* err, cudaStream_t st)
 {
-    return wide(g) ? launch<2, 4>(g, &gc, s, x, b, nullptr, bc, 0.f, err, st)
-                   : launch<2, 8>(g, &gc, s, x, b, nullptr, bc, 0.f, err, st);
+    return launch_any<2>(g, &gc, s, x, b, nullptr, bc, 0.f, err, st);
 }
 
 int vsweep32_prolong_jacobi(const NodalGeom& g, const NodalGeom& gc, const float* s, const float* x, const float* ec,
                             const float* b, float* out, float omega, unsigned* err, cudaStream_t st)
 {
-    return wide(g) ? launch<3, 4>(g, &gc, s, x, b, ec, out, omega, err, st)
-                   : launch<3, 8>(g, &gc, s, x, b, ec, out, omega, err, st);
+    return launch_any<3>(g, &gc, s, x, b, ec, out, omega, err, st);
 }
 
 void vsweep32_forget_maps(const void* pool_base, size_t pool_bytes)

@@ -556,3 +556,12 @@ class MacProjector:
                                          int(phi is not None and phi_guess), ctypes.byref(st)), "gbp_mac_project")
         self.stats = st.as_dict()
         return self.stats
+
+    def getFluxes(self, fluxes, phi, ng_phi=0):  # noqa: N802 (reference name)
+        """MacProjector::getFluxes(fluxes, phi, loc): fluxes[d] = -beta grad phi on the faces of
+        direction d (face centroids of cut faces), the correction project() applies to umac."""
+        self._ensure()
+        f = [array4(x) for x in fluxes]
+        A.check(A.load().gbp_mac_get_fluxes(self.plan.ptr, _ref(array4(phi, ng_phi)), _ref(f[0]), _ref(f[1]),
+                                            _ref(f[2])), "gbp_mac_get_fluxes")
+        return fluxes

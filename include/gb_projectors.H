@@ -231,6 +231,13 @@ public:
     }
     gbp_stats project(double rtol, double atol) { return run(nullptr, rtol, atol); }
     gbp_stats project(gbp_array4 phi, double rtol, double atol) { return run(&phi, rtol, atol); }
+    // MacProjector::getFluxes(fluxes, phi, loc): fluxes[d] = -beta grad phi on the faces (face centroids
+    // of cut faces), the correction project() applied to umac
+    void getFluxes(gbp_array4 fluxes[3], const gbp_array4& phi)
+    {
+        if (!plan_) throw Error(GBP_BAD_ARG, "MacProjector::getFluxes before setDomainBC");
+        check(gbp_mac_get_fluxes(plan_.get(), &phi, &fluxes[0], &fluxes[1], &fluxes[2]), "gbp_mac_get_fluxes");
+    }
     gbp_options& options() { return opt_; }
 
 private:

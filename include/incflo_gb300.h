@@ -244,6 +244,15 @@ int gbp_mac_set_beta_from_density(gbp_plan* plan, const gbp_array4* rho, double 
 int gbp_mac_project(gbp_plan* plan, gbp_array4* umac_x, gbp_array4* umac_y, gbp_array4* umac_z,
                     gbp_array4* phi, int phi_guess, gbp_stats* stats);
 
+/* MacProjector::getFluxes(fluxes, phi, Location::FaceCenter / FaceCentroid)
+ * (src/projection/incflo_apply_cc_projection.cpp:383-390): flux_d = -beta grad phi on the faces
+ * 0..n of direction d ("MINUS (dt/rho) Gphi"), with the plan's boundary types (Dirichlet faces through
+ * the zero boundary value, Neumann faces 0) and, with cut cells, the face-centroid gradient of cut
+ * faces: exactly the correction gbp_mac_project subtracts from umac. phi: cells 0..n-1. Asynchronous
+ * on the plan's stream. */
+int gbp_mac_get_fluxes(gbp_plan* plan, const gbp_array4* phi, gbp_array4* flux_x, gbp_array4* flux_y,
+                       gbp_array4* flux_z);
+
 /* ---- cell-centred ABecLaplacian solve (scalar diffusion) ---------------------------------
  * The implicit scalar diffusion of DiffusionScalarOp::diffuse_scalar
  * (src/diffusion/DiffusionScalarOp.cpp:150-327): MLABecLaplacian alpha a phi - beta div(b grad phi) =

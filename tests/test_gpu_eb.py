@@ -99,3 +99,19 @@ def test_eb_rejects_inconsistent_geometry(gpu_lib):
     bad["vfrac"] = v
     with pytest.raises(Exception):
         _gpu_projector(n, ext, bclo, bchi, bad, beta, "fp64")._ensure()
+
+
+def test_eb_get_fluxes_are_the_projection_correction(gpu_lib):
+    """getFluxes with cut cells (Location::FaceCentroid): the correction the cut-cell projection applied."""
+    n, ext, bclo, bchi, geo, beta, umac, m = _case("channel")
+    mp = _gpu_projector(n, ext, bclo, bchi, geo, beta, "fp64")
+    ut = [cuda(u) for u in umac]
+    mp.setUMAC(ut)
+    phi = cuda(np.zeros((n[2], n[1], n[0])))
+    st = mp.project(rtol=1e-12, atol=0.0, phi=phi, phi_guess=False)
+    assert st["status"] == 0
+    flux = [cuda(np.zeros(u.shape)) for u in umac]
+    mp.getFluxes(flux, phi)
+    for d in range(3):
+        corr = ut[d].cpu().numpy() - umac[d]
+        np.testing.assert_allclose(flux[d].cpu().numpy(), corr, rtol=0, atol=1e-13 * max(np.abs(corr).max(), 1e-300))

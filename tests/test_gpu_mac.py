@@ -139,3 +139,31 @@ def test_mac_all_neumann_inconsistent_rhs(gpu_lib, precision):
     assert rel_l2(phi.cpu().numpy(), phi_or) <= 1e-9
     for d in range(3):
         np.testing.assert_allclose(ut[d].cpu().numpy(), un_or[d], rtol=0, atol=1e-9 * np.abs(un_or[d]).max())
+
+
+@pytest.mark.parametrize("case", [CASES[1], CASES[4]], ids=["dirichlet-inflow", "periodic-walls"])
+def test_get_fluxes_are_the_projection_correction(gpu_lib, case):
+    """MacProjector::getFluxes(fluxes, phi) = -beta grad phi on every face: against the oracle's
+    correction (u_projected - u) from the same solve, and against the GPU's own correction."""
+    n, ext, bclo, bchi = case
+    g = O.Grid(n, hi=ext, bclo=bclo, bchi=bchi)
+    rng = np.random.default_rng(5)
+    beta = [np.abs(b) + 0.2 for b in face_fields(g, rng, zero_neumann=False)]
+    umac = face_fields(g, rng)
+    un_or, phi_or, st_or = O.mac_project(g, beta, umac, rtol=1e-13)
+    ut = [cuda(u) for u in umac]
+    mp = MacProjector(Geometry(n, (0, 0, 0), ext), options=make_options(1, precision="fp64"))
+    mp.initProjector(beta=[cuda(b) for b in beta])
+    mp.setDomainBC(bclo, bchi)
+    mp.setUMAC(ut)
+    phi = cuda(np.zeros(g.cell_shape))
+    st = mp.project(rtol=1e-12, atol=0.0, phi=phi, phi_guess=False)
+    assert st["status"] == 0
+    flux = [cuda(np.full(u.shape, np.nan)) for u in umac]
+    mp.getFluxes(flux, phi)
+    for d in range(3):
+        got = flux[d].cpu().numpy()
+        ref = un_or[d] - umac[d]
+        scale = max(np.abs(ref).max(), 1e-300)
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9 * scale)
+        np.testing.assert_allclose(got, ut[d].cpu().numpy() - umac[d], rtol=0, atol=1e-13 * scale)
