@@ -6,7 +6,9 @@
 // (the solve behind incflo::ApplyNodalProjection, src/projection/incflo_apply_nodal_projection.cpp:215).
 //
 // Tiling. A CTA owns whole x rows (the full padded row, node i at position i + 4) of TY node rows and
-// marches up a chunk of z planes; each thread owns 4 consecutive nodes of one row. Per z step one
+// marches up a chunk of z planes; each thread owns 4 consecutive nodes of RPT rows (2: the loads of
+// the x window and the sigma pair sums are shared by 8 nodes, and the per-step overhead by twice as
+// many nodes). Per z step one
 // elected thread loads by TMA the next x plane with one halo row on each side, the sigma cell layer
 // below it and a b plane into a 3-slot ring of mbarrier-tracked stages. The tensor maps are 4-D
 // ({bw, nbx, rows, planes} with bw * nbx = the padded row length) so that one box holds whole rows
@@ -19,7 +21,10 @@
 //   sum over the 4 cells (a, b) of sigma_ab [(x_inplane_diag - x_c) + (x_body_diag - x_c)]
 //   + sum over x sides (sigma pair along y) (x_xz_diag - x_c) + sum over y sides (sigma pair along x) (x_yz_diag - x_c),
 // differences to the centre (FP32 rounding scales with the local variation of x), times K3; the
-// diagonal is K0 times the sum of the 8 cell sigmas.
+// diagonal is K0 times the sum of the 8 cell sigmas. The in-plane and body-diagonal terms of the node
+// below a layer (centre c_A) and of the node above it (centre c_B) share their cells and corner values:
+//   G_B = G_A - 2 (c_B - c_A) sum_layer(sigma),
+// so the second costs one FMA; both are sums of local differences, so the rounding stays local.
 //
 // Restriction (mode 2). The CTA computes the residual of node rows y0-1 .. y0+TY-1 (one row more than
 // it owns: coarse row y0/2 needs fine rows y0-1 .. y0+1), stages each residual plane in shared memory,
@@ -51,22 +56,22 @@ namespace gbp {
 namespace {
 
 // Launch shape. Pipeline stages (TMA prefetch distance = stages - 1) for the plain sweeps (modes 0, 1)
-// and the transfer sweeps (modes 2, 3, which stage more per plane), resident CTAs per SM they are
-// compiled for, and the rows per CTA of 256-node rows.
+// and the transfer sweeps (modes 2, 3, which stage more per plane), the resident threads per SM the
+// register budget is set for, the rows per CTA of 256-node rows and the node rows per thread.
 #ifndef GBP_VS_STAGES_PLAIN
 #define GBP_VS_STAGES_PLAIN 3
 #endif
 #ifndef GBP_VS_STAGES_XFER
 #define GBP_VS_STAGES_XFER 3
 #endif
-#ifndef GBP_VS_MINB_PLAIN
-#define GBP_VS_MINB_PLAIN 3
-#endif
-#ifndef GBP_VS_MINB_XFER
-#define GBP_VS_MINB_XFER 2
+#ifndef GBP_VS_THREADS_PER_SM
+#define GBP_VS_THREADS_PER_SM 512  // resident threads per SM the kernels are compiled for (registers)
 #endif
 #ifndef GBP_VS_TY_256
-#define GBP_VS_TY_256 4
+#define GBP_VS_TY_256 8
+#endif
+#ifndef GBP_VS_RPT
+#define GBP_VS_RPT 2  // node rows per thread
 #endif
 constexpr int kMaxTX = 128;  // threads per row: 4 * 128 = 512 nodes per row at most
 // CTA shapes: TY rows per CTA by the row width (TX threads of 4 nodes): 8 rows for rows of <= 128
@@ -98,18 +103,18 @@ struct VsArgs {
     unsigned* err;
 };
 
-template <int MODE, int TY>
+template <int MODE, int TY, int RPT>
 struct VsShape {
-    // node rows computed: y0 .. y0+TY-1; mode 2 also the row below, y0-1
-    static constexpr int TYR = MODE == 2 ? TY + 1 : TY;
+    // node rows computed: y0 .. y0+TY-1; mode 2 also the row below, y0-1 (the restriction of coarse row
+    // y0/2 needs fine rows y0-1 .. y0+1), rounded up to whole threads
+    static constexpr int TYR = ((MODE == 2 ? TY + 1 : TY) + RPT - 1) / RPT * RPT;
+    static constexpr int TTR = TYR / RPT;  // thread rows
     static constexpr int XR = TYR + 2;     // x rows staged: first node row - 1 .. last + 1
     static constexpr int SR = TYR + 1;     // sigma cell rows: first node row - 1 .. last
     static constexpr int BR = TYR;         // b rows
     static constexpr int CR = TY / 2 + 3;  // coarse rows (mode 3)
     // scratch rows: mode 2 the residual rows of two planes (the restriction of a plane runs one step later)
     static constexpr int RR = MODE == 2 ? 2 * TYR : 0;
-    // resident CTAs per SM the kernel is compiled for (launch bounds)
-    static constexpr int MINB = MODE <= 1 ? GBP_VS_MINB_PLAIN : (MODE == 2 ? GBP_VS_MINB_XFER : GBP_VS_MINB_PLAIN);
 };
 
 __host__ __device__ constexpr int al128(int b) { return (b + 127) / 128 * 128; }
@@ -121,10 +126,10 @@ struct StageLayout {
     uint32_t tx;  // transaction bytes per stage
 };
 
-template <int MODE, int TY>
+template <int MODE, int TY, int RPT>
 __host__ __device__ inline StageLayout stage_layout(int rowlen, int crowlen)
 {
-    using S = VsShape<MODE, TY>;
+    using S = VsShape<MODE, TY, RPT>;
     const int one = MODE == 2 ? al128(rowlen * 4) : 0;  // the one-row area
     const int sub = MODE == 2 ? 1 : 0;
     StageLayout L;
@@ -142,16 +147,17 @@ __host__ __device__ inline StageLayout stage_layout(int rowlen, int crowlen)
     return L;
 }
 
-template <int MODE, int TY>
+template <int MODE, int TY, int RPT>
 inline int smem_bytes(int rowlen, int crowlen, int rstride)
 {
-    return Stages<MODE>::N * stage_layout<MODE, TY>(rowlen, crowlen).bytes + VsShape<MODE, TY>::RR * rstride * 4;
+    return Stages<MODE>::N * stage_layout<MODE, TY, RPT>(rowlen, crowlen).bytes +
+           VsShape<MODE, TY, RPT>::RR * rstride * 4;
 }
 
 // positions below -1 do not exist in the padded layout; periodic ones map to their alias
 __device__ __forceinline__ int wrapz(const NodalGeom& g, int p) { return (p < -1 && g.per[2]) ? p + g.n[2] : p; }
 
-// Store the 4 node values of a thread with the periodic aliases of x (node 0 -> n, 1 -> n+1,
+// Store the 4 node values of a thread row with the periodic aliases of x (node 0 -> n, 1 -> n+1,
 // n-1 -> -1), y and z. Away from the periodic seams (all but a few rows and planes): one vector store.
 __device__ __forceinline__ void store4(float* out, const NodalGeom& g, int i0, int j, int k, const float (&v)[4],
                                        int nact)
@@ -196,47 +202,33 @@ __device__ __forceinline__ float rcp_approx(float d)
     return r;
 }
 
-// One layer-side: the contribution of the cell layer between planes A (the node's own) and B (the
-// other) to node q of the thread's 4 (window column q + 1), before the factor K3.
-__device__ __forceinline__ float layer_side(const float (&A)[3][6], const float (&B)[3][6], const float (&S)[2][5],
-                                            const float (&SY)[5], const float (&SX)[2][4], int q)
-{
-    // two partial sums (rows below / above the node): two independent chains of four
-    const float c = A[1][q + 1];
-    float t0 = S[0][q] * ((A[0][q] - c) + (B[0][q] - c));
-    float t1 = S[1][q] * ((A[2][q] - c) + (B[2][q] - c));
-    t0 = fmaf(S[0][q + 1], (A[0][q + 2] - c) + (B[0][q + 2] - c), t0);
-    t1 = fmaf(S[1][q + 1], (A[2][q + 2] - c) + (B[2][q + 2] - c), t1);
-    t0 = fmaf(SY[q], B[1][q] - c, t0);
-    t1 = fmaf(SY[q + 1], B[1][q + 2] - c, t1);
-    t0 = fmaf(SX[0][q], B[0][q + 1] - c, t0);
-    t1 = fmaf(SX[1][q], B[2][q + 1] - c, t1);
-    return t0 + t1;
-}
-
 // MODE 0: Jacobi  out = x + omega (b - A x) / diag(A)
 // MODE 1: residual out = b - A x
 // MODE 2: residual + restriction: out (the coarse b) = full weighting of b - A x
 // MODE 3: prolongation + Jacobi: x' = x + P e (e = the coarse correction), out = x' + omega (b - A x') / diag
-template <int MODE, int TY, int TXM>
-__global__ void __launch_bounds__(TXM * VsShape<MODE, TY>::TYR, VsShape<MODE, TY>::MINB)
+template <int MODE, int TY, int TXM, int RPT>
+__global__ void __launch_bounds__(TXM * VsShape<MODE, TY, RPT>::TTR,
+                                  GBP_VS_THREADS_PER_SM / (TXM * VsShape<MODE, TY, RPT>::TTR) > 0
+                                      ? GBP_VS_THREADS_PER_SM / (TXM * VsShape<MODE, TY, RPT>::TTR)
+                                      : 1)
     k_vsweep32(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap ms,
                const __grid_constant__ CUtensorMap mb, const __grid_constant__ CUtensorMap mc,
                const __grid_constant__ CUtensorMap mx1, const __grid_constant__ CUtensorMap ms1,
                const __grid_constant__ CUtensorMap mb1, VsArgs a)
 {
-    using Sh = VsShape<MODE, TY>;
-    extern __shared__ __align__(128) unsigned char smem[];
+    using Sh = VsShape<MODE, TY, RPT>;
     constexpr int kNS = Stages<MODE>::N;
+    constexpr int W = RPT + 2;  // x window rows of a thread
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t bar[kNS];
     __shared__ int abort_flag;
     const NodalGeom& g = a.g;
-    const StageLayout L = stage_layout<MODE, TY>(a.rowlen, a.crowlen);
+    const StageLayout L = stage_layout<MODE, TY, RPT>(a.rowlen, a.crowlen);
     float* R = reinterpret_cast<float*>(smem + kNS * L.bytes);  // mode 2: residual rows of two planes
 
     const int t = threadIdx.x, jr = threadIdx.y;
     const int TX = blockDim.x;
-    const int nthr = TX * Sh::TYR;
+    const int nthr = TX * Sh::TTR;
     const int tid = t + TX * jr;
     const int i0 = 4 * t;
     const int y0 = blockIdx.y * TY;
@@ -245,17 +237,20 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY>::TYR, VsShape<MODE, TY
     const int kfirst = MODE == 2 ? kbeg - 1 : kbeg;  // first node plane computed
     const int nsteps = kend - kfirst + 2;
     const int ybase = MODE == 2 ? y0 - 1 : y0;       // first node row computed
-    const int j = ybase + jr;
+    const int srow0 = RPT * jr;                      // staged row of the thread's first window row
+    const int j0 = ybase + srow0;                    // the thread's first node row
     // nodes of this thread that exist (mode 2: row -1 is the periodic alias of n-1, or zero)
     const int nact = max(0, min(4, g.nu[0] - i0));
-    const bool row_ok = j < g.nu[1];
-    bool dxy[4];
+    unsigned dmask = 0;  // bit r*4+q: node (q, row r) is Dirichlet or does not exist: its value is 0
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int i = i0 + q;
-        dxy[q] = (g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) ||
-                 (g.dhi[1] && j == g.n[1]) || q >= nact || !row_ok;
-    }
+    for (int r = 0; r < RPT; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int i = i0 + q, j = j0 + r;
+            if ((g.dlo[0] && i == 0) || (g.dhi[0] && i == g.n[0]) || (g.dlo[1] && j == 0) || (g.dhi[1] && j == g.n[1]) ||
+                q >= nact || j >= g.nu[1])
+                dmask |= 1u << (r * 4 + q);
+        }
     // mode 2: the coarse row this thread reduces, from the residual rows 2 jr .. 2 jr + 2 (fine rows
     // 2 cJ - 1 .. 2 cJ + 1)
     const int cJ = (MODE == 2 && jr < TY / 2) ? y0 / 2 + jr : -1;
@@ -282,8 +277,8 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY>::TYR, VsShape<MODE, TY
             tma_load_4d(base + L.ba, &mb1, br, 0, 0, yb + 1, pb + 1);
             tma_load_4d(base + L.bo, &mb, br, 0, 0, y0 + 1, pb + 1);
         } else {
-            tma_load_4d(base + L.xo, &mx, br, 0, 0, y0, zx);  // x rows y0-1 .. y0+TY (padded row y0)
-            tma_load_4d(base + L.so, &ms, br, 0, 0, y0, zs);  // sigma cell rows y0-1 .. y0+TY-1
+            tma_load_4d(base + L.xo, &mx, br, 0, 0, y0, zx);  // x rows y0-1 .. (padded row y0)
+            tma_load_4d(base + L.so, &ms, br, 0, 0, y0, zs);  // sigma cell rows y0-1 ..
             tma_load_4d(base + L.bo, &mb, br, 0, 0, y0 + 1, pb + 1);
         }
         if (MODE == 3) {
@@ -306,10 +301,12 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY>::TYR, VsShape<MODE, TY
     if (tid == 0)
         for (int s = 0; s < kNS - 1 && s < nsteps; ++s) issue(s);
 
-    float acc[4], ss[4];
+    float acc[RPT][4], ss[RPT][4];
     float carry0 = 0.f, carry1 = 0.f;  // mode 2: coarse nodes 2t, 2t+1 of coarse row cJ
 #pragma unroll
-    for (int q = 0; q < 4; ++q) acc[q] = ss[q] = 0.f;
+    for (int r = 0; r < RPT; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[r][q] = ss[r][q] = 0.f;
 
     // Mode 2: restrict residual plane k (staged in scratch buffer rb): x and y full weighting of the
     // thread's coarse row, z weights carried in registers; a coarse plane is stored once complete.
@@ -360,7 +357,7 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY>::TYR, VsShape<MODE, TY
     int cslot = 0;
     uint32_t cphase = 0;
     // One z step: Bn receives plane P (prolongated in mode 3); Ao holds plane P-1.
-    auto step = [&](int s, const float (&Ao)[3][6], float (&Bn)[3][6]) {
+    auto step = [&](int s, const float (&Ao)[W][6], float (&Bn)[W][6]) {
         const unsigned char* base = smem + cslot * L.bytes;
         if (!mbar_wait_bounded(&bar[cslot], cphase, a.err)) abort_flag = 1;
         if (++cslot == kNS) {
@@ -377,110 +374,144 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY>::TYR, VsShape<MODE, TY
                               : reinterpret_cast<const float*>(base + main) + (r - 1) * a.rowlen;
             return reinterpret_cast<const float*>(base + main) + r * a.rowlen;
         };
-        // plane P rows j-1, j, j+1 (staged rows jr .. jr+2), nodes i0-1 .. i0+4 (positions i0+3 .. i0+8)
+        // plane P, window rows j0-1 .. j0+RPT (staged rows srow0 ..), nodes i0-1 .. i0+4
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            const float* row = srow(L.xa, L.xo, jr + r) + i0 + 3;
-            Bn[r][0] = row[0];
+        for (int w = 0; w < W; ++w) {
+            const float* row = srow(L.xa, L.xo, srow0 + w) + i0 + 3;
+            Bn[w][0] = row[0];
             const float4 m = *reinterpret_cast<const float4*>(row + 1);
-            Bn[r][1] = m.x;
-            Bn[r][2] = m.y;
-            Bn[r][3] = m.z;
-            Bn[r][4] = m.w;
-            Bn[r][5] = row[5];
+            Bn[w][1] = m.x;
+            Bn[w][2] = m.y;
+            Bn[w][3] = m.z;
+            Bn[w][4] = m.w;
+            Bn[w][5] = row[5];
         }
         if (MODE == 3) {
-            // x' = x + P e. The thread's fine rows j-1 .. j+1 lie between coarse rows jc .. jc+2
-            // (jc = (j-1) >> 1); their coarse nodes 2t-1 .. 2t+2 sit at positions 2t+3 .. 2t+6. Blend the
+            // x' = x + P e. The window rows j0-1 .. j0+RPT lie between coarse rows jc .. jc+RPT
+            // (jc = (j0-1) >> 1); their coarse nodes 2t-1 .. 2t+2 sit at positions 2t+3 .. 2t+6. Blend the
             // two staged coarse planes in z (odd P), then the coarse rows in y (odd fine rows), then x.
             const float* C0 = reinterpret_cast<const float*>(base + L.co);
             const float* C1 = reinterpret_cast<const float*>(base + L.co1);
-            const int cr = ((j - 1) >> 1) - ((y0 - 1) >> 1);
+            const int cr = ((j0 - 1) >> 1) - ((y0 - 1) >> 1);
             const bool oz = P & 1;
-            float Cz[3][4];
+            float Cz[RPT + 1][4];
 #pragma unroll
-            for (int rr = 0; rr < 3; ++rr) {
+            for (int rr = 0; rr <= RPT; ++rr) {
                 const float* p0 = C0 + (cr + rr) * a.crowlen + 2 * t + 3;
                 const float* p1 = C1 + (cr + rr) * a.crowlen + 2 * t + 3;
 #pragma unroll
                 for (int c = 0; c < 4; ++c) Cz[rr][c] = oz ? 0.5f * (p0[c] + p1[c]) : p0[c];
             }
 #pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                const int jf = j - 1 + r;
-                const int b0 = (jf >> 1) - ((j - 1) >> 1);  // 0 or 1
+            for (int w = 0; w < W; ++w) {
+                const int jf = j0 - 1 + w;
+                const int b0 = (jf >> 1) - ((j0 - 1) >> 1);
                 const bool oj = jf & 1;
                 float cyv[4];
 #pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    cyv[c] = oj ? 0.5f * ((b0 ? Cz[1][c] : Cz[0][c]) + (b0 ? Cz[2][c] : Cz[1][c]))
-                                : (b0 ? Cz[1][c] : Cz[0][c]);
-                const float c0 = cyv[0], c1 = cyv[1], c2 = cyv[2], c3 = cyv[3];
-                Bn[r][0] += 0.5f * (c0 + c1);
-                Bn[r][1] += c1;
-                Bn[r][2] += 0.5f * (c1 + c2);
-                Bn[r][3] += c2;
-                Bn[r][4] += 0.5f * (c2 + c3);
-                Bn[r][5] += c3;
+                for (int c = 0; c < 4; ++c) {
+                    float lo = Cz[0][c], hi = Cz[min(1, RPT)][c];
+#pragma unroll
+                    for (int u = 1; u <= RPT; ++u)
+                        if (b0 == u) {
+                            lo = Cz[u][c];
+                            hi = Cz[min(u + 1, RPT)][c];
+                        }
+                    cyv[c] = oj ? 0.5f * (lo + hi) : lo;
+                }
+                Bn[w][0] += 0.5f * (cyv[0] + cyv[1]);
+                Bn[w][1] += cyv[1];
+                Bn[w][2] += 0.5f * (cyv[1] + cyv[2]);
+                Bn[w][3] += cyv[2];
+                Bn[w][4] += 0.5f * (cyv[2] + cyv[3]);
+                Bn[w][5] += cyv[3];
             }
         }
         if (s < 1) return;
-        float S[2][5], SX[2][4], SY[5];
+        float S[RPT + 1][5], SX[RPT + 1][4], SY[RPT][5];
 #pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const float* row = srow(L.sa, L.so, jr + r) + i0 + 3;  // cells i0-1 .. i0+3
-            S[r][0] = row[0];
+        for (int w = 0; w <= RPT; ++w) {
+            const float* row = srow(L.sa, L.so, srow0 + w) + i0 + 3;  // cells i0-1 .. i0+3
+            S[w][0] = row[0];
             const float4 m = *reinterpret_cast<const float4*>(row + 1);
-            S[r][1] = m.x;
-            S[r][2] = m.y;
-            S[r][3] = m.z;
-            S[r][4] = m.w;
+            S[w][1] = m.x;
+            S[w][2] = m.y;
+            S[w][3] = m.z;
+            S[w][4] = m.w;
         }
 #pragma unroll
-        for (int r = 0; r < 2; ++r)
+        for (int w = 0; w <= RPT; ++w)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) SX[r][q] = S[r][q] + S[r][q + 1];
+            for (int q = 0; q < 4; ++q) SX[w][q] = S[w][q] + S[w][q + 1];
 #pragma unroll
-        for (int q = 0; q < 5; ++q) SY[q] = S[0][q] + S[1][q];
-        if (s >= 2) {
-            // node plane P-1 (registers Ao) gets its upper half and is complete
-            const int k = P - 1;
-            const bool dk = (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
-            const float4 bq = *reinterpret_cast<const float4*>(srow(L.ba, L.bo, jr) + 4 + i0);
-            const float bb[4] = {bq.x, bq.y, bq.z, bq.w};
-            float v[4];
+        for (int r = 0; r < RPT; ++r)
+#pragma unroll
+            for (int q = 0; q < 5; ++q) SY[r][q] = S[r][q] + S[r + 1][q];
+        const int k = P - 1;  // node plane completed at this step (s >= 2)
+        const bool dk = (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+        float v[RPT][4];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r) {
+            float bb[4] = {0.f, 0.f, 0.f, 0.f};
+            if (s >= 2) {
+                const float4 bq = *reinterpret_cast<const float4*>(srow(L.ba, L.bo, srow0 + r) + 4 + i0);
+                bb[0] = bq.x;
+                bb[1] = bq.y;
+                bb[2] = bq.z;
+                bb[3] = bq.w;
+            }
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const float tot = acc[q] + layer_side(Ao, Bn, S, SY, SX, q);
-                const float sg = ss[q] + (SX[0][q] + SX[1][q]);
-                const float ax = a.k3 * tot;
-                float val;
-                if (MODE == 1 || MODE == 2)
-                    val = bb[q] - ax;
-                else
-                    val = fmaf(a.omega * (bb[q] - ax), rcp_approx(a.k0 * sg), Ao[1][q + 1]);
-                v[q] = (dxy[q] || dk) ? 0.f : val;
-            }
-            if (MODE == 2) {
-                // stage the residual row; the plane is restricted at the next step, after its barrier
-                float* Rr = R + ((s & 1) * Sh::TYR + jr) * a.rstride;
-                *reinterpret_cast<float4*>(Rr + 4 + i0) = make_float4(v[0], v[1], v[2], v[3]);
-                if (t == TX - 1) Rr[3] = g.per[0] ? v[3] : 0.f;  // node -1 (periodic: n-1 = 4 TX - 1)
-            } else if (j < g.nu[1] && nact > 0) {
-                store4(a.out, g, i0, j, k, v, nact);
+                const float cA = Ao[r + 1][q + 1], cB = Bn[r + 1][q + 1];
+                const float sgl = SX[r][q] + SX[r + 1][q];  // sigma of the layer's 4 cells around the node
+                // in-plane and body diagonals (shared by both nodes), then the xz / yz diagonals of each
+                float G0 = S[r][q] * ((Ao[r][q] - cA) + (Bn[r][q] - cA));
+                float G1 = S[r + 1][q] * ((Ao[r + 2][q] - cA) + (Bn[r + 2][q] - cA));
+                G0 = fmaf(S[r][q + 1], (Ao[r][q + 2] - cA) + (Bn[r][q + 2] - cA), G0);
+                G1 = fmaf(S[r + 1][q + 1], (Ao[r + 2][q + 2] - cA) + (Bn[r + 2][q + 2] - cA), G1);
+                const float G = G0 + G1;
+                float xa = SY[r][q] * (Bn[r + 1][q] - cA);
+                xa = fmaf(SY[r][q + 1], Bn[r + 1][q + 2] - cA, xa);
+                xa = fmaf(SX[r][q], Bn[r][q + 1] - cA, xa);
+                xa = fmaf(SX[r + 1][q], Bn[r + 2][q + 1] - cA, xa);
+                float xb = SY[r][q] * (Ao[r + 1][q] - cB);
+                xb = fmaf(SY[r][q + 1], Ao[r + 1][q + 2] - cB, xb);
+                xb = fmaf(SX[r][q], Ao[r][q + 1] - cB, xb);
+                xb = fmaf(SX[r + 1][q], Ao[r + 2][q + 1] - cB, xb);
+                if (s >= 2) {
+                    // node plane P-1 (registers Ao) gets its upper half and is complete
+                    const float ax = a.k3 * (acc[r][q] + (G + xa));
+                    float val;
+                    if (MODE == 1 || MODE == 2)
+                        val = bb[q] - ax;
+                    else
+                        val = fmaf(a.omega * (bb[q] - ax), rcp_approx(a.k0 * (ss[r][q] + sgl)), cA);
+                    v[r][q] = (dk || ((dmask >> (r * 4 + q)) & 1u)) ? 0.f : val;
+                }
+                // node plane P (registers Bn) gets its lower half
+                acc[r][q] = fmaf(-2.f * (cB - cA), sgl, G) + xb;
+                ss[r][q] = sgl;
             }
         }
-        // node plane P (registers Bn) gets its lower half
+        if (s < 2) return;
+        if (MODE == 2) {
+            // stage the residual rows; the plane is restricted at the next step, after its barrier
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            acc[q] = layer_side(Bn, Ao, S, SY, SX, q);
-            ss[q] = SX[0][q] + SX[1][q];
+            for (int r = 0; r < RPT; ++r) {
+                float* Rr = R + ((s & 1) * Sh::TYR + srow0 + r) * a.rstride;
+                *reinterpret_cast<float4*>(Rr + 4 + i0) = make_float4(v[r][0], v[r][1], v[r][2], v[r][3]);
+                if (t == TX - 1) Rr[3] = g.per[0] ? v[r][3] : 0.f;  // node -1 (periodic: n-1 = 4 TX - 1)
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < RPT; ++r)
+                if (j0 + r < g.nu[1] && nact > 0) store4(a.out, g, i0, j0 + r, k, v[r], nact);
         }
     };
 
-    float A[3][6], B[3][6];
+    float A[W][6], B[W][6];
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+    for (int r = 0; r < W; ++r)
 #pragma unroll
         for (int c = 0; c < 6; ++c) A[r][c] = B[r][c] = 0.f;
     int consumed = 0;
@@ -578,7 +609,8 @@ template <int MODE, int TY, int TXM>
 int launch(const NodalGeom& g, const NodalGeom* gc, const float* s, const float* x, const float* b,
            const float* e, float* out, float omega, unsigned* err, cudaStream_t st)
 {
-    using Sh = VsShape<MODE, TY>;
+    constexpr int RPT = GBP_VS_RPT;
+    using Sh = VsShape<MODE, TY, RPT>;
     const int TX = (g.nu[0] + 3) / 4;
     VsArgs a;
     a.g = g;
@@ -604,14 +636,14 @@ int launch(const NodalGeom& g, const NodalGeom* gc, const float* s, const float*
     if (rc) return rc;
     if (MODE != 3) mc = mb;
     if (MODE != 2) mx1 = mx, ms1 = ms, mb1 = mb;
-    const int smem = smem_bytes<MODE, TY>(a.rowlen, a.crowlen, a.rstride);
-    auto kern = k_vsweep32<MODE, TY, TXM>;
+    const int smem = smem_bytes<MODE, TY, RPT>(a.rowlen, a.crowlen, a.rstride);
+    auto kern = k_vsweep32<MODE, TY, TXM, RPT>;
     static int configured = 0, resident = 1;
     if (configured < smem) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         int r = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, TX * Sh::TYR, smem) == cudaSuccess && r > 0)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, TX * Sh::TTR, smem) == cudaSuccess && r > 0)
             resident = r;
         configured = smem;
     }
@@ -622,7 +654,7 @@ int launch(const NodalGeom& g, const NodalGeom* gc, const float* s, const float*
     if ((MODE == 2 || MODE == 3) && (kchunk & 1)) ++kchunk;
     a.kchunk = kchunk;
     dim3 grid(1, ty, (g.nu[2] + kchunk - 1) / kchunk);
-    kern<<<grid, dim3(TX, Sh::TYR), smem, st>>>(mx, ms, mb, mc, mx1, ms1, mb1, a);
+    kern<<<grid, dim3(TX, Sh::TTR), smem, st>>>(mx, ms, mb, mc, mx1, ms1, mb1, a);
     return GBP_OK;
 }
 

@@ -933,6 +933,20 @@ static void gauge(const lvl* L, double* x)
     for (long u = 0; u < L->n; ++u) x[u] -= c;
 }
 
+/* Singular systems (no phi held at 0): the constants are the null space and r stays orthogonal to
+ * them; the preconditioned residual is projected the same way (its mean removed), so that rounding in
+ * the V-cycle and in the reductions cannot grow a null-space component across iterations. */
+static void remove_null_space(const lvl* L, double* z)
+{
+    if (any_fixed(L)) return;
+    double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+    for (long u = 0; u < L->n; ++u) s += z[u];
+    s /= (double)L->n;
+#pragma omp parallel for schedule(static)
+    for (long u = 0; u < L->n; ++u) z[u] -= s;
+}
+
 /* stats: [0] iterations, [1] final relative residual (max norm of the strong form),
  *        [2] rhs max norm (strong form), [3] initial relative residual */
 static int pcg(mg_t* mg, const double* rhs_in, double* phi, double rtol, double atol, int maxiter, double* stats)
@@ -962,6 +976,7 @@ static int pcg(mg_t* mg, const double* rhs_in, double* phi, double rtol, double 
         memcpy(mg->b[0], r, sizeof(double) * (size_t)n);
         vcycle(mg, 0);
         memcpy(z, mg->x[0], sizeof(double) * (size_t)n);
+        remove_null_space(L, z);
         memcpy(p, z, sizeof(double) * (size_t)n);
         double rz = dot(L, r, z);
         for (it = 1; it <= maxiter; ++it) {
@@ -981,6 +996,7 @@ static int pcg(mg_t* mg, const double* rhs_in, double* phi, double rtol, double 
             memcpy(mg->b[0], r, sizeof(double) * (size_t)n);
             vcycle(mg, 0);
             memcpy(z, mg->x[0], sizeof(double) * (size_t)n);
+            remove_null_space(L, z);
             double rz2 = dot(L, r, z);
             double beta = rz2 / rz;
             rz = rz2;
