@@ -5,10 +5,11 @@ include/incflo_gb300.h; this package holds its build recipe, its ctypes binding 
 mirror of the reference's projector interface. Nothing here computes on the CPU.
 """
 from .projection import (AmrNodalProjector, Geometry, LPInfo, MacProjector, NodalProjector,  # noqa: F401
-                         apply_cc_projection, apply_nodal_projection, array4, make_options, options_from_inputs)
+                         apply_cc_projection, apply_nodal_projection, apply_nodal_projection_boxes, array4,
+                         make_options, options_from_inputs)
 from ._abi import ProjectionError, load  # noqa: F401
 
 __all__ = ["Geometry", "LPInfo", "NodalProjector", "MacProjector", "AmrNodalProjector", "apply_nodal_projection",
-           "apply_cc_projection",
+           "apply_nodal_projection_boxes", "apply_cc_projection",
            "array4",
            "make_options", "options_from_inputs", "ProjectionError", "load"]

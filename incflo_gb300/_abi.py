@@ -23,17 +23,18 @@ EXPORTS = (
     "gbp_plan_create", "gbp_plan_destroy", "gbp_plan_set_options", "gbp_plan_device_bytes",
     "gbp_nodal_set_sigma_from_density", "gbp_nodal_set_sigma", "gbp_nodal_project",
     "gbp_apply_nodal_projection", "gbp_mac_set_beta", "gbp_mac_set_beta_from_density",
-    "gbp_mac_project", "gbp_mac_get_fluxes", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel", "gbp_plan_check_level_kernels",
+    "gbp_mac_project", "gbp_mac_get_fluxes", "gbp_apply_nodal_projection_host", "gbp_plan_time_kernel", "gbp_plan_check_level_kernels", "gbp_plan_check_coarse_cycle",
     "gbp_nodal_divergence", "gbp_nodal_divergence_noalloc", "gbp_nodal_set_overset_mask",
     "gbp_mac_set_robin", "gbp_mac_set_eb", "gbp_average_down",
     "gbp_amr_create", "gbp_amr_destroy", "gbp_amr_set_options", "gbp_amr_device_bytes",
-    "gbp_amr_apply_nodal_projection", "gbp_abec_set_coeffs", "gbp_abec_solve", "gbp_abec_set_coeffs_eta", "gbp_nodal_set_eb", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
+    "gbp_amr_apply_nodal_projection", "gbp_abec_set_coeffs", "gbp_abec_solve", "gbp_abec_set_coeffs_eta", "gbp_nodal_set_eb", "gbp_nodal_set_eb_inflow", "gbp_mac_set_eb_inflow",
+    "gbp_apply_nodal_projection_boxes", "gbp_mac_set_beta_from_density_boxes", "gbp_mac_project_boxes", "gbp_apply_cc_projection", "gbp_enforce_inout_solvability", "gbp_mac_enforce_inout_solvability",
     "gbp_tensor_create", "gbp_tensor_destroy", "gbp_tensor_set_options", "gbp_tensor_device_bytes",
     "gbp_tensor_set_coeffs", "gbp_tensor_solve", "gbp_tensor_apply",
     "gbp_nn_conv3d", "gbp_nn_conv3d_wgrad",
     "gbp_surrogate_create", "gbp_surrogate_destroy", "gbp_surrogate_num_params", "gbp_surrogate_get_params",
     "gbp_surrogate_set_params", "gbp_surrogate_get_grads", "gbp_surrogate_save", "gbp_surrogate_load",
-    "gbp_surrogate_train_pair", "gbp_surrogate_predict", "gbp_surrogate_add_sample", "gbp_surrogate_num_samples",
+    "gbp_surrogate_train_pair", "gbp_surrogate_predict", "gbp_surrogate_add_sample", "gbp_surrogate_train_step", "gbp_surrogate_num_samples",
     "gbp_surrogate_clear_samples", "gbp_surrogate_train", "gbp_plan_set_surrogate",
 )
 
@@ -86,6 +87,7 @@ class Options(ctypes.Structure):
         ("ir_inner_cycles", ctypes.c_int),
         ("use_graphs", ctypes.c_int),
         ("always_use_bnorm", ctypes.c_int),
+        ("initial_guess", ctypes.c_int),
     ]
 
 
@@ -104,6 +106,7 @@ class Stats(ctypes.Structure):
         ("warm_start", ctypes.c_int),
         ("warm_rel_resid", ctypes.c_double),
         ("ms_warm", ctypes.c_double),
+        ("prev_rel_resid", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -150,6 +153,7 @@ def load(path: str = LIB_PATH):
         "gbp_apply_nodal_projection_host": (i, [P, P, P, d, P, P, d, i, ctypes.POINTER(Stats)]),
         "gbp_plan_time_kernel": (i, [P, i, i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
         "gbp_plan_check_level_kernels": (i, [P, ctypes.POINTER(ctypes.c_double)]),
+        "gbp_plan_check_coarse_cycle": (i, [P, ctypes.POINTER(ctypes.c_double)]),
         "gbp_nodal_divergence": (i, [P, A4, i, A4, ctypes.POINTER(ctypes.c_double)]),
         "gbp_nodal_divergence_noalloc": (i, [ctypes.POINTER(Geometry), ctypes.POINTER(ctypes.c_int),
                                              ctypes.POINTER(ctypes.c_int), A4, i, A4,
@@ -163,6 +167,14 @@ def load(path: str = LIB_PATH):
         "gbp_abec_solve": (i, [P, A4, A4, ctypes.POINTER(Stats)]),
         "gbp_abec_set_coeffs_eta": (i, [P, d, A4, d, d, A4]),
         "gbp_nodal_set_eb": (i, [P, A4]),
+        "gbp_nodal_set_eb_inflow": (i, [P, A4, A4, A4]),
+        "gbp_mac_set_eb_inflow": (i, [P, A4]),
+        "gbp_apply_nodal_projection_boxes": (i, [P, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(A4),
+                                                 ctypes.POINTER(A4), ctypes.POINTER(A4), d, ctypes.POINTER(A4),
+                                                 ctypes.POINTER(A4), d, d, d, d, i, i, ctypes.POINTER(Stats)]),
+        "gbp_mac_set_beta_from_density_boxes": (i, [P, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(A4), d]),
+        "gbp_mac_project_boxes": (i, [P, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(A4), ctypes.POINTER(A4),
+                                      ctypes.POINTER(A4), ctypes.POINTER(A4), i, ctypes.POINTER(Stats)]),
         "gbp_amr_set_options": (i, [P, ctypes.POINTER(Options)]),
         "gbp_amr_device_bytes": (ctypes.c_size_t, [P]),
         "gbp_amr_apply_nodal_projection": (i, [P, A4, A4, A4, A4, A4, ctypes.POINTER(A4), ctypes.POINTER(A4),
@@ -201,6 +213,7 @@ def load(path: str = LIB_PATH):
                                          ctypes.c_float, ctypes.POINTER(ctypes.c_double), P]),
         "gbp_surrogate_predict": (i, [P, ctypes.POINTER(ctypes.c_int), P, P, P]),
         "gbp_surrogate_add_sample": (i, [P, P, A4]),
+        "gbp_surrogate_train_step": (i, [P, P, A4, ctypes.c_float, ctypes.POINTER(ctypes.c_double)]),
         "gbp_surrogate_num_samples": (i, [P]),
         "gbp_surrogate_clear_samples": (i, [P]),
         "gbp_surrogate_train": (i, [P, i, ctypes.c_float, ctypes.c_ulonglong, P, P]),

@@ -110,6 +110,7 @@ int gbp_options_default(int kind, gbp_options* o)
     o->ir_inner_cycles = 5;
     o->use_graphs = 1;
     o->always_use_bnorm = 1;
+    o->initial_guess = 0;
     return GBP_OK;
 }
 
@@ -188,6 +189,14 @@ int gbp_options_set(gbp_options* o, const char* key, const char* value)
         ok = parse_int(s, &o->always_use_bnorm);
     else if (k == "smoother")
         ok = v == "jacobi" || v == "rbgs" || v == "default";
+    else if (k == "initial_guess") {
+        if (v == "zero" || v == "0")
+            o->initial_guess = 0;
+        else if (v == "previous" || v == "1")
+            o->initial_guess = 1;
+        else
+            ok = false;
+    }
     else {
         set_error("unknown projection option '" + k + "'");
         return GBP_BAD_ARG;
@@ -284,6 +293,8 @@ int gbp_plan_destroy(gbp_plan* p)
         if (e) cudaEventDestroy(e);
     if (p->dflux) cudaFree(p->dflux);
     if (p->ccbuf) cudaFree(p->ccbuf);
+    if (p->boxbuf) cudaFree(p->boxbuf);
+    if (p->boxtab) cudaFree(p->boxtab);
     delete p;
     return GBP_OK;
 }
@@ -297,7 +308,7 @@ int gbp_plan_set_options(gbp_plan* p, const gbp_options* opt)
 size_t gbp_plan_device_bytes(const gbp_plan* p)
 {
     if (!p) return 0;
-    size_t b = p->hbuf_bytes;
+    size_t b = p->hbuf_bytes + p->boxbuf_bytes + p->boxtab_bytes;
     b += p->nodal ? p->nodal->device_bytes() : p->mac->device_bytes();
     return b;
 }
@@ -596,6 +607,18 @@ int gbp_mac_set_eb(gbp_plan* p, const gbp_array4* vfrac, const gbp_array4* ax, c
     return p->mac->set_eb(vfrac, area, fc);
 }
 
+int gbp_mac_set_eb_inflow(gbp_plan* p, const gbp_array4* eb_vel)
+{
+    if (!p || !p->mac) {
+        set_error("gbp_mac_set_eb_inflow: not a MAC plan");
+        return GBP_BAD_ARG;
+    }
+    if (!eb_vel || !eb_vel->data) return p->mac->set_eb_inflow(nullptr);
+    int rc = check_cells(p, eb_vel, 3, "gbp_mac_set_eb_inflow: eb_vel");
+    if (rc) return rc;
+    return p->mac->set_eb_inflow(eb_vel);
+}
+
 int gbp_mac_project(gbp_plan* p, gbp_array4* ux, gbp_array4* uy, gbp_array4* uz, gbp_array4* phi, int phi_guess,
                     gbp_stats* stats)
 {
@@ -803,6 +826,15 @@ int gbp_plan_check_level_kernels(gbp_plan* p, double diff[4])
     return p->nodal->check_level_kernels(diff);
 }
 
+int gbp_plan_check_coarse_cycle(gbp_plan* p, double* diff)
+{
+    if (!p || !p->nodal || !diff) {
+        set_error("gbp_plan_check_coarse_cycle: needs a nodal plan and an output");
+        return GBP_BAD_ARG;
+    }
+    return p->nodal->check_coarse_cycle(diff);
+}
+
 int gbp_nodal_set_eb(gbp_plan* p, const gbp_array4* moments)
 {
     if (!p || !p->nodal) {
@@ -814,6 +846,21 @@ int gbp_nodal_set_eb(gbp_plan* p, const gbp_array4* moments)
         return GBP_BAD_ARG;
     }
     return p->nodal->set_eb((moments && moments->data) ? moments : nullptr);
+}
+
+int gbp_nodal_set_eb_inflow(gbp_plan* p, const gbp_array4* eb_vel, const gbp_array4* eb_dap,
+                            const gbp_array4* eb_bcent)
+{
+    if (!p || !p->nodal) {
+        set_error("gbp_nodal_set_eb_inflow: not a nodal plan");
+        return GBP_BAD_ARG;
+    }
+    if (!eb_vel || !eb_vel->data) return p->nodal->set_eb_inflow(nullptr, nullptr, nullptr);
+    int rc = check_cells(p, eb_vel, 3, "gbp_nodal_set_eb_inflow: eb_vel");
+    if (!rc) rc = check_cells(p, eb_dap, 3, "gbp_nodal_set_eb_inflow: eb_dap");
+    if (!rc) rc = check_cells(p, eb_bcent, 3, "gbp_nodal_set_eb_inflow: eb_bcent");
+    if (rc) return rc;
+    return p->nodal->set_eb_inflow(eb_vel, eb_dap, eb_bcent);
 }
 
 int gbp_abec_set_coeffs(gbp_plan* p, double alpha, const gbp_array4* a, double a0, double beta,

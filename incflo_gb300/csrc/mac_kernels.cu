@@ -360,7 +360,22 @@ __global__ void __launch_bounds__(256) k_mac_rhs(CellGeom g, gbp_array4 ux, gbp_
         fz1 *= eb.ap[2][p + g.sz];
     }
     const double dv = (fx1 - fx0) / g.h[0] + (fy1 - fy0) / g.h[1] + (fz1 - fz0) / g.h[2];
-    b[p] = -g.vol * dv;
+    b[p] = -g.vol * dv - (eb.ebflux ? eb.ebflux[p] : 0.0);
+}
+
+__global__ void __launch_bounds__(256) k_mac_eb_inflow_flux(CellGeom g, gbp_array4 ev, MacEB eb,
+                                                            double* __restrict__ flux)
+{
+    int i, j, k;
+    if (!decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) return;
+    const long long p = pidx(g.sy, g.sz, i, j, k);
+    double f = 0.0;
+    if (eb.kap[p] > 0.0) {
+        f = a4(ev, i, j, k, 0) * (eb.ap[0][p] - eb.ap[0][p + 1]) * (g.vol / g.h[0]) +
+            a4(ev, i, j, k, 1) * (eb.ap[1][p] - eb.ap[1][p + g.sy]) * (g.vol / g.h[1]) +
+            a4(ev, i, j, k, 2) * (eb.ap[2][p] - eb.ap[2][p + g.sz]) * (g.vol / g.h[2]);
+    }
+    flux[p] = f;
 }
 
 __global__ void __launch_bounds__(256) k_mac_correct(CellGeom g, int d, gbp_array4 u, const double* __restrict__ beta,
@@ -766,6 +781,11 @@ void mac_rhs(const CellGeom& g, const gbp_array4& ux, const gbp_array4& uy, cons
     MacEB e{};
     if (eb) e = *eb;
     k_mac_rhs<<<nblk(ncell(g), 256), 256, 0, st>>>(g, ux, uy, uz, b, e);
+}
+void mac_eb_inflow_flux(const CellGeom& g, const gbp_array4& eb_vel, const MacEB& eb, double* ebflux,
+                        cudaStream_t st)
+{
+    k_mac_eb_inflow_flux<<<nblk(ncell(g), 256), 256, 0, st>>>(g, eb_vel, eb, ebflux);
 }
 void mac_zero_faces(const CellGeom& g, int d, const gbp_array4& u, cudaStream_t st)
 {

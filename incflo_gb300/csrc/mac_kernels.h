@@ -30,6 +30,9 @@ void mac_bottom_dense(const CellGeom& g, const double* M, const unsigned char* a
 struct MacEB {
     double* kap;
     double* ap[3];
+    // flux of the EB inflow velocity out of each cell's fluid through its embedded boundary (padded cell
+    // layout), subtracted from the right-hand side; nullptr: no EB inflow
+    const double* ebflux;
 };
 
 // One cut face (0 < aperture < 1, not on a non-periodic domain side) whose flux uses the normal
@@ -101,6 +104,11 @@ void mac_coarsen_beta(const CellGeom& gf, const CellGeom& gc, int d, const doubl
                       cudaStream_t st);
 void mac_rhs(const CellGeom& g, const gbp_array4& ux, const gbp_array4& uy, const gbp_array4& uz, double* b,
              cudaStream_t st, const MacEB* eb = nullptr);
+// ebflux = sum_d u_eb,d (ap_d(low face) - ap_d(high face)) V / h_d on the cells 0..n-1 (0 on covered
+// cells): the EB inflow velocity's outflow through each cut cell's boundary, whose area vector the
+// divergence theorem gives from the apertures
+void mac_eb_inflow_flux(const CellGeom& g, const gbp_array4& eb_vel, const MacEB& eb, double* ebflux,
+                        cudaStream_t st);
 // ap (cut cells): beta / ap is the raw face beta; faces with ap == 0 are left alone
 void mac_correct(const CellGeom& g, int d, const gbp_array4& u, const double* beta, const double* phi,
                  cudaStream_t st, const double* ap = nullptr);

@@ -647,7 +647,7 @@ int MacSolver::set_eb(const gbp_array4* vfrac, const gbp_array4* const area[3], 
     // device storage
     size_t need = 0;
     auto add = [&](size_t cnt, size_t sz) { need = ((need + 255) & ~size_t(255)) + cnt * sz; };
-    for (int q = 0; q < 5; ++q) add(g.count, 8);
+    for (int q = 0; q < 6; ++q) add(g.count, 8);
     add(g.count, 4);
     add(F.size() + 1, sizeof(EbFace));
     add(C.size() + 1, sizeof(EbCell));
@@ -658,6 +658,7 @@ int MacSolver::set_eb(const gbp_array4* vfrac, const gbp_array4* const area[3], 
     if (rc) return rc;
     eb.m.kap = eb.pool.take<double>(g.count);
     for (int d = 0; d < 3; ++d) eb.m.ap[d] = eb.pool.take<double>(g.count);
+    eb.flux = eb.pool.take<double>(g.count);
     eb.beff64 = eb.pool.take<double>(g.count);
     eb.beff32 = eb.pool.take<float>(g.count);
     eb.faces = eb.pool.take<EbFace>(F.size() + 1);
@@ -673,6 +674,22 @@ int MacSolver::set_eb(const gbp_array4* vfrac, const gbp_array4* const area[3], 
     GBP_CUDA(cudaGetLastError());
     GBP_CUDA(cudaStreamSynchronize(st));  // the host tables go out of scope
     eb.on = true;
+    return GBP_OK;
+}
+
+int MacSolver::set_eb_inflow(const gbp_array4* eb_vel)
+{
+    if (!eb_vel) {
+        eb.m.ebflux = nullptr;
+        return GBP_OK;
+    }
+    if (!eb.on) {
+        set_error("mac_set_eb_inflow: the plan has no embedded boundary (mac_set_eb first)");
+        return GBP_BAD_ARG;
+    }
+    mac_eb_inflow_flux(L[0].g, *eb_vel, eb.m, eb.flux, st);
+    GBP_CUDA(cudaGetLastError());
+    eb.m.ebflux = eb.flux;
     return GBP_OK;
 }
 

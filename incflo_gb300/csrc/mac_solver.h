@@ -36,6 +36,10 @@ public:
     // face betas must be set again afterwards.
     int set_eb(const gbp_array4* vfrac, const gbp_array4* const area[3], const gbp_array4* const fcent[3]);
     bool has_eb() const { return eb.on; }
+    // MacProjector::setEBInflowVelocity: the velocity on the embedded boundary of every cell (3
+    // components, cells 0..n-1); its flux out of each cut cell enters the divergence of the next
+    // projections. nullptr removes it; set_eb drops it.
+    int set_eb_inflow(const gbp_array4* eb_vel);
     // ABecLaplacian on the same levels (MLABecLaplacian::setScalars / setACoeffs / setBCoeffs):
     // alpha a phi - beta div(b grad phi) = rhs; a == nullptr: the constant a0; b == nullptr: the
     // constant b0. alpha = 0 gives back the plain Poisson operator of the projections.
@@ -105,6 +109,7 @@ private:
         int nfaces = 0, ncells = 0;
         double* cb64 = nullptr;
         float* cb32 = nullptr;
+        double* flux = nullptr;    // EB inflow flux per cell (eb_inflow_flux), when m.ebflux is set
         double* beff64 = nullptr;  // finest-level right-hand side with the lagged cut-face terms
         float* beff32 = nullptr;
         double kap_sum = 0.0;

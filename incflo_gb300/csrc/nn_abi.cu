@@ -55,16 +55,53 @@ struct gbp_surrogate {
     double* scr = nullptr;    // device scratch: statistics, losses
     double* phi_prev = nullptr;
     size_t phi_prev_count = 0;
+    SurrogateSample stream_pair;  // the pair of gbp_surrogate_train_step (built, used once, overwritten)
+    long long stream_rows = 0;
     ~gbp_surrogate()
     {
         for (auto& q : samples) {
             cudaFree(q.x0);
             cudaFree(q.target);
         }
+        if (stream_pair.x0) cudaFree(stream_pair.x0);
+        if (stream_pair.target) cudaFree(stream_pair.target);
         if (scr) cudaFree(scr);
         if (phi_prev) cudaFree(phi_prev);
     }
 };
+
+namespace {
+
+// (input, target) of the plan's last projection into q (sized for the plan's network grid): input rhs,
+// sigma and phi_prev (may be null), target phi - phi_prev (phi without one)
+int make_pair(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev, SurrogateSample& q, int dims[3])
+{
+    NodalSolver& ns = *plan->nodal;
+    const NodalGeom& g = ns.geom0();
+    cudaStream_t st = ns.stream();
+    nn::net_dims(g, dims);
+    const nn::Grid3 g0 = nn::make_grid3(dims[0], dims[1], dims[2]);
+    const double* prev = nullptr;
+    if (phi_prev && phi_prev->data) {
+        if ((size_t)g.count > s->phi_prev_count) {
+            if (s->phi_prev) cudaFree(s->phi_prev);
+            s->phi_prev = nullptr;
+            s->phi_prev_count = 0;
+            GBP_CUDA(cudaMalloc(&s->phi_prev, sizeof(double) * g.count));
+            s->phi_prev_count = g.count;
+        }
+        GBP_CUDA(cudaMemsetAsync(s->phi_prev, 0, sizeof(double) * g.count, st));
+        nodal_load_phi(g, *phi_prev, s->phi_prev, st);
+        prev = s->phi_prev;
+    }
+    GBP_CUDA(cudaMemsetAsync(q.x0, 0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16), st));
+    GBP_CUDA(cudaMemsetAsync(q.target, 0, (size_t)g0.R * sizeof(float), st));
+    int rc = nn::build_input<double>(g, ns.rhs64(), ns.sigma64(), prev, g0, q.x0, s->scr, st);
+    if (!rc) rc = nn::build_target(g, ns.phi64(), prev, g0, q.target, s->scr + 4, st);
+    return rc;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -238,6 +275,43 @@ int gbp_surrogate_predict(gbp_surrogate* s, const int dims[3], const void* x0, v
     return finish_sync(s->net.err_word(), st);
 }
 
+int gbp_surrogate_train_step(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev, float lr, double* loss)
+{
+    if (!s || !plan || !plan->nodal || !(lr >= 0.f)) {
+        set_error("gbp_surrogate_train_step: needs a surrogate, a nodal plan after a projection and lr >= 0");
+        return GBP_BAD_ARG;
+    }
+    NodalSolver& ns = *plan->nodal;
+    cudaStream_t st = ns.stream();
+    int dims[3];
+    nn::net_dims(ns.geom0(), dims);
+    const nn::Grid3 g0 = nn::make_grid3(dims[0], dims[1], dims[2]);
+    if (g0.R > s->stream_rows) {
+        if (s->stream_pair.x0) cudaFree(s->stream_pair.x0);
+        if (s->stream_pair.target) cudaFree(s->stream_pair.target);
+        s->stream_pair = SurrogateSample{};
+        s->stream_rows = 0;
+        GBP_CUDA(cudaMalloc(&s->stream_pair.x0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16)));
+        GBP_CUDA(cudaMalloc(&s->stream_pair.target, (size_t)g0.R * sizeof(float)));
+        s->stream_rows = g0.R;
+    }
+    int rc = make_pair(s, plan, phi_prev, s->stream_pair, dims);
+    if (rc) return rc;
+    const int dom[3] = {ns.geom0().nu[0], ns.geom0().nu[1], ns.geom0().nu[2]};
+    rc = s->net.workspace(dims, true);
+    if (rc) return rc;
+    GBP_CUDA(cudaMemsetAsync(s->scr + 8, 0, sizeof(double), st));
+    GBP_CUDA(cudaMemsetAsync(s->net.err_word(), 0, sizeof(unsigned), st));
+    rc = s->net.forward_backward(s->stream_pair.x0, s->stream_pair.target, dom, s->scr + 8, st);
+    if (!rc && lr > 0.f) rc = s->net.adam_step(lr, st);
+    if (rc) return rc;
+    double h = 0.0;
+    GBP_CUDA(cudaMemcpyAsync(&h, s->scr + 8, sizeof(double), cudaMemcpyDeviceToHost, st));
+    rc = finish_sync(s->net.err_word(), st);
+    if (loss) *loss = h;
+    return rc;
+}
+
 int gbp_surrogate_add_sample(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev)
 {
     if (!s || !plan || !plan->nodal) {
@@ -276,7 +350,7 @@ int gbp_surrogate_add_sample(gbp_surrogate* s, gbp_plan* plan, const gbp_array4*
     cudaMemsetAsync(q.x0, 0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16), st);
     cudaMemsetAsync(q.target, 0, (size_t)g0.R * sizeof(float), st);
     int rc = nn::build_input<double>(g, ns.rhs64(), ns.sigma64(), prev, g0, q.x0, s->scr, st);
-    if (!rc) rc = nn::build_target(g, ns.phi64(), g0, q.target, s->scr + 4, st);
+    if (!rc) rc = nn::build_target(g, ns.phi64(), prev, g0, q.target, s->scr + 4, st);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = cuda_fail(e, "add_sample");

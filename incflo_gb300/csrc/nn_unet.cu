@@ -281,7 +281,8 @@ __global__ void k_input_write(NodalGeom g, const T* __restrict__ rhs, const T* _
     st8(o + 8, zz);
 }
 
-__global__ void k_target_stats(NodalGeom g, const double* __restrict__ phi, double* __restrict__ stats)
+__global__ void k_target_stats(NodalGeom g, const double* __restrict__ phi, const double* __restrict__ prev,
+                               double* __restrict__ stats)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     double a = 0.0, n = 0.0;
@@ -289,7 +290,8 @@ __global__ void k_target_stats(NodalGeom g, const double* __restrict__ phi, doub
         const int i = (int)(t % g.nu[0]);
         const int j = (int)((t / g.nu[0]) % g.nu[1]);
         const int k = (int)(t / ((long long)g.nu[0] * g.nu[1]));
-        const double v = phi[pidx(g.sy, g.sz, i, j, k)];
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        const double v = phi[p] - (prev ? prev[p] : 0.0);
         a = v * v;
         n = 1.0;
     }
@@ -301,8 +303,8 @@ __global__ void k_target_stats(NodalGeom g, const double* __restrict__ phi, doub
     }
 }
 
-__global__ void k_target_write(NodalGeom g, const double* __restrict__ phi, Grid3 g0, float* __restrict__ target,
-                               const double* __restrict__ stats)
+__global__ void k_target_write(NodalGeom g, const double* __restrict__ phi, const double* __restrict__ prev, Grid3 g0,
+                               float* __restrict__ target, const double* __restrict__ stats)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)g0.X * g0.Y * g0.Z) return;
@@ -312,7 +314,8 @@ __global__ void k_target_write(NodalGeom g, const double* __restrict__ phi, Grid
     float v = 0.f;
     if (x < g.nu[0] && y < g.nu[1] && z < g.nu[2]) {
         const double ms = stats[0] / fmax(stats[1], 1.0);
-        v = ms > 0.0 ? (float)(phi[pidx(g.sy, g.sz, x, y, z)] / sqrt(ms)) : 0.f;
+        const long long p = pidx(g.sy, g.sz, x, y, z);
+        v = ms > 0.0 ? (float)((phi[p] - (prev ? prev[p] : 0.0)) / sqrt(ms)) : 0.f;
     }
     target[row_of(g0, x, y, z)] = v;
 }
@@ -355,6 +358,23 @@ __global__ void k_scale_to64(long long n, const float* __restrict__ x, double al
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = alpha * (double)x[i];
+}
+
+__global__ void k_axpy_to64(long long n, const double* __restrict__ base, const float* __restrict__ x, double alpha,
+                            double* __restrict__ out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = fma(alpha, (double)x[i], base[i]);
+}
+
+__global__ void k_inject_nodes(NodalGeom gf, NodalGeom gc, int f, const double* __restrict__ src, double* __restrict__ dst)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)gc.nu[0] * gc.nu[1] * gc.nu[2]) return;
+    const int i = (int)(t % gc.nu[0]);
+    const int j = (int)((t / gc.nu[0]) % gc.nu[1]);
+    const int k = (int)(t / ((long long)gc.nu[0] * gc.nu[1]));
+    store_node(dst, gc, i, j, k, src[pidx(gf.sy, gf.sz, f * i, f * j, f * k)]);
 }
 
 uint64_t splitmix(uint64_t& s)
@@ -818,12 +838,13 @@ template int build_input<float>(const NodalGeom&, const float*, const float*, co
 template int build_input<double>(const NodalGeom&, const double*, const double*, const double*, const Grid3&,
                                  __nv_bfloat16*, double*, cudaStream_t);
 
-int build_target(const NodalGeom& g, const double* phi, const Grid3& g0, float* target, double* stats, cudaStream_t st)
+int build_target(const NodalGeom& g, const double* phi, const double* phi_prev, const Grid3& g0, float* target,
+                 double* stats, cudaStream_t st)
 {
     GBP_CUDA(cudaMemsetAsync(stats, 0, 2 * sizeof(double), st));
     const long long nu = (long long)g.nu[0] * g.nu[1] * g.nu[2];
-    k_target_stats<<<nblocks(nu), kT, 0, st>>>(g, phi, stats);
-    k_target_write<<<nblocks((long long)g0.X * g0.Y * g0.Z), kT, 0, st>>>(g, phi, g0, target, stats);
+    k_target_stats<<<nblocks(nu), kT, 0, st>>>(g, phi, phi_prev, stats);
+    k_target_write<<<nblocks((long long)g0.X * g0.Y * g0.Z), kT, 0, st>>>(g, phi, phi_prev, g0, target, stats);
     GBP_CUDA(cudaGetLastError());
     return GBP_OK;
 }
@@ -840,6 +861,21 @@ int node_dot2(const NodalGeom& g, const float* x, const float* b, const float* r
 int scale_to64(long long count, const float* x, double alpha, double* out, cudaStream_t st)
 {
     k_scale_to64<<<nblocks(count), kT, 0, st>>>(count, x, alpha, out);
+    GBP_CUDA(cudaGetLastError());
+    return GBP_OK;
+}
+
+int axpy_to64(long long count, const double* base, const float* x, double alpha, double* out, cudaStream_t st)
+{
+    k_axpy_to64<<<nblocks(count), kT, 0, st>>>(count, base, x, alpha, out);
+    GBP_CUDA(cudaGetLastError());
+    return GBP_OK;
+}
+
+int inject_nodes(const NodalGeom& gf, const NodalGeom& gc, int f, const double* src, double* dst, cudaStream_t st)
+{
+    const long long nu = (long long)gc.nu[0] * gc.nu[1] * gc.nu[2];
+    k_inject_nodes<<<nblocks(nu), kT, 0, st>>>(gf, gc, f, src, dst);
     GBP_CUDA(cudaGetLastError());
     return GBP_OK;
 }

@@ -99,8 +99,11 @@ private:
 template <typename T>
 int build_input(const NodalGeom& g, const T* rhs, const T* sigma, const double* phi_prev, const Grid3& g0,
                 __nv_bfloat16* x0, double* stats, cudaStream_t st);
-// Target tensor of the network from a nodal solution: phi / rms(phi) on the unique nodes.
-int build_target(const NodalGeom& g, const double* phi, const Grid3& g0, float* target, double* stats,
+// Target tensor of the network from a nodal solution, on the unique nodes:
+// target = (phi - phi_prev) / rms (phi_prev == nullptr: phi / rms): the increment the network predicts on
+// top of the previous solution, or the solution itself from a zero start
+int build_target(const NodalGeom& g, const double* phi, const double* phi_prev, const Grid3& g0, float* target,
+                 double* stats,
                  cudaStream_t st);
 // Prediction (channel 0 of hout) onto the unique nodes of a nodal level, with periodic aliases.
 int extract_output(const Grid3& g0, const __nv_bfloat16* hout, const NodalGeom& g, float* out, cudaStream_t st);
@@ -110,6 +113,11 @@ void net_dims(const NodalGeom& g, int dims[3]);
 int node_dot2(const NodalGeom& g, const float* x, const float* b, const float* r, double* out, cudaStream_t st);
 // out[i] = alpha * x[i] over a whole padded level array
 int scale_to64(long long count, const float* x, double alpha, double* out, cudaStream_t st);
+// out = base + alpha x over count padded positions (the previous solution plus the scaled increment)
+int axpy_to64(long long count, const double* base, const float* x, double alpha, double* out, cudaStream_t st);
+// dst = src at every unique node of the coarse level gc (the fine level's node (f i, f j, f k), f = 2^levels
+// apart, periodic aliases written): the previous solution injected onto the network's level
+int inject_nodes(const NodalGeom& gf, const NodalGeom& gc, int f, const double* src, double* dst, cudaStream_t st);
 
 }  // namespace nn
 }  // namespace gbp

@@ -102,8 +102,34 @@ __global__ void __launch_bounds__(128) k_eb_rhs(NodalGeom g, EbNodal e, RhsArgs 
             acc += ec.G[3 * corner + d] * u;
         }
     }
+    // the embedded boundary's inflow: - int_EB (u_eb . n) N_n dA by the cell's one-point rule
+    if (e.inflow)
+        for (int c = 0; c < 8; ++c) {
+            const int cc = nd.cell[c];
+            if (cc < 0) continue;
+            const int corner = (1 - (c & 1)) | ((1 - ((c >> 1) & 1)) << 1) | ((1 - (c >> 2)) << 2);
+            acc -= e.inflow[8 * cc + corner];
+        }
     // the level kernel's convention: g_n = sum over cells of int u . grad N_n
     rhs[p] += acc;
+}
+
+__global__ void __launch_bounds__(128) k_eb_inflow_shares(NodalGeom g, EbNodal e, gbp_array4 ev, gbp_array4 dap,
+                                                          gbp_array4 bc, double* __restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= e.ncells) return;
+    const EbNodeCell& ec = e.cells[t];
+    double F = 0.0, xb[3];
+    for (int d = 0; d < 3; ++d) {
+        F += *at4(ev, ec.i, ec.j, ec.k, d) * *at4(dap, ec.i, ec.j, ec.k, d) * (g.vol / g.h[d]);
+        xb[d] = *at4(bc, ec.i, ec.j, ec.k, d);
+    }
+    for (int b = 0; b < 8; ++b) {
+        double w = F;
+        for (int d = 0; d < 3; ++d) w *= ((b >> d) & 1) ? 0.5 + xb[d] : 0.5 - xb[d];
+        out[8 * t + b] = w;
+    }
 }
 
 __global__ void __launch_bounds__(128) k_eb_correct(NodalGeom g, EbNodal e, CorrArgs a, const double* __restrict__ phi)
@@ -178,6 +204,13 @@ void eb_rhs(const NodalGeom& g, const EbNodal& e, const RhsArgs& a, double* rhs,
 {
     if (e.nnodes <= 0) return;
     k_eb_rhs<<<(unsigned)((e.nnodes + 127) / 128), 128, 0, st>>>(g, e, a, rhs);
+}
+
+void eb_inflow_shares(const NodalGeom& g, const EbNodal& e, const gbp_array4& eb_vel, const gbp_array4& dap,
+                      const gbp_array4& bcent, double* out, cudaStream_t st)
+{
+    if (e.ncells <= 0) return;
+    k_eb_inflow_shares<<<(unsigned)((e.ncells + 127) / 128), 128, 0, st>>>(g, e, eb_vel, dap, bcent, out);
 }
 
 void eb_correct(const NodalGeom& g, const EbNodal& e, const CorrArgs& a, const double* phi, cudaStream_t st)

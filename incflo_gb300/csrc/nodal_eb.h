@@ -36,6 +36,10 @@ struct EbNodal {
     const float* sig32;
     const double* kap;         // volume fraction (padded cells, aliases)
     const unsigned char* reg;  // 1 on regular cells (volume fraction 1)
+    // EB inflow: F_c N_b(x_b) for corner b of cut cell c (8 per cell), F_c the EB inflow velocity's flux
+    // out of the cell's fluid and x_b its boundary centroid; subtracted from the right-hand side of the
+    // corner nodes. nullptr: the boundary carries no flux.
+    const double* inflow;
 };
 
 // out = Jacobi update (mode 0) or residual (mode 1) on the EB nodes, from x and b
@@ -43,6 +47,11 @@ template <typename T>
 void eb_nodes(const NodalGeom& g, const EbNodal& e, int mode, const T* x, const T* b, T* out, double omega,
               cudaStream_t st);
 void eb_rhs(const NodalGeom& g, const EbNodal& e, const RhsArgs& a, double* rhs, cudaStream_t st);
+// out[8 c + b] = F_c N_b(bcent_c) over the cut cells: F_c = sum_d eb_vel_d dap_d V / h_d (dap: the
+// boundary's area vector over the cell's face areas, bcent: the boundary centroid in cell widths from
+// the cell centre; 3 components each, cell arrays)
+void eb_inflow_shares(const NodalGeom& g, const EbNodal& e, const gbp_array4& eb_vel, const gbp_array4& dap,
+                      const gbp_array4& bcent, double* out, cudaStream_t st);
 void eb_correct(const NodalGeom& g, const EbNodal& e, const CorrArgs& a, const double* phi, cudaStream_t st);
 // s_in (the level's sigma as set) -> true sigma (e.sig64 / sig32), s64 / s32 = sigma on regular cells,
 // sk = sigma x volume fraction (the coarsening source)

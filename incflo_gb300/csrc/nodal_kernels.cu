@@ -24,6 +24,17 @@ namespace gbp {
 // ---------------------------------------------------------------------------------------
 // operator at one node
 // ---------------------------------------------------------------------------------------
+// Loads of the operator: plain (the level kernels), or L2-coherent ld.global.cg (kernels whose CTAs
+// read what other CTAs of the same launch wrote before a cluster barrier: no stale L1 / texture line)
+struct LdPlain {
+    template <typename T>
+    __device__ __forceinline__ static T ld(const T* p) { return *p; }
+};
+struct LdCg {
+    __device__ __forceinline__ static float ld(const float* p) { return __ldcg(p); }
+    __device__ __forceinline__ static double ld(const double* p) { return __ldcg(p); }
+};
+
 template <typename T>
 struct NodalOp;
 
@@ -31,12 +42,12 @@ struct NodalOp;
 // (fewest FP64 instructions; FP64 issue rate, not HBM, bounds these kernels on GB300).
 template <>
 struct NodalOp<double> {
-    template <bool ISO>
+    template <bool ISO, typename LD = LdPlain>
     __device__ __forceinline__ static double apply(const double* __restrict__ x, const double* __restrict__ s,
                                                    long long c, long long sy, long long sz,
                                                    const NodalGeom& g, double& diag)
     {
-        const double xc = x[c];
+        const double xc = LD::ld(x + c);
         double acc = 0.0, ssum = 0.0;
 #pragma unroll
         for (int cz = 0; cz < 2; ++cz)
@@ -45,17 +56,18 @@ struct NodalOp<double> {
 #pragma unroll
                 for (int cx = 0; cx < 2; ++cx) {
                     const long long cell = c + (cx - 1) + (cy - 1) * sy + (cz - 1) * sz;
-                    const double sg = s[cell];
+                    const double sg = LD::ld(s + cell);
                     const long long ox = cx ? 1 : -1, oy = cy ? sy : -sy, oz = cz ? sz : -sz;
                     ssum += sg;
                     if (ISO) {
-                        double S = (x[c + ox + oy] + x[c + ox + oz]) + (x[c + oy + oz] + x[c + ox + oy + oz]);
+                        double S = (LD::ld(x + c + ox + oy) + LD::ld(x + c + ox + oz)) +
+                                   (LD::ld(x + c + oy + oz) + LD::ld(x + c + ox + oy + oz));
                         acc = fma(sg, S, acc);
                     } else {
-                        double t = g.K[1] * (x[c + ox] - xc) + g.K[2] * (x[c + oy] - xc) +
-                                   g.K[4] * (x[c + oz] - xc) + g.K[3] * (x[c + ox + oy] - xc) +
-                                   g.K[5] * (x[c + ox + oz] - xc) + g.K[6] * (x[c + oy + oz] - xc) +
-                                   g.K[7] * (x[c + ox + oy + oz] - xc);
+                        double t = g.K[1] * (LD::ld(x + c + ox) - xc) + g.K[2] * (LD::ld(x + c + oy) - xc) +
+                                   g.K[4] * (LD::ld(x + c + oz) - xc) + g.K[3] * (LD::ld(x + c + ox + oy) - xc) +
+                                   g.K[5] * (LD::ld(x + c + ox + oz) - xc) + g.K[6] * (LD::ld(x + c + oy + oz) - xc) +
+                                   g.K[7] * (LD::ld(x + c + ox + oy + oz) - xc);
                         acc = fma(sg, t, acc);
                     }
                 }
@@ -69,12 +81,12 @@ struct NodalOp<double> {
 // local variation of x rather than to x itself.
 template <>
 struct NodalOp<float> {
-    template <bool ISO>
+    template <bool ISO, typename LD = LdPlain>
     __device__ __forceinline__ static float apply(const float* __restrict__ x, const float* __restrict__ s,
                                                   long long c, long long sy, long long sz,
                                                   const NodalGeom& g, float& diag)
     {
-        const float xc = x[c];
+        const float xc = LD::ld(x + c);
         float acc = 0.f, ssum = 0.f;
         const float k1 = (float)g.K[1], k2 = (float)g.K[2], k4 = (float)g.K[4], k3 = (float)g.K[3],
                     k5 = (float)g.K[5], k6 = (float)g.K[6], k7 = (float)g.K[7];
@@ -85,17 +97,18 @@ struct NodalOp<float> {
 #pragma unroll
                 for (int cx = 0; cx < 2; ++cx) {
                     const long long cell = c + (cx - 1) + (cy - 1) * sy + (cz - 1) * sz;
-                    const float sg = s[cell];
+                    const float sg = LD::ld(s + cell);
                     const long long ox = cx ? 1 : -1, oy = cy ? sy : -sy, oz = cz ? sz : -sz;
                     ssum += sg;
                     if (ISO) {
-                        float S = ((x[c + ox + oy] - xc) + (x[c + ox + oz] - xc)) +
-                                  ((x[c + oy + oz] - xc) + (x[c + ox + oy + oz] - xc));
+                        float S = ((LD::ld(x + c + ox + oy) - xc) + (LD::ld(x + c + ox + oz) - xc)) +
+                                  ((LD::ld(x + c + oy + oz) - xc) + (LD::ld(x + c + ox + oy + oz) - xc));
                         acc = fmaf(sg, S, acc);
                     } else {
-                        float t = k1 * (x[c + ox] - xc) + k2 * (x[c + oy] - xc) + k4 * (x[c + oz] - xc) +
-                                  k3 * (x[c + ox + oy] - xc) + k5 * (x[c + ox + oz] - xc) +
-                                  k6 * (x[c + oy + oz] - xc) + k7 * (x[c + ox + oy + oz] - xc);
+                        float t = k1 * (LD::ld(x + c + ox) - xc) + k2 * (LD::ld(x + c + oy) - xc) +
+                                  k4 * (LD::ld(x + c + oz) - xc) + k3 * (LD::ld(x + c + ox + oy) - xc) +
+                                  k5 * (LD::ld(x + c + ox + oz) - xc) + k6 * (LD::ld(x + c + oy + oz) - xc) +
+                                  k7 * (LD::ld(x + c + ox + oy + oz) - xc);
                         acc = fmaf(sg, t, acc);
                     }
                 }
@@ -531,6 +544,293 @@ void nodal_bottom_dense(const NodalGeom& g, const double* M, const T* b, T* x, i
 }
 template void nodal_bottom_dense<double>(const NodalGeom&, const double*, const double*, double*, int, cudaStream_t);
 template void nodal_bottom_dense<float>(const NodalGeom&, const double*, const float*, float*, int, cudaStream_t);
+
+// ---------------------------------------------------------------------------------------
+// coarse V-cycle in one cluster
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void cluster_barrier()
+{
+    // every thread of every CTA of the cluster arrives; release / acquire order the global stores of
+    // one phase before the loads of the next at cluster scope
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ unsigned cluster_nctas()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+
+// one Jacobi sweep xout = xin + omega D^-1 (b - A xin) (zero: xin = 0) over the level's unique nodes
+template <typename T>
+__device__ __forceinline__ void cc_jacobi(const NodalGeom& g, const T* s, const T* xin, const T* b, T* xout, T omega,
+                                          bool zero, long long t0, long long dt)
+{
+    const long long N = (long long)g.nu[0] * g.nu[1] * g.nu[2];
+    for (long long t = t0; t < N; t += dt) {
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        T v = T(0);
+        if (!node_is_dirichlet(g, i, j, k)) {
+            const long long c = pidx(g.sy, g.sz, i, j, k);
+            T diag;
+            if (zero) {
+                T ssum = T(0);
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    ssum += __ldcg(s + c + ((q & 1) - 1) + (((q >> 1) & 1) - 1) * g.sy + (((q >> 2) & 1) - 1) * g.sz);
+                diag = T(g.K[0]) * ssum;
+                v = omega * __ldcg(b + c) * approx_recip(diag);
+            } else {
+                const T ax = g.iso ? NodalOp<T>::template apply<true, LdCg>(xin, s, c, g.sy, g.sz, g, diag)
+                                   : NodalOp<T>::template apply<false, LdCg>(xin, s, c, g.sy, g.sz, g, diag);
+                v = __ldcg(xin + c) + omega * (__ldcg(b + c) - ax) * approx_recip(diag);
+            }
+        }
+        store_node(xout, g, i, j, k, v);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void cc_resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, long long t0,
+                                         long long dt)
+{
+    const long long N = (long long)g.nu[0] * g.nu[1] * g.nu[2];
+    for (long long t = t0; t < N; t += dt) {
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        T v = T(0);
+        if (!node_is_dirichlet(g, i, j, k)) {
+            const long long c = pidx(g.sy, g.sz, i, j, k);
+            T diag;
+            const T ax = g.iso ? NodalOp<T>::template apply<true, LdCg>(x, s, c, g.sy, g.sz, g, diag)
+                               : NodalOp<T>::template apply<false, LdCg>(x, s, c, g.sy, g.sz, g, diag);
+            v = __ldcg(b + c) - ax;
+        }
+        store_node(r, g, i, j, k, v);
+    }
+}
+
+// full-weighting restriction (the transpose of trilinear prolongation), as k_restrict
+template <typename T>
+__device__ __forceinline__ void cc_restrict(const NodalGeom& gf, const NodalGeom& gc, const T* rf, T* bc, long long t0,
+                                            long long dt)
+{
+    const long long N = (long long)gc.nu[0] * gc.nu[1] * gc.nu[2];
+    for (long long t = t0; t < N; t += dt) {
+        int I, J, K;
+        decode_node(gc, t, I, J, K);
+        T v = T(0);
+        if (!node_is_dirichlet(gc, I, J, K)) {
+            const long long f = pidx(gf.sy, gf.sz, 2 * I, 2 * J, 2 * K);
+            T acc = T(0);
+#pragma unroll
+            for (int c = -1; c <= 1; ++c) {
+                T accy = T(0);
+#pragma unroll
+                for (int b = -1; b <= 1; ++b) {
+                    const long long row = f + b * gf.sy + c * gf.sz;
+                    const T rx = T(0.5) * (__ldcg(rf + row - 1) + __ldcg(rf + row + 1)) + __ldcg(rf + row);
+                    accy += (b == 0 ? T(1) : T(0.5)) * rx;
+                }
+                acc += (c == 0 ? T(1) : T(0.5)) * accy;
+            }
+            v = acc;
+        }
+        store_node(bc, gc, I, J, K, v);
+    }
+}
+
+// xf += P xc over the fine unique nodes (trilinear; Dirichlet and masked fine nodes keep their value)
+template <typename T>
+__device__ __forceinline__ void cc_prolong(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T* xf, long long t0,
+                                           long long dt)
+{
+    const long long N = (long long)gf.nu[0] * gf.nu[1] * gf.nu[2];
+    for (long long t = t0; t < N; t += dt) {
+        int i, j, k;
+        decode_node(gf, t, i, j, k);
+        if (node_is_dirichlet(gf, i, j, k)) continue;
+        const int oi = i & 1, oj = j & 1, ok = k & 1;
+        const long long base = pidx(gc.sy, gc.sz, i >> 1, j >> 1, k >> 1);
+        T acc = T(0);
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            if (c && !ok) break;
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                if (b && !oj) break;
+#pragma unroll
+                for (int a = 0; a < 2; ++a) {
+                    if (a && !oi) break;
+                    acc += __ldcg(xc + base + a + b * gc.sy + c * gc.sz);
+                }
+            }
+        }
+        const int sh = oi + oj + ok;
+        const T w = sh == 0 ? T(1) : (sh == 1 ? T(0.5) : (sh == 2 ? T(0.25) : T(0.125)));
+        const long long p = pidx(gf.sy, gf.sz, i, j, k);
+        store_node(xf, gf, i, j, k, __ldcg(xf + p) + w * acc);
+    }
+}
+
+// x = M b on the bottom level by one CTA (the dense inverse; singular: b made consistent first), as
+// k_bottom_dense
+template <typename T>
+__device__ __forceinline__ void cc_bottom(const NodalGeom& g, const double* M, const T* bin, T* xout, int singular,
+                                          double* bb)
+{
+    const int N = g.nu[0] * g.nu[1] * g.nu[2];
+    double part = 0.0, vpart = 0.0;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        const bool held = node_is_dirichlet(g, i, j, k);
+        const double v = held ? 0.0 : (double)__ldcg(bin + pidx(g.sy, g.sz, i, j, k));
+        bb[t] = v;
+        part += v;
+        if (!held) vpart += node_volume(g, i, j, k);
+    }
+    if (singular) {
+        const double sum = block_sum_all(part);
+        const double vs = block_sum_all(vpart);
+        const double c = vs > 0.0 ? sum / vs : 0.0;
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            int i, j, k;
+            decode_node(g, t, i, j, k);
+            if (!node_is_dirichlet(g, i, j, k)) bb[t] -= c * node_volume(g, i, j, k);
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+        double a0 = 0.0, a1 = 0.0;
+        int v = 0;
+        for (; v + 1 < N; v += 2) {
+            a0 = fma(M[(size_t)v * N + t], bb[v], a0);
+            a1 = fma(M[(size_t)(v + 1) * N + t], bb[v + 1], a1);
+        }
+        if (v < N) a0 = fma(M[(size_t)v * N + t], bb[v], a0);
+        int i, j, k;
+        decode_node(g, t, i, j, k);
+        store_node(xout, g, i, j, k, (T)(a0 + a1));
+    }
+}
+
+// Every thread runs the same phase sequence (no early exit: each must reach every cluster barrier).
+template <typename T>
+__global__ void __launch_bounds__(kCoarseThreads) k_coarse_vcycle(CoarseCycle<T> a)
+{
+    extern __shared__ double bb[];
+    const long long t0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
+    const long long dt = (long long)cluster_nctas() * blockDim.x;
+    const int L = a.nl;
+    int slot[kCoarseMaxLevels];  // 0: the level's x holds its iterate, 1: its t
+    for (int q = 0; q + 1 < L; ++q) {
+        const NodalGeom& g = a.g[q];
+        T* buf[2] = {a.x[q], a.t[q]};
+        int cur = 0;
+        if (a.nu1 > 0) {
+            cc_jacobi<T>(g, a.s[q], nullptr, a.b[q], buf[0], a.omega, true, t0, dt);
+            cluster_barrier();
+            for (int p = 1; p < a.nu1; ++p) {
+                cc_jacobi<T>(g, a.s[q], buf[cur], a.b[q], buf[cur ^ 1], a.omega, false, t0, dt);
+                cluster_barrier();
+                cur ^= 1;
+            }
+        } else {
+            for (long long t = t0; t < g.count; t += dt) buf[0][t] = T(0);
+            cluster_barrier();
+        }
+        slot[q] = cur;
+        cc_resid<T>(g, a.s[q], buf[cur], a.b[q], a.r[q], t0, dt);
+        cluster_barrier();
+        cc_restrict<T>(g, a.g[q + 1], a.r[q], a.b[q + 1], t0, dt);
+        cluster_barrier();
+    }
+    if (cluster_rank() == 0) cc_bottom<T>(a.g[L - 1], a.M, a.b[L - 1], a.x[L - 1], a.singular, bb);
+    slot[L - 1] = 0;
+    cluster_barrier();
+    for (int q = L - 2; q >= 0; --q) {
+        const NodalGeom& g = a.g[q];
+        T* buf[2] = {a.x[q], a.t[q]};
+        int cur = slot[q];
+        cc_prolong<T>(g, a.g[q + 1], slot[q + 1] ? a.t[q + 1] : a.x[q + 1], buf[cur], t0, dt);
+        cluster_barrier();
+        for (int p = 0; p < a.nu2; ++p) {
+            cc_jacobi<T>(g, a.s[q], buf[cur], a.b[q], buf[cur ^ 1], a.omega, false, t0, dt);
+            cluster_barrier();
+            cur ^= 1;
+        }
+        slot[q] = cur;
+    }
+}
+
+int coarse_result_slot(int nu1, int nu2)
+{
+    const int pre = nu1 > 0 ? (nu1 - 1) & 1 : 0;
+    return (pre + nu2) & 1;
+}
+
+int nodal_coarse_cluster_size()
+{
+    static int cached = -1;
+    if (cached > 0) return cached;
+    int best = 8;
+    if (cudaFuncSetAttribute(k_coarse_vcycle<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(k_coarse_vcycle<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(16);
+        cfg.blockDim = dim3(kCoarseThreads);
+        cfg.dynamicSmemBytes = 216 * sizeof(double);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 16;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n32 = 0, n64 = 0;
+        if (cudaOccupancyMaxActiveClusters(&n32, k_coarse_vcycle<float>, &cfg) == cudaSuccess &&
+            cudaOccupancyMaxActiveClusters(&n64, k_coarse_vcycle<double>, &cfg) == cudaSuccess && n32 > 0 && n64 > 0)
+            best = 16;
+    }
+    cudaGetLastError();  // a refused attribute or query leaves no sticky error behind
+    cached = best;
+    return best;
+}
+
+template <typename T>
+int nodal_coarse_vcycle(const CoarseCycle<T>& c, int cluster, cudaStream_t st)
+{
+    const NodalGeom& gb = c.g[c.nl - 1];
+    const int nb = gb.nu[0] * gb.nu[1] * gb.nu[2];
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(kCoarseThreads);
+    cfg.dynamicSmemBytes = (size_t)nb * sizeof(double);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_coarse_vcycle<T>, c);
+    return e == cudaSuccess ? GBP_OK : cuda_fail(e, "k_coarse_vcycle launch");
+}
+template int nodal_coarse_vcycle<float>(const CoarseCycle<float>&, int, cudaStream_t);
+template int nodal_coarse_vcycle<double>(const CoarseCycle<double>&, int, cudaStream_t);
 
 // ---------------------------------------------------------------------------------------
 // level-0 set-up and the fused kernels around the solve

@@ -50,6 +50,35 @@ void nodal_bottom(const NodalGeom& g, const double* s64, const T* b, T* x, doubl
 template <typename T>
 void nodal_bottom_dense(const NodalGeom& g, const double* M, const T* b, T* x, int singular, cudaStream_t st);
 
+// The coarse end of a V-cycle in one launch: levels 0 .. nl-1 of this struct (a tail of the hierarchy
+// whose last level is the bottom, solved with the dense inverse M) cycled from a zero start by one
+// thread-block cluster, its CTAs meeting at cluster barriers between the phases (the smoothing sweeps,
+// residual, restriction, bottom and prolongation of each level). Level data stays in L2 and is read
+// with L2-coherent loads.
+constexpr int kCoarseMaxLevels = 10;
+template <typename T>
+struct CoarseCycle {
+    int nl;  // levels, >= 2 (at least one above the bottom)
+    NodalGeom g[kCoarseMaxLevels];
+    const T* s[kCoarseMaxLevels];
+    T* x[kCoarseMaxLevels];
+    T* t[kCoarseMaxLevels];
+    T* b[kCoarseMaxLevels];  // b[0]: the right-hand side of the first level (written by the caller)
+    T* r[kCoarseMaxLevels];
+    const double* M;         // dense inverse of the bottom operator
+    int singular;            // the bottom has the constants as null space
+    T omega;
+    int nu1, nu2;
+};
+constexpr int kCoarseThreads = 1024;
+// cluster size the device co-schedules for the kernel: 16 (non-portable) when possible, else 8
+int nodal_coarse_cluster_size();
+template <typename T>
+int nodal_coarse_vcycle(const CoarseCycle<T>& c, int cluster, cudaStream_t st);
+// which buffer of level 0 of the struct holds the result after nodal_coarse_vcycle: 0 = x, 1 = t (the
+// host's copy of the kernel's ping-pong)
+int coarse_result_slot(int nu1, int nu2);
+
 void nodal_sigma_from_rho(const NodalGeom& g, const gbp_array4* rho, double scale, double rho0, double* s64,
                           float* s32, cudaStream_t st);
 void nodal_sigma_copy(const NodalGeom& g, const gbp_array4* sig, double cval, double* s64, float* s32,

@@ -107,6 +107,11 @@ void NodalSolver::destroy()
     ev0 = ev1 = ev2 = evw = nullptr;
     if (net_x0) cudaFree(net_x0);
     if (net_scr) cudaFree(net_scr);
+    if (phi_last) cudaFree(phi_last);
+    if (net_prev) cudaFree(net_prev);
+    phi_last = net_prev = nullptr;
+    have_last = false;
+    net_prev_count = 0;
     net_x0 = nullptr;
     net_scr = nullptr;
     net_x0_bytes = 0;
@@ -514,6 +519,20 @@ void NodalSolver::resid(const NodalGeom& g, const T* s, const T* x, const T* b, 
     }
 }
 
+// First level of the hierarchy cycled by the cluster kernel (k_coarse_vcycle): the first level below
+// the finest with at most kCoarseNodes nodes, when the bottom uses the dense inverse and the tail fits
+// the kernel's level table; -1 otherwise (every level on its own launches).
+int NodalSolver::coarse_first() const
+{
+    if (!dense_bottom || !use_coarse) return -1;
+    for (int l = 1; l + 1 < (int)L.size(); ++l) {
+        const NodalGeom& g = L[l].g;
+        if ((long long)g.nu[0] * g.nu[1] * g.nu[2] <= kCoarseNodes)
+            return ((int)L.size() - l <= kCoarseMaxLevels) ? l : -1;
+    }
+    return -1;
+}
+
 // V-cycle for A x = b on level l. zero: x starts at 0; otherwise from xres[l].
 template <typename T>
 void NodalSolver::vcycle(int l, const T* b, bool zero)
@@ -524,6 +543,31 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     if (l == (int)L.size() - 1) {
         bottom<T>(l, b, B::x(lv));
         ++nk;
+        return;
+    }
+    // the small levels (this one down to the bottom) in one cluster-resident launch
+    if (zero && l >= 1 && l == coarse_first()) {
+        CoarseCycle<T> c{};
+        c.nl = (int)L.size() - l;
+        for (int q = 0; q < c.nl; ++q) {
+            const NodalLevel& v = L[l + q];
+            c.g[q] = v.g;
+            c.s[q] = B::s(v);
+            c.x[q] = B::x(v);
+            c.t[q] = B::t(v);
+            c.b[q] = B::b(v);
+            c.r[q] = B::r(v);
+        }
+        c.b[0] = const_cast<T*>(b);
+        c.M = dmat;
+        c.singular = bsing ? 1 : 0;
+        c.omega = (T)omega_eff;
+        c.nu1 = opt.nu1;
+        c.nu2 = opt.nu2;
+        int rc = nodal_coarse_vcycle<T>(c, nodal_coarse_cluster_size(), s);
+        if (rc && !launch_rc) launch_rc = rc;
+        ++nk;
+        xres[l] = coarse_result_slot(opt.nu1, opt.nu2) ? B::t(lv) : B::x(lv);
         return;
     }
     T* x = zero ? B::x(lv) : (T*)xres[l];
@@ -696,7 +740,7 @@ static inline double bits_to_double(unsigned long long b)
     return v;
 }
 
-int NodalSolver::solve(bool have_guess, gbp_stats* stats)
+int NodalSolver::solve(bool have_guess, gbp_stats* stats, bool from_prev)
 {
     const NodalLevel& l0 = L[0];
     cap_or_st = st;
@@ -738,14 +782,15 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats)
         stats->warm_start = 0;
         stats->warm_rel_resid = 0.0;
         stats->ms_warm = 0.0;
+        stats->prev_rel_resid = from_prev ? (bnorm > 0.0 ? rn / bnorm : rn) : 0.0;
     }
-    if (!have_guess && net && net_mode && rn > target) {
+    if ((!have_guess || from_prev) && net && net_mode && rn > target) {
         if (warm_skip > 0) {
             // the last attempts were all bypassed: do not pay for the network on this solve
             --warm_skip;
             if (stats) stats->warm_start = 3;
         } else {
-            int rc = warm_start(bnorm, &rn, stats);
+            int rc = warm_start(bnorm, &rn, stats, from_prev);
             if (rc) return rc;
         }
     }
@@ -841,6 +886,7 @@ int NodalSolver::set_mask(const gbp_iarray4* m)
 // and the cut-cell geometry (nodes that touch no fluid on their own level, which do not pin phi).
 int NodalSolver::rebuild_masks()
 {
+    have_last = false;  // the node set changed: the last solution no longer fits
     const bool um = umask8 && user_zeros > 0;
     const bool em = eb.on && eb.has_inactive;
     if (!um && !em) {
@@ -1120,6 +1166,7 @@ int NodalSolver::set_eb(const gbp_array4* M)
     add(g.count, 8);
     add(g.count, 4);
     add(g.count, 8);
+    add(8 * cells.size() + 8, 8);
     need += 4096;
     rc = eb.pool.reserve(need);
     if (rc) return rc;
@@ -1131,6 +1178,7 @@ int NodalSolver::set_eb(const gbp_array4* M)
     double* s64t = eb.pool.take<double>(g.count);
     float* s32t = eb.pool.take<float>(g.count);
     eb.ivol = eb.pool.take<double>(g.count);
+    eb.inflow_buf = eb.pool.take<double>(8 * cells.size() + 8);
     if (!nodes.empty())
         GBP_CUDA(cudaMemcpyAsync(dn, nodes.data(), sizeof(EbNodeEntry) * nodes.size(), cudaMemcpyHostToDevice, st));
     if (!cells.empty())
@@ -1154,6 +1202,23 @@ int NodalSolver::set_eb(const gbp_array4* M)
     eb.has_inactive = inactive;
     eb.on = true;
     return rebuild_masks();
+}
+
+int NodalSolver::set_eb_inflow(const gbp_array4* eb_vel, const gbp_array4* dap, const gbp_array4* bcent)
+{
+    if (!eb_vel) {
+        eb.e.inflow = nullptr;
+        return GBP_OK;
+    }
+    if (!eb.on) {
+        set_error("nodal_set_eb_inflow: the plan has no embedded boundary (nodal_set_eb first)");
+        return GBP_BAD_ARG;
+    }
+    eb.e.inflow = nullptr;  // the shares are computed from the table without the old ones
+    eb_inflow_shares(L[0].g, eb.e, *eb_vel, *dap, *bcent, eb.inflow_buf, st);
+    GBP_CUDA(cudaGetLastError());
+    eb.e.inflow = eb.inflow_buf;
+    return GBP_OK;
 }
 
 int NodalSolver::set_surrogate(nn::UNet* n, int level, int mode)
@@ -1184,10 +1249,13 @@ int NodalSolver::set_surrogate(nn::UNet* n, int level, int mode)
 }
 
 // Warm start from the network: restrict the FP32 right-hand side to the network's level, predict,
-// prolong to level 0, scale by the Galerkin factor alpha = x.b / x.Ax (the scaled prediction is
-// the best multiple of x in the energy norm), then take it only if its FP64 residual beats the
-// zero start's. On return phi / res / *rn describe the chosen start.
-int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
+// prolong to level 0, scale by the Galerkin factor alpha = x.r / x.Ax (the scaled prediction is the best
+// multiple of x in the energy norm), then take it only if its FP64 residual beats the start it would
+// replace. From a zero start the network predicts phi (input phi_prev = 0) and competes with phi = 0;
+// from the previous solution (from_prev: phi / res hold it and its residual) it predicts the increment
+// with phi_prev injected onto its level, the candidate is phi_prev + alpha x, and it competes with the
+// previous-phi start. On return phi / res / *rn describe the chosen start.
+int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats, bool from_prev)
 {
     const NodalLevel& l0 = L[0];
     const int lv = net_level;
@@ -1199,7 +1267,20 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
     int dims[3];
     nn::net_dims(L[lv].g, dims);
     int rc = net->workspace(dims, false);
-    if (!rc) rc = nn::build_input<float>(L[lv].g, L[lv].b32, L[lv].s32, nullptr, net->grid0(), net_x0, net_scr, st);
+    const double* prev_lv = nullptr;
+    if (!rc && from_prev) {
+        if ((size_t)L[lv].g.count > net_prev_count) {
+            if (net_prev) cudaFree(net_prev);
+            net_prev = nullptr;
+            net_prev_count = 0;
+            GBP_CUDA(cudaMalloc(&net_prev, sizeof(double) * L[lv].g.count));
+            GBP_CUDA(cudaMemsetAsync(net_prev, 0, sizeof(double) * L[lv].g.count, st));
+            net_prev_count = L[lv].g.count;
+        }
+        rc = nn::inject_nodes(l0.g, L[lv].g, 1 << lv, phi, net_prev, st);
+        prev_lv = net_prev;
+    }
+    if (!rc) rc = nn::build_input<float>(L[lv].g, L[lv].b32, L[lv].s32, prev_lv, net->grid0(), net_x0, net_scr, st);
     if (!rc) rc = net->forward(net_x0, st);
     if (!rc) rc = nn::extract_output(net->grid0(), net->hout(), L[lv].g, L[lv].x32, st);
     if (rc) return rc;
@@ -1207,6 +1288,8 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
         GBP_CUDA(cudaMemsetAsync(L[l].x32, 0, sizeof(float) * L[l].g.count, st));
         nodal_prolong_add<float>(L[l].g, L[l + 1].g, L[l + 1].x32, L[l].x32, st);
     }
+    // Galerkin factor against the residual of the start being replaced (b itself from zero)
+    if (from_prev) nodal_to_f32(l0.g, res, l0.b32, scale32, st);
     resid<float>(l0.g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st);
     if (launch_rc) return launch_rc;
     rc = nn::node_dot2(l0.g, l0.x32, l0.b32, l0.r32, net_scr, st);
@@ -1216,17 +1299,22 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
     GBP_CUDA(cudaStreamSynchronize(st));
     const double xax = d[0] - d[1];  // x.(b - r) = x.Ax in the scaled units of b32
     const double alpha = (xax > 0.0 && isfinite(d[0])) ? d[0] / xax / scale32 : 0.0;
-    nk += net->launches() - nk0 + 6 + 2 * lv;
-    double rw = bnorm;
+    nk += net->launches() - nk0 + 6 + 2 * lv + (from_prev ? 2 : 0);
+    double rw = *rn;
+    // candidate phi (phi_prev + alpha x, or alpha x) and its FP64 residual, in the level-0 FP64 scratch
+    double* cand = from_prev ? l0.t64 : phi;
+    double* cres = from_prev ? l0.r64 : res;
     if (alpha != 0.0) {
-        rc = nn::scale_to64(l0.g.count, l0.x32, alpha, phi, st);
+        rc = from_prev ? nn::axpy_to64(l0.g.count, phi, l0.x32, alpha, cand, st)
+                       : nn::scale_to64(l0.g.count, l0.x32, alpha, cand, st);
         if (rc) return rc;
-        resid0(phi, rhs0, res, dnorm + 1, st);
+        GBP_CUDA(cudaMemsetAsync(dnorm + 2, 0, sizeof(unsigned long long), st));
+        resid0(cand, rhs0, cres, dnorm + 2, st);
         if (launch_rc) return launch_rc;
         nk += 2;
-        GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         GBP_CUDA(cudaStreamSynchronize(st));
-        rw = bits_to_double(hnorm[1]);
+        rw = bits_to_double(hnorm[2]);
     }
     const bool take = alpha != 0.0 && isfinite(rw) && rw < *rn;
     // two bypasses in a row: skip the next 16 attempts, then try again
@@ -1235,13 +1323,18 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
         warm_skip = 16;
         warm_streak = 0;
     }
-    if (!take) {
-        // bypass: back to the zero start
+    if (take) {
+        if (from_prev) {
+            GBP_CUDA(cudaMemcpyAsync(phi, cand, sizeof(double) * l0.g.count, cudaMemcpyDeviceToDevice, st));
+            GBP_CUDA(cudaMemcpyAsync(res, cres, sizeof(double) * l0.g.count, cudaMemcpyDeviceToDevice, st));
+        }
+        GBP_CUDA(cudaMemcpyAsync(dnorm + 1, dnorm + 2, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+        *rn = rw;
+    } else if (!from_prev) {
+        // bypass: back to the zero start (the previous-phi start was left in phi / res untouched)
         GBP_CUDA(cudaMemsetAsync(phi, 0, sizeof(double) * l0.g.count, st));
         GBP_CUDA(cudaMemcpyAsync(res, rhs0, sizeof(double) * l0.g.count, cudaMemcpyDeviceToDevice, st));
         GBP_CUDA(cudaMemcpyAsync(dnorm + 1, dnorm, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
-    } else {
-        *rn = rw;
     }
     GBP_CUDA(cudaEventRecord(ev2, st));
     GBP_CUDA(cudaEventSynchronize(ev2));
@@ -1253,8 +1346,8 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats)
         stats->ms_warm = ms;
     }
     if (opt.verbose)
-        fprintf(stderr, "gbp nodal: warm start alpha %.4e, rel resid %.3e (%s)\n", alpha, bnorm > 0 ? rw / bnorm : rw,
-                take ? "used" : "bypassed");
+        fprintf(stderr, "gbp nodal: warm start (%s) alpha %.4e, rel resid %.3e (%s)\n", from_prev ? "increment" : "phi",
+                alpha, bnorm > 0 ? rw / bnorm : rw, take ? "used" : "bypassed");
     return GBP_OK;
 }
 
@@ -1288,8 +1381,11 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
     if (singular) {
         // consistent right-hand side, and its max norm (the relative-tolerance reference; with cut
         // cells taken again below over the fluid volumes)
-        nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, 1, nodal_rhs_partials(l0.g), dnorm, st);
-        nk += 2;
+        // (the cut cells' int u . grad N sum to zero over each cell's corners, an EB inflow does not:
+        // then the sums are taken again over the assembled right-hand side)
+        const bool fresh = eb.on && eb.e.inflow != nullptr;
+        nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, fresh ? 0 : 1, nodal_rhs_partials(l0.g), dnorm, st);
+        nk += fresh ? 3 : 2;
     } else {
         nodal_norm(l0.g, rhs0, dnorm, st);
         ++nk;
@@ -1302,9 +1398,17 @@ int NodalSolver::project(const RhsArgs& rhs, const CorrArgs& corr, gbp_array4* p
         nodal_load_phi(l0.g, *phi_guess, phi, st);
         ++nk;
     }
+    // initial_guess = previous: the last solution of this plan is the start (unless the caller gave one)
+    const bool from_prev = !phi_guess && opt.initial_guess == 1 && have_last;
+    if (from_prev) GBP_CUDA(cudaMemcpyAsync(phi, phi_last, sizeof(double) * l0.g.count, cudaMemcpyDeviceToDevice, st));
     GBP_CUDA(cudaGetLastError());
-    int status = solve(phi_guess != nullptr, stats);
+    int status = solve(phi_guess != nullptr || from_prev, stats, from_prev);
     if (status != GBP_OK && status != GBP_NOT_CONVERGED) return status;
+    if (opt.initial_guess == 1) {
+        if (!phi_last) GBP_CUDA(cudaMalloc(&phi_last, sizeof(double) * l0.g.count));
+        GBP_CUDA(cudaMemcpyAsync(phi_last, phi, sizeof(double) * l0.g.count, cudaMemcpyDeviceToDevice, st));
+        have_last = status == GBP_OK;
+    }
     // p_nd first: its copy-out can then overlap the velocity correction
     if (phi_out && phi_out->data) {
         nodal_store_phi(l0.g, *phi_out, phi, phi_accumulate, st);
@@ -1438,7 +1542,8 @@ int NodalSolver::divergence(const RhsArgs& rhs, const gbp_array4* out, double* m
     nodal_rhs(l0.g, ra, l0.s64, rhs0, singular ? partials : nullptr, st);
     if (eb.on) eb_rhs(l0.g, eb.e, ra, rhs0, st);
     if (singular)
-        nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, 1, nodal_rhs_partials(l0.g), dnorm, st);
+        nodal_remove_mean(l0.g, rhs0, partials, dscal, 0, (eb.on && eb.e.inflow) ? 0 : 1, nodal_rhs_partials(l0.g),
+                          dnorm, st);
     else
         nodal_norm(l0.g, rhs0, dnorm, st);
     if (out && out->data) nodal_store_div(l0.g, *out, rhs0, st);
@@ -1589,6 +1694,48 @@ int NodalSolver::check_level_kernels_on(float* A, float* C, double diff[4])
         set_error("check_level_kernels: a bounded device wait ran out");
         return GBP_TIMEOUT;
     }
+    return GBP_OK;
+}
+
+int NodalSolver::check_coarse_cycle(double* diff)
+{
+    const int lc = coarse_first();
+    if (lc < 1 || !sigma_ready) {
+        set_error("check_coarse_cycle: the plan has no cluster-cycled levels (levels " + std::to_string(L.size()) +
+                  ", dense bottom " + std::to_string((int)dense_bottom) + " of " + std::to_string(nbottom) +
+                  " nodes, cluster path " + std::to_string((int)use_coarse) + ") or no sigma (" +
+                  std::to_string((int)sigma_ready) + ")");
+        return GBP_BAD_ARG;
+    }
+    const NodalLevel& v = L[lc];
+    const NodalGeom& g = v.g;
+    const size_t bytes = sizeof(float) * g.count;
+    float* C = nullptr;
+    GBP_CUDA(cudaMalloc(&C, bytes));
+    cap_or_st = st;
+    // the same seeded right-hand side through the per-level launches and through the cluster kernel
+    GBP_CUDA(cudaMemsetAsync(v.b32, 0, bytes, st));
+    k_fill_seeded<<<dim3((g.nu[0] + 127) / 128, g.nu[1], g.nu[2]), 128, 0, st>>>(g, v.b32, 53u, 0);
+    use_coarse = false;
+    vcycle<float>(lc, v.b32, true);
+    cudaMemcpyAsync(C, xres[lc], bytes, cudaMemcpyDeviceToDevice, st);
+    use_coarse = true;
+    vcycle<float>(lc, v.b32, true);
+    unsigned long long* dm = reinterpret_cast<unsigned long long*>(dscal + 4);
+    cudaMemsetAsync(dm, 0, 2 * sizeof(unsigned long long), st);
+    k_maxdiff<<<592, 256, 0, st>>>((const float*)xres[lc], C, (long long)g.count, dm);
+    unsigned long long h[2] = {0, 0};
+    cudaMemcpyAsync(h, dm, sizeof(h), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(C);
+    const int rc = launch_rc;
+    launch_rc = 0;
+    if (e != cudaSuccess) return cuda_fail(e, "check_coarse_cycle");
+    if (rc) return rc;
+    double d, m;
+    memcpy(&d, &h[0], 8);
+    memcpy(&m, &h[1], 8);
+    *diff = m > 0 ? d / m : d;
     return GBP_OK;
 }
 

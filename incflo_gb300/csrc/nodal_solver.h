@@ -90,6 +90,10 @@ public:
     // part of each cell, normalised coordinates in [-1/2, 1/2]); nullptr removes them. Sigma must be set
     // again afterwards.
     int set_eb(const gbp_array4* moments);
+    // MLNodeLaplacian::setEBInflowVelocity: the velocity on the embedded boundary of every cell, with
+    // the boundary's area vector over the face areas (dap) and its centroid (bcent), 3 components each;
+    // enters the right-hand side of the next projections. eb_vel == nullptr removes it; set_eb drops it.
+    int set_eb_inflow(const gbp_array4* eb_vel, const gbp_array4* dap, const gbp_array4* bcent);
 
     // full projection: rhs from vel (+ fused add-back / U^n subtraction), solve, correct.
     // phi_copy: a copy (e.g. p_nd to the host) issued on its own stream once phi_out is stored,
@@ -106,7 +110,9 @@ public:
     size_t device_bytes() const { return pool.bytes; }
     cudaStream_t stream() const { return st; }
     // solve A phi = g on the level-0 arrays already in place (used by project and tests)
-    int solve(bool have_guess, gbp_stats* stats);
+    // from_prev: phi holds the plan's last solution (initial_guess = previous), a start the warm start
+    // must beat
+    int solve(bool have_guess, gbp_stats* stats, bool from_prev = false);
 
     // Preconditioner for a composite (two-level) driver: x += m V-cycles from zero on the FP64 level-0
     // residual r, in the plan's precision (FP32 V-cycles on r * scale in the mixed form). r and x are
@@ -148,7 +154,7 @@ private:
     void resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
                cudaStream_t s_);
     void record_iteration(int m);
-    int warm_start(double bnorm, double* rn, gbp_stats* stats);
+    int warm_start(double bnorm, double* rn, gbp_stats* stats, bool from_prev);
     void drop_graphs();
     int run_iteration(int m);
     int build_bottom();
@@ -160,6 +166,12 @@ private:
     std::vector<NodalLevel> L;
     DevicePool pool;
     double* phi = nullptr;       // level-0 solution (FP64)
+    // the last solution (initial_guess = previous), FP64 level 0, and its injection onto the network's
+    // level (the network's phi_prev input); allocated on first use
+    double* phi_last = nullptr;
+    bool have_last = false;
+    double* net_prev = nullptr;
+    size_t net_prev_count = 0;
     double* rhs0 = nullptr;      // level-0 right-hand side (FP64, weak form)
     double* res = nullptr;       // level-0 outer residual (FP64)
     double* partials = nullptr;  // reduction scratch
@@ -168,6 +180,15 @@ private:
     unsigned long long* dnorm = nullptr;  // [0] rhs norm, [1] residual norm
     unsigned long long* hnorm = nullptr;  // pinned mirror
     bool singular = false;        // the system has the constants as null space (consistent RHS, gauge)
+    // the levels with at most this many nodes (below the finest) run as one cluster launch per V-cycle
+    static constexpr long long kCoarseNodes = 40000;
+    bool use_coarse = true;
+    int coarse_first() const;
+public:
+    // test hook: one FP32 V-cycle from the first cluster-cycled level on a seeded right-hand side, through
+    // the per-level launches and through the cluster kernel; *diff = max |difference| / max |result|
+    int check_coarse_cycle(double* diff);
+private:
     double omega_eff = 0.85;  // the smoother weight in use (see set_omega)
     void set_omega();
     bool bsing = false;           // the coarsest operator does (no node held at 0 on it)
@@ -184,6 +205,7 @@ private:
         // nodes touching fluid on each level (a coarse cell holds fluid when one of its fine cells does)
         unsigned char* active8[kMaxLevels] = {};
         double* ivol = nullptr;            // 1 / fluid volume of each node's dual cell (level 0)
+        double* inflow_buf = nullptr;      // 8 EB inflow shares per cut cell (e.inflow when set)
         bool has_inactive = false;
         bool on = false;
     } eb;

@@ -26,4 +26,9 @@ struct gbp_plan {
     cudaEvent_t ev_rhs[gbp::kRhsGroups] = {};  // one per z-slab of the upload
     double* dflux = nullptr;  // 2 device doubles: inflow / outflow of the solvability fix
     double* ccbuf = nullptr;  // cell-centred projection scratch (unprojected face velocities, phi)
+    // multi-box levels: single-box staging of the fields and the device table of per-FAB transfers
+    void* boxbuf = nullptr;
+    size_t boxbuf_bytes = 0;
+    void* boxtab = nullptr;
+    size_t boxtab_bytes = 0;
 };

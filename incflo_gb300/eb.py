@@ -293,3 +293,106 @@ def moments_components(M):
     p + 3q + 9r."""
     M = np.asarray(M, dtype=np.float64)
     return np.ascontiguousarray(M.transpose(5, 4, 3, 0, 1, 2).reshape((27,) + M.shape[:3]))
+
+
+def _arc_centroid(x0, x1, y0, y1, cx, cy, r):
+    """Centroid of the part of the circle (cx, cy, r) inside the rectangle, or None when the circle
+    does not pass through it. The circle is cut at the angles where it crosses the rectangle's four
+    side lines; each piece between two cuts is wholly inside or outside (tested at its midpoint)."""
+    cuts = [0.0, 2.0 * math.pi]
+    for xb in (x0, x1):
+        c = (xb - cx) / r
+        if abs(c) < 1.0:
+            a = math.acos(c)
+            cuts += [a, 2.0 * math.pi - a]
+    for yb in (y0, y1):
+        s = (yb - cy) / r
+        if abs(s) < 1.0:
+            a = math.asin(s)
+            cuts += [a % (2.0 * math.pi), (math.pi - a) % (2.0 * math.pi)]
+    cuts = sorted(cuts)
+    length = sx = sy = 0.0
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        if b - a <= 1e-15:
+            continue
+        m = 0.5 * (a + b)
+        px, py = cx + r * math.cos(m), cy + r * math.sin(m)
+        if x0 <= px <= x1 and y0 <= py <= y1:
+            length += b - a
+            sx += math.sin(b) - math.sin(a)
+            sy += math.cos(a) - math.cos(b)
+    if length <= 0.0:
+        return None
+    return cx + r * sx / length, cy + r * sy / length
+
+
+def cylinder_boundary(n, lo, hi, center, radius, axis=2, small_volfrac=0.0):
+    """The embedded-boundary face of every cell for the cylinder of `cylinder` (the EB factory's
+    boundary area, normal and centroid, getBndryArea / getBndryNormal / getBndryCent in AMReX).
+    Returns dict(dap, bnorm, bcent), each (3, nz, ny, nx):
+      dap[d]   = ap_d(low face) - ap_d(high face): the boundary's area vector int_EB n dA divided by
+                 the cell's d-face area (n the unit normal out of the fluid, into the body), which the
+                 divergence theorem gives exactly from the area fractions (so it includes any face that
+                 small-cell removal closed);
+      bnorm    = the unit normal out of the fluid (dap scaled by the face areas, normalised), 0 on
+                 cells without a boundary face;
+      bcent    = the boundary centroid's offset from the cell centre in cell widths ([-1/2, 1/2]):
+                 the exact centroid of the circle's arc inside the cell in the circle's plane, 0 along
+                 the axis (and 0 on cells without an arc of their own)."""
+    n = tuple(int(v) for v in n)
+    geo = cylinder(n, lo, hi, center, radius, axis=axis, small_volfrac=small_volfrac)
+    h = [(hi[d] - lo[d]) / n[d] for d in range(3)]
+    ap = (geo["apx"], geo["apy"], geo["apz"])
+    dap = np.zeros((3, n[2], n[1], n[0]))
+    for d in range(3):
+        sl_lo = [slice(None)] * 3
+        sl_hi = [slice(None)] * 3
+        sl_lo[2 - d] = slice(0, n[d])
+        sl_hi[2 - d] = slice(1, n[d] + 1)
+        dap[d] = ap[d][tuple(sl_lo)] - ap[d][tuple(sl_hi)]
+    dap[:, geo["vfrac"] <= 0.0] = 0.0
+    dap[np.abs(dap) < 1e-14] = 0.0
+    V = h[0] * h[1] * h[2]
+    vec = np.stack([dap[d] * V / h[d] for d in range(3)])
+    mag = np.sqrt((vec * vec).sum(axis=0))
+    bnorm = np.where(mag > 0.0, vec / np.where(mag > 0.0, mag, 1.0), 0.0)
+    bcent = np.zeros((3, n[2], n[1], n[0]))
+    p, q = [d for d in range(3) if d != axis]
+    edges = [lo[d] + h[d] * np.arange(n[d] + 1) for d in range(3)]
+    has = mag > 0.0
+    for b in range(n[q]):
+        for a in range(n[p]):
+            x0, x1 = edges[p][a], edges[p][a + 1]
+            y0, y1 = edges[q][b], edges[q][b + 1]
+            if abs(0.5 * (x0 + x1) - center[p]) > radius + h[p] or abs(0.5 * (y0 + y1) - center[q]) > radius + h[q]:
+                continue
+            c = _arc_centroid(x0, x1, y0, y1, center[p], center[q], radius)
+            if c is None:
+                continue
+            idx = [slice(None)] * 3
+            idx[2 - p] = a
+            idx[2 - q] = b
+            idx = tuple(idx)
+            bcent[(p,) + idx] = np.where(has[idx], (c[0] - 0.5 * (x0 + x1)) / h[p], 0.0)
+            bcent[(q,) + idx] = np.where(has[idx], (c[1] - 0.5 * (y0 + y1)) / h[q], 0.0)
+    return dict(dap=dap, bnorm=bnorm, bcent=bcent)
+
+
+def eb_inflow_velocity(bnorm, vel_mag=None, velocity=None, normal=None, normal_tol_deg=0.0):
+    """The velocity on the embedded boundary of every cell (incflo::set_eb_velocity,
+    src/boundary_conditions/incflo_set_bcs.cpp:195-280, from the eb_flow.* inputs): with `vel_mag`
+    the boundary blows into the fluid along its normal (u = -vel_mag n, n out of the fluid); with
+    `velocity` the given vector. With `normal` only the cells whose boundary normal lies within
+    `normal_tol_deg` of -normal take it (the mask of incflo's rule, with its float-epsilon pad).
+    Cells without a boundary face get 0. Returns (3, nz, ny, nx)."""
+    bnorm = np.asarray(bnorm, dtype=np.float64)
+    cut = (bnorm * bnorm).sum(axis=0) > 0.0
+    mask = cut.astype(np.float64)
+    if normal is not None:
+        tol = normal_tol_deg * math.pi / 180.0 + float(np.finfo(np.float32).eps)
+        dot = sum(bnorm[d] * normal[d] for d in range(3))
+        mask = mask * ((dot >= -1.0 - tol) & (dot <= -1.0 + tol))
+    if vel_mag is not None:
+        return -mask[None] * bnorm * vel_mag
+    v = np.asarray(velocity, dtype=np.float64).reshape(3, 1, 1, 1)
+    return mask[None] * v

@@ -275,11 +275,14 @@ def _set_plan_eb(plan, eb_moments):
 def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd, *, time=0.0, dt=1.0,
                            prev_dt=1.0, scaling_factor=1.0, incremental=False, set_inflow_bc=True,
                            vel_old=None, rho0=1.0, ng=1, options: A.Options | None = None, stream=None,
-                           constant_density=False, surrogate=None, surrogate_level=1, eb_moments=None):
+                           constant_density=False, surrogate=None, surrogate_level=1, eb_moments=None,
+                           eb_inflow=None):
     """incflo::ApplyNodalProjection for one level, fused on the device; returns the stats dict.
     ``surrogate`` (incflo_gb300.surrogate.Surrogate) enables the learned warm start on multigrid level
     ``surrogate_level``; ``eb_moments`` (27, nz, ny, nx) the cut cells of an embedded boundary
-    (incflo_gb300.eb.cylinder_moments, components p + 3q + 9r)."""
+    (incflo_gb300.eb.cylinder_moments, components p + 3q + 9r); ``eb_inflow`` = (eb_vel, dap, bcent),
+    each (3, nz, ny, nx), the velocity on the embedded boundary with the boundary's area vector and
+    centroid (incflo_gb300.eb.cylinder_boundary / eb_inflow_velocity; setEBInflowVelocity)."""
     options = options or A.default_options(A.GBP_NODAL)
     key = (tuple(geom.n_cell), tuple(geom.prob_lo), tuple(geom.prob_hi), tuple(bc_lo), tuple(bc_hi),
            options.max_coarsening_level, torch.cuda.current_device())
@@ -293,6 +296,11 @@ def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd,
                                             int(surrogate_level), int(surrogate is not None)),
             "gbp_plan_set_surrogate")
     _set_plan_eb(plan, eb_moments)
+    if eb_inflow is not None:
+        ev, dap, bc = (array4(t) for t in eb_inflow)
+        A.check(A.load().gbp_nodal_set_eb_inflow(plan.ptr, _ref(ev), _ref(dap), _ref(bc)), "gbp_nodal_set_eb_inflow")
+    elif eb_moments is not None:
+        A.check(A.load().gbp_nodal_set_eb_inflow(plan.ptr, None, None, None), "gbp_nodal_set_eb_inflow")
     st = A.Stats()
     rho_a = None if constant_density else array4(density, 0)
     A.check(A.load().gbp_apply_nodal_projection(
@@ -300,6 +308,62 @@ def apply_nodal_projection(geom: Geometry, bc_lo, bc_hi, vel, density, gp, p_nd,
         float(rho0), _ref(array4(gp)), _ref(array4(p_nd)) if p_nd is not None else None, float(time), float(dt),
         float(prev_dt), float(scaling_factor), int(incremental), int(set_inflow_bc), ctypes.byref(st)),
         "gbp_apply_nodal_projection")
+    return st.as_dict()
+
+
+def _fab_ptrs(arrays, keep):
+    """array of nbox pointers to gbp_array4 (the C ABI's per-FAB argument); arrays: list of Array4"""
+    arr = (A.Array4 * len(arrays))(*arrays)
+    ptrs = (ctypes.POINTER(A.Array4) * len(arrays))(*[ctypes.pointer(arr[b]) for b in range(len(arrays))])
+    keep.append((arr, ptrs))
+    return ptrs
+
+
+def _box_table(boxes):
+    """boxes: [((lo_x, lo_y, lo_z), (hi_x, hi_y, hi_z)), ...] of valid cells -> 6 ints per box"""
+    flat = [int(v) for lo, hi in boxes for v in (*lo, *hi)]
+    return (ctypes.c_int * len(flat))(*flat)
+
+
+def fab_array4(t, box, ng=0, nodal=False):
+    """A FAB tensor of box ((lo), (hi)) with ng ghost cells (nodal: nodes lo..hi+1, no ghosts)."""
+    lo = box[0]
+    return array4(t, 0, lo=tuple(int(v) - (0 if nodal else ng) for v in lo))
+
+
+def apply_nodal_projection_boxes(geom: Geometry, bc_lo, bc_hi, boxes, vel, density, gp, p_nd, *, time=0.0, dt=1.0,
+                                 prev_dt=1.0, scaling_factor=1.0, incremental=False, set_inflow_bc=True,
+                                 vel_old=None, rho0=1.0, ng=1, options: A.Options | None = None, stream=None,
+                                 constant_density=False):
+    """incflo::ApplyNodalProjection for one level held in several boxes (the MultiFab's FABs): boxes =
+    [(lo, hi), ...] valid cells tiling the domain; vel (ng ghost cells), density, gp, vel_old: one tensor
+    per box; p_nd: one nodal tensor per box (nodes lo..hi+1). Returns the stats dict."""
+    options = options or A.default_options(A.GBP_NODAL)
+    key = (tuple(geom.n_cell), tuple(geom.prob_lo), tuple(geom.prob_hi), tuple(bc_lo), tuple(bc_hi),
+           options.max_coarsening_level, torch.cuda.current_device())
+    plan = NodalProjector._plans.get(key)
+    if plan is None:
+        plan = _Plan(geom, A.GBP_NODAL, bc_lo, bc_hi, options, stream)
+        NodalProjector._plans[key] = plan
+    else:
+        plan.set_options(options)
+    _set_plan_eb(plan, None)
+    A.check(A.load().gbp_plan_set_surrogate(plan.ptr, None, 1, 0), "gbp_plan_set_surrogate")
+    keep = []
+    nb = len(boxes)
+
+    def fabs(ts, g=0, nodal=False):
+        if ts is None:
+            return None
+        if len(ts) != nb:
+            raise ValueError("one tensor per box is required")
+        return _fab_ptrs([fab_array4(t, boxes[b], g, nodal) for b, t in enumerate(ts)], keep)
+
+    st = A.Stats()
+    A.check(A.load().gbp_apply_nodal_projection_boxes(
+        plan.ptr, nb, _box_table(boxes), fabs(vel, ng), fabs(vel_old), None if constant_density else fabs(density),
+        float(rho0), fabs(gp), fabs(p_nd, 0, True), float(time), float(dt), float(prev_dt), float(scaling_factor),
+        int(incremental), int(set_inflow_bc), ctypes.byref(st)), "gbp_apply_nodal_projection_boxes")
     return st.as_dict()
 
 
@@ -445,6 +509,7 @@ class MacProjector:
         self.stats = None
         self.robin = None
         self.eb = None
+        self.eb_vel = None
 
     def needInitialization(self):  # noqa: N802
         return self.plan is None
@@ -482,9 +547,25 @@ class MacProjector:
         [x (2, nz, ny, nx+1), y, z]: centroid offsets in cell widths along the two tangential
         directions in increasing order (AMReX's fcx / fcy / fcz). vfrac None removes the EB."""
         self.eb = None if vfrac is None else (vfrac, list(areafrac), list(facecent))
+        self.eb_vel = None
         self._push_eb()
         self._push_beta()
         self._push_robin()
+
+    def setEBInflowVelocity(self, lev, eb_vel):  # noqa: N802 (reference name)
+        """The velocity on the embedded boundary (3, nz, ny, nx) of level `lev` (0 only); None removes
+        it. Its flux out of each cut cell is part of the divergence of the next projections."""
+        if lev != 0:
+            raise ValueError("single-level MAC projector: lev must be 0")
+        self.eb_vel = eb_vel
+        self._push_eb_inflow()
+
+    def _push_eb_inflow(self):
+        if self.plan is None:
+            return
+        ev = getattr(self, "eb_vel", None)
+        A.check(A.load().gbp_mac_set_eb_inflow(self.plan.ptr, _ref(array4(ev)) if ev is not None else None),
+                "gbp_mac_set_eb_inflow")
 
     def _push_eb(self):
         if self.plan is None:
@@ -527,13 +608,14 @@ class MacProjector:
                 raise RuntimeError("setDomainBC must be called before project")
             self.plan = _Plan(self.geom, A.GBP_MAC, self.bc_lo, self.bc_hi, self.options, self.stream)
             self._push_eb()
+            self._push_eb_inflow()
             self._push_beta()
             self._push_robin()
         else:
             self.plan.set_options(self.options)
 
     def _push_beta(self):
-        if self.plan is None:
+        if self.plan is None or self.beta is None:  # None: set on the plan from the density already
             return
         L = A.load()
         if isinstance(self.beta, (list, tuple)):
@@ -554,6 +636,34 @@ class MacProjector:
         pa = array4(phi, ng_phi) if phi is not None else None
         A.check(A.load().gbp_mac_project(self.plan.ptr, _ref(u[0]), _ref(u[1]), _ref(u[2]), _ref(pa),
                                          int(phi is not None and phi_guess), ctypes.byref(st)), "gbp_mac_project")
+        self.stats = st.as_dict()
+        return self.stats
+
+    def setBetaFromDensityBoxes(self, boxes, rho, dt, ng=1):  # noqa: N802 (multi-box average_cellcenter_to_face)
+        """beta = dt / (face average of rho) from one density tensor per box (ng ghost cells, read across
+        Dirichlet sides)."""
+        self._ensure()
+        keep = []
+        ptrs = _fab_ptrs([fab_array4(t, boxes[b], ng) for b, t in enumerate(rho)], keep)
+        A.check(A.load().gbp_mac_set_beta_from_density_boxes(self.plan.ptr, len(boxes), _box_table(boxes), ptrs,
+                                                             float(dt)), "gbp_mac_set_beta_from_density_boxes")
+        self.beta = None  # set on the plan; not pushed again
+
+    def projectBoxes(self, boxes, umac, phi=None, phi_guess=True, rtol=None, atol=None):  # noqa: N802
+        """project() on a level held in several boxes: umac = [[ux, uy, uz] per box] (faces lo..hi+1 in
+        their direction), phi = one cell tensor per box or None."""
+        if rtol is not None:
+            self.options.rtol = float(rtol)
+        if atol is not None:
+            self.options.atol = float(atol)
+        self._ensure()
+        keep = []
+        u = [_fab_ptrs([fab_array4(umac[b][d], boxes[b]) for b in range(len(boxes))], keep) for d in range(3)]
+        ph = None if phi is None else _fab_ptrs([fab_array4(t, boxes[b]) for b, t in enumerate(phi)], keep)
+        st = A.Stats()
+        A.check(A.load().gbp_mac_project_boxes(self.plan.ptr, len(boxes), _box_table(boxes), u[0], u[1], u[2], ph,
+                                               int(phi is not None and phi_guess), ctypes.byref(st)),
+                "gbp_mac_project_boxes")
         self.stats = st.as_dict()
         return self.stats
 

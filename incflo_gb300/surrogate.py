@@ -93,6 +93,17 @@ class Surrogate:
         pa = array4(phi_prev) if phi_prev is not None else None
         A.check(self._L.gbp_surrogate_add_sample(self.ptr, plan.ptr, _ref(pa)), "gbp_surrogate_add_sample")
 
+    def train_step(self, projector, phi_prev: torch.Tensor | None = None, lr: float = 1e-3) -> float:
+        """One Adam step on the (rhs, sigma, phi_prev) -> phi - phi_prev pair of a projector's (or a
+        _Plan's) last projection, not stored; returns the loss."""
+        from .projection import _ref, array4
+        plan = projector._plan() if hasattr(projector, "_plan") else projector
+        pa = array4(phi_prev) if phi_prev is not None else None
+        loss = ctypes.c_double()
+        A.check(self._L.gbp_surrogate_train_step(self.ptr, plan.ptr, _ref(pa), float(lr), ctypes.byref(loss)),
+                "gbp_surrogate_train_step")
+        return float(loss.value)
+
     @property
     def num_samples(self) -> int:
         return int(self._L.gbp_surrogate_num_samples(self.ptr))

@@ -60,7 +60,10 @@ def gaussian_random_field(n, seed, slope=-2.0, ncomp=3):
     return out
 
 
-def interface_height(n, seed=2, modes=8, amplitude=0.01):
+def interface_height(n, seed=2, modes=8, amplitude=0.01, t=0.0, growth=0.0):
+    """Interface height 0.5 + h(x, y): a seeded sum of cosine modes (wavenumbers 1..modes) scaled to the
+    amplitude. t > 0 displaces it slowly (the interface of a time sequence): mode m travels by phase
+    0.05 m t and its amplitude grows by the factor 1 + growth t."""
     rng = np.random.Generator(np.random.PCG64(seed))
     x = (np.arange(n[0]) + 0.5) / n[0]
     y = (np.arange(n[1]) + 0.5) / n[1]
@@ -69,9 +72,13 @@ def interface_height(n, seed=2, modes=8, amplitude=0.01):
     th = rng.uniform(0.0, 2 * np.pi, size=(2, modes))
     h = np.zeros_like(X)
     for m in range(1, modes + 1):
-        h += a[0, m - 1] * np.cos(2 * np.pi * m * X + th[0, m - 1])
-        h += a[1, m - 1] * np.cos(2 * np.pi * m * Y + th[1, m - 1])
-    h *= amplitude / np.abs(h).max()
+        h += a[0, m - 1] * np.cos(2 * np.pi * m * X + th[0, m - 1] + 0.05 * m * t)
+        h += a[1, m - 1] * np.cos(2 * np.pi * m * Y + th[1, m - 1] - 0.05 * m * t)
+    h0 = np.zeros_like(X)
+    for m in range(1, modes + 1):
+        h0 += a[0, m - 1] * np.cos(2 * np.pi * m * X + th[0, m - 1])
+        h0 += a[1, m - 1] * np.cos(2 * np.pi * m * Y + th[1, m - 1])
+    h *= amplitude * (1.0 + growth * t) / np.abs(h0).max()
     return 0.5 + h
 
 
@@ -99,6 +106,44 @@ def double_shear_layer(n=128, seed=None, amp_noise=0.0):
         vel += rng.uniform(-amp_noise, amp_noise, size=vel.shape)
     rho = np.ones(X.shape)
     return dict(n=nn, lo=lo, hi=hi, bclo=(PERIODIC,) * 3, bchi=(PERIODIC,) * 3, vel=vel, rho=rho)
+
+
+def rt_sequence(n=256, seed=2, steps=8, dt=1.0, rho_lo=1.0, rho_hi=3.0):
+    """Successive projections of a slowly displaced variable-density interface (the setting of a
+    time-stepping run, where each projection can start from the previous one's phi): step t has the
+    interface of interface_height(t, growth 0.02) and the velocity cos(w t) u_a + sin(w t) u_b of two
+    seeded k^-2 fields, w = 0.05, so consecutive right-hand sides differ by a few percent. Yields the
+    cases of variable_density_rt's layout."""
+    nn = (n, n, n) if np.isscalar(n) else tuple(n)
+    ua = gaussian_random_field(nn, seed + 101)
+    ub = gaussian_random_field(nn, seed + 202)
+    dz = 1.0 / nn[2]
+    z = (np.arange(nn[2]) + 0.5) * dz
+    for q in range(steps):
+        t = q * dt
+        hxy = interface_height(nn, seed, t=t, growth=0.02)
+        rho = rho_lo + (rho_hi - rho_lo) * 0.5 * (1.0 + np.tanh((z[:, None, None] - hxy[None, :, :]) / (2.0 * dz)))
+        vel = np.cos(0.05 * t) * ua + np.sin(0.05 * t) * ub
+        yield dict(n=nn, lo=(0.0,) * 3, hi=(1.0,) * 3, bclo=(PERIODIC, PERIODIC, NEUMANN),
+                   bchi=(PERIODIC, PERIODIC, NEUMANN), vel=vel, rho=rho)
+
+
+def double_shear_sequence(n=128, seed=5, steps=8, dt=1.0, amp_noise=0.05):
+    """Successive projections of a double shear layer (u = tanh(30 (y - 1/4)) for y <= 1/2, tanh(30 (3/4 - y))
+    above, v = 0.05 sin(2 pi (x - 0.01 t)), w = 0) plus a seeded k^-2 perturbation of RMS amp_noise that
+    turns slowly (as rt_sequence's velocity); constant density. Same boundary layout as rt_sequence
+    (periodic x / y, walls in z)."""
+    nn = (n, n, n) if np.isscalar(n) else tuple(n)
+    X, Y, _ = _cell_centres(nn, (0.0,) * 3, (1.0,) * 3)
+    ua = gaussian_random_field(nn, seed + 303)
+    ub = gaussian_random_field(nn, seed + 404)
+    for q in range(steps):
+        t = q * dt
+        vel = amp_noise * (np.cos(0.05 * t) * ua + np.sin(0.05 * t) * ub)
+        vel[0] += np.where(Y <= 0.5, np.tanh(30.0 * (Y - 0.25)), np.tanh(30.0 * (0.75 - Y)))
+        vel[1] += 0.05 * np.sin(2 * np.pi * (X - 0.01 * t))
+        yield dict(n=nn, lo=(0.0,) * 3, hi=(1.0,) * 3, bclo=(PERIODIC, PERIODIC, NEUMANN),
+                   bchi=(PERIODIC, PERIODIC, NEUMANN), vel=vel, rho=np.ones((nn[2], nn[1], nn[0])))
 
 
 def with_ghosts(vel, ng=1):

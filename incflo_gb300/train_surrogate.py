@@ -1,14 +1,21 @@
 """Train the warm-start U-Net on the GPU and save its weights.
 
-  python -m incflo_gb300.train_surrogate --n 128 --samples 32 --steps 600 \
-      --out incflo_gb300/weights/unet16_rt128.bin
+  python -m incflo_gb300.train_surrogate --n 128 --pairs 2000 --seq-len 20 \
+      --out incflo_gb300/weights/unet16_seq128.bin
 
-Training pairs come from this library's own solver: variable-density fields of the 256^3 benchmark's
-family (tanh interface with a random height field, k^-2 random velocity) at n^3 with held-apart
-seeds, each projected to 1e-10 in the mixed form; the network learns rhs, sigma (, previous phi)
--> phi. A fraction of the pairs carries a previous phi (the solution of the same density with an
-unperturbed velocity). Afterwards the script evaluates the warm start on one held-out problem at
---eval-n^3 with the network on multigrid level 1, and prints one JSON line.
+Training pairs come from this library's own plain (FP64) solver, written while it steps through time
+sequences at n^3 (the setting of an incflo run, where every projection has the previous one's phi):
+half of the sequences are slowly displaced variable-density interfaces (synth.rt_sequence: the 256^3
+benchmark's family, tanh interface of random height, turning k^-2 velocity), half are double shear
+layers (synth.double_shear_sequence: u = tanh(30 (y - 1/4)) / tanh(30 (3/4 - y)), v = 0.05 sin(2 pi x),
+plus a turning k^-2 perturbation), seeds held apart from the evaluation's. Each projection of a
+sequence is solved to rtol 1e-10 from the previous phi and gives one pair: inputs (rhs, sigma, phi_prev)
+-> target phi - phi_prev, the increment the solver's initial_guess = previous start is missing (the
+first projection of a sequence: phi_prev = 0, target phi). The pairs stream through
+gbp_surrogate_train_step (one Adam step each, nothing stored), so `--pairs` pairs cost one solve and one
+training step apiece. Afterwards the script evaluates the three starts (zero, previous phi, previous phi
++ the network's increment) on a held-out interface sequence at --eval-n^3 with the network on multigrid
+level 1, and prints one JSON line.
 """
 from __future__ import annotations
 
@@ -31,65 +38,93 @@ from incflo_gb300.surrogate import WEIGHTS, Surrogate  # noqa: E402
 BC = (["Periodic", "Periodic", "Neumann"], ["Periodic", "Periodic", "Neumann"])
 
 
-def projector(case, vel=None, surrogate=None, level=1, rtol=1e-10):
+def projector(case, precision="mixed", initial_guess="zero", surrogate=None, level=1, rtol=1e-10, vel=None):
     geom = Geometry(case["n"], case["lo"], case["hi"])
-    v = torch.from_numpy(synth.with_ghosts(case["vel"] if vel is None else vel)).cuda()
-    sigma = torch.from_numpy(1.0 / case["rho"]).cuda()
-    p = NodalProjector(v, sigma, geom, options=make_options(0, precision="mixed", mg_rtol=rtol, mg_atol=0.0))
+    v = vel if vel is not None else torch.from_numpy(synth.with_ghosts(case["vel"])).cuda()
+    sigma = case["sigma_t"] if "sigma_t" in case else torch.from_numpy(1.0 / case["rho"]).cuda()
+    p = NodalProjector(v, sigma, geom, options=make_options(0, precision=precision, mg_rtol=rtol, mg_atol=0.0,
+                                                            initial_guess=initial_guess))
     p.setDomainBC(*BC)
     if surrogate is not None:
         p.setSurrogate(surrogate, level)
     return p
 
 
-def make_samples(s, n, count, prev_frac, seed0):
-    for i in range(count):
-        case = synth.variable_density_rt(n, seed_h=seed0 + i, seed_u=seed0 + 5000 + i)
+def lr_at(k, total, lr):
+    """step schedule: lr for the first 60 % of the pairs, lr / 3 to 85 %, lr / 10 after"""
+    f = k / max(1, total)
+    return lr if f < 0.6 else (lr / 3.0 if f < 0.85 else lr / 10.0)
+
+
+def stream_pairs(s, n, pairs, seq_len, lr, seed0):
+    """solve the training sequences with the plain solver and take one Adam step per projection"""
+    NodalProjector._plans.clear()
+    losses = []
+    k = 0
+    q = 0
+    while k < pairs:
+        gen = (synth.rt_sequence(n, seed=seed0 + q, steps=seq_len) if q % 2 == 0
+               else synth.double_shear_sequence(n, seed=seed0 + q, steps=seq_len))
         prev = None
-        if i < int(prev_frac * count):
-            p0 = projector(case)
-            p0.project()
-            prev = p0.getPhi().clone()
-            pert = synth.gaussian_random_field(case["n"], seed0 + 9000 + i)
-            vel = case["vel"] + 0.3 * pert
-        else:
-            vel = None
-        p = projector(case, vel)
-        st = p.project()
-        if st["status"] != 0:
-            raise RuntimeError(f"training solve {i} did not converge: {st}")
-        s.add_sample(p, phi_prev=prev)
+        for case in gen:
+            if k >= pairs:
+                break
+            p = projector(case, precision="fp64", initial_guess="previous")
+            st = p.project()
+            if st["status"] != 0:
+                raise RuntimeError(f"training solve {k} did not converge: {st}")
+            losses.append(s.train_step(p, prev, lr=lr_at(k, pairs, lr)))
+            prev = p.getPhi().clone()
+            k += 1
+        q += 1
+    NodalProjector._plans.clear()
+    return losses, q
 
 
-def evaluate(s, n, seed, level=1, reps=3):
-    case = synth.variable_density_rt(n, seed_h=seed, seed_u=seed + 5000)
+def evaluate_sequence(s, n, seed, steps=8, level=1):
+    """The three starts on one held-out interface sequence: per form, V-cycles and device ms of every
+    projection after the first (which has no previous phi), and how the network's candidate fared."""
+    cases = []
+    for case in synth.rt_sequence(n, seed=seed, steps=steps):
+        cases.append(dict(n=case["n"], lo=case["lo"], hi=case["hi"],
+                          vel_t=torch.from_numpy(synth.with_ghosts(case["vel"])).cuda(),
+                          sigma_t=torch.from_numpy(1.0 / case["rho"]).cuda()))
     out = {}
-    for name, sur in (("zero_start", None), ("learned", s)):
-        p = projector(case, surrogate=sur, level=level)
-        p.project()  # warm-up (plans, graphs)
-        ms, st = [], None
-        for _ in range(reps):
-            p.vel.copy_(torch.from_numpy(synth.with_ghosts(case["vel"])).cuda())
+    for name, ig, sur in (("zero_start", "zero", None), ("previous_phi", "previous", None),
+                          ("learned_increment", "previous", s)):
+        NodalProjector._plans.clear()
+        # warm-up on the first case (plan, graphs), then the sequence on the same plan: its first step
+        # starts from zero and, with initial_guess = previous, leaves its phi as the next step's start
+        projector(cases[0], vel=cases[0]["vel_t"].clone()).project()
+        ms, vc, used, rel = [], [], [], []
+        for q, c in enumerate(cases):
+            p = projector(c, initial_guess=ig, surrogate=sur if q > 0 else None, level=level,
+                          vel=c["vel_t"].clone())
             torch.cuda.synchronize()
             st = p.project()
+            if q == 0:
+                continue
             ms.append(st["ms_total"])
-        out[name] = {"ms": round(float(np.median(ms)), 3), "vcycles": st["vcycles"],
-                     "outer_iters": st["outer_iters"], "final_rel_resid": st["final_rel_resid"],
-                     "warm_start": st["warm_start"], "warm_rel_resid": st["warm_rel_resid"],
-                     "ms_warm": round(st["ms_warm"], 3)}
+            vc.append(st["vcycles"])
+            used.append(int(st["warm_start"]))
+            rel.append((st["prev_rel_resid"], st["warm_rel_resid"]))
+        out[name] = {"ms_per_projection": round(float(np.mean(ms)), 3), "vcycles_per_projection": float(np.mean(vc)),
+                     "vcycles": vc, "warm_start": used,
+                     "prev_rel_resid": [round(a, 6) for a, _ in rel], "warm_rel_resid": [round(b, 6) for _, b in rel]}
+    NodalProjector._plans.clear()
     return out
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=128)
-    ap.add_argument("--samples", type=int, default=32)
-    ap.add_argument("--prev-frac", type=float, default=0.25)
-    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--pairs", type=int, default=2000)
+    ap.add_argument("--seq-len", type=int, default=20)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval-n", type=int, default=256)
+    ap.add_argument("--eval-seed", type=int, default=7777)
     args = ap.parse_args()
     from incflo_gb300.build import build
 
@@ -97,17 +132,13 @@ def main():
     torch.cuda.init()
     s = Surrogate(seed=args.seed)
     t0 = time.time()
-    make_samples(s, args.n, args.samples, args.prev_frac, 1000)
+    losses, nseq = stream_pairs(s, args.n, args.pairs, args.seq_len, args.lr, 1000)
+    torch.cuda.synchronize()
     t1 = time.time()
-    torch.cuda.synchronize()
-    losses = s.train(args.steps, lr=args.lr, seed=args.seed)
-    torch.cuda.synchronize()
-    t2 = time.time()
     s.save(args.out)
-    ev = evaluate(s, args.eval_n, 777) if args.eval_n else None
-    print(json.dumps({"samples": args.samples, "n": args.n, "steps": args.steps, "sample_s": round(t1 - t0, 1),
-                      "train_s": round(t2 - t1, 2), "ms_per_step": round(1e3 * (t2 - t1) / max(1, args.steps), 3),
-                      "loss_first": float(np.mean(losses[:20])), "loss_last": float(np.mean(losses[-20:])),
+    ev = evaluate_sequence(s, args.eval_n, args.eval_seed) if args.eval_n else None
+    print(json.dumps({"pairs": len(losses), "sequences": nseq, "n": args.n, "train_s": round(t1 - t0, 1),
+                      "loss_first": float(np.mean(losses[:50])), "loss_last": float(np.mean(losses[-50:])),
                       "weights": os.path.relpath(args.out, ROOT), "eval": ev}), flush=True)
 
 

@@ -134,6 +134,21 @@ public:
         check(gbp_nodal_set_overset_mask(plan_.get(), &mask), "gbp_nodal_set_overset_mask");
     }
 
+    // the EB factory's volume moments of the level (27 components; gbp_nodal_set_eb)
+    void setEB(const gbp_array4& moments)
+    {
+        if (!plan_) throw Error(GBP_BAD_ARG, "NodalProjector::setEB before setDomainBC");
+        check(gbp_nodal_set_eb(plan_.get(), &moments), "gbp_nodal_set_eb");
+    }
+    // getLinOp().setEBInflowVelocity(lev, eb_vel), with the EB factory's boundary area vector (area
+    // fraction differences) and boundary centroid of the level, 3 components each
+    void setEBInflowVelocity(int lev, const gbp_array4& eb_vel, const gbp_array4& eb_dap, const gbp_array4& eb_bcent)
+    {
+        if (lev != 0) throw Error(GBP_BAD_ARG, "NodalProjector::setEBInflowVelocity: single level");
+        if (!plan_) throw Error(GBP_BAD_ARG, "NodalProjector::setEBInflowVelocity before setDomainBC");
+        check(gbp_nodal_set_eb_inflow(plan_.get(), &eb_vel, &eb_dap, &eb_bcent), "gbp_nodal_set_eb_inflow");
+    }
+
     gbp_stats project(double rtol, double atol)
     {
         if (!plan_) throw Error(GBP_BAD_ARG, "NodalProjector::project before setDomainBC");
@@ -228,6 +243,13 @@ public:
         check(gbp_mac_set_eb(plan_.get(), &vfrac, &area[0], &area[1], &area[2], &fcent[0], &fcent[1], &fcent[2]),
               "gbp_mac_set_eb");
         push_beta();
+    }
+    // setEBInflowVelocity(lev, eb_vel): the velocity on the embedded boundary (3 components)
+    void setEBInflowVelocity(int lev, const gbp_array4& eb_vel)
+    {
+        if (lev != 0) throw Error(GBP_BAD_ARG, "MacProjector::setEBInflowVelocity: single level");
+        if (!plan_) throw Error(GBP_BAD_ARG, "MacProjector::setEBInflowVelocity before setDomainBC");
+        check(gbp_mac_set_eb_inflow(plan_.get(), &eb_vel), "gbp_mac_set_eb_inflow");
     }
     gbp_stats project(double rtol, double atol) { return run(nullptr, rtol, atol); }
     gbp_stats project(gbp_array4 phi, double rtol, double atol) { return run(&phi, rtol, atol); }

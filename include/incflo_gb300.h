@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define GBP_ABI_VERSION 2
+#define GBP_ABI_VERSION 3
 
 typedef enum {
     GBP_OK = 0,
@@ -108,6 +108,12 @@ typedef struct {
                                     says fewer reach the tolerance */
     int use_graphs;              /* capture each V-cycle as a CUDA graph (1) */
     int always_use_bnorm;        /* relative tolerance against |b| (1) or |r0| (0) */
+    int initial_guess;           /* initial_guess = zero (0, incflo's: every projection starts from
+                                    phi = 0) | previous (1, nodal plans: start from the plan's last
+                                    solution, the setting of a time-stepping run; with a learned
+                                    warm start attached, the network predicts the increment on top
+                                    of it and is bypassed when its residual is not below the
+                                    previous-phi start's) */
 } gbp_options;
 
 typedef struct {
@@ -126,6 +132,8 @@ typedef struct {
                                     retries after 16 skipped solves) */
     double warm_rel_resid;       /* residual of the scaled prediction / rhs_norm (when attempted) */
     double ms_warm;              /* device time of the warm start (network + scaling + residual) */
+    double prev_rel_resid;       /* initial_guess = previous: residual of the previous-phi start /
+                                    rhs_norm (0 when the solve started from zero) */
 } gbp_stats;
 
 typedef struct gbp_plan gbp_plan;
@@ -188,6 +196,20 @@ int gbp_nodal_set_overset_mask(gbp_plan* plan, const gbp_iarray4* mask);
  * cell. NULL removes the cut cells. Sigma must be set again afterwards (gbp_apply_nodal_projection
  * does on every call). */
 int gbp_nodal_set_eb(gbp_plan* plan, const gbp_array4* moments);
+
+/* Velocity on the embedded boundary of a nodal plan's cut cells: MLNodeLaplacian::setEBInflowVelocity
+ * (src/projection/incflo_apply_nodal_projection.cpp:196-201, eb_vel from incflo::set_eb_velocity,
+ * src/boundary_conditions/incflo_set_bcs.cpp:195-280). Cell arrays with 3 components, valid cells:
+ * eb_vel the velocity on the boundary; eb_dap the boundary's area vector int_EB n dA (n out of the
+ * fluid) divided by the cell's face area of each direction, which equals the area-fraction difference
+ * ap(low face) - ap(high face) (AMReX's barea x bnorm on cubic cells); eb_bcent the boundary centroid's
+ * offset from the cell centre in cell widths (the EB factory's bcent). Each later projection adds the
+ * weak form's boundary term -int_EB (u_eb . n) N_a dA = -F_c N_a(bcent) to the right-hand side of the
+ * corners a of every cut cell c, F_c = sum_d eb_vel_d eb_dap_d V / h_d. The plan keeps the per-cell
+ * terms, not the arrays. eb_vel == NULL removes the inflow; gbp_nodal_set_eb drops it.
+ * GBP_BAD_ARG without cut cells on the plan. */
+int gbp_nodal_set_eb_inflow(gbp_plan* plan, const gbp_array4* eb_vel, const gbp_array4* eb_dap,
+                            const gbp_array4* eb_bcent);
 
 /* The nodal divergence of vel as the projection sees it: the right-hand side of the nodal solve
  * (div_i = weak divergence / control volume, inflow normal velocity from the ghost cells when
@@ -328,6 +350,29 @@ int gbp_amr_apply_nodal_projection(gbp_amr* amr, gbp_array4* vel_c, const gbp_ar
                                    const gbp_array4* const* rho_f, gbp_array4* const* gp_f, gbp_array4* const* p_f,
                                    double rho0, double scaling_factor, int incremental, gbp_stats* stats);
 
+/* ---- multi-box levels ---------------------------------------------------------------------
+ * A level whose MultiFabs hold several FABs (incflo's amr.max_grid_size split; the MFIter loops of
+ * src/projection/incflo_apply_nodal_projection.cpp:58-93, 124-192, 221-257 and
+ * src/convection/incflo_compute_MAC_projected_velocities.cpp:82-90, 272-299). boxes: nbox boxes of
+ * valid cells (lo[3], hi[3] inclusive, 6 ints each) that tile the plan's domain (disjoint, inside it,
+ * covering it: the level's BoxArray); each field is an array of nbox gbp_array4, FAB b covering box b
+ * (cell fields: its cells; nodal p_nd: nodes lo..hi+1; umac of direction d: faces lo..hi+1 in d), and
+ * vel one ghost cell across inflow sides where the box touches them (rho of the MAC plan: across
+ * Dirichlet sides). The plan gathers the FABs into its single-box staging (allocated on first use, kept
+ * with the plan), runs the single-box entry point and scatters the outputs to every FAB (faces and
+ * nodes shared by two boxes receive the same value). Same semantics, options and status codes as the
+ * single-box calls. */
+int gbp_apply_nodal_projection_boxes(gbp_plan* plan, int nbox, const int* boxes, gbp_array4* const* vel,
+                                     const gbp_array4* const* vel_old, const gbp_array4* const* rho, double rho0,
+                                     gbp_array4* const* gp, gbp_array4* const* p_nd, double time, double dt,
+                                     double prev_dt, double scaling_factor, int incremental, int set_inflow_bc,
+                                     gbp_stats* stats);
+int gbp_mac_set_beta_from_density_boxes(gbp_plan* plan, int nbox, const int* boxes, const gbp_array4* const* rho,
+                                        double dt);
+int gbp_mac_project_boxes(gbp_plan* plan, int nbox, const int* boxes, gbp_array4* const* umac_x,
+                          gbp_array4* const* umac_y, gbp_array4* const* umac_z, gbp_array4* const* phi,
+                          int phi_guess, gbp_stats* stats);
+
 /* ---- host-buffer convenience (end-to-end path) ----------------------------------------
  * Same as gbp_apply_nodal_projection with contiguous HOST arrays (no ghost cells):
  * vel [3][nz][ny][nx], rho [nz][ny][nx], gp [3][nz][ny][nx], p_nd nodal [nz+1][ny+1][nx+1].
@@ -354,6 +399,13 @@ int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_lau
  * prolongation + Jacobi. GBP_BAD_ARG when the whole-row kernels do not apply to the plan's level 0. */
 int gbp_plan_check_level_kernels(gbp_plan* plan, double diff[4]);
 
+/* No counterpart in the reference: a test hook. One FP32 V-cycle from the first level that a nodal plan
+ * cycles in one thread-block-cluster launch (the levels of at most 40000 nodes below the finest, with
+ * the dense bottom), on a seeded right-hand side, once through the per-level launches and once through
+ * the cluster kernel; *diff = max |cluster - per-level| / max |per-level| over every padded position.
+ * GBP_BAD_ARG when the plan has no such levels. */
+int gbp_plan_check_coarse_cycle(gbp_plan* plan, double* diff);
+
 /* MacProjector::setLevelBC(lev, nullptr, robin_a, robin_b, robin_f) for the GBP_BC_ROBIN sides
  * (incflo_compute_MAC_projected_velocities.cpp:116-123; data from incflo::make_robinBC_MFs,
  * src/boundary_conditions/incflo_set_bcs.cpp:121-192): cell arrays with one ghost layer whose
@@ -379,6 +431,15 @@ int gbp_mac_set_robin(gbp_plan* plan, const gbp_array4* robin_a, const gbp_array
 int gbp_mac_set_eb(gbp_plan* plan, const gbp_array4* vfrac, const gbp_array4* area_x, const gbp_array4* area_y,
                    const gbp_array4* area_z, const gbp_array4* fcent_x, const gbp_array4* fcent_y,
                    const gbp_array4* fcent_z);
+
+/* MacProjector::setEBInflowVelocity(lev, eb_vel)
+ * (src/convection/incflo_compute_MAC_projected_velocities.cpp:274-281): eb_vel (cells, 3 components,
+ * valid cells) is the velocity on each cut cell's embedded boundary. Its flux out of the fluid,
+ * sum_d eb_vel_d (ap_d(low face) - ap_d(high face)) V / h_d (the boundary's area vector from the area
+ * fractions set by gbp_mac_set_eb), is part of the divergence of the following projections. The plan
+ * keeps the per-cell flux, not the array. eb_vel == NULL removes it; gbp_mac_set_eb drops it.
+ * GBP_BAD_ARG without cut cells on the plan. */
+int gbp_mac_set_eb_inflow(gbp_plan* plan, const gbp_array4* eb_vel);
 
 /* incflo::ApplyCCProjection(density, umac, time, scaling_factor, incremental) for one level,
  * non-EB (src/projection/incflo_apply_cc_projection.cpp:199-487; option incflo.use_cc_proj):
@@ -465,15 +526,23 @@ int gbp_surrogate_train_pair(gbp_surrogate* s, const int dims[3], const int dom[
 int gbp_surrogate_predict(gbp_surrogate* s, const int dims[3], const void* x0, void* hout,
                           void* stream);
 /* append a training pair from a nodal plan after gbp_nodal_project: input from the plan's
- * right-hand side, sigma and phi_prev (nodal, may be NULL), target = the plan's phi */
+ * right-hand side, sigma and phi_prev (nodal, may be NULL), target = the plan's phi - phi_prev (the
+ * increment the network predicts on top of the previous solution; the plan's phi without one) */
 int gbp_surrogate_add_sample(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev);
+/* one training step on the pair of a nodal plan's last projection (built as gbp_surrogate_add_sample
+ * builds it, used once, not stored): forward + backward, and an Adam step when lr > 0; *loss (host,
+ * may be NULL) = the normalised MSE. Training on a stream of such pairs needs no sample storage. */
+int gbp_surrogate_train_step(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev, float lr,
+                             double* loss);
 int gbp_surrogate_num_samples(const gbp_surrogate* s);
 int gbp_surrogate_clear_samples(gbp_surrogate* s);
 /* steps (<= 60 per call) Adam steps on randomly drawn samples; losses[steps] (host) may be NULL */
 int gbp_surrogate_train(gbp_surrogate* s, int steps, float lr, unsigned long long seed,
                         float* losses, void* stream);
 /* attach (s != NULL) or detach a surrogate: the network runs on multigrid level `level` of the
- * plan (0 = finest); mode 1 = use with the bypass rule, 0 = off */
+ * plan (0 = finest); mode 1 = use with the bypass rule, 0 = off. With initial_guess = zero it predicts
+ * phi and competes with the zero start; with initial_guess = previous it predicts the increment on top
+ * of the plan's last solution and competes with that start. */
 int gbp_plan_set_surrogate(gbp_plan* plan, gbp_surrogate* s, int level, int mode);
 
 #ifdef __cplusplus

@@ -15,8 +15,11 @@ Schwartz, Barad, Colella & Ligocki 2015) with the conventions AMReX documents fo
     centroid in the two tangential directions, with weights |fc_t| (the centroid offset in cell
     widths); a neighbour face enters only when it is open (ap > 0), and the corner face f12 only when
     it and both f1 and f2 are open (otherwise the second direction's weight drops to 0);
-  * no interpolation on domain-boundary faces; the embedded boundary itself has no flux (homogeneous
-    Neumann, as the MAC projection sets it);
+  * no interpolation on domain-boundary faces; the embedded boundary itself is homogeneous Neumann
+    for phi; with an EB inflow velocity (MacProjector::setEBInflowVelocity,
+    src/convection/incflo_compute_MAC_projected_velocities.cpp:274-281) its flux out of the fluid,
+    u_eb . (int_EB n dA) = sum_d u_eb,d (ap_lo - ap_hi) area_d (the divergence theorem over the cut
+    cell's closed surface), is part of the divergence: b_c -= that flux;
   * operator (scaled by kappa V, which is how both sides are stored here):
         (A phi)_c = - sum_d [F_hi - F_lo],     b_c = - sum_d area_d (ap_hi u_hi - ap_lo u_lo)
     and the correction u_f -= beta_f * dphi/dn(centroid) on every open face;
@@ -175,8 +178,23 @@ class EBMac:
         A = sp.csr_matrix((vals, (rows, cols)), shape=(self.ncell, self.ncell))
         return A
 
-    def rhs(self, umac):
-        """b = -sum_d area (ap_hi u_hi - ap_lo u_lo) on face-centroid velocities."""
+    def eb_flux(self, eb_vel):
+        """Flux of the EB inflow velocity (3, nz, ny, nx) out of each cell's fluid through its
+        embedded boundary: sum_d u_d (ap_d(low) - ap_d(high)) area_d."""
+        n = self.n
+        f = np.zeros((n[2], n[1], n[0]))
+        for d in range(3):
+            sl_lo = [slice(None)] * 3
+            sl_hi = [slice(None)] * 3
+            sl_lo[2 - d] = slice(0, n[d])
+            sl_hi[2 - d] = slice(1, n[d] + 1)
+            f += np.asarray(eb_vel[d]) * (self.ap[d][tuple(sl_lo)] - self.ap[d][tuple(sl_hi)]) * self.area[d]
+        f[self.kap <= 0.0] = 0.0
+        return f
+
+    def rhs(self, umac, eb_vel=None):
+        """b = -sum_d area (ap_hi u_hi - ap_lo u_lo) on face-centroid velocities, minus the EB inflow
+        flux when an EB velocity is given."""
         n = self.n
         b = np.zeros((n[2], n[1], n[0]))
         for d in range(3):
@@ -193,6 +211,8 @@ class EBMac:
                 src[2 - d] = slice(0, 1)
                 hi[tuple(sl0)] = fl[tuple(src)]
             b -= hi - fl[tuple(sl_lo)]
+        if eb_vel is not None:
+            b -= self.eb_flux(eb_vel)
         b = b.reshape(-1)
         b[~self.active] = 0.0
         return b
@@ -252,9 +272,9 @@ class EBMac:
                 out[d][g[2], g[1], g[0]] = acc
         return out
 
-    def project(self, umac):
+    def project(self, umac, eb_vel=None):
         """Returns (corrected face velocities, phi (nz, ny, nx), rhs after the singular fix)."""
-        b = self.rhs(umac)
+        b = self.rhs(umac, eb_vel)
         phi, b = self.solve(b)
         gf = self.grad_face(phi)
         u = [np.array(x, dtype=np.float64, copy=True) for x in umac]
@@ -262,6 +282,6 @@ class EBMac:
             u[d] = u[d] - gf[d]
         return u, phi.reshape(self.n[2], self.n[1], self.n[0]), b
 
-    def divergence(self, umac):
-        """Max over fluid cells of |sum ap u area| / (kappa V): the discrete EB divergence."""
-        return self.norm(self.rhs(umac))
+    def divergence(self, umac, eb_vel=None):
+        """Max over fluid cells of |sum ap u area (+ EB flux)| / (kappa V): the discrete EB divergence."""
+        return self.norm(self.rhs(umac, eb_vel))

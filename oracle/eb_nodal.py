@@ -8,7 +8,11 @@ factory of the level). AMReX is not vendored; the discretisation is the Q1 finit
 to the fluid: every cell contributes sigma_c int_{fluid part} grad N_a . grad N_b to the operator and
 int_{fluid part} u_c . grad N_a to the right-hand side, with the integrals taken exactly from the cell's
 second moments of the fluid region (the EB factory's volume moments, as MLNodeLaplacian builds its
-integral arrays from them); the embedded boundary carries no flux (no EB inflow); nodes that touch no
+integral arrays from them); the embedded boundary carries no flux unless an EB inflow velocity is given
+(setEBInflowVelocity, src/projection/incflo_apply_nodal_projection.cpp:196-201): then the weak form's
+boundary term -int_EB (u_eb . n) N_a dA is added per cut cell as -F_c N_a(x_b), F_c = u_eb . int_EB n dA
+the boundary's outflow (area vector from the area fractions, eb.cylinder_boundary's dap) and x_b the
+boundary centroid (the EB factory's bcent), the one-point rule on the cell's boundary face; nodes that touch no
 fluid are not unknowns (phi = 0). The velocity correction takes grad phi of the trilinear interpolant
 at the fluid centroid of each cell (the cell centre for regular cells, the usual cell-average gradient).
 
@@ -155,7 +159,22 @@ class EBNodal:
                         node = self._node(idx[0], idx[1], idx[2])
                         np.add.at(b, node.reshape(-1), (w * vals).reshape(-1))
 
-    def assemble(self, sigma, u, u_ghost=None):
+    def _eb_inflow_rhs(self, b, eb_inflow):
+        """eb_inflow = (eb_vel, dap, bcent), each (3, nz, ny, nx): b_a -= F_c N_a(x_b) on every fluid
+        cell with a boundary face, F_c = sum_d u_d dap_d V / h_d."""
+        ev, dap, bc = (np.asarray(a, dtype=np.float64) for a in eb_inflow)
+        k, j, i = self.cell_k, self.cell_j, self.cell_i
+        V = self.h[0] * self.h[1] * self.h[2]
+        F = sum(ev[d][k, j, i] * dap[d][k, j, i] * (V / self.h[d]) for d in range(3))
+        N = self.nu[0] * self.nu[1] * self.nu[2]
+        a = np.arange(8)
+        w = np.ones((len(k), 8))
+        for d in range(3):
+            s = np.where((a >> d) & 1, 1.0, -1.0)
+            w *= 0.5 + s[None, :] * bc[d][k, j, i][:, None]
+        b -= np.bincount(self.ids.reshape(-1), weights=(F[:, None] * w).reshape(-1), minlength=N)
+
+    def assemble(self, sigma, u, u_ghost=None, eb_inflow=None):
         """Sparse operator A (all node positions, unknowns and not) and right-hand side b."""
         N = self.nu[0] * self.nu[1] * self.nu[2]
         s = sigma[self.cell_k, self.cell_j, self.cell_i]
@@ -163,16 +182,18 @@ class EBNodal:
         cols = np.tile(self.ids, (1, 8)).reshape(-1)
         vals = (s[:, None, None] * self.Ku[self.inv]).reshape(-1)
         A = sp.csr_matrix((vals, (rows, cols)), shape=(N, N))
-        b = self.rhs(u, u_ghost)
+        b = self.rhs(u, u_ghost, eb_inflow)
         return A, b
 
-    def rhs(self, u, u_ghost=None):
+    def rhs(self, u, u_ghost=None, eb_inflow=None):
         N = self.nu[0] * self.nu[1] * self.nu[2]
         uc = u[:, self.cell_k, self.cell_j, self.cell_i]  # (3, ncell)
         contrib = np.einsum("cad,dc->ca", self.Gu[self.inv], uc)
         b = np.bincount(self.ids.reshape(-1), weights=contrib.reshape(-1), minlength=N)
         if u_ghost is not None:
             self._inflow_rhs(b, u_ghost)
+        if eb_inflow is not None:
+            self._eb_inflow_rhs(b, eb_inflow)
         return b
 
     def apply(self, sigma, phi_u, chunk=1 << 17):
@@ -203,10 +224,10 @@ class EBNodal:
         del n
         return out
 
-    def residual_norm(self, sigma, u, phi_all, u_ghost=None):
+    def residual_norm(self, sigma, u, phi_all, u_ghost=None, eb_inflow=None):
         """max |b - A phi| / (fluid dual volume) over the unknowns, relative to the same norm of b
         (after the consistency shift on singular systems): a check of a solution at any size."""
-        b = self.rhs(u, u_ghost)
+        b = self.rhs(u, u_ghost, eb_inflow)
         w = self.dual_volume()
         unk = self.active & ~self.fixed
         if self.singular:
@@ -215,9 +236,9 @@ class EBNodal:
         bn = np.max(np.abs(b[unk]) / w[unk])
         return float(np.max(np.abs(r[unk]) / w[unk]) / bn) if bn > 0 else 0.0
 
-    def project(self, sigma, u, u_ghost=None):
+    def project(self, sigma, u, u_ghost=None, eb_inflow=None):
         """Returns dict(phi (all node positions), u (projected), grad (3, nz, ny, nx), b)."""
-        A, b = self.assemble(sigma, u, u_ghost)
+        A, b = self.assemble(sigma, u, u_ghost, eb_inflow)
         unk = np.nonzero(self.active & ~self.fixed)[0]
         Aa = A[unk][:, unk].tocsc()
         ba = b[unk]

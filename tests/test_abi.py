@@ -34,7 +34,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_version_and_status_strings(lib):
-    assert lib.gbp_abi_version() == 2
+    assert lib.gbp_abi_version() == 3
     assert lib.gbp_status_string(A.GBP_NOT_CONVERGED) == b"not converged"
     assert lib.gbp_status_string(99) == b"unknown status"
 

@@ -115,3 +115,33 @@ def test_eb_get_fluxes_are_the_projection_correction(gpu_lib):
     for d in range(3):
         corr = ut[d].cpu().numpy() - umac[d]
         np.testing.assert_allclose(flux[d].cpu().numpy(), corr, rtol=0, atol=1e-13 * max(np.abs(corr).max(), 1e-300))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_eb_inflow_velocity_matches_oracle(gpu_lib, precision):
+    """MacProjector::setEBInflowVelocity: the cylinder of the channel blows into the fluid at unit speed
+    (incflo's eb_flow.vel_mag); phi and the projected face velocities match the cut-cell oracle with the
+    boundary flux in its divergence; removing the inflow gives the plain cut-cell projection again."""
+    n, ext, bclo, bchi, geo, beta, umac, m = _case("channel")
+    c, r = CASES["channel"][4], CASES["channel"][5]
+    bd = eb.cylinder_boundary(n, (0, 0, 0), ext, (c[0], c[1], 0.0), r)
+    ev = eb.eb_inflow_velocity(bd["bnorm"], vel_mag=1.0)
+    un_or, phi_or, _ = m.project(umac, eb_vel=ev)
+    mp = _gpu_projector(n, ext, bclo, bchi, geo, beta, precision)
+    mp.setEBInflowVelocity(0, cuda(ev))
+    ut = [cuda(u) for u in umac]
+    mp.setUMAC(ut)
+    phi = cuda(np.zeros((n[2], n[1], n[0])))
+    st = mp.project(rtol=1e-12, atol=0.0, phi=phi, phi_guess=False)
+    assert st["status"] == 0 and st["final_rel_resid"] <= 1e-12
+    assert rel_l2(phi.cpu().numpy(), phi_or) <= 1e-9
+    assert m.divergence([u.cpu().numpy() for u in ut], eb_vel=ev) <= 1e-9 * m.divergence(umac, eb_vel=ev)
+    for d in range(3):
+        open_ = m.ap[d] > 0
+        np.testing.assert_allclose(ut[d].cpu().numpy()[open_], un_or[d][open_], rtol=0,
+                                   atol=1e-9 * np.abs(un_or[d]).max())
+    mp.setEBInflowVelocity(0, None)
+    mp.setUMAC([cuda(u) for u in umac])
+    phi2 = cuda(np.zeros((n[2], n[1], n[0])))
+    assert mp.project(rtol=1e-12, atol=0.0, phi=phi2, phi_guess=False)["status"] == 0
+    assert rel_l2(phi2.cpu().numpy(), m.project(umac)[1]) <= 1e-9

@@ -246,3 +246,35 @@ def test_whole_row_level_kernels_match_plain_kernels(gpu_lib, case):
     print(f"\n{n}: jacobi {diff[0]:.2e} resid {diff[1]:.2e} resid+restrict {diff[2]:.2e} "
           f"prolong+jacobi {diff[3]:.2e}")
     assert max(diff) <= 1e-5
+
+
+@pytest.mark.parametrize("case", [((64, 64, 64), (1.0, 1.0, 1.0), (P, P, N), (P, P, N)),
+                                  ((48, 32, 64), (1.2, 0.8, 1.6), (D, N, I), (N, D, N)),
+                                  ((32, 32, 32), (1.0, 1.0, 1.0), (P, P, P), (P, P, P))],
+                         ids=["64-periodic-xy", "48x32x64-mixed", "32-periodic"])
+def test_cluster_coarse_cycle_matches_per_level_launches(gpu_lib, case):
+    """The small levels of the hierarchy run as one thread-block-cluster launch per V-cycle. On a seeded
+    right-hand side, one V-cycle from the first such level agrees with the per-level launches to FP32
+    rounding (the prolongation sums in another order); an indexing or synchronisation fault would differ
+    by O(1). A projection through the cluster path then matches the oracle (the parity tests run it in
+    both precisions on every plan with such levels)."""
+    import ctypes
+
+    from incflo_gb300 import _abi
+
+    n, ext, bclo, bchi = case
+    g, sigma, vel = nodal_case(n, ext, bclo, bchi, seed=11)
+    vel_or, phi_or, _, _ = O.nodal_project(g, sigma, vel, rtol=1e-13)
+    for precision in ("mixed", "fp64"):
+        vt = cuda(vel)
+        proj = NodalProjector(vt, cuda(sigma), Geometry(n, (0, 0, 0), ext),
+                              options=make_options(0, precision=precision))
+        proj.setDomainBC(bclo, bchi)
+        st = proj.project(rtol=1e-12, atol=0.0)
+        assert st["status"] == 0
+        phi = proj.getPhi().cpu().numpy()[: g.node_shape[0], : g.node_shape[1], : g.node_shape[2]]
+        assert rel_l2(phi, phi_or) <= 1e-9
+    diff = ctypes.c_double()
+    _abi.check(_abi.load().gbp_plan_check_coarse_cycle(proj._plan().ptr, ctypes.byref(diff)), "check_coarse_cycle")
+    print(f"\n{n}: cluster vs per-level V-cycle {diff.value:.2e}")
+    assert diff.value <= 1e-5

@@ -135,3 +135,72 @@ def test_zero_network_is_bypassed(gpu_lib):
     p = _projector(32, 5, s, level=1)
     st = p.project()
     assert st["warm_start"] == 2 and st["status"] == 0 and st["final_rel_resid"] <= 1e-10
+
+
+def _sequence_projector(case, initial_guess, surrogate=None, level=1):
+    geom = Geometry(case["n"], case["lo"], case["hi"])
+    opts = make_options(0, precision="mixed", mg_rtol=1e-10, mg_atol=0.0, initial_guess=initial_guess)
+    p = NodalProjector(torch.from_numpy(synth.with_ghosts(case["vel"])).cuda(),
+                       torch.from_numpy(1.0 / case["rho"]).cuda(), geom, options=opts)
+    p.setDomainBC(["Periodic", "Periodic", "Neumann"], ["Periodic", "Periodic", "Neumann"])
+    if surrogate is not None:
+        p.setSurrogate(surrogate, level)
+    return p
+
+
+def _run_sequence(n, initial_guess, surrogate=None, steps=4, seed=31):
+    """successive projections of a slowly displaced interface on one plan; returns stats and phis"""
+    from incflo_gb300.projection import NodalProjector as NP
+    NP._plans.clear()  # a fresh plan: no last solution from other tests
+    out = []
+    for case in synth.rt_sequence(n, seed=seed, steps=steps):
+        p = _sequence_projector(case, initial_guess, surrogate)
+        st = p.project()
+        assert st["status"] == 0 and st["final_rel_resid"] <= 1e-10
+        out.append((st, p.getPhi().cpu().numpy().copy()))
+    NP._plans.clear()
+    return out
+
+
+def test_previous_phi_start_saves_vcycles_on_a_sequence(gpu_lib):
+    """initial_guess = previous: each projection of a time sequence starts from the plan's last phi, reaches
+    the same tolerance in fewer V-cycles, and gives the same phi as the zero start (to the tolerance)."""
+    zero = _run_sequence(64, "zero")
+    prev = _run_sequence(64, "previous")
+    assert prev[0][0]["prev_rel_resid"] == 0.0  # nothing before the first step
+    for (sz, pz), (sp, pp) in zip(zero[1:], prev[1:]):
+        assert 0.0 < sp["prev_rel_resid"] < 0.2
+        assert sp["vcycles"] < sz["vcycles"]
+        assert np.linalg.norm(pp - pz) <= 1e-8 * np.linalg.norm(pz)
+
+
+def test_learned_increment_is_taken_only_when_it_beats_the_previous_phi(gpu_lib):
+    """The warm start on top of the previous solution: the network predicts the increment, the Galerkin-
+    scaled candidate is taken only when its residual is below the previous-phi start's, and the solve
+    reaches the same phi either way. A network with zero weights predicts nothing and is bypassed; a
+    briefly trained one is used or bypassed by that rule."""
+    s0 = Surrogate(seed=4)
+    s0.set_params(np.zeros(s0.num_params, np.float32))
+    seq = _run_sequence(64, "previous", surrogate=s0, steps=3)
+    # bypassed (2) on the first attempts; after two bypasses in a row the plan skips (3) the next ones
+    assert seq[0][0]["warm_start"] == 2 and seq[1][0]["warm_start"] == 2
+    assert all(st["warm_start"] in (2, 3) and st["status"] == 0 for st, _ in seq)
+    # a few streamed training steps on sequence pairs (increments), then the rule on a held-out sequence
+    from incflo_gb300.projection import NodalProjector as NP
+    s = Surrogate(seed=5)
+    NP._plans.clear()
+    prev = None
+    losses = []
+    for case in synth.rt_sequence(64, seed=7, steps=6):
+        p = _sequence_projector(case, "zero")
+        assert p.project()["status"] == 0
+        losses.append(s.train_step(p, prev, lr=1e-3))
+        prev = p.getPhi().clone()
+    assert np.isfinite(losses).all()
+    ref = _run_sequence(64, "previous", steps=3)
+    got = _run_sequence(64, "previous", surrogate=s, steps=3)
+    for (sr, pr), (sg, pg) in zip(ref[1:], got[1:]):
+        assert sg["warm_start"] in (1, 2, 3)
+        if sg["warm_start"] == 1:
+            assert sg["warm_rel_resid"] < sg["prev_rel_resid"]
+        assert np.linalg.norm(pg - pr) <= 1e-8 * np.linalg.norm(pr)

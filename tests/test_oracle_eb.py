@@ -110,3 +110,48 @@ def test_cut_cell_generator_fractions():
     for k in ("fcx", "fcy", "fcz"):
         assert np.abs(g[k]).max() <= 0.5
     np.testing.assert_allclose(g["apz"][0], g["vfrac"][0], rtol=0, atol=1e-15)
+
+
+def test_eb_inflow_projection_conserves_the_boundary_source():
+    """A cylinder that blows into a channel at unit speed (setEBInflowVelocity from eb_flow.vel_mag):
+    the projected face velocities carry no divergence once the boundary's flux is counted, and what
+    leaves through the outflow side equals what the boundary puts in (the area vectors of the cut cells,
+    from the area fractions, close around the body)."""
+    n, ext, c, r = (48, 16, 4), (3.0, 1.0, 0.25), (1.0, 0.5), 0.125
+    h = [ext[d] / n[d] for d in range(3)]
+    geo = eb.cylinder(n, (0, 0, 0), ext, (c[0], c[1], 0.0), r, small_volfrac=1e-4)
+    bd = eb.cylinder_boundary(n, (0, 0, 0), ext, (c[0], c[1], 0.0), r, small_volfrac=1e-4)
+    ev = eb.eb_inflow_velocity(bd["bnorm"], vel_mag=1.0)
+    ap = [geo["apx"], geo["apy"], geo["apz"]]
+    fc = [geo["fcx"], geo["fcy"], geo["fcz"]]
+    beta = [np.ones(a.shape) for a in ap]
+    m = EBMac(n, h, (N, N, P), (D, N, P), geo["vfrac"], ap, fc, beta)
+    umac = [np.zeros(a.shape) for a in ap]
+    un, phi, b = m.project(umac, eb_vel=ev)
+    assert m.divergence(un, eb_vel=ev) <= 1e-11 * m.divergence(umac, eb_vel=ev)
+    source = -m.eb_flux(ev).sum()
+    out = (un[0][:, :, -1] * ap[0][:, :, -1]).sum() * h[1] * h[2]
+    assert source > 0.9 * 2 * np.pi * r * ext[2]
+    assert abs(out - source) <= 1e-10 * source
+    # the area vectors close: a uniform velocity through the body carries no net flux
+    assert abs(m.eb_flux(np.broadcast_to(np.array([1.0, 0.4, 0.0]).reshape(3, 1, 1, 1), ev.shape)).sum()) <= 1e-13
+
+
+def test_eb_inflow_velocity_rule():
+    """incflo::set_eb_velocity: vel_mag blows along -n; a normal filter keeps only the cells whose
+    boundary normal is within the tolerance of -normal; `velocity` is taken as given on cut cells."""
+    n, ext = (32, 16, 2), (2.0, 1.0, 0.125)
+    bd = eb.cylinder_boundary(n, (0, 0, 0), ext, (1.0, 0.5, 0.0), 0.2)
+    cut = (bd["bnorm"] ** 2).sum(axis=0) > 0
+    v = eb.eb_inflow_velocity(bd["bnorm"], vel_mag=2.0)
+    np.testing.assert_allclose(np.sqrt((v ** 2).sum(axis=0))[cut], 2.0, rtol=1e-12)
+    assert np.all(v[:, ~cut] == 0.0)
+    # only the cells facing -x (normal out of the fluid along +x, i.e. the body's upstream side); incflo
+    # compares n . normal with -1 +- the tolerance in radians (its rule, kept as it is)
+    tol = np.radians(30.0)
+    vf = eb.eb_inflow_velocity(bd["bnorm"], vel_mag=1.0, normal=(-1.0, 0.0, 0.0), normal_tol_deg=30.0)
+    kept = (vf ** 2).sum(axis=0) > 0
+    assert kept.any() and np.all(bd["bnorm"][0][kept] >= 1.0 - tol - 1e-6)
+    assert np.all(bd["bnorm"][0][cut & ~kept] < 1.0 - tol + 1e-6)
+    vc = eb.eb_inflow_velocity(bd["bnorm"], velocity=(0.5, 0.0, -1.0))
+    assert np.all(vc[0][cut] == 0.5) and np.all(vc[2][cut] == -1.0) and np.all(vc[:, ~cut] == 0.0)

@@ -143,3 +143,36 @@ def test_residual_norm_checks_a_solution():
     assert o.residual_norm(sig, u, r["phi"], vg) <= 1e-11
     bad = r["phi"] * (1 + 1e-6)
     assert o.residual_norm(sig, u, bad, vg) >= 1e-8
+
+
+def test_eb_inflow_term_distributes_the_boundary_flux():
+    """The EB inflow term of the right-hand side: per cut cell the boundary's outflow F_c spread over the
+    eight corners by the trilinear weights at the boundary centroid (they sum to one), so the term adds
+    -sum F_c over all nodes; it is linear in the boundary velocity and absent at zero velocity; the
+    boundary centroids lie on the circle."""
+    n, ext, c, r = (32, 16, 4), (2.0, 1.0, 0.25), (0.7, 0.5), 0.2
+    h = [ext[d] / n[d] for d in range(3)]
+    M = eb.cylinder_moments(n, (0, 0, 0), ext, (c[0], c[1], 0.0), r, small_volfrac=1e-4)
+    bd = eb.cylinder_boundary(n, (0, 0, 0), ext, (c[0], c[1], 0.0), r, small_volfrac=1e-4)
+    o = EBNodal(n, h, (N, N, P), (D, N, P), M)
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((3, n[2], n[1], n[0]))
+    ev = eb.eb_inflow_velocity(bd["bnorm"], vel_mag=1.5)
+    b0 = o.rhs(u)
+    b1 = o.rhs(u, eb_inflow=(ev, bd["dap"], bd["bcent"]))
+    b2 = o.rhs(u, eb_inflow=(2.0 * ev, bd["dap"], bd["bcent"]))
+    V = h[0] * h[1] * h[2]
+    F = sum(ev[d] * bd["dap"][d] * V / h[d] for d in range(3))
+    F[M[..., 0, 0, 0] <= 0] = 0.0
+    assert abs((b1 - b0).sum() + F.sum()) <= 1e-12 * np.abs(F).sum()
+    np.testing.assert_allclose(b2 - b0, 2.0 * (b1 - b0), rtol=0, atol=1e-13 * np.abs(b1 - b0).max())
+    assert np.array_equal(o.rhs(u, eb_inflow=(0.0 * ev, bd["dap"], bd["bcent"])), b0)
+    # blowing out of the whole surface at speed 1.5: total source = 1.5 x the boundary area
+    area = sum((bd["dap"][d] * V / h[d]) ** 2 for d in range(3)) ** 0.5
+    assert abs(-F.sum() - 1.5 * area.sum()) <= 1e-12 * area.sum()
+    kk, jj, ii = np.nonzero(area > 0)
+    xb = (ii + 0.5 + bd["bcent"][0][kk, jj, ii]) * h[0]
+    yb = (jj + 0.5 + bd["bcent"][1][kk, jj, ii]) * h[1]
+    rad = np.hypot(xb - c[0], yb - c[1])
+    own = rad < r * 1.2  # cells whose face was closed by small-cell removal have no arc of their own
+    assert np.abs(rad[own] - r).max() <= 0.02 * r
