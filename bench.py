@@ -233,14 +233,16 @@ def parity_cfg1(dev):
 
 
 def run_amr(args, dev, steps=3, warmup=1):
-    """ms per two-level composite projection (mixed form): base n^3 + a ratio-2 band z in [3/8, 5/8)
-    in 64^3 fine boxes; inputs restored before each call (outside the timed region)."""
+    """ms per two-level composite projection (mixed form): base n^3 variable-density interface, fine level
+    (ratio 2) from tagging: cells within +-0.1 of the interface or with |vorticity| above its 90th
+    percentile, blocking_factor 32, max_grid_size 64 (synth.rt_amr_tagged); inputs restored before each
+    call (outside the timed region)."""
     import numpy as np
     import torch
 
     from incflo_gb300 import AmrNodalProjector, Geometry, make_options, synth
 
-    w = synth.variable_density_rt_amr(args.n)
+    w = synth.rt_amr_tagged(args.n)
     b = w["base"]
     n = b["n"]
     geom = Geometry(n, b["lo"], b["hi"])
@@ -251,16 +253,9 @@ def run_amr(args, dev, steps=3, warmup=1):
     vel_c = vel0.clone()
     gp_c = torch.zeros_like(vel0)
     p_c = torch.zeros((n[2] + 1, n[1] + 1, n[0] + 1), dtype=torch.float64, device=dev)
-    zlo = w["zlo"]
-    vf0 = torch.from_numpy(w["vel_f"]).to(dev)
-    rf = torch.from_numpy(np.ascontiguousarray(w["rho_f"])).to(dev)
-
-    def sl(t, lo, hi, e=0):
-        return t[..., lo[2] - zlo:hi[2] - zlo + 1 + e, lo[1]:hi[1] + 1 + e, lo[0]:hi[0] + 1 + e]
-
-    vel_f = [sl(vf0, lo, hi).clone() for lo, hi in w["boxes"]]
-    vel_f0 = [v.clone() for v in vel_f]
-    rho_f = [sl(rf, lo, hi).contiguous() for lo, hi in w["boxes"]]
+    vel_f0 = [torch.from_numpy(v).to(dev) for v in w["vel_f"]]
+    vel_f = [v.clone() for v in vel_f0]
+    rho_f = [torch.from_numpy(r).to(dev) for r in w["rho_f"]]
     gp_f = [torch.zeros_like(v) for v in vel_f]
     p_f = [torch.zeros((hi[2] - lo[2] + 2, hi[1] - lo[1] + 2, hi[0] - lo[0] + 2), dtype=torch.float64, device=dev)
            for lo, hi in w["boxes"]]
@@ -278,12 +273,70 @@ def run_amr(args, dev, steps=3, warmup=1):
         if i >= warmup:
             times.append(st["ms_total"])
     fine_cells = sum((hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) for lo, hi in w["boxes"])
-    return {"workload": f"{args.n}^3 base + ratio-2 band z in [3/8, 5/8) of the whole x/y extent "
-                        f"({len(w['boxes'])} fine boxes of 64^3, {fine_cells} fine cells), composite nodal "
-                        f"projection, FP32 V-cycles inside FP64 refinement, rtol {args.rtol:g}",
-            "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
-            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"],
-            "device_bytes": proj.device_bytes()}
+    zlo = min(lo[2] for lo, _ in w["boxes"])
+    zhi = max(hi[2] for _, hi in w["boxes"])
+    out = {"workload": f"{args.n}^3 base + ratio-2 fine level from tagging (interface +-0.1 or |vorticity| > "
+                       f"90th percentile; blocking_factor 32, max_grid_size 64): {len(w['boxes'])} fine boxes, "
+                       f"{fine_cells} fine cells, fine z {zlo}..{zhi}; composite nodal projection, FP32 V-cycles "
+                       f"inside FP64 refinement, rtol {args.rtol:g}",
+           "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
+           "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"],
+           "device_bytes": proj.device_bytes()}
+    del proj
+    if not args.no_parity:
+        out["parity"] = amr_parity(dev)
+    return out
+
+
+def amr_parity(dev, n=16):
+    """phi against the composite FE oracle (scipy direct solve) on the same construction at a base the
+    oracle solves in seconds (n^3, the same tagging, box rules scaled to blocking_factor 8 and
+    max_grid_size 16), plain FP64 and mixed forms, rtol 1e-12."""
+    import numpy as np
+    import torch
+
+    from incflo_gb300 import AmrNodalProjector, Geometry, make_options, synth
+    from oracle.amr_nodal import CompositeNodal as Oracle
+
+    w = synth.rt_amr_tagged(n, blocking=8, max_grid=16)
+    b = w["base"]
+    boxes = w["boxes"]
+    nc = b["n"]
+    nf = [2 * v for v in nc]
+    fm = np.zeros((nf[2], nf[1], nf[0]), bool)
+    rho_f = np.ones((nf[2], nf[1], nf[0]))
+    u_f = np.zeros((3, nf[2], nf[1], nf[0]))
+    for (lo, hi), r, v in zip(boxes, w["rho_f"], w["vel_f"]):
+        sl = (slice(lo[2], hi[2] + 1), slice(lo[1], hi[1] + 1), slice(lo[0], hi[0] + 1))
+        fm[sl] = True
+        rho_f[sl] = r
+        u_f[(slice(None),) + sl] = v
+    ref = Oracle(nc, [1.0 / v for v in nc], b["bclo"], b["bchi"], fm).project(1.0 / b["rho"], 1.0 / rho_f, b["vel"],
+                                                                            u_f)
+    geom = Geometry(nc, b["lo"], b["hi"])
+    out = {"base": n, "fine_boxes": len(boxes), "oracle": "scipy direct solve of the composite Q1 system"}
+    for precision in ("fp64", "mixed"):
+        proj = AmrNodalProjector(geom, b["bclo"], b["bchi"], boxes,
+                                 options=make_options(0, precision=precision, mg_rtol=1e-12, mg_atol=0.0))
+        vc = torch.from_numpy(np.ascontiguousarray(b["vel"])).to(dev)
+        gc = torch.zeros_like(vc)
+        pc = torch.zeros((nc[2] + 1, nc[1] + 1, nc[0] + 1), dtype=torch.float64, device=dev)
+        vf = [torch.from_numpy(v).to(dev) for v in w["vel_f"]]
+        gf = [torch.zeros_like(v) for v in vf]
+        pf = [torch.zeros((hi[2] - lo[2] + 2, hi[1] - lo[1] + 2, hi[0] - lo[0] + 2), dtype=torch.float64,
+                          device=dev) for lo, hi in boxes]
+        st = proj.apply(vc, torch.from_numpy(np.ascontiguousarray(b["rho"])).to(dev), gc, pc, vf,
+                        [torch.from_numpy(r).to(dev) for r in w["rho_f"]], gf, pf, scaling_factor=1.0)
+        err_c = rel_l2(pc.cpu().numpy(), ref["phi_c"])
+        num = den = 0.0
+        for t, (lo, hi) in zip(pf, boxes):
+            r = ref["phi_f"][lo[2]:hi[2] + 2, lo[1]:hi[1] + 2, lo[0]:hi[0] + 2]
+            num += float(((t.cpu().numpy() - r) ** 2).sum())
+            den += float((r ** 2).sum())
+        out[precision] = {"status": st["status"], "phi_rel_l2_coarse": float(f"{err_c:.3e}"),
+                          "phi_rel_l2_fine": float(f"{(num / den) ** 0.5:.3e}")}
+        del proj
+    return out
 
 
 def run_mac(args, dev, steps=5, warmup=3):
@@ -649,6 +702,14 @@ def run_ours(args, ws, rank, local):
         eb_nodal = run_eb_nodal(args, dev)
     tensor = None if args.no_tensor else run_tensor(args, dev)
     mac = None if args.no_mac else run_mac(args, dev)
+    # the warm start where it has a previous solution: successive projections of a slowly displaced
+    # interface (held-out seed), zero start vs previous-phi start vs previous phi + the network's increment
+    if warm is not None and not args.no_sequence:
+        from incflo_gb300.train_surrogate import evaluate_sequence
+
+        warm["sequence"] = {"workload": f"{n}^3, 8 successive projections of synth.rt_sequence(seed 7777), "
+                                        "timed: the 7 that have a previous phi",
+                            **evaluate_sequence(surrogate, n, 7777, steps=8, level=args.warm_level)}
 
     cpu = None
     parity = None
@@ -698,9 +759,9 @@ def run_ours(args, ws, rank, local):
                    "speedup_vs_plain_fp64": round(fp64_ms / per_step, 3)},
         "warm_start": warm,
         "wall_ms_per_step": round(wall_mixed * 1e3 / len(ms_mixed), 3),
-        "roofline": {"bound": "hbm", "kernel": "k_sweep32t<0> (FP32 Jacobi sweep, level 0)", "achieved": round(ach, 1),
+        "roofline": {"bound": "hbm", "kernel": "k_vsweep32<0> (FP32 Jacobi sweep, level 0, whole-row TMA tiles)", "achieved": round(ach, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4),
-                     "traffic": ncu_traffic("k_sweep32t_nodal_256.md"), "peak_kind": peak_kind,
+                     "traffic": ncu_traffic("k_vsweep32_nodal_256.md"), "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": bytes_k.value, "ms_per_launch": round(ms_k.value, 5)},
         "roofline_fp64_jacobi": {"achieved_gbs": round(ach64, 1), "frac_hbm": round(ach64 / peak, 4),
                                  "ms_per_launch": round(ms64.value, 5)},
@@ -729,7 +790,7 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--inner", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=5)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-amr", action="store_true")
     ap.add_argument("--no-eb", action="store_true")
@@ -738,6 +799,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-warm-start", action="store_true")
+    ap.add_argument("--no-sequence", action="store_true")
     ap.add_argument("--warm-level", type=int, default=1)
     args = ap.parse_args()
     ws, rank, local = dist_init()

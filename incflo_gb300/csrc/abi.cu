@@ -828,11 +828,11 @@ int gbp_plan_check_level_kernels(gbp_plan* p, double diff[4])
 
 int gbp_plan_check_coarse_cycle(gbp_plan* p, double* diff)
 {
-    if (!p || !p->nodal || !diff) {
-        set_error("gbp_plan_check_coarse_cycle: needs a nodal plan and an output");
+    if (!p || !diff) {
+        set_error("gbp_plan_check_coarse_cycle: needs a plan and an output");
         return GBP_BAD_ARG;
     }
-    return p->nodal->check_coarse_cycle(diff);
+    return p->nodal ? p->nodal->check_coarse_cycle(diff) : p->mac->check_coarse_cycle(diff);
 }
 
 int gbp_nodal_set_eb(gbp_plan* p, const gbp_array4* moments)

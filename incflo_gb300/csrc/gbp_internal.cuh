@@ -138,6 +138,31 @@ __device__ __forceinline__ void store_node(T* a, const NodalGeom& g, int i, int 
     }
 }
 
+// store_node with the alias lists unrolled (at most 3 positions per direction, on levels of 2 cells): for kernels
+// where most nodes lie on a periodic seam (the smallest levels), the rolled candidate loops cost more
+// than the stencil
+template <typename T>
+__device__ __forceinline__ void store_node_unrolled(T* a, const NodalGeom& g, int i, int j, int k, T v)
+{
+    int xs[3], ys[3], zs[3];
+    const int nx = node_aliases(i, g.n[0], g.per[0], xs);
+    const int ny = node_aliases(j, g.n[1], g.per[1], ys);
+    const int nz = node_aliases(k, g.n[2], g.per[2], zs);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (c >= nz) break;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            if (b >= ny) break;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q >= nx) break;
+                a[pidx(g.sy, g.sz, xs[q], ys[b], zs[c])] = v;
+            }
+        }
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void store_cell(T* a, const CellGeom& g, int i, int j, int k, T v)
 {
@@ -189,6 +214,27 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, doubl
     unsigned long long bits = (unsigned long long)__double_as_longlong(v);
     if (v != v) bits = 0x7ff8000000000000ull;
     atomicMax(dst, bits);
+}
+
+__device__ __forceinline__ void cluster_barrier()
+{
+    // every thread of every CTA of the cluster arrives; release / acquire order the global stores of
+    // one phase before the loads of the next at cluster scope
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+__device__ __forceinline__ unsigned cluster_nctas()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
 }
 
 // |v| as an order-preserving integer key: for non-negative doubles the IEEE bit pattern orders like

@@ -33,23 +33,34 @@ __device__ __forceinline__ const double* mac_acoef<double>(const CellGeom& g) { 
 template <>
 __device__ __forceinline__ const float* mac_acoef<float>(const CellGeom& g) { return g.a32; }
 
+// Loads of the operator: plain (the per-level kernels) or L2-coherent (the cluster kernel, whose CTAs read
+// what other CTAs wrote before a cluster barrier)
+struct MacLdPlain {
+    template <typename T>
+    __device__ __forceinline__ static T ld(const T* p) { return *p; }
+};
+struct MacLdCg {
+    __device__ __forceinline__ static float ld(const float* p) { return __ldcg(p); }
+    __device__ __forceinline__ static double ld(const double* p) { return __ldcg(p); }
+};
+
 // (A x)_p = sum over faces of w beta (x_p - x_nb) [+ alpha a V x_p]; diag and the neighbour sum for
 // the Gauss-Seidel update x_p = (b_p + offsum) / diag
-template <typename T>
+template <typename T, typename LD = MacLdPlain>
 __device__ __forceinline__ T mac_Ax(const CellGeom& g, const T* __restrict__ x, const T* __restrict__ bx,
                                     const T* __restrict__ by, const T* __restrict__ bz, long long p, T& diag,
                                     T& offsum)
 {
-    const T xc = x[p];
+    const T xc = LD::ld(x + p);
     const T wx = (T)g.w[0], wy = (T)g.w[1], wz = (T)g.w[2];
     const T b0 = bx[p] * wx, b1 = bx[p + 1] * wx;
     const T b2 = by[p] * wy, b3 = by[p + g.sy] * wy;
     const T b4 = bz[p] * wz, b5 = bz[p + g.sz] * wz;
+    const T xw = LD::ld(x + p - 1), xe = LD::ld(x + p + 1), xs = LD::ld(x + p - g.sy), xn = LD::ld(x + p + g.sy);
+    const T xb = LD::ld(x + p - g.sz), xt = LD::ld(x + p + g.sz);
     diag = ((b0 + b1) + (b2 + b3)) + (b4 + b5);
-    offsum = ((b0 * x[p - 1] + b1 * x[p + 1]) + (b2 * x[p - g.sy] + b3 * x[p + g.sy])) +
-             (b4 * x[p - g.sz] + b5 * x[p + g.sz]);
-    T ax = ((b0 * (xc - x[p - 1]) + b1 * (xc - x[p + 1])) + (b2 * (xc - x[p - g.sy]) + b3 * (xc - x[p + g.sy]))) +
-           (b4 * (xc - x[p - g.sz]) + b5 * (xc - x[p + g.sz]));
+    offsum = ((b0 * xw + b1 * xe) + (b2 * xs + b3 * xn)) + (b4 * xb + b5 * xt);
+    T ax = ((b0 * (xc - xw) + b1 * (xc - xe)) + (b2 * (xc - xs) + b3 * (xc - xn))) + (b4 * (xc - xb) + b5 * (xc - xt));
     const T* ac = mac_acoef<T>(g);
     if (ac) {
         diag += ac[p];
@@ -597,6 +608,171 @@ template void mac_bottom_dense<double>(const CellGeom&, const double*, const uns
                                        int, cudaStream_t);
 template void mac_bottom_dense<float>(const CellGeom&, const double*, const unsigned char*, const float*, float*, int,
                                       cudaStream_t);
+
+// ------------------------------------------------------------------------------------------------
+// coarse V-cycle in one cluster (the small levels of the MAC / ABecLaplacian hierarchy)
+template <typename T>
+__device__ __forceinline__ void mc_rbgs(const CellGeom& g, const T* bx, const T* by, const T* bz, const T* b, T* x,
+                                        int color, long long t0, long long dt)
+{
+    const int hx = (g.n[0] + 1) / 2;
+    const long long n = (long long)g.n[1] * g.n[2] * hx;
+    for (long long t = t0; t < n; t += dt) {
+        const long long row = t / hx;
+        const int k = (int)(row / g.n[1]);
+        const int j = (int)(row - (long long)k * g.n[1]);
+        const int i = 2 * (int)(t - row * hx) + ((j + k + color) & 1);
+        if (i >= g.n[0]) continue;
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        T diag, off;
+        (void)mac_Ax<T, MacLdCg>(g, x, bx, by, bz, p, diag, off);
+        const T v = diag != T(0) ? (__ldcg(b + p) + off) / diag : T(0);
+        store_cell(x, g, i, j, k, v);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kMacCoarseThreads) k_mac_coarse_vcycle(MacCoarseCycle<T> a)
+{
+    extern __shared__ double bb[];
+    const long long t0 = (long long)cluster_rank() * blockDim.x + threadIdx.x;
+    const long long dt = (long long)cluster_nctas() * blockDim.x;
+    const int L = a.nl;
+    for (int q = 0; q + 1 < L; ++q) {
+        const CellGeom& g = a.g[q];
+        for (long long t = t0; t < g.count; t += dt) a.x[q][t] = T(0);
+        cluster_barrier();
+        for (int p = 0; p < a.nu1; ++p) {
+            mc_rbgs<T>(g, a.bx[q], a.by[q], a.bz[q], a.b[q], a.x[q], 0, t0, dt);
+            cluster_barrier();
+            mc_rbgs<T>(g, a.bx[q], a.by[q], a.bz[q], a.b[q], a.x[q], 1, t0, dt);
+            cluster_barrier();
+        }
+        const long long nc = (long long)g.n[0] * g.n[1] * g.n[2];
+        for (long long t = t0; t < nc; t += dt) {
+            int i, j, k;
+            decode_cell(g, t, i, j, k);
+            const long long p = pidx(g.sy, g.sz, i, j, k);
+            T diag, off;
+            a.r[q][p] = __ldcg(a.b[q] + p) - mac_Ax<T, MacLdCg>(g, a.x[q], a.bx[q], a.by[q], a.bz[q], p, diag, off);
+        }
+        cluster_barrier();
+        const CellGeom& gc = a.g[q + 1];
+        const long long ncc = (long long)gc.n[0] * gc.n[1] * gc.n[2];
+        const T* rf = a.r[q];
+        for (long long t = t0; t < ncc; t += dt) {
+            int I, J, K;
+            decode_cell(gc, t, I, J, K);
+            const long long f = pidx(g.sy, g.sz, 2 * I, 2 * J, 2 * K);
+            const T v = ((__ldcg(rf + f) + __ldcg(rf + f + 1)) + (__ldcg(rf + f + g.sy) + __ldcg(rf + f + 1 + g.sy))) +
+                        ((__ldcg(rf + f + g.sz) + __ldcg(rf + f + 1 + g.sz)) +
+                         (__ldcg(rf + f + g.sy + g.sz) + __ldcg(rf + f + 1 + g.sy + g.sz)));
+            a.b[q + 1][pidx(gc.sy, gc.sz, I, J, K)] = v;
+        }
+        cluster_barrier();
+    }
+    if (cluster_rank() == 0) {
+        // x = M b on the bottom (as k_mac_bottom_dense)
+        const CellGeom& g = a.g[L - 1];
+        const int N = g.n[0] * g.n[1] * g.n[2];
+        double sm = 0.0, na = 0.0;
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            int i, j, k;
+            decode_cell(g, t, i, j, k);
+            const double v = a.act[t] ? (double)__ldcg(a.b[L - 1] + pidx(g.sy, g.sz, i, j, k)) : 0.0;
+            bb[t] = v;
+            sm += v;
+            na += a.act[t] ? 1.0 : 0.0;
+        }
+        if (a.singular) {
+            sm = block_sum_all(sm);
+            na = block_sum_all(na);
+            const double mean = na > 0.0 ? sm / na : 0.0;
+            for (int t = threadIdx.x; t < N; t += blockDim.x)
+                if (a.act[t]) bb[t] -= mean;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            double a0 = 0.0;
+            for (int v = 0; v < N; ++v) a0 = fma(a.M[(size_t)v * N + t], bb[v], a0);
+            int i, j, k;
+            decode_cell(g, t, i, j, k);
+            store_cell(a.x[L - 1], g, i, j, k, (T)a0);
+        }
+    }
+    cluster_barrier();
+    for (int q = L - 2; q >= 0; --q) {
+        const CellGeom& g = a.g[q];
+        const CellGeom& gc = a.g[q + 1];
+        const long long nc = (long long)g.n[0] * g.n[1] * g.n[2];
+        for (long long t = t0; t < nc; t += dt) {
+            int i, j, k;
+            decode_cell(g, t, i, j, k);
+            const long long p = pidx(g.sy, g.sz, i, j, k);
+            store_cell(a.x[q], g, i, j, k,
+                       __ldcg(a.x[q] + p) + __ldcg(a.x[q + 1] + pidx(gc.sy, gc.sz, i >> 1, j >> 1, k >> 1)));
+        }
+        cluster_barrier();
+        for (int p = 0; p < a.nu2; ++p) {
+            mc_rbgs<T>(g, a.bx[q], a.by[q], a.bz[q], a.b[q], a.x[q], 1, t0, dt);
+            cluster_barrier();
+            mc_rbgs<T>(g, a.bx[q], a.by[q], a.bz[q], a.b[q], a.x[q], 0, t0, dt);
+            cluster_barrier();
+        }
+    }
+}
+
+int mac_coarse_cluster_size()
+{
+    static int cached = -1;
+    if (cached > 0) return cached;
+    int best = 8;
+    if (cudaFuncSetAttribute(k_mac_coarse_vcycle<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(k_mac_coarse_vcycle<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(16);
+        cfg.blockDim = dim3(kMacCoarseThreads);
+        cfg.dynamicSmemBytes = kMacDenseBottomMax * sizeof(double);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 16;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n32 = 0, n64 = 0;
+        if (cudaOccupancyMaxActiveClusters(&n32, k_mac_coarse_vcycle<float>, &cfg) == cudaSuccess &&
+            cudaOccupancyMaxActiveClusters(&n64, k_mac_coarse_vcycle<double>, &cfg) == cudaSuccess && n32 > 0 &&
+            n64 > 0)
+            best = 16;
+    }
+    cudaGetLastError();
+    cached = best;
+    return best;
+}
+
+template <typename T>
+int mac_coarse_vcycle(const MacCoarseCycle<T>& c, int cluster, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(kMacCoarseThreads);
+    cfg.dynamicSmemBytes = kMacDenseBottomMax * sizeof(double);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_mac_coarse_vcycle<T>, c);
+    return e == cudaSuccess ? GBP_OK : cuda_fail(e, "k_mac_coarse_vcycle launch");
+}
+template int mac_coarse_vcycle<float>(const MacCoarseCycle<float>&, int, cudaStream_t);
+template int mac_coarse_vcycle<double>(const MacCoarseCycle<double>&, int, cudaStream_t);
 
 void mac_set_beta(const CellGeom& g, int d, int source, const gbp_array4* src, double cval, int bclo, int bchi,
                   double* b64, float* b32, cudaStream_t st, const RobinFaces* rb, const double* ap, double mult)

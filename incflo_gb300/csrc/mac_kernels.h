@@ -25,6 +25,31 @@ template <typename T>
 void mac_bottom_dense(const CellGeom& g, const double* M, const unsigned char* act, const T* b, T* x, int singular,
                       cudaStream_t st);
 
+// The coarse end of a MAC / ABecLaplacian V-cycle in one launch: levels 0 .. nl-1 of this struct (a tail of
+// the hierarchy ending at the dense bottom) cycled from a zero start by one thread-block cluster, its CTAs
+// meeting at cluster barriers between the phases (each colour of each red-black sweep, residual,
+// restriction, bottom, prolongation); loads of data written inside the launch are L2-coherent.
+constexpr int kMacCoarseMaxLevels = 10;
+constexpr int kMacCoarseThreads = 1024;
+template <typename T>
+struct MacCoarseCycle {
+    int nl;  // >= 2
+    CellGeom g[kMacCoarseMaxLevels];
+    const T* bx[kMacCoarseMaxLevels];
+    const T* by[kMacCoarseMaxLevels];
+    const T* bz[kMacCoarseMaxLevels];
+    T* x[kMacCoarseMaxLevels];  // the result is x[0]
+    T* b[kMacCoarseMaxLevels];  // b[0]: the first level's right-hand side (caller); b[q > 0]: restricted
+    T* r[kMacCoarseMaxLevels];
+    const double* M;            // dense inverse of the bottom operator
+    const unsigned char* act;   // bottom cells that carry an equation
+    int singular;
+    int nu1, nu2;
+};
+int mac_coarse_cluster_size();
+template <typename T>
+int mac_coarse_vcycle(const MacCoarseCycle<T>& c, int cluster, cudaStream_t st);
+
 // Cut cells of an embedded boundary on the finest level (all nullptr: no EB). Padded layouts: kap like a
 // cell array, ap[d] like the face array of direction d (face (i,j,k) at pidx(i,j,k)).
 struct MacEB {

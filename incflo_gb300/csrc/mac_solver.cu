@@ -762,6 +762,19 @@ struct MacBufs<float> {
     static float* r(const MacLevel& l) { return l.r32; }
 };
 
+// First level cycled by the cluster kernel: the first level below the finest with at most kCoarseCells
+// cells, when the bottom is the dense inverse and the tail fits the kernel's table; -1 otherwise.
+int MacSolver::coarse_first() const
+{
+    if (!dense_bottom || !use_coarse) return -1;
+    for (int l = 1; l + 1 < (int)L.size(); ++l) {
+        const CellGeom& g = L[l].g;
+        if ((long long)g.n[0] * g.n[1] * g.n[2] <= kCoarseCells)
+            return ((int)L.size() - l <= kMacCoarseMaxLevels) ? l : -1;
+    }
+    return -1;
+}
+
 template <typename T>
 void MacSolver::vcycle(int l, const T* b, bool zero)
 {
@@ -769,6 +782,30 @@ void MacSolver::vcycle(int l, const T* b, bool zero)
     const MacLevel& lv = L[l];
     const cudaStream_t s = cap_or_st;
     T* x = B::x(lv);
+    // the small levels (this one down to the bottom) in one cluster-resident launch
+    if (sizeof(T) == 4 && zero && l >= 1 && l == coarse_first()) {
+        MacCoarseCycle<T> c{};
+        c.nl = (int)L.size() - l;
+        for (int q = 0; q < c.nl; ++q) {
+            const MacLevel& v = L[l + q];
+            c.g[q] = v.g;
+            c.bx[q] = B::b(v)[0];
+            c.by[q] = B::b(v)[1];
+            c.bz[q] = B::b(v)[2];
+            c.x[q] = B::x(v);
+            c.b[q] = B::rhs(v);
+            c.r[q] = B::r(v);
+        }
+        c.b[0] = const_cast<T*>(b);
+        c.M = dmat;
+        c.act = dact;
+        c.singular = singular ? 1 : 0;
+        c.nu1 = opt.nu1;
+        c.nu2 = opt.nu2;
+        int rc = mac_coarse_vcycle<T>(c, mac_coarse_cluster_size(), s);
+        if (rc && !launch_rc) launch_rc = rc;
+        return;
+    }
     if (l == (int)L.size() - 1) {
         if (dense_bottom)
             mac_bottom_dense<T>(lv.g, dmat, dact, b, x, singular ? 1 : 0, s);
@@ -842,9 +879,11 @@ void MacSolver::record_iteration(int m)
 int MacSolver::run_iteration(int m)
 {
     // the captured step holds ir_inner_cycles V-cycles; a shortened last step is launched directly
+    launch_rc = 0;
     if (!opt.use_graphs || m != opt.ir_inner_cycles) {
         cap_or_st = st;
         record_iteration(m);
+        if (launch_rc) return launch_rc;
         GBP_CUDA(cudaGetLastError());
         return GBP_OK;
     }
@@ -858,6 +897,10 @@ int MacSolver::run_iteration(int m)
         cudaError_t e = cudaStreamEndCapture(cap, &graph);
         cap_or_st = st;
         if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture(mac refinement step)");
+        if (launch_rc) {
+            cudaGraphDestroy(graph);
+            return launch_rc;
+        }
         e = cudaGraphInstantiate(&gexec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
@@ -1023,6 +1066,80 @@ int MacSolver::project(gbp_array4* u[3], gbp_array4* phi_io, int phi_guess, gbp_
                                  2 * cut + ((phi_io && phi_io->data) ? 1 : 0);
     }
     return status;
+}
+
+namespace {
+
+__global__ void k_mac_fill_seeded(CellGeom g, float* __restrict__ a, unsigned seed)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long nc = (long long)g.n[0] * g.n[1] * g.n[2];
+    if (t >= nc) return;
+    const int i = (int)(t % g.n[0]), j = (int)((t / g.n[0]) % g.n[1]), k = (int)(t / ((long long)g.n[0] * g.n[1]));
+    unsigned h = (unsigned)t * 2654435761u ^ seed;
+    h ^= h >> 15;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    a[pidx(g.sy, g.sz, i, j, k)] = (float)(h & 0xffffff) / 16777216.f - 0.5f;
+}
+
+__global__ void k_mac_maxdiff(const float* __restrict__ a, const float* __restrict__ ref, long long n,
+                              unsigned long long* out)
+{
+    double d = 0.0, m = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        d = fmax(d, fabs((double)a[t] - (double)ref[t]));
+        m = fmax(m, fabs((double)ref[t]));
+    }
+    atomicMax(out, (unsigned long long)__double_as_longlong(d));
+    atomicMax(out + 1, (unsigned long long)__double_as_longlong(m));
+}
+
+}  // namespace
+
+int MacSolver::check_coarse_cycle(double* diff)
+{
+    const int lc = coarse_first();
+    if (lc < 1 || !beta_ready) {
+        set_error("check_coarse_cycle: the MAC plan has no cluster-cycled levels (levels " + std::to_string(L.size()) +
+                  ", dense bottom " + std::to_string((int)dense_bottom) + ") or no beta");
+        return GBP_BAD_ARG;
+    }
+    const MacLevel& v = L[lc];
+    const CellGeom& g = v.g;
+    const size_t bytes = sizeof(float) * g.count;
+    float *B = nullptr, *C = nullptr;
+    unsigned long long* dm = nullptr;
+    GBP_CUDA(cudaMalloc(&B, bytes));
+    GBP_CUDA(cudaMalloc(&C, bytes));
+    GBP_CUDA(cudaMalloc(&dm, 2 * sizeof(unsigned long long)));
+    cap_or_st = st;
+    launch_rc = 0;
+    GBP_CUDA(cudaMemsetAsync(B, 0, bytes, st));
+    const long long nc = (long long)g.n[0] * g.n[1] * g.n[2];
+    k_mac_fill_seeded<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(g, B, 77u);
+    use_coarse = false;
+    vcycle<float>(lc, B, true);
+    cudaMemcpyAsync(C, v.x32, bytes, cudaMemcpyDeviceToDevice, st);
+    use_coarse = true;
+    vcycle<float>(lc, B, true);
+    cudaMemsetAsync(dm, 0, 2 * sizeof(unsigned long long), st);
+    k_mac_maxdiff<<<592, 256, 0, st>>>(v.x32, C, (long long)g.count, dm);
+    unsigned long long h[2] = {0, 0};
+    cudaMemcpyAsync(h, dm, sizeof(h), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(B);
+    cudaFree(C);
+    cudaFree(dm);
+    const int rc = launch_rc;
+    launch_rc = 0;
+    if (e != cudaSuccess) return cuda_fail(e, "check_coarse_cycle (MAC)");
+    if (rc) return rc;
+    double d, m;
+    memcpy(&d, &h[0], 8);
+    memcpy(&m, &h[1], 8);
+    *diff = m > 0 ? d / m : d;
+    return GBP_OK;
 }
 
 }  // namespace gbp

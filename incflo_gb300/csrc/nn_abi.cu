@@ -96,7 +96,10 @@ int make_pair(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev, Surr
     }
     GBP_CUDA(cudaMemsetAsync(q.x0, 0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16), st));
     GBP_CUDA(cudaMemsetAsync(q.target, 0, (size_t)g0.R * sizeof(float), st));
-    int rc = nn::build_input<double>(g, ns.rhs64(), ns.sigma64(), prev, g0, q.x0, s->scr, st);
+    // channel 0 = the residual of the previous solution in this projection's system (rhs itself without
+    // one): the increment is A^-1 of it, the local problem the network learns
+    const double* ch0 = prev ? ns.residual_of(prev) : ns.rhs64();
+    int rc = nn::build_input<double>(g, ch0, ns.sigma64(), prev, g0, q.x0, s->scr, st);
     if (!rc) rc = nn::build_target(g, ns.phi64(), prev, g0, q.target, s->scr + 4, st);
     return rc;
 }
@@ -328,29 +331,13 @@ int gbp_surrogate_add_sample(gbp_surrogate* s, gbp_plan* plan, const gbp_array4*
         return GBP_BAD_ARG;
     }
     const nn::Grid3 g0 = nn::make_grid3(dims[0], dims[1], dims[2]);
-    const double* prev = nullptr;
-    if (phi_prev && phi_prev->data) {
-        if ((size_t)g.count > s->phi_prev_count) {
-            if (s->phi_prev) cudaFree(s->phi_prev);
-            s->phi_prev = nullptr;
-            s->phi_prev_count = 0;
-            GBP_CUDA(cudaMalloc(&s->phi_prev, sizeof(double) * g.count));
-            s->phi_prev_count = g.count;
-        }
-        GBP_CUDA(cudaMemsetAsync(s->phi_prev, 0, sizeof(double) * g.count, st));
-        nodal_load_phi(g, *phi_prev, s->phi_prev, st);
-        prev = s->phi_prev;
-    }
     SurrogateSample q;
     GBP_CUDA(cudaMalloc(&q.x0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16)));
     if (cudaMalloc(&q.target, (size_t)g0.R * sizeof(float)) != cudaSuccess) {
         cudaFree(q.x0);
         return cuda_fail(cudaGetLastError(), "cudaMalloc(sample)");
     }
-    cudaMemsetAsync(q.x0, 0, (size_t)g0.R * nn::kInC * sizeof(__nv_bfloat16), st);
-    cudaMemsetAsync(q.target, 0, (size_t)g0.R * sizeof(float), st);
-    int rc = nn::build_input<double>(g, ns.rhs64(), ns.sigma64(), prev, g0, q.x0, s->scr, st);
-    if (!rc) rc = nn::build_target(g, ns.phi64(), prev, g0, q.target, s->scr + 4, st);
+    int rc = make_pair(s, plan, phi_prev, q, dims);
     if (!rc) {
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = cuda_fail(e, "add_sample");

@@ -548,27 +548,6 @@ template void nodal_bottom_dense<float>(const NodalGeom&, const double*, const f
 // ---------------------------------------------------------------------------------------
 // coarse V-cycle in one cluster
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ void cluster_barrier()
-{
-    // every thread of every CTA of the cluster arrives; release / acquire order the global stores of
-    // one phase before the loads of the next at cluster scope
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-__device__ __forceinline__ unsigned cluster_rank()
-{
-    unsigned r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-
-__device__ __forceinline__ unsigned cluster_nctas()
-{
-    unsigned r;
-    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
-    return r;
-}
-
 // one Jacobi sweep xout = xin + omega D^-1 (b - A xin) (zero: xin = 0) over the level's unique nodes
 template <typename T>
 __device__ __forceinline__ void cc_jacobi(const NodalGeom& g, const T* s, const T* xin, const T* b, T* xout, T omega,
@@ -595,7 +574,7 @@ __device__ __forceinline__ void cc_jacobi(const NodalGeom& g, const T* s, const 
                 v = __ldcg(xin + c) + omega * (__ldcg(b + c) - ax) * approx_recip(diag);
             }
         }
-        store_node(xout, g, i, j, k, v);
+        store_node_unrolled(xout, g, i, j, k, v);
     }
 }
 
@@ -615,7 +594,7 @@ __device__ __forceinline__ void cc_resid(const NodalGeom& g, const T* s, const T
                                : NodalOp<T>::template apply<false, LdCg>(x, s, c, g.sy, g.sz, g, diag);
             v = __ldcg(b + c) - ax;
         }
-        store_node(r, g, i, j, k, v);
+        store_node_unrolled(r, g, i, j, k, v);
     }
 }
 
@@ -645,7 +624,7 @@ __device__ __forceinline__ void cc_restrict(const NodalGeom& gf, const NodalGeom
             }
             v = acc;
         }
-        store_node(bc, gc, I, J, K, v);
+        store_node_unrolled(bc, gc, I, J, K, v);
     }
 }
 
@@ -678,7 +657,7 @@ __device__ __forceinline__ void cc_prolong(const NodalGeom& gf, const NodalGeom&
         const int sh = oi + oj + ok;
         const T w = sh == 0 ? T(1) : (sh == 1 ? T(0.5) : (sh == 2 ? T(0.25) : T(0.125)));
         const long long p = pidx(gf.sy, gf.sz, i, j, k);
-        store_node(xf, gf, i, j, k, __ldcg(xf + p) + w * acc);
+        store_node_unrolled(xf, gf, i, j, k, __ldcg(xf + p) + w * acc);
     }
 }
 
@@ -720,7 +699,7 @@ __device__ __forceinline__ void cc_bottom(const NodalGeom& g, const double* M, c
         if (v < N) a0 = fma(M[(size_t)v * N + t], bb[v], a0);
         int i, j, k;
         decode_node(g, t, i, j, k);
-        store_node(xout, g, i, j, k, (T)(a0 + a1));
+        store_node_unrolled(xout, g, i, j, k, (T)(a0 + a1));
     }
 }
 

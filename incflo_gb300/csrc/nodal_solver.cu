@@ -546,7 +546,7 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
         return;
     }
     // the small levels (this one down to the bottom) in one cluster-resident launch
-    if (zero && l >= 1 && l == coarse_first()) {
+    if (sizeof(T) == 4 && zero && l >= 1 && l == coarse_first()) {
         CoarseCycle<T> c{};
         c.nl = (int)L.size() - l;
         for (int q = 0; q < c.nl; ++q) {
@@ -1204,6 +1204,14 @@ int NodalSolver::set_eb(const gbp_array4* M)
     return rebuild_masks();
 }
 
+double* NodalSolver::residual_of(const double* x)
+{
+    cap_or_st = st;
+    launch_rc = 0;
+    resid0(x, rhs0, L[0].r64, nullptr, st);
+    return L[0].r64;
+}
+
 int NodalSolver::set_eb_inflow(const gbp_array4* eb_vel, const gbp_array4* dap, const gbp_array4* bcent)
 {
     if (!eb_vel) {
@@ -1248,7 +1256,8 @@ int NodalSolver::set_surrogate(nn::UNet* n, int level, int mode)
     return net->workspace(dims, false);
 }
 
-// Warm start from the network: restrict the FP32 right-hand side to the network's level, predict,
+// Warm start from the network: restrict the FP32 residual of the start it would replace (the right-hand
+// side itself from a zero start) to the network's level, predict,
 // prolong to level 0, scale by the Galerkin factor alpha = x.r / x.Ax (the scaled prediction is the best
 // multiple of x in the energy norm), then take it only if its FP64 residual beats the start it would
 // replace. From a zero start the network predicts phi (input phi_prev = 0) and competes with phi = 0;
@@ -1262,7 +1271,8 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats, bool fro
     const long long nk0 = net->launches();
     GBP_CUDA(cudaEventRecord(evw, st));
     launch_rc = 0;
-    nodal_to_f32(l0.g, rhs0, l0.b32, scale32, st);
+    // channel 0: the residual of the start being replaced (the right-hand side itself from zero)
+    nodal_to_f32(l0.g, from_prev ? res : rhs0, l0.b32, scale32, st);
     for (int l = 0; l < lv; ++l) nodal_restrict<float>(L[l].g, L[l + 1].g, L[l].b32, L[l + 1].b32, st);
     int dims[3];
     nn::net_dims(L[lv].g, dims);
@@ -1288,8 +1298,7 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats, bool fro
         GBP_CUDA(cudaMemsetAsync(L[l].x32, 0, sizeof(float) * L[l].g.count, st));
         nodal_prolong_add<float>(L[l].g, L[l + 1].g, L[l + 1].x32, L[l].x32, st);
     }
-    // Galerkin factor against the residual of the start being replaced (b itself from zero)
-    if (from_prev) nodal_to_f32(l0.g, res, l0.b32, scale32, st);
+    // Galerkin factor against the residual of the start being replaced (b32 still holds it)
     resid<float>(l0.g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st);
     if (launch_rc) return launch_rc;
     rc = nn::node_dot2(l0.g, l0.x32, l0.b32, l0.r32, net_scr, st);

@@ -140,6 +140,9 @@ public:
     double* phi64() const { return phi; }
     double* rhs64() const { return rhs0; }
     double* sigma64() const { return L[0].s64; }
+    // r = rhs - A x in FP64 on level 0 (the operator and right-hand side of the last projection), into the
+    // level-0 FP64 residual scratch; returns it (the network input of a start from x)
+    double* residual_of(const double* x);
 
 private:
     template <typename T>
@@ -180,8 +183,10 @@ private:
     unsigned long long* dnorm = nullptr;  // [0] rhs norm, [1] residual norm
     unsigned long long* hnorm = nullptr;  // pinned mirror
     bool singular = false;        // the system has the constants as null space (consistent RHS, gauge)
-    // the levels with at most this many nodes (below the finest) run as one cluster launch per V-cycle
-    static constexpr long long kCoarseNodes = 40000;
+    // the FP32 levels with at most this many nodes (below the finest) run as one cluster launch per V-cycle
+    // (measured at 256^3: 11.92 ms per projection against 11.98 with per-level launches and 12.12 with the
+    // 33^3 level included; FP64 levels stay on per-level launches, which were faster there)
+    static constexpr long long kCoarseNodes = 5000;
     bool use_coarse = true;
     int coarse_first() const;
 public:

@@ -69,6 +69,7 @@ def main():
         import bench
 
         run = getattr(bench, "run_" + args.row)
+        args.no_parity = True  # the row alone: no oracle comparison inside the profiled run
         print(json.dumps(run(args, torch.device("cuda", 0), steps=args.reps, warmup=1)))
         return None
     n = args.n

@@ -21,7 +21,7 @@ import torch
 from . import _abi as A
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-WEIGHTS = os.path.join(HERE, "weights", "unet16_rt128.bin")
+WEIGHTS = os.path.join(HERE, "weights", "unet16_seq128.bin")
 
 
 def _ints(v):

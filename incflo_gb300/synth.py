@@ -174,3 +174,75 @@ def variable_density_rt_amr(n=256, band=(0.375, 0.625), box=64, seed_h=2, seed_u
             for i in range(0, nf[0], box):
                 boxes.append(((i, j, k), (i + box - 1, j + box - 1, k + box - 1)))
     return dict(base=base, boxes=boxes, zlo=zlo, rho_f=rho_f, vel_f=np.ascontiguousarray(vel_f))
+
+
+def tag_and_box(tag, blocking=32, max_grid=64):
+    """incflo's regrid of a tagged coarse level into a ratio-2 fine BoxArray (amr.blocking_factor /
+    amr.max_grid_size, in fine cells): a coarse block of blocking/2 cells per side is refined when any of
+    its cells is tagged; refined blocks are gathered into boxes of at most max_grid fine cells per side
+    (a super-block of (max_grid/2)^3 coarse cells becomes one box when all its blocks are refined, else
+    each refined block is a box of its own). tag: (nz, ny, nx) bool over the coarse cells. Returns the
+    fine boxes [((lo), (hi))] in fine cell indices, disjoint, lo even and hi odd."""
+    nz, ny, nx = tag.shape
+    bc = blocking // 2
+    if any(v % bc for v in (nx, ny, nz)):
+        raise ValueError("the coarse level must be a multiple of the blocking factor / 2")
+    blk = tag.reshape(nz // bc, bc, ny // bc, bc, nx // bc, bc).any(axis=(1, 3, 5))
+    g = max(1, max_grid // blocking)  # blocks per box side
+    boxes = []
+    for K in range(0, blk.shape[0], g):
+        for J in range(0, blk.shape[1], g):
+            for I in range(0, blk.shape[2], g):
+                sub = blk[K:K + g, J:J + g, I:I + g]
+                if sub.size == g ** 3 and sub.all():
+                    lo = (2 * bc * I, 2 * bc * J, 2 * bc * K)
+                    boxes.append((lo, tuple(v + 2 * bc * g - 1 for v in lo)))
+                    continue
+                for k, j, i in zip(*np.nonzero(sub)):
+                    lo = (2 * bc * (I + i), 2 * bc * (J + j), 2 * bc * (K + k))
+                    boxes.append((lo, tuple(v + 2 * bc - 1 for v in lo)))
+    return boxes
+
+
+def rt_amr_tagged(n=256, seed_h=2, seed_u=3, band=0.1, pct=90.0, blocking=32, max_grid=64, rho_lo=1.0,
+                  rho_hi=3.0):
+    """Two-level variable-density interface with the fine level from tagging (incflo_tagging.cpp's rules
+    as the benchmark's two-level case states them): coarse cells within +-band of the interface, or whose
+    vorticity magnitude exceeds its pct-th percentile, refined by 2 with amr.blocking_factor = blocking and
+    amr.max_grid_size = max_grid (fine cells). The velocity is the k^-2 field concentrated at the interface
+    (weight exp(-((z - h) / band)^2)), where a Rayleigh-Taylor run moves the fluid. Fine density from the
+    interface at the fine resolution, fine velocity injected from the base level. Returns the base fields,
+    the fine boxes and per-box fine velocity / density arrays."""
+    base = variable_density_rt(n, seed_h, seed_u, rho_lo, rho_hi)
+    nn = base["n"]
+    dz = 1.0 / nn[2]
+    z = (np.arange(nn[2]) + 0.5) * dz
+    hxy = interface_height(nn, seed_h)
+    dist = z[:, None, None] - hxy[None, :, :]
+    vel = base["vel"] * np.exp(-(dist / band) ** 2)[None]
+    base["vel"] = vel
+    h = [1.0 / v for v in nn]
+    # vorticity by centred differences (periodic x / y, one-sided at the z walls)
+    def ddx(f, axis, hh, periodic):
+        if periodic:
+            return (np.roll(f, -1, axis) - np.roll(f, 1, axis)) / (2 * hh)
+        return np.gradient(f, hh, axis=axis)
+    u, v, w = vel
+    wx = ddx(w, 1, h[1], True) - ddx(v, 0, h[2], False)
+    wy = ddx(u, 0, h[2], False) - ddx(w, 2, h[0], True)
+    wz = ddx(v, 2, h[0], True) - ddx(u, 1, h[1], True)
+    om = np.sqrt(wx * wx + wy * wy + wz * wz)
+    tag = (np.abs(dist) <= band) | (om > np.percentile(om, pct))
+    boxes = tag_and_box(tag, blocking, max_grid)
+    nf = tuple(2 * v for v in nn)
+    dzf = 1.0 / nf[2]
+    hf = interface_height(nf, seed_h)
+    rho_f, vel_f = [], []
+    for lo, hi in boxes:
+        zf = (np.arange(lo[2], hi[2] + 1) + 0.5) * dzf
+        hb = hf[lo[1]:hi[1] + 1, lo[0]:hi[0] + 1]
+        rho_f.append(np.ascontiguousarray(
+            rho_lo + (rho_hi - rho_lo) * 0.5 * (1.0 + np.tanh((zf[:, None, None] - hb[None]) / (2.0 * dzf)))))
+        vc = vel[:, lo[2] // 2:(hi[2] + 1) // 2, lo[1] // 2:(hi[1] + 1) // 2, lo[0] // 2:(hi[0] + 1) // 2]
+        vel_f.append(np.ascontiguousarray(np.repeat(np.repeat(np.repeat(vc, 2, axis=1), 2, axis=2), 2, axis=3)))
+    return dict(base=base, boxes=boxes, rho_f=rho_f, vel_f=vel_f, tagged_fraction=float(tag.mean()))

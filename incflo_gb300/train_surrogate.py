@@ -9,9 +9,10 @@ half of the sequences are slowly displaced variable-density interfaces (synth.rt
 benchmark's family, tanh interface of random height, turning k^-2 velocity), half are double shear
 layers (synth.double_shear_sequence: u = tanh(30 (y - 1/4)) / tanh(30 (3/4 - y)), v = 0.05 sin(2 pi x),
 plus a turning k^-2 perturbation), seeds held apart from the evaluation's. Each projection of a
-sequence is solved to rtol 1e-10 from the previous phi and gives one pair: inputs (rhs, sigma, phi_prev)
--> target phi - phi_prev, the increment the solver's initial_guess = previous start is missing (the
-first projection of a sequence: phi_prev = 0, target phi). The pairs stream through
+sequence is solved to rtol 1e-10 from the previous phi and gives one pair: inputs (rhs - A phi_prev,
+sigma, phi_prev) -> target phi - phi_prev, the increment the solver's initial_guess = previous start is
+missing (channel 0 is the residual of that start, so the increment is A^-1 of it; the first projection of
+a sequence: phi_prev = 0, channel 0 = rhs, target phi). The pairs stream through
 gbp_surrogate_train_step (one Adam step each, nothing stored), so `--pairs` pairs cost one solve and one
 training step apiece. Afterwards the script evaluates the three starts (zero, previous phi, previous phi
 + the network's increment) on a held-out interface sequence at --eval-n^3 with the network on multigrid
@@ -76,6 +77,8 @@ def stream_pairs(s, n, pairs, seq_len, lr, seed0):
             losses.append(s.train_step(p, prev, lr=lr_at(k, pairs, lr)))
             prev = p.getPhi().clone()
             k += 1
+            if k % 100 == 0:
+                print(json.dumps({"pairs": k, "loss_last100": float(np.mean(losses[-100:]))}), flush=True)
         q += 1
     NodalProjector._plans.clear()
     return losses, q
@@ -120,7 +123,7 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--pairs", type=int, default=2000)
     ap.add_argument("--seq-len", type=int, default=20)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=3e-4)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval-n", type=int, default=256)

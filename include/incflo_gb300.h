@@ -399,11 +399,11 @@ int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_lau
  * prolongation + Jacobi. GBP_BAD_ARG when the whole-row kernels do not apply to the plan's level 0. */
 int gbp_plan_check_level_kernels(gbp_plan* plan, double diff[4]);
 
-/* No counterpart in the reference: a test hook. One FP32 V-cycle from the first level that a nodal plan
- * cycles in one thread-block-cluster launch (the levels of at most 40000 nodes below the finest, with
- * the dense bottom), on a seeded right-hand side, once through the per-level launches and once through
- * the cluster kernel; *diff = max |cluster - per-level| / max |per-level| over every padded position.
- * GBP_BAD_ARG when the plan has no such levels. */
+/* No counterpart in the reference: a test hook. One FP32 V-cycle from the first level that a plan cycles
+ * in one thread-block-cluster launch (the FP32 levels of at most 5000 nodes (nodal) / 40000 cells (MAC)
+ * below the finest, with the dense bottom), on a seeded right-hand side, once through the per-level launches and
+ * once through the cluster kernel; *diff = max |cluster - per-level| / max |per-level| over every padded
+ * position. GBP_BAD_ARG when the plan has no such levels. */
 int gbp_plan_check_coarse_cycle(gbp_plan* plan, double* diff);
 
 /* MacProjector::setLevelBC(lev, nullptr, robin_a, robin_b, robin_f) for the GBP_BC_ROBIN sides
@@ -525,9 +525,10 @@ int gbp_surrogate_train_pair(gbp_surrogate* s, const int dims[3], const int dom[
 /* forward pass; hout (device, [R][16] BF16, channel 0 = prediction) may be NULL */
 int gbp_surrogate_predict(gbp_surrogate* s, const int dims[3], const void* x0, void* hout,
                           void* stream);
-/* append a training pair from a nodal plan after gbp_nodal_project: input from the plan's
- * right-hand side, sigma and phi_prev (nodal, may be NULL), target = the plan's phi - phi_prev (the
- * increment the network predicts on top of the previous solution; the plan's phi without one) */
+/* append a training pair from a nodal plan after gbp_nodal_project: input channels from the plan's
+ * right-hand side minus A phi_prev (the residual of the previous solution in this projection's system;
+ * the right-hand side itself when phi_prev is NULL), sigma and phi_prev (nodal); target = the plan's
+ * phi - phi_prev (the increment the network predicts on top of the previous solution; phi without one) */
 int gbp_surrogate_add_sample(gbp_surrogate* s, gbp_plan* plan, const gbp_array4* phi_prev);
 /* one training step on the pair of a nodal plan's last projection (built as gbp_surrogate_add_sample
  * builds it, used once, not stored): forward + backward, and an Adam step when lr > 0; *loss (host,

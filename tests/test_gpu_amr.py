@@ -83,3 +83,40 @@ def test_amr_rejects_bad_boxes(gpu_lib):
         AmrNodalProjector(g, (N, N, N), (N, N, N), [((1, 0, 0), (4, 3, 3))])  # not whole coarse cells
     with pytest.raises(Exception):
         AmrNodalProjector(g, (N, N, N), (N, N, N), [((0, 0, 0), (7, 7, 7)), ((6, 0, 0), (9, 3, 3))])  # overlap
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_amr_tagged_many_boxes_matches_oracle(gpu_lib, precision):
+    """The benchmark's two-level construction at a 16^3 base: the fine level from tagging (interface +-0.1 or
+    vorticity above its 90th percentile, blocking_factor 8, max_grid_size 16 at this size) in many boxes,
+    against the composite oracle on both levels."""
+    from incflo_gb300 import synth
+
+    w = synth.rt_amr_tagged(16, blocking=8, max_grid=16)
+    b, boxes = w["base"], w["boxes"]
+    assert len(boxes) > 8
+    nc = b["n"]
+    nf = [2 * v for v in nc]
+    fm = np.zeros((nf[2], nf[1], nf[0]), bool)
+    rho_f = np.ones((nf[2], nf[1], nf[0]))
+    u_f = np.zeros((3, nf[2], nf[1], nf[0]))
+    for (lo, hi), r, v in zip(boxes, w["rho_f"], w["vel_f"]):
+        sl = (slice(lo[2], hi[2] + 1), slice(lo[1], hi[1] + 1), slice(lo[0], hi[0] + 1))
+        fm[sl] = True
+        rho_f[sl] = r
+        u_f[(slice(None),) + sl] = v
+    ref = CompositeNodal(nc, [1.0 / v for v in nc], b["bclo"], b["bchi"], fm).project(1.0 / b["rho"], 1.0 / rho_f,
+                                                                                      b["vel"], u_f)
+    proj = AmrNodalProjector(Geometry(nc, b["lo"], b["hi"]), b["bclo"], b["bchi"], boxes,
+                             options=make_options(0, precision=precision, mg_rtol=1e-12, mg_atol=0.0))
+    vc = cuda(b["vel"])
+    pc = torch.zeros((nc[2] + 1, nc[1] + 1, nc[0] + 1), dtype=torch.float64, device="cuda")
+    vf = [cuda(v) for v in w["vel_f"]]
+    pf = [torch.zeros((hi[2] - lo[2] + 2, hi[1] - lo[1] + 2, hi[0] - lo[0] + 2), dtype=torch.float64,
+                      device="cuda") for lo, hi in boxes]
+    st = proj.apply(vc, cuda(b["rho"]), torch.zeros_like(vc), pc, vf, [cuda(r) for r in w["rho_f"]],
+                    [torch.zeros_like(v) for v in vf], pf, scaling_factor=1.0)
+    assert st["status"] == 0 and st["final_rel_resid"] <= 1e-12
+    assert rel_l2(pc.cpu().numpy(), ref["phi_c"]) <= 1e-9
+    for t, (lo, hi) in zip(pf, boxes):
+        assert rel_l2(t.cpu().numpy(), ref["phi_f"][lo[2]:hi[2] + 2, lo[1]:hi[1] + 2, lo[0]:hi[0] + 2]) <= 1e-9

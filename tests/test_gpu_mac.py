@@ -167,3 +167,32 @@ def test_get_fluxes_are_the_projection_correction(gpu_lib, case):
         scale = max(np.abs(ref).max(), 1e-300)
         np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9 * scale)
         np.testing.assert_allclose(got, ut[d].cpu().numpy() - umac[d], rtol=0, atol=1e-13 * scale)
+
+
+@pytest.mark.parametrize("case", [CASES[4], ((64, 32, 32), (1.0, 0.5, 0.5), (D, N, P), (N, D, P))],
+                         ids=["32-walls", "64x32x32-dirichlet"])
+def test_cluster_coarse_cycle_matches_per_level_launches(gpu_lib, case):
+    """The small levels of the MAC hierarchy run as one thread-block-cluster launch per V-cycle: one V-cycle
+    from the first such level agrees with the per-level launches to FP32 rounding, and the projection
+    through it matches the oracle."""
+    import ctypes
+
+    from incflo_gb300 import _abi
+
+    n, ext, bclo, bchi = case
+    g = O.Grid(n, hi=ext, bclo=bclo, bchi=bchi)
+    rng = np.random.default_rng(12)
+    beta = [np.abs(b) + 0.2 for b in face_fields(g, rng, zero_neumann=False)]
+    umac = face_fields(g, rng)
+    un_or, phi_or, st_or = O.mac_project(g, beta, umac, rtol=1e-13)
+    mp = MacProjector(Geometry(n, (0, 0, 0), ext), options=make_options(1, precision="mixed"))
+    mp.initProjector(beta=[cuda(b) for b in beta])
+    mp.setDomainBC(bclo, bchi)
+    mp.setUMAC([cuda(u) for u in umac])
+    phi = cuda(np.zeros(g.cell_shape))
+    st = mp.project(rtol=1e-12, atol=0.0, phi=phi, phi_guess=False)
+    assert st["status"] == 0 and rel_l2(phi.cpu().numpy(), phi_or) <= 1e-9
+    diff = ctypes.c_double()
+    _abi.check(_abi.load().gbp_plan_check_coarse_cycle(mp.plan.ptr, ctypes.byref(diff)), "check_coarse_cycle")
+    print(f"\n{n}: MAC cluster vs per-level V-cycle {diff.value:.2e}")
+    assert diff.value <= 1e-5

@@ -91,3 +91,28 @@ def test_linear_potential_exact_across_the_interface():
     ok = ~np.isnan(r["phi_f"])
     shift = (pc - lin).mean()
     np.testing.assert_allclose(r["phi_f"][ok], linf[ok] + shift, rtol=0, atol=1e-11)
+
+
+def test_tagging_boxes_cover_the_tags_and_follow_the_grid_rules():
+    """synth.tag_and_box (incflo's regrid: blocking_factor, max_grid_size): disjoint boxes of whole blocks,
+    at most max_grid fine cells per side, covering every tagged coarse cell and no untagged block."""
+    import numpy as np
+
+    from incflo_gb300 import synth
+
+    rng = np.random.default_rng(2)
+    tag = np.zeros((32, 32, 32), bool)
+    tag[12:20] = True
+    tag[rng.integers(0, 32, 40), rng.integers(0, 32, 40), rng.integers(0, 32, 40)] = True
+    boxes = synth.tag_and_box(tag, blocking=8, max_grid=16)
+    fine = np.zeros((64, 64, 64), int)
+    for lo, hi in boxes:
+        ext = [hi[d] - lo[d] + 1 for d in range(3)]
+        assert all(e in (8, 16) for e in ext) and all(v % 8 == 0 for v in lo)
+        fine[lo[2]:hi[2] + 1, lo[1]:hi[1] + 1, lo[0]:hi[0] + 1] += 1
+    assert fine.max() == 1
+    covered = fine.reshape(32, 2, 32, 2, 32, 2).all(axis=(1, 3, 5))
+    assert np.all(covered[tag])
+    blocks_tagged = tag.reshape(8, 4, 8, 4, 8, 4).any(axis=(1, 3, 5))
+    blocks_fine = covered.reshape(8, 4, 8, 4, 8, 4).all(axis=(1, 3, 5))
+    assert np.array_equal(blocks_tagged, blocks_fine)
