@@ -604,6 +604,8 @@ inline double bits_to_double(unsigned long long b)
 CompositeNodal::~CompositeNodal()
 {
     if (st) cudaStreamSynchronize(st);
+    if (gstep) cudaGraphExecDestroy(gstep);
+    if (capst) cudaStreamDestroy(capst);
     if (hnorm) cudaFreeHost(hnorm);
     if (dboxes) cudaFree(dboxes);
     if (ev0) cudaEventDestroy(ev0);
@@ -618,6 +620,8 @@ int CompositeNodal::set_options(const gbp_options& o)
     int rc = crs.set_options(o);
     if (!rc) rc = fin.set_options(o);
     if (!rc) opt = o;
+    if (gstep) cudaGraphExecDestroy(gstep);  // the step's kernels depend on the options
+    gstep = nullptr;
     return rc;
 }
 
@@ -874,6 +878,48 @@ void CompositeNodal::composite_residual(const double* bc, const double* bf, unsi
     }
 }
 
+// One refinement step on st: coarse correction on the restricted composite residual, fine correction
+// on the fresh fine residual with the interface held, then the composite residual and its norm (read
+// back into hnorm[1]).
+void CompositeNodal::issue_step(double scale32)
+{
+    const int m = 1;  // V-cycles per level per step (one is the fastest on the benchmark's workload)
+    // coarse correction on the restricted composite residual
+    k_amr_restrict_copy<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, r_c, rc_full);
+    {
+        int lo[3], ext[3];
+        for (int d = 0; d < 3; ++d) {
+            // fine global node positions 2i-1 .. 2i+1 against the box's off .. off + nfb
+            lo[d] = std::max(0, (off[d] - 1) / 2);
+            const int hi = std::min(gc.nu[d] - 1, (off[d] + nfb[d] + 1) / 2 + 1);
+            if (gf.per[d]) {
+                lo[d] = 0;
+                ext[d] = gc.nu[d];
+            } else {
+                ext[d] = std::max(0, hi - lo[d] + 1);
+            }
+        }
+        if (ext[0] > 0 && ext[1] > 0 && ext[2] > 0) {
+            const dim3 grid((unsigned)((ext[0] + kB3.x - 1) / kB3.x), (unsigned)((ext[1] + kB3.y - 1) / kB3.y),
+                            (unsigned)((ext[2] + kB3.z - 1) / kB3.z));
+            k_amr_restrict<<<grid, kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], r_c, r_f, rc_full,
+                                                 make_int3(lo[0], lo[1], lo[2]), make_int3(ext[0], ext[1], ext[2]));
+        }
+    }
+    cudaMemsetAsync(e_c, 0, sizeof(double) * gc.count, st);
+    crs.apply_vcycles(rc_full, e_c, m, scale32, st);
+    k_amr_prolong_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, e_c, phi_c);
+    k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], e_c, phi_f);
+    // fine correction on the fresh fine residual, interface held
+    k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], phi_c, phi_f);
+    resid_f(phi_f, b_f, r_f);
+    fin.apply_vcycles(r_f, phi_f, m, scale32, st);
+    // composite residual and its norm
+    cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st);
+    composite_residual(b_c, b_f, dnorm + 1);
+    cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+}
+
 int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
 {
     int rc = check_fields(f);
@@ -1008,9 +1054,6 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
         frexp(bnorm * gc.vol, &ex);
         scale32 = ldexp(1.0, -ex);
     }
-    // V-cycles per level per refinement step: one is the fastest on the 256^3 + band workload (186 ms
-    // against 205 ms with two)
-    const int m = 1;
     int it = 0, status = GBP_OK;
     const double r0 = rn;
     while (rn > target) {
@@ -1019,40 +1062,34 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
             set_error("amr solve: maxiter reached before the tolerance");
             break;
         }
-        // coarse correction on the restricted composite residual
-        k_amr_restrict_copy<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, r_c, rc_full);
-        {
-            int lo[3], ext[3];
-            for (int d = 0; d < 3; ++d) {
-                // fine global node positions 2i-1 .. 2i+1 against the box's off .. off + nfb
-                lo[d] = std::max(0, (off[d] - 1) / 2);
-                const int hi = std::min(gc.nu[d] - 1, (off[d] + nfb[d] + 1) / 2 + 1);
-                if (gf.per[d]) {
-                    lo[d] = 0;
-                    ext[d] = gc.nu[d];
-                } else {
-                    ext[d] = std::max(0, hi - lo[d] + 1);
-                }
+        if (opt.use_graphs && (!gstep || gstep_scale != scale32 || gstep_prec != opt.precision)) {
+            // capture the step once on a stream of its own (the caller's may be the legacy default
+            // stream), with every kernel of the step issued there
+            if (gstep) cudaGraphExecDestroy(gstep);
+            gstep = nullptr;
+            if (!capst) GBP_CUDA(cudaStreamCreateWithFlags(&capst, cudaStreamNonBlocking));
+            cudaStream_t keep = st;
+            st = capst;
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(capst, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                issue_step(scale32);
+                e = cudaStreamEndCapture(capst, &graph);
             }
-            if (ext[0] > 0 && ext[1] > 0 && ext[2] > 0) {
-                const dim3 grid((unsigned)((ext[0] + kB3.x - 1) / kB3.x), (unsigned)((ext[1] + kB3.y - 1) / kB3.y),
-                                (unsigned)((ext[2] + kB3.z - 1) / kB3.z));
-                k_amr_restrict<<<grid, kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], r_c, r_f, rc_full,
-                                                     make_int3(lo[0], lo[1], lo[2]), make_int3(ext[0], ext[1], ext[2]));
+            st = keep;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&gstep, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                gstep = nullptr;
+                return cuda_fail(e, "amr: capture of the refinement step");
             }
+            gstep_scale = scale32;
+            gstep_prec = opt.precision;
         }
-        GBP_CUDA(cudaMemsetAsync(e_c, 0, sizeof(double) * gc.count, st));
-        crs.apply_vcycles(rc_full, e_c, m, scale32, st);
-        k_amr_prolong_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, e_c, phi_c);
-        k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], e_c, phi_f);
-        // fine correction on the fresh fine residual, interface held
-        k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], phi_c, phi_f);
-        resid_f(phi_f, b_f, r_f);
-        fin.apply_vcycles(r_f, phi_f, m, scale32, st);
-        // composite residual and its norm
-        GBP_CUDA(cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st));
-        composite_residual(b_c, b_f, dnorm + 1);
-        GBP_CUDA(cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        if (opt.use_graphs)
+            GBP_CUDA(cudaGraphLaunch(gstep, st));
+        else
+            issue_step(scale32);
         GBP_CUDA(cudaStreamSynchronize(st));
         GBP_CUDA(cudaGetLastError());
         rn = bits_to_double(hnorm[1]);
@@ -1120,7 +1157,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
         memset(stats, 0, sizeof(*stats));
         stats->status = status;
         stats->outer_iters = it + 1;
-        stats->vcycles = 2 * m * it;
+        stats->vcycles = 2 * it;  // one V-cycle per level per step
         stats->num_levels = 2;
         stats->rhs_norm = bnorm;
         stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;

@@ -88,6 +88,14 @@ private:
     void* dboxes = nullptr;  // device table for the batched box kernels
     size_t dboxes_bytes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // one refinement step (restriction, coarse V-cycles, prolongation, fine V-cycles, composite residual
+    // and its norm read-back) captured as a CUDA graph and replayed; recaptured when the FP32 scale or
+    // the options change
+    void issue_step(double scale32);
+    cudaStream_t capst = nullptr;
+    cudaGraphExec_t gstep = nullptr;
+    double gstep_scale = 0.0;
+    int gstep_prec = -1;
 };
 
 }  // namespace gbp

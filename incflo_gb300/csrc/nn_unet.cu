@@ -360,6 +360,12 @@ __global__ void k_scale_to64(long long n, const float* __restrict__ x, double al
     if (i < n) out[i] = alpha * (double)x[i];
 }
 
+__global__ void k_scale32(long long n, float* __restrict__ x, float a)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= a;
+}
+
 __global__ void k_axpy_to64(long long n, const double* __restrict__ base, const float* __restrict__ x, double alpha,
                             double* __restrict__ out)
 {
@@ -861,6 +867,13 @@ int node_dot2(const NodalGeom& g, const float* x, const float* b, const float* r
 int scale_to64(long long count, const float* x, double alpha, double* out, cudaStream_t st)
 {
     k_scale_to64<<<nblocks(count), kT, 0, st>>>(count, x, alpha, out);
+    GBP_CUDA(cudaGetLastError());
+    return GBP_OK;
+}
+
+int scale32(long long count, float* x, float a, cudaStream_t st)
+{
+    k_scale32<<<nblocks(count), kT, 0, st>>>(count, x, a);
     GBP_CUDA(cudaGetLastError());
     return GBP_OK;
 }

@@ -113,6 +113,8 @@ void net_dims(const NodalGeom& g, int dims[3]);
 int node_dot2(const NodalGeom& g, const float* x, const float* b, const float* r, double* out, cudaStream_t st);
 // out[i] = alpha * x[i] over a whole padded level array
 int scale_to64(long long count, const float* x, double alpha, double* out, cudaStream_t st);
+// x *= a over count padded positions
+int scale32(long long count, float* x, float a, cudaStream_t st);
 // out = base + alpha x over count padded positions (the previous solution plus the scaled increment)
 int axpy_to64(long long count, const double* base, const float* x, double alpha, double* out, cudaStream_t st);
 // dst = src at every unique node of the coarse level gc (the fine level's node (f i, f j, f k), f = 2^levels

@@ -104,6 +104,9 @@ void NodalSolver::destroy()
     if (ev1) cudaEventDestroy(ev1);
     if (ev2) cudaEventDestroy(ev2);
     if (evw) cudaEventDestroy(evw);
+    if (evi0) cudaEventDestroy(evi0);
+    if (evi1) cudaEventDestroy(evi1);
+    evi0 = evi1 = nullptr;
     ev0 = ev1 = ev2 = evw = nullptr;
     if (net_x0) cudaFree(net_x0);
     if (net_scr) cudaFree(net_scr);
@@ -800,6 +803,11 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats, bool from_prev)
     const bool mixed = opt.precision == GBP_PREC_MIXED;
     const int mmax = std::min(opt.ir_inner_cycles, kMaxInner);
     int m = mixed ? mmax : 1;
+    if (!evi0) {
+        GBP_CUDA(cudaEventCreate(&evi0));
+        GBP_CUDA(cudaEventCreate(&evi1));
+    }
+    GBP_CUDA(cudaEventRecord(evi0, st));
     while (rn > target) {
         if (it >= opt.maxiter) {
             status = GBP_NOT_CONVERGED;
@@ -827,6 +835,15 @@ int NodalSolver::solve(bool have_guess, gbp_stats* stats, bool from_prev)
             set_error("nodal solve: residual became NaN/Inf");
             break;
         }
+    }
+    GBP_CUDA(cudaEventRecord(evi1, st));
+    if (it > 0 && rn > 0.0 && r0 > rn && isfinite(rn)) {
+        // the warm start's cost model for the next solve
+        float ms_it = 0.f;
+        GBP_CUDA(cudaEventSynchronize(evi1));
+        cudaEventElapsedTime(&ms_it, evi0, evi1);
+        vc_rho = std::min(0.9, pow(rn / r0, 1.0 / vcycles));
+        vc_ms = ms_it / vcycles;
     }
     if (singular) {
         nodal_remove_mean(l0.g, phi, partials, dscal, 1, 0, 0, nullptr, st);
@@ -1298,17 +1315,35 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats, bool fro
         GBP_CUDA(cudaMemsetAsync(L[l].x32, 0, sizeof(float) * L[l].g.count, st));
         nodal_prolong_add<float>(L[l].g, L[l + 1].g, L[l + 1].x32, L[l].x32, st);
     }
-    // Galerkin factor against the residual of the start being replaced (b32 still holds it)
-    resid<float>(l0.g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st);
-    if (launch_rc) return launch_rc;
-    rc = nn::node_dot2(l0.g, l0.x32, l0.b32, l0.r32, net_scr, st);
-    if (rc) return rc;
+    // Galerkin factor against the residual of the start being replaced (b32 still holds it); the
+    // scaled prediction is then smoothed by two Jacobi sweeps of A x = b32 (the short-wavelength error a
+    // prediction leaves dominates its residual, and the smoother removes it for 0.2 ms) and scaled again
     double d[2] = {0.0, 0.0};
-    GBP_CUDA(cudaMemcpyAsync(d, net_scr, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    GBP_CUDA(cudaStreamSynchronize(st));
-    const double xax = d[0] - d[1];  // x.(b - r) = x.Ax in the scaled units of b32
-    const double alpha = (xax > 0.0 && isfinite(d[0])) ? d[0] / xax / scale32 : 0.0;
-    nk += net->launches() - nk0 + 6 + 2 * lv + (from_prev ? 2 : 0);
+    double alpha = 0.0;
+    for (int pass = 0; pass < 2; ++pass) {
+        resid<float>(l0.g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st);
+        if (launch_rc) return launch_rc;
+        rc = nn::node_dot2(l0.g, l0.x32, l0.b32, l0.r32, net_scr, st);
+        if (rc) return rc;
+        GBP_CUDA(cudaMemcpyAsync(d, net_scr, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+        const double xax = d[0] - d[1];  // x.(b - r) = x.Ax in the scaled units of b32
+        const double a = (xax > 0.0 && isfinite(d[0])) ? d[0] / xax : 0.0;
+        if (pass == 1 || a == 0.0) {
+            alpha = a / scale32;
+            break;
+        }
+        rc = nn::scale32(l0.g.count, l0.x32, (float)a, st);
+        if (rc) return rc;
+        for (int q = 0; q < 2; ++q) {
+            float* xin = q == 0 ? l0.x32 : l0.t32;
+            float* xout = q == 0 ? l0.t32 : l0.x32;
+            jacobi<float>(l0.g, l0.s32, xin, l0.b32, xout, st);
+            if (eb.on) eb_nodes<float>(l0.g, eb.e, 0, xin, l0.b32, xout, omega_eff, st);
+        }
+        if (launch_rc) return launch_rc;
+    }
+    nk += net->launches() - nk0 + 6 + 2 * lv + (from_prev ? 2 : 0) + 6;
     double rw = *rn;
     // candidate phi (phi_prev + alpha x, or alpha x) and its FP64 residual, in the level-0 FP64 scratch
     double* cand = from_prev ? l0.t64 : phi;
@@ -1325,7 +1360,20 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats, bool fro
         GBP_CUDA(cudaStreamSynchronize(st));
         rw = bits_to_double(hnorm[2]);
     }
-    const bool take = alpha != 0.0 && isfinite(rw) && rw < *rn;
+    // taken when its residual is below the start it would replace, and (once a solve has measured the
+    // V-cycle contraction and cost) when the V-cycles that smaller residual saves cost more than the
+    // network's device time so far
+    bool take = alpha != 0.0 && isfinite(rw) && rw < *rn;
+    double saved_ms = 0.0, spent_ms = 0.0;
+    if (take && vc_rho > 0.0 && vc_rho < 1.0 && vc_ms > 0.0) {
+        GBP_CUDA(cudaEventRecord(ev2, st));
+        GBP_CUDA(cudaEventSynchronize(ev2));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, evw, ev2);
+        spent_ms = ms;
+        saved_ms = log(rw / *rn) / log(vc_rho) * vc_ms;
+        take = saved_ms > spent_ms;
+    }
     // two bypasses in a row: skip the next 16 attempts, then try again
     warm_streak = take ? 0 : warm_streak + 1;
     if (warm_streak >= 2) {
@@ -1355,8 +1403,9 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats, bool fro
         stats->ms_warm = ms;
     }
     if (opt.verbose)
-        fprintf(stderr, "gbp nodal: warm start (%s) alpha %.4e, rel resid %.3e (%s)\n", from_prev ? "increment" : "phi",
-                alpha, bnorm > 0 ? rw / bnorm : rw, take ? "used" : "bypassed");
+        fprintf(stderr, "gbp nodal: warm start (%s) alpha %.4e, rel resid %.3e, saves %.3f ms of V-cycles for %.3f ms (%s)\n",
+                from_prev ? "increment" : "phi", alpha, bnorm > 0 ? rw / bnorm : rw, saved_ms, spent_ms,
+                take ? "used" : "bypassed");
     return GBP_OK;
 }
 

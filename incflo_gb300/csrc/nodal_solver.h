@@ -242,6 +242,11 @@ private:
     QWeights qw{};               // level-0 sigma sums of the shared-sum FP64 sweep (isotropic levels)
     bool use_qsweep = false;
     int warm_streak = 0;         // consecutive bypassed warm starts
+    // cost model of a warm start, from the last solve: the per-V-cycle residual contraction and the device
+    // time of one V-cycle (a candidate is taken only when the V-cycles its smaller residual saves cost more
+    // than the network did)
+    double vc_rho = 0.0, vc_ms = 0.0;
+    cudaEvent_t evi0 = nullptr, evi1 = nullptr;
     int warm_skip = 0;           // solves left before the next attempt after a streak
 };
 
