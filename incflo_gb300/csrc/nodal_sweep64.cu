@@ -473,7 +473,10 @@ int sm_count_cached()
 int sweep_z_chunks(const NodalGeom& g, int xy_tiles, int resident)
 {
     const int slots = resident * sm_count_cached();
-    const int max_chunks = (g.nu[2] + 15) / 16;
+    // chunks of at least 4 planes: on levels whose x / y tiles alone fill few SMs (128^3: 16 tiles) the
+    // z chunks supply the parallelism (128^3 Jacobi 54.6 -> 37.5 us against a 16-plane minimum; the
+    // 256^3 projection 11.91 -> 11.24 ms), and the wave / halo efficiency below picks the length
+    const int max_chunks = (g.nu[2] + 3) / 4;
     int best = 1;
     double best_eff = 0.0;
     for (int nz = 1; nz <= max_chunks; ++nz) {
