@@ -265,6 +265,35 @@ __global__ void k_amr_mask_sigma(long long count, const double* __restrict__ s, 
     if (t < count) out[t] = m[t] ? s[t] : 0.0;
 }
 
+// out = scale * v over whole padded arrays (FP64 -> FP32: the composite residual as the right-hand side of
+// the FP32 correction equation, the masked coarse sigma)
+__global__ void k_amr_to32(long long count, const double* __restrict__ v, double scale, float* __restrict__ out)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < count) out[t] = (float)(scale * v[t]);
+}
+
+// out = scale * r on the fine unknowns, 0 elsewhere (unique nodes, aliases written): the fine part of the
+// correction equation's right-hand side. The interface residuals are already folded into the coarse
+// interface nodes; the FP32 composite residual adds them again from -A e only.
+__global__ void k_amr_rhs32_fine(NodalGeom gf, const unsigned char* __restrict__ fcls, const double* __restrict__ r,
+                                 double scale, float* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const long long p = pidx(gf.sy, gf.sz, i, j, k);
+    store_node(out, gf, i, j, k, fcls[p] == F_DOF ? (float)(scale * r[p]) : 0.f);
+}
+
+// acc += e over whole padded arrays (the fine hierarchy's correction: zero on the masked nodes)
+__global__ void k_amr_add32(long long count, const float* __restrict__ e, float* __restrict__ acc)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < count) acc[t] += e[t];
+}
+
 // ------------------------------------------------------------------------------ composite operator
 __device__ __forceinline__ int cwrap(const NodalGeom& gc, int d, int v)
 {
@@ -273,8 +302,9 @@ __device__ __forceinline__ int cwrap(const NodalGeom& gc, int d, int v)
 
 // interface values of the fine level from the coarse one: aligned nodes copy, hanging nodes
 // interpolate along the coarse face they lie on
+template <typename T>
 __global__ void k_amr_fill_fine(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0, int off1,
-                                int off2, const double* __restrict__ pc, double* pf)
+                                int off2, const T* __restrict__ pc, T* pf)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -283,10 +313,10 @@ __global__ void k_amr_fill_fine(NodalGeom gc, NodalGeom gf, const unsigned char*
     const unsigned char c = fcls[pidx(gf.sy, gf.sz, i, j, k)];
     if (c != F_ALIGNED && c != F_HANGING) return;
     const int gpos[3] = {i + off0, j + off1, k + off2};
-    double acc = 0.0;
+    T acc = 0;
     int nodd = 0;
     for (int d = 0; d < 3; ++d) nodd += gpos[d] & 1;
-    const double w = nodd == 0 ? 1.0 : (nodd == 1 ? 0.5 : 0.25);
+    const T w = nodd == 0 ? T(1) : (nodd == 1 ? T(0.5) : T(0.25));
     for (int q = 0; q < 8; ++q) {
         int I[3];
         bool use = true;
@@ -306,9 +336,10 @@ __global__ void k_amr_fill_fine(NodalGeom gc, NodalGeom gf, const unsigned char*
 
 // v_c[I] += sum of the interface fine values that map to the coarse interface node I (the aligned
 // node with weight 1, hanging nodes 2I + delta with weight 2^-|delta|)
+template <typename T>
 __global__ void k_amr_sync(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ ccls,
                            const unsigned char* __restrict__ fcls, int off0, int off1, int off2,
-                           const double* __restrict__ vf, double* __restrict__ vc)
+                           const T* __restrict__ vf, T* __restrict__ vc)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -317,7 +348,7 @@ __global__ void k_amr_sync(NodalGeom gc, NodalGeom gf, const unsigned char* __re
     const long long p = pidx(gc.sy, gc.sz, i, j, k);
     if (ccls[p] != C_IFACE) return;
     const int off[3] = {off0, off1, off2};
-    double acc = 0.0;
+    T acc = 0;
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy)
             for (int dx = -1; dx <= 1; ++dx) {
@@ -328,7 +359,7 @@ __global__ void k_amr_sync(NodalGeom gc, NodalGeom gf, const unsigned char* __re
                 const unsigned char c = fcls[q];
                 const int nz = (dx != 0) + (dy != 0) + (dz != 0);
                 if ((nz == 0 && c == F_ALIGNED) || (nz > 0 && c == F_HANGING))
-                    acc += (nz == 0 ? 1.0 : (nz == 1 ? 0.5 : 0.25)) * vf[q];
+                    acc += (nz == 0 ? T(1) : (nz == 1 ? T(0.5) : T(0.25))) * vf[q];
             }
     vc[p] += acc;
 }
@@ -398,8 +429,9 @@ __global__ void k_amr_norm_f(NodalGeom gf, const unsigned char* __restrict__ fcl
 // restriction of the composite residual to the whole coarse level: the coarse unknowns' own residual
 // plus the trilinear (full-weighting) transpose of the fine unknowns' residuals
 // coarse nodes away from the fine region: their own residual only
-__global__ void k_amr_restrict_copy(NodalGeom gc, const unsigned char* __restrict__ ccls, const double* __restrict__ rc,
-                                    double* __restrict__ out)
+template <typename T>
+__global__ void k_amr_restrict_copy(NodalGeom gc, const unsigned char* __restrict__ ccls, const T* __restrict__ rc,
+                                    T* __restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -407,15 +439,16 @@ __global__ void k_amr_restrict_copy(NodalGeom gc, const unsigned char* __restric
     if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
     const long long p = pidx(gc.sy, gc.sz, i, j, k);
     const unsigned char c = ccls[p];
-    store_node(out, gc, i, j, k, (c == C_DOF || c == C_IFACE) ? rc[p] : 0.0);
+    store_node(out, gc, i, j, k, (c == C_DOF || c == C_IFACE) ? rc[p] : T(0));
 }
 
 // the coarse nodes whose 3 x 3 x 3 fine neighbourhood meets the fine bounding box (origin c0, extent
 // ce): own residual plus the fine contributions
+template <typename T>
 __global__ void k_amr_restrict(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ ccls,
                                const unsigned char* __restrict__ fcls, int off0, int off1, int off2,
-                               const double* __restrict__ rc, const double* __restrict__ rf, double* __restrict__ out,
-                               int3 c0, int3 ce)
+                               const T* __restrict__ rc, const T* __restrict__ rf, T* __restrict__ out, int3 c0,
+                               int3 ce)
 {
     const int ti = blockIdx.x * blockDim.x + threadIdx.x;
     const int tj = blockIdx.y * blockDim.y + threadIdx.y;
@@ -424,7 +457,7 @@ __global__ void k_amr_restrict(NodalGeom gc, NodalGeom gf, const unsigned char* 
     const int i = c0.x + ti, j = c0.y + tj, k = c0.z + tk;
     const long long p = pidx(gc.sy, gc.sz, i, j, k);
     const unsigned char c = ccls[p];
-    double acc = (c == C_DOF || c == C_IFACE) ? rc[p] : 0.0;
+    T acc = (c == C_DOF || c == C_IFACE) ? rc[p] : T(0);
     if (c != C_FIXED) {
         const int off[3] = {off0, off1, off2};
         for (int dz = -1; dz <= 1; ++dz)
@@ -436,15 +469,15 @@ __global__ void k_amr_restrict(NodalGeom gc, NodalGeom gf, const unsigned char* 
                     const long long q = pidx(gf.sy, gf.sz, m[0], m[1], m[2]);
                     if (fcls[q] != F_DOF) continue;
                     const int nz = (dx != 0) + (dy != 0) + (dz != 0);
-                    acc += (nz == 0 ? 1.0 : (nz == 1 ? 0.5 : (nz == 2 ? 0.25 : 0.125))) * rf[q];
+                    acc += (nz == 0 ? T(1) : (nz == 1 ? T(0.5) : (nz == 2 ? T(0.25) : T(0.125)))) * rf[q];
                 }
     }
     store_node(out, gc, i, j, k, acc);
 }
 
 // phi_c += e_c on the coarse unknowns; phi_f += (trilinear e_c) on the fine unknowns
-__global__ void k_amr_prolong_c(NodalGeom gc, const unsigned char* __restrict__ ccls, const double* __restrict__ e,
-                                double* pc)
+template <typename T>
+__global__ void k_amr_prolong_c(NodalGeom gc, const unsigned char* __restrict__ ccls, const T* __restrict__ e, T* pc)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -454,8 +487,9 @@ __global__ void k_amr_prolong_c(NodalGeom gc, const unsigned char* __restrict__ 
     const unsigned char c = ccls[p];
     if (c == C_DOF || c == C_IFACE) store_node(pc, gc, i, j, k, pc[p] + e[p]);
 }
+template <typename T>
 __global__ void k_amr_prolong_f(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0, int off1,
-                                int off2, const double* __restrict__ e, double* pf)
+                                int off2, const T* __restrict__ e, T* pf)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -473,13 +507,13 @@ __global__ void k_amr_prolong_f(NodalGeom gc, NodalGeom gf, const unsigned char*
         lo[d] = cwrap(gc, d, (gpos[d] - odd) / 2);
         hi[d] = odd ? cwrap(gc, d, (gpos[d] - 1) / 2 + 1) : lo[d];
     }
-    double acc = 0.0;
+    T acc = 0;
     for (int s = 0; s < 8; ++s) {
         const int sx = s & 1, sy = (s >> 1) & 1, sz = s >> 2;
         if ((sx && !(gpos[0] & 1)) || (sy && !(gpos[1] & 1)) || (sz && !(gpos[2] & 1))) continue;
         acc += e[pidx(gc.sy, gc.sz, sx ? hi[0] : lo[0], sy ? hi[1] : lo[1], sz ? hi[2] : lo[2])];
     }
-    const double scale = nodd == 0 ? 1.0 : (nodd == 1 ? 0.5 : (nodd == 2 ? 0.25 : 0.125));
+    const T scale = nodd == 0 ? T(1) : (nodd == 1 ? T(0.5) : (nodd == 2 ? T(0.25) : T(0.125)));
     store_node(pf, gf, i, j, k, fma(scale, acc, pf[q]));
 }
 
@@ -720,6 +754,8 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     add(gf.count, 1);
     for (int q = 0; q < 7; ++q) add(gc.count, 8);  // sc_m, sc_t, phi_c, b_c, r_c, rc_full, e_c
     for (int q = 0; q < 3; ++q) add(gf.count, 8);  // phi_f, b_f, r_f
+    for (int q = 0; q < 5; ++q) add(gc.count, 4);  // bc32, rc32, ec32, rcf32, scm32
+    for (int q = 0; q < 3; ++q) add(gf.count, 4);  // bf32, rf32, ef32
     add(3 * ncf, 8);                               // vel_f
     add(3 * ncf, 8);                               // gp_f
     add(ncf, 8);                                   // rho_f
@@ -759,6 +795,14 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     phi_f = pool.take<double>(gf.count);
     b_f = pool.take<double>(gf.count);
     r_f = pool.take<double>(gf.count);
+    bc32 = pool.take<float>(gc.count);
+    rc32 = pool.take<float>(gc.count);
+    ec32 = pool.take<float>(gc.count);
+    rcf32 = pool.take<float>(gc.count);
+    scm32 = pool.take<float>(gc.count);
+    bf32 = pool.take<float>(gf.count);
+    rf32 = pool.take<float>(gf.count);
+    ef32 = pool.take<float>(gf.count);
     vel_f = pool.take<double>(3 * ncf);
     gp_f = pool.take<double>(3 * ncf);
     rho_f = pool.take<double>(ncf);
@@ -878,34 +922,39 @@ void CompositeNodal::composite_residual(const double* bc, const double* bf, unsi
     }
 }
 
-// One refinement step on st: coarse correction on the restricted composite residual, fine correction
-// on the fresh fine residual with the interface held, then the composite residual and its norm (read
-// back into hnorm[1]).
+// out (whole coarse level) = the coarse unknowns' composite residual rc plus the full-weighting transpose
+// of the fine unknowns' residual rf
+template <typename T>
+void CompositeNodal::restrict_to_coarse(const T* rc, const T* rf, T* out)
+{
+    k_amr_restrict_copy<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, rc, out);
+    int lo[3], ext[3];
+    for (int d = 0; d < 3; ++d) {
+        // fine global node positions 2i-1 .. 2i+1 against the box's off .. off + nfb
+        lo[d] = std::max(0, (off[d] - 1) / 2);
+        const int hi = std::min(gc.nu[d] - 1, (off[d] + nfb[d] + 1) / 2 + 1);
+        if (gf.per[d]) {
+            lo[d] = 0;
+            ext[d] = gc.nu[d];
+        } else {
+            ext[d] = std::max(0, hi - lo[d] + 1);
+        }
+    }
+    if (ext[0] > 0 && ext[1] > 0 && ext[2] > 0) {
+        const dim3 grid((unsigned)((ext[0] + kB3.x - 1) / kB3.x), (unsigned)((ext[1] + kB3.y - 1) / kB3.y),
+                        (unsigned)((ext[2] + kB3.z - 1) / kB3.z));
+        k_amr_restrict<<<grid, kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], rc, rf, out,
+                                             make_int3(lo[0], lo[1], lo[2]), make_int3(ext[0], ext[1], ext[2]));
+    }
+}
+
+// One refinement step on st (plain FP64 form): coarse correction on the restricted composite residual,
+// fine correction on the fresh fine residual with the interface held, then the composite residual and
+// its norm (read back into hnorm[1]).
 void CompositeNodal::issue_step(double scale32)
 {
     const int m = 1;  // V-cycles per level per step (one is the fastest on the benchmark's workload)
-    // coarse correction on the restricted composite residual
-    k_amr_restrict_copy<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, r_c, rc_full);
-    {
-        int lo[3], ext[3];
-        for (int d = 0; d < 3; ++d) {
-            // fine global node positions 2i-1 .. 2i+1 against the box's off .. off + nfb
-            lo[d] = std::max(0, (off[d] - 1) / 2);
-            const int hi = std::min(gc.nu[d] - 1, (off[d] + nfb[d] + 1) / 2 + 1);
-            if (gf.per[d]) {
-                lo[d] = 0;
-                ext[d] = gc.nu[d];
-            } else {
-                ext[d] = std::max(0, hi - lo[d] + 1);
-            }
-        }
-        if (ext[0] > 0 && ext[1] > 0 && ext[2] > 0) {
-            const dim3 grid((unsigned)((ext[0] + kB3.x - 1) / kB3.x), (unsigned)((ext[1] + kB3.y - 1) / kB3.y),
-                            (unsigned)((ext[2] + kB3.z - 1) / kB3.z));
-            k_amr_restrict<<<grid, kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], r_c, r_f, rc_full,
-                                                 make_int3(lo[0], lo[1], lo[2]), make_int3(ext[0], ext[1], ext[2]));
-        }
-    }
+    restrict_to_coarse(r_c, r_f, rc_full);
     cudaMemsetAsync(e_c, 0, sizeof(double) * gc.count, st);
     crs.apply_vcycles(rc_full, e_c, m, scale32, st);
     k_amr_prolong_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, e_c, phi_c);
@@ -915,6 +964,43 @@ void CompositeNodal::issue_step(double scale32)
     resid_f(phi_f, b_f, r_f);
     fin.apply_vcycles(r_f, phi_f, m, scale32, st);
     // composite residual and its norm
+    cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st);
+    composite_residual(b_c, b_f, dnorm + 1);
+    cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+}
+
+// One refinement step of the mixed form: the FP64 composite residual (r_c, r_f), scaled into FP32, is the
+// right-hand side of the correction equation A e = r, which kInner two-level steps solve in FP32
+// arithmetic (the same steps as issue_step on e, with FP32 composite residuals between them); then
+// phi += e / scale on both levels in FP64 and the FP64 composite residual with its norm.
+void CompositeNodal::issue_outer32(double scale32)
+{
+    const unsigned ncb = (unsigned)((gc.count + kT - 1) / kT), nfb_ = (unsigned)((gf.count + kT - 1) / kT);
+    k_amr_to32<<<ncb, kT, 0, st>>>(gc.count, r_c, scale32, bc32);
+    k_amr_rhs32_fine<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, r_f, scale32, bf32);
+    cudaMemsetAsync(ec32, 0, sizeof(float) * gc.count, st);
+    cudaMemsetAsync(ef32, 0, sizeof(float) * gf.count, st);
+    for (int q = 0; q < kInner; ++q) {
+        const float* rc = q == 0 ? bc32 : rc32;
+        const float* rf = q == 0 ? bf32 : rf32;
+        restrict_to_coarse(rc, rf, rcf32);
+        crs.apply_vcycles32(rcf32, 1, st);
+        k_amr_prolong_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, crs.correction32(), ec32);
+        k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], crs.correction32(), ef32);
+        k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], (const float*)ec32, ef32);
+        nodal_resid<float>(gf_nomask, fin.sigma32(), ef32, bf32, rf32, nullptr, st);
+        fin.apply_vcycles32(rf32, 1, st);
+        k_amr_add32<<<nfb_, kT, 0, st>>>(gf.count, fin.correction32(), ef32);
+        if (q + 1 < kInner) {
+            // FP32 composite residual of e (the interface values of e_f are those of e_c already)
+            nodal_resid<float>(gf_nomask, fin.sigma32(), ef32, bf32, rf32, nullptr, st);
+            nodal_resid<float>(gc, scm32, ec32, bc32, rc32, nullptr, st);
+            k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], (const float*)rf32,
+                                                   rc32);
+        }
+    }
+    nodal_add_correction<float>(gc, phi_c, ec32, 1.0 / scale32, st);
+    nodal_add_correction<float>(gf_nomask, phi_f, ef32, 1.0 / scale32, st);
     cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st);
     composite_residual(b_c, b_f, dnorm + 1);
     cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
@@ -976,6 +1062,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     GBP_CUDA(cudaMemsetAsync(sc_t, 0, sizeof(double) * gc.count, st));
     nodal_sigma_from_rho(gc, f.rho_c, f.scale, f.rho0, sc_t, nullptr, st);
     k_amr_mask_sigma<<<(unsigned)((gc.count + kT - 1) / kT), kT, 0, st>>>(gc.count, sc_t, cmask_c, sc_m);
+    k_amr_to32<<<(unsigned)((gc.count + kT - 1) / kT), kT, 0, st>>>(gc.count, sc_m, 1.0, scm32);
     gbp_array4 sa{};
     sa.data = sig_f;
     for (int d = 0; d < 3; ++d) sa.hi[d] = nfb[d] - 1;
@@ -1056,6 +1143,13 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     }
     int it = 0, status = GBP_OK;
     const double r0 = rn;
+    const bool mixed = opt.precision == GBP_PREC_MIXED;
+    auto issue = [&](double sc) {
+        if (mixed)
+            issue_outer32(sc);
+        else
+            issue_step(sc);
+    };
     while (rn > target) {
         if (it >= opt.maxiter) {
             status = GBP_NOT_CONVERGED;
@@ -1073,7 +1167,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamBeginCapture(capst, cudaStreamCaptureModeThreadLocal);
             if (e == cudaSuccess) {
-                issue_step(scale32);
+                issue(scale32);
                 e = cudaStreamEndCapture(capst, &graph);
             }
             st = keep;
@@ -1089,7 +1183,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
         if (opt.use_graphs)
             GBP_CUDA(cudaGraphLaunch(gstep, st));
         else
-            issue_step(scale32);
+            issue(scale32);
         GBP_CUDA(cudaStreamSynchronize(st));
         GBP_CUDA(cudaGetLastError());
         rn = bits_to_double(hnorm[1]);
@@ -1157,7 +1251,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
         memset(stats, 0, sizeof(*stats));
         stats->status = status;
         stats->outer_iters = it + 1;
-        stats->vcycles = 2 * it;  // one V-cycle per level per step
+        stats->vcycles = 2 * it * (mixed ? kInner : 1);  // one V-cycle per level per two-level step
         stats->num_levels = 2;
         stats->rhs_norm = bnorm;
         stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;

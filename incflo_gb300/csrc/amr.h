@@ -14,7 +14,9 @@
 // filled from the coarse level, coarse residual with sigma zero on covered cells, plus the fine interface
 // residuals restricted to their coarse nodes), then one two-level correction per step: coarse V-cycles
 // on the restricted composite residual (prolonged trilinearly to the fine unknowns), a fresh fine
-// residual, fine V-cycles on the fine unknowns with the interface held.
+// residual, fine V-cycles on the fine unknowns with the interface held. In the mixed form the FP64
+// composite residual is the right-hand side of a correction equation that several such steps solve in
+// FP32 arithmetic before the next FP64 residual (iterative refinement, as in the single-level solve).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -92,6 +94,17 @@ private:
     // and its norm read-back) captured as a CUDA graph and replayed; recaptured when the FP32 scale or
     // the options change
     void issue_step(double scale32);
+    // the mixed form's step: kInner FP32 two-level steps on the correction equation per FP64 composite
+    // residual
+    void issue_outer32(double scale32);
+    template <typename T>
+    void restrict_to_coarse(const T* rc, const T* rf, T* out);
+#ifndef GBP_AMR_INNER
+#define GBP_AMR_INNER 8
+#endif
+    static constexpr int kInner = GBP_AMR_INNER;
+    float *bc32 = nullptr, *rc32 = nullptr, *ec32 = nullptr, *rcf32 = nullptr, *scm32 = nullptr;  // coarse
+    float *bf32 = nullptr, *rf32 = nullptr, *ef32 = nullptr;                                       // fine
     cudaStream_t capst = nullptr;
     cudaGraphExec_t gstep = nullptr;
     double gstep_scale = 0.0;

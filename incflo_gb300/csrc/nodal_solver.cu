@@ -696,6 +696,14 @@ void NodalSolver::apply_vcycles(const double* r, double* x, int m, double scale,
     cap_or_st = st;
 }
 
+void NodalSolver::apply_vcycles32(const float* b32, int m, cudaStream_t s)
+{
+    cap_or_st = s;
+    vcycle<float>(0, b32, true);
+    for (int c = 1; c < m; ++c) vcycle<float>(0, b32, false);
+    cap_or_st = st;
+}
+
 int NodalSolver::run_iteration(int m)
 {
     if (!opt.use_graphs) {

@@ -118,6 +118,11 @@ public:
     // residual r, in the plan's precision (FP32 V-cycles on r * scale in the mixed form). r and x are
     // level-0 arrays in the padded layout; r is not modified.
     void apply_vcycles(const double* r, double* x, int m, double scale, cudaStream_t s);
+    // The same on an FP32 level-0 right-hand side already scaled (mixed form only): m FP32 V-cycles from
+    // zero on b32; the correction stays in correction32() until the next V-cycle of this solver.
+    void apply_vcycles32(const float* b32, int m, cudaStream_t s);
+    const float* correction32() const { return (const float*)xres[0]; }
+    float* sigma32() const { return L[0].s32; }
 
     void reset_count() { nk = 0; }
     long long kernel_count() const { return nk; }
