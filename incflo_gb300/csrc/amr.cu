@@ -10,6 +10,7 @@
 #include "amr.h"
 #include "gbp_internal.cuh"
 #include "nodal_kernels.h"
+#include "nodal_sweep.h"
 
 namespace gbp {
 
@@ -129,6 +130,69 @@ __device__ __forceinline__ bool fine_local(const NodalGeom& gf, const int off[3]
         out[d] = v;
     }
     return true;
+}
+
+// the fine unknowns' values, 0 elsewhere (unique nodes, aliases written): the fine part of the composite
+// residual as the standard full-weighting restriction sees it
+__global__ void k_amr_dof_only(NodalGeom gf, const unsigned char* __restrict__ fcls, const float* __restrict__ v,
+                               float* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const long long p = pidx(gf.sy, gf.sz, i, j, k);
+    store_node(out, gf, i, j, k, fcls[p] == F_DOF ? v[p] : 0.f);
+}
+
+// coarse node (I, J, K) -> node of the fine box's coarsened level g1 (origin o = off / 2), or false
+__device__ __forceinline__ bool coarse_to_g1(const NodalGeom& g1, const int o[3], const int I[3], int q[3])
+{
+    for (int d = 0; d < 3; ++d) {
+        int v = I[d] - o[d];
+        if (g1.per[d]) {
+            v = wrap_period(v, g1.n[d]);
+        } else if (v < 0 || v >= g1.nu[d]) {
+            return false;
+        }
+        q[d] = v;
+    }
+    return true;
+}
+
+// out (whole coarse level) = the coarse unknowns' own residual + the full weighting r1 of the fine
+// unknowns' residual (on g1, the fine box coarsened by 2), except on fixed nodes
+__global__ void k_amr_combine(NodalGeom gc, NodalGeom g1, const unsigned char* __restrict__ ccls, int o0, int o1,
+                              int o2, const float* __restrict__ rc, const float* __restrict__ r1, float* out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gc.nu[0] || j >= gc.nu[1] || k >= gc.nu[2]) return;
+    const long long p = pidx(gc.sy, gc.sz, i, j, k);
+    const unsigned char c = ccls[p];
+    float v = (c == C_DOF || c == C_IFACE) ? rc[p] : 0.f;
+    const int o[3] = {o0, o1, o2}, I[3] = {i, j, k};
+    int q[3];
+    if (c != C_FIXED && coarse_to_g1(g1, o, I, q)) v += r1[pidx(g1.sy, g1.sz, q[0], q[1], q[2])];
+    store_node(out, gc, i, j, k, v);
+}
+
+// x1 (g1, the fine box coarsened by 2) = the coarse-level values at the same positions (aliases written)
+__global__ void k_amr_gather_g1(NodalGeom gc, NodalGeom g1, int o0, int o1, int o2, const float* __restrict__ xc,
+                                float* x1)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= g1.nu[0] || j >= g1.nu[1] || k >= g1.nu[2]) return;
+    const int o[3] = {o0, o1, o2}, q[3] = {i, j, k};
+    int I[3];
+    for (int d = 0; d < 3; ++d) {
+        I[d] = q[d] + o[d];
+        if (gc.per[d]) I[d] = wrap_period(I[d], gc.n[d]);
+    }
+    store_node(x1, g1, i, j, k, xc[pidx(gc.sy, gc.sz, I[0], I[1], I[2])]);
 }
 
 __global__ void k_amr_classify_coarse(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0,
@@ -756,6 +820,17 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     for (int q = 0; q < 3; ++q) add(gf.count, 8);  // phi_f, b_f, r_f
     for (int q = 0; q < 5; ++q) add(gc.count, 4);  // bc32, rc32, ec32, rcf32, scm32
     for (int q = 0; q < 3; ++q) add(gf.count, 4);  // bf32, rf32, ef32
+    xfer1 = fin.num_levels() >= 2;
+    if (xfer1) {
+        g1n = fin.level(1).g;
+        g1n.mask = nullptr;
+        for (int d = 0; d < 3; ++d)
+            if (g1n.n[d] * 2 != gf.n[d] || g1n.per[d] != gf.per[d] || (off[d] & 1)) xfer1 = false;
+    }
+    if (xfer1) {
+        add(gf.count, 4);   // rm32
+        add(g1n.count, 4);  // x1_32
+    }
     add(3 * ncf, 8);                               // vel_f
     add(3 * ncf, 8);                               // gp_f
     add(ncf, 8);                                   // rho_f
@@ -772,6 +847,7 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     add(nparts + 64, 8);
     add(8, 8);
     add(8, 8);
+    add(8, 4);  // derr
     need += 4096;
     rc = pool.reserve(need);
     if (rc) return rc;
@@ -803,6 +879,10 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     bf32 = pool.take<float>(gf.count);
     rf32 = pool.take<float>(gf.count);
     ef32 = pool.take<float>(gf.count);
+    if (xfer1) {
+        rm32 = pool.take<float>(gf.count);
+        x1_32 = pool.take<float>(g1n.count);
+    }
     vel_f = pool.take<double>(3 * ncf);
     gp_f = pool.take<double>(3 * ncf);
     rho_f = pool.take<double>(ncf);
@@ -812,6 +892,8 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     part = pool.take<double>(nparts + 64);
     scal = pool.take<double>(8);
     dnorm = pool.take<unsigned long long>(8);
+    derr = pool.take<unsigned>(8);
+    GBP_CUDA(cudaMemsetAsync(derr, 0, 8 * sizeof(unsigned), st));
     GBP_CUDA(cudaMallocHost(&hnorm, 8 * sizeof(unsigned long long)));
     GBP_CUDA(cudaEventCreate(&ev0));
     GBP_CUDA(cudaEventCreate(&ev1));
@@ -969,6 +1051,39 @@ void CompositeNodal::issue_step(double scale32)
     cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
 }
 
+// launch errors and bounded-wait time-outs of the level sweeps issued by a step (both solvers' and this
+// object's own); the error words are cleared
+int CompositeNodal::sweep_status()
+{
+    int rc = launch_rc;
+    launch_rc = 0;
+    for (NodalSolver* sv : {&crs, &fin}) {
+        const int r = sv->take_sweep_status(st);
+        if (!rc) rc = r;
+    }
+    unsigned herr = 0;
+    GBP_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    GBP_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+        GBP_CUDA(cudaMemsetAsync(derr, 0, sizeof(unsigned), st));
+        if (!rc) {
+            set_error("amr solve: a bounded device wait (TMA pipeline) ran out");
+            rc = GBP_TIMEOUT;
+        }
+    }
+    return rc;
+}
+
+void CompositeNodal::resid32(const NodalGeom& g, const float* s, const float* x, const float* b, float* r)
+{
+    if (vsweep32_supported(g)) {
+        const int rc = vsweep32(g, 1, s, x, b, r, 0.f, derr, st);
+        if (rc && !launch_rc) launch_rc = rc;
+    } else {
+        nodal_resid<float>(g, s, x, b, r, nullptr, st);
+    }
+}
+
 // One refinement step of the mixed form: the FP64 composite residual (r_c, r_f), scaled into FP32, is the
 // right-hand side of the correction equation A e = r, which kInner two-level steps solve in FP32
 // arithmetic (the same steps as issue_step on e, with FP32 composite residuals between them); then
@@ -983,18 +1098,31 @@ void CompositeNodal::issue_outer32(double scale32)
     for (int q = 0; q < kInner; ++q) {
         const float* rc = q == 0 ? bc32 : rc32;
         const float* rf = q == 0 ? bf32 : rf32;
-        restrict_to_coarse(rc, rf, rcf32);
+        const int o0 = off[0] / 2, o1 = off[1] / 2, o2 = off[2] / 2;
+        if (xfer1) {
+            k_amr_dof_only<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, rf, rm32);
+            nodal_restrict<float>(gf_nomask, g1n, rm32, x1_32, st);
+            k_amr_combine<<<gnodes(gc), kB3, 0, st>>>(gc, g1n, ccls, o0, o1, o2, rc, x1_32, rcf32);
+        } else {
+            restrict_to_coarse(rc, rf, rcf32);
+        }
         crs.apply_vcycles32(rcf32, 1, st);
         k_amr_prolong_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, crs.correction32(), ec32);
-        k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], crs.correction32(), ef32);
+        if (xfer1) {
+            k_amr_gather_g1<<<gnodes(g1n), kB3, 0, st>>>(gc, g1n, o0, o1, o2, crs.correction32(), x1_32);
+            nodal_prolong_add<float>(gf, g1n, x1_32, ef32, st);
+        } else {
+            k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], crs.correction32(),
+                                                        ef32);
+        }
         k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], (const float*)ec32, ef32);
-        nodal_resid<float>(gf_nomask, fin.sigma32(), ef32, bf32, rf32, nullptr, st);
+        resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
         fin.apply_vcycles32(rf32, 1, st);
         k_amr_add32<<<nfb_, kT, 0, st>>>(gf.count, fin.correction32(), ef32);
         if (q + 1 < kInner) {
             // FP32 composite residual of e (the interface values of e_f are those of e_c already)
-            nodal_resid<float>(gf_nomask, fin.sigma32(), ef32, bf32, rf32, nullptr, st);
-            nodal_resid<float>(gc, scm32, ec32, bc32, rc32, nullptr, st);
+            resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
+            resid32(gc, scm32, ec32, bc32, rc32);
             k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], (const float*)rf32,
                                                    rc32);
         }
@@ -1186,6 +1314,7 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
             issue(scale32);
         GBP_CUDA(cudaStreamSynchronize(st));
         GBP_CUDA(cudaGetLastError());
+        if ((rc = sweep_status())) return rc;
         rn = bits_to_double(hnorm[1]);
         ++it;
         if (opt.verbose > 1) fprintf(stderr, "gbp amr: iter %d rel resid %.3e\n", it, bnorm > 0 ? rn / bnorm : rn);

@@ -105,6 +105,16 @@ private:
     static constexpr int kInner = GBP_AMR_INNER;
     float *bc32 = nullptr, *rc32 = nullptr, *ec32 = nullptr, *rcf32 = nullptr, *scm32 = nullptr;  // coarse
     float *bf32 = nullptr, *rf32 = nullptr, *ef32 = nullptr;                                       // fine
+    // FP32 residual of one composite part: the whole-row sweep where it applies
+    void resid32(const NodalGeom& g, const float* s, const float* x, const float* b, float* r);
+    // the inner steps' transfers through the fine box coarsened by 2 (the fine solver's level 1, g1n
+    // without its mask): the standard full weighting / trilinear kernels plus a gather and a combine
+    bool xfer1 = false;
+    NodalGeom g1n{};
+    float *rm32 = nullptr, *x1_32 = nullptr;
+    unsigned* derr = nullptr;  // device error word of the whole-row sweeps issued here
+    int launch_rc = 0;         // first launch error of a step (tensor-map set-up)
+    int sweep_status();
     cudaStream_t capst = nullptr;
     cudaGraphExec_t gstep = nullptr;
     double gstep_scale = 0.0;

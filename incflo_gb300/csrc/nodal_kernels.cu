@@ -353,12 +353,32 @@ __global__ void k_mask_load(NodalGeom g, gbp_iarray4 m, unsigned char* __restric
     if (!v) atomicAdd(zeros, 1u);
 }
 
+// A coarse node is free only where every fine node of its support (2I-1 .. 2I+1 per direction, inside
+// the domain) is free. Injection alone moves the held region's edge outwards by up to one coarse spacing
+// per level; the coarse correction then overshoots next to it and the V-cycle can diverge (measured at
+// 128^3 with masks that vary within the planes).
 __global__ void k_mask_coarsen(NodalGeom gf, NodalGeom gc, const unsigned char* __restrict__ mf,
                                unsigned char* __restrict__ mc)
 {
     int I, J, K;
     if (!grid3_node(gc, I, J, K)) return;
-    store_node(mc, gc, I, J, K, mf[pidx(gf.sy, gf.sz, 2 * I, 2 * J, 2 * K)]);
+    const int C[3] = {I, J, K};
+    unsigned char v = 1;
+    for (int q = 0; q < 27 && v; ++q) {
+        int f[3];
+        bool in = true;
+        for (int d = 0; d < 3; ++d) {
+            f[d] = 2 * C[d] + (d == 0 ? q % 3 : (d == 1 ? (q / 3) % 3 : q / 9)) - 1;
+            if (gf.per[d]) {
+                if (f[d] < 0) f[d] += gf.n[d];
+                if (f[d] >= gf.n[d]) f[d] -= gf.n[d];
+            } else if (f[d] < 0 || f[d] > gf.n[d]) {
+                in = false;
+            }
+        }
+        if (in && !mf[pidx(gf.sy, gf.sz, f[0], f[1], f[2])]) v = 0;
+    }
+    store_node(mc, gc, I, J, K, v);
 }
 
 // ---------------------------------------------------------------------------------------

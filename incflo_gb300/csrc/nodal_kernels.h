@@ -111,7 +111,8 @@ void nodal_load_phi(const NodalGeom& g, const gbp_array4& in, double* phi, cudaS
 void stream_triad(const float* a, const float* b, const float* c, float* out, long long n, cudaStream_t st);
 // strong-form divergence -b_i / V_i into a nodal array (all nodes 0..n)
 void nodal_store_div(const NodalGeom& g, const gbp_array4& out, const double* b, cudaStream_t st);
-// overset mask: level 0 from the caller's int array (zeros counted into *zeros), coarse levels by injection
+// overset mask: level 0 from the caller's int array (zeros counted into *zeros); a coarse node is free where
+// every fine node of its support is
 void nodal_mask_load(const NodalGeom& g, const gbp_iarray4& m, unsigned char* out, unsigned* zeros, cudaStream_t st);
 void nodal_mask_coarsen(const NodalGeom& gf, const NodalGeom& gc, const unsigned char* mf, unsigned char* mc,
                         cudaStream_t st);

@@ -122,6 +122,10 @@ public:
     // zero on b32; the correction stays in correction32() until the next V-cycle of this solver.
     void apply_vcycles32(const float* b32, int m, cudaStream_t s);
     const float* correction32() const { return (const float*)xres[0]; }
+    // For work issued through apply_vcycles / apply_vcycles32: GBP_OK, the first launch error (cleared), or
+    // GBP_TIMEOUT when a bounded device wait of a level sweep ran out (the device error word is read and
+    // cleared; synchronises s).
+    int take_sweep_status(cudaStream_t s);
     float* sigma32() const { return L[0].s32; }
 
     void reset_count() { nk = 0; }
@@ -131,7 +135,8 @@ public:
     // Test hook: the level-0 FP32 whole-row sweeps against the one-node-per-thread kernels on seeded
     // level-0 / level-1 data (the plan's sigma): max |new - reference| / max |reference| over every
     // padded position for [0] Jacobi, [1] residual, [2] residual + restriction (coarse level), [3]
-    // prolongation + Jacobi. Overwrites solver scratch (the next solve refills it).
+    // prolongation + Jacobi ([2], [3] -1 with an overset mask). Overwrites solver scratch (the next solve
+    // refills it).
     int check_level_kernels(double diff[4]);
     int check_level_kernels_on(float* A, float* C, double diff[4]);
 

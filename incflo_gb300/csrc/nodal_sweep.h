@@ -41,10 +41,11 @@ int sm_count_cached();
 int sweep32_run(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,
                 unsigned* err, unsigned long long* norm, cudaStream_t st);
 
-// FP32 whole-row sweeps with fused grid transfers (nodal_vsweep32.cu), isotropic levels without an
-// overset mask whose rows hold at most 512 nodes.
+// FP32 whole-row sweeps with fused grid transfers (nodal_vsweep32.cu), isotropic levels whose rows hold
+// at most 512 nodes (Jacobi and residual also with an overset mask: masked nodes are held at 0).
 bool vsweep32_supported(const NodalGeom& g);
-// ... and whose coarse level is the standard coarsening by 2 (residual + restriction, prolongation + sweep)
+// ... and whose coarse level is the standard coarsening by 2 (residual + restriction, prolongation + sweep),
+// neither of them with an overset mask
 bool vsweep32_transfer_supported(const NodalGeom& g, const NodalGeom& gc);
 // mode 0: Jacobi sweep, 1: residual
 int vsweep32(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,

@@ -449,6 +449,19 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY, RPT>::TTR,
             for (int q = 0; q < 5; ++q) SY[r][q] = S[r][q] + S[r + 1][q];
         const int k = P - 1;  // node plane completed at this step (s >= 2)
         const bool dk = (g.dlo[2] && k == 0) || (g.dhi[2] && k == g.n[2]);
+        // overset mask (Jacobi and residual only): masked nodes of plane k are held at 0 like Dirichlet
+        // nodes; bit r*4+q as in dmask
+        unsigned mk = 0;
+        if (MODE <= 1 && g.mask && s >= 2) {
+#pragma unroll
+            for (int r = 0; r < RPT; ++r)
+                if (j0 + r < g.nu[1]) {
+                    const unsigned char* mr = g.mask + pidx(g.sy, g.sz, i0, j0 + r, k);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (q < nact && !mr[q]) mk |= 1u << (r * 4 + q);
+                }
+        }
         float v[RPT][4];
 #pragma unroll
         for (int r = 0; r < RPT; ++r) {
@@ -486,7 +499,7 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY, RPT>::TTR,
                         val = bb[q] - ax;
                     else
                         val = fmaf(a.omega * (bb[q] - ax), rcp_approx(a.k0 * (ss[r][q] + sgl)), cA);
-                    v[r][q] = (dk || ((dmask >> (r * 4 + q)) & 1u)) ? 0.f : val;
+                    v[r][q] = (dk || (((dmask | mk) >> (r * 4 + q)) & 1u)) ? 0.f : val;
                 }
                 // node plane P (registers Bn) gets its lower half
                 acc[r][q] = fmaf(-2.f * (cB - cA), sgl, G) + xb;
@@ -664,18 +677,20 @@ bool vsweep32_supported(const NodalGeom& g)
 {
     const long long nodes = (long long)g.nu[0] * g.nu[1] * g.nu[2];
     int bw = 0;
-    // isotropic, no overset mask, whole rows in one CTA (periodic x: a multiple of 4 nodes so that node
+    // isotropic, whole rows in one CTA (periodic x: a multiple of 4 nodes so that node
     // n-1 is the last thread's last node); a thread reads staged columns up to 4 TX + 4, which must lie
     // inside the padded row
     const int TX = (g.nu[0] + 3) / 4;
-    return g.iso && !g.mask && nodes >= (1ll << 20) && g.nu[0] <= 4 * kMaxTX && g.nu[0] >= 16 && g.nu[1] >= 4 &&
+    return g.iso && nodes >= (1ll << 20) && g.nu[0] <= 4 * kMaxTX && g.nu[0] >= 16 && g.nu[1] >= 4 &&
            g.nu[2] >= 4 && (!g.per[0] || g.nu[0] % 4 == 0) && 4 * TX + 5 <= (int)g.sy &&
            row_boxes((int)g.sy, &bw) > 0;
 }
 
 bool vsweep32_transfer_supported(const NodalGeom& g, const NodalGeom& gc)
 {
-    // the coarse level is the standard coarsening by 2 of this one
+    // the coarse level is the standard coarsening by 2 of this one; no overset mask on either (the fused
+    // prolongation would add the coarse correction to masked fine nodes)
+    if (g.mask || gc.mask) return false;
     for (int d = 0; d < 3; ++d)
         if (gc.n[d] * 2 != g.n[d] || gc.per[d] != g.per[d]) return false;
     int bw = 0;

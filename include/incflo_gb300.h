@@ -183,7 +183,8 @@ int gbp_nodal_project(gbp_plan* plan, gbp_array4* vel, gbp_array4* phi, gbp_arra
 /* getLinOp().setOversetMask(lev, mask) (incflo_apply_nodal_projection.cpp:203-210, mask from
  * incflo::make_nodalBC_mask, src/boundary_conditions/incflo_set_bcs.cpp:10-53): nodal integer
  * mask over nodes 0..n, 0 = phi is held at 0 there (the Dirichlet part of a mixed boundary), nonzero
- * = solve. Coarse levels take the mask by injection. NULL (or data == NULL) removes the mask. */
+ * = solve. A coarse-level node is free where every fine node of its support (2I-1 .. 2I+1 per
+ * direction) is. NULL (or data == NULL) removes the mask. */
 int gbp_nodal_set_overset_mask(gbp_plan* plan, const gbp_iarray4* mask);
 
 /* Cut cells of a nodal plan: the EB factory of the NodalProjector's MultiFabs
@@ -396,7 +397,8 @@ int gbp_plan_time_kernel(gbp_plan* plan, int which, int reps, double* ms_per_lau
  * sigma), runs the FP32 whole-row level kernels and the one-node-per-thread kernels they replace and
  * writes max |new - reference| / max |reference| over every padded position (periodic aliases
  * included) for diff[0] Jacobi, diff[1] residual, diff[2] residual + restriction, diff[3]
- * prolongation + Jacobi. GBP_BAD_ARG when the whole-row kernels do not apply to the plan's level 0. */
+ * prolongation + Jacobi (-1 for [2] and [3] on a level with an overset mask, where the fused transfers do
+ * not run). GBP_BAD_ARG when the whole-row kernels do not apply to the plan's level 0. */
 int gbp_plan_check_level_kernels(gbp_plan* plan, double diff[4]);
 
 /* No counterpart in the reference: a test hook. One FP32 V-cycle from the first level that a plan cycles
