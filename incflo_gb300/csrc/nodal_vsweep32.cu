@@ -70,12 +70,15 @@ namespace {
 #ifndef GBP_VS_TY_256
 #define GBP_VS_TY_256 8
 #endif
+#ifndef GBP_VS_TY_512
+#define GBP_VS_TY_512 2
+#endif
 #ifndef GBP_VS_RPT
 #define GBP_VS_RPT 2  // node rows per thread
 #endif
 constexpr int kMaxTX = 128;  // threads per row: 4 * 128 = 512 nodes per row at most
 // CTA shapes: TY rows per CTA by the row width (TX threads of 4 nodes): 8 rows for rows of <= 128
-// nodes (TX <= 32), GBP_VS_TY_256 for <= 256 (TX <= 64), 2 for <= 512 (TX <= 128)
+// nodes (TX <= 32), GBP_VS_TY_256 for <= 256 (TX <= 64), GBP_VS_TY_512 for <= 512 (TX <= 128)
 template <int MODE>
 struct Stages {
     static constexpr int N = MODE <= 1 ? GBP_VS_STAGES_PLAIN : GBP_VS_STAGES_XFER;
@@ -701,7 +704,7 @@ bool vsweep32_transfer_supported(const NodalGeom& g, const NodalGeom& gc)
            2 * TX + 7 <= (int)gc.sy;
 }
 
-// rows per CTA by the row width: 8 (<= 128 nodes), GBP_VS_TY_256 (<= 256), 2 (<= 512)
+// rows per CTA by the row width: 8 (<= 128 nodes), GBP_VS_TY_256 (<= 256), GBP_VS_TY_512 (<= 512)
 template <int MODE>
 static int launch_any(const NodalGeom& g, const NodalGeom* gc, const float* s, const float* x, const float* b,
                       const float* e, float* out, float omega, unsigned* err, cudaStream_t st)
@@ -709,7 +712,7 @@ static int launch_any(const NodalGeom& g, const NodalGeom* gc, const float* s, c
     const int TX = (g.nu[0] + 3) / 4;
     if (TX <= 32) return launch<MODE, 8, 32>(g, gc, s, x, b, e, out, omega, err, st);
     if (TX <= 64) return launch<MODE, GBP_VS_TY_256, 64>(g, gc, s, x, b, e, out, omega, err, st);
-    return launch<MODE, 2, 128>(g, gc, s, x, b, e, out, omega, err, st);
+    return launch<MODE, GBP_VS_TY_512, 128>(g, gc, s, x, b, e, out, omega, err, st);
 }
 
 int vsweep32(const NodalGeom& g, int mode, const float* s, const float* x, const float* b, float* out, float omega,

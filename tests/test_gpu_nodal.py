@@ -274,8 +274,9 @@ def test_whole_row_sweeps_with_overset_mask(gpu_lib):
         proj.setOversetMask(None)  # the shared plan goes back to the unmasked operator
 
 
-@pytest.mark.parametrize("case", [((256, 256, 256), (1.0, 1.0, 1.0), (P, P, N), (P, P, N)), LARGE[1]],
-                         ids=["256-periodic-xy", "192-dirichlet-inflow"])
+@pytest.mark.parametrize("case", [((256, 256, 256), (1.0, 1.0, 1.0), (P, P, N), (P, P, N)), LARGE[1],
+                                  ((512, 64, 64), (8.0, 1.0, 1.0), (P, P, N), (P, P, N))],
+                         ids=["256-periodic-xy", "192-dirichlet-inflow", "512-rows"])
 def test_whole_row_level_kernels_match_plain_kernels(gpu_lib, case):
     """The FP32 whole-row sweeps (Jacobi, residual, fused residual + restriction, fused prolongation +
     Jacobi) against the one-node-per-thread kernels on seeded level data (the plan's sigma), over every
