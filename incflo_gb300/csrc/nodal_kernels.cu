@@ -737,10 +737,10 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_vcycle(CoarseCycle<T>
         T* buf[2] = {a.x[q], a.t[q]};
         int cur = 0;
         if (a.nu1 > 0) {
-            cc_jacobi<T>(g, a.s[q], nullptr, a.b[q], buf[0], a.omega, true, t0, dt);
+            cc_jacobi<T>(g, a.s[q], nullptr, a.b[q], buf[0], a.wpre[0], true, t0, dt);
             cluster_barrier();
             for (int p = 1; p < a.nu1; ++p) {
-                cc_jacobi<T>(g, a.s[q], buf[cur], a.b[q], buf[cur ^ 1], a.omega, false, t0, dt);
+                cc_jacobi<T>(g, a.s[q], buf[cur], a.b[q], buf[cur ^ 1], a.wpre[p % kSweepWeights], false, t0, dt);
                 cluster_barrier();
                 cur ^= 1;
             }
@@ -764,7 +764,7 @@ __global__ void __launch_bounds__(kCoarseThreads) k_coarse_vcycle(CoarseCycle<T>
         cc_prolong<T>(g, a.g[q + 1], slot[q + 1] ? a.t[q + 1] : a.x[q + 1], buf[cur], t0, dt);
         cluster_barrier();
         for (int p = 0; p < a.nu2; ++p) {
-            cc_jacobi<T>(g, a.s[q], buf[cur], a.b[q], buf[cur ^ 1], a.omega, false, t0, dt);
+            cc_jacobi<T>(g, a.s[q], buf[cur], a.b[q], buf[cur ^ 1], a.wpost[p % kSweepWeights], false, t0, dt);
             cluster_barrier();
             cur ^= 1;
         }

@@ -56,6 +56,8 @@ void nodal_bottom_dense(const NodalGeom& g, const double* M, const T* b, T* x, i
 // residual, restriction, bottom and prolongation of each level). Level data stays in L2 and is read
 // with L2-coherent loads.
 constexpr int kCoarseMaxLevels = 10;
+// weights of the smoothing sweeps of one V-cycle level (pre and post each), repeated beyond this count
+constexpr int kSweepWeights = 8;
 template <typename T>
 struct CoarseCycle {
     int nl;  // levels, >= 2 (at least one above the bottom)
@@ -67,7 +69,8 @@ struct CoarseCycle {
     T* r[kCoarseMaxLevels];
     const double* M;         // dense inverse of the bottom operator
     int singular;            // the bottom has the constants as null space
-    T omega;
+    T wpre[kSweepWeights];   // Jacobi weight of pre-smoothing sweep p: wpre[p % kSweepWeights]
+    T wpost[kSweepWeights];  // ... and of post-smoothing sweep p
     int nu1, nu2;
 };
 constexpr int kCoarseThreads = 1024;

@@ -135,9 +135,9 @@ void NodalSolver::destroy()
 
 int NodalSolver::set_options(const gbp_options& o)
 {
-    if (o.nu1 < 0 || o.nu2 < 0 || o.nu1 + o.nu2 < 1 || !(o.omega > 0.0 && o.omega < 2.0) ||
+    if (o.nu1 < 0 || o.nu2 < 0 || o.nu1 + o.nu2 < 1 || !(o.omega >= 0.0 && o.omega < 2.0) ||
         o.ir_inner_cycles < 1 || o.maxiter < 0) {
-        set_error("nodal options: need nu1+nu2 >= 1, 0 < omega < 2, ir_inner_cycles >= 1, maxiter >= 0");
+        set_error("nodal options: need nu1+nu2 >= 1, 0 <= omega < 2, ir_inner_cycles >= 1, maxiter >= 0");
         return GBP_BAD_ARG;
     }
     const bool regraph = o.precision != opt.precision || o.nu1 != opt.nu1 || o.nu2 != opt.nu2 ||
@@ -154,19 +154,50 @@ int NodalSolver::set_options(const gbp_options& o)
     return GBP_OK;
 }
 
-// The smoother's weight: the requested omega, capped by the Gershgorin bound of the Jacobi-scaled
-// operator, lambda_max(D^-1 A) <= 1 + sum_{q != 0} |K_q| / K_0 per element (every cell's row of a node has
-// that ratio, so the sigma-weighted sum does too). Cubic cells give 1 + 1 and keep omega = 0.85; cells
-// stretched beyond an aspect ratio of about 2 have positive couplings, a larger bound, and a damped
-// Jacobi at 0.85 that would diverge. All levels share the ratio (every direction coarsens by 2).
+// The smoother's weights. The Jacobi-scaled operator has lambda_max(D^-1 A) <= lb = 1 + sum_{q != 0} |K_q| /
+// K_0 per element (Gershgorin; every cell's row of a node has that ratio, so the sigma-weighted sum does
+// too): 2 for cubic cells, more for cells stretched beyond an aspect ratio of about 2, whose positive
+// couplings would make a damped Jacobi at 0.85 diverge. All levels share the ratio (every direction
+// coarsens by 2).
+// omega > 0 (0.85 by default): that fixed weight for every sweep, capped at 0.85 * 2 / lb. omega = 0: the
+// nu sweeps of a level's pre- (post-) smoothing take the weights 1 / lambda_k, lambda_k the roots of the
+// degree-nu Chebyshev polynomial on [lb / 4, lb], so that together they minimise the largest amplification
+// over that interval: for cubic cells and two sweeps 0.220 against 0.490 at 0.85 (the constant-coefficient
+// high-frequency modes, lambda in [0.5, 1.5]: 0.220 against 0.331). Post-smoothing takes the weights in
+// the reverse order. Cut cells keep the fixed weight (their elements' couplings are not bounded by lb).
+// On the 256^3 interface workload the V-cycle contraction is set by the coarse-grid correction: 0.093 per
+// V-cycle with the Chebyshev weights against 0.113 at 0.85, but a weaker first V-cycle, and both reach
+// 1e-10 in 10 V-cycles, so the fixed weight stays the default.
 void NodalSolver::set_omega()
 {
-    omega_eff = opt.omega;
-    if (L.empty()) return;
-    const double* K = L[0].g.K;
-    double off = 0.0;
-    for (int q = 1; q < 8; ++q) off += fabs(K[q]);
-    if (K[0] > 0.0) omega_eff = std::min(opt.omega, 0.85 * 2.0 / (1.0 + off / K[0]));
+    const double w0 = opt.omega > 0.0 ? opt.omega : 0.85;
+    omega_eff = w0;
+    double lb = 2.0;
+    if (!L.empty()) {
+        const double* K = L[0].g.K;
+        double off = 0.0;
+        for (int q = 1; q < 8; ++q) off += fabs(K[q]);
+        if (K[0] > 0.0) {
+            lb = 1.0 + off / K[0];
+            omega_eff = std::min(w0, 0.85 * 2.0 / lb);
+        }
+    }
+    const bool cheb = opt.omega == 0.0 && !eb.on;
+    auto fill = [&](double* w, int nu, bool reverse) {
+        const int deg = std::max(1, std::min(nu, kSweepWeights));
+        for (int p = 0; p < kSweepWeights; ++p) {
+            if (!cheb) {
+                w[p] = omega_eff;
+                continue;
+            }
+            const int k = (reverse ? deg - 1 - (p % deg) : (p % deg));
+            // roots in decreasing order: the smallest weight first
+            const double lam = 0.625 * lb + 0.375 * lb * cos((2 * k + 1) * M_PI / (2 * deg));
+            w[p] = 1.0 / lam;
+        }
+    };
+    fill(wpre, opt.nu1, false);
+    fill(wpost, opt.nu2, true);
 }
 
 int NodalSolver::init(const gbp_geometry& geom, const int bc_lo[3], const int bc_hi[3], const gbp_options& o,
@@ -486,20 +517,20 @@ struct LevelBufs<float> {
 };
 
 template <typename T>
-void NodalSolver::jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, cudaStream_t s_)
+void NodalSolver::jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, double w, cudaStream_t s_)
 {
     if (sizeof(T) == 8 && use_qsweep && &g == &L[0].g) {
         nodal_qsweep64(g, 0, reinterpret_cast<const double*>(s), qw, reinterpret_cast<const double*>(x),
-                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(out), omega_eff, nullptr, s_);
+                       reinterpret_cast<const double*>(b), reinterpret_cast<double*>(out), w, nullptr, s_);
     } else if (sizeof(T) == 4 && use_tma && vsweep32_supported(g)) {
         int rc = vsweep32(g, 0, reinterpret_cast<const float*>(s), reinterpret_cast<const float*>(x),
-                          reinterpret_cast<const float*>(b), reinterpret_cast<float*>(out), (float)omega_eff, derr, s_);
+                          reinterpret_cast<const float*>(b), reinterpret_cast<float*>(out), (float)w, derr, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else if (use_tma && sweep_supported(g, (int)sizeof(T))) {
-        int rc = nodal_sweep<T>(g, 0, s, x, b, out, omega_eff, derr, nullptr, s_);
+        int rc = nodal_sweep<T>(g, 0, s, x, b, out, w, derr, nullptr, s_);
         if (rc && !launch_rc) launch_rc = rc;
     } else {
-        nodal_jacobi<T>(g, s, x, b, out, omega_eff, false, s_);
+        nodal_jacobi<T>(g, s, x, b, out, w, false, s_);
     }
 }
 
@@ -564,7 +595,10 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
         c.b[0] = const_cast<T*>(b);
         c.M = dmat;
         c.singular = bsing ? 1 : 0;
-        c.omega = (T)omega_eff;
+        for (int q = 0; q < kSweepWeights; ++q) {
+            c.wpre[q] = (T)wpre[q];
+            c.wpost[q] = (T)wpost[q];
+        }
         c.nu1 = opt.nu1;
         c.nu2 = opt.nu2;
         int rc = nodal_coarse_vcycle<T>(c, nodal_coarse_cluster_size(), s);
@@ -578,19 +612,21 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     int pre = opt.nu1;
     // cut cells (finest level): the EB nodes are recomputed from the same input after each sweep
     const bool cut = l == 0 && eb.on;
+    int q0 = 0;  // pre-smoothing sweeps done
     if (zero) {
         if (pre > 0) {
-            nodal_jacobi<T>(lv.g, B::s(lv), nullptr, b, x, omega_eff, true, s);
-            if (cut) eb_nodes<T>(lv.g, eb.e, 0, nullptr, b, x, omega_eff, s);
+            nodal_jacobi<T>(lv.g, B::s(lv), nullptr, b, x, wpre[0], true, s);
+            if (cut) eb_nodes<T>(lv.g, eb.e, 0, nullptr, b, x, wpre[0], s);
             ++nk;
-            --pre;
+            q0 = 1;
         } else {
             cudaMemsetAsync(x, 0, sizeof(T) * lv.g.count, s);
         }
     }
-    for (int q = 0; q < pre; ++q) {
-        jacobi<T>(lv.g, B::s(lv), x, b, t, s);
-        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, omega_eff, s);
+    for (int q = q0; q < pre; ++q) {
+        const double w = wpre[q % kSweepWeights];
+        jacobi<T>(lv.g, B::s(lv), x, b, t, w, s);
+        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, w, s);
         ++nk;
         std::swap(x, t);
     }
@@ -604,13 +640,13 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
             if (rc && !launch_rc) launch_rc = rc;
             ++nk;
             vcycle<T>(l + 1, B::b(cv), true);
-            rc = vsweep32_prolong_jacobi(lv.g, cv.g, B::s(lv), x, (const T*)xres[l + 1], b, t, (float)omega_eff, derr,
+            rc = vsweep32_prolong_jacobi(lv.g, cv.g, B::s(lv), x, (const T*)xres[l + 1], b, t, (float)wpost[0], derr,
                                          s);
             if (rc && !launch_rc) launch_rc = rc;
             ++nk;
             std::swap(x, t);
             for (int q = 1; q < opt.nu2; ++q) {
-                jacobi<T>(lv.g, B::s(lv), x, b, t, s);
+                jacobi<T>(lv.g, B::s(lv), x, b, t, wpost[q % kSweepWeights], s);
                 ++nk;
                 std::swap(x, t);
             }
@@ -626,8 +662,9 @@ void NodalSolver::vcycle(int l, const T* b, bool zero)
     nodal_prolong_add<T>(lv.g, cv.g, (const T*)xres[l + 1], x, s);
     ++nk;
     for (int q = 0; q < opt.nu2; ++q) {
-        jacobi<T>(lv.g, B::s(lv), x, b, t, s);
-        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, omega_eff, s);
+        const double w = wpost[q % kSweepWeights];
+        jacobi<T>(lv.g, B::s(lv), x, b, t, w, s);
+        if (cut) eb_nodes<T>(lv.g, eb.e, 0, x, b, t, w, s);
         ++nk;
         std::swap(x, t);
     }
@@ -1015,6 +1052,7 @@ int NodalSolver::set_eb(const gbp_array4* M)
     eb.pool.release();
     eb = EbState{};
     sigma_ready = false;  // the level-0 sigma split depends on the geometry: set sigma again
+    set_omega();          // cut cells take the fixed smoother weight
     if (!M || !M->data) return rebuild_masks();
     if (M->ncomp < 27) {
         set_error("nodal_set_eb: the moments array needs 27 components");
@@ -1245,6 +1283,7 @@ int NodalSolver::set_eb(const gbp_array4* M)
     eb.e.reg = dr;
     eb.has_inactive = inactive;
     eb.on = true;
+    set_omega();
     return rebuild_masks();
 }
 
@@ -1365,7 +1404,7 @@ int NodalSolver::warm_start(double bnorm, double* rn, gbp_stats* stats, bool fro
         for (int q = 0; q < 2; ++q) {
             float* xin = q == 0 ? l0.x32 : l0.t32;
             float* xout = q == 0 ? l0.t32 : l0.x32;
-            jacobi<float>(l0.g, l0.s32, xin, l0.b32, xout, st);
+            jacobi<float>(l0.g, l0.s32, xin, l0.b32, xout, omega_eff, st);
             if (eb.on) eb_nodes<float>(l0.g, eb.e, 0, xin, l0.b32, xout, omega_eff, st);
         }
         if (launch_rc) return launch_rc;
@@ -1586,8 +1625,9 @@ int NodalSolver::time_kernel(int which, int reps, double* ms, double* bytes)
     GBP_CUDA(cudaEventRecord(ev0, st));
     for (int r = 0; r < reps; ++r) {
         switch (which) {
-        case 0: jacobi<double>(g, l0.s64, (r & 1) ? l0.t64 : l0.x64, res, (r & 1) ? l0.x64 : l0.t64, st); break;
-        case 1: jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, st); break;
+        case 0: jacobi<double>(g, l0.s64, (r & 1) ? l0.t64 : l0.x64, res, (r & 1) ? l0.x64 : l0.t64, omega_eff, st); break;
+        case 1: jacobi<float>(g, l0.s32, (r & 1) ? l0.t32 : l0.x32, l0.b32, (r & 1) ? l0.x32 : l0.t32, omega_eff, st);
+                break;
         case 2: resid<double>(g, l0.s64, phi, rhs0, l0.r64, nullptr, st); break;
         case 3: resid<float>(g, l0.s32, l0.x32, l0.b32, l0.r32, nullptr, st); break;
         case 4: stream_triad(l0.x32, l0.s32, l0.b32, l0.r32, g.count, st); break;

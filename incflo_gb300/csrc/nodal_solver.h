@@ -162,7 +162,7 @@ private:
     // Jacobi sweep / residual on one level: the TMA-staged sweep where the level is large enough,
     // the plain kernels on small levels
     template <typename T>
-    void jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, cudaStream_t s_);
+    void jacobi(const NodalGeom& g, const T* s, const T* x, const T* b, T* out, double w, cudaStream_t s_);
     template <typename T>
     void resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, unsigned long long* norm,
                cudaStream_t s_);
@@ -204,7 +204,9 @@ public:
     // the per-level launches and through the cluster kernel; *diff = max |difference| / max |result|
     int check_coarse_cycle(double* diff);
 private:
-    double omega_eff = 0.85;  // the smoother weight in use (see set_omega)
+    double omega_eff = 0.85;  // the fixed smoother weight (see set_omega)
+    // weights of the pre- and post-smoothing sweeps of a V-cycle level (sweep p: [p % kSweepWeights])
+    double wpre[kSweepWeights] = {}, wpost[kSweepWeights] = {};
     void set_omega();
     bool bsing = false;           // the coarsest operator does (no node held at 0 on it)
     bool singular_faces = false;  // singular from the boundary types alone (no overset mask)

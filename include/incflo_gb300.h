@@ -102,7 +102,9 @@ typedef struct {
     int precision;               /* precision = fp64 | mixed  (new key; default fp64) */
     int nu1;                     /* num_pre_smooth  (2) */
     int nu2;                     /* num_post_smooth (2) */
-    double omega;                /* Jacobi weight of the nodal smoother (0.85) */
+    double omega;                /* Jacobi weight of the nodal smoother (0.85, capped for stretched cells);
+                                    0 = per-sweep weights from the Chebyshev roots on [lb/4, lb], lb the
+                                    Gershgorin bound of the Jacobi-scaled operator */
     int ir_inner_cycles;         /* mixed form: at most this many FP32 V-cycles per FP64
                                     refinement step (5); fewer when the observed contraction
                                     says fewer reach the tolerance */
