@@ -55,6 +55,7 @@ struct CellGeom {
     double w[3];   // V / h_d^2: face weight per unit beta
     double vol;
     double h[3];
+    double ih[3];  // 1 / h_d (kernels multiply: an FP64 division is a dozen FP64 instructions)
     // diagonal term alpha a V per cell (the ABecLaplacian's alpha a), or null (the Poisson operator)
     const double* a64;
     const float* a32;

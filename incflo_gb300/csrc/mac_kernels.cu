@@ -18,11 +18,42 @@ namespace gbp {
 __device__ __forceinline__ bool decode_cell(const CellGeom& g, long long t, int& i, int& j, int& k)
 {
     const long long nxy = (long long)g.n[0] * g.n[1];
-    if (t >= nxy * g.n[2]) return false;
+    const long long n = nxy * g.n[2];
+    if (t >= n) return false;
+    if (n <= 0xffffffffll) {
+        // 32-bit unsigned division (a 64-bit one is emulated in far more instructions)
+        const unsigned u = (unsigned)t, nx = (unsigned)g.n[0], nxy32 = (unsigned)nxy;
+        const unsigned kk = u / nxy32, r = u - kk * nxy32, jj = r / nx;
+        k = (int)kk;
+        j = (int)jj;
+        i = (int)(r - jj * nx);
+        return true;
+    }
     k = (int)(t / nxy);
     long long r = t - (long long)k * nxy;
     j = (int)(r / g.n[0]);
     i = (int)(r - (long long)j * g.n[0]);
+    return true;
+}
+
+// face (f0, f1, f2) of linear index t over extents fn (faces of one direction), as decode_cell
+__device__ __forceinline__ bool decode_face(const int fn[3], long long t, int f[3])
+{
+    const long long nxy = (long long)fn[0] * fn[1];
+    const long long n = nxy * fn[2];
+    if (t >= n) return false;
+    if (n <= 0xffffffffll) {
+        const unsigned u = (unsigned)t, nx = (unsigned)fn[0], nxy32 = (unsigned)nxy;
+        const unsigned kk = u / nxy32, r = u - kk * nxy32, jj = r / nx;
+        f[2] = (int)kk;
+        f[1] = (int)jj;
+        f[0] = (int)(r - jj * nx);
+        return true;
+    }
+    f[2] = (int)(t / nxy);
+    const long long rem = t - (long long)f[2] * nxy;
+    f[1] = (int)(rem / fn[0]);
+    f[0] = (int)(rem - (long long)f[1] * fn[0]);
     return true;
 }
 
@@ -78,10 +109,19 @@ __global__ void __launch_bounds__(256) k_mac_rbgs(CellGeom g, const T* __restric
     const int hx = (g.n[0] + 1) / 2;
     const long long rows = (long long)g.n[1] * g.n[2];
     if (t >= rows * hx) return;
-    const long long row = t / hx;
-    const int k = (int)(row / g.n[1]);
-    const int j = (int)(row - (long long)k * g.n[1]);
-    const int i = 2 * (int)(t - row * hx) + ((j + k + color) & 1);
+    int i, j, k;
+    if (rows * hx <= 0xffffffffll) {
+        // 32-bit unsigned division (a 64-bit one is emulated in far more instructions)
+        const unsigned u = (unsigned)t, row = u / (unsigned)hx, kk = row / (unsigned)g.n[1];
+        k = (int)kk;
+        j = (int)(row - kk * (unsigned)g.n[1]);
+        i = 2 * (int)(u - row * (unsigned)hx) + ((j + k + color) & 1);
+    } else {
+        const long long row = t / hx;
+        k = (int)(row / g.n[1]);
+        j = (int)(row - (long long)k * g.n[1]);
+        i = 2 * (int)(t - row * hx) + ((j + k + color) & 1);
+    }
     if (i >= g.n[0]) return;
     const long long p = pidx(g.sy, g.sz, i, j, k);
     T diag, off;
@@ -108,6 +148,35 @@ __global__ void __launch_bounds__(256) k_mac_resid(CellGeom g, const T* __restri
     if (norm) {
         nv = block_max(nv);
         if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
+    }
+}
+
+// The FP64 residual (outer refinement steps, plain-form V-cycles): one face weight multiplication per
+// direction instead of per face, and the max norm as an integer key of |r| scaled by 1 / V once per
+// block (no FP64 division per cell). FP64 instructions bound it.
+template <>
+__global__ void __launch_bounds__(256) k_mac_resid<double>(CellGeom g, const double* __restrict__ bx,
+                                                           const double* __restrict__ by, const double* __restrict__ bz,
+                                                           const double* __restrict__ x, const double* __restrict__ b,
+                                                           double* __restrict__ r, unsigned long long* norm)
+{
+    int i, j, k;
+    unsigned long long key = 0;
+    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+        const long long p = pidx(g.sy, g.sz, i, j, k);
+        const double xc = x[p];
+        const double dx = fma(bx[p], xc - x[p - 1], bx[p + 1] * (xc - x[p + 1]));
+        const double dy = fma(by[p], xc - x[p - g.sy], by[p + g.sy] * (xc - x[p + g.sy]));
+        const double dz = fma(bz[p], xc - x[p - g.sz], bz[p + g.sz] * (xc - x[p + g.sz]));
+        double ax = fma(g.w[0], dx, fma(g.w[1], dy, g.w[2] * dz));
+        if (g.a64) ax = fma(g.a64[p], xc, ax);
+        const double v = b[p] - ax;
+        r[p] = v;
+        key = abs_key(v);
+    }
+    if (norm) {
+        key = block_max_key(key);
+        if (threadIdx.x == 0) atomic_max_nonneg(norm, key_value(key) * (1.0 / g.vol));
     }
 }
 
@@ -265,13 +334,8 @@ __global__ void k_mac_beta(CellGeom g, int d, int source, gbp_array4 src, double
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int fn[3] = {g.n[0], g.n[1], g.n[2]};
     fn[d] += 1;
-    const long long nxy = (long long)fn[0] * fn[1];
-    if (t >= nxy * fn[2]) return;
     int f[3];
-    f[2] = (int)(t / nxy);
-    const long long rem = t - (long long)f[2] * nxy;
-    f[1] = (int)(rem / fn[0]);
-    f[0] = (int)(rem - (long long)f[1] * fn[0]);
+    if (!decode_face(fn, t, f)) return;
     const int fd = f[d];
     const bool per = g.per[d];
     const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
@@ -333,13 +397,8 @@ __global__ void k_mac_beta_coarsen(CellGeom gf, CellGeom gc, int d, const double
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int fn[3] = {gc.n[0], gc.n[1], gc.n[2]};
     fn[d] += 1;
-    const long long nxy = (long long)fn[0] * fn[1];
-    if (t >= nxy * fn[2]) return;
     int f[3];
-    f[2] = (int)(t / nxy);
-    const long long rem = t - (long long)f[2] * nxy;
-    f[1] = (int)(rem / fn[0]);
-    f[0] = (int)(rem - (long long)f[1] * fn[0]);
+    if (!decode_face(fn, t, f)) return;
     const long long base = pidx(gf.sy, gf.sz, 2 * f[0], 2 * f[1], 2 * f[2]);
     const long long s1 = d == 0 ? gf.sy : 1;
     const long long s2 = d == 2 ? gf.sy : gf.sz;
@@ -370,7 +429,7 @@ __global__ void __launch_bounds__(256) k_mac_rhs(CellGeom g, gbp_array4 ux, gbp_
         fz0 *= eb.ap[2][p];
         fz1 *= eb.ap[2][p + g.sz];
     }
-    const double dv = (fx1 - fx0) / g.h[0] + (fy1 - fy0) / g.h[1] + (fz1 - fz0) / g.h[2];
+    const double dv = (fx1 - fx0) * g.ih[0] + (fy1 - fy0) * g.ih[1] + (fz1 - fz0) * g.ih[2];
     b[p] = -g.vol * dv - (eb.ebflux ? eb.ebflux[p] : 0.0);
 }
 
@@ -395,20 +454,15 @@ __global__ void __launch_bounds__(256) k_mac_correct(CellGeom g, int d, gbp_arra
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int fn[3] = {g.n[0], g.n[1], g.n[2]};
     fn[d] += 1;
-    const long long nxy = (long long)fn[0] * fn[1];
-    if (t >= nxy * fn[2]) return;
     int f[3];
-    f[2] = (int)(t / nxy);
-    const long long rem = t - (long long)f[2] * nxy;
-    f[1] = (int)(rem / fn[0]);
-    f[0] = (int)(rem - (long long)f[1] * fn[0]);
+    if (!decode_face(fn, t, f)) return;
     const long long p = pidx(g.sy, g.sz, f[0], f[1], f[2]);
     const long long s = d == 0 ? 1 : (d == 1 ? g.sy : g.sz);
     double be = beta[p];
     if (be == 0.0) return;
     if (ap) be /= ap[p];  // beta here is ap x beta (be != 0 implies ap > 0)
     double* up = a4p(u, f[0], f[1], f[2], 0);
-    *up -= be * (phi[p] - phi[p - s]) / g.h[d];
+    *up -= be * (phi[p] - phi[p - s]) * g.ih[d];
 }
 
 // zero the faces 0..n (direction d) of a caller face array
@@ -444,44 +498,58 @@ __global__ void __launch_bounds__(256) k_mac_norm(CellGeom g, const double* __re
                                                   const double* __restrict__ kap)
 {
     int i, j, k;
+    if (!kap) {
+        // max |v| / V: an integer key of |v| per cell, one multiplication by 1 / V per block
+        unsigned long long key = 0;
+        if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k))
+            key = abs_key(v[pidx(g.sy, g.sz, i, j, k)]);
+        key = block_max_key(key);
+        if (threadIdx.x == 0) atomic_max_nonneg(norm, key_value(key) * (1.0 / g.vol));
+        return;
+    }
     double nv = 0.0;
     if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
         const long long p = pidx(g.sy, g.sz, i, j, k);
-        if (!kap)
-            nv = fabs(v[p]) / g.vol;
-        else if (kap[p] > 0.0)
-            nv = fabs(v[p]) / (kap[p] * g.vol);  // the cut-cell operator divides by the volume fraction
+        if (kap[p] > 0.0) nv = fabs(v[p]) / (kap[p] * g.vol);  // the cut-cell operator divides by the volume fraction
     }
     nv = block_max(nv);
     if (threadIdx.x == 0) atomic_max_nonneg(norm, nv);
 }
 
-// per-block sums of v (kap != null and weighted: of kap * v)
+// per-block sums of v (kap != null and weighted: of kap * v): each thread sums its cells of a grid-stride
+// walk in a fixed order, then a fixed block tree (the grid size is fixed by the host: deterministic)
 __global__ void k_mac_sums(CellGeom g, const double* __restrict__ v, double* __restrict__ part,
                            const double* __restrict__ kap, int weighted)
 {
     __shared__ double red[32];
-    int i, j, k;
     double acc = 0.0;
-    if (decode_cell(g, blockIdx.x * (long long)blockDim.x + threadIdx.x, i, j, k)) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        if (!decode_cell(g, t, i, j, k)) break;
         const long long p = pidx(g.sy, g.sz, i, j, k);
-        acc = (kap && weighted) ? kap[p] * v[p] : v[p];
+        acc += (kap && weighted) ? kap[p] * v[p] : v[p];
     }
     acc = mac_block_sum(acc, red);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// part[nparts] = (sum of the nparts block sums) / nfluid, by one block in a fixed order
+__global__ void k_mac_fold(double* __restrict__ part, int nparts, double nfluid)
+{
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int t = threadIdx.x; t < nparts; t += blockDim.x) acc += part[t];
+    acc = mac_block_sum(acc, red);
+    if (threadIdx.x == 0) part[nparts] = acc / nfluid;
 }
 
 // mode 0: b_c -= kappa_c sum(b) / sum(kappa), so that sum(b) = 0 (the range of the operator);
 // mode 1: x -= its volume-weighted mean, with periodic aliases, and 0 in covered cells. Without cut
 // cells kappa = 1 and nfluid = the cell count.
 __global__ void k_mac_remove_mean(CellGeom g, double* __restrict__ v, const double* __restrict__ part, int nparts,
-                                  int mode, const double* __restrict__ kap, double nfluid)
+                                  int mode, const double* __restrict__ kap)
 {
-    __shared__ double red[32];
-    double acc = 0.0;
-    for (int t = threadIdx.x; t < nparts; t += blockDim.x) acc += part[t];
-    acc = mac_block_sum(acc, red);
-    const double c = acc / nfluid;
+    const double c = part[nparts];  // the mean (k_mac_fold)
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;; t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         if (!decode_cell(g, t, i, j, k)) break;
@@ -985,14 +1053,23 @@ void mac_norm(const CellGeom& g, const double* v, unsigned long long* norm, cuda
 {
     k_mac_norm<<<nblk(ncell(g), 256), 256, 0, st>>>(g, v, norm, kap);
 }
-int mac_partials_needed(const CellGeom& g) { return (int)nblk(ncell(g), 256); }
+// the sums' grid: at most 1184 blocks (8 per SM of a 148-SM part and more than enough on 152), each
+// thread walking its cells; partials holds one sum per block and the folded mean after them
+static unsigned mac_sum_blocks(const CellGeom& g)
+{
+    const unsigned nb = nblk(ncell(g), 256);
+    return nb < 1184 ? nb : 1184;
+}
+int mac_partials_needed(const CellGeom& g) { return (int)mac_sum_blocks(g) + 1; }
 void mac_remove_mean(const CellGeom& g, double* v, double* partials, int mode, cudaStream_t st, const double* kap,
                      double nfluid)
 {
-    const unsigned nb = nblk(ncell(g), 256);
+    const unsigned nb = mac_sum_blocks(g);
     if (!kap) nfluid = (double)g.n[0] * g.n[1] * g.n[2];
     k_mac_sums<<<nb, 256, 0, st>>>(g, v, partials, kap, mode);
-    k_mac_remove_mean<<<nb < 1024 ? nb : 1024, 256, 0, st>>>(g, v, partials, (int)nb, mode, kap, nfluid);
+    k_mac_fold<<<1, 1024, 0, st>>>(partials, (int)nb, nfluid);
+    const unsigned na = nblk(ncell(g), 256);
+    k_mac_remove_mean<<<na < 2368 ? na : 2368, 256, 0, st>>>(g, v, partials, (int)nb, mode, kap);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -22,6 +22,7 @@ static CellGeom make_cgeom(const int n[3], const double h[3], const int per[3], 
         g.dlo[d] = per[d] ? 0 : dlo[d];
         g.dhi[d] = per[d] ? 0 : dhi[d];
         g.h[d] = h[d];
+        g.ih[d] = 1.0 / h[d];
     }
     const long long P0 = padded_row(n[0]);
     g.sy = P0;
