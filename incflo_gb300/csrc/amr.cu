@@ -43,9 +43,11 @@ __global__ void k_amr_cmask_fine(NodalGeom gf, const BoxEntry* __restrict__ bx, 
     const int ex = b.hi[0] - b.lo[0] + 1, ey = b.hi[1] - b.lo[1] + 1, ez = b.hi[2] - b.lo[2] + 1;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = b.lo[0] + (int)(t % ex) - off0;
-        const int j = b.lo[1] + (int)((t / ex) % ey) - off1;
-        const int k = b.lo[2] + (int)(t / ((long long)ex * ey)) - off2;
+        int i, j, k;
+        split3(t, ex, ey, (long long)ex * ey * ez, i, j, k);
+        i += b.lo[0] - off0;
+        j += b.lo[1] - off1;
+        k += b.lo[2] - off2;
         store_sigma_cell(m, gf, i, j, k, (unsigned char)1);
     }
 }
@@ -242,8 +244,11 @@ __global__ void k_amr_gather(const BoxEntry* __restrict__ bx, int off0, int off1
     const long long ncell = (long long)nb0 * nb1 * nb2;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
          t += (long long)gridDim.x * blockDim.x) {
-        const int gi = b.lo[0] + (int)(t % ex), gj = b.lo[1] + (int)((t / ex) % ey),
-                  gk = b.lo[2] + (int)(t / ((long long)ex * ey));
+        int gi, gj, gk;
+        split3(t, ex, ey, (long long)ex * ey * ez, gi, gj, gk);
+        gi += b.lo[0];
+        gj += b.lo[1];
+        gk += b.lo[2];
         const long long q = (gi - off0) + (long long)nb0 * ((gj - off1) + (long long)nb1 * (gk - off2));
         for (int c = 0; c < ncomp; ++c) dst[q + c * ncell] = *at4(b.a, gi, gj, gk, c);
     }
@@ -258,8 +263,11 @@ __global__ void k_amr_scatter(const BoxEntry* __restrict__ bx, int off0, int off
     const long long ncell = (long long)nb0 * nb1 * nb2;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
          t += (long long)gridDim.x * blockDim.x) {
-        const int gi = b.lo[0] + (int)(t % ex), gj = b.lo[1] + (int)((t / ex) % ey),
-                  gk = b.lo[2] + (int)(t / ((long long)ex * ey));
+        int gi, gj, gk;
+        split3(t, ex, ey, (long long)ex * ey * ez, gi, gj, gk);
+        gi += b.lo[0];
+        gj += b.lo[1];
+        gk += b.lo[2];
         const long long q = (gi - off0) + (long long)nb0 * ((gj - off1) + (long long)nb1 * (gk - off2));
         for (int c = 0; c < ncomp; ++c) *at4(b.a, gi, gj, gk, c) = src[q + c * ncell];
     }
@@ -274,8 +282,11 @@ __global__ void k_amr_scatter_nodes(const BoxEntry* __restrict__ bx, int off0, i
     const int ex = b.hi[0] - b.lo[0] + 2, ey = b.hi[1] - b.lo[1] + 2, ez = b.hi[2] - b.lo[2] + 2;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)ex * ey * ez;
          t += (long long)gridDim.x * blockDim.x) {
-        const int gi = b.lo[0] + (int)(t % ex), gj = b.lo[1] + (int)((t / ex) % ey),
-                  gk = b.lo[2] + (int)(t / ((long long)ex * ey));
+        int gi, gj, gk;
+        split3(t, ex, ey, (long long)ex * ey * ez, gi, gj, gk);
+        gi += b.lo[0];
+        gj += b.lo[1];
+        gk += b.lo[2];
         const long long q = (gi - off0) + (long long)(nb0 + 1) * ((gj - off1) + (long long)(nb1 + 1) * (gk - off2));
         double* p = at4(b.a, gi, gj, gk, 0);
         *p = accumulate ? *p + src[q] : src[q];

@@ -36,7 +36,8 @@ __global__ void k_cc_prep(CcGeom g, CcArgs a)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)g.n[0] * g.n[1] * g.n[2]) return;
-    const int i = (int)(t % g.n[0]), j = (int)((t / g.n[0]) % g.n[1]), k = (int)(t / ((long long)g.n[0] * g.n[1]));
+    int i, j, k;
+    split3(t, g.n[0], g.n[1], (long long)g.n[0] * g.n[1] * g.n[2], i, j, k);
     const double rho = a.rho.data ? A(a.rho, i, j, k, 0) : a.rho0;
     for (int d = 0; d < 3; ++d) {
         double u = A(a.vel, i, j, k, d);
@@ -77,9 +78,7 @@ __global__ void k_mol_faces(CcGeom g, CcArgs a, int d, gbp_array4 uf, double* __
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)fn[0] * fn[1] * fn[2]) return;
     int f[3];
-    f[0] = (int)(t % fn[0]);
-    f[1] = (int)((t / fn[0]) % fn[1]);
-    f[2] = (int)(t / ((long long)fn[0] * fn[1]));
+    split3(t, fn[0], fn[1], (long long)fn[0] * fn[1] * fn[2], f[0], f[1], f[2]);
     const int n = g.n[d], fi = f[d];
     double val;
     if (!g.per[d] && (fi == 0 || fi == n)) {
@@ -113,7 +112,8 @@ __global__ void k_cc_final(CcGeom g, CcArgs a, gbp_array4 ux, gbp_array4 uy, gbp
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)g.n[0] * g.n[1] * g.n[2]) return;
-    const int i = (int)(t % g.n[0]), j = (int)((t / g.n[0]) % g.n[1]), k = (int)(t / ((long long)g.n[0] * g.n[1]));
+    int i, j, k;
+    split3(t, g.n[0], g.n[1], (long long)g.n[0] * g.n[1] * g.n[2], i, j, k);
     const long long nx1 = g.n[0] + 1, ny1 = g.n[1] + 1;
     // unprojected copies are dense face arrays in x-fastest order
     const long long fx = i + nx1 * (j + (long long)g.n[1] * k);

@@ -196,6 +196,25 @@ __device__ __forceinline__ bool node_is_dirichlet(const NodalGeom& g, int i, int
            (g.mask && !g.mask[pidx(g.sy, g.sz, i, j, k)]);
 }
 
+// (i, j, k) of the linear index t < total = n0 n1 n2 (x fastest): 32-bit unsigned divisions when the range
+// allows (a 64-bit integer division is emulated in far more instructions)
+__device__ __forceinline__ void split3(long long t, int n0, int n1, long long total, int& i, int& j, int& k)
+{
+    if (total <= 0xffffffffll) {
+        const unsigned u = (unsigned)t, a = (unsigned)n0, ab = (unsigned)n0 * (unsigned)n1;
+        const unsigned kk = u / ab, r = u - kk * ab, jj = r / a;
+        k = (int)kk;
+        j = (int)jj;
+        i = (int)(r - jj * a);
+    } else {
+        const long long ab = (long long)n0 * n1;
+        k = (int)(t / ab);
+        const long long r = t - (long long)k * ab;
+        j = (int)(r / n0);
+        i = (int)(r - (long long)j * n0);
+    }
+}
+
 // Control volume of a node: h per direction, h/2 on a non-periodic boundary.
 __device__ __forceinline__ double node_volume(const NodalGeom& g, int i, int j, int k)
 {

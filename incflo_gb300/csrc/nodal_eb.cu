@@ -163,7 +163,8 @@ __global__ void k_eb_pack(gbp_array4 in, int c, int n0, int n1, int n2, double* 
 {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)n0 * n1 * n2) return;
-    const int i = (int)(t % n0), j = (int)((t / n0) % n1), k = (int)(t / ((long long)n0 * n1));
+    int i, j, k;
+    split3(t, n0, n1, (long long)n0 * n1 * n2, i, j, k);
     out[t] = *at4(in, i, j, k, c);
 }
 

@@ -892,10 +892,8 @@ __global__ void k_sigma_coarsen(NodalGeom gf, NodalGeom gc, const double* __rest
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long nxy = (long long)gc.n[0] * gc.n[1];
     if (t >= nxy * gc.n[2]) return;
-    const int k = (int)(t / nxy);
-    const long long rem = t - (long long)k * nxy;
-    const int j = (int)(rem / gc.n[0]);
-    const int i = (int)(rem - (long long)j * gc.n[0]);
+    int i, j, k;
+    split3(t, gc.n[0], gc.n[1], nxy * gc.n[2], i, j, k);
     const long long f = pidx(gf.sy, gf.sz, 2 * i, 2 * j, 2 * k);
     double acc = 0.0;
 #pragma unroll
@@ -1209,10 +1207,8 @@ __global__ void k_nodal_store_div(NodalGeom g, gbp_array4 out, const double* __r
     const int n0 = g.n[0] + 1, n1 = g.n[1] + 1, n2 = g.n[2] + 1;
     const long long nxy = (long long)n0 * n1;
     if (t >= nxy * n2) return;
-    const int k = (int)(t / nxy);
-    const long long rem = t - (long long)k * nxy;
-    const int j = (int)(rem / n0);
-    const int i = (int)(rem - (long long)j * n0);
+    int i, j, k;
+    split3(t, n0, n1, nxy * n2, i, j, k);
     const int iu = (g.per[0] && i == g.n[0]) ? 0 : i;
     const int ju = (g.per[1] && j == g.n[1]) ? 0 : j;
     const int ku = (g.per[2] && k == g.n[2]) ? 0 : k;
