@@ -828,8 +828,8 @@ int gbp_plan_check_level_kernels(gbp_plan* p, double diff[4])
 
 int gbp_plan_check_coarse_cycle(gbp_plan* p, double* diff)
 {
-    if (!p || !diff) {
-        set_error("gbp_plan_check_coarse_cycle: needs a plan and an output");
+    if (!p || !diff || (!p->nodal && !p->mac)) {
+        set_error("gbp_plan_check_coarse_cycle: needs a nodal or MAC plan and an output");
         return GBP_BAD_ARG;
     }
     return p->nodal ? p->nodal->check_coarse_cycle(diff) : p->mac->check_coarse_cycle(diff);
