@@ -450,6 +450,13 @@ void MacSolver::add_vcycle_correction(const double* r, double* e, double sc)
     }
 }
 
+void MacSolver::vcycles32(const float* b32)
+{
+    cap_or_st = st;
+    vcycle<float>(0, b32, true);
+    for (int c = 1; c < opt.ir_inner_cycles; ++c) vcycle<float>(0, b32, false);
+}
+
 void MacSolver::eb_refresh_beta()
 {
     if (!eb.on) return;

@@ -64,6 +64,10 @@ public:
     const CellGeom& finest() const { return L[0].g; }
     const gbp_options& options() const { return opt; }
     void add_vcycle_correction(const double* r, double* e, double scale32_);
+    // its FP32 V-cycles on an FP32 right-hand side already scaled (mixed form); the correction stays in
+    // correction32() until the next V-cycle of this solver
+    void vcycles32(const float* b32);
+    const float* correction32() const { return L[0].x32; }
     size_t device_bytes() const { return pool.bytes; }
 
 private:

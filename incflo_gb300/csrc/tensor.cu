@@ -35,12 +35,16 @@ __device__ __forceinline__ bool cell3(const CellGeom& g, int& i, int& j, int& k)
     return i < g.n[0] && j < g.n[1] && k < g.n[2];
 }
 
-struct U3 {
-    double* c[3];
+template <typename T>
+struct V3 {
+    T* c[3];
 };
-struct CU3 {
-    const double* c[3];
+template <typename T>
+struct CV3 {
+    const T* c[3];
 };
+using U3 = V3<double>;
+using CU3 = CV3<double>;
 
 // raw face eta of direction d (no boundary factors): source 0 = face arrays, 1 = constant, 3 = the face
 // average of a cell field with the adjacent cell on non-periodic domain sides
@@ -138,8 +142,10 @@ __device__ __forceinline__ int edge_weights(int q, int n, int per, int idx[2], d
 // Ghost cells of direction d on both sides, all three components. Tangential ranges: directions before
 // d over their ghosts too (-1 .. n), directions after d over the interior (they are filled later).
 // bc[2][3]: the types of the low / high side per component. Dirichlet values come from vel's ghost cells.
-__global__ void k_tensor_ghost(CellGeom g, int d, int bl0, int bl1, int bl2, int bh0, int bh1, int bh2, U3 u,
-                               gbp_array4 vel)
+// homog: the boundary values are zero (the correction equation of the FP32 inner steps)
+template <typename T>
+__global__ void k_tensor_ghost(CellGeom g, int d, int bl0, int bl1, int bl2, int bh0, int bh1, int bh2, V3<T> u,
+                               gbp_array4 vel, int homog)
 {
     const int e = d == 0 ? 1 : 0, f = d == 2 ? 1 : 2;
     const int ext_e = e < d ? 1 : 0, ext_f = f < d ? 1 : 0;
@@ -167,11 +173,13 @@ __global__ void k_tensor_ghost(CellGeom g, int d, int bl0, int bl1, int bl2, int
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int bc = bcs[side][c];
-        double v;
+        T v;
         if (bc == GBP_BC_PERIODIC) {
             v = u.c[c][pw];
         } else if (bc == GBP_BC_NEUMANN) {
             v = u.c[c][pi];
+        } else if (homog) {
+            v = -u.c[c][pi];
         } else {
             double ub = 0.0;
             for (int a = 0; a < ne; ++a)
@@ -182,7 +190,7 @@ __global__ void k_tensor_ghost(CellGeom g, int d, int bl0, int bl1, int bl2, int
                     q[f] = iff[b];
                     ub += we[a] * wf[b] * at(vel, q[0], q[1], q[2], c);
                 }
-            v = 2.0 * ub - u.c[c][pi];
+            v = (T)(2.0 * ub - u.c[c][pi]);
         }
         u.c[c][pg] = v;
     }
@@ -190,29 +198,31 @@ __global__ void k_tensor_ghost(CellGeom g, int d, int bl0, int bl1, int bl2, int
 
 // Host-computed scale factors (FP64 division and most FP64 arithmetic are kept out of the kernels: GB300
 // issues FP64 at 1/64 of the FP32 rate, and these kernels are bound by it)
-struct FaceK {
-    double ih[3];   // 1 / h_d
-    double q[3];    // 1 / (4 h_e): tangential derivative from the four-cell difference sum
-    double n43[3];  // (4/3) / h_d
-    double t23[3];  // (2/3) / (4 h_e)
+template <typename T>
+struct FaceKT {
+    T ih[3];   // 1 / h_d
+    T q[3];    // 1 / (4 h_e): tangential derivative from the four-cell difference sum
+    T n43[3];  // (4/3) / h_d
+    T t23[3];  // (2/3) / (4 h_e)
 };
+using FaceK = FaceKT<double>;
 
 // tau_{c,d} / h_d (c = 0..2) on the face between cells L and R of direction d
-template <int d>
-__device__ __forceinline__ void face_tau(const CU3& u, long long L, long long R, const long long s[3], const FaceK& K,
-                                         double eta, double tau[3])
+template <int d, typename T>
+__device__ __forceinline__ void face_tau(const CV3<T>& u, long long L, long long R, const long long s[3],
+                                         const FaceKT<T>& K, T eta, T tau[3])
 {
     constexpr int e1 = d == 0 ? 1 : 0, e2 = d == 2 ? 1 : 2;
-    const double* u0 = u.c[d];
-    const double* u1 = u.c[e1];
-    const double* u2 = u.c[e2];
+    const T* u0 = u.c[d];
+    const T* u1 = u.c[e1];
+    const T* u2 = u.c[e2];
     // four-cell difference sums (tangential derivatives times 4 h_e)
-    const double Tdd1 = (u0[R + s[e1]] - u0[R - s[e1]]) + (u0[L + s[e1]] - u0[L - s[e1]]);
-    const double Tdd2 = (u0[R + s[e2]] - u0[R - s[e2]]) + (u0[L + s[e2]] - u0[L - s[e2]]);
-    const double T11 = (u1[R + s[e1]] - u1[R - s[e1]]) + (u1[L + s[e1]] - u1[L - s[e1]]);
-    const double T22 = (u2[R + s[e2]] - u2[R - s[e2]]) + (u2[L + s[e2]] - u2[L - s[e2]]);
-    const double a = eta * K.ih[d];
-    double t = K.n43[d] * (u0[R] - u0[L]);
+    const T Tdd1 = (u0[R + s[e1]] - u0[R - s[e1]]) + (u0[L + s[e1]] - u0[L - s[e1]]);
+    const T Tdd2 = (u0[R + s[e2]] - u0[R - s[e2]]) + (u0[L + s[e2]] - u0[L - s[e2]]);
+    const T T11 = (u1[R + s[e1]] - u1[R - s[e1]]) + (u1[L + s[e1]] - u1[L - s[e1]]);
+    const T T22 = (u2[R + s[e2]] - u2[R - s[e2]]) + (u2[L + s[e2]] - u2[L - s[e2]]);
+    const T a = eta * K.ih[d];
+    T t = K.n43[d] * (u0[R] - u0[L]);
     t = fma(-K.t23[e1], T11, t);
     t = fma(-K.t23[e2], T22, t);
     tau[d] = a * t;
@@ -222,8 +232,9 @@ __device__ __forceinline__ void face_tau(const CU3& u, long long L, long long R,
 
 // tau_{c,d} / h_d of every face of direction d (faces 0 .. n_d), once per face: fl[c] at the face's
 // padded index
-template <int d>
-__global__ void __launch_bounds__(256) k_tensor_flux(CellGeom g, CU3 u, const double* __restrict__ eta, U3 fl, FaceK K)
+template <int d, typename T>
+__global__ void __launch_bounds__(256) k_tensor_flux(CellGeom g, CV3<T> u, const T* __restrict__ eta, V3<T> fl,
+                                                     FaceKT<T> K)
 {
     int f[3] = {(int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(blockIdx.y * blockDim.y + threadIdx.y),
                 (int)(blockIdx.z * blockDim.z + threadIdx.z)};
@@ -231,21 +242,23 @@ __global__ void __launch_bounds__(256) k_tensor_flux(CellGeom g, CU3 u, const do
         if (f[e] >= g.n[e] + (e == d ? 1 : 0)) return;
     const long long s[3] = {1, g.sy, g.sz};
     const long long R = pidx(g.sy, g.sz, f[0], f[1], f[2]);
-    double tau[3];
-    face_tau<d>(u, R - s[d], R, s, K, eta[R], tau);
+    T tau[3];
+    face_tau<d, T>(u, R - s[d], R, s, K, eta[R], tau);
 #pragma unroll
     for (int c = 0; c < 3; ++c) fl.c[c][R] = tau[c];
 }
 
-struct Fl9 {
-    const double* f[3][3];  // [direction][component]
+template <typename T>
+struct Fl9T {
+    const T* f[3][3];  // [direction][component]
 };
+using Fl9 = Fl9T<double>;
 
-// MODE 0: r = b - (alpha a V u - beta V div tau) per component, max |r| / V into *norm (bvol = beta V).
-// MODE 1: out(i, j, k, c) = div tau.
-template <int MODE>
-__global__ void __launch_bounds__(256) k_tensor_div(CellGeom g, Fl9 fl, CU3 u, const double* __restrict__ a64,
-                                                    double bvol, double ivol, CU3 b, U3 r, unsigned long long* norm,
+// MODE 0: r = b - (alpha a V u - beta V div tau) per component, max |r| / V into *norm when given (bvol =
+// beta V). MODE 1: out(i, j, k, c) = div tau (FP64).
+template <int MODE, typename T>
+__global__ void __launch_bounds__(256) k_tensor_div(CellGeom g, Fl9T<T> fl, CV3<T> u, const T* __restrict__ a, T bvol,
+                                                    double ivol, CV3<T> b, V3<T> r, unsigned long long* norm,
                                                     gbp_array4 out)
 {
     int i, j, k;
@@ -253,29 +266,50 @@ __global__ void __launch_bounds__(256) k_tensor_div(CellGeom g, Fl9 fl, CU3 u, c
     if (cell3(g, i, j, k)) {
         const long long p = pidx(g.sy, g.sz, i, j, k);
         const long long s[3] = {1, g.sy, g.sz};
-        double div[3];
+        T div[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             div[c] = ((fl.f[0][c][p + s[0]] - fl.f[0][c][p]) + (fl.f[1][c][p + s[1]] - fl.f[1][c][p])) +
                      (fl.f[2][c][p + s[2]] - fl.f[2][c][p]);
-        if (MODE == 0) {
+        if constexpr (MODE == 0) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const double ax = a64 ? fma(a64[p], u.c[c][p], -bvol * div[c]) : -bvol * div[c];
-                const double v = b.c[c][p] - ax;
+                const T ax = a ? fma(a[p], u.c[c][p], -bvol * div[c]) : -bvol * div[c];
+                const T v = b.c[c][p] - ax;
                 r.c[c][p] = v;
-                const unsigned long long kv = abs_key(v);
+                const unsigned long long kv = abs_key((double)v);
                 key = kv > key ? kv : key;
             }
         } else {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) *atp(out, i, j, k, c) = div[c];
+            for (int c = 0; c < 3; ++c) *atp(out, i, j, k, c) = (double)div[c];
         }
     }
-    if (MODE == 0) {
+    if (MODE == 0 && norm) {
         key = block_max_key(key);
         if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) atomic_max_nonneg(norm, key_value(key) * ivol);
     }
+}
+
+// out = scale * v over whole padded arrays (FP64 -> FP32)
+__global__ void k_tensor_to32(long long count, const double* __restrict__ v, double scale, float* __restrict__ out)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < count) out[t] = (float)(scale * v[t]);
+}
+
+// acc += e over whole padded arrays
+__global__ void k_tensor_acc32(long long count, const float* __restrict__ e, float* __restrict__ acc)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < count) acc[t] += e[t];
+}
+
+// u += e / scale over whole padded arrays (FP32 correction into FP64)
+__global__ void k_tensor_add(long long count, const float* __restrict__ e, double inv_scale, double* __restrict__ u)
+{
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < count) u[t] += (double)e[t] * inv_scale;
 }
 
 const dim3 kBlk(32, 4, 2);
@@ -293,12 +327,54 @@ inline double bits_to_double(unsigned long long b)
 
 }  // namespace
 
-static Fl9 make_fl9(double* const fl[3][3])
+template <typename T>
+static Fl9T<T> make_fl9(T* const fl[3][3])
 {
-    Fl9 t{};
+    Fl9T<T> t{};
     for (int d = 0; d < 3; ++d)
         for (int c = 0; c < 3; ++c) t.f[d][c] = fl[d][c];
     return t;
+}
+
+// tau on every face of the three directions, once per face, in precision T
+template <typename T>
+static void tensor_fluxes(const CellGeom& g, T* const uu[3], T* const et[3], T* const f[3][3], cudaStream_t st)
+{
+    const CV3<T> uc{{uu[0], uu[1], uu[2]}};
+    FaceKT<T> K;
+    for (int d = 0; d < 3; ++d) {
+        K.ih[d] = (T)(1.0 / g.h[d]);
+        K.q[d] = (T)(0.25 / g.h[d]);
+        K.n43[d] = (T)((4.0 / 3.0) / g.h[d]);
+        K.t23[d] = (T)((2.0 / 3.0) * 0.25 / g.h[d]);
+    }
+    for (int d = 0; d < 3; ++d) {
+        int fn[3] = {g.n[0], g.n[1], g.n[2]};
+        fn[d] += 1;
+        dim3 grid((unsigned)((fn[0] + 31) / 32), (unsigned)((fn[1] + 3) / 4), (unsigned)((fn[2] + 1) / 2));
+        const V3<T> out{{f[d][0], f[d][1], f[d][2]}};
+        if (d == 0)
+            k_tensor_flux<0, T><<<grid, kBlk, 0, st>>>(g, uc, et[0], out, K);
+        else if (d == 1)
+            k_tensor_flux<1, T><<<grid, kBlk, 0, st>>>(g, uc, et[1], out, K);
+        else
+            k_tensor_flux<2, T><<<grid, kBlk, 0, st>>>(g, uc, et[2], out, K);
+    }
+}
+
+// ghost cells of all three components, direction by direction (homog: zero boundary values)
+template <typename T>
+static void tensor_ghosts(const CellGeom& g, const int bclo[9], const int bchi[9], T* const uu[3],
+                          const gbp_array4& vel, int homog, cudaStream_t st)
+{
+    for (int d = 0; d < 3; ++d) {
+        const int e = d == 0 ? 1 : 0, f = d == 2 ? 1 : 2;
+        const int ne = g.n[e] + (e < d ? 2 : 0), nf = g.n[f] + (f < d ? 2 : 0);
+        dim3 grid((unsigned)((ne + 31) / 32), (unsigned)((nf + 7) / 8), 2);
+        k_tensor_ghost<T><<<grid, dim3(32, 8, 1), 0, st>>>(g, d, bclo[d], bclo[3 + d], bclo[6 + d], bchi[d],
+                                                           bchi[3 + d], bchi[6 + d], V3<T>{{uu[0], uu[1], uu[2]}},
+                                                           vel, homog);
+    }
 }
 
 TensorSolver::~TensorSolver()
@@ -348,7 +424,7 @@ int TensorSolver::init(const gbp_geometry& g, const int bc_lo[9], const int bc_h
     }
     const CellGeom& cg = comp[0].finest();
     const size_t cnt = (size_t)cg.count;
-    int rc = pool.reserve(21 * (cnt * sizeof(double) + 256) + 4096);
+    int rc = pool.reserve(21 * (cnt * sizeof(double) + 256) + 21 * (cnt * sizeof(float) + 256) + 4096);
     if (rc) return rc;
     for (int c = 0; c < 3; ++c) {
         u[c] = pool.take<double>(cnt);
@@ -361,6 +437,19 @@ int TensorSolver::init(const gbp_geometry& g, const int bc_lo[9], const int bc_h
         for (int c = 0; c < 3; ++c) {
             fl[d][c] = pool.take<double>(cnt);
             GBP_CUDA(cudaMemsetAsync(fl[d][c], 0, sizeof(double) * cnt, st));
+        }
+    // FP32 inner steps: correction, right-hand side, residual, face eta, fluxes
+    for (int c = 0; c < 3; ++c) {
+        e32[c] = pool.take<float>(cnt);
+        b32[c] = pool.take<float>(cnt);
+        r32[c] = pool.take<float>(cnt);
+        eta32[c] = pool.take<float>(cnt);
+        for (float* q : {e32[c], b32[c], r32[c], eta32[c]}) GBP_CUDA(cudaMemsetAsync(q, 0, sizeof(float) * cnt, st));
+    }
+    for (int d = 0; d < 3; ++d)
+        for (int c = 0; c < 3; ++c) {
+            fl32[d][c] = pool.take<float>(cnt);
+            GBP_CUDA(cudaMemsetAsync(fl32[d][c], 0, sizeof(float) * cnt, st));
         }
     dnorm = pool.take<unsigned long long>(4);
     GBP_CUDA(cudaMallocHost(&hnorm, 4 * sizeof(unsigned long long)));
@@ -415,6 +504,7 @@ int TensorSolver::set_coeffs(double a_alpha, const gbp_array4* a, double a0, dou
             source = 0;
         }
         k_tensor_eta<<<grid, kBlk, 0, st>>>(g, d, source, src, eta0, eta[d]);
+        k_tensor_to32<<<(unsigned)((g.count + 255) / 256), 256, 0, st>>>(g.count, eta[d], 1.0, eta32[d]);
     }
     GBP_CUDA(cudaGetLastError());
     alpha = a_alpha;
@@ -441,42 +531,9 @@ void TensorSolver::load(const gbp_array4& vel)
     k_tensor_load<<<cells_grid(g), kBlk, 0, st>>>(g, vel, U3{{u[0], u[1], u[2]}});
 }
 
-void TensorSolver::fluxes()
-{
-    const CellGeom& g = comp[0].finest();
-    const CU3 uc{{u[0], u[1], u[2]}};
-    FaceK K;
-    for (int d = 0; d < 3; ++d) {
-        K.ih[d] = 1.0 / g.h[d];
-        K.q[d] = 0.25 / g.h[d];
-        K.n43[d] = (4.0 / 3.0) / g.h[d];
-        K.t23[d] = (2.0 / 3.0) * 0.25 / g.h[d];
-    }
-    for (int d = 0; d < 3; ++d) {
-        int fn[3] = {g.n[0], g.n[1], g.n[2]};
-        fn[d] += 1;
-        dim3 grid((unsigned)((fn[0] + 31) / 32), (unsigned)((fn[1] + 3) / 4), (unsigned)((fn[2] + 1) / 2));
-        const U3 out{{fl[d][0], fl[d][1], fl[d][2]}};
-        if (d == 0)
-            k_tensor_flux<0><<<grid, kBlk, 0, st>>>(g, uc, eta[0], out, K);
-        else if (d == 1)
-            k_tensor_flux<1><<<grid, kBlk, 0, st>>>(g, uc, eta[1], out, K);
-        else
-            k_tensor_flux<2><<<grid, kBlk, 0, st>>>(g, uc, eta[2], out, K);
-    }
-}
+void TensorSolver::fluxes() { tensor_fluxes<double>(comp[0].finest(), u, eta, fl, st); }
 
-void TensorSolver::fill_ghosts(const gbp_array4& vel)
-{
-    const CellGeom& g = comp[0].finest();
-    for (int d = 0; d < 3; ++d) {
-        const int e = d == 0 ? 1 : 0, f = d == 2 ? 1 : 2;
-        const int ne = g.n[e] + (e < d ? 2 : 0), nf = g.n[f] + (f < d ? 2 : 0);
-        dim3 grid((unsigned)((ne + 31) / 32), (unsigned)((nf + 7) / 8), 2);
-        k_tensor_ghost<<<grid, dim3(32, 8, 1), 0, st>>>(g, d, bclo[d], bclo[3 + d], bclo[6 + d], bchi[d], bchi[3 + d],
-                                                        bchi[6 + d], U3{{u[0], u[1], u[2]}}, vel);
-    }
-}
+void TensorSolver::fill_ghosts(const gbp_array4& vel) { tensor_ghosts<double>(comp[0].finest(), bclo, bchi, u, vel, 0, st); }
 
 int TensorSolver::solve(const gbp_array4& rhs_in, gbp_array4& vel, gbp_stats* stats)
 {
@@ -502,8 +559,8 @@ int TensorSolver::solve(const gbp_array4& rhs_in, gbp_array4& vel, gbp_stats* st
     load(vel);
     fill_ghosts(vel);
     fluxes();
-    k_tensor_div<0><<<cells_grid(g), kBlk, 0, st>>>(g, f9, uc, g.a64, beta * g.vol, 1.0 / g.vol, bc, rr, dnorm + 1,
-                                                    gbp_array4{});
+    k_tensor_div<0, double><<<cells_grid(g), kBlk, 0, st>>>(g, f9, uc, g.a64, beta * g.vol, 1.0 / g.vol, bc, rr,
+                                                            dnorm + 1, gbp_array4{});
     GBP_CUDA(cudaGetLastError());
     GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     GBP_CUDA(cudaStreamSynchronize(st));
@@ -522,19 +579,49 @@ int TensorSolver::solve(const gbp_array4& rhs_in, gbp_array4& vel, gbp_stats* st
         frexp(bnorm * g.vol, &ex);
         scale32 = ldexp(1.0, -ex);
     }
-    int it = 0, status = GBP_OK;
+    int it = 0, status = GBP_OK, steps = 0;
+    // mixed form: kInner block steps on the FP32 correction equation per FP64 residual (the residual of
+    // the full operator in FP32 between them), as the single-level projections refine
+    const bool inner32 = opt.precision == GBP_PREC_MIXED;
+    const long long cnt = g.count;
+    const unsigned nb = (unsigned)((cnt + 255) / 256);
+    const Fl9T<float> f9s = make_fl9(fl32);
+    const CV3<float> ce{{e32[0], e32[1], e32[2]}}, cb32{{b32[0], b32[1], b32[2]}};
+    const V3<float> rr32{{r32[0], r32[1], r32[2]}};
     while (rn > target) {
         if (it >= opt.maxiter) {
             status = GBP_NOT_CONVERGED;
             set_error("tensor solve: maxiter reached before the tolerance");
             break;
         }
-        for (int c = 0; c < 3; ++c) comp[c].add_vcycle_correction(r[c], u[c], scale32);
+        if (inner32) {
+            for (int c = 0; c < 3; ++c) {
+                k_tensor_to32<<<nb, 256, 0, st>>>(cnt, r[c], scale32, b32[c]);
+                GBP_CUDA(cudaMemsetAsync(e32[c], 0, sizeof(float) * cnt, st));
+            }
+            for (int q = 0; q < kInner; ++q) {
+                for (int c = 0; c < 3; ++c) {
+                    comp[c].vcycles32(q == 0 ? b32[c] : r32[c]);
+                    k_tensor_acc32<<<nb, 256, 0, st>>>(cnt, comp[c].correction32(), e32[c]);
+                }
+                if (q + 1 < kInner) {
+                    tensor_ghosts<float>(g, bclo, bchi, e32, vel, 1, st);
+                    tensor_fluxes<float>(g, e32, eta32, fl32, st);
+                    k_tensor_div<0, float><<<cells_grid(g), kBlk, 0, st>>>(g, f9s, ce, g.a32, (float)(beta * g.vol),
+                                                                           0.0, cb32, rr32, nullptr, gbp_array4{});
+                }
+            }
+            for (int c = 0; c < 3; ++c) k_tensor_add<<<nb, 256, 0, st>>>(cnt, e32[c], 1.0 / scale32, u[c]);
+            steps += kInner;
+        } else {
+            for (int c = 0; c < 3; ++c) comp[c].add_vcycle_correction(r[c], u[c], scale32);
+            ++steps;
+        }
         fill_ghosts(vel);
         GBP_CUDA(cudaMemsetAsync(dnorm + 1, 0, sizeof(unsigned long long), st));
         fluxes();
-        k_tensor_div<0><<<cells_grid(g), kBlk, 0, st>>>(g, f9, uc, g.a64, beta * g.vol, 1.0 / g.vol, bc, rr, dnorm + 1,
-                                                        gbp_array4{});
+        k_tensor_div<0, double><<<cells_grid(g), kBlk, 0, st>>>(g, f9, uc, g.a64, beta * g.vol, 1.0 / g.vol, bc, rr,
+                                                                dnorm + 1, gbp_array4{});
         GBP_CUDA(cudaGetLastError());
         GBP_CUDA(cudaMemcpyAsync(hnorm + 1, dnorm + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         GBP_CUDA(cudaStreamSynchronize(st));
@@ -556,7 +643,7 @@ int TensorSolver::solve(const gbp_array4& rhs_in, gbp_array4& vel, gbp_stats* st
         cudaEventElapsedTime(&ms, ev0, ev1);
         stats->status = status;
         stats->outer_iters = it + 1;
-        stats->vcycles = 3 * it;  // one per component block and step
+        stats->vcycles = 3 * steps;  // one per component block and block step
         stats->rhs_norm = bnorm;
         stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;
         stats->final_rel_resid = bnorm > 0 ? rn / bnorm : rn;
@@ -580,9 +667,9 @@ int TensorSolver::apply(const gbp_array4& vel, gbp_array4& out)
     load(vel);
     fill_ghosts(vel);
     fluxes();
-    k_tensor_div<1><<<cells_grid(g), kBlk, 0, st>>>(g, make_fl9(fl), CU3{{u[0], u[1], u[2]}}, nullptr, 0.0, 0.0,
-                                                    CU3{{nullptr, nullptr, nullptr}}, U3{{nullptr, nullptr, nullptr}},
-                                                    nullptr, out);
+    k_tensor_div<1, double><<<cells_grid(g), kBlk, 0, st>>>(g, make_fl9(fl), CU3{{u[0], u[1], u[2]}}, nullptr, 0.0,
+                                                            0.0, CU3{{nullptr, nullptr, nullptr}},
+                                                            U3{{nullptr, nullptr, nullptr}}, nullptr, out);
     GBP_CUDA(cudaGetLastError());
     GBP_CUDA(cudaStreamSynchronize(st));
     return GBP_OK;

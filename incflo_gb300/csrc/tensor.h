@@ -12,7 +12,8 @@
 // one V-cycle of its ABecLaplacian block (the normal-derivative part: b = 4/3 eta on the
 // component's own faces, eta on the others, the component's boundary types) on a MacSolver hierarchy;
 // the cross-derivative terms only enter the residual (as MLTensorOp treats them). The blocks' V-cycles run
-// in FP32 (mixed form) or FP64.
+// in FP32 (mixed form) or FP64. In the mixed form several block steps solve the correction equation of one
+// FP64 residual in FP32 (the full operator's residual in FP32 between them, homogeneous boundary values).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -57,6 +58,16 @@ private:
     double* r[3] = {};
     double* eta[3] = {};
     double* fl[3][3] = {};  // [face direction][component]: tau_{c,d} on the faces of direction d
+    // the mixed form's FP32 inner steps: correction, scaled FP64 residual, FP32 residual, face eta, fluxes
+#ifndef GBP_TENSOR_INNER
+#define GBP_TENSOR_INNER 6
+#endif
+    static constexpr int kInner = GBP_TENSOR_INNER;  // block steps per FP64 residual
+    float* e32[3] = {};
+    float* b32[3] = {};
+    float* r32[3] = {};
+    float* eta32[3] = {};
+    float* fl32[3][3] = {};
     double alpha = 0.0, beta = 0.0;
     bool ready = false;
     unsigned long long *dnorm = nullptr, *hnorm = nullptr;
