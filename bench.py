@@ -277,8 +277,8 @@ def run_amr(args, dev, steps=3, warmup=1):
     zhi = max(hi[2] for _, hi in w["boxes"])
     out = {"workload": f"{args.n}^3 base + ratio-2 fine level from tagging (interface +-0.1 or |vorticity| > "
                        f"90th percentile; blocking_factor 32, max_grid_size 64): {len(w['boxes'])} fine boxes, "
-                       f"{fine_cells} fine cells, fine z {zlo}..{zhi}; composite nodal projection, FP32 V-cycles "
-                       f"inside FP64 refinement, rtol {args.rtol:g}",
+                       f"{fine_cells} fine cells, fine z {zlo}..{zhi}; composite nodal projection, FP32 two-level "
+                       f"steps (coarse V-cycle, fine Jacobi sweeps) inside FP64 refinement, rtol {args.rtol:g}",
            "ms_per_projection": round(sum(times) / len(times), 3), "outer_iters": st["outer_iters"],
            "vcycles": st["vcycles"], "final_rel_resid": st["final_rel_resid"],
            "device_bytes": proj.device_bytes()}

@@ -1128,7 +1128,10 @@ void CompositeNodal::issue_outer32(double scale32)
         }
         k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], (const float*)ec32, ef32);
         resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
-        fin.apply_vcycles32(rf32, 1, st);
+        if (kFineSweeps > 0)
+            fin.smooth32(rf32, kFineSweeps, st);
+        else
+            fin.apply_vcycles32(rf32, 1, st);
         k_amr_add32<<<nfb_, kT, 0, st>>>(gf.count, fin.correction32(), ef32);
         if (q + 1 < kInner) {
             // FP32 composite residual of e (the interface values of e_f are those of e_c already)
@@ -1391,7 +1394,9 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
         memset(stats, 0, sizeof(*stats));
         stats->status = status;
         stats->outer_iters = it + 1;
-        stats->vcycles = 2 * it * (mixed ? kInner : 1);  // one V-cycle per level per two-level step
+        // V-cycles: the coarse one of every two-level step, and the fine one where the fine correction is a
+        // V-cycle (the plain form; the mixed form with kFineSweeps = 0)
+        stats->vcycles = it * (mixed ? kInner * (kFineSweeps > 0 ? 1 : 2) : 2);
         stats->num_levels = 2;
         stats->rhs_norm = bnorm;
         stats->initial_rel_resid = bnorm > 0 ? r0 / bnorm : r0;

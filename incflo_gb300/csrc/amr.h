@@ -103,6 +103,14 @@ private:
 #define GBP_AMR_INNER 8
 #endif
     static constexpr int kInner = GBP_AMR_INNER;
+#ifndef GBP_AMR_FINE_SWEEPS
+#define GBP_AMR_FINE_SWEEPS 2
+#endif
+    // the fine correction of a mixed-form two-level step: 0 = one V-cycle of the fine hierarchy, n > 0 = n
+    // Jacobi sweeps on the fine level only (the coarse V-cycle already corrects every scale above the fine
+    // spacing; measured on the 256^3 tagged workload: V-cycle 102.1 ms, 2 sweeps 75.9 ms, 4 sweeps 86.4 ms,
+    // each in 2 refinement steps of 8 two-level steps)
+    static constexpr int kFineSweeps = GBP_AMR_FINE_SWEEPS;
     float *bc32 = nullptr, *rc32 = nullptr, *ec32 = nullptr, *rcf32 = nullptr, *scm32 = nullptr;  // coarse
     float *bf32 = nullptr, *rf32 = nullptr, *ef32 = nullptr;                                       // fine
     // FP32 residual of one composite part: the whole-row sweep where it applies

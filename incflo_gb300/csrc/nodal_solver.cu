@@ -741,6 +741,21 @@ void NodalSolver::apply_vcycles32(const float* b32, int m, cudaStream_t s)
     cap_or_st = st;
 }
 
+void NodalSolver::smooth32(const float* b32, int nu, cudaStream_t s)
+{
+    const NodalLevel& l0 = L[0];
+    cap_or_st = s;
+    float* x = l0.x32;
+    float* t = l0.t32;
+    nodal_jacobi<float>(l0.g, l0.s32, nullptr, b32, x, wpre[0], true, s);
+    for (int q = 1; q < nu; ++q) {
+        jacobi<float>(l0.g, l0.s32, x, b32, t, wpre[q % kSweepWeights], s);
+        std::swap(x, t);
+    }
+    xres[0] = x;
+    cap_or_st = st;
+}
+
 int NodalSolver::take_sweep_status(cudaStream_t s)
 {
     if (launch_rc) {

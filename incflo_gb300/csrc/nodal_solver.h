@@ -122,6 +122,9 @@ public:
     // zero on b32; the correction stays in correction32() until the next V-cycle of this solver.
     void apply_vcycles32(const float* b32, int m, cudaStream_t s);
     const float* correction32() const { return (const float*)xres[0]; }
+    // nu FP32 Jacobi sweeps from zero on level 0 only (b32 scaled as for apply_vcycles32); the correction
+    // stays in correction32()
+    void smooth32(const float* b32, int nu, cudaStream_t s);
     // For work issued through apply_vcycles / apply_vcycles32: GBP_OK, the first launch error (cleared), or
     // GBP_TIMEOUT when a bounded device wait of a level sweep ran out (the device error word is read and
     // cleared; synchronises s).
