@@ -134,19 +134,6 @@ __device__ __forceinline__ bool fine_local(const NodalGeom& gf, const int off[3]
     return true;
 }
 
-// the fine unknowns' values, 0 elsewhere (unique nodes, aliases written): the fine part of the composite
-// residual as the standard full-weighting restriction sees it
-__global__ void k_amr_dof_only(NodalGeom gf, const unsigned char* __restrict__ fcls, const float* __restrict__ v,
-                               float* out)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
-    const long long p = pidx(gf.sy, gf.sz, i, j, k);
-    store_node(out, gf, i, j, k, fcls[p] == F_DOF ? v[p] : 0.f);
-}
-
 // coarse node (I, J, K) -> node of the fine box's coarsened level g1 (origin o = off / 2), or false
 __device__ __forceinline__ bool coarse_to_g1(const NodalGeom& g1, const int o[3], const int I[3], int q[3])
 {
@@ -378,15 +365,9 @@ __device__ __forceinline__ int cwrap(const NodalGeom& gc, int d, int v)
 // interface values of the fine level from the coarse one: aligned nodes copy, hanging nodes
 // interpolate along the coarse face they lie on
 template <typename T>
-__global__ void k_amr_fill_fine(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0, int off1,
-                                int off2, const T* __restrict__ pc, T* pf)
+__device__ __forceinline__ void fill_fine_node(const NodalGeom& gc, const NodalGeom& gf, int off0, int off1, int off2,
+                                               const T* __restrict__ pc, T* pf, int i, int j, int k)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z * blockDim.z + threadIdx.z;
-    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
-    const unsigned char c = fcls[pidx(gf.sy, gf.sz, i, j, k)];
-    if (c != F_ALIGNED && c != F_HANGING) return;
     const int gpos[3] = {i + off0, j + off1, k + off2};
     T acc = 0;
     int nodd = 0;
@@ -407,6 +388,44 @@ __global__ void k_amr_fill_fine(NodalGeom gc, NodalGeom gf, const unsigned char*
         if (use) acc += pc[pidx(gc.sy, gc.sz, I[0], I[1], I[2])];
     }
     store_node(pf, gf, i, j, k, w * acc);
+}
+
+template <typename T>
+__global__ void k_amr_fill_fine(NodalGeom gc, NodalGeom gf, const unsigned char* __restrict__ fcls, int off0, int off1,
+                                int off2, const T* __restrict__ pc, T* pf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const unsigned char c = fcls[pidx(gf.sy, gf.sz, i, j, k)];
+    if (c != F_ALIGNED && c != F_HANGING) return;
+    fill_fine_node<T>(gc, gf, off0, off1, off2, pc, pf, i, j, k);
+}
+
+// the same over the listed interface nodes only
+template <typename T>
+__global__ void k_amr_fill_fine_list(NodalGeom gc, NodalGeom gf, int off0, int off1, int off2,
+                                     const int4* __restrict__ list, int n, const T* __restrict__ pc, T* pf)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 q = list[t];
+    fill_fine_node<T>(gc, gf, off0, off1, off2, pc, pf, q.x, q.y, q.z);
+}
+
+// the fine interface nodes (aligned and hanging) as (i, j, k): counted into *count, and listed when list
+// is given (in no particular order: every entry is used on its own)
+__global__ void k_amr_iface_list(NodalGeom gf, const unsigned char* __restrict__ fcls, int* count, int4* list)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= gf.nu[0] || j >= gf.nu[1] || k >= gf.nu[2]) return;
+    const unsigned char c = fcls[pidx(gf.sy, gf.sz, i, j, k)];
+    if (c != F_ALIGNED && c != F_HANGING) return;
+    const int t = atomicAdd(count, 1);
+    if (list) list[t] = make_int4(i, j, k, 0);
 }
 
 // v_c[I] += sum of the interface fine values that map to the coarse interface node I (the aligned
@@ -712,6 +731,7 @@ inline double bits_to_double(unsigned long long b)
 
 CompositeNodal::~CompositeNodal()
 {
+    if (iface) cudaFree(iface);
     if (st) cudaStreamSynchronize(st);
     if (gstep) cudaGraphExecDestroy(gstep);
     if (capst) cudaStreamDestroy(capst);
@@ -722,7 +742,10 @@ CompositeNodal::~CompositeNodal()
     pool.release();
 }
 
-size_t CompositeNodal::device_bytes() const { return pool.bytes + crs.device_bytes() + fin.device_bytes(); }
+size_t CompositeNodal::device_bytes() const
+{
+    return pool.bytes + crs.device_bytes() + fin.device_bytes() + sizeof(int4) * (size_t)niface;
+}
 
 int CompositeNodal::set_options(const gbp_options& o)
 {
@@ -944,6 +967,21 @@ int CompositeNodal::init(const gbp_geometry& coarse, const int bc_lo[3], const i
     cudaFree(im);
     if (rc) return rc;
     gf = fin.geom0();  // now carries the mask
+    // the interface node list: count, then fill
+    {
+        int* dcount = reinterpret_cast<int*>(dnorm + 4);
+        GBP_CUDA(cudaMemsetAsync(dcount, 0, sizeof(int), st));
+        k_amr_iface_list<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, dcount, nullptr);
+        GBP_CUDA(cudaMemcpyAsync(&niface, dcount, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GBP_CUDA(cudaStreamSynchronize(st));
+        if (niface > 0) {
+            GBP_CUDA(cudaMalloc(&iface, sizeof(int4) * (size_t)niface));
+            GBP_CUDA(cudaMemsetAsync(dcount, 0, sizeof(int), st));
+            k_amr_iface_list<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, dcount, iface);
+            GBP_CUDA(cudaStreamSynchronize(st));
+        }
+        GBP_CUDA(cudaGetLastError());
+    }
     return GBP_OK;
 }
 
@@ -1111,8 +1149,8 @@ void CompositeNodal::issue_outer32(double scale32)
         const float* rf = q == 0 ? bf32 : rf32;
         const int o0 = off[0] / 2, o1 = off[1] / 2, o2 = off[2] / 2;
         if (xfer1) {
-            k_amr_dof_only<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, rf, rm32);
-            nodal_restrict<float>(gf_nomask, g1n, rm32, x1_32, st);
+            // rf holds the fine unknowns' residuals and 0 elsewhere (bf32, or the masked fine residual)
+            nodal_restrict<float>(gf_nomask, g1n, rf, x1_32, st);
             k_amr_combine<<<gnodes(gc), kB3, 0, st>>>(gc, g1n, ccls, o0, o1, o2, rc, x1_32, rcf32);
         } else {
             restrict_to_coarse(rc, rf, rcf32);
@@ -1126,8 +1164,16 @@ void CompositeNodal::issue_outer32(double scale32)
             k_amr_prolong_f<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], crs.correction32(),
                                                         ef32);
         }
-        k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], (const float*)ec32, ef32);
-        resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
+        if (xfer1) {
+            if (niface > 0)
+                k_amr_fill_fine_list<<<(unsigned)((niface + kT - 1) / kT), kT, 0, st>>>(
+                    gc, gf, off[0], off[1], off[2], (const int4*)iface, niface, (const float*)ec32, ef32);
+            resid32(gf, fin.sigma32(), ef32, bf32, rf32);  // the fine unknowns only (the mask holds the rest)
+        } else {
+            k_amr_fill_fine<<<gnodes(gf), kB3, 0, st>>>(gc, gf, fcls, off[0], off[1], off[2], (const float*)ec32,
+                                                        ef32);
+            resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
+        }
         if (kFineSweeps > 0)
             fin.smooth32(rf32, kFineSweeps, st);
         else
@@ -1135,10 +1181,17 @@ void CompositeNodal::issue_outer32(double scale32)
         k_amr_add32<<<nfb_, kT, 0, st>>>(gf.count, fin.correction32(), ef32);
         if (q + 1 < kInner) {
             // FP32 composite residual of e (the interface values of e_f are those of e_c already)
-            resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
+            const float* rif = rf32;
+            if (xfer1) {
+                // the fine unknowns' residuals, and the interface nodes' into rm32 for the coarse interface
+                resid32(gf, fin.sigma32(), ef32, bf32, rf32);
+                nodal_resid_list<float>(gf_nomask, fin.sigma32(), ef32, bf32, rm32, (const int4*)iface, niface, st);
+                rif = rm32;
+            } else {
+                resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
+            }
             resid32(gc, scm32, ec32, bc32, rc32);
-            k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], (const float*)rf32,
-                                                   rc32);
+            k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], rif, rc32);
         }
     }
     nodal_add_correction<float>(gc, phi_c, ec32, 1.0 / scale32, st);

@@ -119,7 +119,11 @@ private:
     // without its mask): the standard full weighting / trilinear kernels plus a gather and a combine
     bool xfer1 = false;
     NodalGeom g1n{};
-    float *rm32 = nullptr, *x1_32 = nullptr;
+    float *rm32 = nullptr, *x1_32 = nullptr;  // rm32: the fine interface nodes' FP32 residuals
+    // the fine interface nodes (aligned and hanging), (i, j, k) each: their values and residuals of the
+    // inner steps are computed over this list instead of the whole bounding box
+    int4* iface = nullptr;
+    int niface = 0;
     unsigned* derr = nullptr;  // device error word of the whole-row sweeps issued here
     int launch_rc = 0;         // first launch error of a step (tensor-map set-up)
     int sweep_status();

@@ -212,6 +212,24 @@ __global__ void __launch_bounds__(256) k_resid(NodalGeom g, const T* __restrict_
     }
 }
 
+// r = b - A x at the listed unique nodes only (nodes[t] = (i, j, k)); no aliases written
+template <typename T, bool ISO>
+__global__ void __launch_bounds__(256) k_resid_list(NodalGeom g, const T* __restrict__ s, const T* __restrict__ x,
+                                                    const T* __restrict__ b, T* __restrict__ r,
+                                                    const int4* __restrict__ nodes, int n)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int4 q = nodes[t];
+    const long long c = pidx(g.sy, g.sz, q.x, q.y, q.z);
+    T v = T(0);
+    if (!node_is_dirichlet(g, q.x, q.y, q.z)) {
+        T diag;
+        v = b[c] - NodalOp<T>::template apply<ISO>(x, s, c, g.sy, g.sz, g, diag);
+    }
+    r[c] = v;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_restrict(NodalGeom gf, NodalGeom gc, const T* __restrict__ rf,
                                                   T* __restrict__ bc)
@@ -1286,6 +1304,20 @@ void nodal_resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, u
     else
         k_resid<T, false><<<grid3(g), kBlock3, 0, st>>>(g, s, x, b, r, norm);
 }
+
+template <typename T>
+void nodal_resid_list(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, const int4* nodes, int n,
+                      cudaStream_t st)
+{
+    if (n <= 0) return;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    if (g.iso)
+        k_resid_list<T, true><<<nb, 256, 0, st>>>(g, s, x, b, r, nodes, n);
+    else
+        k_resid_list<T, false><<<nb, 256, 0, st>>>(g, s, x, b, r, nodes, n);
+}
+template void nodal_resid_list<float>(const NodalGeom&, const float*, const float*, const float*, float*, const int4*,
+                                      int, cudaStream_t);
 
 template <typename T>
 void nodal_restrict(const NodalGeom& gf, const NodalGeom& gc, const T* rf, T* bc, cudaStream_t st)

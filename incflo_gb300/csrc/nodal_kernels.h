@@ -41,6 +41,10 @@ void nodal_resid(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, u
                  cudaStream_t st);
 template <typename T>
 void nodal_restrict(const NodalGeom& gf, const NodalGeom& gc, const T* rf, T* bc, cudaStream_t st);
+// r = b - A x at the n listed unique nodes (i, j, k) only
+template <typename T>
+void nodal_resid_list(const NodalGeom& g, const T* s, const T* x, const T* b, T* r, const int4* nodes, int n,
+                      cudaStream_t st);
 template <typename T>
 void nodal_prolong_add(const NodalGeom& gf, const NodalGeom& gc, const T* xc, T* xf, cudaStream_t st);
 template <typename T>
