@@ -8,7 +8,7 @@
  * layers, and the solver is a conjugate-gradient iteration preconditioned by a symmetric
  * multigrid V-cycle with 8-colour Gauss-Seidel smoothing and a dense direct bottom solve.
  * It converges to the discrete solution regardless of how good the preconditioner is, so
- * the GPU solver is judged against the discrete operator, not against this solver's path.
+ * the GPU solver is compared with the discrete operator, not with this solver's path.
  */
 #include "proj_oracle.h"
 

@@ -1,4 +1,4 @@
-"""Pins the CPU oracle (oracle/proj_oracle.c) before anything is judged against it.
+"""Pins the CPU oracle (oracle/proj_oracle.c) before anything is compared with it.
 
 incflo ships no golden projection outputs and its MLMG (AMReX / AMReX-Hydro) is not vendored, so
 the oracle is pinned by: the analytic Taylor-Green pressure of incflo's probtype 1
