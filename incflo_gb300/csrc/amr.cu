@@ -1317,8 +1317,15 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     GBP_CUDA(cudaMemsetAsync(dnorm, 0, 2 * sizeof(unsigned long long), st));
     k_amr_norm_c<<<gnodes(gc), kB3, 0, st>>>(gc, ccls, b_c, dnorm);
     k_amr_norm_f<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, b_f, dnorm);
-    GBP_CUDA(cudaMemsetAsync(phi_c, 0, sizeof(double) * gc.count, st));
-    GBP_CUDA(cudaMemsetAsync(phi_f, 0, sizeof(double) * gf.count, st));
+    // initial_guess = previous: both levels start from the last converged composite phi of this box layout
+    // (phi_c / phi_f keep it between calls); the tolerance refers to that start's residual, as in the
+    // single-level solve
+    const bool from_prev = opt.initial_guess == 1 && have_last;
+    have_last = false;
+    if (!from_prev) {
+        GBP_CUDA(cudaMemsetAsync(phi_c, 0, sizeof(double) * gc.count, st));
+        GBP_CUDA(cudaMemsetAsync(phi_f, 0, sizeof(double) * gf.count, st));
+    }
     composite_residual(b_c, b_f, dnorm + 1);
     GBP_CUDA(cudaMemcpyAsync(hnorm, dnorm, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     GBP_CUDA(cudaStreamSynchronize(st));
@@ -1443,10 +1450,12 @@ int CompositeNodal::project(const AmrFields& f, gbp_stats* stats)
     GBP_CUDA(cudaEventRecord(ev1, st));
     GBP_CUDA(cudaEventSynchronize(ev1));
     GBP_CUDA(cudaGetLastError());
+    have_last = status == GBP_OK;
     if (stats) {
         memset(stats, 0, sizeof(*stats));
         stats->status = status;
         stats->outer_iters = it + 1;
+        stats->prev_rel_resid = from_prev ? (bnorm > 0 ? r0 / bnorm : r0) : 0.0;
         // V-cycles: the coarse one of every two-level step, and the fine one where the fine correction is a
         // V-cycle (the plain form; the mixed form with kFineSweeps = 0)
         stats->vcycles = it * (mixed ? kInner * (kFineSweeps > 0 ? 1 : 2) : 2);

@@ -86,6 +86,7 @@ private:
     int nparts = 0;
     unsigned long long *dnorm = nullptr, *hnorm = nullptr;
     bool qsw = false;      // shared-sum FP64 residuals (isotropic cells)
+    bool have_last = false;  // phi_c / phi_f hold the last converged solution (initial_guess = previous)
     QWeights qwf{}, qwc{};  // their edge weights, fine and coarse
     void* dboxes = nullptr;  // device table for the batched box kernels
     size_t dboxes_bytes = 0;
