@@ -1144,6 +1144,13 @@ void CompositeNodal::issue_outer32(double scale32)
     k_amr_rhs32_fine<<<gnodes(gf), kB3, 0, st>>>(gf, fcls, r_f, scale32, bf32);
     cudaMemsetAsync(ec32, 0, sizeof(float) * gc.count, st);
     cudaMemsetAsync(ef32, 0, sizeof(float) * gf.count, st);
+    // FP32 composite residual of e into rc32 / rf32 (fine unknowns) and rm32 (fine interface nodes)
+    auto composite32 = [&]() {
+        resid32(gf, fin.sigma32(), ef32, bf32, rf32);
+        nodal_resid_list<float>(gf_nomask, fin.sigma32(), ef32, bf32, rm32, (const int4*)iface, niface, st);
+        resid32(gc, scm32, ec32, bc32, rc32);
+        k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], (const float*)rm32, rc32);
+    };
     for (int q = 0; q < kInner; ++q) {
         const float* rc = q == 0 ? bc32 : rc32;
         const float* rf = q == 0 ? bf32 : rf32;
@@ -1181,17 +1188,15 @@ void CompositeNodal::issue_outer32(double scale32)
         k_amr_add32<<<nfb_, kT, 0, st>>>(gf.count, fin.correction32(), ef32);
         if (q + 1 < kInner) {
             // FP32 composite residual of e (the interface values of e_f are those of e_c already)
-            const float* rif = rf32;
             if (xfer1) {
                 // the fine unknowns' residuals, and the interface nodes' into rm32 for the coarse interface
-                resid32(gf, fin.sigma32(), ef32, bf32, rf32);
-                nodal_resid_list<float>(gf_nomask, fin.sigma32(), ef32, bf32, rm32, (const int4*)iface, niface, st);
-                rif = rm32;
+                composite32();
             } else {
                 resid32(gf_nomask, fin.sigma32(), ef32, bf32, rf32);
+                resid32(gc, scm32, ec32, bc32, rc32);
+                k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], (const float*)rf32,
+                                                       rc32);
             }
-            resid32(gc, scm32, ec32, bc32, rc32);
-            k_amr_sync<<<gnodes(gc), kB3, 0, st>>>(gc, gf, ccls, fcls, off[0], off[1], off[2], rif, rc32);
         }
     }
     nodal_add_correction<float>(gc, phi_c, ec32, 1.0 / scale32, st);
