@@ -360,6 +360,11 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY, RPT>::TTR,
     int cslot = 0;
     uint32_t cphase = 0;
     // One z step: Bn receives plane P (prolongated in mode 3); Ao holds plane P-1.
+    // overset mask words of the thread's rows, loaded one plane ahead (a global load on the critical path of
+    // every plane would stall the z march)
+    unsigned mw[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) mw[r] = 0xffffffffu;
     auto step = [&](int s, const float (&Ao)[W][6], float (&Bn)[W][6]) {
         const unsigned char* base = smem + cslot * L.bytes;
         if (!mbar_wait_bounded(&bar[cslot], cphase, a.err)) abort_flag = 1;
@@ -455,15 +460,24 @@ __global__ void __launch_bounds__(TXM * VsShape<MODE, TY, RPT>::TTR,
         // overset mask (Jacobi and residual only): masked nodes of plane k are held at 0 like Dirichlet
         // nodes; bit r*4+q as in dmask
         unsigned mk = 0;
-        if (MODE <= 1 && g.mask && s >= 2) {
+        if (MODE <= 1 && g.mask) {
+            if (s >= 2) {
 #pragma unroll
-            for (int r = 0; r < RPT; ++r)
-                if (j0 + r < g.nu[1]) {
-                    const unsigned char* mr = g.mask + pidx(g.sy, g.sz, i0, j0 + r, k);
+                for (int r = 0; r < RPT; ++r)
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
-                        if (q < nact && !mr[q]) mk |= 1u << (r * 4 + q);
-                }
+                        if (q < nact && !((mw[r] >> (8 * q)) & 0xffu)) mk |= 1u << (r * 4 + q);
+            }
+            // the next plane's words (plane P, completed at the next step): the thread's 4 mask bytes as one
+            // word (i0 + kOX and the row / plane strides are multiples of 4; bytes past the last node stay
+            // inside the padded row)
+            if (P < g.nu[2]) {
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                    mw[r] = j0 + r < g.nu[1]
+                                ? __ldg(reinterpret_cast<const unsigned*>(g.mask + pidx(g.sy, g.sz, i0, j0 + r, P)))
+                                : 0xffffffffu;
+            }
         }
         float v[RPT][4];
 #pragma unroll
