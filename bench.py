@@ -786,7 +786,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=256)
+    # --size: the same, for command lines under torchrun (whose own options take every --n... prefix)
+    ap.add_argument("--n", "--size", dest="n", type=int, default=256)
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--inner", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=5)
